@@ -1,0 +1,203 @@
+"""Python front end of the oracle (test infrastructure only).
+
+The oracle is the CPU restatement of SIMCOFlow's projection path in
+``oracle.c`` (coefficients, literal CSR matrix, rhs, scatter, correction,
+boundary conditions) plus the CPU multigrid-preconditioned CG of ``gmg.cpp``.
+Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` use it, and only as the checker or the timed CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+import subprocess
+from typing import Optional
+
+import numpy as np
+
+from simcoflow3d_gb300 import capi
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+
+
+def build(quiet: bool = True) -> str:
+    subprocess.run(["make", "-C", _HERE], check=True,
+                   stdout=subprocess.DEVNULL if quiet else None)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = C.CDLL(LIB)
+        dp, ip = capi.c_double_p, capi.c_int32_p
+        i64p = C.POINTER(C.c_int64)
+        L.oracle_pocoef.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(capi.ScfPoissonIn), C.c_double,
+                                    C.c_double, C.c_double, C.c_double, C.c_double, C.c_double, dp]
+        L.oracle_matrix_csr.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(capi.ScfPoissonIn), dp, i64p, ip, dp]
+        L.oracle_matrix_csr.restype = C.c_int64
+        L.oracle_rhs.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(capi.ScfPoissonIn), dp, dp]
+        L.oracle_scatter.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(capi.ScfPoissonIn), dp, dp]
+        L.oracle_correct.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(capi.ScfPoissonIn),
+                                     C.POINTER(capi.ScfCorrectIn), dp, dp, dp, dp, dp, dp, dp, C.c_int]
+        L.oracle_csr_apply.argtypes = [C.c_int32, i64p, ip, dp, dp, dp]
+        L.oracle_csr_pcg.argtypes = [C.c_int32, i64p, ip, dp, dp, dp, C.c_double, C.c_int, C.c_int,
+                                     C.POINTER(C.c_double)]
+        L.oracle_csr_relres.argtypes = [C.c_int32, i64p, ip, dp, dp, dp, C.c_int]
+        L.oracle_csr_relres.restype = C.c_double
+        L.oracle_gmg_solve.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(capi.ScfPoissonIn), dp, dp, dp,
+                                       C.POINTER(GmgParams)]
+        L.oracle_num_threads.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+class GmgParams(C.Structure):
+    _fields_ = [
+        ("precision", C.c_int), ("rel_tol", C.c_double), ("max_iter", C.c_int), ("max_rounds", C.c_int),
+        ("inner_rtol", C.c_double), ("degree", C.c_int), ("ratio", C.c_double), ("coarse_max", C.c_int),
+        ("iterations", C.c_int), ("rounds", C.c_int), ("levels", C.c_int),
+        ("rel_residual", C.c_double), ("rhs_norm", C.c_double),
+    ]
+
+
+def _dp(a):
+    return a.ctypes.data_as(capi.c_double_p)
+
+
+def singular(w) -> bool:
+    return all(f == 1 for f in w.bcp_flag)
+
+
+def pocoef(w, rho_ref=None, epsi=1.0e-3, tol=1.0e-30, stale_init=float("nan")):
+    """PoCoef (I,J,K,6) by Compute1DGFMCoefficient (ProjectionP.f90:123-265)."""
+    I, J, K = w.imax, w.jmax, w.kmax
+    out = np.zeros((I, J, K, 6), order="F")
+    s = capi.poisson_in(w)
+    lib().oracle_pocoef(I, J, K, C.byref(s), w.rho_l, w.rho_g, rho_ref or w.rho_l, epsi, tol, stale_init, _dp(out))
+    return out
+
+
+def csr(w, pc):
+    """Literal SetPoissonMatrix (ProjectionP.f90:301-482): CSR in PosNu order."""
+    I, J, K = w.imax, w.jmax, w.kmax
+    n = w.ext_cell + 1
+    rp = np.zeros(n + 1, dtype=np.int64)
+    ci = np.zeros(7 * n, dtype=np.int32)
+    va = np.zeros(7 * n, dtype=np.float64)
+    s = capi.poisson_in(w)
+    bad = lib().oracle_matrix_csr(I, J, K, C.byref(s), _dp(pc), rp.ctypes.data_as(C.POINTER(C.c_int64)),
+                                  ci.ctypes.data_as(capi.c_int32_p), _dp(va))
+    if bad < 0:
+        raise ValueError("PosNu inconsistent with ExtCell")
+    nnz = int(rp[-1])
+    return rp, ci[:nnz].copy(), va[:nnz].copy(), int(bad)
+
+
+def rhs(w, pc):
+    """Literal SetPoissonVectors (ProjectionP.f90:484-576): b in PosNu order."""
+    I, J, K = w.imax, w.jmax, w.kmax
+    b = np.zeros(w.ext_cell + 1)
+    s = capi.poisson_in(w)
+    lib().oracle_rhs(I, J, K, C.byref(s), _dp(pc), _dp(b))
+    return b
+
+
+def csr_apply(A, x):
+    rp, ci, va = A[:3]
+    y = np.zeros(rp.size - 1)
+    lib().oracle_csr_apply(rp.size - 1, rp.ctypes.data_as(C.POINTER(C.c_int64)), ci.ctypes.data_as(capi.c_int32_p),
+                           _dp(va), _dp(np.ascontiguousarray(x, dtype=np.float64)), _dp(y))
+    return y
+
+
+def csr_pcg(A, b, tol=1e-13, maxit=200000, singular_=False):
+    rp, ci, va = A[:3]
+    x = np.zeros(rp.size - 1)
+    rr = C.c_double(0)
+    it = lib().oracle_csr_pcg(rp.size - 1, rp.ctypes.data_as(C.POINTER(C.c_int64)), ci.ctypes.data_as(capi.c_int32_p),
+                              _dp(va), _dp(b), _dp(x), tol, maxit, int(singular_), C.byref(rr))
+    return x, it, rr.value
+
+
+def csr_relres(A, b, x, singular_=False):
+    rp, ci, va = A[:3]
+    return lib().oracle_csr_relres(rp.size - 1, rp.ctypes.data_as(C.POINTER(C.c_int64)),
+                                   ci.ctypes.data_as(capi.c_int32_p), _dp(va), _dp(b),
+                                   _dp(np.ascontiguousarray(x, dtype=np.float64)), int(singular_))
+
+
+def gmg_solve(w, pc, b, precision=0, rel_tol=1e-13, max_iter=400, degree=2, ratio=6.0, coarse_max=64,
+              max_rounds=12, inner_rtol=1e-4):
+    """CPU multigrid-preconditioned CG; returns (x in PosNu order, stats)."""
+    I, J, K = w.imax, w.jmax, w.kmax
+    x = np.zeros(w.ext_cell + 1)
+    prm = GmgParams(precision=precision, rel_tol=rel_tol, max_iter=max_iter, max_rounds=max_rounds,
+                    inner_rtol=inner_rtol, degree=degree, ratio=ratio, coarse_max=coarse_max)
+    s = capi.poisson_in(w)
+    rc = lib().oracle_gmg_solve(I, J, K, C.byref(s), _dp(pc), _dp(b), _dp(x), C.byref(prm))
+    st = {f: getattr(prm, f) for f, _ in GmgParams._fields_}
+    st["rc"] = rc
+    return x, st
+
+
+def scatter(w, x, pp0: Optional[np.ndarray] = None):
+    """DeltaPressureGetValues + DeltaPressureBoundaryCondition."""
+    I, J, K = w.imax, w.jmax, w.kmax
+    pp = np.zeros(w.shape_g, order="F") if pp0 is None else pp0.copy(order="F")
+    s = capi.poisson_in(w)
+    lib().oracle_scatter(I, J, K, C.byref(s), _dp(np.ascontiguousarray(x)), _dp(pp))
+    return pp
+
+
+def correct(w, pc, pp, north_mass_fix=0):
+    """Velocity correction + BoundaryConditionVarNew + mass correction.
+    Returns (u, v, w, p, bcvar[4][6], status)."""
+    I, J, K = w.imax, w.jmax, w.kmax
+    a = w.arrays
+    u, v, ww, p = (a[k].copy(order="F") for k in ("tvar_u", "tvar_v", "tvar_w", "tvar_p"))
+    shapes = capi.bc_plane_shapes(I, J, K)
+    total = 4 * sum(x * y for x, y in shapes)
+    bc = np.zeros(total)
+    s = capi.poisson_in(w)
+    c = capi.correct_in(w)
+    rc = lib().oracle_correct(I, J, K, C.byref(s), C.byref(c), _dp(pc), _dp(pp), _dp(u), _dp(v), _dp(ww), _dp(p),
+                              _dp(bc), int(north_mass_fix))
+    planes = []
+    off = 0
+    for f in range(4):
+        row = []
+        for shp in shapes:
+            n = shp[0] * shp[1]
+            row.append(bc[off:off + n].reshape(shp, order="F").copy(order="F"))
+            off += n
+        planes.append(row)
+    return u, v, ww, p, planes, rc
+
+
+def project(w, solver="gmg", rel_tol=1e-13, precision=0, north_mass_fix=0, **kw):
+    """Whole projection on the CPU.  Returns a dict with PoCoef, the CSR
+    system, the solution, Pp and the corrected fields."""
+    pc = pocoef(w)
+    A = csr(w, pc)
+    b = rhs(w, pc)
+    sing = singular(w)
+    if solver == "csr":
+        x, its, rr = csr_pcg(A, b, tol=rel_tol, singular_=sing)
+        st = {"iterations": its, "rel_residual": rr}
+    else:
+        x, st = gmg_solve(w, pc, b, precision=precision, rel_tol=rel_tol, **kw)
+    st["csr_relres"] = csr_relres(A, b, x, sing)
+    pp = scatter(w, x)
+    u, v, ww, p, bcv, rc = correct(w, pc, pp, north_mass_fix=north_mass_fix)
+    return {"pocoef": pc, "A": A, "b": b, "x": x, "stats": st, "pp": pp, "u": u, "v": v, "w": ww, "p": p,
+            "bcvar": bcv, "correct_rc": rc, "singular": sing}
+
+
+def num_threads() -> int:
+    return int(lib().oracle_num_threads())

@@ -1,0 +1,556 @@
+// k_solver.cu -- multigrid-preconditioned CG on the 7-point pressure operator.
+//
+// Fine level: FP64 CG (SpMV, vector updates, dot products) on the ghosted
+// layout.  Preconditioner: one V-cycle, T = double (FP64 mode) or T = float
+// (mixed mode), with Chebyshev smoothing of the Jacobi-preconditioned
+// operator, sum restriction, piecewise-constant prolongation, and a dense
+// FP64 inverse on the coarsest level.  Coarse operators: per coarse face, the
+// fine face conductances summed over the face and divided by the coarsening
+// factor along the normal (the cell-centre distance doubles); the coarse
+// diagonal is the sum of the coarse couplings plus half the children's
+// Dirichlet terms.  Dot products are reduced per block and then in one block
+// in a fixed order, so results are bitwise reproducible.
+#include "scf_kernels.h"
+
+#define INTERIOR_IJK(L)                                       \
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1; \
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1; \
+    const int k = blockIdx.z * blockDim.z + threadIdx.z + 1; \
+    const bool in = i <= (L).n0 && j <= (L).n1 && k <= (L).n2; \
+    const int c = i + (L).sy * j + (L).sz * k;
+
+// ---------------------------------------------------------------------------
+// reductions
+
+enum ReduceMode { RM_STORE = 0, RM_ALPHA = 1, RM_BETA = 2, RM_MEAN = 3 };
+
+__global__ void __launch_bounds__(1024) k_reduce(const double *__restrict__ part, int n, double *scal, int slot,
+                                                 int mode)
+{
+    double s = 0.0;
+    for (int t = threadIdx.x; t < n; t += blockDim.x) s += part[t];
+    s = block_sum(s);
+    if (threadIdx.x == 0) {
+        if (mode == RM_ALPHA) {
+            scal[S_PQ] = s;
+            scal[S_ALPHA] = s != 0.0 ? scal[S_RZ] / s : 0.0;
+        } else if (mode == RM_BETA) {
+            const double old = scal[S_RZ];
+            scal[S_BETA] = old != 0.0 ? s / old : 0.0;
+            scal[S_RZ] = s;
+        } else if (mode == RM_MEAN) {
+            scal[S_SUM] = s;
+            scal[S_MEAN] = scal[S_COUNT] > 0.0 ? s / scal[S_COUNT] : 0.0;
+        } else {
+            scal[slot] = s;
+        }
+    }
+}
+
+void reduce_to(Reducer &R, int nblocks, int slot, cudaStream_t st, int *launches)
+{
+    k_reduce<<<1, 1024, 0, st>>>(R.partials, nblocks, R.scal, slot, RM_STORE);
+    *launches += 1;
+}
+
+void cg_finish_alpha(Reducer &R, int nblocks, cudaStream_t st, int *launches)
+{
+    k_reduce<<<1, 1024, 0, st>>>(R.partials, nblocks, R.scal, 0, RM_ALPHA);
+    *launches += 1;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 CG kernels on the fine level
+
+__global__ void __launch_bounds__(256) k_spmv_dot(LevelView<double> A, const double *__restrict__ p,
+                                                  double *__restrict__ q, double *__restrict__ part)
+{
+    INTERIOR_IJK(A);
+    double v = 0.0;
+    if (in) {
+        const double y = apply_row(A, p, c);
+        q[c] = y;
+        v = p[c] * y;
+    }
+    v = block_sum(v);
+    if (thread_linear() == 0) part[block_linear()] = v;
+}
+
+void cg_spmv_dot(const LevelView<double> &A, const double *p, double *q, Reducer &R, int slot_out,
+                 cudaStream_t st, int *launches)
+{
+    (void)slot_out;
+    Launch3 l = launch_interior(A.n0, A.n1, A.n2);
+    k_spmv_dot<<<l.grid, l.block, 0, st>>>(A, p, q, R.partials);
+    *launches += 1;
+    cg_finish_alpha(R, (int)nblocks(l), st, launches);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_cg_update(LevelView<double> A, double *__restrict__ x,
+                                                   double *__restrict__ r, const double *__restrict__ p,
+                                                   const double *__restrict__ q, T *__restrict__ rlow,
+                                                   const double *__restrict__ scal, double *__restrict__ part)
+{
+    INTERIOR_IJK(A);
+    double v = 0.0;
+    if (in) {
+        const double alpha = scal[S_ALPHA];
+        x[c] = x[c] + alpha * p[c];
+        const double rn = r[c] - alpha * q[c];
+        r[c] = rn;
+        if (rlow) rlow[c] = (T)rn;
+        v = rn * rn;
+    }
+    v = block_sum(v);
+    if (thread_linear() == 0) part[block_linear()] = v;
+}
+
+template <typename T>
+void cg_update(const LevelView<double> &A, double *x, double *r, const double *p, const double *q, T *rlow,
+               Reducer &R, cudaStream_t st, int *launches)
+{
+    Launch3 l = launch_interior(A.n0, A.n1, A.n2);
+    k_cg_update<T><<<l.grid, l.block, 0, st>>>(A, x, r, p, q, rlow, R.scal, R.partials);
+    *launches += 1;
+    reduce_to(R, (int)nblocks(l), S_RR, st, launches);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_dot_rz(LevelView<double> A, const double *__restrict__ r,
+                                                const T *__restrict__ z, double *__restrict__ part)
+{
+    INTERIOR_IJK(A);
+    double v = 0.0;
+    if (in) v = r[c] * (double)z[c];
+    v = block_sum(v);
+    if (thread_linear() == 0) part[block_linear()] = v;
+}
+
+template <typename T>
+void cg_dot_rz(const LevelView<double> &A, const double *r, const T *z, Reducer &R, cudaStream_t st, int *launches)
+{
+    Launch3 l = launch_interior(A.n0, A.n1, A.n2);
+    k_dot_rz<T><<<l.grid, l.block, 0, st>>>(A, r, z, R.partials);
+    k_reduce<<<1, 1024, 0, st>>>(R.partials, (int)nblocks(l), R.scal, 0, RM_BETA);
+    *launches += 2;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_pupdate(LevelView<double> A, const T *__restrict__ z,
+                                                 double *__restrict__ p, const double *__restrict__ scal, int first)
+{
+    INTERIOR_IJK(A);
+    if (!in) return;
+    const double zz = (double)z[c];
+    p[c] = first ? zz : zz + scal[S_BETA] * p[c];
+}
+
+template <typename T>
+void cg_pupdate(const LevelView<double> &A, const T *z, double *p, const double *scal, bool first, cudaStream_t st,
+                int *launches)
+{
+    Launch3 l = launch_interior(A.n0, A.n1, A.n2);
+    k_pupdate<T><<<l.grid, l.block, 0, st>>>(A, z, p, scal, first ? 1 : 0);
+    *launches += 1;
+}
+
+__global__ void __launch_bounds__(256) k_residual(LevelView<double> A, const double *__restrict__ b,
+                                                  const double *__restrict__ x, double *__restrict__ r,
+                                                  double *__restrict__ part)
+{
+    INTERIOR_IJK(A);
+    double v = 0.0;
+    if (in) {
+        const double rr = b[c] - apply_row(A, x, c);
+        r[c] = rr;
+        v = rr * rr;
+    }
+    v = block_sum(v);
+    if (thread_linear() == 0) part[block_linear()] = v;
+}
+
+void cg_residual(const LevelView<double> &A, const double *b, const double *x, double *r, Reducer &R,
+                 cudaStream_t st, int *launches)
+{
+    Launch3 l = launch_interior(A.n0, A.n1, A.n2);
+    k_residual<<<l.grid, l.block, 0, st>>>(A, b, x, r, R.partials);
+    *launches += 1;
+    reduce_to(R, (int)nblocks(l), S_RR, st, launches);
+}
+
+__global__ void __launch_bounds__(256) k_active_sum(LevelView<double> A, const unsigned char *__restrict__ act,
+                                                    const double *__restrict__ v, double *__restrict__ part)
+{
+    INTERIOR_IJK(A);
+    double s = 0.0;
+    if (in && act[c]) s = v ? v[c] : 1.0;
+    s = block_sum(s);
+    if (thread_linear() == 0) part[block_linear()] = s;
+}
+
+void active_sum(const LevelView<double> &A, const unsigned char *active, const double *v, Reducer &R,
+                cudaStream_t st, int *launches)
+{
+    Launch3 l = launch_interior(A.n0, A.n1, A.n2);
+    k_active_sum<<<l.grid, l.block, 0, st>>>(A, active, v, R.partials);
+    if (v)
+        k_reduce<<<1, 1024, 0, st>>>(R.partials, (int)nblocks(l), R.scal, 0, RM_MEAN);
+    else
+        k_reduce<<<1, 1024, 0, st>>>(R.partials, (int)nblocks(l), R.scal, S_COUNT, RM_STORE);
+    *launches += 2;
+}
+
+__global__ void __launch_bounds__(256) k_subtract_mean(LevelView<double> A, const unsigned char *__restrict__ act,
+                                                       double *__restrict__ v, const double *__restrict__ scal)
+{
+    INTERIOR_IJK(A);
+    if (in && act[c]) v[c] = v[c] - scal[S_MEAN];
+}
+
+void subtract_mean(const LevelView<double> &A, const unsigned char *active, double *v, const double *scal,
+                   cudaStream_t st, int *launches)
+{
+    Launch3 l = launch_interior(A.n0, A.n1, A.n2);
+    k_subtract_mean<<<l.grid, l.block, 0, st>>>(A, active, v, scal);
+    *launches += 1;
+}
+
+__global__ void __launch_bounds__(256) k_dot_self(LevelView<double> A, const double *__restrict__ v,
+                                                  double *__restrict__ part)
+{
+    INTERIOR_IJK(A);
+    double s = 0.0;
+    if (in) s = v[c] * v[c];
+    s = block_sum(s);
+    if (thread_linear() == 0) part[block_linear()] = s;
+}
+
+void dot_self(const LevelView<double> &A, const double *v, Reducer &R, int slot, cudaStream_t st, int *launches)
+{
+    Launch3 l = launch_interior(A.n0, A.n1, A.n2);
+    k_dot_self<<<l.grid, l.block, 0, st>>>(A, v, R.partials);
+    *launches += 1;
+    reduce_to(R, (int)nblocks(l), slot, st, launches);
+}
+
+__global__ void __launch_bounds__(256) k_copy_low(LevelView<double> A, const double *__restrict__ s,
+                                                  float *__restrict__ d)
+{
+    INTERIOR_IJK(A);
+    if (in) d[c] = (float)s[c];
+}
+
+void copy_to_low(const LevelView<double> &A, const double *src, float *dst, cudaStream_t st, int *launches)
+{
+    Launch3 l = launch_interior(A.n0, A.n1, A.n2);
+    k_copy_low<<<l.grid, l.block, 0, st>>>(A, src, dst);
+    *launches += 1;
+}
+
+// ---------------------------------------------------------------------------
+// V-cycle kernels
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_cheb_first(LevelView<T> L, const T *__restrict__ b, T *__restrict__ x,
+                                                    T coef)
+{
+    INTERIOR_IJK(L);
+    if (in) x[c] = coef * L.dinv[c] * b[c];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_cheb_step(LevelView<T> L, const T *__restrict__ b,
+                                                   const T *__restrict__ xin, const T *dprev,
+                                                   T *__restrict__ xout, T *dout, T c1, T c2)
+{
+    INTERIOR_IJK(L);
+    if (!in) return;
+    const T r = b[c] - apply_row(L, xin, c);
+    const T dn = c1 * dprev[c] + c2 * L.dinv[c] * r;
+    xout[c] = xin[c] + dn;
+    if (dout) dout[c] = dn;
+}
+
+// residual of the fine level, summed over each coarse cell's children
+template <typename T>
+__global__ void __launch_bounds__(256) k_restrict(LevelView<T> F, const T *__restrict__ b,
+                                                  const T *__restrict__ x, LevelView<T> C, T *__restrict__ bc,
+                                                  int f0, int f1, int f2)
+{
+    INTERIOR_IJK(C);
+    if (!in) return;
+    const int i0 = (i - 1) * f0 + 1, j0 = (j - 1) * f1 + 1, k0 = (k - 1) * f2 + 1;
+    const int i1 = min(i0 + f0 - 1, F.n0), j1 = min(j0 + f1 - 1, F.n1), k1 = min(k0 + f2 - 1, F.n2);
+    T s = T(0);
+    for (int kk = k0; kk <= k1; ++kk)
+        for (int jj = j0; jj <= j1; ++jj)
+            for (int ii = i0; ii <= i1; ++ii) {
+                const int fc = ii + F.sy * jj + F.sz * kk;
+                s += b[fc] - apply_row(F, x, fc);
+            }
+    bc[c] = s;
+}
+
+// prolongation (piecewise constant, active cells only) fused with the first
+// post-smoothing Chebyshev step
+template <typename T>
+__global__ void __launch_bounds__(256) k_post_first(LevelView<T> F, const T *__restrict__ b,
+                                                    const T *__restrict__ x, LevelView<T> C,
+                                                    const T *__restrict__ e, T *__restrict__ xout,
+                                                    T *__restrict__ dout, int f0, int f1, int f2, T coef)
+{
+    INTERIOR_IJK(F);
+    if (!in) return;
+    auto xc = [&](int ii, int jj, int kk) -> T {
+        const int fc = ii + F.sy * jj + F.sz * kk;
+        T v = x[fc];
+        if (F.dinv[fc] != T(0)) {
+            const int I = (ii - 1) / f0 + 1, J = (jj - 1) / f1 + 1, K = (kk - 1) / f2 + 1;
+            v += e[I + C.sy * J + C.sz * K];
+        }
+        return v;
+    };
+    const T x0 = xc(i, j, k);
+    const T ax = F.diag[c] * x0 - (F.cE[c] * xc(i + 1, j, k) + F.cE[c - 1] * xc(i - 1, j, k) +
+                                   F.cN[c] * xc(i, j + 1, k) + F.cN[c - F.sy] * xc(i, j - 1, k) +
+                                   F.cT[c] * xc(i, j, k + 1) + F.cT[c - F.sz] * xc(i, j, k - 1));
+    const T dn = coef * F.dinv[c] * (b[c] - ax);
+    xout[c] = x0 + dn;
+    if (dout) dout[c] = dn;
+}
+
+// coarsest level: y = Ainv (b - mean) on the active cells (one block)
+template <typename T>
+__global__ void __launch_bounds__(128) k_coarse_solve(const T *__restrict__ b, T *__restrict__ x,
+                                                      const unsigned char *__restrict__ act,
+                                                      const double *__restrict__ ainv, const int *__restrict__ map,
+                                                      int n, int singular)
+{
+    __shared__ double sb[128];
+    __shared__ double red[2];
+    const int t = threadIdx.x;
+    double bv = 0.0, a = 0.0;
+    if (t < n) {
+        bv = (double)b[map[t]];
+        a = act[map[t]] ? 1.0 : 0.0;
+    }
+    if (singular) {
+        double s = block_sum(bv * a);
+        __syncthreads();
+        double cnt = block_sum(a);
+        if (t == 0) { red[0] = s; red[1] = cnt; }
+        __syncthreads();
+        if (red[1] > 0.0) bv -= a * (red[0] / red[1]);
+    }
+    if (t < n) sb[t] = bv;
+    __syncthreads();
+    if (t < n) {
+        double y = 0.0;
+        for (int s = 0; s < n; ++s) y += ainv[(size_t)t * n + s] * sb[s];
+        x[map[t]] = a != 0.0 ? (T)y : T(0);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// hierarchy construction
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_coarsen_cpl(MgLevel<T> F, MgLevel<T> C)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z + 1;
+    if (i > C.n0 || j > C.n1 || k > C.n2) return;
+    const int cc = i + C.sy * j + C.sz * k;
+    const int f0 = F.f0, f1 = F.f1, f2 = F.f2;
+    const int i0 = (i - 1) * f0 + 1, j0 = (j - 1) * f1 + 1, k0 = (k - 1) * f2 + 1;
+    const int i1 = min(i0 + f0 - 1, F.n0), j1 = min(j0 + f1 - 1, F.n1), k1 = min(k0 + f2 - 1, F.n2);
+    unsigned char act = 0;
+    T ex = T(0), se = T(0), sn = T(0), sT = T(0);
+    for (int kk = k0; kk <= k1; ++kk)
+        for (int jj = j0; jj <= j1; ++jj)
+            for (int ii = i0; ii <= i1; ++ii) {
+                const int fc = ii + F.sy * jj + F.sz * kk;
+                act |= F.active[fc];
+                ex += F.extra[fc];
+                if (ii == i1) se += F.cE[fc];
+                if (jj == j1) sn += F.cN[fc];
+                if (kk == k1) sT += F.cT[fc];
+            }
+    C.active[cc] = act;
+    C.extra[cc] = T(0.5) * ex;
+    C.cE[cc] = i < C.n0 ? se / T(f0) : T(0);
+    C.cN[cc] = j < C.n1 ? sn / T(f1) : T(0);
+    C.cT[cc] = k < C.n2 ? sT / T(f2) : T(0);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_coarsen_diag(MgLevel<T> C)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z + 1;
+    if (i > C.n0 || j > C.n1 || k > C.n2) return;
+    const int c = i + C.sy * j + C.sz * k;
+    if (!C.active[c]) {
+        C.diag[c] = T(1);
+        C.dinv[c] = T(0);
+        return;
+    }
+    const T dg = C.cE[c] + C.cE[c - 1] + C.cN[c] + C.cN[c - C.sy] + C.cT[c] + C.cT[c - C.sz] + C.extra[c];
+    C.diag[c] = dg;
+    C.dinv[c] = dg > T(0) ? T(1) / dg : T(0);
+}
+
+template <typename T>
+void mg_coarsen(const MgLevel<T> &F, MgLevel<T> &C, cudaStream_t st, int *launches)
+{
+    Launch3 l = launch_interior(C.n0, C.n1, C.n2);
+    k_coarsen_cpl<T><<<l.grid, l.block, 0, st>>>(F, C);
+    k_coarsen_diag<T><<<l.grid, l.block, 0, st>>>(C);
+    *launches += 2;
+}
+
+// Dense inverse of the coarsest operator by in-place Gauss-Jordan (SPD, no
+// pivoting); all-Neumann systems get the rank-one term s*1*1^T on the active
+// cells so that the inverse maps zero-mean vectors to the zero-mean solution.
+template <typename T>
+__global__ void __launch_bounds__(256) k_coarse_inverse(MgLevel<T> L, double *__restrict__ A,
+                                                        const int *__restrict__ map, int n, int singular)
+{
+    __shared__ double fcol[128];
+    __shared__ double red[2];
+    const int t = threadIdx.x;
+    const int nt = blockDim.x;
+    for (int e = t; e < n * n; e += nt) A[e] = 0.0;
+    __syncthreads();
+    double dsum = 0.0, cnt = 0.0;
+    for (int a = t; a < n; a += nt) {
+        const int c = map[a];
+        A[(size_t)a * n + a] = (double)L.diag[c];
+        if (L.active[c]) { dsum += (double)L.diag[c]; cnt += 1.0; }
+        const int nb[6] = {c + 1, c - 1, c + L.sy, c - L.sy, c + L.sz, c - L.sz};
+        const T w[6] = {L.cE[c], L.cE[c - 1], L.cN[c], L.cN[c - L.sy], L.cT[c], L.cT[c - L.sz]};
+        for (int q = 0; q < 6; ++q) {
+            if (w[q] == T(0)) continue;
+            for (int b = 0; b < n; ++b)
+                if (map[b] == nb[q]) { A[(size_t)a * n + b] -= (double)w[q]; break; }
+        }
+    }
+    dsum = block_sum(dsum);
+    __syncthreads();
+    cnt = block_sum(cnt);
+    if (t == 0) { red[0] = dsum; red[1] = cnt; }
+    __syncthreads();
+    if (singular && red[1] > 0.0) {
+        const double s = red[0] / red[1] / red[1];
+        for (int e = t; e < n * n; e += nt) {
+            const int a = e / n, b = e % n;
+            if (L.active[map[a]] && L.active[map[b]]) A[e] += s;
+        }
+    }
+    __syncthreads();
+    for (int kk = 0; kk < n; ++kk) {
+        const double piv = A[(size_t)kk * n + kk];
+        const double pinv = piv > 0.0 ? 1.0 / piv : 0.0;
+        for (int a = t; a < n; a += nt) fcol[a] = A[(size_t)a * n + kk];
+        __syncthreads();
+        for (int b = t; b < n; b += nt) A[(size_t)kk * n + b] = (b == kk) ? pinv : A[(size_t)kk * n + b] * pinv;
+        __syncthreads();
+        for (int e = t; e < n * n; e += nt) {
+            const int a = e / n, b = e % n;
+            if (a == kk) continue;
+            if (b == kk)
+                A[e] = -fcol[a] * pinv;
+            else
+                A[e] -= fcol[a] * A[(size_t)kk * n + b];
+        }
+        __syncthreads();
+    }
+}
+
+template <typename T>
+void mg_coarse_inverse(const MgLevel<T> &L, double *ainv, int *map, int n, bool singular, cudaStream_t st,
+                       int *launches)
+{
+    k_coarse_inverse<T><<<1, 256, 0, st>>>(L, ainv, map, n, singular ? 1 : 0);
+    *launches += 1;
+}
+
+template <typename T>
+T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, const int *map, int ncoarse,
+             bool singular, cudaStream_t st, int *launches)
+{
+    T *cur[32];
+    const int last = nlev - 1;
+    for (int l = 0; l < last; ++l) {
+        MgLevel<T> &F = L[l];
+        LevelView<T> v = F.view();
+        Launch3 lf = launch_interior(F.n0, F.n1, F.n2);
+        T *xa = F.x, *xb = F.xb;
+        k_cheb_first<T><<<lf.grid, lf.block, 0, st>>>(v, F.b, xa, (T)cc.first);
+        *launches += 1;
+        for (int s = 1; s < cc.degree; ++s) {
+            const T *dprev = (s == 1) ? xa : F.d;
+            k_cheb_step<T><<<lf.grid, lf.block, 0, st>>>(v, F.b, xa, dprev, xb, F.d, (T)cc.c1[s], (T)cc.c2[s]);
+            *launches += 1;
+            T *tmp = xa; xa = xb; xb = tmp;
+        }
+        cur[l] = xa;
+        MgLevel<T> &C = L[l + 1];
+        Launch3 lc = launch_interior(C.n0, C.n1, C.n2);
+        k_restrict<T><<<lc.grid, lc.block, 0, st>>>(v, F.b, xa, C.view(), C.b, F.f0, F.f1, F.f2);
+        *launches += 1;
+    }
+    {
+        MgLevel<T> &Cst = L[last];
+        k_coarse_solve<T><<<1, 128, 0, st>>>(Cst.b, Cst.x, Cst.active, ainv, map, ncoarse, singular ? 1 : 0);
+        *launches += 1;
+        cur[last] = Cst.x;
+    }
+    for (int l = last - 1; l >= 0; --l) {
+        MgLevel<T> &F = L[l];
+        MgLevel<T> &C = L[l + 1];
+        LevelView<T> v = F.view();
+        Launch3 lf = launch_interior(F.n0, F.n1, F.n2);
+        T *xa = cur[l];
+        T *xb = (xa == F.x) ? F.xb : F.x;
+        const bool more = cc.degree > 1;
+        k_post_first<T><<<lf.grid, lf.block, 0, st>>>(v, F.b, xa, C.view(), cur[l + 1], xb, more ? F.d : nullptr,
+                                                      F.f0, F.f1, F.f2, (T)cc.first);
+        *launches += 1;
+        { T *tmp = xa; xa = xb; xb = tmp; }
+        for (int s = 1; s < cc.degree; ++s) {
+            const bool last_step = s == cc.degree - 1;
+            k_cheb_step<T><<<lf.grid, lf.block, 0, st>>>(v, F.b, xa, F.d, xb, last_step ? nullptr : F.d,
+                                                         (T)cc.c1[s], (T)cc.c2[s]);
+            *launches += 1;
+            T *tmp = xa; xa = xb; xb = tmp;
+        }
+        cur[l] = xa;
+    }
+    return cur[0];
+}
+
+// explicit instantiations
+template void mg_coarsen<float>(const MgLevel<float> &, MgLevel<float> &, cudaStream_t, int *);
+template void mg_coarsen<double>(const MgLevel<double> &, MgLevel<double> &, cudaStream_t, int *);
+template void mg_coarse_inverse<float>(const MgLevel<float> &, double *, int *, int, bool, cudaStream_t, int *);
+template void mg_coarse_inverse<double>(const MgLevel<double> &, double *, int *, int, bool, cudaStream_t, int *);
+template float *mg_vcycle<float>(MgLevel<float> *, int, const ChebCoef &, const double *, const int *, int, bool,
+                                 cudaStream_t, int *);
+template double *mg_vcycle<double>(MgLevel<double> *, int, const ChebCoef &, const double *, const int *, int, bool,
+                                   cudaStream_t, int *);
+template void cg_update<float>(const LevelView<double> &, double *, double *, const double *, const double *, float *,
+                               Reducer &, cudaStream_t, int *);
+template void cg_update<double>(const LevelView<double> &, double *, double *, const double *, const double *,
+                                double *, Reducer &, cudaStream_t, int *);
+template void cg_dot_rz<float>(const LevelView<double> &, const double *, const float *, Reducer &, cudaStream_t,
+                               int *);
+template void cg_dot_rz<double>(const LevelView<double> &, const double *, const double *, Reducer &, cudaStream_t,
+                                int *);
+template void cg_pupdate<float>(const LevelView<double> &, const float *, double *, const double *, bool,
+                                cudaStream_t, int *);
+template void cg_pupdate<double>(const LevelView<double> &, const double *, double *, const double *, bool,
+                                 cudaStream_t, int *);

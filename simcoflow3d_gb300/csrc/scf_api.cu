@@ -1,0 +1,887 @@
+// scf_api.cu -- C ABI of the GB300 projection (include/scf_projection.h).
+//
+// Host orchestration: device mirrors of the Fortran arrays, assembly, the
+// multigrid hierarchy, the preconditioned CG loop and the correction.  All
+// work of a context runs on one CUDA stream; calls are synchronous.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <chrono>
+#include <vector>
+#include "scf_kernels.h"
+#include "../../include/scf_projection.h"
+
+namespace {
+
+struct DevBuf {
+    std::vector<void *> ptrs;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        for (void *p : ptrs) cudaFree(p);
+        ptrs.clear();
+    }
+};
+
+}  // namespace
+
+struct scf_ctx {
+    Dims d;
+    scf_opts opts;
+    cudaStream_t st = nullptr;
+    char err[512] = {0};
+    DevBuf mem, mgmem;
+    // inputs (device)
+    double *pdx, *pdy, *pdz, *udx, *vdy, *wdz;
+    double *phil, *vofl, *vof, *ee, *ne, *te, *vofo, *us, *vs, *ws, *dpu, *dpv, *dpw;
+    int *ct, *pos;
+    int *umoex, *uct, *vmoex, *vct, *wmoex, *wct;
+    double *tu, *tv, *tw, *tp;
+    double *bvar[6];
+    int ext_cell = -1;
+    int bcp_flag[6];
+    double dt = 0.0;
+    scf_correct_in corr;
+    bool have_corr = false;
+    bool staged = false;
+    bool solved = false;
+    bool assembled = false;
+    // assembly scratch
+    double *pocoef;
+    unsigned *stale_count, *flags;
+    long long *stale_list;
+    unsigned stale_cap;
+    double *col_val, *grp_val;
+    unsigned short *col_mask, *grp_mask;
+    // level-0 operator, FP64
+    double *diag, *dinv, *cE, *cN, *cT, *extra, *b;
+    unsigned char *active;
+    float *diag32, *dinv32, *cE32, *cN32, *cT32, *extra32;
+    // CG vectors
+    double *x, *r, *p, *q;
+    // multigrid
+    int nlev = 0;
+    int mg_precision = -1;
+    MgLevel<double> L64[32];
+    MgLevel<float> L32[32];
+    double *ainv;
+    int *map;
+    int ncoarse = 0;
+    Reducer R;
+    // correction
+    double *pp;
+    double *bcvar[4][6];
+    // host pinned scratch
+    double *h_scal = nullptr;
+    unsigned *h_u32 = nullptr;
+    cudaEvent_t ev[8];
+    int launches = 0;
+};
+
+namespace {
+
+void set_err(scf_ctx *c, const char *fmt, ...)
+{
+    if (!c) return;
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(c->err, sizeof(c->err), fmt, ap);
+    va_end(ap);
+}
+
+#define CK(call)                                                                           \
+    do {                                                                                   \
+        cudaError_t e_ = (call);                                                           \
+        if (e_ != cudaSuccess) {                                                           \
+            set_err(ctx, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return e_ == cudaErrorMemoryAllocation ? SCF_ERR_OUT_OF_MEMORY : SCF_ERR_CUDA;  \
+        }                                                                                  \
+    } while (0)
+
+template <typename P>
+int dalloc(scf_ctx *ctx, DevBuf &mem, P **ptr, size_t count)
+{
+    void *p = nullptr;
+    size_t bytes = count * sizeof(P);
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) {
+        set_err(ctx, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
+        return SCF_ERR_OUT_OF_MEMORY;
+    }
+    cudaMemset(p, 0, bytes);
+    mem.ptrs.push_back(p);
+    *ptr = (P *)p;
+    return SCF_OK;
+}
+
+#define DALLOC(mem, ptr, n)                          \
+    do {                                             \
+        int rc_ = dalloc(ctx, mem, &(ptr), (size_t)(n)); \
+        if (rc_) return rc_;                         \
+    } while (0)
+
+bool is_singular(const scf_ctx *ctx)
+{
+    for (int q = 0; q < 6; ++q)
+        if (ctx->bcp_flag[q] == 0) return false;
+    return true;
+}
+
+template <typename T>
+int alloc_level(scf_ctx *ctx, MgLevel<T> &L, int n0, int n1, int n2, bool own_op)
+{
+    L.n0 = n0; L.n1 = n1; L.n2 = n2;
+    L.sy = n0 + 2;
+    L.sz = L.sy * (n1 + 2);
+    L.tot = L.sz * (n2 + 2);
+    if (own_op) {
+        DALLOC(ctx->mgmem, L.diag, L.tot);
+        DALLOC(ctx->mgmem, L.dinv, L.tot);
+        DALLOC(ctx->mgmem, L.cE, L.tot);
+        DALLOC(ctx->mgmem, L.cN, L.tot);
+        DALLOC(ctx->mgmem, L.cT, L.tot);
+        DALLOC(ctx->mgmem, L.extra, L.tot);
+        DALLOC(ctx->mgmem, L.active, L.tot);
+        DALLOC(ctx->mgmem, L.b, L.tot);
+    }
+    DALLOC(ctx->mgmem, L.x, L.tot);
+    DALLOC(ctx->mgmem, L.xb, L.tot);
+    DALLOC(ctx->mgmem, L.d, L.tot);
+    return SCF_OK;
+}
+
+// Level sizes and factors; fills ctx->nlev.
+void plan_levels(scf_ctx *ctx, int dims[][3], int fac[][3])
+{
+    int n0 = ctx->d.I, n1 = ctx->d.J, n2 = ctx->d.K;
+    int cmax = ctx->opts.coarse_max_cells;
+    int l = 0;
+    dims[0][0] = n0; dims[0][1] = n1; dims[0][2] = n2;
+    while ((long long)n0 * n1 * n2 > cmax && (n0 > 2 || n1 > 2 || n2 > 2) && l < 30) {
+        fac[l][0] = n0 > 2 ? 2 : 1;
+        fac[l][1] = n1 > 2 ? 2 : 1;
+        fac[l][2] = n2 > 2 ? 2 : 1;
+        n0 = (n0 + fac[l][0] - 1) / fac[l][0];
+        n1 = (n1 + fac[l][1] - 1) / fac[l][1];
+        n2 = (n2 + fac[l][2] - 1) / fac[l][2];
+        ++l;
+        dims[l][0] = n0; dims[l][1] = n1; dims[l][2] = n2;
+    }
+    fac[l][0] = fac[l][1] = fac[l][2] = 1;
+    ctx->nlev = l + 1;
+}
+
+template <typename T>
+int build_levels(scf_ctx *ctx, MgLevel<T> *L, int dims[][3], int fac[][3])
+{
+    for (int l = 0; l < ctx->nlev; ++l) {
+        int rc = alloc_level<T>(ctx, L[l], dims[l][0], dims[l][1], dims[l][2], l > 0);
+        if (rc) return rc;
+        L[l].f0 = fac[l][0]; L[l].f1 = fac[l][1]; L[l].f2 = fac[l][2];
+    }
+    return SCF_OK;
+}
+
+int ensure_mg(scf_ctx *ctx)
+{
+    const int prec = ctx->opts.precision;
+    if (ctx->mg_precision == prec) return SCF_OK;
+    ctx->mgmem.release();
+    int dims[32][3], fac[32][3];
+    plan_levels(ctx, dims, fac);
+    int rc;
+    if (prec == SCF_PREC_FP64) {
+        rc = build_levels<double>(ctx, ctx->L64, dims, fac);
+        if (rc) return rc;
+        MgLevel<double> &L0 = ctx->L64[0];
+        L0.diag = ctx->diag; L0.dinv = ctx->dinv; L0.cE = ctx->cE; L0.cN = ctx->cN; L0.cT = ctx->cT;
+        L0.extra = ctx->extra; L0.active = ctx->active; L0.b = ctx->r;
+    } else {
+        rc = build_levels<float>(ctx, ctx->L32, dims, fac);
+        if (rc) return rc;
+        MgLevel<float> &L0 = ctx->L32[0];
+        DALLOC(ctx->mgmem, ctx->diag32, L0.tot);
+        DALLOC(ctx->mgmem, ctx->dinv32, L0.tot);
+        DALLOC(ctx->mgmem, ctx->cE32, L0.tot);
+        DALLOC(ctx->mgmem, ctx->cN32, L0.tot);
+        DALLOC(ctx->mgmem, ctx->cT32, L0.tot);
+        DALLOC(ctx->mgmem, ctx->extra32, L0.tot);
+        DALLOC(ctx->mgmem, L0.b, L0.tot);
+        L0.diag = ctx->diag32; L0.dinv = ctx->dinv32; L0.cE = ctx->cE32; L0.cN = ctx->cN32; L0.cT = ctx->cT32;
+        L0.extra = ctx->extra32; L0.active = ctx->active;
+    }
+    // coarsest dense map
+    const int last = ctx->nlev - 1;
+    const int c0 = dims[last][0], c1 = dims[last][1], c2 = dims[last][2];
+    ctx->ncoarse = c0 * c1 * c2;
+    std::vector<int> hmap;
+    const int sy = c0 + 2, sz = sy * (c1 + 2);
+    for (int k = 1; k <= c2; ++k)
+        for (int j = 1; j <= c1; ++j)
+            for (int i = 1; i <= c0; ++i) hmap.push_back(i + sy * j + sz * k);
+    DALLOC(ctx->mgmem, ctx->map, hmap.size());
+    DALLOC(ctx->mgmem, ctx->ainv, (size_t)ctx->ncoarse * ctx->ncoarse);
+    CK(cudaMemcpy(ctx->map, hmap.data(), hmap.size() * sizeof(int), cudaMemcpyHostToDevice));
+    ctx->mg_precision = prec;
+    return SCF_OK;
+}
+
+int check_flags(scf_ctx *ctx)
+{
+    CK(cudaMemcpyAsync(ctx->h_u32, ctx->flags, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    const unsigned f = *ctx->h_u32;
+    if (!f) return SCF_OK;
+    if (f & FLAG_NONFINITE) { set_err(ctx, "non-finite value in the assembled system (flags 0x%x)", f); return SCF_ERR_NONFINITE; }
+    if (f & FLAG_BAD_POSNU) { set_err(ctx, "PosNu is not -1 exactly on the Cell_Type==2 cells, or exceeds ExtCell"); return SCF_ERR_BAD_INPUT; }
+    if (f & FLAG_STALE_OVERFLOW) { set_err(ctx, "too many cells with a carried GFM coefficient"); return SCF_ERR_BAD_INPUT; }
+    if (ctx->opts.check_inputs) {
+        if (f & FLAG_NEITHER_ACTIVE) { set_err(ctx, "an active cell (Cell_Type/=2) is neither wet nor dry (vof <= epsi)"); return SCF_ERR_BAD_INPUT; }
+        if (f & FLAG_BAD_DIAG) { set_err(ctx, "an active row has a non-positive diagonal (all faces closed)"); return SCF_ERR_BAD_INPUT; }
+    }
+    return SCF_OK;
+}
+
+AsmArgs asm_args(scf_ctx *ctx)
+{
+    AsmArgs a;
+    a.d = ctx->d;
+    a.pdx = ctx->pdx; a.pdy = ctx->pdy; a.pdz = ctx->pdz;
+    a.udx = ctx->udx; a.vdy = ctx->vdy; a.wdz = ctx->wdz;
+    a.phil = ctx->phil; a.vofl = ctx->vofl; a.vof = ctx->vof; a.ee = ctx->ee; a.ne = ctx->ne; a.te = ctx->te;
+    a.vofo = ctx->vofo; a.us = ctx->us; a.vs = ctx->vs; a.ws = ctx->ws;
+    a.dpu = ctx->dpu; a.dpv = ctx->dpv; a.dpw = ctx->dpw;
+    a.ct = ctx->ct; a.pos = ctx->pos; a.ext_cell = ctx->ext_cell;
+    for (int q = 0; q < 6; ++q) { a.flag[q] = ctx->bcp_flag[q]; a.bvar[q] = ctx->bvar[q]; }
+    const double rho_ref = ctx->opts.rho_ref > 0.0 ? ctx->opts.rho_ref : ctx->opts.rho_l;
+    a.dt = ctx->dt;
+    a.betap = 1.0 / (ctx->opts.rho_l / rho_ref);
+    a.betam = 1.0 / (ctx->opts.rho_g / rho_ref);
+    a.epsi = ctx->opts.epsi;
+    a.tol = ctx->opts.gfm_tol;
+    a.stale_init = ctx->opts.stale_init;
+    a.pocoef = ctx->pocoef;
+    a.stale_count = ctx->stale_count; a.stale_cap = ctx->stale_cap; a.stale_list = ctx->stale_list;
+    a.col_val = ctx->col_val; a.col_mask = ctx->col_mask; a.grp_val = ctx->grp_val; a.grp_mask = ctx->grp_mask;
+    a.flags = ctx->flags;
+    return a;
+}
+
+LevelView<double> fine_view(scf_ctx *ctx)
+{
+    LevelView<double> v;
+    v.n0 = ctx->d.I; v.n1 = ctx->d.J; v.n2 = ctx->d.K;
+    v.sy = ctx->d.gx; v.sz = ctx->d.gx * ctx->d.gy;
+    v.diag = ctx->diag; v.dinv = ctx->dinv; v.cE = ctx->cE; v.cN = ctx->cN; v.cT = ctx->cT;
+    return v;
+}
+
+int assemble(scf_ctx *ctx)
+{
+    int rc = ensure_mg(ctx);
+    if (rc) return rc;
+    CK(cudaMemsetAsync(ctx->flags, 0, sizeof(unsigned), ctx->st));
+    AsmArgs a = asm_args(ctx);
+    OpArgs o;
+    o.diag = ctx->diag; o.dinv = ctx->dinv; o.cE = ctx->cE; o.cN = ctx->cN; o.cT = ctx->cT;
+    o.extra = ctx->extra; o.b = ctx->b; o.active = ctx->active;
+    const bool mixed = ctx->opts.precision == SCF_PREC_MIXED;
+    o.diag32 = ctx->diag32; o.dinv32 = ctx->dinv32; o.cE32 = ctx->cE32; o.cN32 = ctx->cN32; o.cT32 = ctx->cT32;
+    o.extra32 = ctx->extra32;
+    int e = launch_assemble(a, o, mixed, ctx->st, ctx->h_u32, &ctx->launches);
+    if (e) { set_err(ctx, "assembly launch: %s", cudaGetErrorString((cudaError_t)e)); return SCF_ERR_CUDA; }
+    rc = check_flags(ctx);
+    if (rc) return rc;
+    ctx->assembled = true;
+    return SCF_OK;
+}
+
+template <typename T>
+void build_hierarchy(scf_ctx *ctx, MgLevel<T> *L)
+{
+    for (int l = 0; l + 1 < ctx->nlev; ++l) mg_coarsen<T>(L[l], L[l + 1], ctx->st, &ctx->launches);
+    mg_coarse_inverse<T>(L[ctx->nlev - 1], ctx->ainv, ctx->map, ctx->ncoarse, is_singular(ctx), ctx->st,
+                         &ctx->launches);
+}
+
+ChebCoef cheb_coef(int degree)
+{
+    ChebCoef cc;
+    if (degree < 1) degree = 1;
+    if (degree > 8) degree = 8;
+    cc.degree = degree;
+    const double lmax = 2.0, lmin = lmax / 6.0;
+    const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin), sigma = theta / delta;
+    cc.first = 1.0 / theta;
+    double rho = 1.0 / sigma;
+    for (int s = 1; s < degree; ++s) {
+        const double rn = 1.0 / (2.0 * sigma - rho);
+        cc.c1[s] = rn * rho;
+        cc.c2[s] = 2.0 * rn / delta;
+        rho = rn;
+    }
+    return cc;
+}
+
+double read_scal(scf_ctx *ctx, int slot)
+{
+    cudaMemcpyAsync(ctx->h_scal, ctx->R.scal + slot, sizeof(double), cudaMemcpyDeviceToHost, ctx->st);
+    cudaStreamSynchronize(ctx->st);
+    return ctx->h_scal[0];
+}
+
+template <typename T>
+T *precondition(scf_ctx *ctx, MgLevel<T> *L, const ChebCoef &cc)
+{
+    return mg_vcycle<T>(L, ctx->nlev, cc, ctx->ainv, ctx->map, ctx->ncoarse, is_singular(ctx), ctx->st,
+                        &ctx->launches);
+}
+
+template <typename T>
+int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
+{
+    const LevelView<double> A = fine_view(ctx);
+    const bool singular = is_singular(ctx);
+    const bool mixed = sizeof(T) == 4;
+    float *rlow = mixed ? (float *)L[0].b : nullptr;
+    const ChebCoef cc = cheb_coef(ctx->opts.smoother_degree);
+    auto t0 = std::chrono::steady_clock::now();
+    if (singular) {
+        active_sum(A, ctx->active, nullptr, ctx->R, ctx->st, &ctx->launches);
+        active_sum(A, ctx->active, ctx->b, ctx->R, ctx->st, &ctx->launches);
+        subtract_mean(A, ctx->active, ctx->b, ctx->R.scal, ctx->st, &ctx->launches);
+    }
+    build_hierarchy<T>(ctx, L);
+    dot_self(A, ctx->b, ctx->R, S_BB, ctx->st, &ctx->launches);
+    const double bb = read_scal(ctx, S_BB);
+    const double bn = std::sqrt(bb);
+    stats->rhs_norm = bn;
+    stats->singular = singular ? 1 : 0;
+    stats->levels = ctx->nlev;
+    int its = 0;
+    double rel = 0.0;
+    if (!(bn > 0.0)) {
+        CK(cudaMemsetAsync(ctx->x, 0, sizeof(double) * ctx->d.ng, ctx->st));
+        stats->iterations = 0;
+        stats->rounds = 1;
+        stats->rel_residual = 0.0;
+        stats->converged = 1;
+        return std::isfinite(bb) ? SCF_OK : SCF_ERR_NONFINITE;
+    }
+    if (ctx->opts.warm_start && ctx->solved) {
+        cg_residual(A, ctx->b, ctx->x, ctx->r, ctx->R, ctx->st, &ctx->launches);
+        if (singular) {
+            active_sum(A, ctx->active, ctx->r, ctx->R, ctx->st, &ctx->launches);
+            subtract_mean(A, ctx->active, ctx->r, ctx->R.scal, ctx->st, &ctx->launches);
+        }
+    } else {
+        CK(cudaMemsetAsync(ctx->x, 0, sizeof(double) * ctx->d.ng, ctx->st));
+        CK(cudaMemcpyAsync(ctx->r, ctx->b, sizeof(double) * ctx->d.ng, cudaMemcpyDeviceToDevice, ctx->st));
+    }
+    const double tol = ctx->opts.rel_tol;
+    int restarts = 0;
+    for (;;) {
+        if (mixed) copy_to_low(A, ctx->r, rlow, ctx->st, &ctx->launches);
+        T *z = precondition<T>(ctx, L, cc);
+        cg_dot_rz<T>(A, ctx->r, z, ctx->R, ctx->st, &ctx->launches);
+        cg_pupdate<T>(A, z, ctx->p, ctx->R.scal, true, ctx->st, &ctx->launches);
+        bool conv = false;
+        while (its < ctx->opts.max_iter) {
+            ++its;
+            cg_spmv_dot(A, ctx->p, ctx->q, ctx->R, S_PQ, ctx->st, &ctx->launches);
+            cg_update<float>(A, ctx->x, ctx->r, ctx->p, ctx->q, rlow, ctx->R, ctx->st, &ctx->launches);
+            const double rr = read_scal(ctx, S_RR);
+            if (!std::isfinite(rr)) {
+                set_err(ctx, "CG residual became non-finite at iteration %d", its);
+                stats->iterations = its;
+                return SCF_ERR_NONFINITE;
+            }
+            if (std::sqrt(rr) <= tol * bn) { conv = true; break; }
+            const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            if (el > ctx->opts.time_limit_s) break;
+            z = precondition<T>(ctx, L, cc);
+            cg_dot_rz<T>(A, ctx->r, z, ctx->R, ctx->st, &ctx->launches);
+            cg_pupdate<T>(A, z, ctx->p, ctx->R.scal, false, ctx->st, &ctx->launches);
+        }
+        // true FP64 residual (the refinement check)
+        if (singular) {
+            active_sum(A, ctx->active, ctx->x, ctx->R, ctx->st, &ctx->launches);
+            subtract_mean(A, ctx->active, ctx->x, ctx->R.scal, ctx->st, &ctx->launches);
+        }
+        cg_residual(A, ctx->b, ctx->x, ctx->r, ctx->R, ctx->st, &ctx->launches);
+        if (singular) {
+            active_sum(A, ctx->active, ctx->r, ctx->R, ctx->st, &ctx->launches);
+            subtract_mean(A, ctx->active, ctx->r, ctx->R.scal, ctx->st, &ctx->launches);
+            dot_self(A, ctx->r, ctx->R, S_RR, ctx->st, &ctx->launches);
+        }
+        rel = std::sqrt(read_scal(ctx, S_RR)) / bn;
+        if (rel <= tol || !conv || its >= ctx->opts.max_iter || restarts >= ctx->opts.max_rounds) break;
+        ++restarts;  // recursive residual drifted below the true one: restart from the true residual
+    }
+    stats->iterations = its;
+    stats->rounds = restarts + 1;
+    stats->rel_residual = rel;
+    stats->converged = rel <= tol ? 1 : 0;
+    if (!stats->converged) {
+        set_err(ctx, "not converged: relative residual %.3e after %d iterations (tolerance %.1e)", rel, its, tol);
+        return SCF_ERR_NOT_CONVERGED;
+    }
+    return SCF_OK;
+}
+
+CorrArgs corr_args(scf_ctx *ctx)
+{
+    CorrArgs a;
+    a.d = ctx->d;
+    a.x = ctx->x; a.ct = ctx->ct; a.pp = ctx->pp; a.pocoef = ctx->pocoef;
+    a.us = ctx->us; a.vs = ctx->vs; a.ws = ctx->ws;
+    a.umoex = ctx->umoex; a.uct = ctx->uct; a.vmoex = ctx->vmoex; a.vct = ctx->vct;
+    a.wmoex = ctx->wmoex; a.wct = ctx->wct;
+    a.u = ctx->tu; a.v = ctx->tv; a.w = ctx->tw; a.p = ctx->tp;
+    a.pdx = ctx->pdx; a.pdy = ctx->pdy; a.pdz = ctx->pdz;
+    a.ee = ctx->ee; a.ne = ctx->ne; a.te = ctx->te;
+    for (int q = 0; q < 6; ++q) {
+        a.bcp_flag[q] = ctx->bcp_flag[q];
+        a.flag[0][q] = ctx->corr.bcu_flag[q]; a.flag[1][q] = ctx->corr.bcv_flag[q];
+        a.flag[2][q] = ctx->corr.bcw_flag[q]; a.flag[3][q] = ctx->bcp_flag[q];
+        a.cst[0][q] = ctx->corr.bcu_const[q]; a.cst[1][q] = ctx->corr.bcv_const[q];
+        a.cst[2][q] = ctx->corr.bcw_const[q]; a.cst[3][q] = ctx->corr.bcp_const[q];
+        for (int f = 0; f < 4; ++f) a.bcvar[f][q] = ctx->bcvar[f][q];
+    }
+    a.north_fix = ctx->opts.north_mass_fix;
+    a.flags = ctx->flags;
+    return a;
+}
+
+size_t plane_size(const Dims &d, int face)
+{
+    const int axis = face >> 1;
+    return axis == 0 ? (size_t)d.J * d.K : axis == 1 ? (size_t)d.I * d.K : (size_t)d.I * d.J;
+}
+
+int check_ctx(scf_ctx *ctx)
+{
+    if (!ctx) return SCF_ERR_BAD_ARG;
+    cudaError_t e = cudaSetDevice(ctx->opts.device);
+    if (e != cudaSuccess) { set_err(ctx, "cudaSetDevice: %s", cudaGetErrorString(e)); return SCF_ERR_CUDA; }
+    return SCF_OK;
+}
+
+int run(scf_ctx *ctx, bool with_correction, scf_stats *stats)
+{
+    scf_stats local;
+    if (!stats) stats = &local;
+    memset(stats, 0, sizeof(*stats));
+    if (!ctx->staged) { set_err(ctx, "no inputs staged"); return SCF_ERR_NO_SOLVE; }
+    if (with_correction && !ctx->have_corr) { set_err(ctx, "no correction inputs staged"); return SCF_ERR_BAD_ARG; }
+    if (with_correction && ctx->bcp_flag[0] != 0 && ctx->bcp_flag[1] != 0 && ctx->bcp_flag[2] != 0 &&
+        ctx->bcp_flag[3] == 0 && !ctx->opts.north_mass_fix) {
+        set_err(ctx, "the reference's North-face mass correction (ComputePUVW.f90:323-341) has no defined "
+                     "result (stale k, PGrid indexed out of bounds); set opts.north_mass_fix = 1 for the "
+                     "evident intent");
+        return SCF_ERR_UNDEFINED_IN_REFERENCE;
+    }
+    ctx->launches = 0;
+    cudaEventRecord(ctx->ev[0], ctx->st);
+    int rc = assemble(ctx);
+    if (rc) return rc;
+    cudaEventRecord(ctx->ev[1], ctx->st);
+    if (ctx->opts.precision == SCF_PREC_FP64)
+        rc = solve_impl<double>(ctx, ctx->L64, stats);
+    else
+        rc = solve_impl<float>(ctx, ctx->L32, stats);
+    cudaEventRecord(ctx->ev[2], ctx->st);
+    if (rc && rc != SCF_ERR_NOT_CONVERGED) return rc;
+    const int solve_rc = rc;
+    ctx->solved = true;
+    CorrArgs ca = corr_args(ctx);
+    launch_scatter(ca, ctx->st, &ctx->launches);
+    if (with_correction) launch_correct(ca, ctx->st, &ctx->launches);
+    cudaEventRecord(ctx->ev[3], ctx->st);
+    CK(cudaEventSynchronize(ctx->ev[3]));
+    CK(cudaGetLastError());
+    float ms;
+    cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]); stats->ms_assemble = ms;
+    cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]); stats->ms_solve = ms;
+    cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]); stats->ms_correct = ms;
+    cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[3]); stats->ms_total = ms;
+    stats->gpu_launches = ctx->launches;
+    return solve_rc;
+}
+
+template <typename P>
+int h2d(scf_ctx *ctx, P *dst, const P *src, size_t n, int64_t *bytes)
+{
+    if (!src) { set_err(ctx, "null input array"); return SCF_ERR_BAD_ARG; }
+    CK(cudaMemcpyAsync(dst, src, n * sizeof(P), cudaMemcpyHostToDevice, ctx->st));
+    *bytes += (int64_t)(n * sizeof(P));
+    return SCF_OK;
+}
+#define H2D(dst, src, n)                                   \
+    do {                                                   \
+        int rc_ = h2d(ctx, dst, src, (size_t)(n), &bytes); \
+        if (rc_) return rc_;                               \
+    } while (0)
+
+int stage(scf_ctx *ctx, const scf_poisson_in *in, const scf_correct_in *corr, const double *u, const double *v,
+          const double *w, const double *p, int64_t *bytes_out)
+{
+    if (!in) { set_err(ctx, "null scf_poisson_in"); return SCF_ERR_BAD_ARG; }
+    const Dims &d = ctx->d;
+    int64_t bytes = 0;
+    for (int q = 0; q < 6; ++q) {
+        if (in->bcp_flag[q] != 0 && in->bcp_flag[q] != 1) { set_err(ctx, "BCp flag %d is %d (0 or 1 expected)", q + 1, in->bcp_flag[q]); return SCF_ERR_BAD_ARG; }
+    }
+    if (!(in->dt > 0.0) || !std::isfinite(in->dt)) { set_err(ctx, "dt must be positive and finite"); return SCF_ERR_BAD_ARG; }
+    if (in->pcell_extcell < -1 || in->pcell_extcell >= d.n) { set_err(ctx, "ExtCell %d out of range", in->pcell_extcell); return SCF_ERR_BAD_ARG; }
+    H2D(ctx->pdx, in->pgrid_dx, d.n); H2D(ctx->pdy, in->pgrid_dy, d.n); H2D(ctx->pdz, in->pgrid_dz, d.n);
+    H2D(ctx->udx, in->ugrid_dx, d.n); H2D(ctx->vdy, in->vgrid_dy, d.n); H2D(ctx->wdz, in->wgrid_dz, d.n);
+    H2D(ctx->phil, in->pcell_phil, d.ng); H2D(ctx->vofl, in->pcell_vofl, d.ng); H2D(ctx->vof, in->pcell_vof, d.ng);
+    H2D(ctx->ee, in->pcell_eearea, d.ng); H2D(ctx->ne, in->pcell_nearea, d.ng); H2D(ctx->te, in->pcell_tearea, d.ng);
+    H2D(ctx->ct, in->pcell_cell_type, d.n); H2D(ctx->pos, in->pcell_posnu, d.n);
+    H2D(ctx->vofo, in->vof_old, d.ng);
+    H2D(ctx->us, in->pred_u, d.ng); H2D(ctx->vs, in->pred_v, d.ng); H2D(ctx->ws, in->pred_w, d.ng);
+    H2D(ctx->dpu, in->pu_dp, d.ng); H2D(ctx->dpv, in->pv_dp, d.ng); H2D(ctx->dpw, in->pw_dp, d.ng);
+    for (int q = 0; q < 6; ++q) {
+        ctx->bcp_flag[q] = in->bcp_flag[q];
+        if (in->bcp_flag[q] == 0) H2D(ctx->bvar[q], in->bcp_var[q], plane_size(d, q));
+    }
+    ctx->ext_cell = in->pcell_extcell;
+    ctx->dt = in->dt;
+    ctx->have_corr = false;
+    if (corr) {
+        const int *fl[3] = {corr->bcu_flag, corr->bcv_flag, corr->bcw_flag};
+        for (int f = 0; f < 3; ++f)
+            for (int q = 0; q < 6; ++q)
+                if (fl[f][q] != 0 && fl[f][q] != 1) { set_err(ctx, "velocity BC flag must be 0 or 1"); return SCF_ERR_BAD_ARG; }
+        if (!u || !v || !w || !p) { set_err(ctx, "null TVar array"); return SCF_ERR_BAD_ARG; }
+        H2D(ctx->umoex, corr->ucell_moexcell, d.n); H2D(ctx->uct, corr->ucell_cell_type, d.n);
+        H2D(ctx->vmoex, corr->vcell_moexcell, d.n); H2D(ctx->vct, corr->vcell_cell_type, d.n);
+        H2D(ctx->wmoex, corr->wcell_moexcell, d.n); H2D(ctx->wct, corr->wcell_cell_type, d.n);
+        H2D(ctx->tu, u, d.ng); H2D(ctx->tv, v, d.ng); H2D(ctx->tw, w, d.ng); H2D(ctx->tp, p, d.ng);
+        ctx->corr = *corr;
+        ctx->have_corr = true;
+    }
+    ctx->staged = true;
+    ctx->assembled = false;
+    if (bytes_out) *bytes_out = bytes;
+    return SCF_OK;
+}
+
+template <typename P>
+int d2h(scf_ctx *ctx, P *dst, const P *src, size_t n, int64_t *bytes)
+{
+    if (!dst) return SCF_OK;
+    CK(cudaMemcpyAsync(dst, src, n * sizeof(P), cudaMemcpyDeviceToHost, ctx->st));
+    *bytes += (int64_t)(n * sizeof(P));
+    return SCF_OK;
+}
+
+int fetch(scf_ctx *ctx, double *u, double *v, double *w, double *p, double *pocoef, double *pp, scf_bc_out *bc,
+          int64_t *bytes_out)
+{
+    const Dims &d = ctx->d;
+    int64_t bytes = 0;
+    int rc;
+    if ((rc = d2h(ctx, u, ctx->tu, d.ng, &bytes))) return rc;
+    if ((rc = d2h(ctx, v, ctx->tv, d.ng, &bytes))) return rc;
+    if ((rc = d2h(ctx, w, ctx->tw, d.ng, &bytes))) return rc;
+    if ((rc = d2h(ctx, p, ctx->tp, d.ng, &bytes))) return rc;
+    if ((rc = d2h(ctx, pocoef, ctx->pocoef, (size_t)d.n * 6, &bytes))) return rc;
+    if ((rc = d2h(ctx, pp, ctx->pp, d.ng, &bytes))) return rc;
+    if (bc)
+        for (int f = 0; f < 4; ++f)
+            for (int q = 0; q < 6; ++q)
+                if ((rc = d2h(ctx, bc->var[f][q], ctx->bcvar[f][q], plane_size(d, q), &bytes))) return rc;
+    CK(cudaStreamSynchronize(ctx->st));
+    if (bytes_out) *bytes_out = bytes;
+    return SCF_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+void scf_opts_default(scf_opts *o)
+{
+    if (!o) return;
+    memset(o, 0, sizeof(*o));
+    o->precision = SCF_PREC_FP64;
+    o->rel_tol = 1.0e-10;
+    o->max_iter = 500;
+    o->max_rounds = 12;
+    o->inner_rtol = 1.0e-4;
+    o->smoother_degree = 3;
+    o->coarse_max_cells = 64;
+    o->rho_l = 998.3;
+    o->rho_g = 1.205;
+    o->rho_ref = 0.0;
+    o->epsi = 1.0e-3;
+    o->gfm_tol = 1.0e-30;
+    o->stale_init = std::nan("");
+    o->warm_start = 0;
+    o->north_mass_fix = 0;
+    o->check_inputs = 1;
+    o->device = 0;
+    o->time_limit_s = 60.0;
+}
+
+static int validate_opts(scf_ctx *ctx, const scf_opts *o)
+{
+    if (o->precision != SCF_PREC_FP64 && o->precision != SCF_PREC_MIXED) { set_err(ctx, "bad precision"); return SCF_ERR_BAD_ARG; }
+    if (!(o->rel_tol > 0.0) || o->max_iter < 1 || o->smoother_degree < 1 || o->smoother_degree > 8) { set_err(ctx, "bad solver options"); return SCF_ERR_BAD_ARG; }
+    if (o->coarse_max_cells < 8 || o->coarse_max_cells > 128) { set_err(ctx, "coarse_max_cells must be in [8,128]"); return SCF_ERR_BAD_ARG; }
+    if (!(o->rho_l > 0.0) || !(o->rho_g > 0.0)) { set_err(ctx, "densities must be positive"); return SCF_ERR_BAD_ARG; }
+    return SCF_OK;
+}
+
+int scf_ctx_create(scf_ctx **out, int32_t imax, int32_t jmax, int32_t kmax, const scf_opts *opts)
+{
+    if (!out) return SCF_ERR_BAD_ARG;
+    *out = nullptr;
+    if (imax < 2 || jmax < 2 || kmax < 2) return SCF_ERR_BAD_ARG;
+    const long long n = (long long)imax * jmax * kmax;
+    const long long ng = (long long)(imax + 2) * (jmax + 2) * (kmax + 2);
+    if (6 * n >= (1LL << 31) || ng >= (1LL << 31)) return SCF_ERR_BAD_ARG;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return SCF_ERR_NO_DEVICE;
+    scf_ctx *ctx = new scf_ctx();
+    if (opts) ctx->opts = *opts; else scf_opts_default(&ctx->opts);
+    int rc = validate_opts(ctx, &ctx->opts);
+    if (rc) { delete ctx; return rc; }
+    if (ctx->opts.device < 0 || ctx->opts.device >= ndev) { delete ctx; return SCF_ERR_BAD_ARG; }
+    if (cudaSetDevice(ctx->opts.device) != cudaSuccess) { delete ctx; return SCF_ERR_CUDA; }
+    Dims &d = ctx->d;
+    d.I = imax; d.J = jmax; d.K = kmax;
+    d.gx = imax + 2; d.gy = jmax + 2; d.gz = kmax + 2;
+    d.ng = (int)ng; d.n = (int)n;
+    auto fail = [&](int code) { scf_ctx_destroy(ctx); return code; };
+#define A(ptr, cnt) do { if ((rc = dalloc(ctx, ctx->mem, &(ptr), (size_t)(cnt)))) return fail(rc); } while (0)
+    A(ctx->pdx, n); A(ctx->pdy, n); A(ctx->pdz, n); A(ctx->udx, n); A(ctx->vdy, n); A(ctx->wdz, n);
+    A(ctx->phil, ng); A(ctx->vofl, ng); A(ctx->vof, ng); A(ctx->ee, ng); A(ctx->ne, ng); A(ctx->te, ng);
+    A(ctx->vofo, ng); A(ctx->us, ng); A(ctx->vs, ng); A(ctx->ws, ng);
+    A(ctx->dpu, ng); A(ctx->dpv, ng); A(ctx->dpw, ng);
+    A(ctx->ct, n); A(ctx->pos, n);
+    A(ctx->umoex, n); A(ctx->uct, n); A(ctx->vmoex, n); A(ctx->vct, n); A(ctx->wmoex, n); A(ctx->wct, n);
+    A(ctx->tu, ng); A(ctx->tv, ng); A(ctx->tw, ng); A(ctx->tp, ng);
+    for (int q = 0; q < 6; ++q) A(ctx->bvar[q], plane_size(d, q));
+    A(ctx->pocoef, 6 * n);
+    A(ctx->stale_count, 1); A(ctx->flags, 4);
+    ctx->stale_cap = (unsigned)(n < (1LL << 30) ? n : (1LL << 30));
+    A(ctx->stale_list, ctx->stale_cap);
+    const long long ncol = (long long)imax * jmax, ngrp = (ncol + 63) / 64;
+    A(ctx->col_val, 12 * ncol); A(ctx->col_mask, ncol); A(ctx->grp_val, 12 * ngrp); A(ctx->grp_mask, ngrp);
+    A(ctx->diag, ng); A(ctx->dinv, ng); A(ctx->cE, ng); A(ctx->cN, ng); A(ctx->cT, ng); A(ctx->extra, ng);
+    A(ctx->b, ng); A(ctx->active, ng);
+    A(ctx->x, ng); A(ctx->r, ng); A(ctx->p, ng); A(ctx->q, ng);
+    A(ctx->pp, ng);
+    for (int f = 0; f < 4; ++f)
+        for (int q = 0; q < 6; ++q) A(ctx->bcvar[f][q], plane_size(d, q));
+    Launch3 l = launch_interior(imax, jmax, kmax);
+    ctx->R.max_blocks = (int)nblocks(l);
+    A(ctx->R.partials, ctx->R.max_blocks + 1024);
+    A(ctx->R.scal, S_NUM);
+#undef A
+    if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) return fail(SCF_ERR_CUDA);
+    for (int e = 0; e < 8; ++e) cudaEventCreate(&ctx->ev[e]);
+    if (cudaMallocHost(&ctx->h_scal, 64 * sizeof(double)) != cudaSuccess) return fail(SCF_ERR_OUT_OF_MEMORY);
+    if (cudaMallocHost(&ctx->h_u32, 64 * sizeof(unsigned)) != cudaSuccess) return fail(SCF_ERR_OUT_OF_MEMORY);
+    rc = ensure_mg(ctx);
+    if (rc) return fail(rc);
+    if (cudaDeviceSynchronize() != cudaSuccess) return fail(SCF_ERR_CUDA);
+    *out = ctx;
+    return SCF_OK;
+}
+
+int scf_ctx_destroy(scf_ctx *ctx)
+{
+    if (!ctx) return SCF_OK;
+    cudaSetDevice(ctx->opts.device);
+    if (ctx->st) cudaStreamSynchronize(ctx->st);
+    ctx->mgmem.release();
+    ctx->mem.release();
+    for (int e = 0; e < 8; ++e)
+        if (ctx->ev[e]) cudaEventDestroy(ctx->ev[e]);
+    if (ctx->h_scal) cudaFreeHost(ctx->h_scal);
+    if (ctx->h_u32) cudaFreeHost(ctx->h_u32);
+    if (ctx->st) cudaStreamDestroy(ctx->st);
+    delete ctx;
+    return SCF_OK;
+}
+
+int scf_ctx_set_opts(scf_ctx *ctx, const scf_opts *opts)
+{
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!opts) return SCF_ERR_BAD_ARG;
+    rc = validate_opts(ctx, opts);
+    if (rc) return rc;
+    if (opts->device != ctx->opts.device) { set_err(ctx, "the device of a context cannot change"); return SCF_ERR_BAD_ARG; }
+    const bool replan = opts->coarse_max_cells != ctx->opts.coarse_max_cells;
+    ctx->opts = *opts;
+    if (replan) ctx->mg_precision = -1;
+    return ensure_mg(ctx);
+}
+
+int scf_stage_inputs(scf_ctx *ctx, const scf_poisson_in *in, const scf_correct_in *corr, const double *u,
+                     const double *v, const double *w, const double *p)
+{
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    rc = stage(ctx, in, corr, u, v, w, p, nullptr);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(ctx->st));
+    return SCF_OK;
+}
+
+int scf_run_projection(scf_ctx *ctx, scf_stats *stats)
+{
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    return run(ctx, ctx->have_corr, stats);
+}
+
+int scf_fetch_outputs(scf_ctx *ctx, double *u, double *v, double *w, double *p, double *pocoef, double *pp,
+                      scf_bc_out *bc)
+{
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!ctx->solved) { set_err(ctx, "no projection has run"); return SCF_ERR_NO_SOLVE; }
+    if ((u || v || w || p || bc) && !ctx->have_corr) { set_err(ctx, "the last run had no correction"); return SCF_ERR_BAD_ARG; }
+    return fetch(ctx, u, v, w, p, pocoef, pp, bc, nullptr);
+}
+
+int scf_poisson_solve(scf_ctx *ctx, const scf_poisson_in *in, double *pocoef, double *pp, scf_stats *stats)
+{
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    scf_stats local;
+    if (!stats) stats = &local;
+    auto t0 = std::chrono::steady_clock::now();
+    int64_t bi = 0, bo = 0;
+    rc = stage(ctx, in, nullptr, nullptr, nullptr, nullptr, nullptr, &bi);
+    if (rc) return rc;
+    rc = run(ctx, false, stats);
+    if (rc && rc != SCF_ERR_NOT_CONVERGED) return rc;
+    const int solve_rc = rc;
+    rc = fetch(ctx, nullptr, nullptr, nullptr, nullptr, pocoef, pp, nullptr, &bo);
+    if (rc) return rc;
+    stats->bytes_h2d = bi;
+    stats->bytes_d2h = bo;
+    stats->ms_h2d = 0.0;
+    stats->ms_d2h = 0.0;
+    stats->ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return solve_rc;
+}
+
+int scf_update_puvw(scf_ctx *ctx, const scf_poisson_in *in, const scf_correct_in *corr, double *u, double *v,
+                    double *w, double *p, scf_bc_out *bc, scf_stats *stats)
+{
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!corr || !u || !v || !w || !p) { set_err(ctx, "null correction argument"); return SCF_ERR_BAD_ARG; }
+    scf_stats local;
+    if (!stats) stats = &local;
+    auto t0 = std::chrono::steady_clock::now();
+    int64_t bi = 0, bo = 0;
+    rc = stage(ctx, in, corr, u, v, w, p, &bi);
+    if (rc) return rc;
+    rc = run(ctx, true, stats);
+    if (rc && rc != SCF_ERR_NOT_CONVERGED) return rc;
+    const int solve_rc = rc;
+    rc = fetch(ctx, u, v, w, p, nullptr, nullptr, bc, &bo);
+    if (rc) return rc;
+    stats->bytes_h2d = bi;
+    stats->bytes_d2h = bo;
+    stats->ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return solve_rc;
+}
+
+int scf_debug_apply(scf_ctx *ctx, const double *xh, double *yh)
+{
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!xh || !yh) return SCF_ERR_BAD_ARG;
+    if (!ctx->staged) { set_err(ctx, "no inputs staged"); return SCF_ERR_NO_SOLVE; }
+    if (!ctx->assembled) { ctx->launches = 0; rc = assemble(ctx); if (rc) return rc; }
+    const Dims &d = ctx->d;
+    // p <- x (ghost layer forced to zero), q <- A p
+    std::vector<double> xz(xh, xh + d.ng);
+    for (int k = 0; k < d.gz; ++k)
+        for (int j = 0; j < d.gy; ++j)
+            for (int i = 0; i < d.gx; ++i)
+                if (i == 0 || j == 0 || k == 0 || i == d.gx - 1 || j == d.gy - 1 || k == d.gz - 1)
+                    xz[gidx(d, i, j, k)] = 0.0;
+    CK(cudaMemcpyAsync(ctx->p, xz.data(), sizeof(double) * d.ng, cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemsetAsync(ctx->q, 0, sizeof(double) * d.ng, ctx->st));
+    cg_spmv_dot(fine_view(ctx), ctx->p, ctx->q, ctx->R, S_PQ, ctx->st, &ctx->launches);
+    CK(cudaMemcpyAsync(yh, ctx->q, sizeof(double) * d.ng, cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->solved = false;  // p/q were overwritten
+    return SCF_OK;
+}
+
+int scf_debug_operator(scf_ctx *ctx, double *diag, double *cpl_e, double *cpl_n, double *cpl_t, double *rhs)
+{
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!ctx->staged) { set_err(ctx, "no inputs staged"); return SCF_ERR_NO_SOLVE; }
+    if (!ctx->assembled) { ctx->launches = 0; rc = assemble(ctx); if (rc) return rc; }
+    const Dims &d = ctx->d;
+    std::vector<double> tmp(d.ng);
+    double *outs[5] = {diag, cpl_e, cpl_n, cpl_t, rhs};
+    double *srcs[5] = {ctx->diag, ctx->cE, ctx->cN, ctx->cT, ctx->b};
+    for (int q = 0; q < 5; ++q) {
+        if (!outs[q]) continue;
+        CK(cudaMemcpyAsync(tmp.data(), srcs[q], sizeof(double) * d.ng, cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        for (int k = 1; k <= d.K; ++k)
+            for (int j = 1; j <= d.J; ++j)
+                for (int i = 1; i <= d.I; ++i) outs[q][nidx(d, i, j, k)] = tmp[gidx(d, i, j, k)];
+    }
+    return SCF_OK;
+}
+
+const char *scf_status_string(int s)
+{
+    switch (s) {
+    case SCF_OK: return "ok";
+    case SCF_ERR_BAD_ARG: return "bad argument";
+    case SCF_ERR_NOT_CONVERGED: return "not converged";
+    case SCF_ERR_NONFINITE: return "non-finite value";
+    case SCF_ERR_CUDA: return "CUDA error";
+    case SCF_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case SCF_ERR_BAD_INPUT: return "input outside the reference's model";
+    case SCF_ERR_UNDEFINED_IN_REFERENCE: return "reference path has no defined result";
+    case SCF_ERR_NO_DEVICE: return "no CUDA device";
+    case SCF_ERR_NO_SOLVE: return "no solve/staged inputs";
+    default: return "unknown status";
+    }
+}
+
+int scf_last_error(const scf_ctx *ctx, char *buf, size_t len)
+{
+    if (!ctx || !buf || len == 0) return SCF_ERR_BAD_ARG;
+    snprintf(buf, len, "%s", ctx->err);
+    return SCF_OK;
+}
+
+int scf_host_register(void *ptr, size_t bytes)
+{
+    if (!ptr || !bytes) return SCF_ERR_BAD_ARG;
+    return cudaHostRegister(ptr, bytes, cudaHostRegisterDefault) == cudaSuccess ? SCF_OK : SCF_ERR_CUDA;
+}
+
+int scf_host_unregister(void *ptr)
+{
+    if (!ptr) return SCF_ERR_BAD_ARG;
+    return cudaHostUnregister(ptr) == cudaSuccess ? SCF_OK : SCF_ERR_CUDA;
+}
+
+int scf_abi_version(void) { return SCF_ABI_VERSION; }
+
+}  // extern "C"

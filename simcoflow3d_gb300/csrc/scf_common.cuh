@@ -1,0 +1,100 @@
+// scf_common.cuh -- shared definitions of the GB300 projection library.
+//
+// Layout conventions (the reference's, kept on the device so that every
+// host array moves with one contiguous copy):
+//   ghosted   (0:I+1, 0:J+1, 0:K+1), i fastest: g = i + gx*(j + gy*k)
+//   interior  (1:I, 1:J, 1:K):                  n = (i-1) + I*((j-1) + J*(k-1))
+//   PoCoef    (1:I, 1:J, 1:K, 1:6):             n + N*(f-1), faces W,S,B,E,N,T
+// Solver arrays of the fine level use the ghosted layout with a zero ghost
+// layer; coarse levels use the same padded layout for their own sizes.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define SCF_HD __host__ __device__ __forceinline__
+
+struct Dims {
+    int I, J, K;
+    int gx, gy, gz;     // I+2, J+2, K+2
+    int ng;             // ghosted cell count
+    int n;              // interior cell count
+};
+
+SCF_HD int gidx(const Dims &d, int i, int j, int k) { return i + d.gx * (j + d.gy * k); }
+SCF_HD int nidx(const Dims &d, int i, int j, int k) { return (i - 1) + d.I * ((j - 1) + d.J * (k - 1)); }
+
+// Device error flags (bitwise OR into ctx->flags[0]).
+enum ScfFlag : unsigned {
+    FLAG_BAD_POSNU = 1u,          // PosNu == -1 differs from Cell_Type == 2, or out of range
+    FLAG_STALE_OVERFLOW = 2u,     // stale-coefficient list full
+    FLAG_STALE_LIMIT = 4u,        // stale search hit its step limit
+    FLAG_NONFINITE = 8u,          // NaN/Inf in the assembled system
+    FLAG_BAD_DIAG = 16u,          // active row with diagonal <= 0
+    FLAG_NEITHER_ACTIVE = 32u,    // active cell that is neither wet nor dry
+};
+
+// Scalars kept on the device during CG (no host round trip for alpha/beta).
+enum ScfScalar {
+    S_RZ = 0,      // (r, z) of the current iteration
+    S_PQ,          // (p, A p)
+    S_ALPHA,
+    S_BETA,
+    S_RR,          // (r, r)
+    S_BB,          // (b, b)
+    S_SUM,         // scratch sum (mean projection)
+    S_COUNT,       // active cell count
+    S_MEAN,
+    S_RZ_NEW,
+    S_NUM
+};
+
+// One multigrid level as the kernels see it (padded layout).
+template <typename T>
+struct LevelView {
+    int n0, n1, n2;       // interior sizes
+    int sy, sz;           // strides (n0+2, (n0+2)*(n1+2))
+    const T *diag, *dinv, *cE, *cN, *cT;
+};
+
+template <typename T>
+__device__ __forceinline__ T apply_row(const LevelView<T> &L, const T *__restrict__ x, int c)
+{
+    return L.diag[c] * x[c] -
+           (L.cE[c] * x[c + 1] + L.cE[c - 1] * x[c - 1] + L.cN[c] * x[c + L.sy] + L.cN[c - L.sy] * x[c - L.sy] +
+            L.cT[c] * x[c + L.sz] + L.cT[c - L.sz] * x[c - L.sz]);
+}
+
+// Launch helpers -----------------------------------------------------------
+struct Launch3 {
+    dim3 grid, block;
+};
+
+inline Launch3 launch_interior(int n0, int n1, int n2)
+{
+    Launch3 l;
+    l.block = dim3(32, 4, 2);
+    l.grid = dim3((n0 + 31) / 32, (n1 + 3) / 4, (n2 + 1) / 2);
+    return l;
+}
+
+inline unsigned nblocks(const Launch3 &l) { return l.grid.x * l.grid.y * l.grid.z; }
+
+// Block-wide FP64 sum; result valid in thread 0.  blockDim.x*y*z <= 1024.
+__device__ __forceinline__ double block_sum(double v)
+{
+    __shared__ double warp_part[32];
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int nthreads = blockDim.x * blockDim.y * blockDim.z;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = tid & 31, w = tid >> 5;
+    if (lane == 0) warp_part[w] = v;
+    __syncthreads();
+    const int nw = (nthreads + 31) >> 5;
+    v = (tid < nw) ? warp_part[tid] : 0.0;
+    if (w == 0)
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ int block_linear() { return blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z); }
+__device__ __forceinline__ int thread_linear() { return threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z); }

@@ -1,0 +1,125 @@
+// scf_kernels.h -- argument blocks and launchers shared by the .cu files.
+#pragma once
+#include "scf_common.cuh"
+
+// Inputs of the assembly (device mirrors of scf_poisson_in) plus scratch.
+struct AsmArgs {
+    Dims d;
+    const double *pdx, *pdy, *pdz, *udx, *vdy, *wdz;      // interior
+    const double *phil, *vofl, *vof, *ee, *ne, *te;       // ghosted
+    const double *vofo, *us, *vs, *ws, *dpu, *dpv, *dpw;  // ghosted
+    const int *ct, *pos;                                  // interior
+    int ext_cell;
+    int flag[6];
+    const double *bvar[6];
+    double dt, betap, betam, epsi, tol, stale_init;
+    double *pocoef;                                       // (I,J,K,6)
+    // stale-coefficient bookkeeping
+    unsigned *stale_count;
+    unsigned stale_cap;
+    long long *stale_list;
+    double *col_val;        // [I*J][12]
+    unsigned short *col_mask;
+    double *grp_val;        // [groups][12]
+    unsigned short *grp_mask;
+    unsigned *flags;
+};
+
+// Level-0 operator outputs (ghosted layout).
+struct OpArgs {
+    double *diag, *dinv, *cE, *cN, *cT, *extra, *b;
+    unsigned char *active;
+    float *diag32, *dinv32, *cE32, *cN32, *cT32, *extra32;  // mixed only
+};
+
+int launch_assemble(const AsmArgs &a, const OpArgs &o, bool mixed, cudaStream_t st, unsigned *stale_count_host,
+                    int *launches);
+
+// ---- solver --------------------------------------------------------------
+template <typename T>
+struct MgLevel {
+    int n0, n1, n2, sy, sz, tot;
+    int f0, f1, f2;                 // coarsening factors towards the next level
+    T *diag, *dinv, *cE, *cN, *cT, *extra;
+    unsigned char *active;
+    T *x, *xb, *d, *b;              // x/xb ping-pong, Chebyshev update, rhs
+    LevelView<T> view() const
+    {
+        LevelView<T> v;
+        v.n0 = n0; v.n1 = n1; v.n2 = n2; v.sy = sy; v.sz = sz;
+        v.diag = diag; v.dinv = dinv; v.cE = cE; v.cN = cN; v.cT = cT;
+        return v;
+    }
+};
+
+struct ChebCoef {
+    int degree;
+    double first;        // 1/theta
+    double c1[8], c2[8]; // steps 1..degree-1
+};
+
+struct Reducer {
+    double *partials;    // >= max blocks of any reducing launch
+    double *scal;        // ScfScalar slots
+    int max_blocks;
+};
+
+// Coarsening and the coarsest dense inverse.
+template <typename T>
+void mg_coarsen(const MgLevel<T> &F, MgLevel<T> &C, cudaStream_t st, int *launches);
+template <typename T>
+void mg_coarse_inverse(const MgLevel<T> &L, double *ainv, int *map, int n, bool singular, cudaStream_t st,
+                       int *launches);
+// One V-cycle: level 0 rhs in L[0].b, result in *z (== L[0].x or L[0].xb).
+template <typename T>
+T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, const int *map, int ncoarse,
+             bool singular, cudaStream_t st, int *launches);
+
+// CG building blocks on the fine level (FP64 vectors, ghosted layout).
+void cg_spmv_dot(const LevelView<double> &A, const double *p, double *q, Reducer &R, int slot_out,
+                 cudaStream_t st, int *launches);
+void cg_finish_alpha(Reducer &R, int nblocks, cudaStream_t st, int *launches);
+template <typename T>
+void cg_update(const LevelView<double> &A, double *x, double *r, const double *p, const double *q, T *rlow,
+               Reducer &R, cudaStream_t st, int *launches);
+template <typename T>
+void cg_dot_rz(const LevelView<double> &A, const double *r, const T *z, Reducer &R, cudaStream_t st,
+               int *launches);
+template <typename T>
+void cg_pupdate(const LevelView<double> &A, const T *z, double *p, const double *scal, bool first,
+                cudaStream_t st, int *launches);
+void reduce_to(Reducer &R, int nblocks, int slot, cudaStream_t st, int *launches);
+// r = b - A x (active), partial (r,r)
+void cg_residual(const LevelView<double> &A, const double *b, const double *x, double *r, Reducer &R,
+                 cudaStream_t st, int *launches);
+// sum and count over active cells (mean projection)
+void active_sum(const LevelView<double> &A, const unsigned char *active, const double *v, Reducer &R,
+                cudaStream_t st, int *launches);
+void subtract_mean(const LevelView<double> &A, const unsigned char *active, double *v, const double *scal,
+                   cudaStream_t st, int *launches);
+void dot_self(const LevelView<double> &A, const double *v, Reducer &R, int slot, cudaStream_t st, int *launches);
+void copy_to_low(const LevelView<double> &A, const double *src, float *dst, cudaStream_t st, int *launches);
+
+// ---- correction ------------------------------------------------------------
+struct CorrArgs {
+    Dims d;
+    const double *x;                 // solution, ghosted (0 on solid/ghost)
+    const int *ct;
+    double *pp;                      // Proj%Pp, ghosted
+    const double *pocoef;
+    const double *us, *vs, *ws;      // u*
+    const int *umoex, *uct, *vmoex, *vct, *wmoex, *wct;
+    double *u, *v, *w, *p;           // TVar, ghosted
+    const double *pdx, *pdy, *pdz;
+    const double *ee, *ne, *te;
+    int bcp_flag[6];
+    int flag[4][6];
+    double cst[4][6];
+    double *bcvar[4][6];             // device planes (always written)
+    double *tmp[4];                  // plane scratch for the top face
+    int north_fix;
+    unsigned *flags;
+};
+
+void launch_scatter(const CorrArgs &c, cudaStream_t st, int *launches);
+void launch_correct(const CorrArgs &c, cudaStream_t st, int *launches);

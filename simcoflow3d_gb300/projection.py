@@ -1,0 +1,194 @@
+"""Python mirror of SIMCOFlow's projection interface over the C ABI.
+
+``Projection.poisson_solve`` stands in for ``PoissonEquationSolver``
+(``src/ProjectionP.f90:33-121``) and ``Projection.update_puvw`` for the
+projection part of ``UpdatePUVW`` (``src/ComputePUVW.f90:127-129,179-384``).
+Arguments are the reference's arrays (Fortran-ordered numpy arrays, ghosted
+where the reference ghosts them), bundled in a ``workloads.Workload``.
+
+There is no CPU fallback: if ``libscf_projection.so`` is missing or no GPU is
+visible, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+from . import capi
+
+_lib = None
+
+
+class ScfError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{capi_status(status)} ({status}): {message}")
+        self.status = status
+
+
+def load_library(path: Optional[str] = None):
+    """Loads the CUDA library (never a substitute)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or capi.LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with __graft_entry__.build() "
+                           "(there is no CPU fallback)")
+    L = C.CDLL(path)
+    P = C.POINTER
+    L.scf_opts_default.argtypes = [P(capi.ScfOpts)]
+    L.scf_opts_default.restype = None
+    L.scf_ctx_create.argtypes = [P(C.c_void_p), C.c_int32, C.c_int32, C.c_int32, P(capi.ScfOpts)]
+    L.scf_ctx_destroy.argtypes = [C.c_void_p]
+    L.scf_ctx_set_opts.argtypes = [C.c_void_p, P(capi.ScfOpts)]
+    L.scf_poisson_solve.argtypes = [C.c_void_p, P(capi.ScfPoissonIn), capi.c_double_p, capi.c_double_p,
+                                    P(capi.ScfStats)]
+    L.scf_update_puvw.argtypes = [C.c_void_p, P(capi.ScfPoissonIn), P(capi.ScfCorrectIn), capi.c_double_p,
+                                  capi.c_double_p, capi.c_double_p, capi.c_double_p, P(capi.ScfBcOut),
+                                  P(capi.ScfStats)]
+    L.scf_stage_inputs.argtypes = [C.c_void_p, P(capi.ScfPoissonIn), P(capi.ScfCorrectIn), capi.c_double_p,
+                                   capi.c_double_p, capi.c_double_p, capi.c_double_p]
+    L.scf_run_projection.argtypes = [C.c_void_p, P(capi.ScfStats)]
+    L.scf_fetch_outputs.argtypes = [C.c_void_p, capi.c_double_p, capi.c_double_p, capi.c_double_p,
+                                    capi.c_double_p, capi.c_double_p, capi.c_double_p, P(capi.ScfBcOut)]
+    L.scf_debug_apply.argtypes = [C.c_void_p, capi.c_double_p, capi.c_double_p]
+    L.scf_debug_operator.argtypes = [C.c_void_p] + [capi.c_double_p] * 5
+    L.scf_status_string.argtypes = [C.c_int]
+    L.scf_status_string.restype = C.c_char_p
+    L.scf_last_error.argtypes = [C.c_void_p, C.c_char_p, C.c_size_t]
+    L.scf_host_register.argtypes = [C.c_void_p, C.c_size_t]
+    L.scf_host_unregister.argtypes = [C.c_void_p]
+    L.scf_abi_version.argtypes = []
+    _lib = L
+    return L
+
+
+def capi_status(s: int) -> str:
+    try:
+        return load_library().scf_status_string(int(s)).decode()
+    except Exception:
+        return f"status {s}"
+
+
+def default_opts(**kw) -> capi.ScfOpts:
+    o = capi.ScfOpts()
+    load_library().scf_opts_default(C.byref(o))
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise KeyError(k)
+        setattr(o, k, v)
+    return o
+
+
+class Projection:
+    """One device context for an I x J x K grid."""
+
+    def __init__(self, imax: int, jmax: int, kmax: int, **opts):
+        self.L = load_library()
+        self.shape = (imax, jmax, kmax)
+        self.opts = default_opts(**opts)
+        self.ctx = C.c_void_p()
+        rc = self.L.scf_ctx_create(C.byref(self.ctx), imax, jmax, kmax, C.byref(self.opts))
+        if rc != 0:
+            raise ScfError(rc, "scf_ctx_create failed")
+
+    @classmethod
+    def for_workload(cls, w, **opts):
+        opts.setdefault("rho_l", w.rho_l)
+        opts.setdefault("rho_g", w.rho_g)
+        return cls(w.imax, w.jmax, w.kmax, **opts)
+
+    # -- helpers ---------------------------------------------------------------
+    def last_error(self) -> str:
+        buf = C.create_string_buffer(512)
+        self.L.scf_last_error(self.ctx, buf, 512)
+        return buf.value.decode(errors="replace")
+
+    def _check(self, rc: int, allow=()):
+        if rc != 0 and rc not in allow:
+            raise ScfError(rc, self.last_error())
+        return rc
+
+    def set_opts(self, **kw):
+        for k, v in kw.items():
+            setattr(self.opts, k, v)
+        self._check(self.L.scf_ctx_set_opts(self.ctx, C.byref(self.opts)))
+
+    def close(self):
+        if self.ctx:
+            self.L.scf_ctx_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- the reference's entry points ------------------------------------------
+    def poisson_solve(self, w, want_pocoef: bool = True, allow_not_converged: bool = False):
+        """PoissonEquationSolver: returns (PoCoef (I,J,K,6) or None, Pp ghosted, stats)."""
+        I, J, K = self.shape
+        pin = capi.poisson_in(w)
+        pc = np.zeros((I, J, K, 6), order="F") if want_pocoef else None
+        pp = np.zeros(w.shape_g, order="F")
+        st = capi.ScfStats()
+        rc = self.L.scf_poisson_solve(self.ctx, C.byref(pin), capi.dptr(pc), capi.dptr(pp), C.byref(st))
+        self._check(rc, (capi.SCF_ERR_NOT_CONVERGED,) if allow_not_converged else ())
+        return pc, pp, st.as_dict()
+
+    def update_puvw(self, w, tvar=None, want_bc: bool = True, allow_not_converged: bool = False):
+        """UpdatePUVW's projection: returns (u, v, w, p, bcvar[4][6] or None, stats).
+        ``tvar`` defaults to copies of the workload's TVar arrays."""
+        a = w.arrays
+        if tvar is None:
+            tvar = [a[k].copy(order="F") for k in ("tvar_u", "tvar_v", "tvar_w", "tvar_p")]
+        u, v, ww, p = tvar
+        pin = capi.poisson_in(w)
+        cin = capi.correct_in(w)
+        bc_struct, bc = (capi.new_bc_out(*self.shape) if want_bc else (None, None))
+        st = capi.ScfStats()
+        rc = self.L.scf_update_puvw(self.ctx, C.byref(pin), C.byref(cin), capi.dptr(u), capi.dptr(v),
+                                    capi.dptr(ww), capi.dptr(p), C.byref(bc_struct) if want_bc else None,
+                                    C.byref(st))
+        self._check(rc, (capi.SCF_ERR_NOT_CONVERGED,) if allow_not_converged else ())
+        return u, v, ww, p, bc, st.as_dict()
+
+    # -- split API ---------------------------------------------------------------
+    def stage(self, w, tvar=None, correction: bool = True):
+        a = w.arrays
+        self._pin = capi.poisson_in(w)
+        if correction:
+            if tvar is None:
+                tvar = [a[k] for k in ("tvar_u", "tvar_v", "tvar_w", "tvar_p")]
+            self._cin = capi.correct_in(w)
+            rc = self.L.scf_stage_inputs(self.ctx, C.byref(self._pin), C.byref(self._cin),
+                                         *(capi.dptr(t) for t in tvar))
+        else:
+            rc = self.L.scf_stage_inputs(self.ctx, C.byref(self._pin), None, None, None, None, None)
+        self._check(rc)
+
+    def run(self, allow_not_converged: bool = False):
+        st = capi.ScfStats()
+        self._check(self.L.scf_run_projection(self.ctx, C.byref(st)),
+                    (capi.SCF_ERR_NOT_CONVERGED,) if allow_not_converged else ())
+        return st.as_dict()
+
+    def fetch(self, u=None, v=None, w=None, p=None, pocoef=None, pp=None, bc=None):
+        self._check(self.L.scf_fetch_outputs(self.ctx, capi.dptr(u), capi.dptr(v), capi.dptr(w), capi.dptr(p),
+                                             capi.dptr(pocoef), capi.dptr(pp), C.byref(bc) if bc else None))
+
+    # -- diagnostics ---------------------------------------------------------------
+    def debug_apply(self, x: np.ndarray) -> np.ndarray:
+        y = np.zeros(x.shape, order="F")
+        self._check(self.L.scf_debug_apply(self.ctx, capi.dptr(np.asfortranarray(x)), capi.dptr(y)))
+        return y
+
+    def debug_operator(self):
+        I, J, K = self.shape
+        outs = [np.zeros((I, J, K), order="F") for _ in range(5)]
+        self._check(self.L.scf_debug_operator(self.ctx, *(capi.dptr(o) for o in outs)))
+        return dict(zip(("diag", "cpl_e", "cpl_n", "cpl_t", "rhs"), outs))
