@@ -1,0 +1,369 @@
+#!/usr/bin/env python
+"""Benchmark: ms per pressure projection at 256^3 (the c2 workload).
+
+One step = one pressure projection of SIMCOFlow's projection step on the 256^3
+cut-cell sphere + gas-bubble column (density ratio 1000): GFM coefficients,
+operator and right-hand side, the multigrid-preconditioned CG solve to
+relative residual 1e-8, the pressure scatter, the velocity correction and the
+boundary conditions.  ``value`` is the device time per projection of the
+mixed solver (FP32 V-cycle, FP64 CG/residual/dots/coarsest solve) with the
+inputs resident in HBM; the same projection with the FP64 V-cycle is timed
+beside it.  ``e2e`` is the drop-in call ``scf_update_puvw`` with the
+reference's host arrays in pinned memory (host->device copy of every input
+and device->host copy of u, v, w, p and the BC planes inside the timed
+region).
+
+``--impl reference`` times the CPU path (the oracle's restatement of the
+reference path, multigrid-preconditioned CG with OpenMP on all host cores).
+
+Multi-GPU: the path runs on one GPU per projection (the reference builds the
+whole system on every rank), so ``--gpus N`` runs N independent replicas.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "ms/projection & HBM GB/s at 256^3: mixed vs FP64 GPU solve at rel res 1e-8"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def init_dist(ws):
+    if ws <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group("gloo")
+    return dist
+
+
+def allreduce_max(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(prefix="clocks_", suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            time.sleep(0.1)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if not self.path or not os.path.exists(self.path):
+            return out
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), f[5], f[6], f[7], f[8]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return out
+        out["samples"] = len(rows)
+        out["sm_mhz"] = statistics.median(r[0] for r in rows)
+        out["sm_max_mhz"] = max(r[1] for r in rows)
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = set()
+        for r in rows:
+            for name, val in zip(names, r[2:]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        out["reasons"] = sorted(reasons)
+        return out
+
+
+def measured_peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            d = json.load(open(p))
+            for k in ("hbm_gbs", "hbm_GBs", "copy_gbs"):
+                if k in d:
+                    return float(d[k]), "measured"
+        except Exception:
+            pass
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def committed_traffic():
+    """DRAM bytes per launch of the smoother from the committed ncu summary."""
+    p = os.path.join(HERE, "profiles", "roofline_traffic.json")
+    if os.path.exists(p):
+        try:
+            return json.load(open(p))
+        except Exception:
+            return None
+    return None
+
+
+def make_workload(name: str, seed: int, n=None):
+    from simcoflow3d_gb300 import workloads as W
+    return W.config(name, seed=seed, n=n)
+
+
+def pin_arrays(lib, w):
+    """Pins the workload's host arrays in place (cudaHostRegister)."""
+    pinned = []
+    for a in w.arrays.values():
+        if a.nbytes and lib.scf_host_register(a.ctypes.data, a.nbytes) == 0:
+            pinned.append(a)
+    return pinned
+
+
+def unpin(lib, arrs):
+    for a in arrs:
+        lib.scf_host_unregister(a.ctypes.data)
+
+
+def time_device(proj, steps, warmup):
+    """W untimed + K timed device-resident projections; returns (list of ms, stats)."""
+    for _ in range(warmup):
+        proj.run()
+    ms, launches, last = [], 0, None
+    for _ in range(steps):
+        st = proj.run()
+        ms.append(st["ms_total"])
+        launches += st["gpu_launches"]
+        last = st
+    return ms, launches, last
+
+
+def cpu_projection_ms(w, threads: int):
+    """One projection on the host cores with the oracle's restatement."""
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    pc = O.pocoef(w)
+    b = O.rhs(w, pc)
+    x, st = O.gmg_solve(w, pc, b, precision=0, rel_tol=1e-8, degree=3)
+    pp = O.scatter(w, x)
+    O.correct(w, pc, pp)
+    return (time.perf_counter() - t0) * 1e3, st
+
+
+def run_reference(args):
+    ws, rank, local = dist_env()
+    dist = init_dist(ws)
+    if rank != 0:
+        barrier(dist)
+        return 0
+    threads = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    w = make_workload(args.config, args.seed, args.n)
+    ms = []
+    for i in range(args.warmup + args.steps):
+        t, st = cpu_projection_ms(w, threads)
+        if i >= args.warmup:
+            ms.append(t)
+        if args.max_cpu_s and sum(ms) / 1e3 > args.max_cpu_s and len(ms) >= 1:
+            break
+    v = statistics.mean(ms)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": "ms/projection",
+        "n_gpus": ws, "steps": len(ms), "warmup": args.warmup, "ms_per_step": round(v, 3),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded u*, cut-cell sphere + gas bubble)",
+        "config": {"workload": f"{args.config}: 256^3 cut-cell sphere r=0.15 + gas bubble r=0.1, rho ratio 1000, "
+                               "all-Neumann p, rel res 1e-8", "grid": [w.imax, w.jmax, w.kmax]},
+        "cpu_baseline": {"value": round(v, 3), "unit": "ms/projection", "cores": threads, "kind": "port",
+                         "sample": "full projection per step (oracle restatement: coefficients, rhs, "
+                                   "FP64 MG-PCG to 1e-8, scatter, correction)"},
+        "e2e": {"value": round(v, 3), "unit": "ms/projection", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "iterations": st.get("iterations"),
+    }
+    print(json.dumps(line), flush=True)
+    barrier(dist)
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    ws, rank, local = dist_env()
+    dist = init_dist(ws)
+    from simcoflow3d_gb300 import capi
+    from simcoflow3d_gb300.projection import Projection, load_library
+    lib = load_library()
+    w = make_workload(args.config, args.seed + rank, args.n)
+    pinned = pin_arrays(lib, w)
+
+    # device-resident timing: mixed (value) and FP64 (comparison)
+    results = {}
+    for name, prec in (("mixed", capi.SCF_PREC_MIXED), ("fp64", capi.SCF_PREC_FP64)):
+        proj = Projection.for_workload(w, precision=prec, rel_tol=args.tol, device=local)
+        proj.stage(w)
+        barrier(dist)
+        if name == "mixed":
+            with ClockSampler(local) as cs:
+                ms, launches, st = time_device(proj, args.steps, args.warmup)
+            clocks = cs.summary()
+        else:
+            ms, launches, st = time_device(proj, args.steps, args.warmup)
+        total = allreduce_max(dist, sum(ms))
+        results[name] = {"ms": ms, "total": total, "launches": launches, "stats": st, "proj": proj}
+
+    # dominant-kernel roofline on the mixed context (fine-level smoother)
+    mixed = results["mixed"]["proj"]
+    k_ms, k_bytes = mixed.time_kernel(capi.SCF_K_SMOOTH, reps=50)
+    s_ms, s_bytes = mixed.time_kernel(capi.SCF_K_SPMV, reps=50)
+    peak, peak_kind = measured_peaks()
+    achieved = k_bytes / (k_ms * 1e-3) / 1e9
+    traffic = committed_traffic()
+    trf = traffic.get("smooth_fp32_bytes_per_launch") if traffic else None
+
+    # end to end through the drop-in call, host arrays pinned
+    a = w.arrays
+    tv = [a[k].copy(order="F") for k in ("tvar_u", "tvar_v", "tvar_w", "tvar_p")]
+    pinned += [x for x in tv if lib.scf_host_register(x.ctypes.data, x.nbytes) == 0]
+    e2e_ms = []
+    e2e_stats = None
+    for i in range(args.warmup + args.steps):
+        for t, k in zip(tv, ("tvar_u", "tvar_v", "tvar_w", "tvar_p")):
+            t[...] = a[k]
+        barrier(dist) if i == args.warmup else None
+        t0 = time.perf_counter()
+        u, v, ww, p, bc, st = mixed.update_puvw(w, tvar=tv, want_bc=True)
+        dt = (time.perf_counter() - t0) * 1e3
+        if i >= args.warmup:
+            e2e_ms.append(dt)
+            e2e_stats = st
+    e2e_total = allreduce_max(dist, sum(e2e_ms))
+    bc_bytes = sum(x.nbytes for row in bc for x in row) if bc else 0
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        cpu_ms, cpu_st = cpu_projection_ms(w, threads)
+        cpu = {"value": round(cpu_ms, 3), "unit": "ms/projection", "cores": threads, "kind": "port",
+               "sample": "one full 256^3 projection (oracle restatement: coefficients, rhs, FP64 MG-PCG to "
+                         f"1e-8 in {cpu_st['iterations']} iterations, scatter, correction), OpenMP"}
+
+    unpin(lib, pinned)
+    if rank != 0:
+        barrier(dist)
+        return 0
+    nproj = ws * args.steps
+    value = results["mixed"]["total"] / nproj
+    fp64 = results["fp64"]["total"] / nproj
+    smx, s64 = results["mixed"]["stats"], results["fp64"]["stats"]
+    line = {
+        "metric": METRIC,
+        "value": round(value, 4),
+        "unit": "ms/projection",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(value, 4),
+        "higher_is_better": False,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 V-cycle / f64 CG",
+        "data": "synthetic (seeded u*, cut-cell sphere + gas bubble)",
+        "config": {
+            "workload": f"{args.config}: 256^3 cut-cell sphere r=0.15 at (0.5,0.5,0.3) + gas bubble r=0.1 at "
+                        "(0.5,0.5,0.65) in a water column, rho ratio 1000, all-Neumann p, rel res 1e-8",
+            "grid": [w.imax, w.jmax, w.kmax],
+            "rel_tol": args.tol,
+            "l2": "inputs larger than L2 (about 3.5 GB resident per projection)",
+            "parallelism": f"replicas x{ws}",
+        },
+        "fp64": {"ms_per_projection": round(fp64, 4), "iterations": s64["iterations"],
+                 "rel_residual": s64["rel_residual"]},
+        "mixed": {"iterations": smx["iterations"], "rel_residual": smx["rel_residual"],
+                  "ms_assemble": round(smx["ms_assemble"], 3), "ms_solve": round(smx["ms_solve"], 3),
+                  "ms_correct": round(smx["ms_correct"], 3)},
+        "speedup_mixed_vs_fp64": round(fp64 / value, 3),
+        "e2e": {"value": round(e2e_total / nproj, 4), "unit": "ms/projection",
+                "h2d_bytes_per_step": int(e2e_stats["bytes_h2d"]),
+                "d2h_bytes_per_step": int(e2e_stats["bytes_d2h"])},
+        "roofline": {"bound": "hbm", "kernel": "k_cheb_step<float> (fine-level Chebyshev step)",
+                     "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                     "bytes_per_launch": k_bytes, "ms_per_launch": round(k_ms, 5), "traffic": trf},
+        "fp64_spmv": {"GB/s": round(s_bytes / (s_ms * 1e-3) / 1e9, 1), "ms_per_launch": round(s_ms, 5)},
+        "clocks": clocks,
+        "gpu_launches": results["mixed"]["launches"],
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    barrier(dist)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c2")
+    ap.add_argument("--tol", type=float, default=1e-8)
+    ap.add_argument("--seed", type=int, default=20261203)
+    ap.add_argument("--n", type=int, default=None, help="smaller grid (profiling captures only)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--max-cpu-s", type=float, default=150.0, help="stop the reference arm after this many s")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -76,7 +76,8 @@ typedef struct scf_opts {
     int32_t coarse_max_cells; /* coarsen until a level has <= this many cells
                                  (default 64); solved densely in FP64          */
     double  rho_l, rho_g;     /* liquid/gas densities (StateVariables.f90:9)   */
-    double  rho_ref;          /* reference density Roref (ProjectionP.f90:53)  */
+    double  rho_ref;          /* reference density Roref (ProjectionP.f90:53);
+                                 <= 0 means rho_l, as the reference passes row */
     double  epsi;             /* cut-cell threshold (CutCell.f90:11), 1e-3      */
     double  gfm_tol;          /* GFM lambda guard (ProjectionP.f90:18), 1e-30  */
     double  stale_init;       /* value of the reference's uninitialised BetaW/
@@ -175,7 +176,8 @@ int scf_ctx_set_opts(scf_ctx *ctx, const scf_opts *opts);
  *   pocoef : (I,J,K,6) FP64 output, PoCoef; may be NULL.
  *   pp     : ghosted FP64 output, Proj%Pp after DeltaPressureGetValues and
  *            DeltaPressureBoundaryCondition; may be NULL.  Ghost edges and
- *            corners, which the reference never writes, are left unchanged.
+ *            corners, which the reference never writes, are 0 (UpdatePUVW
+ *            zeroes Proj%Pp before the call, ComputePUVW.f90:102).
  * For an all-Neumann system the zero-mean (over active cells) solution is
  * returned; the reference's constant is HYPRE's.                            */
 int scf_poisson_solve(scf_ctx *ctx, const scf_poisson_in *in,
@@ -211,6 +213,20 @@ int scf_debug_apply(scf_ctx *ctx, const double *x, double *y);
  * the right-hand side b (interior, 0 on solid cells).  Any may be NULL.     */
 int scf_debug_operator(scf_ctx *ctx, double *diag, double *cpl_e,
                        double *cpl_n, double *cpl_t, double *rhs);
+
+/* Times `reps` back-to-back launches of one kernel class of the last run's
+ * state with CUDA events on the context's stream and reports the mean device
+ * time per launch and the algorithmic bytes one launch moves (each array
+ * touched once per cell).  kernel: SCF_K_SMOOTH (fine-level Chebyshev step
+ * of the V-cycle, in its precision), SCF_K_SPMV (FP64 CG operator apply with
+ * its dot product), SCF_K_RESTRICT (fine residual + restriction),
+ * SCF_K_PROLONG (prolongation + first post-smoothing step), SCF_K_CGUPDATE
+ * (FP64 x/r update with its dot product).  Needs a previous run.          */
+enum scf_kernel_class {
+    SCF_K_SMOOTH = 0, SCF_K_SPMV = 1, SCF_K_RESTRICT = 2, SCF_K_PROLONG = 3, SCF_K_CGUPDATE = 4
+};
+int scf_debug_time_kernel(scf_ctx *ctx, int kernel, int reps, double *ms_per_launch,
+                          double *bytes_per_launch);
 
 /* ---- misc -------------------------------------------------------------- */
 const char *scf_status_string(int status);

@@ -29,6 +29,12 @@ SCF_ERR_UNDEFINED_IN_REFERENCE = 7
 SCF_ERR_NO_DEVICE = 8
 SCF_ERR_NO_SOLVE = 9
 
+SCF_K_SMOOTH = 0
+SCF_K_SPMV = 1
+SCF_K_RESTRICT = 2
+SCF_K_PROLONG = 3
+SCF_K_CGUPDATE = 4
+
 SCF_PREC_FP64 = 0
 SCF_PREC_MIXED = 1
 

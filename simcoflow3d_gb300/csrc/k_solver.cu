@@ -533,6 +533,44 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
     return cur[0];
 }
 
+// ---------------------------------------------------------------------------
+// single launches for timing (scf_debug_time_kernel)
+template <typename T>
+void probe_smooth(MgLevel<T> &F, const ChebCoef &cc, cudaStream_t st)
+{
+    Launch3 lf = launch_interior(F.n0, F.n1, F.n2);
+    const int s = cc.degree > 1 ? 1 : 0;
+    k_cheb_step<T><<<lf.grid, lf.block, 0, st>>>(F.view(), F.b, F.x, F.d, F.xb, F.d, (T)cc.c1[s], (T)cc.c2[s]);
+}
+
+template <typename T>
+void probe_restrict(MgLevel<T> &F, MgLevel<T> &C, cudaStream_t st)
+{
+    Launch3 lc = launch_interior(C.n0, C.n1, C.n2);
+    k_restrict<T><<<lc.grid, lc.block, 0, st>>>(F.view(), F.b, F.x, C.view(), C.b, F.f0, F.f1, F.f2);
+}
+
+template <typename T>
+void probe_prolong(MgLevel<T> &F, MgLevel<T> &C, const ChebCoef &cc, cudaStream_t st)
+{
+    Launch3 lf = launch_interior(F.n0, F.n1, F.n2);
+    k_post_first<T><<<lf.grid, lf.block, 0, st>>>(F.view(), F.b, F.x, C.view(), C.x, F.xb, F.d, F.f0, F.f1, F.f2,
+                                                   (T)cc.first);
+}
+
+void probe_spmv(const LevelView<double> &A, const double *p, double *q, Reducer &R, cudaStream_t st)
+{
+    Launch3 l = launch_interior(A.n0, A.n1, A.n2);
+    k_spmv_dot<<<l.grid, l.block, 0, st>>>(A, p, q, R.partials);
+}
+
+template void probe_smooth<float>(MgLevel<float> &, const ChebCoef &, cudaStream_t);
+template void probe_smooth<double>(MgLevel<double> &, const ChebCoef &, cudaStream_t);
+template void probe_restrict<float>(MgLevel<float> &, MgLevel<float> &, cudaStream_t);
+template void probe_restrict<double>(MgLevel<double> &, MgLevel<double> &, cudaStream_t);
+template void probe_prolong<float>(MgLevel<float> &, MgLevel<float> &, const ChebCoef &, cudaStream_t);
+template void probe_prolong<double>(MgLevel<double> &, MgLevel<double> &, const ChebCoef &, cudaStream_t);
+
 // explicit instantiations
 template void mg_coarsen<float>(const MgLevel<float> &, MgLevel<float> &, cudaStream_t, int *);
 template void mg_coarsen<double>(const MgLevel<double> &, MgLevel<double> &, cudaStream_t, int *);

@@ -846,6 +846,61 @@ int scf_debug_operator(scf_ctx *ctx, double *diag, double *cpl_e, double *cpl_n,
     return SCF_OK;
 }
 
+int scf_debug_time_kernel(scf_ctx *ctx, int kernel, int reps, double *ms_per_launch, double *bytes_per_launch)
+{
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!ms_per_launch || !bytes_per_launch || reps < 1) return SCF_ERR_BAD_ARG;
+    if (!ctx->solved) { set_err(ctx, "no projection has run"); return SCF_ERR_NO_SOLVE; }
+    if (ctx->nlev < 2 && (kernel == SCF_K_RESTRICT || kernel == SCF_K_PROLONG)) return SCF_ERR_BAD_ARG;
+    const bool mixed = ctx->opts.precision == SCF_PREC_MIXED;
+    const double s = mixed ? 4.0 : 8.0;
+    const double n = (double)ctx->d.n;
+    const ChebCoef cc = cheb_coef(ctx->opts.smoother_degree);
+    auto launch = [&]() {
+        switch (kernel) {
+        case SCF_K_SMOOTH:
+            if (mixed) probe_smooth<float>(ctx->L32[0], cc, ctx->st); else probe_smooth<double>(ctx->L64[0], cc, ctx->st);
+            break;
+        case SCF_K_SPMV: probe_spmv(fine_view(ctx), ctx->p, ctx->q, ctx->R, ctx->st); break;
+        case SCF_K_RESTRICT:
+            if (mixed) probe_restrict<float>(ctx->L32[0], ctx->L32[1], ctx->st);
+            else probe_restrict<double>(ctx->L64[0], ctx->L64[1], ctx->st);
+            break;
+        case SCF_K_PROLONG:
+            if (mixed) probe_prolong<float>(ctx->L32[0], ctx->L32[1], cc, ctx->st);
+            else probe_prolong<double>(ctx->L64[0], ctx->L64[1], cc, ctx->st);
+            break;
+        default: {
+            int dummy = 0;
+            cg_update<float>(fine_view(ctx), ctx->x, ctx->r, ctx->p, ctx->q, mixed ? (float *)ctx->L32[0].b : nullptr,
+                             ctx->R, ctx->st, &dummy);
+        }
+        }
+    };
+    double bytes;
+    switch (kernel) {
+    case SCF_K_SMOOTH: bytes = 10.0 * s * n; break;                 // b,x,d,diag,dinv,cE,cN,cT in; x,d out
+    case SCF_K_SPMV: bytes = 6.0 * 8.0 * n; break;                  // p,diag,cE,cN,cT in; q out
+    case SCF_K_RESTRICT: bytes = 6.0 * s * n + s * n / 8.0; break;  // b,x,diag,cE,cN,cT in; coarse b out
+    case SCF_K_PROLONG: bytes = 9.0 * s * n + s * n / 8.0; break;   // b,x,diag,dinv,cE,cN,cT,e in; x,d out
+    case SCF_K_CGUPDATE: bytes = (6.0 * 8.0 + (mixed ? 4.0 : 0.0)) * n; break;
+    default: return SCF_ERR_BAD_ARG;
+    }
+    launch();  // warm
+    CK(cudaEventRecord(ctx->ev[4], ctx->st));
+    for (int r = 0; r < reps; ++r) launch();
+    CK(cudaEventRecord(ctx->ev[5], ctx->st));
+    CK(cudaEventSynchronize(ctx->ev[5]));
+    CK(cudaGetLastError());
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev[4], ctx->ev[5]);
+    *ms_per_launch = ms / reps;
+    *bytes_per_launch = bytes;
+    ctx->solved = false;  // scratch vectors were overwritten
+    return SCF_OK;
+}
+
 const char *scf_status_string(int s)
 {
     switch (s) {

@@ -75,6 +75,15 @@ template <typename T>
 T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, const int *map, int ncoarse,
              bool singular, cudaStream_t st, int *launches);
 
+// Single launches of the fine-level kernels, for timing.
+template <typename T>
+void probe_smooth(MgLevel<T> &F, const ChebCoef &cc, cudaStream_t st);
+template <typename T>
+void probe_restrict(MgLevel<T> &F, MgLevel<T> &C, cudaStream_t st);
+template <typename T>
+void probe_prolong(MgLevel<T> &F, MgLevel<T> &C, const ChebCoef &cc, cudaStream_t st);
+void probe_spmv(const LevelView<double> &A, const double *p, double *q, Reducer &R, cudaStream_t st);
+
 // CG building blocks on the fine level (FP64 vectors, ghosted layout).
 void cg_spmv_dot(const LevelView<double> &A, const double *p, double *q, Reducer &R, int slot_out,
                  cudaStream_t st, int *launches);

@@ -62,6 +62,7 @@ def load_library(path: Optional[str] = None):
     L.scf_host_register.argtypes = [C.c_void_p, C.c_size_t]
     L.scf_host_unregister.argtypes = [C.c_void_p]
     L.scf_abi_version.argtypes = []
+    L.scf_debug_time_kernel.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     _lib = L
     return L
 
@@ -186,6 +187,12 @@ class Projection:
         y = np.zeros(x.shape, order="F")
         self._check(self.L.scf_debug_apply(self.ctx, capi.dptr(np.asfortranarray(x)), capi.dptr(y)))
         return y
+
+    def time_kernel(self, kernel: int, reps: int = 20):
+        """(ms per launch, algorithmic bytes per launch) of one kernel class."""
+        ms, by = C.c_double(), C.c_double()
+        self._check(self.L.scf_debug_time_kernel(self.ctx, int(kernel), int(reps), C.byref(ms), C.byref(by)))
+        return ms.value, by.value
 
     def debug_operator(self):
         I, J, K = self.shape

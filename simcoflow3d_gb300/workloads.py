@@ -55,31 +55,42 @@ def volume_fraction_calc(dx, dy, dz, nxx, nyy, nzz, s):
 
     Restates ``Volume_Fraction_Calc`` (``Clsvof.f90:1475-1550``, the
     Griebel-Klitz formula) element-wise.  Returns the volume (not the fraction).
+    Boxes entirely on one side (s <= 0 or s >= sm) take the reference's early
+    returns; only cut boxes evaluate the polynomial branches.
     """
-    dx, dy, dz, nxx, nyy, nzz, s = np.broadcast_arrays(
-        *(np.asarray(a, dtype=np.float64) for a in (dx, dy, dz, nxx, nyy, nzz, s)))
-    nx1, ny1, nz1 = np.abs(nxx), np.abs(nyy), np.abs(nzz)
-    a, b, c = nx1 * dx, ny1 * dy, nz1 * dz
-    dx1 = np.maximum(np.maximum(a, b), c)
-    dz1 = np.minimum(np.minimum(a, b), c)
-    dy1 = (a + b + c) - dx1 - dz1
-    sm = dx1 + dy1 + dz1
-    sc = np.minimum(s, sm - s)
-    with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
-        f1 = sc ** 3 / (6.0 * dx1 * dy1 * dz1)
-        f2 = (sc ** 2 - dz1 * sc + dz1 ** 2 / 3.0) / (2.0 * dx1 * dy1)
-        f3 = (2.0 * sc - dy1 - dz1) / (2.0 * dx1)
-        f4 = (sc ** 3 - (sc - dz1) ** 3 - (sc - dy1) ** 3) / (6.0 * dx1 * dy1 * dz1)
-        f5 = (sc ** 3 - (sc - dz1) ** 3 - (sc - dy1) ** 3 - (sc - dx1) ** 3) / (6.0 * dx1 * dy1 * dz1)
-    fc = np.where(sc <= dz1, f1,
-         np.where(sc <= dy1, f2,
-         np.where(dx1 >= dy1 + dz1,
-                  np.where(sc >= dy1 + dz1, f3, f4),
-                  np.where(sc > dx1, f5, f4))))
+    dx, dy, dz, nxx, nyy, nzz, s = (np.ascontiguousarray(a) for a in np.broadcast_arrays(
+        *(np.asarray(a, dtype=np.float64) for a in (dx, dy, dz, nxx, nyy, nzz, s))))
+    shape = s.shape
+    a, b, c = np.abs(nxx) * dx, np.abs(nyy) * dy, np.abs(nzz) * dz
+    sm = (a + b + c)
     vbox = dx * dy * dz
-    vol = np.where(s <= 0.5 * sm, fc * vbox, (1.0 - fc) * vbox)
-    vol = np.where(s >= sm, vbox, vol)
-    vol = np.where(s <= 0.0, 0.0, vol)
+    vol = np.where(s >= sm, vbox, 0.0)
+    cut = (s > 0.0) & (s < sm)
+    idx = np.nonzero(cut.ravel())[0]
+    if idx.size:
+        g = lambda v: v.ravel()[idx]
+        a, b, c, S, VB = g(a), g(b), g(c), g(s), g(vbox)
+        dx1 = np.maximum(np.maximum(a, b), c)
+        dz1 = np.minimum(np.minimum(a, b), c)
+        dy1 = (a + b + c) - dx1 - dz1
+        smc = dx1 + dy1 + dz1
+        sc = np.minimum(S, smc - S)
+        with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+            f1 = sc ** 3 / (6.0 * dx1 * dy1 * dz1)
+            f2 = (sc ** 2 - dz1 * sc + dz1 ** 2 / 3.0) / (2.0 * dx1 * dy1)
+            f3 = (2.0 * sc - dy1 - dz1) / (2.0 * dx1)
+            f4 = (sc ** 3 - (sc - dz1) ** 3 - (sc - dy1) ** 3) / (6.0 * dx1 * dy1 * dz1)
+            f5 = (sc ** 3 - (sc - dz1) ** 3 - (sc - dy1) ** 3 - (sc - dx1) ** 3) / (6.0 * dx1 * dy1 * dz1)
+        fc = np.where(sc <= dz1, f1,
+             np.where(sc <= dy1, f2,
+             np.where(dx1 >= dy1 + dz1,
+                      np.where(sc >= dy1 + dz1, f3, f4),
+                      np.where(sc > dx1, f5, f4))))
+        vcut = np.where(S <= 0.5 * smc, fc * VB, (1.0 - fc) * VB)
+        vcut = np.where(S >= smc, VB, vcut)
+        flat = vol.ravel().copy()
+        flat[idx] = vcut
+        vol = flat.reshape(shape)
     return vol
 
 
