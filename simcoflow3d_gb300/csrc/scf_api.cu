@@ -46,7 +46,8 @@ struct scf_ctx {
     scf_correct_in corr;
     bool have_corr = false;
     bool staged = false;
-    bool solved = false;
+    bool solved = false;      // a projection has run (hierarchy and vectors exist)
+    bool warm_ok = false;     // x holds the last solution (warm start)
     bool assembled = false;
     // assembly scratch
     double *pocoef;
@@ -371,7 +372,7 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
         stats->converged = 1;
         return std::isfinite(bb) ? SCF_OK : SCF_ERR_NONFINITE;
     }
-    if (ctx->opts.warm_start && ctx->solved) {
+    if (ctx->opts.warm_start && ctx->warm_ok) {
         cg_residual(A, ctx->b, ctx->x, ctx->r, ctx->R, ctx->st, &ctx->launches);
         if (singular) {
             active_sum(A, ctx->active, ctx->r, ctx->R, ctx->st, &ctx->launches);
@@ -497,6 +498,7 @@ int run(scf_ctx *ctx, bool with_correction, scf_stats *stats)
     if (rc && rc != SCF_ERR_NOT_CONVERGED) return rc;
     const int solve_rc = rc;
     ctx->solved = true;
+    ctx->warm_ok = true;
     CorrArgs ca = corr_args(ctx);
     launch_scatter(ca, ctx->st, &ctx->launches);
     if (with_correction) launch_correct(ca, ctx->st, &ctx->launches);
@@ -821,7 +823,6 @@ int scf_debug_apply(scf_ctx *ctx, const double *xh, double *yh)
     cg_spmv_dot(fine_view(ctx), ctx->p, ctx->q, ctx->R, S_PQ, ctx->st, &ctx->launches);
     CK(cudaMemcpyAsync(yh, ctx->q, sizeof(double) * d.ng, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
-    ctx->solved = false;  // p/q were overwritten
     return SCF_OK;
 }
 
@@ -897,7 +898,7 @@ int scf_debug_time_kernel(scf_ctx *ctx, int kernel, int reps, double *ms_per_lau
     cudaEventElapsedTime(&ms, ctx->ev[4], ctx->ev[5]);
     *ms_per_launch = ms / reps;
     *bytes_per_launch = bytes;
-    ctx->solved = false;  // scratch vectors were overwritten
+    if (kernel == SCF_K_CGUPDATE) ctx->warm_ok = false;  // x was modified
     return SCF_OK;
 }
 
