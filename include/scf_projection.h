@@ -228,6 +228,35 @@ enum scf_kernel_class {
 int scf_debug_time_kernel(scf_ctx *ctx, int kernel, int reps, double *ms_per_launch,
                           double *bytes_per_launch);
 
+/* ---- allocation-free operator apply ---------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory during a time step -- GPU-resident hosts that serve every device
+ * buffer from their own preallocated arena, or jobs running at a fixed memory
+ * budget on a shared GPU, where a late cudaMalloc may fail and, since it
+ * synchronises the device, stalls their asynchronous work.
+ *
+ * Computes y = A x on the interior cells and x_dot_ax = sum x*(A x), with
+ * A given by its diagonal and E/N/T couplings (the layout scf_debug_operator
+ * reports, here as ghosted device arrays with a zero ghost layer).  Every
+ * pointer is caller-owned DEVICE memory; x_dot_ax may be NULL.  Work is
+ * queued on `stream` (a cudaStream_t; NULL = legacy default stream) and the
+ * call returns without waiting for it.
+ *
+ * Scratch: a file-scope device array of SCF_NOALLOC_PARTIALS + 1 doubles
+ * (32 KiB) that every device loading the library holds until exit.  The
+ * first call on a device looks up that array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the array and it keeps the last call's contents; calls
+ * that overlap on the GPU race on it.  Grids with more than
+ * SCF_NOALLOC_MAX_CELLS ghosted cells are rejected with SCF_ERR_BAD_ARG.    */
+#define SCF_NOALLOC_PARTIALS 4096
+#define SCF_NOALLOC_MAX_CELLS 2147483647LL
+int scf_apply_operator_noalloc(int32_t imax, int32_t jmax, int32_t kmax,
+                               const double *diag, const double *cpl_e,
+                               const double *cpl_n, const double *cpl_t,
+                               const double *x, double *y, double *x_dot_ax,
+                               void *stream);
+
 /* ---- misc -------------------------------------------------------------- */
 const char *scf_status_string(int status);
 /* Copies the context's last error message (NUL-terminated) into buf.       */

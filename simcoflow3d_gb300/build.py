@@ -25,6 +25,7 @@ UNITS = {
     "k_correct.cu": ["-fmad=false"],
     "k_solver.cu": [],
     "scf_api.cu": [],
+    "k_noalloc.cu": [],
 }
 
 

@@ -63,6 +63,7 @@ def load_library(path: Optional[str] = None):
     L.scf_host_unregister.argtypes = [C.c_void_p]
     L.scf_abi_version.argtypes = []
     L.scf_debug_time_kernel.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.scf_apply_operator_noalloc.argtypes = [C.c_int32, C.c_int32, C.c_int32] + [C.c_void_p] * 8
     _lib = L
     return L
 
