@@ -244,7 +244,17 @@ def run_ours(args):
 
     # device-resident timing: mixed (value) and FP64 (comparison)
     results = {}
-    for name, prec in (("mixed", capi.SCF_PREC_MIXED), ("fp64", capi.SCF_PREC_FP64)):
+    precs = (("mixed", capi.SCF_PREC_MIXED), ("fp64", capi.SCF_PREC_FP64))
+    if args.only:
+        # profiling captures: one precision, device-resident loop only
+        name, prec = [x for x in precs if x[0] == args.only][0]
+        proj = Projection.for_workload(w, precision=prec, rel_tol=args.tol, device=local)
+        proj.stage(w)
+        ms, launches, st = time_device(proj, args.steps, args.warmup)
+        print(json.dumps({"only": name, "ms_per_projection": statistics.mean(ms), "stats": st}), flush=True)
+        unpin(lib, pinned)
+        return 0
+    for name, prec in precs:
         proj = Projection.for_workload(w, precision=prec, rel_tol=args.tol, device=local)
         proj.stage(w)
         barrier(dist)
@@ -330,7 +340,8 @@ def run_ours(args):
         "speedup_mixed_vs_fp64": round(fp64 / value, 3),
         "e2e": {"value": round(e2e_total / nproj, 4), "unit": "ms/projection",
                 "h2d_bytes_per_step": int(e2e_stats["bytes_h2d"]),
-                "d2h_bytes_per_step": int(e2e_stats["bytes_d2h"])},
+                "d2h_bytes_per_step": int(e2e_stats["bytes_d2h"]),
+                "ms_h2d": round(e2e_stats["ms_h2d"], 3), "ms_d2h": round(e2e_stats["ms_d2h"], 3)},
         "roofline": {"bound": "hbm", "kernel": "k_cheb_step<float> (fine-level Chebyshev step)",
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
@@ -355,6 +366,8 @@ def main():
     ap.add_argument("--tol", type=float, default=1e-8)
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--n", type=int, default=None, help="smaller grid (profiling captures only)")
+    ap.add_argument("--only", choices=["mixed", "fp64"], default=None,
+                    help="time one precision device-resident only (profiling captures)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--max-cpu-s", type=float, default=150.0, help="stop the reference arm after this many s")
     args = ap.parse_args()

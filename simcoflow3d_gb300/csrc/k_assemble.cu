@@ -84,6 +84,36 @@ __device__ __forceinline__ double beta_of(int pc, int pn, double lam, double bet
 }
 }  // namespace
 
+// Results are memoised on the bit patterns of their inputs: along a column
+// the inputs of a face repeat in uniform regions, and an IEEE operation on
+// identical inputs gives an identical result, so reusing it is exact.  This
+// removes almost all FP64 divisions, whose throughput on this GPU is low.
+struct CoefMemo {
+    unsigned long long dp, dg, beta;
+    double coef;
+    bool valid;
+};
+
+__device__ __forceinline__ double coef_memo(CoefMemo &m, double dp, double dg, double beta, double betap,
+                                            double betam)
+{
+    const unsigned long long a = __double_as_longlong(dp), b = __double_as_longlong(dg),
+                             c = __double_as_longlong(beta);
+    if (!m.valid || a != m.dp || b != m.dg || c != m.beta) {
+        m.dp = a; m.dg = b; m.beta = c; m.valid = true;
+        m.coef = coef_expr(dp, dg, betap, betam, beta);
+    }
+    return m.coef;
+}
+
+// Phase of every ghosted cell (1 wet, 2 dry, 0 neither), once per call.
+__global__ void __launch_bounds__(256) k_phase(AsmArgs a)
+{
+    const int ng = a.d.ng;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < ng; g += gridDim.x * blockDim.x)
+        a.phase[g] = (unsigned char)phase_of(a.vofl[g], a.vof[g], a.phil[g], a.epsi);
+}
+
 __global__ void __launch_bounds__(128) k_pocoef(AsmArgs a)
 {
     const Dims &d = a.d;
@@ -91,46 +121,76 @@ __global__ void __launch_bounds__(128) k_pocoef(AsmArgs a)
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     if (i > d.I || j > d.J) return;
     const int col = (i - 1) * d.J + (j - 1);   // column index in loop order
-    double carry[12];
-    unsigned mask = 0;
+    const int sy = d.gx, sz = d.gx * d.gy;
+    const int goff[6] = {-1, -sy, -sz, 1, sy, sz};
+    double carryW[6], carryD[6];
+    unsigned maskW = 0, maskD = 0;
+    CoefMemo memo[6];
 #pragma unroll
-    for (int s = 0; s < 12; ++s) carry[s] = 0.0;
+    for (int f = 0; f < 6; ++f) {
+        carryW[f] = 0.0; carryD[f] = 0.0;
+        memo[f].valid = false; memo[f].dp = memo[f].dg = memo[f].beta = 0ull; memo[f].coef = 0.0;
+    }
+    const int im = i > 1 ? i - 1 : 1, jm = j > 1 ? j - 1 : 1;
     for (int k = 1; k <= d.K; ++k) {
         const int gc = gidx(d, i, j, k), nc = nidx(d, i, j, k);
-        const int pc = phase_of(a.vofl[gc], a.vof[gc], a.phil[gc], a.epsi);
+        const int pc = a.phase[gc];
+        const int km = k > 1 ? k - 1 : 1;
 #pragma unroll
         for (int f = 0; f < 6; ++f) {
             double coef = 0.0;
             if (pc != 0) {
-                const int gn = gidx(d, i + c_di[f], j + c_dj[f], k + c_dk[f]);
-                const int pn = phase_of(a.vofl[gn], a.vof[gn], a.phil[gn], a.epsi);
-                const int s = 2 * f + (pc == 2);
+                const int gn = gc + goff[f];
+                int pn = a.phase[gn];
                 double dp, dg;
-                face_terms(a, f, i, j, k, dp, dg);
-                if (pn != 0) {
-                    const double lam = (pc != pn) ? lamda_of(a, gc, gn) : 0.0;
-                    const double beta = beta_of(pc, pn, lam, a.betap, a.betam);
-                    carry[s] = beta;
-                    mask |= 1u << s;
-                    coef = coef_expr(dp, dg, a.betap, a.betam, beta);
-                } else if (mask & (1u << s)) {
-                    coef = coef_expr(dp, dg, a.betap, a.betam, carry[s]);
+                switch (f) {   // Dp(im,jm,km) and DGrid(max(im,1),...) (ProjectionP.f90:145-153)
+                case 0: dp = a.dpu[gc - 1];  dg = a.udx[nidx(d, im, j, k)]; break;
+                case 1: dp = a.dpv[gc - sy]; dg = a.vdy[nidx(d, i, jm, k)]; break;
+                case 2: dp = a.dpw[gc - sz]; dg = a.wdz[nidx(d, i, j, km)]; break;
+                case 3: dp = a.dpu[gc];      dg = a.udx[nc]; break;
+                case 4: dp = a.dpv[gc];      dg = a.vdy[nc]; break;
+                default: dp = a.dpw[gc];     dg = a.wdz[nc]; break;
+                }
+                double beta;
+                bool have = true;
+                if (pn == pc) {
+                    beta = pc == 1 ? a.betam : a.betap;
+                } else if (pn != 0) {
+                    const double lam = lamda_of(a, gc, gn);
+                    beta = pc == 1 ? lam * a.betam + (1.0 - lam) * a.betap : lam * a.betap + (1.0 - lam) * a.betam;
+                } else if (pc == 1 ? (maskW >> f) & 1u : (maskD >> f) & 1u) {
+                    beta = pc == 1 ? carryW[f] : carryD[f];
+                    pn = -1;   // carried, not assigned
                 } else {
+                    have = false;
                     unsigned slot = atomicAdd(a.stale_count, 1u);
                     if (slot < a.stale_cap) {
                         const long long L = ((long long)col) * d.K + (k - 1);
-                        a.stale_list[slot] = (L << 4) | ((long long)s);
+                        a.stale_list[slot] = (L << 4) | ((long long)(2 * f + (pc == 2)));
                     } else {
                         atomicOr(a.flags, FLAG_STALE_OVERFLOW);
                     }
+                }
+                if (have) {
+                    if (pn > 0) {
+                        if (pc == 1) { carryW[f] = beta; maskW |= 1u << f; }
+                        else { carryD[f] = beta; maskD |= 1u << f; }
+                    }
+                    coef = coef_memo(memo[f], dp, dg, beta, a.betap, a.betam);
                 }
             }
             a.pocoef[nc + (long long)d.n * f] = coef;
         }
     }
 #pragma unroll
-    for (int s = 0; s < 12; ++s) a.col_val[(long long)col * 12 + s] = carry[s];
-    a.col_mask[col] = (unsigned short)mask;
+    for (int f = 0; f < 6; ++f) {
+        a.col_val[(long long)col * 12 + 2 * f] = carryW[f];
+        a.col_val[(long long)col * 12 + 2 * f + 1] = carryD[f];
+    }
+    unsigned m = 0;
+#pragma unroll
+    for (int f = 0; f < 6; ++f) m |= (((maskW >> f) & 1u) << (2 * f)) | (((maskD >> f) & 1u) << (2 * f + 1));
+    a.col_mask[col] = (unsigned short)m;
 }
 
 // Group summaries: the last assignment of each (face, W/D) stream within
@@ -215,82 +275,142 @@ __global__ void k_pocoef_boundary(AsmArgs a)
 // Per active cell: the exact diagonal, the couplings towards E/N/T from the
 // cell's own row, the diagonal part without a coupling (Dirichlet faces and
 // faces to solid cells, used to coarsen), and b.  Solid cells: identity.
+namespace {
+__device__ __forceinline__ bool finite_bits(double x)
+{
+    return ((unsigned long long)__double_as_longlong(x) & 0x7ff0000000000000ull) != 0x7ff0000000000000ull;
+}
+__device__ __forceinline__ unsigned long long bits(double x) { return (unsigned long long)__double_as_longlong(x); }
+
+// ((p*area)*d1)*d2, the face term of SetPoissonMatrix, memoised on its inputs.
+struct TermMemo {
+    unsigned long long p, ar, d1, d2;
+    double t;
+    bool valid;
+};
+__device__ __forceinline__ double term_memo(TermMemo &m, double p, double ar, double d1, double d2)
+{
+    if (!m.valid || bits(p) != m.p || bits(ar) != m.ar || bits(d1) != m.d1 || bits(d2) != m.d2) {
+        m.p = bits(p); m.ar = bits(ar); m.d1 = bits(d1); m.d2 = bits(d2); m.valid = true;
+        m.t = p * ar * d1 * d2;
+    }
+    return m.t;
+}
+// a*u with a == 1.0 short-cut (exact: 1.0*u == u)
+__device__ __forceinline__ double amul(double ar, double u) { return bits(ar) == 0x3ff0000000000000ull ? u : ar * u; }
+}  // namespace
+
 template <bool MIXED>
-__global__ void k_operator(AsmArgs a, OpArgs o)
+__global__ void __launch_bounds__(128) k_operator(AsmArgs a, OpArgs o)
 {
     const Dims &d = a.d;
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const int k = blockIdx.z * blockDim.z + threadIdx.z + 1;
-    if (i > d.I || j > d.J || k > d.K) return;
-    const int g = gidx(d, i, j, k), n = nidx(d, i, j, k);
-    const int ct = a.ct[n], pos = a.pos[n];
-    if ((pos == -1) != (ct == 2) || pos > a.ext_cell || pos < -1) atomicOr(a.flags, FLAG_BAD_POSNU);
-    if (ct == 2) {
-        o.diag[g] = 1.0; o.dinv[g] = 0.0; o.cE[g] = 0.0; o.cN[g] = 0.0; o.cT[g] = 0.0;
-        o.extra[g] = 0.0; o.b[g] = 0.0; o.active[g] = 0;
-        if (MIXED) {
-            o.diag32[g] = 1.0f; o.dinv32[g] = 0.0f; o.cE32[g] = 0.0f; o.cN32[g] = 0.0f; o.cT32[g] = 0.0f;
-            o.extra32[g] = 0.0f;
-        }
-        return;
-    }
-    const double dx = a.pdx[n], dy = a.pdy[n], dz = a.pdz[n];
-    const long long N = d.n;
-    const double p1 = a.pocoef[n], p2 = a.pocoef[n + N], p3 = a.pocoef[n + 2 * N];
-    const double p4 = a.pocoef[n + 3 * N], p5 = a.pocoef[n + 4 * N], p6 = a.pocoef[n + 5 * N];
-    const double eW = a.ee[g - 1], eE = a.ee[g];
-    const double nS = a.ne[g - d.gx], nN = a.ne[g];
-    const double tB = a.te[g - d.gx * d.gy], tT = a.te[g];
-    const double t1 = p1 * eW * dy * dz, t2 = p2 * nS * dx * dz, t3 = p3 * tB * dx * dy;
-    const double t4 = p4 * eE * dy * dz, t5 = p5 * nN * dx * dz, t6 = p6 * tT * dx * dy;
-    double dg = t1 + t2 + t3 + t4 + t5 + t6;
-    const int *fl = a.flag;
-    if (fl[0] == 1 && i == 1) dg = dg - t1;
-    if (fl[2] == 1 && j == 1) dg = dg - t2;
-    if (fl[4] == 1 && k == 1) dg = dg - t3;
-    if (fl[1] == 1 && i == d.I) dg = dg - t4;
-    if (fl[3] == 1 && j == d.J) dg = dg - t5;
-    if (fl[5] == 1 && k == d.K) dg = dg - t6;
-    double cE = 0.0, cN = 0.0, cT = 0.0, ex = 0.0;
-    if (i == 1) { if (fl[0] == 0) ex += t1; } else if (a.pos[n - 1] == -1) ex += t1;
-    if (j == 1) { if (fl[2] == 0) ex += t2; } else if (a.pos[n - d.I] == -1) ex += t2;
-    if (k == 1) { if (fl[4] == 0) ex += t3; } else if (a.pos[n - d.I * d.J] == -1) ex += t3;
-    if (i == d.I) { if (fl[1] == 0) ex += t4; } else if (a.pos[n + 1] == -1) ex += t4; else cE = t4;
-    if (j == d.J) { if (fl[3] == 0) ex += t5; } else if (a.pos[n + d.I] == -1) ex += t5; else cN = t5;
-    if (k == d.K) { if (fl[5] == 0) ex += t6; } else if (a.pos[n + d.I * d.J] == -1) ex += t6; else cT = t6;
-
-    // right-hand side (ProjectionP.f90:521-546)
-    const double *u = a.us, *v = a.vs, *w = a.ws;
+    if (i > d.I || j > d.J) return;
     const int sy = d.gx, sz = d.gx * d.gy;
-    double r = -dy * dz * (eE * u[g] - eW * u[g - 1]) - dx * dz * (nN * v[g] - nS * v[g - sy]) -
-               dx * dy * (tT * w[g] - tB * w[g - sz]);
-    r = r + (a.vof[g] - a.vofo[g]) * dx * dy * dz / a.dt;
-    if (fl[0] == 0 && i == 1) r = r + p1 * a.bvar[0][(j - 1) + d.J * (k - 1)];
-    if (fl[1] == 0 && i == d.I) r = r + p4 * a.bvar[1][(j - 1) + d.J * (k - 1)];
-    if (fl[2] == 0 && j == 1) r = r + p2 * a.bvar[2][(i - 1) + d.I * (k - 1)];
-    if (fl[3] == 0 && j == d.J) r = r + p5 * a.bvar[3][(i - 1) + d.I * (k - 1)];
-    if (fl[4] == 0 && k == 1) r = r + p3 * a.bvar[4][(i - 1) + d.I * (j - 1)];
-    if (fl[5] == 0 && k == d.K) r = r + p6 * a.bvar[5][(i - 1) + d.I * (j - 1)];
+    const long long N = d.n;
+    const int *fl = a.flag;
+    TermMemo tm[6];
+#pragma unroll
+    for (int f = 0; f < 6; ++f) { tm[f].valid = false; tm[f].p = tm[f].ar = tm[f].d1 = tm[f].d2 = 0ull; tm[f].t = 0.0; }
+    // memo of the row (diag and dependants) on the six terms
+    unsigned long long rt[6] = {0, 0, 0, 0, 0, 0};
+    bool rvalid = false;
+    double dg = 0.0, dinv = 0.0;
+    float d32 = 0.f, di32 = 0.f;
+    // memo of the spacing products of the rhs
+    unsigned long long pdx = 0, pdy = 0, pdz = 0;
+    double dydz = 0.0, dxdz = 0.0, dxdy = 0.0, dxdydz = 0.0;
+    bool pvalid = false;
+    for (int k = 1; k <= d.K; ++k) {
+        const int g = gidx(d, i, j, k), n = nidx(d, i, j, k);
+        const int ct = a.ct[n], pos = a.pos[n];
+        if ((pos == -1) != (ct == 2) || pos > a.ext_cell || pos < -1) atomicOr(a.flags, FLAG_BAD_POSNU);
+        if (ct == 2) {
+            o.diag[g] = 1.0; o.dinv[g] = 0.0; o.cE[g] = 0.0; o.cN[g] = 0.0; o.cT[g] = 0.0;
+            o.extra[g] = 0.0; o.b[g] = 0.0; o.active[g] = 0;
+            if (MIXED) {
+                o.diag32[g] = 1.0f; o.dinv32[g] = 0.0f; o.cE32[g] = 0.0f; o.cN32[g] = 0.0f; o.cT32[g] = 0.0f;
+                o.extra32[g] = 0.0f;
+            }
+            continue;
+        }
+        const double dx = a.pdx[n], dy = a.pdy[n], dz = a.pdz[n];
+        const double p1 = a.pocoef[n], p2 = a.pocoef[n + N], p3 = a.pocoef[n + 2 * N];
+        const double p4 = a.pocoef[n + 3 * N], p5 = a.pocoef[n + 4 * N], p6 = a.pocoef[n + 5 * N];
+        const double eW = a.ee[g - 1], eE = a.ee[g];
+        const double nS = a.ne[g - sy], nN = a.ne[g];
+        const double tB = a.te[g - sz], tT = a.te[g];
+        const double t1 = term_memo(tm[0], p1, eW, dy, dz), t2 = term_memo(tm[1], p2, nS, dx, dz);
+        const double t3 = term_memo(tm[2], p3, tB, dx, dy), t4 = term_memo(tm[3], p4, eE, dy, dz);
+        const double t5 = term_memo(tm[4], p5, nN, dx, dz), t6 = term_memo(tm[5], p6, tT, dx, dy);
+        const bool bnd = i == 1 || j == 1 || k == 1 || i == d.I || j == d.J || k == d.K;
+        if (bnd || !rvalid || bits(t1) != rt[0] || bits(t2) != rt[1] || bits(t3) != rt[2] || bits(t4) != rt[3] ||
+            bits(t5) != rt[4] || bits(t6) != rt[5]) {
+            double v = t1 + t2 + t3 + t4 + t5 + t6;
+            if (fl[0] == 1 && i == 1) v = v - t1;
+            if (fl[2] == 1 && j == 1) v = v - t2;
+            if (fl[4] == 1 && k == 1) v = v - t3;
+            if (fl[1] == 1 && i == d.I) v = v - t4;
+            if (fl[3] == 1 && j == d.J) v = v - t5;
+            if (fl[5] == 1 && k == d.K) v = v - t6;
+            dg = v;
+            if (!MIXED) dinv = dg > 0.0 ? 1.0 / dg : 0.0;
+            if (MIXED) { d32 = (float)dg; di32 = d32 > 0.0f ? 1.0f / d32 : 0.0f; }
+            // a boundary row is never reused by an interior one
+            rvalid = !bnd;
+            rt[0] = bits(t1); rt[1] = bits(t2); rt[2] = bits(t3); rt[3] = bits(t4); rt[4] = bits(t5); rt[5] = bits(t6);
+        }
+        double cE = 0.0, cN = 0.0, cT = 0.0, ex = 0.0;
+        if (i == 1) { if (fl[0] == 0) ex += t1; } else if (a.pos[n - 1] == -1) ex += t1;
+        if (j == 1) { if (fl[2] == 0) ex += t2; } else if (a.pos[n - d.I] == -1) ex += t2;
+        if (k == 1) { if (fl[4] == 0) ex += t3; } else if (a.pos[n - d.I * d.J] == -1) ex += t3;
+        if (i == d.I) { if (fl[1] == 0) ex += t4; } else if (a.pos[n + 1] == -1) ex += t4; else cE = t4;
+        if (j == d.J) { if (fl[3] == 0) ex += t5; } else if (a.pos[n + d.I] == -1) ex += t5; else cN = t5;
+        if (k == d.K) { if (fl[5] == 0) ex += t6; } else if (a.pos[n + d.I * d.J] == -1) ex += t6; else cT = t6;
 
-    if (!(dg > 0.0) || !isfinite(dg)) atomicOr(a.flags, isfinite(dg) ? FLAG_BAD_DIAG : FLAG_NONFINITE);
-    if (!isfinite(r) || !isfinite(cE) || !isfinite(cN) || !isfinite(cT) || !isfinite(ex))
-        atomicOr(a.flags, FLAG_NONFINITE);
-    const int phc = phase_of(a.vofl[g], a.vof[g], a.phil[g], a.epsi);
-    if (phc == 0) atomicOr(a.flags, FLAG_NEITHER_ACTIVE);
+        // right-hand side (ProjectionP.f90:521-546), same rounding as the
+        // Fortran expression: -dy*dz*(A) - dx*dz*(B) - dx*dy*(C)
+        if (!pvalid || bits(dx) != pdx || bits(dy) != pdy || bits(dz) != pdz) {
+            pdx = bits(dx); pdy = bits(dy); pdz = bits(dz); pvalid = true;
+            dydz = -dy * dz; dxdz = dx * dz; dxdy = dx * dy;
+        }
+        const double A = amul(eE, a.us[g]) - amul(eW, a.us[g - 1]);
+        const double B = amul(nN, a.vs[g]) - amul(nS, a.vs[g - sy]);
+        const double Cc = amul(tT, a.ws[g]) - amul(tB, a.ws[g - sz]);
+        double r = dydz * A - dxdz * B - dxdy * Cc;
+        const double vf = a.vof[g], vo = a.vofo[g];
+        if (bits(vf) == bits(vo) && finite_bits(vf)) {
+            r = r + 0.0;   // (vof - vofO)*dx*dy*dz/dt is +0 exactly
+        } else {
+            r = r + (vf - vo) * dx * dy * dz / a.dt;
+        }
+        if (bnd) {
+            if (fl[0] == 0 && i == 1) r = r + p1 * a.bvar[0][(j - 1) + d.J * (k - 1)];
+            if (fl[1] == 0 && i == d.I) r = r + p4 * a.bvar[1][(j - 1) + d.J * (k - 1)];
+            if (fl[2] == 0 && j == 1) r = r + p2 * a.bvar[2][(i - 1) + d.I * (k - 1)];
+            if (fl[3] == 0 && j == d.J) r = r + p5 * a.bvar[3][(i - 1) + d.I * (k - 1)];
+            if (fl[4] == 0 && k == 1) r = r + p3 * a.bvar[4][(i - 1) + d.I * (j - 1)];
+            if (fl[5] == 0 && k == d.K) r = r + p6 * a.bvar[5][(i - 1) + d.I * (j - 1)];
+        }
+        if (!finite_bits(dg)) atomicOr(a.flags, FLAG_NONFINITE);
+        else if (!(dg > 0.0)) atomicOr(a.flags, FLAG_BAD_DIAG);
+        if (!finite_bits(r) || !finite_bits(cE) || !finite_bits(cN) || !finite_bits(cT) || !finite_bits(ex))
+            atomicOr(a.flags, FLAG_NONFINITE);
+        if (a.phase[g] == 0) atomicOr(a.flags, FLAG_NEITHER_ACTIVE);
 
-    o.diag[g] = dg;
-    o.dinv[g] = dg > 0.0 ? 1.0 / dg : 0.0;
-    o.cE[g] = cE; o.cN[g] = cN; o.cT[g] = cT;
-    o.extra[g] = ex;
-    o.b[g] = r;
-    o.active[g] = 1;
-    if (MIXED) {
-        const float d32 = (float)dg;
-        o.diag32[g] = d32;
-        o.dinv32[g] = d32 > 0.0f ? 1.0f / d32 : 0.0f;
-        o.cE32[g] = (float)cE; o.cN32[g] = (float)cN; o.cT32[g] = (float)cT;
-        o.extra32[g] = (float)ex;
+        o.diag[g] = dg;
+        if (!MIXED) o.dinv[g] = dinv;
+        o.cE[g] = cE; o.cN[g] = cN; o.cT[g] = cT;
+        o.extra[g] = ex;
+        o.b[g] = r;
+        o.active[g] = 1;
+        if (MIXED) {
+            o.diag32[g] = d32;
+            o.dinv32[g] = di32;
+            o.cE32[g] = (float)cE; o.cN32[g] = (float)cN; o.cT32[g] = (float)cT;
+            o.extra32[g] = (float)ex;
+        }
     }
 }
 
@@ -303,8 +423,9 @@ int launch_assemble(const AsmArgs &a, const OpArgs &o, bool mixed, cudaStream_t 
     cudaMemsetAsync(a.stale_count, 0, sizeof(unsigned), st);
     {
         dim3 b(32, 4), g((d.I + 31) / 32, (d.J + 3) / 4);
+        k_phase<<<2 * 152 * 8, 256, 0, st>>>(a);
         k_pocoef<<<g, b, 0, st>>>(a);
-        *launches += 1;
+        *launches += 2;
     }
     cudaMemcpyAsync(stale_count_host, a.stale_count, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
     cudaStreamSynchronize(st);
@@ -324,11 +445,11 @@ int launch_assemble(const AsmArgs &a, const OpArgs &o, bool mixed, cudaStream_t 
         k_pocoef_boundary<<<g, 256, 0, st>>>(a);
         *launches += 1;
     }
-    Launch3 l = launch_interior(d.I, d.J, d.K);
+    dim3 ob(32, 4), og((d.I + 31) / 32, (d.J + 3) / 4);
     if (mixed)
-        k_operator<true><<<l.grid, l.block, 0, st>>>(a, o);
+        k_operator<true><<<og, ob, 0, st>>>(a, o);
     else
-        k_operator<false><<<l.grid, l.block, 0, st>>>(a, o);
+        k_operator<false><<<og, ob, 0, st>>>(a, o);
     *launches += 1;
     return (int)cudaGetLastError();
 }

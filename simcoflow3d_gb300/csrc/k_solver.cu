@@ -62,15 +62,42 @@ void cg_finish_alpha(Reducer &R, int nblocks, cudaStream_t st, int *launches)
 // ---------------------------------------------------------------------------
 // FP64 CG kernels on the fine level
 
-__global__ void __launch_bounds__(256) k_spmv_dot(LevelView<double> A, const double *__restrict__ p,
+// Fine-level FP64 kernels march KZ cells along k per thread: the k-neighbours
+// stay in registers and the FP64 block reduction (costly on this GPU's FP64
+// pipe) is paid once per KZ cells.
+constexpr int KZ = 8;
+
+inline Launch3 launch_zchunk(int n0, int n1, int n2)
+{
+    Launch3 l;
+    l.block = dim3(32, 4, 1);
+    l.grid = dim3((n0 + 31) / 32, (n1 + 3) / 4, (n2 + KZ - 1) / KZ);
+    return l;
+}
+
+#define ZCHUNK_IJK(L)                                                  \
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;          \
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;          \
+    const int k0 = blockIdx.z * KZ + 1;                               \
+    const int k1 = min(k0 + KZ - 1, (L).n2);                          \
+    const bool in = i <= (L).n0 && j <= (L).n1;
+
+__global__ void __launch_bounds__(128) k_spmv_dot(LevelView<double> A, const double *__restrict__ p,
                                                   double *__restrict__ q, double *__restrict__ part)
 {
-    INTERIOR_IJK(A);
+    ZCHUNK_IJK(A);
     double v = 0.0;
     if (in) {
-        const double y = apply_row(A, p, c);
-        q[c] = y;
-        v = p[c] * y;
+        int c = i + A.sy * j + A.sz * k0;
+        double xm = p[c - A.sz], x0 = p[c], tb = A.cT[c - A.sz];
+        for (int k = k0; k <= k1; ++k, c += A.sz) {
+            const double xp = p[c + A.sz], tt = A.cT[c];
+            const double y = A.diag[c] * x0 - (A.cE[c] * p[c + 1] + A.cE[c - 1] * p[c - 1] + A.cN[c] * p[c + A.sy] +
+                                               A.cN[c - A.sy] * p[c - A.sy] + tt * xp + tb * xm);
+            q[c] = y;
+            v += x0 * y;
+            xm = x0; x0 = xp; tb = tt;
+        }
     }
     v = block_sum(v);
     if (thread_linear() == 0) part[block_linear()] = v;
@@ -80,27 +107,30 @@ void cg_spmv_dot(const LevelView<double> &A, const double *p, double *q, Reducer
                  cudaStream_t st, int *launches)
 {
     (void)slot_out;
-    Launch3 l = launch_interior(A.n0, A.n1, A.n2);
+    Launch3 l = launch_zchunk(A.n0, A.n1, A.n2);
     k_spmv_dot<<<l.grid, l.block, 0, st>>>(A, p, q, R.partials);
     *launches += 1;
     cg_finish_alpha(R, (int)nblocks(l), st, launches);
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_cg_update(LevelView<double> A, double *__restrict__ x,
+__global__ void __launch_bounds__(128) k_cg_update(LevelView<double> A, double *__restrict__ x,
                                                    double *__restrict__ r, const double *__restrict__ p,
                                                    const double *__restrict__ q, T *__restrict__ rlow,
                                                    const double *__restrict__ scal, double *__restrict__ part)
 {
-    INTERIOR_IJK(A);
+    ZCHUNK_IJK(A);
     double v = 0.0;
     if (in) {
         const double alpha = scal[S_ALPHA];
-        x[c] = x[c] + alpha * p[c];
-        const double rn = r[c] - alpha * q[c];
-        r[c] = rn;
-        if (rlow) rlow[c] = (T)rn;
-        v = rn * rn;
+        int c = i + A.sy * j + A.sz * k0;
+        for (int k = k0; k <= k1; ++k, c += A.sz) {
+            x[c] = x[c] + alpha * p[c];
+            const double rn = r[c] - alpha * q[c];
+            r[c] = rn;
+            if (rlow) rlow[c] = (T)rn;
+            v += rn * rn;
+        }
     }
     v = block_sum(v);
     if (thread_linear() == 0) part[block_linear()] = v;
@@ -110,47 +140,66 @@ template <typename T>
 void cg_update(const LevelView<double> &A, double *x, double *r, const double *p, const double *q, T *rlow,
                Reducer &R, cudaStream_t st, int *launches)
 {
-    Launch3 l = launch_interior(A.n0, A.n1, A.n2);
+    Launch3 l = launch_zchunk(A.n0, A.n1, A.n2);
     k_cg_update<T><<<l.grid, l.block, 0, st>>>(A, x, r, p, q, rlow, R.scal, R.partials);
     *launches += 1;
     reduce_to(R, (int)nblocks(l), S_RR, st, launches);
 }
 
+// (r, z): in mixed mode r is taken from its FP32 copy (the V-cycle's rhs) and
+// the products are formed in FP32, accumulated per thread in FP32 over KZ
+// cells and across threads in FP64; z is an FP32 preconditioner output, so
+// this loses nothing that matters for beta.  FP64 mode: FP64 throughout.
 template <typename T>
-__global__ void __launch_bounds__(256) k_dot_rz(LevelView<double> A, const double *__restrict__ r,
-                                                const T *__restrict__ z, double *__restrict__ part)
+__global__ void __launch_bounds__(128) k_dot_rz(LevelView<double> A, const double *__restrict__ r,
+                                                const T *__restrict__ rlow, const T *__restrict__ z,
+                                                double *__restrict__ part)
 {
-    INTERIOR_IJK(A);
+    ZCHUNK_IJK(A);
     double v = 0.0;
-    if (in) v = r[c] * (double)z[c];
+    if (in) {
+        int c = i + A.sy * j + A.sz * k0;
+        if (sizeof(T) == 4) {
+            float acc = 0.f;
+            for (int k = k0; k <= k1; ++k, c += A.sz) acc += (float)rlow[c] * (float)z[c];
+            v = (double)acc;
+        } else {
+            for (int k = k0; k <= k1; ++k, c += A.sz) v += r[c] * (double)z[c];
+        }
+    }
     v = block_sum(v);
     if (thread_linear() == 0) part[block_linear()] = v;
 }
 
 template <typename T>
-void cg_dot_rz(const LevelView<double> &A, const double *r, const T *z, Reducer &R, cudaStream_t st, int *launches)
+void cg_dot_rz(const LevelView<double> &A, const double *r, const T *rlow, const T *z, Reducer &R, cudaStream_t st,
+               int *launches)
 {
-    Launch3 l = launch_interior(A.n0, A.n1, A.n2);
-    k_dot_rz<T><<<l.grid, l.block, 0, st>>>(A, r, z, R.partials);
+    Launch3 l = launch_zchunk(A.n0, A.n1, A.n2);
+    k_dot_rz<T><<<l.grid, l.block, 0, st>>>(A, r, rlow, z, R.partials);
     k_reduce<<<1, 1024, 0, st>>>(R.partials, (int)nblocks(l), R.scal, 0, RM_BETA);
     *launches += 2;
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_pupdate(LevelView<double> A, const T *__restrict__ z,
+__global__ void __launch_bounds__(128) k_pupdate(LevelView<double> A, const T *__restrict__ z,
                                                  double *__restrict__ p, const double *__restrict__ scal, int first)
 {
-    INTERIOR_IJK(A);
+    ZCHUNK_IJK(A);
     if (!in) return;
-    const double zz = (double)z[c];
-    p[c] = first ? zz : zz + scal[S_BETA] * p[c];
+    const double beta = first ? 0.0 : scal[S_BETA];
+    int c = i + A.sy * j + A.sz * k0;
+    for (int k = k0; k <= k1; ++k, c += A.sz) {
+        const double zz = (double)z[c];
+        p[c] = first ? zz : zz + beta * p[c];
+    }
 }
 
 template <typename T>
 void cg_pupdate(const LevelView<double> &A, const T *z, double *p, const double *scal, bool first, cudaStream_t st,
                 int *launches)
 {
-    Launch3 l = launch_interior(A.n0, A.n1, A.n2);
+    Launch3 l = launch_zchunk(A.n0, A.n1, A.n2);
     k_pupdate<T><<<l.grid, l.block, 0, st>>>(A, z, p, scal, first ? 1 : 0);
     *launches += 1;
 }
@@ -302,11 +351,12 @@ __global__ void __launch_bounds__(256) k_post_first(LevelView<T> F, const T *__r
 {
     INTERIOR_IJK(F);
     if (!in) return;
+    const int s0 = f0 - 1, s1 = f1 - 1, s2 = f2 - 1;   // factors are 1 or 2
     auto xc = [&](int ii, int jj, int kk) -> T {
         const int fc = ii + F.sy * jj + F.sz * kk;
         T v = x[fc];
         if (F.dinv[fc] != T(0)) {
-            const int I = (ii - 1) / f0 + 1, J = (jj - 1) / f1 + 1, K = (kk - 1) / f2 + 1;
+            const int I = ((ii - 1) >> s0) + 1, J = ((jj - 1) >> s1) + 1, K = ((kk - 1) >> s2) + 1;
             v += e[I + C.sy * J + C.sz * K];
         }
         return v;
@@ -560,7 +610,7 @@ void probe_prolong(MgLevel<T> &F, MgLevel<T> &C, const ChebCoef &cc, cudaStream_
 
 void probe_spmv(const LevelView<double> &A, const double *p, double *q, Reducer &R, cudaStream_t st)
 {
-    Launch3 l = launch_interior(A.n0, A.n1, A.n2);
+    Launch3 l = launch_zchunk(A.n0, A.n1, A.n2);
     k_spmv_dot<<<l.grid, l.block, 0, st>>>(A, p, q, R.partials);
 }
 
@@ -584,10 +634,10 @@ template void cg_update<float>(const LevelView<double> &, double *, double *, co
                                Reducer &, cudaStream_t, int *);
 template void cg_update<double>(const LevelView<double> &, double *, double *, const double *, const double *,
                                 double *, Reducer &, cudaStream_t, int *);
-template void cg_dot_rz<float>(const LevelView<double> &, const double *, const float *, Reducer &, cudaStream_t,
-                               int *);
-template void cg_dot_rz<double>(const LevelView<double> &, const double *, const double *, Reducer &, cudaStream_t,
-                                int *);
+template void cg_dot_rz<float>(const LevelView<double> &, const double *, const float *, const float *, Reducer &,
+                               cudaStream_t, int *);
+template void cg_dot_rz<double>(const LevelView<double> &, const double *, const double *, const double *,
+                                Reducer &, cudaStream_t, int *);
 template void cg_pupdate<float>(const LevelView<double> &, const float *, double *, const double *, bool,
                                 cudaStream_t, int *);
 template void cg_pupdate<double>(const LevelView<double> &, const double *, double *, const double *, bool,

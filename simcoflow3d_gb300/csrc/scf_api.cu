@@ -56,6 +56,7 @@ struct scf_ctx {
     unsigned stale_cap;
     double *col_val, *grp_val;
     unsigned short *col_mask, *grp_mask;
+    unsigned char *phase;
     // level-0 operator, FP64
     double *diag, *dinv, *cE, *cN, *cT, *extra, *b;
     unsigned char *active;
@@ -268,6 +269,8 @@ AsmArgs asm_args(scf_ctx *ctx)
     a.stale_count = ctx->stale_count; a.stale_cap = ctx->stale_cap; a.stale_list = ctx->stale_list;
     a.col_val = ctx->col_val; a.col_mask = ctx->col_mask; a.grp_val = ctx->grp_val; a.grp_mask = ctx->grp_mask;
     a.flags = ctx->flags;
+    a.phase = ctx->phase;
+    a.rdt = 1.0 / ctx->dt;
     return a;
 }
 
@@ -387,7 +390,7 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
     for (;;) {
         if (mixed) copy_to_low(A, ctx->r, rlow, ctx->st, &ctx->launches);
         T *z = precondition<T>(ctx, L, cc);
-        cg_dot_rz<T>(A, ctx->r, z, ctx->R, ctx->st, &ctx->launches);
+        cg_dot_rz<T>(A, ctx->r, (const T *)L[0].b, z, ctx->R, ctx->st, &ctx->launches);
         cg_pupdate<T>(A, z, ctx->p, ctx->R.scal, true, ctx->st, &ctx->launches);
         bool conv = false;
         while (its < ctx->opts.max_iter) {
@@ -404,7 +407,7 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
             const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
             if (el > ctx->opts.time_limit_s) break;
             z = precondition<T>(ctx, L, cc);
-            cg_dot_rz<T>(A, ctx->r, z, ctx->R, ctx->st, &ctx->launches);
+            cg_dot_rz<T>(A, ctx->r, (const T *)L[0].b, z, ctx->R, ctx->st, &ctx->launches);
             cg_pupdate<T>(A, z, ctx->p, ctx->R.scal, false, ctx->st, &ctx->launches);
         }
         // true FP64 residual (the refinement check)
@@ -677,6 +680,7 @@ int scf_ctx_create(scf_ctx **out, int32_t imax, int32_t jmax, int32_t kmax, cons
     A(ctx->stale_list, ctx->stale_cap);
     const long long ncol = (long long)imax * jmax, ngrp = (ncol + 63) / 64;
     A(ctx->col_val, 12 * ncol); A(ctx->col_mask, ncol); A(ctx->grp_val, 12 * ngrp); A(ctx->grp_mask, ngrp);
+    A(ctx->phase, ng);
     A(ctx->diag, ng); A(ctx->dinv, ng); A(ctx->cE, ng); A(ctx->cN, ng); A(ctx->cT, ng); A(ctx->extra, ng);
     A(ctx->b, ng); A(ctx->active, ng);
     A(ctx->x, ng); A(ctx->r, ng); A(ctx->p, ng); A(ctx->q, ng);
@@ -790,13 +794,24 @@ int scf_update_puvw(scf_ctx *ctx, const scf_poisson_in *in, const scf_correct_in
     if (!stats) stats = &local;
     auto t0 = std::chrono::steady_clock::now();
     int64_t bi = 0, bo = 0;
+    cudaEventRecord(ctx->ev[6], ctx->st);
     rc = stage(ctx, in, corr, u, v, w, p, &bi);
     if (rc) return rc;
+    cudaEventRecord(ctx->ev[7], ctx->st);
     rc = run(ctx, true, stats);
     if (rc && rc != SCF_ERR_NOT_CONVERGED) return rc;
     const int solve_rc = rc;
+    float h2d_ms = 0.f;
+    cudaEventElapsedTime(&h2d_ms, ctx->ev[6], ctx->ev[7]);
+    cudaEventRecord(ctx->ev[6], ctx->st);
     rc = fetch(ctx, u, v, w, p, nullptr, nullptr, bc, &bo);
     if (rc) return rc;
+    cudaEventRecord(ctx->ev[7], ctx->st);
+    cudaEventSynchronize(ctx->ev[7]);
+    float d2h_ms = 0.f;
+    cudaEventElapsedTime(&d2h_ms, ctx->ev[6], ctx->ev[7]);
+    stats->ms_h2d = h2d_ms;
+    stats->ms_d2h = d2h_ms;
     stats->bytes_h2d = bi;
     stats->bytes_d2h = bo;
     stats->ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();

@@ -23,6 +23,8 @@ struct AsmArgs {
     double *grp_val;        // [groups][12]
     unsigned short *grp_mask;
     unsigned *flags;
+    unsigned char *phase;   // ghosted, 1 wet / 2 dry / 0 neither
+    double rdt;             // 1/dt
 };
 
 // Level-0 operator outputs (ghosted layout).
@@ -92,7 +94,7 @@ template <typename T>
 void cg_update(const LevelView<double> &A, double *x, double *r, const double *p, const double *q, T *rlow,
                Reducer &R, cudaStream_t st, int *launches);
 template <typename T>
-void cg_dot_rz(const LevelView<double> &A, const double *r, const T *z, Reducer &R, cudaStream_t st,
+void cg_dot_rz(const LevelView<double> &A, const double *r, const T *rlow, const T *z, Reducer &R, cudaStream_t st,
                int *launches);
 template <typename T>
 void cg_pupdate(const LevelView<double> &A, const T *z, double *p, const double *scal, bool first,
