@@ -73,9 +73,13 @@ __device__ __forceinline__ double lamda_of(const AsmArgs &a, int gc, int gn)
 // (BetaD) of the latest earlier cell, in its loop order (i outer, j, k
 // innermost), that assigned it within the same face call.  Each thread
 // marches one (i,j) column in k -- exactly a contiguous run of that loop
-// order -- and carries the twelve (face, W/D) values in registers.  Cells
-// with no earlier assignment inside their column ("head" cells) are listed
-// and resolved from per-column and per-group summaries (k_pocoef_heads).
+// order -- and carries the twelve (face, W/D) values in registers.  For
+// parallelism a column is cut into segments of KSEG cells; segments are
+// contiguous runs of the loop order too.  Cells with no earlier assignment
+// inside their segment ("head" cells) are listed and resolved from
+// per-segment and per-group summaries (k_pocoef_heads).
+constexpr int KSEG = SCF_KSEG;
+
 namespace {
 __device__ __forceinline__ double beta_of(int pc, int pn, double lam, double betap, double betam)
 {
@@ -120,7 +124,10 @@ __global__ void __launch_bounds__(128) k_pocoef(AsmArgs a)
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     if (i > d.I || j > d.J) return;
+    const int nsk = (d.K + KSEG - 1) / KSEG, sk = blockIdx.z;
     const int col = (i - 1) * d.J + (j - 1);   // column index in loop order
+    const int seg = col * nsk + sk;            // segment index in loop order
+    const int kbeg = sk * KSEG + 1, kend = min(kbeg + KSEG - 1, d.K);
     const int sy = d.gx, sz = d.gx * d.gy;
     const int goff[6] = {-1, -sy, -sz, 1, sy, sz};
     double carryW[6], carryD[6];
@@ -132,7 +139,7 @@ __global__ void __launch_bounds__(128) k_pocoef(AsmArgs a)
         memo[f].valid = false; memo[f].dp = memo[f].dg = memo[f].beta = 0ull; memo[f].coef = 0.0;
     }
     const int im = i > 1 ? i - 1 : 1, jm = j > 1 ? j - 1 : 1;
-    for (int k = 1; k <= d.K; ++k) {
+    for (int k = kbeg; k <= kend; ++k) {
         const int gc = gidx(d, i, j, k), nc = nidx(d, i, j, k);
         const int pc = a.phase[gc];
         const int km = k > 1 ? k - 1 : 1;
@@ -184,17 +191,17 @@ __global__ void __launch_bounds__(128) k_pocoef(AsmArgs a)
     }
 #pragma unroll
     for (int f = 0; f < 6; ++f) {
-        a.col_val[(long long)col * 12 + 2 * f] = carryW[f];
-        a.col_val[(long long)col * 12 + 2 * f + 1] = carryD[f];
+        a.col_val[(long long)seg * 12 + 2 * f] = carryW[f];
+        a.col_val[(long long)seg * 12 + 2 * f + 1] = carryD[f];
     }
     unsigned m = 0;
 #pragma unroll
     for (int f = 0; f < 6; ++f) m |= (((maskW >> f) & 1u) << (2 * f)) | (((maskD >> f) & 1u) << (2 * f + 1));
-    a.col_mask[col] = (unsigned short)m;
+    a.col_mask[seg] = (unsigned short)m;
 }
 
 // Group summaries: the last assignment of each (face, W/D) stream within
-// 64 consecutive columns.
+// 64 consecutive segments.
 __global__ void k_pocoef_groups(AsmArgs a, int ncol, int ngrp)
 {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
@@ -217,7 +224,7 @@ __global__ void k_pocoef_groups(AsmArgs a, int ncol, int ngrp)
     a.grp_mask[g] = (unsigned short)m;
 }
 
-// Head cells: the carried value comes from the latest earlier column (first
+// Head cells: the carried value comes from the latest earlier segment (first
 // within the cell's group, then whole groups) that assigned the stream.
 __global__ void k_pocoef_heads(AsmArgs a, unsigned count)
 {
@@ -230,11 +237,13 @@ __global__ void k_pocoef_heads(AsmArgs a, unsigned count)
     const long long L = e >> 4;
     const int col = (int)(L / d.K), k = (int)(L % d.K) + 1;
     const int i = col / d.J + 1, j = col % d.J + 1;
+    const int nsk = (d.K + KSEG - 1) / KSEG;
+    const int seg = col * nsk + (k - 1) / KSEG;
     const unsigned bit = 1u << s;
     double beta = a.stale_init;
     bool found = false;
-    const int g = col / 64;
-    for (int c = col - 1; c >= g * 64; --c)
+    const int g = seg / 64;
+    for (int c = seg - 1; c >= g * 64; --c)
         if (a.col_mask[c] & bit) { beta = a.col_val[(long long)c * 12 + s]; found = true; break; }
     if (!found)
         for (int q = g - 1; q >= 0; --q)
@@ -307,6 +316,7 @@ __global__ void __launch_bounds__(128) k_operator(AsmArgs a, OpArgs o)
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     if (i > d.I || j > d.J) return;
+    const int kbeg = blockIdx.z * KSEG + 1, kend = min(kbeg + KSEG - 1, d.K);
     const int sy = d.gx, sz = d.gx * d.gy;
     const long long N = d.n;
     const int *fl = a.flag;
@@ -322,7 +332,7 @@ __global__ void __launch_bounds__(128) k_operator(AsmArgs a, OpArgs o)
     unsigned long long pdx = 0, pdy = 0, pdz = 0;
     double dydz = 0.0, dxdz = 0.0, dxdy = 0.0, dxdydz = 0.0;
     bool pvalid = false;
-    for (int k = 1; k <= d.K; ++k) {
+    for (int k = kbeg; k <= kend; ++k) {
         const int g = gidx(d, i, j, k), n = nidx(d, i, j, k);
         const int ct = a.ct[n], pos = a.pos[n];
         if ((pos == -1) != (ct == 2) || pos > a.ext_cell || pos < -1) atomicOr(a.flags, FLAG_BAD_POSNU);
@@ -422,7 +432,7 @@ int launch_assemble(const AsmArgs &a, const OpArgs &o, bool mixed, cudaStream_t 
     const Dims &d = a.d;
     cudaMemsetAsync(a.stale_count, 0, sizeof(unsigned), st);
     {
-        dim3 b(32, 4), g((d.I + 31) / 32, (d.J + 3) / 4);
+        dim3 b(32, 4), g((d.I + 31) / 32, (d.J + 3) / 4, (d.K + KSEG - 1) / KSEG);
         k_phase<<<2 * 152 * 8, 256, 0, st>>>(a);
         k_pocoef<<<g, b, 0, st>>>(a);
         *launches += 2;
@@ -432,7 +442,7 @@ int launch_assemble(const AsmArgs &a, const OpArgs &o, bool mixed, cudaStream_t 
     unsigned cnt = *stale_count_host;
     if (cnt > a.stale_cap) cnt = a.stale_cap;
     if (cnt) {
-        const int ncol = d.I * d.J, ngrp = (ncol + 63) / 64;
+        const int ncol = d.I * d.J * ((d.K + KSEG - 1) / KSEG), ngrp = (ncol + 63) / 64;
         k_pocoef_groups<<<(ngrp + 127) / 128, 128, 0, st>>>(a, ncol, ngrp);
         k_pocoef_heads<<<(cnt + 127) / 128, 128, 0, st>>>(a, cnt);
         *launches += 2;
@@ -445,7 +455,7 @@ int launch_assemble(const AsmArgs &a, const OpArgs &o, bool mixed, cudaStream_t 
         k_pocoef_boundary<<<g, 256, 0, st>>>(a);
         *launches += 1;
     }
-    dim3 ob(32, 4), og((d.I + 31) / 32, (d.J + 3) / 4);
+    dim3 ob(32, 4), og((d.I + 31) / 32, (d.J + 3) / 4, (d.K + KSEG - 1) / KSEG);
     if (mixed)
         k_operator<true><<<og, ob, 0, st>>>(a, o);
     else

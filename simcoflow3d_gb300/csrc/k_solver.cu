@@ -65,7 +65,7 @@ void cg_finish_alpha(Reducer &R, int nblocks, cudaStream_t st, int *launches)
 // Fine-level FP64 kernels march KZ cells along k per thread: the k-neighbours
 // stay in registers and the FP64 block reduction (costly on this GPU's FP64
 // pipe) is paid once per KZ cells.
-constexpr int KZ = 8;
+constexpr int KZ = 32;
 
 inline Launch3 launch_zchunk(int n0, int n1, int n2)
 {
@@ -204,83 +204,135 @@ void cg_pupdate(const LevelView<double> &A, const T *z, double *p, const double 
     *launches += 1;
 }
 
-__global__ void __launch_bounds__(256) k_residual(LevelView<double> A, const double *__restrict__ b,
-                                                  const double *__restrict__ x, double *__restrict__ r,
-                                                  double *__restrict__ part)
+// two-slot reduction: sums of part[0..n) and part[n0..n0+n)
+__global__ void __launch_bounds__(1024) k_reduce2(const double *__restrict__ part, int n, int n0,
+                                                  double *scal, int mode)
 {
-    INTERIOR_IJK(A);
-    double v = 0.0;
-    if (in) {
-        const double rr = b[c] - apply_row(A, x, c);
-        r[c] = rr;
-        v = rr * rr;
+    double s = 0.0, t = 0.0;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        s += part[q];
+        t += part[n0 + q];
     }
-    v = block_sum(v);
-    if (thread_linear() == 0) part[block_linear()] = v;
+    s = block_sum(s);
+    __syncthreads();
+    t = block_sum(t);
+    if (threadIdx.x == 0) {
+        if (mode == 0) {           // sum of b, count
+            scal[S_SUM] = s;
+            scal[S_COUNT] = t;
+            scal[S_MEAN] = t > 0.0 ? s / t : 0.0;
+        } else {                   // (r, r), sum of x
+            scal[S_RR] = s;
+            scal[S_MEANX] = scal[S_COUNT] > 0.0 ? t / scal[S_COUNT] : 0.0;
+        }
+    }
 }
 
-void cg_residual(const LevelView<double> &A, const double *b, const double *x, double *r, Reducer &R,
-                 cudaStream_t st, int *launches)
+__global__ void __launch_bounds__(128) k_sum_count(LevelView<double> A, const unsigned char *__restrict__ act,
+                                                   const double *__restrict__ v, double *__restrict__ part, int n0)
 {
-    Launch3 l = launch_interior(A.n0, A.n1, A.n2);
-    k_residual<<<l.grid, l.block, 0, st>>>(A, b, x, r, R.partials);
-    *launches += 1;
-    reduce_to(R, (int)nblocks(l), S_RR, st, launches);
+    ZCHUNK_IJK(A);
+    double s = 0.0, cnt = 0.0;
+    if (in) {
+        int c = i + A.sy * j + A.sz * k0;
+        for (int k = k0; k <= k1; ++k, c += A.sz)
+            if (act[c]) { s += v[c]; cnt += 1.0; }
+    }
+    s = block_sum(s);
+    __syncthreads();
+    cnt = block_sum(cnt);
+    if (thread_linear() == 0) {
+        part[block_linear()] = s;
+        part[n0 + block_linear()] = cnt;
+    }
 }
 
-__global__ void __launch_bounds__(256) k_active_sum(LevelView<double> A, const unsigned char *__restrict__ act,
-                                                    const double *__restrict__ v, double *__restrict__ part)
+__global__ void __launch_bounds__(128) k_center_norm(LevelView<double> A, const unsigned char *__restrict__ act,
+                                                     double *__restrict__ b, const double *__restrict__ scal,
+                                                     int singular, double *__restrict__ part)
 {
-    INTERIOR_IJK(A);
+    ZCHUNK_IJK(A);
     double s = 0.0;
-    if (in && act[c]) s = v ? v[c] : 1.0;
+    if (in) {
+        const double mu = singular ? scal[S_MEAN] : 0.0;
+        int c = i + A.sy * j + A.sz * k0;
+        for (int k = k0; k <= k1; ++k, c += A.sz) {
+            double v = b[c];
+            if (singular && act[c]) { v = v - mu; b[c] = v; }
+            s += v * v;
+        }
+    }
     s = block_sum(s);
     if (thread_linear() == 0) part[block_linear()] = s;
 }
 
-void active_sum(const LevelView<double> &A, const unsigned char *active, const double *v, Reducer &R,
-                cudaStream_t st, int *launches)
+void rhs_prologue(const LevelView<double> &A, const unsigned char *active, double *b, bool singular, Reducer &R,
+                  cudaStream_t st, int *launches)
 {
-    Launch3 l = launch_interior(A.n0, A.n1, A.n2);
-    k_active_sum<<<l.grid, l.block, 0, st>>>(A, active, v, R.partials);
-    if (v)
-        k_reduce<<<1, 1024, 0, st>>>(R.partials, (int)nblocks(l), R.scal, 0, RM_MEAN);
-    else
-        k_reduce<<<1, 1024, 0, st>>>(R.partials, (int)nblocks(l), R.scal, S_COUNT, RM_STORE);
+    Launch3 l = launch_zchunk(A.n0, A.n1, A.n2);
+    const int nb = (int)nblocks(l);
+    if (singular) {
+        k_sum_count<<<l.grid, l.block, 0, st>>>(A, active, b, R.partials, R.max_blocks);
+        k_reduce2<<<1, 1024, 0, st>>>(R.partials, nb, R.max_blocks, R.scal, 0);
+        *launches += 2;
+    }
+    k_center_norm<<<l.grid, l.block, 0, st>>>(A, active, b, R.scal, singular ? 1 : 0, R.partials);
+    k_reduce<<<1, 1024, 0, st>>>(R.partials, nb, R.scal, S_BB, RM_STORE);
     *launches += 2;
 }
 
-__global__ void __launch_bounds__(256) k_subtract_mean(LevelView<double> A, const unsigned char *__restrict__ act,
-                                                       double *__restrict__ v, const double *__restrict__ scal)
+__global__ void __launch_bounds__(128) k_final_residual(LevelView<double> A, const unsigned char *__restrict__ act,
+                                                        const double *__restrict__ b, const double *__restrict__ x,
+                                                        double *__restrict__ r, int singular,
+                                                        double *__restrict__ part, int n0)
 {
-    INTERIOR_IJK(A);
-    if (in && act[c]) v[c] = v[c] - scal[S_MEAN];
-}
-
-void subtract_mean(const LevelView<double> &A, const unsigned char *active, double *v, const double *scal,
-                   cudaStream_t st, int *launches)
-{
-    Launch3 l = launch_interior(A.n0, A.n1, A.n2);
-    k_subtract_mean<<<l.grid, l.block, 0, st>>>(A, active, v, scal);
-    *launches += 1;
-}
-
-__global__ void __launch_bounds__(256) k_dot_self(LevelView<double> A, const double *__restrict__ v,
-                                                  double *__restrict__ part)
-{
-    INTERIOR_IJK(A);
-    double s = 0.0;
-    if (in) s = v[c] * v[c];
+    ZCHUNK_IJK(A);
+    double s = 0.0, sx = 0.0;
+    if (in) {
+        int c = i + A.sy * j + A.sz * k0;
+        for (int k = k0; k <= k1; ++k, c += A.sz) {
+            const double rr = b[c] - apply_row(A, x, c);
+            r[c] = rr;
+            s += rr * rr;
+            if (singular && act[c]) sx += x[c];
+        }
+    }
     s = block_sum(s);
-    if (thread_linear() == 0) part[block_linear()] = s;
+    __syncthreads();
+    sx = block_sum(sx);
+    if (thread_linear() == 0) {
+        part[block_linear()] = s;
+        part[n0 + block_linear()] = sx;
+    }
 }
 
-void dot_self(const LevelView<double> &A, const double *v, Reducer &R, int slot, cudaStream_t st, int *launches)
+void final_residual(const LevelView<double> &A, const unsigned char *active, const double *b, const double *x,
+                    double *r, bool singular, Reducer &R, cudaStream_t st, int *launches)
 {
-    Launch3 l = launch_interior(A.n0, A.n1, A.n2);
-    k_dot_self<<<l.grid, l.block, 0, st>>>(A, v, R.partials);
+    Launch3 l = launch_zchunk(A.n0, A.n1, A.n2);
+    const int nb = (int)nblocks(l);
+    k_final_residual<<<l.grid, l.block, 0, st>>>(A, active, b, x, r, singular ? 1 : 0, R.partials, R.max_blocks);
+    k_reduce2<<<1, 1024, 0, st>>>(R.partials, nb, R.max_blocks, R.scal, 1);
+    *launches += 2;
+}
+
+__global__ void __launch_bounds__(128) k_shift(LevelView<double> A, const unsigned char *__restrict__ act,
+                                               double *__restrict__ x, const double *__restrict__ scal)
+{
+    ZCHUNK_IJK(A);
+    if (!in) return;
+    const double mu = scal[S_MEANX];
+    int c = i + A.sy * j + A.sz * k0;
+    for (int k = k0; k <= k1; ++k, c += A.sz)
+        if (act[c]) x[c] = x[c] - mu;
+}
+
+void shift_solution(const LevelView<double> &A, const unsigned char *active, double *x, const double *scal,
+                    cudaStream_t st, int *launches)
+{
+    Launch3 l = launch_zchunk(A.n0, A.n1, A.n2);
+    k_shift<<<l.grid, l.block, 0, st>>>(A, active, x, scal);
     *launches += 1;
-    reduce_to(R, (int)nblocks(l), slot, st, launches);
 }
 
 __global__ void __launch_bounds__(256) k_copy_low(LevelView<double> A, const double *__restrict__ s,
@@ -466,26 +518,29 @@ void mg_coarsen(const MgLevel<T> &F, MgLevel<T> &C, cudaStream_t st, int *launch
 // pivoting); all-Neumann systems get the rank-one term s*1*1^T on the active
 // cells so that the inverse maps zero-mean vectors to the zero-mean solution.
 template <typename T>
-__global__ void __launch_bounds__(256) k_coarse_inverse(MgLevel<T> L, double *__restrict__ A,
+__global__ void __launch_bounds__(256) k_coarse_inverse(MgLevel<T> L, double *__restrict__ Aout,
                                                         const int *__restrict__ map, int n, int singular)
 {
+    extern __shared__ double A[];      // n*n, in shared memory
     __shared__ double fcol[128];
     __shared__ double red[2];
+    __shared__ int smap[128];
     const int t = threadIdx.x;
     const int nt = blockDim.x;
     for (int e = t; e < n * n; e += nt) A[e] = 0.0;
+    for (int a = t; a < n; a += nt) smap[a] = map[a];
     __syncthreads();
     double dsum = 0.0, cnt = 0.0;
     for (int a = t; a < n; a += nt) {
-        const int c = map[a];
-        A[(size_t)a * n + a] = (double)L.diag[c];
+        const int c = smap[a];
+        A[a * n + a] = (double)L.diag[c];
         if (L.active[c]) { dsum += (double)L.diag[c]; cnt += 1.0; }
         const int nb[6] = {c + 1, c - 1, c + L.sy, c - L.sy, c + L.sz, c - L.sz};
         const T w[6] = {L.cE[c], L.cE[c - 1], L.cN[c], L.cN[c - L.sy], L.cT[c], L.cT[c - L.sz]};
         for (int q = 0; q < 6; ++q) {
             if (w[q] == T(0)) continue;
             for (int b = 0; b < n; ++b)
-                if (map[b] == nb[q]) { A[(size_t)a * n + b] -= (double)w[q]; break; }
+                if (smap[b] == nb[q]) { A[a * n + b] -= (double)w[q]; break; }
         }
     }
     dsum = block_sum(dsum);
@@ -497,16 +552,17 @@ __global__ void __launch_bounds__(256) k_coarse_inverse(MgLevel<T> L, double *__
         const double s = red[0] / red[1] / red[1];
         for (int e = t; e < n * n; e += nt) {
             const int a = e / n, b = e % n;
-            if (L.active[map[a]] && L.active[map[b]]) A[e] += s;
+            if (L.active[smap[a]] && L.active[smap[b]]) A[e] += s;
         }
     }
     __syncthreads();
     for (int kk = 0; kk < n; ++kk) {
-        const double piv = A[(size_t)kk * n + kk];
+        const double piv = A[kk * n + kk];
         const double pinv = piv > 0.0 ? 1.0 / piv : 0.0;
-        for (int a = t; a < n; a += nt) fcol[a] = A[(size_t)a * n + kk];
         __syncthreads();
-        for (int b = t; b < n; b += nt) A[(size_t)kk * n + b] = (b == kk) ? pinv : A[(size_t)kk * n + b] * pinv;
+        for (int a = t; a < n; a += nt) fcol[a] = A[a * n + kk];
+        __syncthreads();
+        for (int b = t; b < n; b += nt) A[kk * n + b] = (b == kk) ? pinv : A[kk * n + b] * pinv;
         __syncthreads();
         for (int e = t; e < n * n; e += nt) {
             const int a = e / n, b = e % n;
@@ -514,17 +570,24 @@ __global__ void __launch_bounds__(256) k_coarse_inverse(MgLevel<T> L, double *__
             if (b == kk)
                 A[e] = -fcol[a] * pinv;
             else
-                A[e] -= fcol[a] * A[(size_t)kk * n + b];
+                A[e] -= fcol[a] * A[kk * n + b];
         }
         __syncthreads();
     }
+    for (int e = t; e < n * n; e += nt) Aout[e] = A[e];
 }
 
 template <typename T>
 void mg_coarse_inverse(const MgLevel<T> &L, double *ainv, int *map, int n, bool singular, cudaStream_t st,
                        int *launches)
 {
-    k_coarse_inverse<T><<<1, 256, 0, st>>>(L, ainv, map, n, singular ? 1 : 0);
+    const size_t smem = (size_t)n * n * sizeof(double);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_coarse_inverse<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 128 * 128 * 8);
+        attr_set = true;
+    }
+    k_coarse_inverse<T><<<1, 256, smem, st>>>(L, ainv, map, n, singular ? 1 : 0);
     *launches += 1;
 }
 

@@ -353,13 +353,8 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
     float *rlow = mixed ? (float *)L[0].b : nullptr;
     const ChebCoef cc = cheb_coef(ctx->opts.smoother_degree);
     auto t0 = std::chrono::steady_clock::now();
-    if (singular) {
-        active_sum(A, ctx->active, nullptr, ctx->R, ctx->st, &ctx->launches);
-        active_sum(A, ctx->active, ctx->b, ctx->R, ctx->st, &ctx->launches);
-        subtract_mean(A, ctx->active, ctx->b, ctx->R.scal, ctx->st, &ctx->launches);
-    }
+    rhs_prologue(A, ctx->active, ctx->b, singular, ctx->R, ctx->st, &ctx->launches);
     build_hierarchy<T>(ctx, L);
-    dot_self(A, ctx->b, ctx->R, S_BB, ctx->st, &ctx->launches);
     const double bb = read_scal(ctx, S_BB);
     const double bn = std::sqrt(bb);
     stats->rhs_norm = bn;
@@ -369,6 +364,7 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
     double rel = 0.0;
     if (!(bn > 0.0)) {
         CK(cudaMemsetAsync(ctx->x, 0, sizeof(double) * ctx->d.ng, ctx->st));
+        CK(cudaMemsetAsync(ctx->R.scal + S_MEANX, 0, sizeof(double), ctx->st));
         stats->iterations = 0;
         stats->rounds = 1;
         stats->rel_residual = 0.0;
@@ -376,11 +372,7 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
         return std::isfinite(bb) ? SCF_OK : SCF_ERR_NONFINITE;
     }
     if (ctx->opts.warm_start && ctx->warm_ok) {
-        cg_residual(A, ctx->b, ctx->x, ctx->r, ctx->R, ctx->st, &ctx->launches);
-        if (singular) {
-            active_sum(A, ctx->active, ctx->r, ctx->R, ctx->st, &ctx->launches);
-            subtract_mean(A, ctx->active, ctx->r, ctx->R.scal, ctx->st, &ctx->launches);
-        }
+        final_residual(A, ctx->active, ctx->b, ctx->x, ctx->r, false, ctx->R, ctx->st, &ctx->launches);
     } else {
         CK(cudaMemsetAsync(ctx->x, 0, sizeof(double) * ctx->d.ng, ctx->st));
         CK(cudaMemcpyAsync(ctx->r, ctx->b, sizeof(double) * ctx->d.ng, cudaMemcpyDeviceToDevice, ctx->st));
@@ -410,21 +402,14 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
             cg_dot_rz<T>(A, ctx->r, (const T *)L[0].b, z, ctx->R, ctx->st, &ctx->launches);
             cg_pupdate<T>(A, z, ctx->p, ctx->R.scal, false, ctx->st, &ctx->launches);
         }
-        // true FP64 residual (the refinement check)
-        if (singular) {
-            active_sum(A, ctx->active, ctx->x, ctx->R, ctx->st, &ctx->launches);
-            subtract_mean(A, ctx->active, ctx->x, ctx->R.scal, ctx->st, &ctx->launches);
-        }
-        cg_residual(A, ctx->b, ctx->x, ctx->r, ctx->R, ctx->st, &ctx->launches);
-        if (singular) {
-            active_sum(A, ctx->active, ctx->r, ctx->R, ctx->st, &ctx->launches);
-            subtract_mean(A, ctx->active, ctx->r, ctx->R.scal, ctx->st, &ctx->launches);
-            dot_self(A, ctx->r, ctx->R, S_RR, ctx->st, &ctx->launches);
-        }
+        // true FP64 residual (the refinement check); for an all-Neumann
+        // system also the mean of x, removed below
+        final_residual(A, ctx->active, ctx->b, ctx->x, ctx->r, singular, ctx->R, ctx->st, &ctx->launches);
         rel = std::sqrt(read_scal(ctx, S_RR)) / bn;
         if (rel <= tol || !conv || its >= ctx->opts.max_iter || restarts >= ctx->opts.max_rounds) break;
         ++restarts;  // recursive residual drifted below the true one: restart from the true residual
     }
+    if (singular) shift_solution(A, ctx->active, ctx->x, ctx->R.scal, ctx->st, &ctx->launches);
     stats->iterations = its;
     stats->rounds = restarts + 1;
     stats->rel_residual = rel;
@@ -678,7 +663,8 @@ int scf_ctx_create(scf_ctx **out, int32_t imax, int32_t jmax, int32_t kmax, cons
     A(ctx->stale_count, 1); A(ctx->flags, 4);
     ctx->stale_cap = (unsigned)(n < (1LL << 30) ? n : (1LL << 30));
     A(ctx->stale_list, ctx->stale_cap);
-    const long long ncol = (long long)imax * jmax, ngrp = (ncol + 63) / 64;
+    // per-segment summaries of the coefficient kernel (segments of 32 cells)
+    const long long ncol = (long long)imax * jmax * ((kmax + SCF_KSEG - 1) / SCF_KSEG), ngrp = (ncol + 63) / 64;
     A(ctx->col_val, 12 * ncol); A(ctx->col_mask, ncol); A(ctx->grp_val, 12 * ngrp); A(ctx->grp_mask, ngrp);
     A(ctx->phase, ng);
     A(ctx->diag, ng); A(ctx->dinv, ng); A(ctx->cE, ng); A(ctx->cN, ng); A(ctx->cT, ng); A(ctx->extra, ng);
@@ -689,7 +675,7 @@ int scf_ctx_create(scf_ctx **out, int32_t imax, int32_t jmax, int32_t kmax, cons
         for (int q = 0; q < 6; ++q) A(ctx->bcvar[f][q], plane_size(d, q));
     Launch3 l = launch_interior(imax, jmax, kmax);
     ctx->R.max_blocks = (int)nblocks(l);
-    A(ctx->R.partials, ctx->R.max_blocks + 1024);
+    A(ctx->R.partials, 2 * ctx->R.max_blocks + 1024);
     A(ctx->R.scal, S_NUM);
 #undef A
     if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) return fail(SCF_ERR_CUDA);

@@ -45,6 +45,7 @@ enum ScfScalar {
     S_COUNT,       // active cell count
     S_MEAN,
     S_RZ_NEW,
+    S_MEANX,       // mean of x over the active cells (all-Neumann systems)
     S_NUM
 };
 

@@ -2,6 +2,9 @@
 #pragma once
 #include "scf_common.cuh"
 
+// Cells per thread segment of the column-marching assembly kernels.
+constexpr int SCF_KSEG = 32;
+
 // Inputs of the assembly (device mirrors of scf_poisson_in) plus scratch.
 struct AsmArgs {
     Dims d;
@@ -100,15 +103,17 @@ template <typename T>
 void cg_pupdate(const LevelView<double> &A, const T *z, double *p, const double *scal, bool first,
                 cudaStream_t st, int *launches);
 void reduce_to(Reducer &R, int nblocks, int slot, cudaStream_t st, int *launches);
-// r = b - A x (active), partial (r,r)
-void cg_residual(const LevelView<double> &A, const double *b, const double *x, double *r, Reducer &R,
-                 cudaStream_t st, int *launches);
-// sum and count over active cells (mean projection)
-void active_sum(const LevelView<double> &A, const unsigned char *active, const double *v, Reducer &R,
-                cudaStream_t st, int *launches);
-void subtract_mean(const LevelView<double> &A, const unsigned char *active, double *v, const double *scal,
-                   cudaStream_t st, int *launches);
-void dot_self(const LevelView<double> &A, const double *v, Reducer &R, int slot, cudaStream_t st, int *launches);
+// Right-hand side prologue: for an all-Neumann system the mean of b over the
+// active cells is removed (S_COUNT, S_MEAN); then S_BB = (b, b).
+void rhs_prologue(const LevelView<double> &A, const unsigned char *active, double *b, bool singular, Reducer &R,
+                  cudaStream_t st, int *launches);
+// r = b - A x, S_RR = (r, r); for an all-Neumann system also S_MEANX = mean
+// of x over the active cells (removed from the scattered pressure).
+void final_residual(const LevelView<double> &A, const unsigned char *active, const double *b, const double *x,
+                    double *r, bool singular, Reducer &R, cudaStream_t st, int *launches);
+// x -= S_MEANX on the active cells
+void shift_solution(const LevelView<double> &A, const unsigned char *active, double *x, const double *scal,
+                    cudaStream_t st, int *launches);
 void copy_to_low(const LevelView<double> &A, const double *src, float *dst, cudaStream_t st, int *launches);
 
 // ---- correction ------------------------------------------------------------
