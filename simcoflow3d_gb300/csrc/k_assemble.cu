@@ -336,11 +336,11 @@ __global__ void __launch_bounds__(128) k_operator(AsmArgs a, OpArgs o)
         const int g = gidx(d, i, j, k), n = nidx(d, i, j, k);
         const int ct = a.ct[n], pos = a.pos[n];
         if ((pos == -1) != (ct == 2) || pos > a.ext_cell || pos < -1) atomicOr(a.flags, FLAG_BAD_POSNU);
-        if (ct == 2) {
-            o.diag[g] = 1.0; o.dinv[g] = 0.0; o.cE[g] = 0.0; o.cN[g] = 0.0; o.cT[g] = 0.0;
+        if (ct == 2) {   // solid: identity-free row, marked by diag = -1 (x stays 0 there)
+            o.diag[g] = -1.0; o.dinv[g] = 0.0; o.cE[g] = 0.0; o.cN[g] = 0.0; o.cT[g] = 0.0;
             o.extra[g] = 0.0; o.b[g] = 0.0; o.active[g] = 0;
             if (MIXED) {
-                o.diag32[g] = 1.0f; o.dinv32[g] = 0.0f; o.cE32[g] = 0.0f; o.cN32[g] = 0.0f; o.cT32[g] = 0.0f;
+                o.diag32[g] = -1.0f; o.dinv32[g] = 0.0f; o.cE32[g] = 0.0f; o.cN32[g] = 0.0f; o.cT32[g] = 0.0f;
                 o.extra32[g] = 0.0f;
             }
             continue;

@@ -20,6 +20,37 @@
     const int c = i + (L).sy * j + (L).sz * k;
 
 // ---------------------------------------------------------------------------
+// Jacobi scaling.  FP32 levels compute 1/diag on the fly (FP32 division is
+// cheap, and it saves one array per pass); FP64 levels read a stored inverse
+// (FP64 division is slow on this GPU).  Inactive cells carry diag = -1 and
+// get no update and no coarse correction.
+template <typename T>
+__device__ __forceinline__ T dinv_at(const LevelView<T> &L, int c);
+template <>
+__device__ __forceinline__ float dinv_at<float>(const LevelView<float> &L, int c)
+{
+    const float d = L.diag[c];
+    return d > 0.0f ? 1.0f / d : 0.0f;
+}
+template <>
+__device__ __forceinline__ double dinv_at<double>(const LevelView<double> &L, int c)
+{
+    return L.dinv[c];
+}
+template <typename T>
+__device__ __forceinline__ bool active_at(const LevelView<T> &L, int c);
+template <>
+__device__ __forceinline__ bool active_at<float>(const LevelView<float> &L, int c)
+{
+    return L.diag[c] > 0.0f;
+}
+template <>
+__device__ __forceinline__ bool active_at<double>(const LevelView<double> &L, int c)
+{
+    return __double_as_longlong(L.dinv[c]) != 0;
+}
+
+// ---------------------------------------------------------------------------
 // reductions
 
 enum ReduceMode { RM_STORE = 0, RM_ALPHA = 1, RM_BETA = 2, RM_MEAN = 3 };
@@ -113,10 +144,15 @@ void cg_spmv_dot(const LevelView<double> &A, const double *p, double *q, Reducer
     cg_finish_alpha(R, (int)nblocks(l), st, launches);
 }
 
+// x += alpha p, r -= alpha q, (r, r); also writes the preconditioner's
+// level-0 rhs (FP32 copy of r in mixed mode) and the first Chebyshev step
+// of the V-cycle from a zero guess, x0 = dinv * r / theta, which saves that
+// pass in the V-cycle.
 template <typename T>
 __global__ void __launch_bounds__(128) k_cg_update(LevelView<double> A, double *__restrict__ x,
                                                    double *__restrict__ r, const double *__restrict__ p,
                                                    const double *__restrict__ q, T *__restrict__ rlow,
+                                                   LevelView<T> L0, T *__restrict__ x0, T first,
                                                    const double *__restrict__ scal, double *__restrict__ part)
 {
     ZCHUNK_IJK(A);
@@ -128,7 +164,9 @@ __global__ void __launch_bounds__(128) k_cg_update(LevelView<double> A, double *
             x[c] = x[c] + alpha * p[c];
             const double rn = r[c] - alpha * q[c];
             r[c] = rn;
-            if (rlow) rlow[c] = (T)rn;
+            const T rl = (T)rn;
+            if (rlow) rlow[c] = rl;
+            if (x0) x0[c] = first * dinv_at(L0, c) * rl;
             v += rn * rn;
         }
     }
@@ -138,10 +176,10 @@ __global__ void __launch_bounds__(128) k_cg_update(LevelView<double> A, double *
 
 template <typename T>
 void cg_update(const LevelView<double> &A, double *x, double *r, const double *p, const double *q, T *rlow,
-               Reducer &R, cudaStream_t st, int *launches)
+               const LevelView<T> &L0, T *x0, double first, Reducer &R, cudaStream_t st, int *launches)
 {
     Launch3 l = launch_zchunk(A.n0, A.n1, A.n2);
-    k_cg_update<T><<<l.grid, l.block, 0, st>>>(A, x, r, p, q, rlow, R.scal, R.partials);
+    k_cg_update<T><<<l.grid, l.block, 0, st>>>(A, x, r, p, q, rlow, L0, x0, (T)first, R.scal, R.partials);
     *launches += 1;
     reduce_to(R, (int)nblocks(l), S_RR, st, launches);
 }
@@ -357,7 +395,7 @@ __global__ void __launch_bounds__(256) k_cheb_first(LevelView<T> L, const T *__r
                                                     T coef)
 {
     INTERIOR_IJK(L);
-    if (in) x[c] = coef * L.dinv[c] * b[c];
+    if (in) x[c] = coef * dinv_at(L, c) * b[c];
 }
 
 template <typename T>
@@ -368,29 +406,42 @@ __global__ void __launch_bounds__(256) k_cheb_step(LevelView<T> L, const T *__re
     INTERIOR_IJK(L);
     if (!in) return;
     const T r = b[c] - apply_row(L, xin, c);
-    const T dn = c1 * dprev[c] + c2 * L.dinv[c] * r;
+    const T dn = c1 * dprev[c] + c2 * dinv_at(L, c) * r;
     xout[c] = xin[c] + dn;
     if (dout) dout[c] = dn;
 }
 
-// residual of the fine level, summed over each coarse cell's children
+// Residual of the fine level summed over each coarse cell's children.  One
+// thread per fine i and coarse (J,K): it sums the residuals of its (up to
+// 2x2) fine cells in j and k, then lanes i and i^1 add their sums with a
+// shuffle (always in the order even + odd), so the result is reproducible.
 template <typename T>
-__global__ void __launch_bounds__(256) k_restrict(LevelView<T> F, const T *__restrict__ b,
+__global__ void __launch_bounds__(128) k_restrict(LevelView<T> F, const T *__restrict__ b,
                                                   const T *__restrict__ x, LevelView<T> C, T *__restrict__ bc,
                                                   int f0, int f1, int f2)
 {
-    INTERIOR_IJK(C);
-    if (!in) return;
-    const int i0 = (i - 1) * f0 + 1, j0 = (j - 1) * f1 + 1, k0 = (k - 1) * f2 + 1;
-    const int i1 = min(i0 + f0 - 1, F.n0), j1 = min(j0 + f1 - 1, F.n1), k1 = min(k0 + f2 - 1, F.n2);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int K = blockIdx.z + 1;
+    const bool in = i <= F.n0 && J <= C.n1;
     T s = T(0);
-    for (int kk = k0; kk <= k1; ++kk)
+    if (in) {
+        const int j0 = (J - 1) * f1 + 1, j1 = min(j0 + f1 - 1, F.n1);
+        const int k0 = (K - 1) * f2 + 1, k1 = min(k0 + f2 - 1, F.n2);
         for (int jj = j0; jj <= j1; ++jj)
-            for (int ii = i0; ii <= i1; ++ii) {
-                const int fc = ii + F.sy * jj + F.sz * kk;
+            for (int kk = k0; kk <= k1; ++kk) {
+                const int fc = i + F.sy * jj + F.sz * kk;
                 s += b[fc] - apply_row(F, x, fc);
             }
-    bc[c] = s;
+    }
+    if (f0 == 2) {
+        const T o = __shfl_xor_sync(0xffffffffu, s, 1);
+        if ((threadIdx.x & 1) == 0) s = s + o;
+        else return;
+    }
+    if (!in) return;
+    const int I = f0 == 2 ? ((i - 1) >> 1) + 1 : i;
+    bc[I + C.sy * J + C.sz * K] = s;
 }
 
 // prolongation (piecewise constant, active cells only) fused with the first
@@ -407,7 +458,7 @@ __global__ void __launch_bounds__(256) k_post_first(LevelView<T> F, const T *__r
     auto xc = [&](int ii, int jj, int kk) -> T {
         const int fc = ii + F.sy * jj + F.sz * kk;
         T v = x[fc];
-        if (F.dinv[fc] != T(0)) {
+        if (active_at(F, fc)) {
             const int I = ((ii - 1) >> s0) + 1, J = ((jj - 1) >> s1) + 1, K = ((kk - 1) >> s2) + 1;
             v += e[I + C.sy * J + C.sz * K];
         }
@@ -417,7 +468,7 @@ __global__ void __launch_bounds__(256) k_post_first(LevelView<T> F, const T *__r
     const T ax = F.diag[c] * x0 - (F.cE[c] * xc(i + 1, j, k) + F.cE[c - 1] * xc(i - 1, j, k) +
                                    F.cN[c] * xc(i, j + 1, k) + F.cN[c - F.sy] * xc(i, j - 1, k) +
                                    F.cT[c] * xc(i, j, k + 1) + F.cT[c - F.sz] * xc(i, j, k - 1));
-    const T dn = coef * F.dinv[c] * (b[c] - ax);
+    const T dn = coef * dinv_at(F, c) * (b[c] - ax);
     xout[c] = x0 + dn;
     if (dout) dout[c] = dn;
 }
@@ -496,7 +547,7 @@ __global__ void __launch_bounds__(256) k_coarsen_diag(MgLevel<T> C)
     if (i > C.n0 || j > C.n1 || k > C.n2) return;
     const int c = i + C.sy * j + C.sz * k;
     if (!C.active[c]) {
-        C.diag[c] = T(1);
+        C.diag[c] = T(-1);
         C.dinv[c] = T(0);
         return;
     }
@@ -593,7 +644,7 @@ void mg_coarse_inverse(const MgLevel<T> &L, double *ainv, int *map, int n, bool 
 
 template <typename T>
 T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, const int *map, int ncoarse,
-             bool singular, cudaStream_t st, int *launches)
+             bool singular, bool first_done, cudaStream_t st, int *launches)
 {
     T *cur[32];
     const int last = nlev - 1;
@@ -602,8 +653,10 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
         LevelView<T> v = F.view();
         Launch3 lf = launch_interior(F.n0, F.n1, F.n2);
         T *xa = F.x, *xb = F.xb;
-        k_cheb_first<T><<<lf.grid, lf.block, 0, st>>>(v, F.b, xa, (T)cc.first);
-        *launches += 1;
+        if (!(l == 0 && first_done)) {
+            k_cheb_first<T><<<lf.grid, lf.block, 0, st>>>(v, F.b, xa, (T)cc.first);
+            *launches += 1;
+        }
         for (int s = 1; s < cc.degree; ++s) {
             const T *dprev = (s == 1) ? xa : F.d;
             k_cheb_step<T><<<lf.grid, lf.block, 0, st>>>(v, F.b, xa, dprev, xb, F.d, (T)cc.c1[s], (T)cc.c2[s]);
@@ -612,8 +665,8 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
         }
         cur[l] = xa;
         MgLevel<T> &C = L[l + 1];
-        Launch3 lc = launch_interior(C.n0, C.n1, C.n2);
-        k_restrict<T><<<lc.grid, lc.block, 0, st>>>(v, F.b, xa, C.view(), C.b, F.f0, F.f1, F.f2);
+        dim3 rg((F.n0 + 31) / 32, (C.n1 + 3) / 4, C.n2), rb(32, 4, 1);
+        k_restrict<T><<<rg, rb, 0, st>>>(v, F.b, xa, C.view(), C.b, F.f0, F.f1, F.f2);
         *launches += 1;
     }
     {
@@ -659,8 +712,8 @@ void probe_smooth(MgLevel<T> &F, const ChebCoef &cc, cudaStream_t st)
 template <typename T>
 void probe_restrict(MgLevel<T> &F, MgLevel<T> &C, cudaStream_t st)
 {
-    Launch3 lc = launch_interior(C.n0, C.n1, C.n2);
-    k_restrict<T><<<lc.grid, lc.block, 0, st>>>(F.view(), F.b, F.x, C.view(), C.b, F.f0, F.f1, F.f2);
+    dim3 rg((F.n0 + 31) / 32, (C.n1 + 3) / 4, C.n2), rb(32, 4, 1);
+    k_restrict<T><<<rg, rb, 0, st>>>(F.view(), F.b, F.x, C.view(), C.b, F.f0, F.f1, F.f2);
 }
 
 template <typename T>
@@ -690,13 +743,13 @@ template void mg_coarsen<double>(const MgLevel<double> &, MgLevel<double> &, cud
 template void mg_coarse_inverse<float>(const MgLevel<float> &, double *, int *, int, bool, cudaStream_t, int *);
 template void mg_coarse_inverse<double>(const MgLevel<double> &, double *, int *, int, bool, cudaStream_t, int *);
 template float *mg_vcycle<float>(MgLevel<float> *, int, const ChebCoef &, const double *, const int *, int, bool,
-                                 cudaStream_t, int *);
+                                 bool, cudaStream_t, int *);
 template double *mg_vcycle<double>(MgLevel<double> *, int, const ChebCoef &, const double *, const int *, int, bool,
-                                   cudaStream_t, int *);
+                                   bool, cudaStream_t, int *);
 template void cg_update<float>(const LevelView<double> &, double *, double *, const double *, const double *, float *,
-                               Reducer &, cudaStream_t, int *);
+                               const LevelView<float> &, float *, double, Reducer &, cudaStream_t, int *);
 template void cg_update<double>(const LevelView<double> &, double *, double *, const double *, const double *,
-                                double *, Reducer &, cudaStream_t, int *);
+                                double *, const LevelView<double> &, double *, double, Reducer &, cudaStream_t, int *);
 template void cg_dot_rz<float>(const LevelView<double> &, const double *, const float *, const float *, Reducer &,
                                cudaStream_t, int *);
 template void cg_dot_rz<double>(const LevelView<double> &, const double *, const double *, const double *,

@@ -338,10 +338,10 @@ double read_scal(scf_ctx *ctx, int slot)
 }
 
 template <typename T>
-T *precondition(scf_ctx *ctx, MgLevel<T> *L, const ChebCoef &cc)
+T *precondition(scf_ctx *ctx, MgLevel<T> *L, const ChebCoef &cc, bool first_done)
 {
-    return mg_vcycle<T>(L, ctx->nlev, cc, ctx->ainv, ctx->map, ctx->ncoarse, is_singular(ctx), ctx->st,
-                        &ctx->launches);
+    return mg_vcycle<T>(L, ctx->nlev, cc, ctx->ainv, ctx->map, ctx->ncoarse, is_singular(ctx), first_done,
+                        ctx->st, &ctx->launches);
 }
 
 template <typename T>
@@ -381,14 +381,18 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
     int restarts = 0;
     for (;;) {
         if (mixed) copy_to_low(A, ctx->r, rlow, ctx->st, &ctx->launches);
-        T *z = precondition<T>(ctx, L, cc);
+        T *z = precondition<T>(ctx, L, cc, false);
         cg_dot_rz<T>(A, ctx->r, (const T *)L[0].b, z, ctx->R, ctx->st, &ctx->launches);
         cg_pupdate<T>(A, z, ctx->p, ctx->R.scal, true, ctx->st, &ctx->launches);
         bool conv = false;
         while (its < ctx->opts.max_iter) {
             ++its;
             cg_spmv_dot(A, ctx->p, ctx->q, ctx->R, S_PQ, ctx->st, &ctx->launches);
-            cg_update<float>(A, ctx->x, ctx->r, ctx->p, ctx->q, rlow, ctx->R, ctx->st, &ctx->launches);
+            // the update also writes level 0's first smoothing step when the
+            // hierarchy has more than one level
+            const bool fuse = ctx->nlev > 1;
+            cg_update<T>(A, ctx->x, ctx->r, ctx->p, ctx->q, (T *)(mixed ? (void *)rlow : nullptr), L[0].view(),
+                         fuse ? L[0].x : nullptr, cc.first, ctx->R, ctx->st, &ctx->launches);
             const double rr = read_scal(ctx, S_RR);
             if (!std::isfinite(rr)) {
                 set_err(ctx, "CG residual became non-finite at iteration %d", its);
@@ -398,7 +402,7 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
             if (std::sqrt(rr) <= tol * bn) { conv = true; break; }
             const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
             if (el > ctx->opts.time_limit_s) break;
-            z = precondition<T>(ctx, L, cc);
+            z = precondition<T>(ctx, L, cc, ctx->nlev > 1);
             cg_dot_rz<T>(A, ctx->r, (const T *)L[0].b, z, ctx->R, ctx->st, &ctx->launches);
             cg_pupdate<T>(A, z, ctx->p, ctx->R.scal, false, ctx->st, &ctx->launches);
         }
@@ -875,17 +879,22 @@ int scf_debug_time_kernel(scf_ctx *ctx, int kernel, int reps, double *ms_per_lau
             break;
         default: {
             int dummy = 0;
-            cg_update<float>(fine_view(ctx), ctx->x, ctx->r, ctx->p, ctx->q, mixed ? (float *)ctx->L32[0].b : nullptr,
-                             ctx->R, ctx->st, &dummy);
+            if (mixed)
+                cg_update<float>(fine_view(ctx), ctx->x, ctx->r, ctx->p, ctx->q, ctx->L32[0].b, ctx->L32[0].view(),
+                                 ctx->L32[0].x, cc.first, ctx->R, ctx->st, &dummy);
+            else
+                cg_update<double>(fine_view(ctx), ctx->x, ctx->r, ctx->p, ctx->q, nullptr, ctx->L64[0].view(),
+                                  ctx->L64[0].x, cc.first, ctx->R, ctx->st, &dummy);
         }
         }
     };
     double bytes;
     switch (kernel) {
-    case SCF_K_SMOOTH: bytes = 10.0 * s * n; break;                 // b,x,d,diag,dinv,cE,cN,cT in; x,d out
-    case SCF_K_SPMV: bytes = 6.0 * 8.0 * n; break;                  // p,diag,cE,cN,cT in; q out
-    case SCF_K_RESTRICT: bytes = 6.0 * s * n + s * n / 8.0; break;  // b,x,diag,cE,cN,cT in; coarse b out
-    case SCF_K_PROLONG: bytes = 9.0 * s * n + s * n / 8.0; break;   // b,x,diag,dinv,cE,cN,cT,e in; x,d out
+    // each array counted once per cell; FP32 levels derive 1/diag, FP64 read dinv
+    case SCF_K_SMOOTH: bytes = (mixed ? 9.0 : 10.0) * s * n; break;  // b,x,d,diag,[dinv],cE,cN,cT in; x,d out
+    case SCF_K_SPMV: bytes = 6.0 * 8.0 * n; break;                   // p,diag,cE,cN,cT in; q out
+    case SCF_K_RESTRICT: bytes = 6.0 * s * n + s * n / 8.0; break;   // b,x,diag,cE,cN,cT in; coarse b out
+    case SCF_K_PROLONG: bytes = (mixed ? 8.0 : 9.0) * s * n + s * n / 8.0; break;  // + coarse e; x,d out
     case SCF_K_CGUPDATE: bytes = (6.0 * 8.0 + (mixed ? 4.0 : 0.0)) * n; break;
     default: return SCF_ERR_BAD_ARG;
     }

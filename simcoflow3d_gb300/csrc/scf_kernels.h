@@ -76,9 +76,11 @@ template <typename T>
 void mg_coarse_inverse(const MgLevel<T> &L, double *ainv, int *map, int n, bool singular, cudaStream_t st,
                        int *launches);
 // One V-cycle: level 0 rhs in L[0].b, result in *z (== L[0].x or L[0].xb).
+// first_done: level 0's first Chebyshev step was already written to L[0].x
+// (fused into the CG update).
 template <typename T>
 T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, const int *map, int ncoarse,
-             bool singular, cudaStream_t st, int *launches);
+             bool singular, bool first_done, cudaStream_t st, int *launches);
 
 // Single launches of the fine-level kernels, for timing.
 template <typename T>
@@ -95,7 +97,7 @@ void cg_spmv_dot(const LevelView<double> &A, const double *p, double *q, Reducer
 void cg_finish_alpha(Reducer &R, int nblocks, cudaStream_t st, int *launches);
 template <typename T>
 void cg_update(const LevelView<double> &A, double *x, double *r, const double *p, const double *q, T *rlow,
-               Reducer &R, cudaStream_t st, int *launches);
+               const LevelView<T> &L0, T *x0, double first, Reducer &R, cudaStream_t st, int *launches);
 template <typename T>
 void cg_dot_rz(const LevelView<double> &A, const double *r, const T *rlow, const T *z, Reducer &R, cudaStream_t st,
                int *launches);
