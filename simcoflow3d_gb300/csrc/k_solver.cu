@@ -30,7 +30,7 @@ template <>
 __device__ __forceinline__ float dinv_at<float>(const LevelView<float> &L, int c)
 {
     const float d = L.diag[c];
-    return d > 0.0f ? 1.0f / d : 0.0f;
+    return d > 0.0f ? __frcp_rn(d) : 0.0f;
 }
 template <>
 __device__ __forceinline__ double dinv_at<double>(const LevelView<double> &L, int c)
