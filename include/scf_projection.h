@@ -203,6 +203,26 @@ int scf_run_projection(scf_ctx *ctx, scf_stats *stats);
 int scf_fetch_outputs(scf_ctx *ctx, double *u, double *v, double *w,
                       double *p, double *pocoef, double *pp, scf_bc_out *bc);
 
+/* ---- loss and adjoint gradient ---------------------------------------------
+ * For the differentiable harness (no counterpart call in the reference; the
+ * loss restates PrintDragLiftCoef's pressure force, Solver.f90:684-706).
+ *   J[0] = sum_c g_c p_c   (g interior, e.g. -nz*WlLh on cut cells)
+ *   J[1] = 1/2 sum over active cells of (D u)^2, u the corrected velocity of
+ *          ComputePUVW.f90:181-232 before the boundary routines, D the
+ *          divergence of SetPoissonVectors (ProjectionP.f90:521-526).
+ * rho_cell: optional ghosted per-cell density field; face coefficients then
+ * use the GFM face density lam*rho_a + (1-lam)*rho_b (ProjectionP.f90:155-
+ * 235 with per-cell densities; identical to the reference, up to rounding,
+ * when rho is each cell's phase density).  NULL: the reference's two
+ * densities.  All-Neumann pressure boundaries only.
+ * scf_loss_backward returns dJ/du*, dJ/dv*, dJ/dw* (ghosted, indexed like
+ * the u*, v*, w* arrays) and dJ/drho (ghosted) of J[0] + J[1], by one
+ * adjoint solve with the same operator.  Any output may be NULL.           */
+int scf_loss_forward(scf_ctx *ctx, const scf_poisson_in *in, const scf_correct_in *corr,
+                     const double *rho_cell, const double *g, double *J, scf_stats *stats);
+int scf_loss_backward(scf_ctx *ctx, double *grad_u, double *grad_v, double *grad_w,
+                      double *grad_rho, scf_stats *stats);
+
 /* ---- diagnostics used by the parity tests ----------------------------------
  * All act on the operator of the last staged inputs (assembled on demand). */
 /* y = A x on active cells, with the FP64 operator as stored on the device;

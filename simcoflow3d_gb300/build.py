@@ -26,6 +26,7 @@ UNITS = {
     "k_solver.cu": [],
     "scf_api.cu": [],
     "k_noalloc.cu": [],
+    "k_adjoint.cu": [],
 }
 
 

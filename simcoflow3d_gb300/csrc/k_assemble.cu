@@ -426,19 +426,24 @@ __global__ void __launch_bounds__(128) k_operator(AsmArgs a, OpArgs o)
 
 // ---------------------------------------------------------------------------
 // host launchers
-int launch_assemble(const AsmArgs &a, const OpArgs &o, bool mixed, cudaStream_t st, unsigned *stale_count_host,
-                    int *launches)
+int launch_assemble(const AsmArgs &a, const OpArgs &o, bool mixed, const double *rho, double rho_ref,
+                    cudaStream_t st, unsigned *stale_count_host, int *launches)
 {
     const Dims &d = a.d;
     cudaMemsetAsync(a.stale_count, 0, sizeof(unsigned), st);
-    {
+    if (rho) {
+        k_phase<<<2 * 152 * 8, 256, 0, st>>>(a);
+        launch_pocoef_rho(a, rho, rho_ref, st, launches);
+        *launches += 1;
+        *stale_count_host = 0;
+    } else {
         dim3 b(32, 4), g((d.I + 31) / 32, (d.J + 3) / 4, (d.K + KSEG - 1) / KSEG);
         k_phase<<<2 * 152 * 8, 256, 0, st>>>(a);
         k_pocoef<<<g, b, 0, st>>>(a);
         *launches += 2;
+        cudaMemcpyAsync(stale_count_host, a.stale_count, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+        cudaStreamSynchronize(st);
     }
-    cudaMemcpyAsync(stale_count_host, a.stale_count, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
-    cudaStreamSynchronize(st);
     unsigned cnt = *stale_count_host;
     if (cnt > a.stale_cap) cnt = a.stale_cap;
     if (cnt) {

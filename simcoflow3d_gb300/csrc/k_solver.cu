@@ -53,7 +53,7 @@ __device__ __forceinline__ bool active_at<double>(const LevelView<double> &L, in
 // ---------------------------------------------------------------------------
 // reductions
 
-enum ReduceMode { RM_STORE = 0, RM_ALPHA = 1, RM_BETA = 2, RM_MEAN = 3 };
+enum ReduceMode { RM_STORE = 0, RM_BETA = 2, RM_MEAN = 3 };
 
 __global__ void __launch_bounds__(1024) k_reduce(const double *__restrict__ part, int n, double *scal, int slot,
                                                  int mode)
@@ -62,10 +62,7 @@ __global__ void __launch_bounds__(1024) k_reduce(const double *__restrict__ part
     for (int t = threadIdx.x; t < n; t += blockDim.x) s += part[t];
     s = block_sum(s);
     if (threadIdx.x == 0) {
-        if (mode == RM_ALPHA) {
-            scal[S_PQ] = s;
-            scal[S_ALPHA] = s != 0.0 ? scal[S_RZ] / s : 0.0;
-        } else if (mode == RM_BETA) {
+        if (mode == RM_BETA) {
             const double old = scal[S_RZ];
             scal[S_BETA] = old != 0.0 ? s / old : 0.0;
             scal[S_RZ] = s;
@@ -81,12 +78,6 @@ __global__ void __launch_bounds__(1024) k_reduce(const double *__restrict__ part
 void reduce_to(Reducer &R, int nblocks, int slot, cudaStream_t st, int *launches)
 {
     k_reduce<<<1, 1024, 0, st>>>(R.partials, nblocks, R.scal, slot, RM_STORE);
-    *launches += 1;
-}
-
-void cg_finish_alpha(Reducer &R, int nblocks, cudaStream_t st, int *launches)
-{
-    k_reduce<<<1, 1024, 0, st>>>(R.partials, nblocks, R.scal, 0, RM_ALPHA);
     *launches += 1;
 }
 
@@ -113,11 +104,13 @@ inline Launch3 launch_zchunk(int n0, int n1, int n2)
     const int k1 = min(k0 + KZ - 1, (L).n2);                          \
     const bool in = i <= (L).n0 && j <= (L).n1;
 
+// q = A p and the block partials of (p, q) and of the sum of q (q is zero on
+// inactive cells, whose p is zero and which couple to nothing).
 __global__ void __launch_bounds__(128) k_spmv_dot(LevelView<double> A, const double *__restrict__ p,
-                                                  double *__restrict__ q, double *__restrict__ part)
+                                                  double *__restrict__ q, double *__restrict__ part, int n0)
 {
     ZCHUNK_IJK(A);
-    double v = 0.0;
+    double v = 0.0, sq = 0.0;
     if (in) {
         int c = i + A.sy * j + A.sz * k0;
         double xm = p[c - A.sz], x0 = p[c], tb = A.cT[c - A.sz];
@@ -127,24 +120,53 @@ __global__ void __launch_bounds__(128) k_spmv_dot(LevelView<double> A, const dou
                                                A.cN[c - A.sy] * p[c - A.sy] + tt * xp + tb * xm);
             q[c] = y;
             v += x0 * y;
+            sq += y;
             xm = x0; x0 = xp; tb = tt;
         }
     }
     v = block_sum(v);
-    if (thread_linear() == 0) part[block_linear()] = v;
+    __syncthreads();
+    sq = block_sum(sq);
+    if (thread_linear() == 0) {
+        part[block_linear()] = v;
+        part[n0 + block_linear()] = sq;
+    }
 }
 
-void cg_spmv_dot(const LevelView<double> &A, const double *p, double *q, Reducer &R, int slot_out,
+// alpha = (r, z) / (p, q); for an all-Neumann system also the mean of q over
+// the active cells.  That mean is zero in exact arithmetic (the constant is
+// the null vector of the symmetric operator); the CG update subtracts the
+// rounding that it carries, so that the recursive residual stays in the
+// range of the operator instead of collecting a component that no iterate
+// can remove.
+__global__ void __launch_bounds__(1024) k_reduce_alpha(const double *__restrict__ part, int n, int n0,
+                                                       double *scal, int singular)
+{
+    double s = 0.0, t = 0.0;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        s += part[q];
+        t += part[n0 + q];
+    }
+    s = block_sum(s);
+    __syncthreads();
+    t = block_sum(t);
+    if (threadIdx.x == 0) {
+        scal[S_PQ] = s;
+        scal[S_ALPHA] = s != 0.0 ? scal[S_RZ] / s : 0.0;
+        scal[S_QMEAN] = (singular && scal[S_COUNT] > 0.0) ? t / scal[S_COUNT] : 0.0;
+    }
+}
+
+void cg_spmv_dot(const LevelView<double> &A, const double *p, double *q, Reducer &R, bool singular,
                  cudaStream_t st, int *launches)
 {
-    (void)slot_out;
     Launch3 l = launch_zchunk(A.n0, A.n1, A.n2);
-    k_spmv_dot<<<l.grid, l.block, 0, st>>>(A, p, q, R.partials);
-    *launches += 1;
-    cg_finish_alpha(R, (int)nblocks(l), st, launches);
+    k_spmv_dot<<<l.grid, l.block, 0, st>>>(A, p, q, R.partials, R.max_blocks);
+    k_reduce_alpha<<<1, 1024, 0, st>>>(R.partials, (int)nblocks(l), R.max_blocks, R.scal, singular ? 1 : 0);
+    *launches += 2;
 }
 
-// x += alpha p, r -= alpha q, (r, r); also writes the preconditioner's
+// x += alpha p, r -= alpha (q - mean q), (r, r); also writes the preconditioner's
 // level-0 rhs (FP32 copy of r in mixed mode) and the first Chebyshev step
 // of the V-cycle from a zero guess, x0 = dinv * r / theta, which saves that
 // pass in the V-cycle.
@@ -158,11 +180,11 @@ __global__ void __launch_bounds__(128) k_cg_update(LevelView<double> A, double *
     ZCHUNK_IJK(A);
     double v = 0.0;
     if (in) {
-        const double alpha = scal[S_ALPHA];
+        const double alpha = scal[S_ALPHA], qm = scal[S_QMEAN];
         int c = i + A.sy * j + A.sz * k0;
         for (int k = k0; k <= k1; ++k, c += A.sz) {
             x[c] = x[c] + alpha * p[c];
-            const double rn = r[c] - alpha * q[c];
+            const double rn = r[c] - alpha * (q[c] - (active_at(L0, c) ? qm : 0.0));
             r[c] = rn;
             const T rl = (T)rn;
             if (rlow) rlow[c] = rl;
@@ -184,61 +206,103 @@ void cg_update(const LevelView<double> &A, double *x, double *r, const double *p
     reduce_to(R, (int)nblocks(l), S_RR, st, launches);
 }
 
-// (r, z): in mixed mode r is taken from its FP32 copy (the V-cycle's rhs) and
-// the products are formed in FP32, accumulated per thread in FP32 over KZ
-// cells and across threads in FP64; z is an FP32 preconditioner output, so
-// this loses nothing that matters for beta.  FP64 mode: FP64 throughout.
+// (r, z) and the sum of z: in mixed mode r is taken from its FP32 copy (the
+// V-cycle's rhs) and the products are formed in FP32, accumulated per thread
+// in FP32 over KZ cells and across threads in FP64; z is an FP32
+// preconditioner output, so this loses nothing that matters for beta.  FP64
+// mode: FP64 throughout.  The sum of z is FP64 in both (z is zero on
+// inactive cells).
 template <typename T>
 __global__ void __launch_bounds__(128) k_dot_rz(LevelView<double> A, const double *__restrict__ r,
                                                 const T *__restrict__ rlow, const T *__restrict__ z,
-                                                double *__restrict__ part)
+                                                double *__restrict__ part, int n0)
 {
     ZCHUNK_IJK(A);
-    double v = 0.0;
+    double v = 0.0, sz = 0.0;
     if (in) {
         int c = i + A.sy * j + A.sz * k0;
         if (sizeof(T) == 4) {
             float acc = 0.f;
-            for (int k = k0; k <= k1; ++k, c += A.sz) acc += (float)rlow[c] * (float)z[c];
+            for (int k = k0; k <= k1; ++k, c += A.sz) {
+                const float zz = (float)z[c];
+                acc += (float)rlow[c] * zz;
+                sz += (double)zz;
+            }
             v = (double)acc;
         } else {
-            for (int k = k0; k <= k1; ++k, c += A.sz) v += r[c] * (double)z[c];
+            for (int k = k0; k <= k1; ++k, c += A.sz) {
+                const double zz = (double)z[c];
+                v += r[c] * zz;
+                sz += zz;
+            }
         }
     }
     v = block_sum(v);
-    if (thread_linear() == 0) part[block_linear()] = v;
+    __syncthreads();
+    sz = block_sum(sz);
+    if (thread_linear() == 0) {
+        part[block_linear()] = v;
+        part[n0 + block_linear()] = sz;
+    }
+}
+
+// beta = (r, z) / (r, z)_previous; for an all-Neumann system also the mean of
+// z over the active cells, which the search-direction update removes: the
+// V-cycle's rounding leaves a constant (null-vector) part in z, and once the
+// residual nears the rounding floor that part dominates p, (p, A p) collapses
+// and alpha explodes.  Removing it keeps p in the range of the operator.
+__global__ void __launch_bounds__(1024) k_reduce_beta(const double *__restrict__ part, int n, int n0, double *scal,
+                                                      int singular)
+{
+    double s = 0.0, t = 0.0;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        s += part[q];
+        t += part[n0 + q];
+    }
+    s = block_sum(s);
+    __syncthreads();
+    t = block_sum(t);
+    if (threadIdx.x == 0) {
+        const double old = scal[S_RZ];
+        scal[S_BETA] = old != 0.0 ? s / old : 0.0;
+        scal[S_RZ] = s;
+        scal[S_ZMEAN] = (singular && scal[S_COUNT] > 0.0) ? t / scal[S_COUNT] : 0.0;
+    }
 }
 
 template <typename T>
-void cg_dot_rz(const LevelView<double> &A, const double *r, const T *rlow, const T *z, Reducer &R, cudaStream_t st,
-               int *launches)
+void cg_dot_rz(const LevelView<double> &A, const double *r, const T *rlow, const T *z, bool singular, Reducer &R,
+               cudaStream_t st, int *launches)
 {
     Launch3 l = launch_zchunk(A.n0, A.n1, A.n2);
-    k_dot_rz<T><<<l.grid, l.block, 0, st>>>(A, r, rlow, z, R.partials);
-    k_reduce<<<1, 1024, 0, st>>>(R.partials, (int)nblocks(l), R.scal, 0, RM_BETA);
+    k_dot_rz<T><<<l.grid, l.block, 0, st>>>(A, r, rlow, z, R.partials, R.max_blocks);
+    k_reduce_beta<<<1, 1024, 0, st>>>(R.partials, (int)nblocks(l), R.max_blocks, R.scal, singular ? 1 : 0);
     *launches += 2;
 }
 
+// p = (z - mean z) + beta p on the active cells
 template <typename T>
 __global__ void __launch_bounds__(128) k_pupdate(LevelView<double> A, const T *__restrict__ z,
-                                                 double *__restrict__ p, const double *__restrict__ scal, int first)
+                                                 const unsigned char *__restrict__ act, double *__restrict__ p,
+                                                 const double *__restrict__ scal, int first)
 {
     ZCHUNK_IJK(A);
     if (!in) return;
     const double beta = first ? 0.0 : scal[S_BETA];
+    const double zm = scal[S_ZMEAN];
     int c = i + A.sy * j + A.sz * k0;
     for (int k = k0; k <= k1; ++k, c += A.sz) {
-        const double zz = (double)z[c];
+        const double zz = (double)z[c] - ((zm != 0.0 && act[c]) ? zm : 0.0);
         p[c] = first ? zz : zz + beta * p[c];
     }
 }
 
 template <typename T>
-void cg_pupdate(const LevelView<double> &A, const T *z, double *p, const double *scal, bool first, cudaStream_t st,
-                int *launches)
+void cg_pupdate(const LevelView<double> &A, const T *z, const unsigned char *act, double *p, const double *scal,
+                bool first, cudaStream_t st, int *launches)
 {
     Launch3 l = launch_zchunk(A.n0, A.n1, A.n2);
-    k_pupdate<T><<<l.grid, l.block, 0, st>>>(A, z, p, scal, first ? 1 : 0);
+    k_pupdate<T><<<l.grid, l.block, 0, st>>>(A, z, act, p, scal, first ? 1 : 0);
     *launches += 1;
 }
 
@@ -259,9 +323,12 @@ __global__ void __launch_bounds__(1024) k_reduce2(const double *__restrict__ par
             scal[S_SUM] = s;
             scal[S_COUNT] = t;
             scal[S_MEAN] = t > 0.0 ? s / t : 0.0;
-        } else {                   // (r, r), sum of x
+        } else if (mode == 1) {    // (r, r), sum of x
             scal[S_RR] = s;
             scal[S_MEANX] = scal[S_COUNT] > 0.0 ? t / scal[S_COUNT] : 0.0;
+        } else {                   // loss terms
+            scal[S_JP] = s;
+            scal[S_JD] = t;
         }
     }
 }
@@ -302,6 +369,21 @@ __global__ void __launch_bounds__(128) k_center_norm(LevelView<double> A, const 
     }
     s = block_sum(s);
     if (thread_linear() == 0) part[block_linear()] = s;
+}
+
+void reduce2_to(Reducer &R, int nblocks, int mode, cudaStream_t st, int *launches)
+{
+    k_reduce2<<<1, 1024, 0, st>>>(R.partials, nblocks, R.max_blocks, R.scal, mode);
+    *launches += 1;
+}
+
+void active_mean(const LevelView<double> &A, const unsigned char *active, const double *v, Reducer &R,
+                 cudaStream_t st, int *launches)
+{
+    Launch3 l = launch_zchunk(A.n0, A.n1, A.n2);
+    k_sum_count<<<l.grid, l.block, 0, st>>>(A, active, v, R.partials, R.max_blocks);
+    *launches += 1;
+    reduce2_to(R, (int)nblocks(l), 0, st, launches);
 }
 
 void rhs_prologue(const LevelView<double> &A, const unsigned char *active, double *b, bool singular, Reducer &R,
@@ -727,7 +809,7 @@ void probe_prolong(MgLevel<T> &F, MgLevel<T> &C, const ChebCoef &cc, cudaStream_
 void probe_spmv(const LevelView<double> &A, const double *p, double *q, Reducer &R, cudaStream_t st)
 {
     Launch3 l = launch_zchunk(A.n0, A.n1, A.n2);
-    k_spmv_dot<<<l.grid, l.block, 0, st>>>(A, p, q, R.partials);
+    k_spmv_dot<<<l.grid, l.block, 0, st>>>(A, p, q, R.partials, R.max_blocks);
 }
 
 template void probe_smooth<float>(MgLevel<float> &, const ChebCoef &, cudaStream_t);
@@ -750,11 +832,11 @@ template void cg_update<float>(const LevelView<double> &, double *, double *, co
                                const LevelView<float> &, float *, double, Reducer &, cudaStream_t, int *);
 template void cg_update<double>(const LevelView<double> &, double *, double *, const double *, const double *,
                                 double *, const LevelView<double> &, double *, double, Reducer &, cudaStream_t, int *);
-template void cg_dot_rz<float>(const LevelView<double> &, const double *, const float *, const float *, Reducer &,
-                               cudaStream_t, int *);
-template void cg_dot_rz<double>(const LevelView<double> &, const double *, const double *, const double *,
+template void cg_dot_rz<float>(const LevelView<double> &, const double *, const float *, const float *, bool,
+                               Reducer &, cudaStream_t, int *);
+template void cg_dot_rz<double>(const LevelView<double> &, const double *, const double *, const double *, bool,
                                 Reducer &, cudaStream_t, int *);
-template void cg_pupdate<float>(const LevelView<double> &, const float *, double *, const double *, bool,
-                                cudaStream_t, int *);
-template void cg_pupdate<double>(const LevelView<double> &, const double *, double *, const double *, bool,
-                                 cudaStream_t, int *);
+template void cg_pupdate<float>(const LevelView<double> &, const float *, const unsigned char *, double *,
+                                const double *, bool, cudaStream_t, int *);
+template void cg_pupdate<double>(const LevelView<double> &, const double *, const unsigned char *, double *,
+                                 const double *, bool, cudaStream_t, int *);

@@ -63,6 +63,7 @@ struct scf_ctx {
     float *diag32, *dinv32, *cE32, *cN32, *cT32, *extra32;
     // CG vectors
     double *x, *r, *p, *q;
+    double *xbest;             // best round-end iterate of a solve that restarts
     // multigrid
     int nlev = 0;
     int mg_precision = -1;
@@ -80,6 +81,13 @@ struct scf_ctx {
     unsigned *h_u32 = nullptr;
     cudaEvent_t ev[8];
     int launches = 0;
+    // loss and adjoint (allocated on first use)
+    DevBuf adjmem;
+    double *adj_rho = nullptr, *adj_g = nullptr, *adj_r = nullptr, *adj_pfwd = nullptr;
+    double *adj_gu = nullptr, *adj_gv = nullptr, *adj_gw = nullptr, *adj_grho = nullptr;
+    bool use_rho = false;          // assemble with per-cell densities
+    bool have_loss = false;        // a loss forward has run on the current state
+    bool rho_given_last = false;   // the last loss forward used a density field
 };
 
 namespace {
@@ -295,7 +303,9 @@ int assemble(scf_ctx *ctx)
     const bool mixed = ctx->opts.precision == SCF_PREC_MIXED;
     o.diag32 = ctx->diag32; o.dinv32 = ctx->dinv32; o.cE32 = ctx->cE32; o.cN32 = ctx->cN32; o.cT32 = ctx->cT32;
     o.extra32 = ctx->extra32;
-    int e = launch_assemble(a, o, mixed, ctx->st, ctx->h_u32, &ctx->launches);
+    const double rho_ref = ctx->opts.rho_ref > 0.0 ? ctx->opts.rho_ref : ctx->opts.rho_l;
+    int e = launch_assemble(a, o, mixed, ctx->use_rho ? ctx->adj_rho : nullptr, rho_ref, ctx->st, ctx->h_u32,
+                            &ctx->launches);
     if (e) { set_err(ctx, "assembly launch: %s", cudaGetErrorString((cudaError_t)e)); return SCF_ERR_CUDA; }
     rc = check_flags(ctx);
     if (rc) return rc;
@@ -344,6 +354,10 @@ T *precondition(scf_ctx *ctx, MgLevel<T> *L, const ChebCoef &cc, bool first_done
                         ctx->st, &ctx->launches);
 }
 
+// Iterations without a new smallest CG residual after which a round of the
+// solve ends (the tolerance is below what FP64 can reach for the system).
+constexpr int kStallWindow = 50;
+
 template <typename T>
 int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
 {
@@ -379,15 +393,20 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
     }
     const double tol = ctx->opts.rel_tol;
     int restarts = 0;
+    bool stalled = false, have_best = false;
+    double best_rel = HUGE_VAL;
     for (;;) {
         if (mixed) copy_to_low(A, ctx->r, rlow, ctx->st, &ctx->launches);
         T *z = precondition<T>(ctx, L, cc, false);
-        cg_dot_rz<T>(A, ctx->r, (const T *)L[0].b, z, ctx->R, ctx->st, &ctx->launches);
-        cg_pupdate<T>(A, z, ctx->p, ctx->R.scal, true, ctx->st, &ctx->launches);
+        cg_dot_rz<T>(A, ctx->r, (const T *)L[0].b, z, singular, ctx->R, ctx->st, &ctx->launches);
+        cg_pupdate<T>(A, z, ctx->active, ctx->p, ctx->R.scal, true, ctx->st, &ctx->launches);
         bool conv = false;
+        stalled = false;
+        double best = HUGE_VAL;
+        int best_it = its;
         while (its < ctx->opts.max_iter) {
             ++its;
-            cg_spmv_dot(A, ctx->p, ctx->q, ctx->R, S_PQ, ctx->st, &ctx->launches);
+            cg_spmv_dot(A, ctx->p, ctx->q, ctx->R, singular, ctx->st, &ctx->launches);
             // the update also writes level 0's first smoothing step when the
             // hierarchy has more than one level
             const bool fuse = ctx->nlev > 1;
@@ -400,18 +419,38 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
                 return SCF_ERR_NONFINITE;
             }
             if (std::sqrt(rr) <= tol * bn) { conv = true; break; }
+            // Below the rounding floor of the system (where the recursive
+            // residual has left the true one behind) the recursion turns
+            // around and grows: stop at a tenfold rise over the smallest
+            // residual of this round, or after a long stretch without a new
+            // smallest one, and restart from the true residual.
+            if (rr < best) { best = rr; best_it = its; }
+            else if (rr > 100.0 * best || its - best_it >= kStallWindow) { stalled = true; break; }
             const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
             if (el > ctx->opts.time_limit_s) break;
             z = precondition<T>(ctx, L, cc, ctx->nlev > 1);
-            cg_dot_rz<T>(A, ctx->r, (const T *)L[0].b, z, ctx->R, ctx->st, &ctx->launches);
-            cg_pupdate<T>(A, z, ctx->p, ctx->R.scal, false, ctx->st, &ctx->launches);
+            cg_dot_rz<T>(A, ctx->r, (const T *)L[0].b, z, singular, ctx->R, ctx->st, &ctx->launches);
+            cg_pupdate<T>(A, z, ctx->active, ctx->p, ctx->R.scal, false, ctx->st, &ctx->launches);
         }
         // true FP64 residual (the refinement check); for an all-Neumann
         // system also the mean of x, removed below
         final_residual(A, ctx->active, ctx->b, ctx->x, ctx->r, singular, ctx->R, ctx->st, &ctx->launches);
         rel = std::sqrt(read_scal(ctx, S_RR)) / bn;
-        if (rel <= tol || !conv || its >= ctx->opts.max_iter || restarts >= ctx->opts.max_rounds) break;
-        ++restarts;  // recursive residual drifted below the true one: restart from the true residual
+        if (rel <= tol || !(conv || stalled) || its >= ctx->opts.max_iter || restarts >= ctx->opts.max_rounds)
+            break;
+        // recursive residual drifted away from the true one: restart from the
+        // true residual, keeping the best round-end iterate
+        if (rel < best_rel) {
+            best_rel = rel;
+            CK(cudaMemcpyAsync(ctx->xbest, ctx->x, sizeof(double) * ctx->d.ng, cudaMemcpyDeviceToDevice, ctx->st));
+            have_best = true;
+        }
+        ++restarts;
+    }
+    if (have_best && rel > best_rel) {
+        CK(cudaMemcpyAsync(ctx->x, ctx->xbest, sizeof(double) * ctx->d.ng, cudaMemcpyDeviceToDevice, ctx->st));
+        final_residual(A, ctx->active, ctx->b, ctx->x, ctx->r, singular, ctx->R, ctx->st, &ctx->launches);
+        rel = std::sqrt(read_scal(ctx, S_RR)) / bn;
     }
     if (singular) shift_solution(A, ctx->active, ctx->x, ctx->R.scal, ctx->st, &ctx->launches);
     stats->iterations = its;
@@ -419,7 +458,8 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
     stats->rel_residual = rel;
     stats->converged = rel <= tol ? 1 : 0;
     if (!stats->converged) {
-        set_err(ctx, "not converged: relative residual %.3e after %d iterations (tolerance %.1e)", rel, its, tol);
+        set_err(ctx, "not converged: relative residual %.3e after %d iterations (tolerance %.1e)%s", rel, its, tol,
+                stalled ? "; the residual stopped decreasing at the rounding floor" : "");
         return SCF_ERR_NOT_CONVERGED;
     }
     return SCF_OK;
@@ -551,16 +591,17 @@ int stage(scf_ctx *ctx, const scf_poisson_in *in, const scf_correct_in *corr, co
         for (int f = 0; f < 3; ++f)
             for (int q = 0; q < 6; ++q)
                 if (fl[f][q] != 0 && fl[f][q] != 1) { set_err(ctx, "velocity BC flag must be 0 or 1"); return SCF_ERR_BAD_ARG; }
-        if (!u || !v || !w || !p) { set_err(ctx, "null TVar array"); return SCF_ERR_BAD_ARG; }
+        if ((u || v || w || p) && !(u && v && w && p)) { set_err(ctx, "null TVar array"); return SCF_ERR_BAD_ARG; }
         H2D(ctx->umoex, corr->ucell_moexcell, d.n); H2D(ctx->uct, corr->ucell_cell_type, d.n);
         H2D(ctx->vmoex, corr->vcell_moexcell, d.n); H2D(ctx->vct, corr->vcell_cell_type, d.n);
         H2D(ctx->wmoex, corr->wcell_moexcell, d.n); H2D(ctx->wct, corr->wcell_cell_type, d.n);
-        H2D(ctx->tu, u, d.ng); H2D(ctx->tv, v, d.ng); H2D(ctx->tw, w, d.ng); H2D(ctx->tp, p, d.ng);
+        if (u) { H2D(ctx->tu, u, d.ng); H2D(ctx->tv, v, d.ng); H2D(ctx->tw, w, d.ng); H2D(ctx->tp, p, d.ng); }
         ctx->corr = *corr;
         ctx->have_corr = true;
     }
     ctx->staged = true;
     ctx->assembled = false;
+    ctx->have_loss = false;
     if (bytes_out) *bytes_out = bytes;
     return SCF_OK;
 }
@@ -673,7 +714,7 @@ int scf_ctx_create(scf_ctx **out, int32_t imax, int32_t jmax, int32_t kmax, cons
     A(ctx->phase, ng);
     A(ctx->diag, ng); A(ctx->dinv, ng); A(ctx->cE, ng); A(ctx->cN, ng); A(ctx->cT, ng); A(ctx->extra, ng);
     A(ctx->b, ng); A(ctx->active, ng);
-    A(ctx->x, ng); A(ctx->r, ng); A(ctx->p, ng); A(ctx->q, ng);
+    A(ctx->x, ng); A(ctx->r, ng); A(ctx->p, ng); A(ctx->q, ng); A(ctx->xbest, ng);
     A(ctx->pp, ng);
     for (int f = 0; f < 4; ++f)
         for (int q = 0; q < 6; ++q) A(ctx->bcvar[f][q], plane_size(d, q));
@@ -699,6 +740,7 @@ int scf_ctx_destroy(scf_ctx *ctx)
     cudaSetDevice(ctx->opts.device);
     if (ctx->st) cudaStreamSynchronize(ctx->st);
     ctx->mgmem.release();
+    ctx->adjmem.release();
     ctx->mem.release();
     for (int e = 0; e < 8; ++e)
         if (ctx->ev[e]) cudaEventDestroy(ctx->ev[e]);
@@ -808,6 +850,135 @@ int scf_update_puvw(scf_ctx *ctx, const scf_poisson_in *in, const scf_correct_in
     return solve_rc;
 }
 
+// ---------------------------------------------------------------------------
+// loss and adjoint
+namespace {
+
+AdjArgs adj_args(scf_ctx *ctx)
+{
+    AdjArgs A;
+    A.d = ctx->d;
+    A.us = ctx->us; A.vs = ctx->vs; A.ws = ctx->ws;
+    A.pp = ctx->pp; A.pfwd = ctx->adj_pfwd; A.pocoef = ctx->pocoef;
+    A.umoex = ctx->umoex; A.uct = ctx->uct; A.vmoex = ctx->vmoex; A.vct = ctx->vct;
+    A.wmoex = ctx->wmoex; A.wct = ctx->wct; A.ct = ctx->ct;
+    A.ee = ctx->ee; A.ne = ctx->ne; A.te = ctx->te;
+    A.pdx = ctx->pdx; A.pdy = ctx->pdy; A.pdz = ctx->pdz;
+    A.gw = ctx->adj_g; A.r = ctx->adj_r;
+    A.phase = ctx->phase; A.phil = ctx->phil; A.tol = ctx->opts.gfm_tol;
+    return A;
+}
+
+int ensure_adj(scf_ctx *ctx)
+{
+    if (ctx->adj_rho) return SCF_OK;
+    const int ng = ctx->d.ng;
+    DALLOC(ctx->adjmem, ctx->adj_rho, ng);
+    DALLOC(ctx->adjmem, ctx->adj_g, ng);
+    DALLOC(ctx->adjmem, ctx->adj_r, ng);
+    DALLOC(ctx->adjmem, ctx->adj_pfwd, ng);
+    DALLOC(ctx->adjmem, ctx->adj_gu, ng);
+    DALLOC(ctx->adjmem, ctx->adj_gv, ng);
+    DALLOC(ctx->adjmem, ctx->adj_gw, ng);
+    DALLOC(ctx->adjmem, ctx->adj_grho, ng);
+    return SCF_OK;
+}
+
+}  // namespace
+
+extern "C" int scf_loss_forward(scf_ctx *ctx, const scf_poisson_in *in, const scf_correct_in *corr,
+                                const double *rho_cell, const double *g, double *J, scf_stats *stats)
+{
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!in || !corr || !g || !J) { set_err(ctx, "null argument"); return SCF_ERR_BAD_ARG; }
+    for (int q = 0; q < 6; ++q)
+        if (in->bcp_flag[q] != 1) {
+            set_err(ctx, "the loss gradient supports all-Neumann pressure boundaries only");
+            return SCF_ERR_BAD_ARG;
+        }
+    if ((rc = ensure_adj(ctx))) return rc;
+    scf_stats local;
+    if (!stats) stats = &local;
+    rc = stage(ctx, in, corr, nullptr, nullptr, nullptr, nullptr, nullptr);
+    if (rc) return rc;
+    const Dims &d = ctx->d;
+    // g (interior) -> ghosted device array
+    std::vector<double> gg(d.ng, 0.0);
+    for (int k = 1; k <= d.K; ++k)
+        for (int j = 1; j <= d.J; ++j)
+            for (int i = 1; i <= d.I; ++i) gg[gidx(d, i, j, k)] = g[nidx(d, i, j, k)];
+    CK(cudaMemcpyAsync(ctx->adj_g, gg.data(), sizeof(double) * d.ng, cudaMemcpyHostToDevice, ctx->st));
+    if (rho_cell) {
+        CK(cudaMemcpyAsync(ctx->adj_rho, rho_cell, sizeof(double) * d.ng, cudaMemcpyHostToDevice, ctx->st));
+        ctx->use_rho = true;
+    } else {
+        ctx->use_rho = false;
+    }
+    CK(cudaStreamSynchronize(ctx->st));
+    ctx->warm_ok = false;
+    rc = run(ctx, false, stats);   // coefficients, operator, solve, scatter
+    ctx->use_rho = false;
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->adj_pfwd, ctx->pp, sizeof(double) * d.ng, cudaMemcpyDeviceToDevice, ctx->st));
+    AdjArgs A = adj_args(ctx);
+    launch_adj_divergence(A, ctx->R, ctx->st, &ctx->launches);
+    CK(cudaMemcpyAsync(ctx->h_scal, ctx->R.scal + S_JP, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    CK(cudaStreamSynchronize(ctx->st));
+    J[0] = ctx->h_scal[0];
+    J[1] = ctx->h_scal[1];
+    ctx->have_loss = true;
+    ctx->rho_given_last = rho_cell != nullptr;
+    return SCF_OK;
+}
+
+extern "C" int scf_loss_backward(scf_ctx *ctx, double *grad_u, double *grad_v, double *grad_w, double *grad_rho,
+                                 scf_stats *stats)
+{
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!ctx->have_loss) { set_err(ctx, "scf_loss_backward needs a preceding scf_loss_forward"); return SCF_ERR_NO_SOLVE; }
+    scf_stats local;
+    if (!stats) stats = &local;
+    memset(stats, 0, sizeof(*stats));
+    const Dims &d = ctx->d;
+    const LevelView<double> V = fine_view(ctx);
+    AdjArgs A = adj_args(ctx);
+    // adjoint right-hand side (P g + A_m r) into b, then the same solve
+    active_mean(V, ctx->active, ctx->adj_g, ctx->R, ctx->st, &ctx->launches);
+    launch_adj_rhs(A, ctx->R.scal, ctx->b, ctx->st, &ctx->launches);
+    ctx->warm_ok = false;
+    cudaEventRecord(ctx->ev[1], ctx->st);
+    if (ctx->opts.precision == SCF_PREC_FP64)
+        rc = solve_impl<double>(ctx, ctx->L64, stats);
+    else
+        rc = solve_impl<float>(ctx, ctx->L32, stats);
+    cudaEventRecord(ctx->ev[2], ctx->st);
+    if (rc) return rc;
+    // densities for the derivative: the given field or the phase densities
+    if (!ctx->rho_given_last) fill_phase_density(ctx->phase, ctx->adj_rho, d.ng, ctx->opts.rho_l, ctx->opts.rho_g,
+                                                 ctx->st, &ctx->launches);
+    const double rho_ref = ctx->opts.rho_ref > 0.0 ? ctx->opts.rho_ref : ctx->opts.rho_l;
+    CK(cudaMemsetAsync(ctx->adj_gu, 0, sizeof(double) * d.ng, ctx->st));
+    CK(cudaMemsetAsync(ctx->adj_gv, 0, sizeof(double) * d.ng, ctx->st));
+    CK(cudaMemsetAsync(ctx->adj_gw, 0, sizeof(double) * d.ng, ctx->st));
+    CK(cudaMemsetAsync(ctx->adj_grho, 0, sizeof(double) * d.ng, ctx->st));
+    launch_adj_grad(A, ctx->x, ctx->adj_rho, rho_ref, ctx->adj_gu, ctx->adj_gv, ctx->adj_gw, ctx->adj_grho, ctx->st,
+                    &ctx->launches);
+    int64_t bo = 0;
+    if ((rc = d2h(ctx, grad_u, ctx->adj_gu, d.ng, &bo))) return rc;
+    if ((rc = d2h(ctx, grad_v, ctx->adj_gv, d.ng, &bo))) return rc;
+    if ((rc = d2h(ctx, grad_w, ctx->adj_gw, d.ng, &bo))) return rc;
+    if ((rc = d2h(ctx, grad_rho, ctx->adj_grho, d.ng, &bo))) return rc;
+    CK(cudaStreamSynchronize(ctx->st));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev[1], ctx->ev[2]);
+    stats->ms_solve = ms;
+    stats->bytes_d2h = bo;
+    stats->gpu_launches = ctx->launches;
+    return SCF_OK;
+}
+
 int scf_debug_apply(scf_ctx *ctx, const double *xh, double *yh)
 {
     int rc = check_ctx(ctx);
@@ -825,7 +996,7 @@ int scf_debug_apply(scf_ctx *ctx, const double *xh, double *yh)
                     xz[gidx(d, i, j, k)] = 0.0;
     CK(cudaMemcpyAsync(ctx->p, xz.data(), sizeof(double) * d.ng, cudaMemcpyHostToDevice, ctx->st));
     CK(cudaMemsetAsync(ctx->q, 0, sizeof(double) * d.ng, ctx->st));
-    cg_spmv_dot(fine_view(ctx), ctx->p, ctx->q, ctx->R, S_PQ, ctx->st, &ctx->launches);
+    cg_spmv_dot(fine_view(ctx), ctx->p, ctx->q, ctx->R, false, ctx->st, &ctx->launches);
     CK(cudaMemcpyAsync(yh, ctx->q, sizeof(double) * d.ng, cudaMemcpyDeviceToHost, ctx->st));
     CK(cudaStreamSynchronize(ctx->st));
     return SCF_OK;

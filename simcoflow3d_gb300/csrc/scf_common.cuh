@@ -46,6 +46,10 @@ enum ScfScalar {
     S_MEAN,
     S_RZ_NEW,
     S_MEANX,       // mean of x over the active cells (all-Neumann systems)
+    S_JP,          // loss: pressure term
+    S_JD,          // loss: divergence term
+    S_QMEAN,       // mean of A p over the active cells (all-Neumann systems)
+    S_ZMEAN,       // mean of the preconditioned residual over the active cells
     S_NUM
 };
 

@@ -37,8 +37,10 @@ struct OpArgs {
     float *diag32, *dinv32, *cE32, *cN32, *cT32, *extra32;  // mixed only
 };
 
-int launch_assemble(const AsmArgs &a, const OpArgs &o, bool mixed, cudaStream_t st, unsigned *stale_count_host,
-                    int *launches);
+// rho: per-cell densities (ghosted) or nullptr for the reference's two-phase
+// coefficients.
+int launch_assemble(const AsmArgs &a, const OpArgs &o, bool mixed, const double *rho, double rho_ref,
+                    cudaStream_t st, unsigned *stale_count_host, int *launches);
 
 // ---- solver --------------------------------------------------------------
 template <typename T>
@@ -92,18 +94,18 @@ void probe_prolong(MgLevel<T> &F, MgLevel<T> &C, const ChebCoef &cc, cudaStream_
 void probe_spmv(const LevelView<double> &A, const double *p, double *q, Reducer &R, cudaStream_t st);
 
 // CG building blocks on the fine level (FP64 vectors, ghosted layout).
-void cg_spmv_dot(const LevelView<double> &A, const double *p, double *q, Reducer &R, int slot_out,
+void cg_spmv_dot(const LevelView<double> &A, const double *p, double *q, Reducer &R, bool singular,
                  cudaStream_t st, int *launches);
-void cg_finish_alpha(Reducer &R, int nblocks, cudaStream_t st, int *launches);
 template <typename T>
 void cg_update(const LevelView<double> &A, double *x, double *r, const double *p, const double *q, T *rlow,
                const LevelView<T> &L0, T *x0, double first, Reducer &R, cudaStream_t st, int *launches);
 template <typename T>
-void cg_dot_rz(const LevelView<double> &A, const double *r, const T *rlow, const T *z, Reducer &R, cudaStream_t st,
-               int *launches);
+void cg_dot_rz(const LevelView<double> &A, const double *r, const T *rlow, const T *z, bool singular, Reducer &R,
+               cudaStream_t st, int *launches);
+// p = (z - mean z) + beta p (the mean over the active cells, all-Neumann systems)
 template <typename T>
-void cg_pupdate(const LevelView<double> &A, const T *z, double *p, const double *scal, bool first,
-                cudaStream_t st, int *launches);
+void cg_pupdate(const LevelView<double> &A, const T *z, const unsigned char *act, double *p, const double *scal,
+                bool first, cudaStream_t st, int *launches);
 void reduce_to(Reducer &R, int nblocks, int slot, cudaStream_t st, int *launches);
 // Right-hand side prologue: for an all-Neumann system the mean of b over the
 // active cells is removed (S_COUNT, S_MEAN); then S_BB = (b, b).
@@ -117,6 +119,34 @@ void final_residual(const LevelView<double> &A, const unsigned char *active, con
 void shift_solution(const LevelView<double> &A, const unsigned char *active, double *x, const double *scal,
                     cudaStream_t st, int *launches);
 void copy_to_low(const LevelView<double> &A, const double *src, float *dst, cudaStream_t st, int *launches);
+
+// sums of two partial arrays: mode 0 sum+count (S_SUM, S_COUNT, S_MEAN),
+// 1 (S_RR, S_MEANX), 2 loss terms (S_JP, S_JD)
+void reduce2_to(Reducer &R, int nblocks, int mode, cudaStream_t st, int *launches);
+// S_MEAN = mean of v over the active cells
+void active_mean(const LevelView<double> &A, const unsigned char *active, const double *v, Reducer &R,
+                 cudaStream_t st, int *launches);
+
+// ---- loss and adjoint --------------------------------------------------------
+struct AdjArgs {
+    Dims d;
+    const double *us, *vs, *ws, *pp, *pfwd, *pocoef;
+    const int *umoex, *uct, *vmoex, *vct, *wmoex, *wct, *ct;
+    const double *ee, *ne, *te, *pdx, *pdy, *pdz;
+    const double *gw;            // pressure-loss weights, ghosted
+    double *r;                   // divergence of the corrected velocity, ghosted
+    const unsigned char *phase;
+    const double *phil;
+    double tol;
+};
+void launch_pocoef_rho(const AsmArgs &a, const double *rho, double rho_ref, cudaStream_t st, int *launches);
+// rho = rho_g on dry cells, rho_l elsewhere (the reference's two densities)
+void fill_phase_density(const unsigned char *phase, double *rho, int ng, double rho_l, double rho_g, cudaStream_t st,
+                        int *launches);
+void launch_adj_divergence(const AdjArgs &A, Reducer &R, cudaStream_t st, int *launches);
+void launch_adj_rhs(const AdjArgs &A, const double *scal, double *b, cudaStream_t st, int *launches);
+void launch_adj_grad(const AdjArgs &A, const double *lam, const double *rho, double rho_ref, double *gu, double *gv,
+                     double *gw, double *grho, cudaStream_t st, int *launches);
 
 // ---- correction ------------------------------------------------------------
 struct CorrArgs {

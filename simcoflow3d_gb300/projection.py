@@ -63,6 +63,9 @@ def load_library(path: Optional[str] = None):
     L.scf_host_unregister.argtypes = [C.c_void_p]
     L.scf_abi_version.argtypes = []
     L.scf_debug_time_kernel.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.scf_loss_forward.argtypes = [C.c_void_p, P(capi.ScfPoissonIn), P(capi.ScfCorrectIn), capi.c_double_p,
+                                   capi.c_double_p, capi.c_double_p, P(capi.ScfStats)]
+    L.scf_loss_backward.argtypes = [C.c_void_p] + [capi.c_double_p] * 4 + [P(capi.ScfStats)]
     L.scf_apply_operator_noalloc.argtypes = [C.c_int32, C.c_int32, C.c_int32] + [C.c_void_p] * 8
     _lib = L
     return L
@@ -182,6 +185,29 @@ class Projection:
     def fetch(self, u=None, v=None, w=None, p=None, pocoef=None, pp=None, bc=None):
         self._check(self.L.scf_fetch_outputs(self.ctx, capi.dptr(u), capi.dptr(v), capi.dptr(w), capi.dptr(p),
                                              capi.dptr(pocoef), capi.dptr(pp), C.byref(bc) if bc else None))
+
+    # -- loss and adjoint gradient -------------------------------------------------
+    def loss_forward(self, w, g, rho=None, pred=None):
+        """(J_pressure, J_divergence) of the projection of workload ``w``.
+        ``g``: interior weights of the pressure term; ``rho``: optional
+        ghosted per-cell densities; ``pred``: optional (u*, v*, w*)."""
+        self._lpin = capi.poisson_in(w, pred)
+        self._lcin = capi.correct_in(w)
+        self._lg = np.asfortranarray(g, dtype=np.float64)
+        self._lrho = None if rho is None else np.asfortranarray(rho, dtype=np.float64)
+        J = (C.c_double * 2)()
+        st = capi.ScfStats()
+        self._check(self.L.scf_loss_forward(self.ctx, C.byref(self._lpin), C.byref(self._lcin),
+                                            capi.dptr(self._lrho), capi.dptr(self._lg),
+                                            C.cast(J, capi.c_double_p), C.byref(st)))
+        return float(J[0]), float(J[1]), st.as_dict()
+
+    def loss_backward(self, shape_g):
+        """Gradients of J_pressure + J_divergence: (du*, dv*, dw*, drho), ghosted."""
+        out = [np.zeros(shape_g, order="F") for _ in range(4)]
+        st = capi.ScfStats()
+        self._check(self.L.scf_loss_backward(self.ctx, *(capi.dptr(o) for o in out), C.byref(st)))
+        return out, st.as_dict()
 
     # -- diagnostics ---------------------------------------------------------------
     def debug_apply(self, x: np.ndarray) -> np.ndarray:

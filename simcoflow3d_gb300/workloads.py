@@ -383,6 +383,8 @@ def _cell_geo_areas(dx, dy, dz, nx, ny, nz, phi, ct):
     ne = face_geo_area(dz, dx, nz, nx, ny, dy / 2.0, phi)
     se = face_geo_area(dz, dx, nz, nx, ny, -dy / 2.0, phi)
     tol = 1.0e-20
+    # wetted solid area of each cell (CutCell.f90:455-462), before sharing
+    wllh = np.sqrt(((ee - we) * dy * dz) ** 2 + ((ne - se) * dx * dz) ** 2 + ((te - be) * dx * dy) ** 2)
     EE = np.ones((I + 2, J + 2, K + 2), order="F")
     NE = np.ones((I + 2, J + 2, K + 2), order="F")
     TE = np.ones((I + 2, J + 2, K + 2), order="F")
@@ -413,7 +415,7 @@ def _cell_geo_areas(dx, dy, dz, nx, ny, nz, phi, ct):
     NE[1:I + 1, 1:J, 1:K + 1][m] = 0.0
     m = cut[:, :, :-1] & (ct[:, :, 1:] == 2)
     TE[1:I + 1, 1:J + 1, 1:K][m] = 0.0
-    return EE, NE, TE
+    return EE, NE, TE, wllh
 
 
 def _staggered_vof(solid, xs, ys, zs, dxs, dys, dzs):
@@ -529,7 +531,7 @@ def build_workload(name: str, imax: int, jmax: int, kmax: int, *,
     vofl_g = np.array(vofl_g)
     vofl_g[1:-1, 1:-1, 1:-1] = vofl_d
     vof_g = _ghost_copy(vof_d)
-    EE, NE, TE = _cell_geo_areas(DX, DY, DZ, nx, ny, nz, phi, ct)
+    EE, NE, TE, wllh = _cell_geo_areas(DX, DY, DZ, nx, ny, nz, phi, ct)
 
     # --- staggered velocity cells
     xs_u = _bcast3(gx.c + 0.5 * gx.d, 0, shp)
@@ -621,7 +623,7 @@ def build_workload(name: str, imax: int, jmax: int, kmax: int, *,
         "tvar_u": tu, "tvar_v": tv, "tvar_w": tw, "tvar_p": tp,
         # not read by the hot path; kept for the pressure-force loss of the
         # gradient harness (Solver.f90:684-706 uses the solid normal)
-        "pcell_nz": F(nz), "pcell_phi": F(phi),
+        "pcell_nz": F(nz), "pcell_phi": F(phi), "pcell_wllh": F(wllh),
     }
     # Velocity BCs: no-slip walls (Dirichlet 0); an open (Dirichlet-p) face
     # gets Neumann velocity, like the dam-break driver's top
@@ -652,6 +654,15 @@ def _surface(z0, amp, kx, ky=None, kind="sinsin"):
 # Named workloads -------------------------------------------------------------
 
 SPHERE_C1 = ("sphere", 0.5, 0.5, 0.3, 0.15)
+
+
+def pressure_force_weights(w) -> np.ndarray:
+    """Weights g of the vertical pressure force on the solid: the sum over
+    cut cells of p * (-nz) * WlLh (the Clpz1 sum of PrintDragLiftCoef,
+    Solver.f90:684-706); interior (I,J,K) array."""
+    a = w.arrays
+    g = -a["pcell_nz"] * a["pcell_wllh"]
+    return np.asfortranarray(np.where(a["cell_type"] == 1, g, 0.0))
 
 
 def config(name: str, n: Optional[int] = None, seed: int = DEFAULT_SEED, **kw) -> Workload:

@@ -282,3 +282,22 @@ def test_mixed_matches_fp64_at_64(lib):
     d = (a - b)[1:-1, 1:-1, 1:-1][act]
     assert np.abs(d).max() <= 1e-5 * np.abs(a[1:-1, 1:-1, 1:-1][act]).max()
     assert abs(sa["iterations"] - sb["iterations"]) <= 2
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_tolerance_below_rounding_floor_stops_early(lib, precision):
+    """A tolerance FP64 cannot reach ends in NOT_CONVERGED soon after the
+    residual stops decreasing, with the solution no worse than that of a
+    reachable tolerance (the floor of this system is near 5e-14)."""
+    w = W.config("c1", n=32)
+    p = _proj(w, rel_tol=1e-17, precision=precision, max_iter=500)
+    _, pp, st = p.poisson_solve(w, want_pocoef=False, allow_not_converged=True)
+    assert st["converged"] == 0
+    assert st["iterations"] < 150
+    assert st["rel_residual"] < 1e-12
+    assert "rounding floor" in p.last_error()
+    q = _proj(w, rel_tol=1e-12, precision=precision)
+    _, pq, sq = q.poisson_solve(w, want_pocoef=False)
+    act = w.arrays["cell_type"] != 2
+    d = (pp - pq)[1:-1, 1:-1, 1:-1][act]
+    assert np.abs(d).max() <= 1e-9 * np.abs(pq[1:-1, 1:-1, 1:-1][act]).max()
