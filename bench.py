@@ -171,10 +171,14 @@ def unpin(lib, arrs):
         lib.scf_host_unregister(a.ctypes.data)
 
 
-def time_device(proj, steps, warmup):
-    """W untimed + K timed device-resident projections; returns (list of ms, stats)."""
+def time_device(proj, steps, warmup, live_kernel_timing=False):
+    """W untimed + K timed device-resident projections; returns (list of ms, stats).
+    With live_kernel_timing the fine-level kernels of the timed projections are
+    bracketed by CUDA events on the context's stream (Projection.kernel_timing)."""
     for _ in range(warmup):
         proj.run()
+    if live_kernel_timing:
+        proj.kernel_timing(True)
     ms, launches, last = [], 0, None
     for _ in range(steps):
         st = proj.run()
@@ -260,17 +264,27 @@ def run_ours(args):
         barrier(dist)
         if name == "mixed":
             with ClockSampler(local) as cs:
-                ms, launches, st = time_device(proj, args.steps, args.warmup)
+                ms, launches, st = time_device(proj, args.steps, args.warmup, live_kernel_timing=True)
             clocks = cs.summary()
         else:
             ms, launches, st = time_device(proj, args.steps, args.warmup)
         total = allreduce_max(dist, sum(ms))
         results[name] = {"ms": ms, "total": total, "launches": launches, "stats": st, "proj": proj}
 
-    # dominant-kernel roofline on the mixed context (fine-level smoother)
+    # dominant-kernel roofline on the mixed context (fine-level smoother),
+    # from the launches of the timed projections themselves
     mixed = results["mixed"]["proj"]
-    k_ms, k_bytes = mixed.time_kernel(capi.SCF_K_SMOOTH, reps=50)
-    s_ms, s_bytes = mixed.time_kernel(capi.SCF_K_SPMV, reps=50)
+    live = {}
+    for name, kc in (("smooth", capi.SCF_K_SMOOTH), ("spmv", capi.SCF_K_SPMV), ("restrict", capi.SCF_K_RESTRICT),
+                     ("prolong", capi.SCF_K_PROLONG), ("cg_update", capi.SCF_K_CGUPDATE)):
+        tot, nl, by = mixed.kernel_timing_read(kc)
+        live[name] = {"launches": nl, "ms_per_launch": round(tot / max(nl, 1), 5),
+                      "GB/s": round(by * nl / (tot * 1e-3) / 1e9, 1) if tot > 0 else None,
+                      "bytes_per_launch": by}
+    mixed.kernel_timing(False)
+    k_nl, k_bytes = live["smooth"]["launches"], live["smooth"]["bytes_per_launch"]
+    k_ms = live["smooth"]["ms_per_launch"]
+    iso_ms, _ = mixed.time_kernel(capi.SCF_K_SMOOTH, reps=50)
     peak, peak_kind = measured_peaks()
     achieved = k_bytes / (k_ms * 1e-3) / 1e9
     traffic = committed_traffic()
@@ -345,8 +359,10 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "kernel": "k_cheb_step<float> (fine-level Chebyshev step)",
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
-                     "bytes_per_launch": k_bytes, "ms_per_launch": round(k_ms, 5), "traffic": trf},
-        "fp64_spmv": {"GB/s": round(s_bytes / (s_ms * 1e-3) / 1e9, 1), "ms_per_launch": round(s_ms, 5)},
+                     "bytes_per_launch": k_bytes, "ms_per_launch": k_ms, "launches_timed": k_nl,
+                     "timing": "CUDA events around each launch of the timed projections",
+                     "ms_per_launch_isolated": round(iso_ms, 5), "traffic": trf},
+        "kernels_live": live,
         "clocks": clocks,
         "gpu_launches": results["mixed"]["launches"],
         "cpu_baseline": cpu,

@@ -248,6 +248,17 @@ enum scf_kernel_class {
 int scf_debug_time_kernel(scf_ctx *ctx, int kernel, int reps, double *ms_per_launch,
                           double *bytes_per_launch);
 
+/* Live per-kernel timing of real projections.  While enabled, every
+ * fine-level launch of the kernel classes above inside a solve is bracketed
+ * by CUDA events on the context's stream (at most 512 launches per solve);
+ * the elapsed times accumulate per class across runs.  Enabling or disabling
+ * resets the totals.  _read returns the total device milliseconds, the
+ * number of timed launches and the algorithmic bytes of one launch (the
+ * byte model of scf_debug_time_kernel); any output may be NULL.            */
+int scf_kernel_timing(scf_ctx *ctx, int enable);
+int scf_kernel_timing_read(scf_ctx *ctx, int kernel, double *ms_total, long long *launches,
+                           double *bytes_per_launch);
+
 /* ---- allocation-free operator apply ---------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory during a time step -- GPU-resident hosts that serve every device

@@ -158,10 +158,12 @@ __global__ void __launch_bounds__(1024) k_reduce_alpha(const double *__restrict_
 }
 
 void cg_spmv_dot(const LevelView<double> &A, const double *p, double *q, Reducer &R, bool singular,
-                 cudaStream_t st, int *launches)
+                 cudaStream_t st, int *launches, KTimer *kt)
 {
     Launch3 l = launch_zchunk(A.n0, A.n1, A.n2);
+    const int id = kt_begin(kt, KC_SPMV, st);
     k_spmv_dot<<<l.grid, l.block, 0, st>>>(A, p, q, R.partials, R.max_blocks);
+    kt_end(kt, id, st);
     k_reduce_alpha<<<1, 1024, 0, st>>>(R.partials, (int)nblocks(l), R.max_blocks, R.scal, singular ? 1 : 0);
     *launches += 2;
 }
@@ -198,111 +200,72 @@ __global__ void __launch_bounds__(128) k_cg_update(LevelView<double> A, double *
 
 template <typename T>
 void cg_update(const LevelView<double> &A, double *x, double *r, const double *p, const double *q, T *rlow,
-               const LevelView<T> &L0, T *x0, double first, Reducer &R, cudaStream_t st, int *launches)
+               const LevelView<T> &L0, T *x0, double first, Reducer &R, cudaStream_t st, int *launches,
+               KTimer *kt)
 {
     Launch3 l = launch_zchunk(A.n0, A.n1, A.n2);
+    const int id = kt_begin(kt, KC_CGUPDATE, st);
     k_cg_update<T><<<l.grid, l.block, 0, st>>>(A, x, r, p, q, rlow, L0, x0, (T)first, R.scal, R.partials);
+    kt_end(kt, id, st);
     *launches += 1;
     reduce_to(R, (int)nblocks(l), S_RR, st, launches);
 }
 
-// (r, z) and the sum of z: in mixed mode r is taken from its FP32 copy (the
-// V-cycle's rhs) and the products are formed in FP32, accumulated per thread
-// in FP32 over KZ cells and across threads in FP64; z is an FP32
-// preconditioner output, so this loses nothing that matters for beta.  FP64
-// mode: FP64 throughout.  The sum of z is FP64 in both (z is zero on
-// inactive cells).
+// (r, z): in mixed mode r is taken from its FP32 copy (the V-cycle's rhs) and
+// the products are formed in FP32, accumulated per thread in FP32 over KZ
+// cells and across threads in FP64; z is an FP32 preconditioner output, so
+// this loses nothing that matters for beta.  FP64 mode: FP64 throughout.
 template <typename T>
 __global__ void __launch_bounds__(128) k_dot_rz(LevelView<double> A, const double *__restrict__ r,
                                                 const T *__restrict__ rlow, const T *__restrict__ z,
-                                                double *__restrict__ part, int n0)
+                                                double *__restrict__ part)
 {
     ZCHUNK_IJK(A);
-    double v = 0.0, sz = 0.0;
+    double v = 0.0;
     if (in) {
         int c = i + A.sy * j + A.sz * k0;
         if (sizeof(T) == 4) {
             float acc = 0.f;
-            for (int k = k0; k <= k1; ++k, c += A.sz) {
-                const float zz = (float)z[c];
-                acc += (float)rlow[c] * zz;
-                sz += (double)zz;
-            }
+            for (int k = k0; k <= k1; ++k, c += A.sz) acc += (float)rlow[c] * (float)z[c];
             v = (double)acc;
         } else {
-            for (int k = k0; k <= k1; ++k, c += A.sz) {
-                const double zz = (double)z[c];
-                v += r[c] * zz;
-                sz += zz;
-            }
+            for (int k = k0; k <= k1; ++k, c += A.sz) v += r[c] * (double)z[c];
         }
     }
     v = block_sum(v);
-    __syncthreads();
-    sz = block_sum(sz);
-    if (thread_linear() == 0) {
-        part[block_linear()] = v;
-        part[n0 + block_linear()] = sz;
-    }
-}
-
-// beta = (r, z) / (r, z)_previous; for an all-Neumann system also the mean of
-// z over the active cells, which the search-direction update removes: the
-// V-cycle's rounding leaves a constant (null-vector) part in z, and once the
-// residual nears the rounding floor that part dominates p, (p, A p) collapses
-// and alpha explodes.  Removing it keeps p in the range of the operator.
-__global__ void __launch_bounds__(1024) k_reduce_beta(const double *__restrict__ part, int n, int n0, double *scal,
-                                                      int singular)
-{
-    double s = 0.0, t = 0.0;
-    for (int q = threadIdx.x; q < n; q += blockDim.x) {
-        s += part[q];
-        t += part[n0 + q];
-    }
-    s = block_sum(s);
-    __syncthreads();
-    t = block_sum(t);
-    if (threadIdx.x == 0) {
-        const double old = scal[S_RZ];
-        scal[S_BETA] = old != 0.0 ? s / old : 0.0;
-        scal[S_RZ] = s;
-        scal[S_ZMEAN] = (singular && scal[S_COUNT] > 0.0) ? t / scal[S_COUNT] : 0.0;
-    }
+    if (thread_linear() == 0) part[block_linear()] = v;
 }
 
 template <typename T>
-void cg_dot_rz(const LevelView<double> &A, const double *r, const T *rlow, const T *z, bool singular, Reducer &R,
-               cudaStream_t st, int *launches)
+void cg_dot_rz(const LevelView<double> &A, const double *r, const T *rlow, const T *z, Reducer &R, cudaStream_t st,
+               int *launches)
 {
     Launch3 l = launch_zchunk(A.n0, A.n1, A.n2);
-    k_dot_rz<T><<<l.grid, l.block, 0, st>>>(A, r, rlow, z, R.partials, R.max_blocks);
-    k_reduce_beta<<<1, 1024, 0, st>>>(R.partials, (int)nblocks(l), R.max_blocks, R.scal, singular ? 1 : 0);
+    k_dot_rz<T><<<l.grid, l.block, 0, st>>>(A, r, rlow, z, R.partials);
+    k_reduce<<<1, 1024, 0, st>>>(R.partials, (int)nblocks(l), R.scal, 0, RM_BETA);
     *launches += 2;
 }
 
-// p = (z - mean z) + beta p on the active cells
 template <typename T>
 __global__ void __launch_bounds__(128) k_pupdate(LevelView<double> A, const T *__restrict__ z,
-                                                 const unsigned char *__restrict__ act, double *__restrict__ p,
-                                                 const double *__restrict__ scal, int first)
+                                                 double *__restrict__ p, const double *__restrict__ scal, int first)
 {
     ZCHUNK_IJK(A);
     if (!in) return;
     const double beta = first ? 0.0 : scal[S_BETA];
-    const double zm = scal[S_ZMEAN];
     int c = i + A.sy * j + A.sz * k0;
     for (int k = k0; k <= k1; ++k, c += A.sz) {
-        const double zz = (double)z[c] - ((zm != 0.0 && act[c]) ? zm : 0.0);
+        const double zz = (double)z[c];
         p[c] = first ? zz : zz + beta * p[c];
     }
 }
 
 template <typename T>
-void cg_pupdate(const LevelView<double> &A, const T *z, const unsigned char *act, double *p, const double *scal,
-                bool first, cudaStream_t st, int *launches)
+void cg_pupdate(const LevelView<double> &A, const T *z, double *p, const double *scal, bool first, cudaStream_t st,
+                int *launches)
 {
     Launch3 l = launch_zchunk(A.n0, A.n1, A.n2);
-    k_pupdate<T><<<l.grid, l.block, 0, st>>>(A, z, act, p, scal, first ? 1 : 0);
+    k_pupdate<T><<<l.grid, l.block, 0, st>>>(A, z, p, scal, first ? 1 : 0);
     *launches += 1;
 }
 
@@ -726,7 +689,7 @@ void mg_coarse_inverse(const MgLevel<T> &L, double *ainv, int *map, int n, bool 
 
 template <typename T>
 T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, const int *map, int ncoarse,
-             bool singular, bool first_done, cudaStream_t st, int *launches)
+             bool singular, bool first_done, cudaStream_t st, int *launches, KTimer *kt)
 {
     T *cur[32];
     const int last = nlev - 1;
@@ -741,14 +704,18 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
         }
         for (int s = 1; s < cc.degree; ++s) {
             const T *dprev = (s == 1) ? xa : F.d;
+            const int id = l == 0 ? kt_begin(kt, KC_SMOOTH, st) : -1;
             k_cheb_step<T><<<lf.grid, lf.block, 0, st>>>(v, F.b, xa, dprev, xb, F.d, (T)cc.c1[s], (T)cc.c2[s]);
+            kt_end(kt, id, st);
             *launches += 1;
             T *tmp = xa; xa = xb; xb = tmp;
         }
         cur[l] = xa;
         MgLevel<T> &C = L[l + 1];
         dim3 rg((F.n0 + 31) / 32, (C.n1 + 3) / 4, C.n2), rb(32, 4, 1);
+        const int id = l == 0 ? kt_begin(kt, KC_RESTRICT, st) : -1;
         k_restrict<T><<<rg, rb, 0, st>>>(v, F.b, xa, C.view(), C.b, F.f0, F.f1, F.f2);
+        kt_end(kt, id, st);
         *launches += 1;
     }
     {
@@ -765,14 +732,18 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
         T *xa = cur[l];
         T *xb = (xa == F.x) ? F.xb : F.x;
         const bool more = cc.degree > 1;
+        const int idp = l == 0 ? kt_begin(kt, KC_PROLONG, st) : -1;
         k_post_first<T><<<lf.grid, lf.block, 0, st>>>(v, F.b, xa, C.view(), cur[l + 1], xb, more ? F.d : nullptr,
                                                       F.f0, F.f1, F.f2, (T)cc.first);
+        kt_end(kt, idp, st);
         *launches += 1;
         { T *tmp = xa; xa = xb; xb = tmp; }
         for (int s = 1; s < cc.degree; ++s) {
             const bool last_step = s == cc.degree - 1;
+            const int id = l == 0 ? kt_begin(kt, KC_SMOOTH, st) : -1;
             k_cheb_step<T><<<lf.grid, lf.block, 0, st>>>(v, F.b, xa, F.d, xb, last_step ? nullptr : F.d,
                                                          (T)cc.c1[s], (T)cc.c2[s]);
+            kt_end(kt, id, st);
             *launches += 1;
             T *tmp = xa; xa = xb; xb = tmp;
         }
@@ -825,18 +796,19 @@ template void mg_coarsen<double>(const MgLevel<double> &, MgLevel<double> &, cud
 template void mg_coarse_inverse<float>(const MgLevel<float> &, double *, int *, int, bool, cudaStream_t, int *);
 template void mg_coarse_inverse<double>(const MgLevel<double> &, double *, int *, int, bool, cudaStream_t, int *);
 template float *mg_vcycle<float>(MgLevel<float> *, int, const ChebCoef &, const double *, const int *, int, bool,
-                                 bool, cudaStream_t, int *);
+                                 bool, cudaStream_t, int *, KTimer *);
 template double *mg_vcycle<double>(MgLevel<double> *, int, const ChebCoef &, const double *, const int *, int, bool,
-                                   bool, cudaStream_t, int *);
+                                   bool, cudaStream_t, int *, KTimer *);
 template void cg_update<float>(const LevelView<double> &, double *, double *, const double *, const double *, float *,
-                               const LevelView<float> &, float *, double, Reducer &, cudaStream_t, int *);
+                               const LevelView<float> &, float *, double, Reducer &, cudaStream_t, int *, KTimer *);
 template void cg_update<double>(const LevelView<double> &, double *, double *, const double *, const double *,
-                                double *, const LevelView<double> &, double *, double, Reducer &, cudaStream_t, int *);
-template void cg_dot_rz<float>(const LevelView<double> &, const double *, const float *, const float *, bool,
-                               Reducer &, cudaStream_t, int *);
-template void cg_dot_rz<double>(const LevelView<double> &, const double *, const double *, const double *, bool,
+                                double *, const LevelView<double> &, double *, double, Reducer &, cudaStream_t, int *,
+                                KTimer *);
+template void cg_dot_rz<float>(const LevelView<double> &, const double *, const float *, const float *, Reducer &,
+                               cudaStream_t, int *);
+template void cg_dot_rz<double>(const LevelView<double> &, const double *, const double *, const double *,
                                 Reducer &, cudaStream_t, int *);
-template void cg_pupdate<float>(const LevelView<double> &, const float *, const unsigned char *, double *,
-                                const double *, bool, cudaStream_t, int *);
-template void cg_pupdate<double>(const LevelView<double> &, const double *, const unsigned char *, double *,
-                                 const double *, bool, cudaStream_t, int *);
+template void cg_pupdate<float>(const LevelView<double> &, const float *, double *, const double *, bool,
+                                cudaStream_t, int *);
+template void cg_pupdate<double>(const LevelView<double> &, const double *, double *, const double *, bool,
+                                 cudaStream_t, int *);

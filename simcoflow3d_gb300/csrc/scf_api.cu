@@ -64,6 +64,9 @@ struct scf_ctx {
     // CG vectors
     double *x, *r, *p, *q;
     double *xbest;             // best round-end iterate of a solve that restarts
+    KTimer kt;                 // live per-launch timing (scf_kernel_timing)
+    bool kt_events = false;
+    double kt_ms[KC_NUM] = {0}, kt_launches[KC_NUM] = {0};
     // multigrid
     int nlev = 0;
     int mg_precision = -1;
@@ -347,11 +350,43 @@ double read_scal(scf_ctx *ctx, int slot)
     return ctx->h_scal[0];
 }
 
+// Adds the elapsed times of the recorded event pairs to the per-class totals.
+void kt_harvest(scf_ctx *ctx)
+{
+    if (!ctx->kt.on || ctx->kt.n == 0) return;
+    cudaEventSynchronize(ctx->kt.ev[2 * ctx->kt.n - 1]);
+    for (int i = 0; i < ctx->kt.n; ++i) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, ctx->kt.ev[2 * i], ctx->kt.ev[2 * i + 1]) == cudaSuccess) {
+            ctx->kt_ms[ctx->kt.cls[i]] += ms;
+            ctx->kt_launches[ctx->kt.cls[i]] += 1.0;
+        }
+    }
+    ctx->kt.n = 0;
+}
+
+// Algorithmic bytes of one fine-level launch of a kernel class: each array
+// counted once per cell; FP32 levels derive 1/diag, FP64 levels read dinv.
+double kernel_bytes(const scf_ctx *ctx, int kernel)
+{
+    const bool mixed = ctx->opts.precision == SCF_PREC_MIXED;
+    const double s = mixed ? 4.0 : 8.0;
+    const double n = (double)ctx->d.n;
+    switch (kernel) {
+    case SCF_K_SMOOTH: return (mixed ? 9.0 : 10.0) * s * n;               // b,x,d,diag,[dinv],cE,cN,cT in; x,d out
+    case SCF_K_SPMV: return 6.0 * 8.0 * n;                                // p,diag,cE,cN,cT in; q out
+    case SCF_K_RESTRICT: return 6.0 * s * n + s * n / 8.0;                // b,x,diag,cE,cN,cT in; coarse b out
+    case SCF_K_PROLONG: return (mixed ? 8.0 : 9.0) * s * n + s * n / 8.0; // + coarse e; x,d out
+    case SCF_K_CGUPDATE: return (6.0 * 8.0 + (mixed ? 4.0 : 0.0)) * n;    // x,r,p,q in; x,r,[rlow],x0 out
+    default: return -1.0;
+    }
+}
+
 template <typename T>
 T *precondition(scf_ctx *ctx, MgLevel<T> *L, const ChebCoef &cc, bool first_done)
 {
     return mg_vcycle<T>(L, ctx->nlev, cc, ctx->ainv, ctx->map, ctx->ncoarse, is_singular(ctx), first_done,
-                        ctx->st, &ctx->launches);
+                        ctx->st, &ctx->launches, ctx->kt.on ? &ctx->kt : nullptr);
 }
 
 // Iterations without a new smallest CG residual after which a round of the
@@ -398,20 +433,21 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
     for (;;) {
         if (mixed) copy_to_low(A, ctx->r, rlow, ctx->st, &ctx->launches);
         T *z = precondition<T>(ctx, L, cc, false);
-        cg_dot_rz<T>(A, ctx->r, (const T *)L[0].b, z, singular, ctx->R, ctx->st, &ctx->launches);
-        cg_pupdate<T>(A, z, ctx->active, ctx->p, ctx->R.scal, true, ctx->st, &ctx->launches);
+        cg_dot_rz<T>(A, ctx->r, (const T *)L[0].b, z, ctx->R, ctx->st, &ctx->launches);
+        cg_pupdate<T>(A, z, ctx->p, ctx->R.scal, true, ctx->st, &ctx->launches);
         bool conv = false;
         stalled = false;
         double best = HUGE_VAL;
         int best_it = its;
         while (its < ctx->opts.max_iter) {
             ++its;
-            cg_spmv_dot(A, ctx->p, ctx->q, ctx->R, singular, ctx->st, &ctx->launches);
+            KTimer *kt = ctx->kt.on ? &ctx->kt : nullptr;
+            cg_spmv_dot(A, ctx->p, ctx->q, ctx->R, singular, ctx->st, &ctx->launches, kt);
             // the update also writes level 0's first smoothing step when the
             // hierarchy has more than one level
             const bool fuse = ctx->nlev > 1;
             cg_update<T>(A, ctx->x, ctx->r, ctx->p, ctx->q, (T *)(mixed ? (void *)rlow : nullptr), L[0].view(),
-                         fuse ? L[0].x : nullptr, cc.first, ctx->R, ctx->st, &ctx->launches);
+                         fuse ? L[0].x : nullptr, cc.first, ctx->R, ctx->st, &ctx->launches, kt);
             const double rr = read_scal(ctx, S_RR);
             if (!std::isfinite(rr)) {
                 set_err(ctx, "CG residual became non-finite at iteration %d", its);
@@ -429,8 +465,8 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
             const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
             if (el > ctx->opts.time_limit_s) break;
             z = precondition<T>(ctx, L, cc, ctx->nlev > 1);
-            cg_dot_rz<T>(A, ctx->r, (const T *)L[0].b, z, singular, ctx->R, ctx->st, &ctx->launches);
-            cg_pupdate<T>(A, z, ctx->active, ctx->p, ctx->R.scal, false, ctx->st, &ctx->launches);
+            cg_dot_rz<T>(A, ctx->r, (const T *)L[0].b, z, ctx->R, ctx->st, &ctx->launches);
+            cg_pupdate<T>(A, z, ctx->p, ctx->R.scal, false, ctx->st, &ctx->launches);
         }
         // true FP64 residual (the refinement check); for an all-Neumann
         // system also the mean of x, removed below
@@ -453,6 +489,7 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
         rel = std::sqrt(read_scal(ctx, S_RR)) / bn;
     }
     if (singular) shift_solution(A, ctx->active, ctx->x, ctx->R.scal, ctx->st, &ctx->launches);
+    kt_harvest(ctx);
     stats->iterations = its;
     stats->rounds = restarts + 1;
     stats->rel_residual = rel;
@@ -744,6 +781,8 @@ int scf_ctx_destroy(scf_ctx *ctx)
     ctx->mem.release();
     for (int e = 0; e < 8; ++e)
         if (ctx->ev[e]) cudaEventDestroy(ctx->ev[e]);
+    if (ctx->kt_events)
+        for (int e = 0; e < 2 * KTimer::CAP; ++e) cudaEventDestroy(ctx->kt.ev[e]);
     if (ctx->h_scal) cudaFreeHost(ctx->h_scal);
     if (ctx->h_u32) cudaFreeHost(ctx->h_u32);
     if (ctx->st) cudaStreamDestroy(ctx->st);
@@ -1031,8 +1070,6 @@ int scf_debug_time_kernel(scf_ctx *ctx, int kernel, int reps, double *ms_per_lau
     if (!ctx->solved) { set_err(ctx, "no projection has run"); return SCF_ERR_NO_SOLVE; }
     if (ctx->nlev < 2 && (kernel == SCF_K_RESTRICT || kernel == SCF_K_PROLONG)) return SCF_ERR_BAD_ARG;
     const bool mixed = ctx->opts.precision == SCF_PREC_MIXED;
-    const double s = mixed ? 4.0 : 8.0;
-    const double n = (double)ctx->d.n;
     const ChebCoef cc = cheb_coef(ctx->opts.smoother_degree);
     auto launch = [&]() {
         switch (kernel) {
@@ -1059,16 +1096,8 @@ int scf_debug_time_kernel(scf_ctx *ctx, int kernel, int reps, double *ms_per_lau
         }
         }
     };
-    double bytes;
-    switch (kernel) {
-    // each array counted once per cell; FP32 levels derive 1/diag, FP64 read dinv
-    case SCF_K_SMOOTH: bytes = (mixed ? 9.0 : 10.0) * s * n; break;  // b,x,d,diag,[dinv],cE,cN,cT in; x,d out
-    case SCF_K_SPMV: bytes = 6.0 * 8.0 * n; break;                   // p,diag,cE,cN,cT in; q out
-    case SCF_K_RESTRICT: bytes = 6.0 * s * n + s * n / 8.0; break;   // b,x,diag,cE,cN,cT in; coarse b out
-    case SCF_K_PROLONG: bytes = (mixed ? 8.0 : 9.0) * s * n + s * n / 8.0; break;  // + coarse e; x,d out
-    case SCF_K_CGUPDATE: bytes = (6.0 * 8.0 + (mixed ? 4.0 : 0.0)) * n; break;
-    default: return SCF_ERR_BAD_ARG;
-    }
+    const double bytes = kernel_bytes(ctx, kernel);
+    if (bytes < 0.0) return SCF_ERR_BAD_ARG;
     launch();  // warm
     CK(cudaEventRecord(ctx->ev[4], ctx->st));
     for (int r = 0; r < reps; ++r) launch();
@@ -1080,6 +1109,36 @@ int scf_debug_time_kernel(scf_ctx *ctx, int kernel, int reps, double *ms_per_lau
     *ms_per_launch = ms / reps;
     *bytes_per_launch = bytes;
     if (kernel == SCF_K_CGUPDATE) ctx->warm_ok = false;  // x was modified
+    return SCF_OK;
+}
+
+int scf_kernel_timing(scf_ctx *ctx, int enable)
+{
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (enable && !ctx->kt_events) {
+        for (int i = 0; i < 2 * KTimer::CAP; ++i)
+            if (cudaEventCreate(&ctx->kt.ev[i]) != cudaSuccess) {
+                while (i-- > 0) cudaEventDestroy(ctx->kt.ev[i]);
+                set_err(ctx, "cudaEventCreate failed");
+                return SCF_ERR_CUDA;
+            }
+        ctx->kt_events = true;
+    }
+    ctx->kt.on = enable != 0;
+    ctx->kt.n = 0;
+    for (int c = 0; c < KC_NUM; ++c) ctx->kt_ms[c] = ctx->kt_launches[c] = 0.0;
+    return SCF_OK;
+}
+
+int scf_kernel_timing_read(scf_ctx *ctx, int kernel, double *ms_total, long long *launches, double *bytes_per_launch)
+{
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (kernel < 0 || kernel >= KC_NUM) return SCF_ERR_BAD_ARG;
+    if (ms_total) *ms_total = ctx->kt_ms[kernel];
+    if (launches) *launches = (long long)ctx->kt_launches[kernel];
+    if (bytes_per_launch) *bytes_per_launch = kernel_bytes(ctx, kernel);
     return SCF_OK;
 }
 

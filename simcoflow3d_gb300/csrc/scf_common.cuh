@@ -49,7 +49,6 @@ enum ScfScalar {
     S_JP,          // loss: pressure term
     S_JD,          // loss: divergence term
     S_QMEAN,       // mean of A p over the active cells (all-Neumann systems)
-    S_ZMEAN,       // mean of the preconditioned residual over the active cells
     S_NUM
 };
 

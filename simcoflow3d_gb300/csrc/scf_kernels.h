@@ -77,12 +77,40 @@ void mg_coarsen(const MgLevel<T> &F, MgLevel<T> &C, cudaStream_t st, int *launch
 template <typename T>
 void mg_coarse_inverse(const MgLevel<T> &L, double *ainv, int *map, int n, bool singular, cudaStream_t st,
                        int *launches);
+// Live per-launch timing: CUDA events on the launching stream around the
+// fine-level launches of the kernel classes below (the same numbering as the
+// public scf_kernel_class).  Pairs beyond CAP in one solve go untimed.
+enum KClass { KC_SMOOTH = 0, KC_SPMV = 1, KC_RESTRICT = 2, KC_PROLONG = 3, KC_CGUPDATE = 4, KC_NUM = 5 };
+struct KTimer {
+    static constexpr int CAP = 512;
+    cudaEvent_t ev[2 * CAP];
+    int cls[CAP];
+    int n = 0;
+    bool on = false;
+    int begin(int c, cudaStream_t st)
+    {
+        if (!on || n >= CAP) return -1;
+        cls[n] = c;
+        cudaEventRecord(ev[2 * n], st);
+        return n++;
+    }
+    void end(int id, cudaStream_t st)
+    {
+        if (id >= 0) cudaEventRecord(ev[2 * id + 1], st);
+    }
+};
+inline int kt_begin(KTimer *kt, int c, cudaStream_t st) { return kt ? kt->begin(c, st) : -1; }
+inline void kt_end(KTimer *kt, int id, cudaStream_t st)
+{
+    if (kt) kt->end(id, st);
+}
+
 // One V-cycle: level 0 rhs in L[0].b, result in *z (== L[0].x or L[0].xb).
 // first_done: level 0's first Chebyshev step was already written to L[0].x
 // (fused into the CG update).
 template <typename T>
 T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, const int *map, int ncoarse,
-             bool singular, bool first_done, cudaStream_t st, int *launches);
+             bool singular, bool first_done, cudaStream_t st, int *launches, KTimer *kt = nullptr);
 
 // Single launches of the fine-level kernels, for timing.
 template <typename T>
@@ -95,17 +123,17 @@ void probe_spmv(const LevelView<double> &A, const double *p, double *q, Reducer 
 
 // CG building blocks on the fine level (FP64 vectors, ghosted layout).
 void cg_spmv_dot(const LevelView<double> &A, const double *p, double *q, Reducer &R, bool singular,
-                 cudaStream_t st, int *launches);
+                 cudaStream_t st, int *launches, KTimer *kt = nullptr);
 template <typename T>
 void cg_update(const LevelView<double> &A, double *x, double *r, const double *p, const double *q, T *rlow,
-               const LevelView<T> &L0, T *x0, double first, Reducer &R, cudaStream_t st, int *launches);
+               const LevelView<T> &L0, T *x0, double first, Reducer &R, cudaStream_t st, int *launches,
+               KTimer *kt = nullptr);
 template <typename T>
-void cg_dot_rz(const LevelView<double> &A, const double *r, const T *rlow, const T *z, bool singular, Reducer &R,
-               cudaStream_t st, int *launches);
-// p = (z - mean z) + beta p (the mean over the active cells, all-Neumann systems)
+void cg_dot_rz(const LevelView<double> &A, const double *r, const T *rlow, const T *z, Reducer &R, cudaStream_t st,
+               int *launches);
 template <typename T>
-void cg_pupdate(const LevelView<double> &A, const T *z, const unsigned char *act, double *p, const double *scal,
-                bool first, cudaStream_t st, int *launches);
+void cg_pupdate(const LevelView<double> &A, const T *z, double *p, const double *scal, bool first, cudaStream_t st,
+                int *launches);
 void reduce_to(Reducer &R, int nblocks, int slot, cudaStream_t st, int *launches);
 // Right-hand side prologue: for an all-Neumann system the mean of b over the
 // active cells is removed (S_COUNT, S_MEAN); then S_BB = (b, b).

@@ -63,6 +63,9 @@ def load_library(path: Optional[str] = None):
     L.scf_host_unregister.argtypes = [C.c_void_p]
     L.scf_abi_version.argtypes = []
     L.scf_debug_time_kernel.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.scf_kernel_timing.argtypes = [C.c_void_p, C.c_int]
+    L.scf_kernel_timing_read.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_longlong),
+                                         C.POINTER(C.c_double)]
     L.scf_loss_forward.argtypes = [C.c_void_p, P(capi.ScfPoissonIn), P(capi.ScfCorrectIn), capi.c_double_p,
                                    capi.c_double_p, capi.c_double_p, P(capi.ScfStats)]
     L.scf_loss_backward.argtypes = [C.c_void_p] + [capi.c_double_p] * 4 + [P(capi.ScfStats)]
@@ -220,6 +223,16 @@ class Projection:
         ms, by = C.c_double(), C.c_double()
         self._check(self.L.scf_debug_time_kernel(self.ctx, int(kernel), int(reps), C.byref(ms), C.byref(by)))
         return ms.value, by.value
+
+    def kernel_timing(self, enable: bool = True):
+        """Starts (or stops) live per-launch timing; resets the totals."""
+        self._check(self.L.scf_kernel_timing(self.ctx, 1 if enable else 0))
+
+    def kernel_timing_read(self, kernel: int):
+        """(total ms, launches, algorithmic bytes per launch) of a kernel class."""
+        ms, n, by = C.c_double(), C.c_longlong(), C.c_double()
+        self._check(self.L.scf_kernel_timing_read(self.ctx, int(kernel), C.byref(ms), C.byref(n), C.byref(by)))
+        return ms.value, n.value, by.value
 
     def debug_operator(self):
         I, J, K = self.shape
