@@ -141,15 +141,18 @@ def measured_peaks():
     return FALLBACK_HBM_GBS, "fallback"
 
 
-def committed_traffic():
-    """DRAM bytes per launch of the smoother from the committed ncu summary."""
-    p = os.path.join(HERE, "profiles", "roofline_traffic.json")
-    if os.path.exists(p):
-        try:
-            return json.load(open(p))
-        except Exception:
-            return None
-    return None
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
+# the fine-level FP32 Chebyshev step, from the ncu capture summarised in
+# profiles/k_cheb_step_f32_c2_192.md: 213.5 MB for a first pre-smoothing step
+# at 192^3, scaled to 256^3 by the number of cells (x 16777216/7077888).
+SMOOTH_TRAFFIC_256 = {"bytes": 213.5e6 * 16777216 / 7077888,
+                      "note": "first pre-smoothing step (32 B/cell algorithmic), ncu at 192^3 scaled by cells"}
+
+
+def smoother_traffic(n_cells: int):
+    if n_cells != 16777216:
+        return None
+    return SMOOTH_TRAFFIC_256
 
 
 def make_workload(name: str, seed: int, n=None):
@@ -249,17 +252,22 @@ def run_ours(args):
     # device-resident timing: mixed (value) and FP64 (comparison)
     results = {}
     precs = (("mixed", capi.SCF_PREC_MIXED), ("fp64", capi.SCF_PREC_FP64))
+    # Each arm runs at its fastest Chebyshev degree on this workload (sweep of
+    # degrees 2-6 at 256^3): 3 for the FP32 V-cycle, 2 for the FP64 one.
+    degree = {"mixed": 3, "fp64": 2}
     if args.only:
         # profiling captures: one precision, device-resident loop only
         name, prec = [x for x in precs if x[0] == args.only][0]
-        proj = Projection.for_workload(w, precision=prec, rel_tol=args.tol, device=local)
+        proj = Projection.for_workload(w, precision=prec, rel_tol=args.tol, device=local,
+                                       smoother_degree=degree[name])
         proj.stage(w)
         ms, launches, st = time_device(proj, args.steps, args.warmup)
         print(json.dumps({"only": name, "ms_per_projection": statistics.mean(ms), "stats": st}), flush=True)
         unpin(lib, pinned)
         return 0
     for name, prec in precs:
-        proj = Projection.for_workload(w, precision=prec, rel_tol=args.tol, device=local)
+        proj = Projection.for_workload(w, precision=prec, rel_tol=args.tol, device=local,
+                                       smoother_degree=degree[name])
         proj.stage(w)
         barrier(dist)
         if name == "mixed":
@@ -287,8 +295,7 @@ def run_ours(args):
     iso_ms, _ = mixed.time_kernel(capi.SCF_K_SMOOTH, reps=50)
     peak, peak_kind = measured_peaks()
     achieved = k_bytes / (k_ms * 1e-3) / 1e9
-    traffic = committed_traffic()
-    trf = traffic.get("smooth_fp32_bytes_per_launch") if traffic else None
+    trf = smoother_traffic(w.imax * w.jmax * w.kmax)
 
     # end to end through the drop-in call, host arrays pinned
     a = w.arrays
@@ -346,7 +353,7 @@ def run_ours(args):
             "l2": "inputs larger than L2 (about 3.5 GB resident per projection)",
             "parallelism": f"replicas x{ws}",
         },
-        "fp64": {"ms_per_projection": round(fp64, 4), "iterations": s64["iterations"],
+        "fp64": {"ms_per_projection": round(fp64, 4), "iterations": s64["iterations"], "smoother_degree": 2,
                  "rel_residual": s64["rel_residual"]},
         "mixed": {"iterations": smx["iterations"], "rel_residual": smx["rel_residual"],
                   "ms_assemble": round(smx["ms_assemble"], 3), "ms_solve": round(smx["ms_solve"], 3),
@@ -361,7 +368,9 @@ def run_ours(args):
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                      "bytes_per_launch": k_bytes, "ms_per_launch": k_ms, "launches_timed": k_nl,
                      "timing": "CUDA events around each launch of the timed projections",
-                     "ms_per_launch_isolated": round(iso_ms, 5), "traffic": trf},
+                     "ms_per_launch_isolated": round(iso_ms, 5),
+                     "traffic": round(trf["bytes"]) if trf else None,
+                     "traffic_note": trf["note"] if trf else None},
         "kernels_live": live,
         "clocks": clocks,
         "gpu_launches": results["mixed"]["launches"],
@@ -369,6 +378,34 @@ def run_ours(args):
     }
     print(json.dumps(line), flush=True)
     barrier(dist)
+    return 0
+
+
+def run_sequence(args):
+    """A sequence of warm-started projections on a fixed geometry (default:
+    the 512x256x256 wave tank): each call gets a freshly seeded prediction,
+    staged outside the timed region, and starts from the previous call's
+    pressure.  Prints one JSON line per precision."""
+    from simcoflow3d_gb300 import capi, workloads as W
+    from simcoflow3d_gb300.projection import Projection
+    w = make_workload(args.config, args.seed, args.n)
+    preds = W.PredictionSequence(w, seed=args.seed + 1)
+    degree = {"mixed": 3, "fp64": 2}
+    for name, prec in (("mixed", capi.SCF_PREC_MIXED), ("fp64", capi.SCF_PREC_FP64)):
+        proj = Projection.for_workload(w, precision=prec, rel_tol=args.tol, smoother_degree=degree[name])
+        for timed in (False, True):     # the first pass warms the context up
+            ms, its = [], []
+            for c in range(args.sequence):
+                proj.set_opts(warm_start=0 if c == 0 else 1)   # call 0 starts cold
+                proj.stage(w, pred=preds(c))
+                st = proj.run()
+                ms.append(st["ms_total"])
+                its.append(st["iterations"])
+        print(json.dumps({"sequence": args.config, "precision": name, "grid": [w.imax, w.jmax, w.kmax],
+                          "calls": len(ms), "ms_per_call": round(statistics.mean(ms), 3),
+                          "ms_min": round(min(ms), 3), "ms_max": round(max(ms), 3),
+                          "iterations": its, "rel_tol": args.tol, "bcp_flag": list(w.bcp_flag)}), flush=True)
+        proj.close()
     return 0
 
 
@@ -382,6 +419,8 @@ def main():
     ap.add_argument("--tol", type=float, default=1e-8)
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--n", type=int, default=None, help="smaller grid (profiling captures only)")
+    ap.add_argument("--sequence", type=int, default=0,
+                    help="time N warm-started calls with fresh predictions (e.g. --config c4 --sequence 20)")
     ap.add_argument("--only", choices=["mixed", "fp64"], default=None,
                     help="time one precision device-resident only (profiling captures)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
@@ -391,6 +430,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.sequence:
+        return run_sequence(args)
     return run_ours(args)
 
 

@@ -59,9 +59,9 @@ enum scf_status {
 /* ---- options ------------------------------------------------------------ */
 enum scf_precision {
     SCF_PREC_FP64 = 0,   /* FP64 CG with an FP64 multigrid preconditioner     */
-    SCF_PREC_MIXED = 1   /* FP64 iterative refinement around an FP32 CG with an
-                            FP32 multigrid preconditioner; FP64 dot products,
-                            FP64 outer residual and FP64 coarsest solve       */
+    SCF_PREC_MIXED = 1   /* FP64 CG (vectors, operator, dot products, true
+                            residual) with an FP32 multigrid V-cycle as the
+                            preconditioner; FP64 coarsest solve              */
 };
 
 typedef struct scf_opts {
@@ -69,10 +69,11 @@ typedef struct scf_opts {
     double  rel_tol;          /* stop when ||b-Ax||_2/||b||_2 <= rel_tol, with
                                  the FP64 operator (default 1e-10)             */
     int32_t max_iter;         /* cap on CG iterations, all rounds (default 500) */
-    int32_t max_rounds;       /* mixed: cap on refinement rounds (default 12)  */
-    double  inner_rtol;       /* mixed: residual reduction asked of one FP32
-                                 round (default 1e-4)                          */
-    int32_t smoother_degree;  /* Chebyshev degree per pre/post smoothing (2)   */
+    int32_t max_rounds;       /* cap on CG restarts from the true FP64 residual
+                                 (when the recursive residual has drifted from
+                                 it near the rounding floor), default 12       */
+    double  inner_rtol;       /* reserved (default 1e-4; not used)             */
+    int32_t smoother_degree;  /* Chebyshev degree per pre/post smoothing (3)   */
     int32_t coarse_max_cells; /* coarsen until a level has <= this many cells
                                  (default 64); solved densely in FP64          */
     double  rho_l, rho_g;     /* liquid/gas densities (StateVariables.f90:9)   */
@@ -101,7 +102,7 @@ typedef struct scf_opts {
 /* ---- per-call statistics -------------------------------------------------- */
 typedef struct scf_stats {
     int32_t iterations;       /* CG iterations (all rounds)                    */
-    int32_t rounds;           /* refinement rounds (mixed) or 1                */
+    int32_t rounds;           /* CG rounds: 1 + restarts from the true residual */
     int32_t converged;        /* 1 if rel_residual <= rel_tol                  */
     int32_t singular;         /* 1 if the system is all-Neumann (p defined up to
                                  a constant; the zero-mean solution is returned)*/
@@ -253,8 +254,9 @@ int scf_debug_time_kernel(scf_ctx *ctx, int kernel, int reps, double *ms_per_lau
  * by CUDA events on the context's stream (at most 512 launches per solve);
  * the elapsed times accumulate per class across runs.  Enabling or disabling
  * resets the totals.  _read returns the total device milliseconds, the
- * number of timed launches and the algorithmic bytes of one launch (the
- * byte model of scf_debug_time_kernel); any output may be NULL.            */
+ * number of timed launches and the mean algorithmic bytes of a timed launch
+ * (each array a launch reads or writes counted once per cell; the smoother's
+ * first and last steps move one array less); any output may be NULL.      */
 int scf_kernel_timing(scf_ctx *ctx, int enable);
 int scf_kernel_timing_read(scf_ctx *ctx, int kernel, double *ms_total, long long *launches,
                            double *bytes_per_launch);

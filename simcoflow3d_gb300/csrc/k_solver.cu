@@ -687,6 +687,18 @@ void mg_coarse_inverse(const MgLevel<T> &L, double *ainv, int *map, int n, bool 
     *launches += 1;
 }
 
+// Algorithmic bytes of one Chebyshev step on level F: b, x, diag, cE, cN,
+// cT (+ the stored inverse diagonal on FP64 levels) and the previous update
+// (absent in the first step, where it is x) read; x and, except in the last
+// step, the update written.
+template <typename T>
+double smooth_bytes(const MgLevel<T> &F, bool first, bool writes_d)
+{
+    const double cells = (double)F.n0 * F.n1 * F.n2;
+    const int arrays = 6 + (sizeof(T) == 8 ? 1 : 0) + (first ? 0 : 1) + 1 + (writes_d ? 1 : 0);
+    return arrays * sizeof(T) * cells;
+}
+
 template <typename T>
 T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, const int *map, int ncoarse,
              bool singular, bool first_done, cudaStream_t st, int *launches, KTimer *kt)
@@ -703,9 +715,12 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
             *launches += 1;
         }
         for (int s = 1; s < cc.degree; ++s) {
+            // the first step's previous update is x itself (zero guess); the
+            // last step's update is not needed by anything that follows
             const T *dprev = (s == 1) ? xa : F.d;
-            const int id = l == 0 ? kt_begin(kt, KC_SMOOTH, st) : -1;
-            k_cheb_step<T><<<lf.grid, lf.block, 0, st>>>(v, F.b, xa, dprev, xb, F.d, (T)cc.c1[s], (T)cc.c2[s]);
+            T *dout = (s == cc.degree - 1) ? nullptr : F.d;
+            const int id = l == 0 ? kt_begin(kt, KC_SMOOTH, st, smooth_bytes<T>(F, s == 1, dout != nullptr)) : -1;
+            k_cheb_step<T><<<lf.grid, lf.block, 0, st>>>(v, F.b, xa, dprev, xb, dout, (T)cc.c1[s], (T)cc.c2[s]);
             kt_end(kt, id, st);
             *launches += 1;
             T *tmp = xa; xa = xb; xb = tmp;
@@ -740,7 +755,7 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
         { T *tmp = xa; xa = xb; xb = tmp; }
         for (int s = 1; s < cc.degree; ++s) {
             const bool last_step = s == cc.degree - 1;
-            const int id = l == 0 ? kt_begin(kt, KC_SMOOTH, st) : -1;
+            const int id = l == 0 ? kt_begin(kt, KC_SMOOTH, st, smooth_bytes<T>(F, false, !last_step)) : -1;
             k_cheb_step<T><<<lf.grid, lf.block, 0, st>>>(v, F.b, xa, F.d, xb, last_step ? nullptr : F.d,
                                                          (T)cc.c1[s], (T)cc.c2[s]);
             kt_end(kt, id, st);

@@ -66,7 +66,7 @@ struct scf_ctx {
     double *xbest;             // best round-end iterate of a solve that restarts
     KTimer kt;                 // live per-launch timing (scf_kernel_timing)
     bool kt_events = false;
-    double kt_ms[KC_NUM] = {0}, kt_launches[KC_NUM] = {0};
+    double kt_ms[KC_NUM] = {0}, kt_launches[KC_NUM] = {0}, kt_bytes[KC_NUM] = {0};
     // multigrid
     int nlev = 0;
     int mg_precision = -1;
@@ -350,21 +350,6 @@ double read_scal(scf_ctx *ctx, int slot)
     return ctx->h_scal[0];
 }
 
-// Adds the elapsed times of the recorded event pairs to the per-class totals.
-void kt_harvest(scf_ctx *ctx)
-{
-    if (!ctx->kt.on || ctx->kt.n == 0) return;
-    cudaEventSynchronize(ctx->kt.ev[2 * ctx->kt.n - 1]);
-    for (int i = 0; i < ctx->kt.n; ++i) {
-        float ms = 0.f;
-        if (cudaEventElapsedTime(&ms, ctx->kt.ev[2 * i], ctx->kt.ev[2 * i + 1]) == cudaSuccess) {
-            ctx->kt_ms[ctx->kt.cls[i]] += ms;
-            ctx->kt_launches[ctx->kt.cls[i]] += 1.0;
-        }
-    }
-    ctx->kt.n = 0;
-}
-
 // Algorithmic bytes of one fine-level launch of a kernel class: each array
 // counted once per cell; FP32 levels derive 1/diag, FP64 levels read dinv.
 double kernel_bytes(const scf_ctx *ctx, int kernel)
@@ -377,9 +362,26 @@ double kernel_bytes(const scf_ctx *ctx, int kernel)
     case SCF_K_SPMV: return 6.0 * 8.0 * n;                                // p,diag,cE,cN,cT in; q out
     case SCF_K_RESTRICT: return 6.0 * s * n + s * n / 8.0;                // b,x,diag,cE,cN,cT in; coarse b out
     case SCF_K_PROLONG: return (mixed ? 8.0 : 9.0) * s * n + s * n / 8.0; // + coarse e; x,d out
-    case SCF_K_CGUPDATE: return (6.0 * 8.0 + (mixed ? 4.0 : 0.0)) * n;    // x,r,p,q in; x,r,[rlow],x0 out
+    case SCF_K_CGUPDATE: return (mixed ? 60.0 : 64.0) * n;                // x,r,p,q,diag|dinv in; x,r,[rlow],x0 out
     default: return -1.0;
     }
+}
+
+// Adds the elapsed times of the recorded event pairs to the per-class totals.
+void kt_harvest(scf_ctx *ctx)
+{
+    if (!ctx->kt.on || ctx->kt.n == 0) return;
+    cudaEventSynchronize(ctx->kt.ev[2 * ctx->kt.n - 1]);
+    for (int i = 0; i < ctx->kt.n; ++i) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, ctx->kt.ev[2 * i], ctx->kt.ev[2 * i + 1]) == cudaSuccess) {
+            const int c = ctx->kt.cls[i];
+            ctx->kt_ms[c] += ms;
+            ctx->kt_launches[c] += 1.0;
+            ctx->kt_bytes[c] += ctx->kt.bytes[i] >= 0.0 ? ctx->kt.bytes[i] : kernel_bytes(ctx, c);
+        }
+    }
+    ctx->kt.n = 0;
 }
 
 template <typename T>
@@ -1127,7 +1129,7 @@ int scf_kernel_timing(scf_ctx *ctx, int enable)
     }
     ctx->kt.on = enable != 0;
     ctx->kt.n = 0;
-    for (int c = 0; c < KC_NUM; ++c) ctx->kt_ms[c] = ctx->kt_launches[c] = 0.0;
+    for (int c = 0; c < KC_NUM; ++c) ctx->kt_ms[c] = ctx->kt_launches[c] = ctx->kt_bytes[c] = 0.0;
     return SCF_OK;
 }
 
@@ -1138,7 +1140,9 @@ int scf_kernel_timing_read(scf_ctx *ctx, int kernel, double *ms_total, long long
     if (kernel < 0 || kernel >= KC_NUM) return SCF_ERR_BAD_ARG;
     if (ms_total) *ms_total = ctx->kt_ms[kernel];
     if (launches) *launches = (long long)ctx->kt_launches[kernel];
-    if (bytes_per_launch) *bytes_per_launch = kernel_bytes(ctx, kernel);
+    if (bytes_per_launch)
+        *bytes_per_launch = ctx->kt_launches[kernel] > 0.0 ? ctx->kt_bytes[kernel] / ctx->kt_launches[kernel]
+                                                            : kernel_bytes(ctx, kernel);
     return SCF_OK;
 }
 

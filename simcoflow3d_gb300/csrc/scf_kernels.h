@@ -85,12 +85,14 @@ struct KTimer {
     static constexpr int CAP = 512;
     cudaEvent_t ev[2 * CAP];
     int cls[CAP];
+    double bytes[CAP];     // algorithmic bytes of the launch (< 0: the class's model)
     int n = 0;
     bool on = false;
-    int begin(int c, cudaStream_t st)
+    int begin(int c, cudaStream_t st, double b = -1.0)
     {
         if (!on || n >= CAP) return -1;
         cls[n] = c;
+        bytes[n] = b;
         cudaEventRecord(ev[2 * n], st);
         return n++;
     }
@@ -99,7 +101,10 @@ struct KTimer {
         if (id >= 0) cudaEventRecord(ev[2 * id + 1], st);
     }
 };
-inline int kt_begin(KTimer *kt, int c, cudaStream_t st) { return kt ? kt->begin(c, st) : -1; }
+inline int kt_begin(KTimer *kt, int c, cudaStream_t st, double bytes = -1.0)
+{
+    return kt ? kt->begin(c, st, bytes) : -1;
+}
 inline void kt_end(KTimer *kt, int id, cudaStream_t st)
 {
     if (kt) kt->end(id, st);

@@ -148,14 +148,15 @@ class Projection:
         self._check(rc, (capi.SCF_ERR_NOT_CONVERGED,) if allow_not_converged else ())
         return pc, pp, st.as_dict()
 
-    def update_puvw(self, w, tvar=None, want_bc: bool = True, allow_not_converged: bool = False):
+    def update_puvw(self, w, tvar=None, want_bc: bool = True, allow_not_converged: bool = False, pred=None):
         """UpdatePUVW's projection: returns (u, v, w, p, bcvar[4][6] or None, stats).
-        ``tvar`` defaults to copies of the workload's TVar arrays."""
+        ``tvar`` defaults to copies of the workload's TVar arrays; ``pred``
+        optionally replaces the workload's (u*, v*, w*)."""
         a = w.arrays
         if tvar is None:
             tvar = [a[k].copy(order="F") for k in ("tvar_u", "tvar_v", "tvar_w", "tvar_p")]
         u, v, ww, p = tvar
-        pin = capi.poisson_in(w)
+        pin = capi.poisson_in(w, pred)
         cin = capi.correct_in(w)
         bc_struct, bc = (capi.new_bc_out(*self.shape) if want_bc else (None, None))
         st = capi.ScfStats()
@@ -166,9 +167,10 @@ class Projection:
         return u, v, ww, p, bc, st.as_dict()
 
     # -- split API ---------------------------------------------------------------
-    def stage(self, w, tvar=None, correction: bool = True):
+    def stage(self, w, tvar=None, correction: bool = True, pred=None):
         a = w.arrays
-        self._pin = capi.poisson_in(w)
+        self._pred = pred
+        self._pin = capi.poisson_in(w, pred)
         if correction:
             if tvar is None:
                 tvar = [a[k] for k in ("tvar_u", "tvar_v", "tvar_w", "tvar_p")]

@@ -497,6 +497,61 @@ def _smoothed_velocity(rng, shape_g, sigma=0.1, passes=3):
     return f
 
 
+def _consistent_velocity(us, vs, ws, bcp_flag, ct_u, ct_v, ct_w):
+    """Wall-normal velocity zero on Neumann-pressure walls and no velocity in
+    solid velocity cells (in place)."""
+    I, J, K = us.shape[0] - 2, us.shape[1] - 2, us.shape[2] - 2
+    if bcp_flag[0] == 1: us[0, :, :] = 0.0
+    if bcp_flag[1] == 1: us[I, :, :] = 0.0; us[I + 1, :, :] = 0.0
+    if bcp_flag[2] == 1: vs[:, 0, :] = 0.0
+    if bcp_flag[3] == 1: vs[:, J, :] = 0.0; vs[:, J + 1, :] = 0.0
+    if bcp_flag[4] == 1: ws[:, :, 0] = 0.0
+    if bcp_flag[5] == 1: ws[:, :, K] = 0.0; ws[:, :, K + 1] = 0.0
+    us[1:-1, 1:-1, 1:-1][ct_u == 2] = 0.0
+    vs[1:-1, 1:-1, 1:-1][ct_v == 2] = 0.0
+    ws[1:-1, 1:-1, 1:-1][ct_w == 2] = 0.0
+
+
+def perturbed_prediction(w, seed: int, amp: float = 0.1):
+    """(u*, v*, w*) of workload ``w`` plus ``amp`` times a fresh seeded field
+    of the same kind (N(0, 0.1^2), three Jacobi passes), made consistent with
+    the walls and the solid like the original: the next call of a sequence of
+    projections on a fixed geometry."""
+    rng = np.random.default_rng(seed)
+    a = w.arrays
+    out = []
+    for key in ("u_star", "v_star", "w_star"):
+        out.append(np.asfortranarray(a[key] + amp * _smoothed_velocity(rng, w.shape_g)))
+    _consistent_velocity(*out, w.bcp_flag, a["ucell_cell_type"], a["vcell_cell_type"], a["wcell_cell_type"])
+    return tuple(out)
+
+
+class PredictionSequence:
+    """Seeded predictions for a sequence of calls on one geometry, cheap at
+    full size: call c gets the workload's (u*, v*, w*) plus ``amp`` times a
+    combination of ``pool`` smoothed fields (generated once) with N(0, 1/pool)
+    coefficients drawn from seed + c, made consistent with walls and solid."""
+
+    def __init__(self, w, seed: int, pool: int = 4, amp: float = 0.1):
+        self.w, self.seed, self.amp = w, seed, amp
+        rng = np.random.default_rng(seed)
+        self.fields = [[_smoothed_velocity(rng, w.shape_g) for _ in range(3)] for _ in range(pool)]
+
+    def __call__(self, call: int):
+        a = self.w.arrays
+        xi = np.random.default_rng(self.seed + 1 + call).normal(0.0, 1.0 / np.sqrt(len(self.fields)),
+                                                                 size=len(self.fields))
+        out = []
+        for comp, key in enumerate(("u_star", "v_star", "w_star")):
+            f = a[key].copy(order="F")
+            for m, fm in enumerate(self.fields):
+                f += (self.amp * xi[m]) * fm[comp]
+            out.append(f)
+        _consistent_velocity(*out, self.w.bcp_flag, a["ucell_cell_type"], a["vcell_cell_type"],
+                             a["wcell_cell_type"])
+        return tuple(out)
+
+
 def build_workload(name: str, imax: int, jmax: int, kmax: int, *,
                    extent=((0.0, 1.0), (0.0, 1.0), (0.0, 1.0)),
                    zstretch: Optional[float] = None,
@@ -578,17 +633,7 @@ def build_workload(name: str, imax: int, jmax: int, kmax: int, *,
     us = _smoothed_velocity(rng, shg)
     vs = _smoothed_velocity(rng, shg)
     ws = _smoothed_velocity(rng, shg)
-    # wall-normal velocity zero on Neumann-pressure walls (consistency)
-    if bcp_flag[0] == 1: us[0, :, :] = 0.0
-    if bcp_flag[1] == 1: us[I, :, :] = 0.0; us[I + 1, :, :] = 0.0
-    if bcp_flag[2] == 1: vs[:, 0, :] = 0.0
-    if bcp_flag[3] == 1: vs[:, J, :] = 0.0; vs[:, J + 1, :] = 0.0
-    if bcp_flag[4] == 1: ws[:, :, 0] = 0.0
-    if bcp_flag[5] == 1: ws[:, :, K] = 0.0; ws[:, :, K + 1] = 0.0
-    # solid velocity cells carry no velocity
-    us[1:-1, 1:-1, 1:-1][ct_u == 2] = 0.0
-    vs[1:-1, 1:-1, 1:-1][ct_v == 2] = 0.0
-    ws[1:-1, 1:-1, 1:-1][ct_w == 2] = 0.0
+    _consistent_velocity(us, vs, ws, bcp_flag, ct_u, ct_v, ct_w)
 
     vof_old = vof_g.copy(order="F")
     if perturb_vof_old:

@@ -1,0 +1,39 @@
+"""A sequence of projections on a fixed geometry (the wave-tank workload:
+512x256x256 in full, here 2n x n x n, z-stretched, vertical cylinder, free
+surface, Dirichlet-p top): each call gets a freshly seeded prediction and
+starts from the previous call's pressure.  Every call must reach the
+tolerance in both precisions, the warm-started pressure must match a cold
+FP64 solve of the same call, and warm starts must not cost iterations."""
+import numpy as np
+import pytest
+
+from simcoflow3d_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_warm_started_sequence_wave_tank(gpu_lib, precision):
+    from simcoflow3d_gb300.projection import Projection
+    w = W.config("c4", n=24)
+    assert w.bcp_flag[5] == 0
+    seq = Projection.for_workload(w, rel_tol=1e-8, precision=precision, warm_start=1)
+    cold = Projection.for_workload(w, rel_tol=1e-8, precision=0)
+    act = w.arrays["cell_type"] != 2
+    its_warm, its_cold = [], []
+    for call in range(20):
+        pred = W.perturbed_prediction(w, seed=4000 + call)
+        seq.stage(w, pred=pred)
+        st = seq.run()
+        assert st["converged"] == 1 and st["rel_residual"] <= 1e-8
+        its_warm.append(st["iterations"])
+        pw = np.zeros(w.shape_g, order="F")
+        seq.fetch(pp=pw)
+        cold.stage(w, pred=pred)
+        sc = cold.run()
+        its_cold.append(sc["iterations"])
+        pc = np.zeros(w.shape_g, order="F")
+        cold.fetch(pp=pc)
+        d = (pw - pc)[1:-1, 1:-1, 1:-1][act]
+        assert np.abs(d).max() <= 1e-5 * np.abs(pc[1:-1, 1:-1, 1:-1][act]).max(), call
+    assert sum(its_warm[1:]) <= sum(its_cold[1:])
