@@ -229,6 +229,10 @@ int scf_loss_backward(scf_ctx *ctx, double *grad_u, double *grad_v, double *grad
 /* y = A x on active cells, with the FP64 operator as stored on the device;
  * x and y are ghosted FP64 host arrays (ghost/solid entries of y are 0).    */
 int scf_debug_apply(scf_ctx *ctx, const double *x, double *y);
+/* z = M r: one V-cycle of the last run's multigrid hierarchy, in the
+ * context's precision.  r and z are ghosted FP64 host arrays; z is 0 off the
+ * active cells.  Needs a previous run.                                      */
+int scf_debug_precondition(scf_ctx *ctx, const double *r, double *z);
 /* Device operator: diag and the E/N/T couplings of each cell (interior
  * arrays; coupling = |off-diagonal| of row c towards c+e, 0 if none), and
  * the right-hand side b (interior, 0 on solid cells).  Any may be NULL.     */

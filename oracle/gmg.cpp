@@ -25,6 +25,7 @@
 #include <cstring>
 #include <vector>
 #include <algorithm>
+#include <type_traits>
 #ifdef _OPENMP
 #include <omp.h>
 #endif
@@ -590,6 +591,55 @@ done:
     prm->rounds = rounds;
     prm->rel_residual = relres;
     return relres <= prm->rel_tol ? 0 : 2;
+}
+
+// One V-cycle of the hierarchy built from (in, pocoef): z = M r.  r and z
+// are ghosted FP64 arrays ((I+2)(J+2)(K+2), the level-0 padded layout); r is
+// read on the active cells only, z is 0 elsewhere.  prm->precision selects
+// the FP64 (0) or FP32 (1) V-cycle; prm->degree, ratio and coarse_max as in
+// oracle_gmg_solve.  This is the reference of the device V-cycle's parity
+// test.
+int oracle_gmg_vcycle(int I, int J, int K, const scf_poisson_in *in, const double *pocoef, const double *r,
+                      double *z, oracle_gmg_params *prm)
+{
+    std::vector<Level> lv(1);
+    std::vector<double> b;
+    std::vector<double> zero_rhs((size_t)in->pcell_extcell + 1, 0.0);
+    build_level0(I, J, K, in, pocoef, zero_rhs.data(), lv[0], b);
+    bool singular = true;
+    for (int q = 0; q < 6; ++q)
+        if (in->bcp_flag[q] == 0) singular = false;
+    while ((size_t)lv.back().n[0] * lv.back().n[1] * lv.back().n[2] > (size_t)prm->coarse_max &&
+           (lv.back().n[0] > 2 || lv.back().n[1] > 2 || lv.back().n[2] > 2)) {
+        lv.emplace_back();
+        coarsen(lv[lv.size() - 2], lv.back());
+    }
+    prm->levels = (int)lv.size();
+    Params P;
+    P.degree = prm->degree;
+    P.ratio = prm->ratio;
+    const Level &L0 = lv[0];
+    auto run = [&](auto &H) {
+        H.lv = &lv;
+        H.m.resize(lv.size());
+        for (size_t l = 0; l < lv.size(); ++l) load_level(lv[l], H.m[l]);
+        coarse_factor(lv.back(), H.coarse, singular);
+        H.singular = singular;
+        H.P = P;
+        auto &M = H.m[0];
+        using TT = typename std::remove_reference<decltype(M.x[0])>::type;
+        for (size_t c = 0; c < L0.tot; ++c) M.b[c] = L0.active[c] ? (TT)r[c] : TT(0);
+        vcycle(H, 0);
+        for (size_t c = 0; c < L0.tot; ++c) z[c] = L0.active[c] ? (double)M.x[c] : 0.0;
+    };
+    if (prm->precision == 0) {
+        Hier<double> H;
+        run(H);
+    } else {
+        Hier<float> H;
+        run(H);
+    }
+    return 0;
 }
 
 }  // extern "C"

@@ -146,6 +146,18 @@ def gmg_solve(w, pc, b, precision=0, rel_tol=1e-13, max_iter=400, degree=2, rati
     return x, st
 
 
+def gmg_vcycle(w, pc, r, precision=0, degree=3, ratio=6.0, coarse_max=64):
+    """One CPU V-cycle z = M r of the multigrid hierarchy of (w, pc); r and z
+    ghosted FP64 arrays."""
+    I, J, K = w.imax, w.jmax, w.kmax
+    z = np.zeros(w.shape_g, order="F")
+    prm = GmgParams(precision=precision, degree=degree, ratio=ratio, coarse_max=coarse_max)
+    s = capi.poisson_in(w)
+    rr = np.asfortranarray(r, dtype=np.float64)
+    lib().oracle_gmg_vcycle(I, J, K, C.byref(s), _dp(pc), _dp(rr), _dp(z), C.byref(prm))
+    return z
+
+
 def scatter(w, x, pp0: Optional[np.ndarray] = None):
     """DeltaPressureGetValues + DeltaPressureBoundaryCondition."""
     I, J, K = w.imax, w.jmax, w.kmax

@@ -1043,6 +1043,31 @@ int scf_debug_apply(scf_ctx *ctx, const double *xh, double *yh)
     return SCF_OK;
 }
 
+int scf_debug_precondition(scf_ctx *ctx, const double *rh, double *zh)
+{
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (!rh || !zh) return SCF_ERR_BAD_ARG;
+    if (!ctx->solved) { set_err(ctx, "no projection has run"); return SCF_ERR_NO_SOLVE; }
+    const Dims &d = ctx->d;
+    const ChebCoef cc = cheb_coef(ctx->opts.smoother_degree);
+    CK(cudaMemcpyAsync(ctx->r, rh, sizeof(double) * d.ng, cudaMemcpyHostToDevice, ctx->st));
+    if (ctx->opts.precision == SCF_PREC_FP64) {
+        const double *z = precondition<double>(ctx, ctx->L64, cc, false);
+        CK(cudaMemcpyAsync(zh, z, sizeof(double) * d.ng, cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+    } else {
+        copy_to_low(fine_view(ctx), ctx->r, ctx->L32[0].b, ctx->st, &ctx->launches);
+        const float *z = precondition<float>(ctx, ctx->L32, cc, false);
+        std::vector<float> zf(d.ng);
+        CK(cudaMemcpyAsync(zf.data(), z, sizeof(float) * d.ng, cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        for (int c = 0; c < d.ng; ++c) zh[c] = zf[c];
+    }
+    ctx->warm_ok = false;  // r was overwritten
+    return SCF_OK;
+}
+
 int scf_debug_operator(scf_ctx *ctx, double *diag, double *cpl_e, double *cpl_n, double *cpl_t, double *rhs)
 {
     int rc = check_ctx(ctx);

@@ -56,6 +56,7 @@ def load_library(path: Optional[str] = None):
                                     capi.c_double_p, capi.c_double_p, capi.c_double_p, P(capi.ScfBcOut)]
     L.scf_debug_apply.argtypes = [C.c_void_p, capi.c_double_p, capi.c_double_p]
     L.scf_debug_operator.argtypes = [C.c_void_p] + [capi.c_double_p] * 5
+    L.scf_debug_precondition.argtypes = [C.c_void_p, capi.c_double_p, capi.c_double_p]
     L.scf_status_string.argtypes = [C.c_int]
     L.scf_status_string.restype = C.c_char_p
     L.scf_last_error.argtypes = [C.c_void_p, C.c_char_p, C.c_size_t]
@@ -225,6 +226,12 @@ class Projection:
         ms, by = C.c_double(), C.c_double()
         self._check(self.L.scf_debug_time_kernel(self.ctx, int(kernel), int(reps), C.byref(ms), C.byref(by)))
         return ms.value, by.value
+
+    def debug_precondition(self, r: np.ndarray) -> np.ndarray:
+        """z = M r, one V-cycle of the last run's hierarchy (ghosted arrays)."""
+        z = np.zeros_like(r, order="F")
+        self._check(self.L.scf_debug_precondition(self.ctx, capi.dptr(np.asfortranarray(r)), capi.dptr(z)))
+        return z
 
     def kernel_timing(self, enable: bool = True):
         """Starts (or stops) live per-launch timing; resets the totals."""
