@@ -327,7 +327,7 @@ __global__ void __launch_bounds__(128) k_operator(AsmArgs a, OpArgs o)
     unsigned long long rt[6] = {0, 0, 0, 0, 0, 0};
     bool rvalid = false;
     double dg = 0.0, dinv = 0.0;
-    float d32 = 0.f, di32 = 0.f;
+    float d32 = 0.f;
     // memo of the spacing products of the rhs
     unsigned long long pdx = 0, pdy = 0, pdz = 0;
     double dydz = 0.0, dxdz = 0.0, dxdy = 0.0, dxdydz = 0.0;
@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(128) k_operator(AsmArgs a, OpArgs o)
             o.diag[g] = -1.0; o.dinv[g] = 0.0; o.cE[g] = 0.0; o.cN[g] = 0.0; o.cT[g] = 0.0;
             o.extra[g] = 0.0; o.b[g] = 0.0; o.active[g] = 0;
             if (MIXED) {
-                o.diag32[g] = -1.0f; o.dinv32[g] = 0.0f; o.cE32[g] = 0.0f; o.cN32[g] = 0.0f; o.cT32[g] = 0.0f;
+                o.diag32[g] = -1.0f; o.cE32[g] = 0.0f; o.cN32[g] = 0.0f; o.cT32[g] = 0.0f;
                 o.extra32[g] = 0.0f;
             }
             continue;
@@ -366,7 +366,7 @@ __global__ void __launch_bounds__(128) k_operator(AsmArgs a, OpArgs o)
             if (fl[5] == 1 && k == d.K) v = v - t6;
             dg = v;
             if (!MIXED) dinv = dg > 0.0 ? 1.0 / dg : 0.0;
-            if (MIXED) { d32 = (float)dg; di32 = d32 > 0.0f ? 1.0f / d32 : 0.0f; }
+            if (MIXED) d32 = (float)dg;
             // a boundary row is never reused by an interior one
             rvalid = !bnd;
             rt[0] = bits(t1); rt[1] = bits(t2); rt[2] = bits(t3); rt[3] = bits(t4); rt[4] = bits(t5); rt[5] = bits(t6);
@@ -417,7 +417,6 @@ __global__ void __launch_bounds__(128) k_operator(AsmArgs a, OpArgs o)
         o.active[g] = 1;
         if (MIXED) {
             o.diag32[g] = d32;
-            o.dinv32[g] = di32;
             o.cE32[g] = (float)cE; o.cN32[g] = (float)cN; o.cT32[g] = (float)cT;
             o.extra32[g] = (float)ex;
         }

@@ -60,7 +60,7 @@ struct scf_ctx {
     // level-0 operator, FP64
     double *diag, *dinv, *cE, *cN, *cT, *extra, *b;
     unsigned char *active;
-    float *diag32, *dinv32, *cE32, *cN32, *cT32, *extra32;
+    float *diag32, *cE32, *cN32, *cT32, *extra32;
     // CG vectors
     double *x, *r, *p, *q;
     double *xbest;             // best round-end iterate of a solve that restarts
@@ -217,13 +217,12 @@ int ensure_mg(scf_ctx *ctx)
         if (rc) return rc;
         MgLevel<float> &L0 = ctx->L32[0];
         DALLOC(ctx->mgmem, ctx->diag32, L0.tot);
-        DALLOC(ctx->mgmem, ctx->dinv32, L0.tot);
         DALLOC(ctx->mgmem, ctx->cE32, L0.tot);
         DALLOC(ctx->mgmem, ctx->cN32, L0.tot);
         DALLOC(ctx->mgmem, ctx->cT32, L0.tot);
         DALLOC(ctx->mgmem, ctx->extra32, L0.tot);
         DALLOC(ctx->mgmem, L0.b, L0.tot);
-        L0.diag = ctx->diag32; L0.dinv = ctx->dinv32; L0.cE = ctx->cE32; L0.cN = ctx->cN32; L0.cT = ctx->cT32;
+        L0.diag = ctx->diag32; L0.dinv = nullptr; L0.cE = ctx->cE32; L0.cN = ctx->cN32; L0.cT = ctx->cT32;
         L0.extra = ctx->extra32; L0.active = ctx->active;
     }
     // coarsest dense map
@@ -304,7 +303,7 @@ int assemble(scf_ctx *ctx)
     o.diag = ctx->diag; o.dinv = ctx->dinv; o.cE = ctx->cE; o.cN = ctx->cN; o.cT = ctx->cT;
     o.extra = ctx->extra; o.b = ctx->b; o.active = ctx->active;
     const bool mixed = ctx->opts.precision == SCF_PREC_MIXED;
-    o.diag32 = ctx->diag32; o.dinv32 = ctx->dinv32; o.cE32 = ctx->cE32; o.cN32 = ctx->cN32; o.cT32 = ctx->cT32;
+    o.diag32 = ctx->diag32; o.cE32 = ctx->cE32; o.cN32 = ctx->cN32; o.cT32 = ctx->cT32;
     o.extra32 = ctx->extra32;
     const double rho_ref = ctx->opts.rho_ref > 0.0 ? ctx->opts.rho_ref : ctx->opts.rho_l;
     int e = launch_assemble(a, o, mixed, ctx->use_rho ? ctx->adj_rho : nullptr, rho_ref, ctx->st, ctx->h_u32,

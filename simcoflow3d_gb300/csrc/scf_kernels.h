@@ -34,7 +34,7 @@ struct AsmArgs {
 struct OpArgs {
     double *diag, *dinv, *cE, *cN, *cT, *extra, *b;
     unsigned char *active;
-    float *diag32, *dinv32, *cE32, *cN32, *cT32, *extra32;  // mixed only
+    float *diag32, *cE32, *cN32, *cT32, *extra32;  // mixed only (FP32 levels derive 1/diag)
 };
 
 // rho: per-cell densities (ghosted) or nullptr for the reference's two-phase
