@@ -518,6 +518,20 @@ __global__ void __launch_bounds__(256) k_post_first(LevelView<T> F, const T *__r
     if (dout) dout[c] = dn;
 }
 
+// x += e(parent) on the active cells (piecewise-constant prolongation of
+// the coarse correction, in place); on large levels this and a plain first
+// Chebyshev step replace k_post_first, whose seven recomputed neighbour
+// prolongations cost more than one extra pass over x.
+template <typename T>
+__global__ void __launch_bounds__(256) k_prolong(LevelView<T> F, const unsigned char *__restrict__ act,
+                                                 T *__restrict__ x, LevelView<T> C, const T *__restrict__ e, int s0,
+                                                 int s1, int s2)
+{
+    INTERIOR_IJK(F);
+    if (!in || !act[c]) return;
+    x[c] += e[(((i - 1) >> s0) + 1) + C.sy * (((j - 1) >> s1) + 1) + C.sz * (((k - 1) >> s2) + 1)];
+}
+
 // coarsest level: y = Ainv (b - mean) on the active cells (one block)
 template <typename T>
 __global__ void __launch_bounds__(128) k_coarse_solve(const T *__restrict__ b, T *__restrict__ x,
@@ -699,6 +713,18 @@ double smooth_bytes(const MgLevel<T> &F, bool first, bool writes_d)
     return arrays * sizeof(T) * cells;
 }
 
+// Algorithmic bytes of the split prolongation + first post-smoothing step:
+// x read and written, the active mask and the coarse correction read; then
+// b, x, diag, cE, cN, cT (+ dinv on FP64 levels) read, x (+ the update)
+// written.
+template <typename T>
+double prolong_bytes(const MgLevel<T> &F, bool writes_d)
+{
+    const double cells = (double)F.n0 * F.n1 * F.n2;
+    const double s = sizeof(T);
+    return cells * (2.0 * s + 1.0 + s / 8.0 + (6 + (sizeof(T) == 8 ? 1 : 0) + 1 + (writes_d ? 1 : 0)) * s);
+}
+
 template <typename T>
 T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, const int *map, int ncoarse,
              bool singular, bool first_done, cudaStream_t st, int *launches, KTimer *kt)
@@ -747,11 +773,22 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
         T *xa = cur[l];
         T *xb = (xa == F.x) ? F.xb : F.x;
         const bool more = cc.degree > 1;
-        const int idp = l == 0 ? kt_begin(kt, KC_PROLONG, st) : -1;
-        k_post_first<T><<<lf.grid, lf.block, 0, st>>>(v, F.b, xa, C.view(), cur[l + 1], xb, more ? F.d : nullptr,
-                                                      F.f0, F.f1, F.f2, (T)cc.first);
-        kt_end(kt, idp, st);
-        *launches += 1;
+        if ((long long)F.n0 * F.n1 * F.n2 >= (1LL << 18)) {
+            const int idp = l == 0 ? kt_begin(kt, KC_PROLONG, st, prolong_bytes<T>(F, more)) : -1;
+            k_prolong<T><<<lf.grid, lf.block, 0, st>>>(v, F.active, xa, C.view(), cur[l + 1], F.f0 - 1, F.f1 - 1,
+                                                       F.f2 - 1);
+            // first post-smoothing step from x: the previous update term is 0
+            k_cheb_step<T><<<lf.grid, lf.block, 0, st>>>(v, F.b, xa, xa, xb, more ? F.d : nullptr, T(0),
+                                                         (T)cc.first);
+            kt_end(kt, idp, st);
+            *launches += 2;
+        } else {
+            const int idp = l == 0 ? kt_begin(kt, KC_PROLONG, st) : -1;
+            k_post_first<T><<<lf.grid, lf.block, 0, st>>>(v, F.b, xa, C.view(), cur[l + 1], xb, more ? F.d : nullptr,
+                                                          F.f0, F.f1, F.f2, (T)cc.first);
+            kt_end(kt, idp, st);
+            *launches += 1;
+        }
         { T *tmp = xa; xa = xb; xb = tmp; }
         for (int s = 1; s < cc.degree; ++s) {
             const bool last_step = s == cc.degree - 1;

@@ -65,6 +65,12 @@ struct scf_ctx {
     double *x, *r, *p, *q;
     double *xbest;             // best round-end iterate of a solve that restarts
     KTimer kt;                 // live per-launch timing (scf_kernel_timing)
+    // captured CG iteration (V-cycle, direction update, SpMV, x/r update)
+    cudaGraphExec_t iter_exec = nullptr;
+    unsigned long long iter_key = 0;
+    int iter_launches = 0;     // kernels in one replay
+    bool graphs_ok = true;     // cleared if capture is not available
+    unsigned mg_gen = 0;       // bumped whenever the hierarchy is reallocated
     bool kt_events = false;
     double kt_ms[KC_NUM] = {0}, kt_launches[KC_NUM] = {0}, kt_bytes[KC_NUM] = {0};
     // multigrid
@@ -203,6 +209,8 @@ int ensure_mg(scf_ctx *ctx)
     const int prec = ctx->opts.precision;
     if (ctx->mg_precision == prec) return SCF_OK;
     ctx->mgmem.release();
+    ctx->mg_gen++;
+    if (ctx->iter_exec) { cudaGraphExecDestroy(ctx->iter_exec); ctx->iter_exec = nullptr; }
     int dims[32][3], fac[32][3];
     plan_levels(ctx, dims, fac);
     int rc;
@@ -366,12 +374,10 @@ double kernel_bytes(const scf_ctx *ctx, int kernel)
     }
 }
 
-// Adds the elapsed times of the recorded event pairs to the per-class totals.
-void kt_harvest(scf_ctx *ctx)
+// Adds the elapsed times of event pairs [a, b) to the per-class totals.
+void kt_add(scf_ctx *ctx, int a, int b)
 {
-    if (!ctx->kt.on || ctx->kt.n == 0) return;
-    cudaEventSynchronize(ctx->kt.ev[2 * ctx->kt.n - 1]);
-    for (int i = 0; i < ctx->kt.n; ++i) {
+    for (int i = a; i < b; ++i) {
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, ctx->kt.ev[2 * i], ctx->kt.ev[2 * i + 1]) == cudaSuccess) {
             const int c = ctx->kt.cls[i];
@@ -380,7 +386,22 @@ void kt_harvest(scf_ctx *ctx)
             ctx->kt_bytes[c] += ctx->kt.bytes[i] >= 0.0 ? ctx->kt.bytes[i] : kernel_bytes(ctx, c);
         }
     }
+    cudaGetLastError();
+}
+
+// Eagerly recorded pairs (after the stream has been synchronised).
+void kt_harvest(scf_ctx *ctx)
+{
+    if (!ctx->kt.on || ctx->kt.n == 0) return;
+    cudaEventSynchronize(ctx->kt.ev[2 * ctx->kt.n - 1]);
+    kt_add(ctx, 0, ctx->kt.n);
     ctx->kt.n = 0;
+}
+
+// The pairs of the captured iteration graph, after one replay has finished.
+void kt_harvest_graph(scf_ctx *ctx)
+{
+    if (ctx->kt.on && ctx->kt.ng > KTimer::EAGER) kt_add(ctx, KTimer::EAGER, ctx->kt.ng);
 }
 
 template <typename T>
@@ -388,6 +409,66 @@ T *precondition(scf_ctx *ctx, MgLevel<T> *L, const ChebCoef &cc, bool first_done
 {
     return mg_vcycle<T>(L, ctx->nlev, cc, ctx->ainv, ctx->map, ctx->ncoarse, is_singular(ctx), first_done,
                         ctx->st, &ctx->launches, ctx->kt.on ? &ctx->kt : nullptr);
+}
+
+// The part of a CG iteration after the stopping test: precondition, new
+// search direction, SpMV with (p, Ap) and the x/r update with (r, r).  Its
+// kernel sequence is fixed for a context, so it is captured once as a CUDA
+// graph and replayed (one launch instead of ~50, which matters on the small
+// coarse levels); the capture is redone when anything it bakes in changes.
+template <typename T>
+void iteration_kernels(scf_ctx *ctx, MgLevel<T> *L, const ChebCoef &cc, bool singular)
+{
+    const LevelView<double> A = fine_view(ctx);
+    const bool mixed = sizeof(T) == 4;
+    float *rlow = mixed ? (float *)L[0].b : nullptr;
+    KTimer *kt = ctx->kt.on ? &ctx->kt : nullptr;
+    T *z = precondition<T>(ctx, L, cc, ctx->nlev > 1);
+    cg_dot_rz<T>(A, ctx->r, (const T *)L[0].b, z, ctx->R, ctx->st, &ctx->launches);
+    cg_pupdate<T>(A, z, ctx->p, ctx->R.scal, false, ctx->st, &ctx->launches);
+    cg_spmv_dot(A, ctx->p, ctx->q, ctx->R, singular, ctx->st, &ctx->launches, kt);
+    const bool fuse = ctx->nlev > 1;
+    cg_update<T>(A, ctx->x, ctx->r, ctx->p, ctx->q, (T *)(mixed ? (void *)rlow : nullptr), L[0].view(),
+                 fuse ? L[0].x : nullptr, cc.first, ctx->R, ctx->st, &ctx->launches, kt);
+}
+
+template <typename T>
+void run_iteration(scf_ctx *ctx, MgLevel<T> *L, const ChebCoef &cc, bool singular)
+{
+    const unsigned long long key = 1ull + (unsigned long long)ctx->mg_gen * 1000003ull +
+                                   (unsigned long long)cc.degree * 131ull + (singular ? 7ull : 0ull) +
+                                   (ctx->kt.on ? 3ull : 0ull) + (sizeof(T) == 4 ? 11ull : 0ull) +
+                                   (unsigned long long)ctx->nlev * 17ull;
+    if (ctx->graphs_ok && (!ctx->iter_exec || ctx->iter_key != key)) {
+        if (ctx->iter_exec) { cudaGraphExecDestroy(ctx->iter_exec); ctx->iter_exec = nullptr; }
+        cudaGraph_t g = nullptr;
+        const int before = ctx->launches;
+        ctx->kt.ng = KTimer::EAGER;
+        ctx->kt.capturing = ctx->kt.on;
+        bool ok = cudaStreamBeginCapture(ctx->st, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        if (ok) iteration_kernels<T>(ctx, L, cc, singular);
+        ok = (cudaStreamEndCapture(ctx->st, &g) == cudaSuccess) && ok && g;
+        ctx->kt.capturing = false;
+        ctx->iter_launches = ctx->launches - before;
+        ctx->launches = before;
+        if (ok) ok = cudaGraphInstantiate(&ctx->iter_exec, g, 0) == cudaSuccess;
+        if (g) cudaGraphDestroy(g);
+        if (!ok) {
+            cudaGetLastError();
+            if (ctx->iter_exec) { cudaGraphExecDestroy(ctx->iter_exec); ctx->iter_exec = nullptr; }
+            ctx->graphs_ok = false;
+            ctx->kt.ng = KTimer::EAGER;
+        } else {
+            ctx->iter_key = key;
+        }
+    }
+    if (ctx->graphs_ok && ctx->iter_exec && cudaGraphLaunch(ctx->iter_exec, ctx->st) == cudaSuccess) {
+        ctx->launches += ctx->iter_launches;
+        return;
+    }
+    cudaGetLastError();
+    ctx->kt.ng = KTimer::EAGER;
+    iteration_kernels<T>(ctx, L, cc, singular);
 }
 
 // Iterations without a new smallest CG residual after which a round of the
@@ -440,7 +521,8 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
         stalled = false;
         double best = HUGE_VAL;
         int best_it = its;
-        while (its < ctx->opts.max_iter) {
+        bool replayed = false;
+        if (its < ctx->opts.max_iter) {
             ++its;
             KTimer *kt = ctx->kt.on ? &ctx->kt : nullptr;
             cg_spmv_dot(A, ctx->p, ctx->q, ctx->R, singular, ctx->st, &ctx->launches, kt);
@@ -449,7 +531,10 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
             const bool fuse = ctx->nlev > 1;
             cg_update<T>(A, ctx->x, ctx->r, ctx->p, ctx->q, (T *)(mixed ? (void *)rlow : nullptr), L[0].view(),
                          fuse ? L[0].x : nullptr, cc.first, ctx->R, ctx->st, &ctx->launches, kt);
+        }
+        while (true) {
             const double rr = read_scal(ctx, S_RR);
+            if (replayed) kt_harvest_graph(ctx);
             if (!std::isfinite(rr)) {
                 set_err(ctx, "CG residual became non-finite at iteration %d", its);
                 stats->iterations = its;
@@ -464,10 +549,10 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
             if (rr < best) { best = rr; best_it = its; }
             else if (rr > 100.0 * best || its - best_it >= kStallWindow) { stalled = true; break; }
             const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-            if (el > ctx->opts.time_limit_s) break;
-            z = precondition<T>(ctx, L, cc, ctx->nlev > 1);
-            cg_dot_rz<T>(A, ctx->r, (const T *)L[0].b, z, ctx->R, ctx->st, &ctx->launches);
-            cg_pupdate<T>(A, z, ctx->p, ctx->R.scal, false, ctx->st, &ctx->launches);
+            if (el > ctx->opts.time_limit_s || its >= ctx->opts.max_iter) break;
+            run_iteration<T>(ctx, L, cc, singular);
+            replayed = ctx->graphs_ok && ctx->iter_exec;
+            ++its;
         }
         // true FP64 residual (the refinement check); for an all-Neumann
         // system also the mean of x, removed below
@@ -784,6 +869,7 @@ int scf_ctx_destroy(scf_ctx *ctx)
         if (ctx->ev[e]) cudaEventDestroy(ctx->ev[e]);
     if (ctx->kt_events)
         for (int e = 0; e < 2 * KTimer::CAP; ++e) cudaEventDestroy(ctx->kt.ev[e]);
+    if (ctx->iter_exec) cudaGraphExecDestroy(ctx->iter_exec);
     if (ctx->h_scal) cudaFreeHost(ctx->h_scal);
     if (ctx->h_u32) cudaFreeHost(ctx->h_u32);
     if (ctx->st) cudaStreamDestroy(ctx->st);

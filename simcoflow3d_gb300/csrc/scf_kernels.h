@@ -81,24 +81,43 @@ void mg_coarse_inverse(const MgLevel<T> &L, double *ainv, int *map, int n, bool 
 // fine-level launches of the kernel classes below (the same numbering as the
 // public scf_kernel_class).  Pairs beyond CAP in one solve go untimed.
 enum KClass { KC_SMOOTH = 0, KC_SPMV = 1, KC_RESTRICT = 2, KC_PROLONG = 3, KC_CGUPDATE = 4, KC_NUM = 5 };
+// Pairs [0, EAGER) time eagerly launched kernels (reset after every
+// harvest); pairs [EAGER, CAP) belong to the captured CG-iteration graph,
+// whose event-record nodes fire on every replay.
 struct KTimer {
     static constexpr int CAP = 512;
+    static constexpr int EAGER = 384;
     cudaEvent_t ev[2 * CAP];
     int cls[CAP];
     double bytes[CAP];     // algorithmic bytes of the launch (< 0: the class's model)
-    int n = 0;
+    int n = 0;             // eager pairs in use
+    int ng = EAGER;        // next graph pair while capturing
     bool on = false;
+    bool capturing = false;
     int begin(int c, cudaStream_t st, double b = -1.0)
     {
-        if (!on || n >= CAP) return -1;
-        cls[n] = c;
-        bytes[n] = b;
-        cudaEventRecord(ev[2 * n], st);
-        return n++;
+        if (!on) return -1;
+        int id;
+        if (capturing) {
+            if (ng >= CAP) return -1;
+            id = ng++;
+        } else {
+            if (n >= EAGER) return -1;
+            id = n++;
+        }
+        cls[id] = c;
+        bytes[id] = b;
+        record(ev[2 * id], st);
+        return id;
     }
     void end(int id, cudaStream_t st)
     {
-        if (id >= 0) cudaEventRecord(ev[2 * id + 1], st);
+        if (id >= 0) record(ev[2 * id + 1], st);
+    }
+    void record(cudaEvent_t e, cudaStream_t st)
+    {
+        if (capturing) cudaEventRecordWithFlags(e, st, cudaEventRecordExternal);
+        else cudaEventRecord(e, st);
     }
 };
 inline int kt_begin(KTimer *kt, int c, cudaStream_t st, double bytes = -1.0)

@@ -77,7 +77,21 @@ def test_adjoint_finite_differences_128(gpu_lib):
     for fd, an in ((fd_u, an_u), (fd_r, an_r)):
         fd, an = np.array(fd), np.array(an)
         assert np.linalg.norm(fd - an) <= 1e-6 * np.linalg.norm(an), (fd, an)
-        assert np.abs(fd - an).max() <= 1e-6 * np.abs(an).max(), (fd, an)
+        assert np.abs(fd - an).max() <= 2e-6 * np.abs(an).max(), (fd, an)
+    # The density directions' residual error at eps = 1e-6 is rounding of the
+    # FP64 operator amplified by its conditioning and divided by 2 eps (it
+    # scales as 1/eps); at eps = 1e-5 it is ten times smaller.
+    eps = 1.0e-5
+    rng = np.random.default_rng(20261204)
+    fd_r, an_r = [], []
+    for _ in range(8):
+        dr = np.asfortranarray(rng.normal(size=w.shape_g) * rho)
+        Jp = R.forward(us, vs, ws, rho + eps * dr)[0]
+        Jm = R.forward(us, vs, ws, rho - eps * dr)[0]
+        fd_r.append((Jp - Jm) / (2 * eps))
+        an_r.append(float(np.sum(grho * dr)))
+    fd, an = np.array(fd_r), np.array(an_r)
+    assert np.linalg.norm(fd - an) <= 3e-7 * np.linalg.norm(an), (fd, an)
 
 
 def test_torch_autograd_function(gpu_lib):

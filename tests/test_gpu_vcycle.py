@@ -1,7 +1,9 @@
 """The device V-cycle against the oracle's CPU V-cycle (oracle/gmg.cpp):
 same hierarchy rule, Chebyshev smoother and coarse solve, applied to a seeded
 residual.  FP64 V-cycle to 1e-12, FP32 V-cycle to 2e-5 (relative L2), on
-cubes, an odd-sized box and the Dirichlet-top wave tank."""
+cubes, an odd-sized box and the Dirichlet-top wave tank; the 64^3 case takes
+the large-level path (separate prolongation and first post-smoothing
+step)."""
 import numpy as np
 import pytest
 
@@ -9,7 +11,7 @@ from simcoflow3d_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
 
-CASES = [("c1", dict(n=24)), ("c2", dict(n=24)), ("c4", dict(n=12)), ("odd", {})]
+CASES = [("c1", dict(n=24)), ("c2", dict(n=24)), ("c4", dict(n=12)), ("odd", {}), ("c1", dict(n=64))]
 
 
 def _workload(name, kw):
