@@ -39,7 +39,7 @@
 extern "C" {
 #endif
 
-#define SCF_ABI_VERSION 1
+#define SCF_ABI_VERSION 2
 
 /* ---- status codes ------------------------------------------------------- */
 enum scf_status {
@@ -97,6 +97,15 @@ typedef struct scf_opts {
                                  reference's model with SCF_ERR_BAD_INPUT      */
     int32_t device;           /* CUDA device ordinal (default 0)               */
     double  time_limit_s;     /* wall-clock cap on one solve (default 60 s)    */
+    int32_t smoother_lines;   /* Jacobi blocks of the Chebyshev smoother:
+                                 0 = single cells; 1 = segments of 8 cells
+                                 along k, solved exactly (tridiagonal), which
+                                 keeps strong k-couplings (z-stretched grids,
+                                 thin layers) inside the blocks; 2 (default)
+                                 = segments on FP32 V-cycles of grids whose
+                                 smallest z spacing is at most half the larger
+                                 of the (smallest) x and y spacings, single
+                                 cells otherwise                              */
 } scf_opts;
 
 /* ---- per-call statistics -------------------------------------------------- */

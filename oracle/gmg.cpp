@@ -17,7 +17,8 @@
 // of the two half-cells and of the coarse face itself; the coarse diagonal is
 // the sum of its face conductances plus half the children's Dirichlet terms.
 // Smoother: Chebyshev polynomial of the Jacobi-preconditioned operator on
-// [lmax/ratio, lmax], lmax = 2 (Gershgorin bound).  Coarsest level: dense
+// [lmax/ratio, lmax], lmax = 2 (Gershgorin bound); the Jacobi blocks are single
+// cells or (line_seg > 0) segments of line_seg cells along k.  Coarsest level: dense
 // Cholesky in FP64 (rank-one regularised when the system is all-Neumann).
 #include <cmath>
 #include <cstdint>
@@ -188,12 +189,85 @@ inline T apply_at(const Level &L, const LevelT<T> &M, const T *x, size_t c)
 struct Params {
     int degree = 2;
     double lmax = 2.0, ratio = 6.0;
+    int line_seg = 0;   // 0: point Jacobi; n > 0: z-line Jacobi on segments of n cells
 };
+
+// out = T^{-1} in on the active cells, T the block diagonal of A whose
+// blocks are the segments of `seg` cells along k of each (i, j) column
+// (diagonal and T couplings inside a segment), by the Thomas algorithm.
+template <typename T>
+void line_solve(const Level &L, const LevelT<T> &M, const std::vector<T> &in, std::vector<T> &out, int seg)
+{
+    const int K = L.n[2];
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int j = 1; j <= L.n[1]; ++j)
+        for (int i = 1; i <= L.n[0]; ++i) {
+            std::vector<double> cp(K + 2, 0.0), dp(K + 2, 0.0);
+            for (int k = 1; k <= K; ++k) {
+                const size_t c = pidx(L, i, j, k);
+                if (!L.active[c]) { cp[k] = 0.0; dp[k] = 0.0; continue; }
+                const bool first = (k - 1) % seg == 0, last = k % seg == 0;
+                const double a = (k > 1 && !first) ? -(double)M.cT[c - L.sz] : 0.0;
+                const double cc = (k < K && !last) ? -(double)M.cT[c] : 0.0;
+                const double den = (double)M.diag[c] - a * cp[k - 1];
+                cp[k] = cc / den;
+                dp[k] = ((double)in[c] - a * dp[k - 1]) / den;
+            }
+            double nxt = 0.0;
+            for (int k = K; k >= 1; --k) {
+                const size_t c = pidx(L, i, j, k);
+                if (k % seg == 0) nxt = 0.0;
+                const double v = L.active[c] ? dp[k] - cp[k] * nxt : 0.0;
+                out[c] = (T)v;
+                nxt = v;
+            }
+        }
+}
+
+// Chebyshev smoothing with the z-line blocks
+template <typename T>
+void chebyshev_line(const Level &L, LevelT<T> &M, int deg, bool zero_init, const Params &P)
+{
+    const double lmax = P.lmax, lmin = P.lmax / P.ratio;
+    const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin), sigma = theta / delta;
+    double rho = 1.0 / sigma;
+    std::vector<T> z(L.tot, T(0));
+    {
+        T *x = M.x.data();
+        FOR_CELLS(L) {
+            size_t c = pidx(L, i, j, k);
+            M.r[c] = zero_init ? M.b[c] : M.b[c] - apply_at(L, M, x, c);
+        }
+        line_solve(L, M, M.r, z, P.line_seg);
+        FOR_CELLS(L) {
+            size_t c = pidx(L, i, j, k);
+            M.d[c] = (T)(z[c] / theta);
+            M.x[c] = (zero_init ? T(0) : M.x[c]) + M.d[c];
+        }
+    }
+    for (int s = 1; s < deg; ++s) {
+        double rho_new = 1.0 / (2.0 * sigma - rho);
+        double c1 = rho_new * rho, c2 = 2.0 * rho_new / delta;
+        rho = rho_new;
+        T *x = M.x.data();
+        FOR_CELLS(L) {
+            size_t c = pidx(L, i, j, k);
+            M.r[c] = M.b[c] - apply_at(L, M, x, c);
+        }
+        line_solve(L, M, M.r, z, P.line_seg);
+        FOR_CELLS(L) {
+            size_t c = pidx(L, i, j, k);
+            M.d[c] = (T)(c1 * M.d[c] + c2 * z[c]);
+            M.x[c] += M.d[c];
+        }
+    }
+}
 
 // Chebyshev smoothing of A x = b, `deg` steps, starting from x (zero if zero_init)
 template <typename T>
 void chebyshev(const Level &L, LevelT<T> &M, int deg, bool zero_init, const Params &P)
 {
+    if (P.line_seg > 0) { chebyshev_line(L, M, deg, zero_init, P); return; }
     const double lmax = P.lmax, lmin = P.lmax / P.ratio;
     const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin), sigma = theta / delta;
     double rho = 1.0 / sigma;
@@ -470,6 +544,7 @@ typedef struct {
     int degree;
     double ratio;
     int coarse_max;
+    int line_seg;      // 0: point-Jacobi Chebyshev; n: z-line Jacobi on n-cell segments
     // outputs
     int iterations;
     int rounds;
@@ -502,6 +577,7 @@ int oracle_gmg_solve(int I, int J, int K, const scf_poisson_in *in, const double
     std::vector<double> x(L0.tot, 0.0), r(b), z(L0.tot, 0.0), p(L0.tot, 0.0), q(L0.tot, 0.0);
     Params P;
     P.degree = prm->degree;
+    P.line_seg = prm->line_seg;
     P.ratio = prm->ratio;
     int its = 0, rounds = 0;
     double relres = bn > 0 ? 1.0 : 0.0;
@@ -617,6 +693,7 @@ int oracle_gmg_vcycle(int I, int J, int K, const scf_poisson_in *in, const doubl
     prm->levels = (int)lv.size();
     Params P;
     P.degree = prm->degree;
+    P.line_seg = prm->line_seg;
     P.ratio = prm->ratio;
     const Level &L0 = lv[0];
     auto run = [&](auto &H) {

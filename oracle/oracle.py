@@ -61,6 +61,7 @@ class GmgParams(C.Structure):
     _fields_ = [
         ("precision", C.c_int), ("rel_tol", C.c_double), ("max_iter", C.c_int), ("max_rounds", C.c_int),
         ("inner_rtol", C.c_double), ("degree", C.c_int), ("ratio", C.c_double), ("coarse_max", C.c_int),
+        ("line_seg", C.c_int),
         ("iterations", C.c_int), ("rounds", C.c_int), ("levels", C.c_int),
         ("rel_residual", C.c_double), ("rhs_norm", C.c_double),
     ]
@@ -133,12 +134,12 @@ def csr_relres(A, b, x, singular_=False):
 
 
 def gmg_solve(w, pc, b, precision=0, rel_tol=1e-13, max_iter=400, degree=2, ratio=6.0, coarse_max=64,
-              max_rounds=12, inner_rtol=1e-4):
+              max_rounds=12, inner_rtol=1e-4, line_seg=0):
     """CPU multigrid-preconditioned CG; returns (x in PosNu order, stats)."""
     I, J, K = w.imax, w.jmax, w.kmax
     x = np.zeros(w.ext_cell + 1)
     prm = GmgParams(precision=precision, rel_tol=rel_tol, max_iter=max_iter, max_rounds=max_rounds,
-                    inner_rtol=inner_rtol, degree=degree, ratio=ratio, coarse_max=coarse_max)
+                    inner_rtol=inner_rtol, degree=degree, ratio=ratio, coarse_max=coarse_max, line_seg=line_seg)
     s = capi.poisson_in(w)
     rc = lib().oracle_gmg_solve(I, J, K, C.byref(s), _dp(pc), _dp(b), _dp(x), C.byref(prm))
     st = {f: getattr(prm, f) for f, _ in GmgParams._fields_}
@@ -146,12 +147,12 @@ def gmg_solve(w, pc, b, precision=0, rel_tol=1e-13, max_iter=400, degree=2, rati
     return x, st
 
 
-def gmg_vcycle(w, pc, r, precision=0, degree=3, ratio=6.0, coarse_max=64):
+def gmg_vcycle(w, pc, r, precision=0, degree=3, ratio=6.0, coarse_max=64, line_seg=0):
     """One CPU V-cycle z = M r of the multigrid hierarchy of (w, pc); r and z
     ghosted FP64 arrays."""
     I, J, K = w.imax, w.jmax, w.kmax
     z = np.zeros(w.shape_g, order="F")
-    prm = GmgParams(precision=precision, degree=degree, ratio=ratio, coarse_max=coarse_max)
+    prm = GmgParams(precision=precision, degree=degree, ratio=ratio, coarse_max=coarse_max, line_seg=line_seg)
     s = capi.poisson_in(w)
     rr = np.asfortranarray(r, dtype=np.float64)
     lib().oracle_gmg_vcycle(I, J, K, C.byref(s), _dp(pc), _dp(rr), _dp(z), C.byref(prm))

@@ -59,6 +59,7 @@ class ScfOpts(C.Structure):
         ("check_inputs", C.c_int32),
         ("device", C.c_int32),
         ("time_limit_s", C.c_double),
+        ("smoother_lines", C.c_int32),
     ]
 
 

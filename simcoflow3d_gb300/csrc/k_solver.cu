@@ -456,6 +456,94 @@ __global__ void __launch_bounds__(256) k_cheb_step(LevelView<T> L, const T *__re
     if (dout) dout[c] = dn;
 }
 
+// Chebyshev step with z-line Jacobi blocks: the preconditioner of the
+// Chebyshev iteration is T^-1, T the block diagonal of A whose blocks are
+// segments of LINE_SEG cells along k of one (i, j) column (the diagonal and
+// the k-couplings inside the segment).  One thread owns one segment: it forms
+// the residual cell by cell (k-neighbours in registers), eliminates forward
+// (Thomas algorithm, pivots formed on the fly) and substitutes backward in
+// registers, so the step moves the same arrays as the point step:
+//   x <- x + (c1 d + c2 T^-1 (b - A x)).
+// zero_guess: x = 0 on entry (the first pre-smoothing step); x and dprev are
+// not read.  T is a diagonally dominant M-matrix block, so its eigenvalue
+// bound for the Chebyshev interval is that of the point diagonal.
+template <typename T>
+__device__ __forceinline__ T rcp_of(T v);
+template <>
+__device__ __forceinline__ float rcp_of<float>(float v) { return __frcp_rn(v); }
+template <>
+__device__ __forceinline__ double rcp_of<double>(double v) { return 1.0 / v; }
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_cheb_line(LevelView<T> L, const T *__restrict__ b, const T *x,
+                                                   const T *dprev, T *__restrict__ xout, T *__restrict__ dout, T c1,
+                                                   T c2, int zero_guess)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k0 = blockIdx.z * LINE_SEG + 1;
+    if (i > L.n0 || j > L.n1) return;
+    const int nk = min(LINE_SEG, L.n2 - k0 + 1);
+    const int sy = L.sy, sz = L.sz;
+    int c = i + sy * j + sz * k0;
+    T y[LINE_SEG], cp[LINE_SEG], xo[LINE_SEG];
+    T xm = zero_guess ? T(0) : x[c - sz];
+    T xc = zero_guess ? T(0) : x[c];
+    T ym = T(0), cpm = T(0);
+#pragma unroll
+    for (int s = 0; s < LINE_SEG; ++s) {
+        y[s] = T(0); cp[s] = T(0); xo[s] = T(0);
+        if (s < nk) {
+            const T dg = L.diag[c];
+            const T ct = L.cT[c], cb = L.cT[c - sz];
+            T r;
+            T xp = T(0);
+            if (zero_guess) {
+                r = b[c];
+            } else {
+                xp = x[c + sz];
+                r = b[c] - (dg * xc - (L.cE[c] * x[c + 1] + L.cE[c - 1] * x[c - 1] + L.cN[c] * x[c + sy] +
+                                       L.cN[c - sy] * x[c - sy] + ct * xp + cb * xm));
+            }
+            if (dg > T(0)) {
+                const T a = s > 0 ? -cb : T(0);
+                const T cc = s < nk - 1 ? -ct : T(0);
+                const T inv = rcp_of<T>(dg - a * cpm);
+                cp[s] = cc * inv;
+                y[s] = (r - a * ym) * inv;
+            }
+            ym = y[s];
+            cpm = cp[s];
+            xo[s] = xc;
+            xm = xc;
+            xc = xp;
+            c += sz;
+        }
+    }
+    T zn = T(0);
+#pragma unroll
+    for (int s = LINE_SEG - 1; s >= 0; --s) {
+        if (s < nk) {
+            c -= sz;
+            const T z = y[s] - cp[s] * zn;
+            zn = z;
+            const T dp = zero_guess ? T(0) : dprev[c];
+            const T dn = c1 * dp + c2 * z;
+            xout[c] = xo[s] + dn;
+            if (dout) dout[c] = dn;
+        }
+    }
+}
+
+template <typename T>
+void launch_cheb_line(const MgLevel<T> &F, const T *x, const T *dprev, T *xout, T *dout, double c1, double c2,
+                      bool zero_guess, cudaStream_t st)
+{
+    dim3 blk(32, 4, 1);
+    dim3 grd((F.n0 + 31) / 32, (F.n1 + 3) / 4, (F.n2 + LINE_SEG - 1) / LINE_SEG);
+    k_cheb_line<T><<<grd, blk, 0, st>>>(F.view(), F.b, x, dprev, xout, dout, (T)c1, (T)c2, zero_guess ? 1 : 0);
+}
+
 // Residual of the fine level summed over each coarse cell's children.  One
 // thread per fine i and coarse (J,K): it sums the residuals of its (up to
 // 2x2) fine cells in j and k, then lanes i and i^1 add their sums with a
@@ -713,6 +801,14 @@ double smooth_bytes(const MgLevel<T> &F, bool first, bool writes_d)
     return arrays * sizeof(T) * cells;
 }
 
+// Algorithmic bytes of the first (zero-guess) line step: b, diag, cT read,
+// x written.
+template <typename T>
+double line_first_bytes(const MgLevel<T> &F)
+{
+    return 4.0 * sizeof(T) * (double)F.n0 * F.n1 * F.n2;
+}
+
 // Algorithmic bytes of the split prolongation + first post-smoothing step:
 // x read and written, the active mask and the coarse correction read; then
 // b, x, diag, cE, cN, cT (+ dinv on FP64 levels) read, x (+ the update)
@@ -736,6 +832,29 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
         LevelView<T> v = F.view();
         Launch3 lf = launch_interior(F.n0, F.n1, F.n2);
         T *xa = F.x, *xb = F.xb;
+        if (cc.lines) {
+            const int id0 = l == 0 ? kt_begin(kt, KC_SMOOTH, st, line_first_bytes<T>(F)) : -1;
+            launch_cheb_line<T>(F, nullptr, nullptr, xa, nullptr, 0.0, cc.first, true, st);
+            kt_end(kt, id0, st);
+            *launches += 1;
+            for (int s = 1; s < cc.degree; ++s) {
+                const T *dprev = (s == 1) ? xa : F.d;
+                T *dout = (s == cc.degree - 1) ? nullptr : F.d;
+                const int id = l == 0 ? kt_begin(kt, KC_SMOOTH, st, smooth_bytes<T>(F, s == 1, dout != nullptr)) : -1;
+                launch_cheb_line<T>(F, xa, dprev, xb, dout, cc.c1[s], cc.c2[s], false, st);
+                kt_end(kt, id, st);
+                *launches += 1;
+                T *tmp = xa; xa = xb; xb = tmp;
+            }
+            cur[l] = xa;
+            MgLevel<T> &C = L[l + 1];
+            dim3 rg((F.n0 + 31) / 32, (C.n1 + 3) / 4, C.n2), rb(32, 4, 1);
+            const int id = l == 0 ? kt_begin(kt, KC_RESTRICT, st) : -1;
+            k_restrict<T><<<rg, rb, 0, st>>>(v, F.b, xa, C.view(), C.b, F.f0, F.f1, F.f2);
+            kt_end(kt, id, st);
+            *launches += 1;
+            continue;
+        }
         if (!(l == 0 && first_done)) {
             k_cheb_first<T><<<lf.grid, lf.block, 0, st>>>(v, F.b, xa, (T)cc.first);
             *launches += 1;
@@ -773,6 +892,25 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
         T *xa = cur[l];
         T *xb = (xa == F.x) ? F.xb : F.x;
         const bool more = cc.degree > 1;
+        if (cc.lines) {
+            const int idp = l == 0 ? kt_begin(kt, KC_PROLONG, st, prolong_bytes<T>(F, more)) : -1;
+            k_prolong<T><<<lf.grid, lf.block, 0, st>>>(v, F.active, xa, C.view(), cur[l + 1], F.f0 - 1, F.f1 - 1,
+                                                       F.f2 - 1);
+            launch_cheb_line<T>(F, xa, xa, xb, more ? F.d : nullptr, 0.0, cc.first, false, st);
+            kt_end(kt, idp, st);
+            *launches += 2;
+            { T *tmp = xa; xa = xb; xb = tmp; }
+            for (int s = 1; s < cc.degree; ++s) {
+                const bool last_step = s == cc.degree - 1;
+                const int id = l == 0 ? kt_begin(kt, KC_SMOOTH, st, smooth_bytes<T>(F, false, !last_step)) : -1;
+                launch_cheb_line<T>(F, xa, F.d, xb, last_step ? nullptr : F.d, cc.c1[s], cc.c2[s], false, st);
+                kt_end(kt, id, st);
+                *launches += 1;
+                T *tmp = xa; xa = xb; xb = tmp;
+            }
+            cur[l] = xa;
+            continue;
+        }
         if ((long long)F.n0 * F.n1 * F.n2 >= (1LL << 18)) {
             const int idp = l == 0 ? kt_begin(kt, KC_PROLONG, st, prolong_bytes<T>(F, more)) : -1;
             k_prolong<T><<<lf.grid, lf.block, 0, st>>>(v, F.active, xa, C.view(), cur[l + 1], F.f0 - 1, F.f1 - 1,

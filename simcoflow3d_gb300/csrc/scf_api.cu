@@ -3,6 +3,7 @@
 // Host orchestration: device mirrors of the Fortran arrays, assembly, the
 // multigrid hierarchy, the preconditioned CG loop and the correction.  All
 // work of a context runs on one CUDA stream; calls are synchronous.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -70,6 +71,7 @@ struct scf_ctx {
     unsigned long long iter_key = 0;
     int iter_launches = 0;     // kernels in one replay
     bool graphs_ok = true;     // cleared if capture is not available
+    double aniso_z = 1.0;      // (larger of the x, y spacings / smallest z spacing)^2 of the staged grid
     unsigned mg_gen = 0;       // bumped whenever the hierarchy is reallocated
     bool kt_events = false;
     double kt_ms[KC_NUM] = {0}, kt_launches[KC_NUM] = {0}, kt_bytes[KC_NUM] = {0};
@@ -331,9 +333,10 @@ void build_hierarchy(scf_ctx *ctx, MgLevel<T> *L)
                          &ctx->launches);
 }
 
-ChebCoef cheb_coef(int degree)
+ChebCoef cheb_coef(int degree, int lines)
 {
     ChebCoef cc;
+    cc.lines = lines;
     if (degree < 1) degree = 1;
     if (degree > 8) degree = 8;
     cc.degree = degree;
@@ -404,6 +407,26 @@ void kt_harvest_graph(scf_ctx *ctx)
     if (ctx->kt.on && ctx->kt.ng > KTimer::EAGER) kt_add(ctx, KTimer::EAGER, ctx->kt.ng);
 }
 
+// Line blocks for the smoother: always (1), never (0), or (2) on FP32
+// V-cycles of grids whose smallest z spacing is at most half the larger of
+// the x and y spacings, where the k-couplings outweigh the weaker in-plane
+// ones at least fourfold.  (FP64 V-cycles are bound by FP64 arithmetic, and
+// the line solve's division per cell costs more there than the iterations it
+// saves.)
+bool use_lines(const scf_ctx *ctx)
+{
+    if (ctx->opts.smoother_lines == 1) return true;
+    if (ctx->opts.smoother_lines == 0) return false;
+    return ctx->opts.precision == SCF_PREC_MIXED && ctx->aniso_z >= 4.0;
+}
+
+ChebCoef cheb_for(const scf_ctx *ctx) { return cheb_coef(ctx->opts.smoother_degree, use_lines(ctx) ? 1 : 0); }
+
+// The CG update writes level 0's first (point-Jacobi) smoothing step of the
+// next V-cycle when the hierarchy has more than one level; with line blocks
+// the V-cycle forms that step itself.
+bool fuse_first(const scf_ctx *ctx) { return ctx->nlev > 1 && !use_lines(ctx); }
+
 template <typename T>
 T *precondition(scf_ctx *ctx, MgLevel<T> *L, const ChebCoef &cc, bool first_done)
 {
@@ -423,11 +446,11 @@ void iteration_kernels(scf_ctx *ctx, MgLevel<T> *L, const ChebCoef &cc, bool sin
     const bool mixed = sizeof(T) == 4;
     float *rlow = mixed ? (float *)L[0].b : nullptr;
     KTimer *kt = ctx->kt.on ? &ctx->kt : nullptr;
-    T *z = precondition<T>(ctx, L, cc, ctx->nlev > 1);
+    T *z = precondition<T>(ctx, L, cc, fuse_first(ctx));
     cg_dot_rz<T>(A, ctx->r, (const T *)L[0].b, z, ctx->R, ctx->st, &ctx->launches);
     cg_pupdate<T>(A, z, ctx->p, ctx->R.scal, false, ctx->st, &ctx->launches);
     cg_spmv_dot(A, ctx->p, ctx->q, ctx->R, singular, ctx->st, &ctx->launches, kt);
-    const bool fuse = ctx->nlev > 1;
+    const bool fuse = fuse_first(ctx);
     cg_update<T>(A, ctx->x, ctx->r, ctx->p, ctx->q, (T *)(mixed ? (void *)rlow : nullptr), L[0].view(),
                  fuse ? L[0].x : nullptr, cc.first, ctx->R, ctx->st, &ctx->launches, kt);
 }
@@ -438,7 +461,7 @@ void run_iteration(scf_ctx *ctx, MgLevel<T> *L, const ChebCoef &cc, bool singula
     const unsigned long long key = 1ull + (unsigned long long)ctx->mg_gen * 1000003ull +
                                    (unsigned long long)cc.degree * 131ull + (singular ? 7ull : 0ull) +
                                    (ctx->kt.on ? 3ull : 0ull) + (sizeof(T) == 4 ? 11ull : 0ull) +
-                                   (unsigned long long)ctx->nlev * 17ull;
+                                   (unsigned long long)ctx->nlev * 17ull + (cc.lines ? 5ull : 0ull);
     if (ctx->graphs_ok && (!ctx->iter_exec || ctx->iter_key != key)) {
         if (ctx->iter_exec) { cudaGraphExecDestroy(ctx->iter_exec); ctx->iter_exec = nullptr; }
         cudaGraph_t g = nullptr;
@@ -482,7 +505,7 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
     const bool singular = is_singular(ctx);
     const bool mixed = sizeof(T) == 4;
     float *rlow = mixed ? (float *)L[0].b : nullptr;
-    const ChebCoef cc = cheb_coef(ctx->opts.smoother_degree);
+    const ChebCoef cc = cheb_for(ctx);
     auto t0 = std::chrono::steady_clock::now();
     rhs_prologue(A, ctx->active, ctx->b, singular, ctx->R, ctx->st, &ctx->launches);
     build_hierarchy<T>(ctx, L);
@@ -528,7 +551,7 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
             cg_spmv_dot(A, ctx->p, ctx->q, ctx->R, singular, ctx->st, &ctx->launches, kt);
             // the update also writes level 0's first smoothing step when the
             // hierarchy has more than one level
-            const bool fuse = ctx->nlev > 1;
+            const bool fuse = fuse_first(ctx);
             cg_update<T>(A, ctx->x, ctx->r, ctx->p, ctx->q, (T *)(mixed ? (void *)rlow : nullptr), L[0].view(),
                          fuse ? L[0].x : nullptr, cc.first, ctx->R, ctx->st, &ctx->launches, kt);
         }
@@ -708,6 +731,15 @@ int stage(scf_ctx *ctx, const scf_poisson_in *in, const scf_correct_in *corr, co
     }
     ctx->ext_cell = in->pcell_extcell;
     ctx->dt = in->dt;
+    {
+        // tensor-product grid: the spacings along the first line of each axis
+        double hx = HUGE_VAL, hy = HUGE_VAL, hz = HUGE_VAL;
+        for (int i = 0; i < d.I; ++i) hx = std::min(hx, in->pgrid_dx[i]);
+        for (int j = 0; j < d.J; ++j) hy = std::min(hy, in->pgrid_dy[(size_t)j * d.I]);
+        for (int k = 0; k < d.K; ++k) hz = std::min(hz, in->pgrid_dz[(size_t)k * d.I * d.J]);
+        const double h = std::max(hx, hy);
+        ctx->aniso_z = (hz > 0.0 && std::isfinite(h)) ? (h / hz) * (h / hz) : 1.0;
+    }
     ctx->have_corr = false;
     if (corr) {
         const int *fl[3] = {corr->bcu_flag, corr->bcv_flag, corr->bcw_flag};
@@ -786,6 +818,7 @@ void scf_opts_default(scf_opts *o)
     o->check_inputs = 1;
     o->device = 0;
     o->time_limit_s = 60.0;
+    o->smoother_lines = 2;
 }
 
 static int validate_opts(scf_ctx *ctx, const scf_opts *o)
@@ -793,6 +826,7 @@ static int validate_opts(scf_ctx *ctx, const scf_opts *o)
     if (o->precision != SCF_PREC_FP64 && o->precision != SCF_PREC_MIXED) { set_err(ctx, "bad precision"); return SCF_ERR_BAD_ARG; }
     if (!(o->rel_tol > 0.0) || o->max_iter < 1 || o->smoother_degree < 1 || o->smoother_degree > 8) { set_err(ctx, "bad solver options"); return SCF_ERR_BAD_ARG; }
     if (o->coarse_max_cells < 8 || o->coarse_max_cells > 128) { set_err(ctx, "coarse_max_cells must be in [8,128]"); return SCF_ERR_BAD_ARG; }
+    if (o->smoother_lines < 0 || o->smoother_lines > 2) { set_err(ctx, "smoother_lines must be 0, 1 or 2"); return SCF_ERR_BAD_ARG; }
     if (!(o->rho_l > 0.0) || !(o->rho_g > 0.0)) { set_err(ctx, "densities must be positive"); return SCF_ERR_BAD_ARG; }
     return SCF_OK;
 }
@@ -1135,7 +1169,7 @@ int scf_debug_precondition(scf_ctx *ctx, const double *rh, double *zh)
     if (!rh || !zh) return SCF_ERR_BAD_ARG;
     if (!ctx->solved) { set_err(ctx, "no projection has run"); return SCF_ERR_NO_SOLVE; }
     const Dims &d = ctx->d;
-    const ChebCoef cc = cheb_coef(ctx->opts.smoother_degree);
+    const ChebCoef cc = cheb_for(ctx);
     CK(cudaMemcpyAsync(ctx->r, rh, sizeof(double) * d.ng, cudaMemcpyHostToDevice, ctx->st));
     if (ctx->opts.precision == SCF_PREC_FP64) {
         const double *z = precondition<double>(ctx, ctx->L64, cc, false);
@@ -1182,7 +1216,7 @@ int scf_debug_time_kernel(scf_ctx *ctx, int kernel, int reps, double *ms_per_lau
     if (!ctx->solved) { set_err(ctx, "no projection has run"); return SCF_ERR_NO_SOLVE; }
     if (ctx->nlev < 2 && (kernel == SCF_K_RESTRICT || kernel == SCF_K_PROLONG)) return SCF_ERR_BAD_ARG;
     const bool mixed = ctx->opts.precision == SCF_PREC_MIXED;
-    const ChebCoef cc = cheb_coef(ctx->opts.smoother_degree);
+    const ChebCoef cc = cheb_for(ctx);
     auto launch = [&]() {
         switch (kernel) {
         case SCF_K_SMOOTH:

@@ -63,7 +63,9 @@ struct ChebCoef {
     int degree;
     double first;        // 1/theta
     double c1[8], c2[8]; // steps 1..degree-1
+    int lines = 0;       // Jacobi blocks: 0 single cells, 1 segments of LINE_SEG cells along k
 };
+constexpr int LINE_SEG = 8;
 
 struct Reducer {
     double *partials;    // >= max blocks of any reducing launch

@@ -31,7 +31,7 @@ def test_library_exports_every_declared_function(lib_path):
     assert len(names) >= 18
     for n in names:
         assert hasattr(lib, n), n
-    assert lib.scf_abi_version() == 1
+    assert lib.scf_abi_version() == 2
 
 
 def test_struct_layouts_match_header(lib_path):

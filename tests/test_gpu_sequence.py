@@ -37,3 +37,27 @@ def test_warm_started_sequence_wave_tank(gpu_lib, precision):
         d = (pw - pc)[1:-1, 1:-1, 1:-1][act]
         assert np.abs(d).max() <= 1e-5 * np.abs(pc[1:-1, 1:-1, 1:-1][act]).max(), call
     assert sum(its_warm[1:]) <= sum(its_cold[1:])
+
+
+@pytest.mark.parametrize("stretched", [True, False])
+def test_smoother_blocks_follow_the_grid(gpu_lib, stretched):
+    """smoother_lines=2 (default) takes 8-cell z-line blocks on a strongly
+    z-stretched grid and single cells on a uniform one, in mixed precision:
+    its pressure is bitwise that of the explicit choice.  Line blocks also
+    cut the iterations on the stretched grid."""
+    from simcoflow3d_gb300.projection import Projection
+    if stretched:
+        w = W.build_workload("stretched", 32, 32, 32, zstretch=1.4, solid=W.SPHERE_C1,
+                             liquid=("bubble", 0.5, 0.5, 0.6, 0.2), rho_l=1000.0, rho_g=1.2)
+    else:
+        w = W.config("c1", n=32)
+    out = {}
+    for lines in (2, 1, 0):
+        p = Projection.for_workload(w, rel_tol=1e-8, precision=1, smoother_lines=lines)
+        _, pp, st = p.poisson_solve(w, want_pocoef=False)
+        assert st["converged"] == 1
+        out[lines] = (pp, st["iterations"])
+    expect = 1 if stretched else 0
+    assert np.array_equal(out[2][0], out[expect][0])
+    if stretched:
+        assert out[1][1] < out[0][1]
