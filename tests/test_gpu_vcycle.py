@@ -1,9 +1,9 @@
 """The device V-cycle against the oracle's CPU V-cycle (oracle/gmg.cpp):
 same hierarchy rule, Chebyshev smoother (point-Jacobi or 8-cell z-line
-blocks) and coarse solve, applied to a seeded residual.  FP64 V-cycle to 1e-12, FP32 V-cycle to 2e-5 (relative L2), on
-cubes, an odd-sized box and the Dirichlet-top wave tank; the 64^3 case takes
-the large-level path (separate prolongation and first post-smoothing
-step)."""
+blocks) and coarse solve, applied to a seeded residual.  FP64 V-cycle to
+1e-12, FP32 V-cycle to 2e-5 (relative L2), on cubes, an odd-sized box and the
+Dirichlet-top wave tank; the 64^3 case takes the large-level path (separate
+prolongation and first post-smoothing step)."""
 import numpy as np
 import pytest
 
