@@ -378,7 +378,7 @@ def run_ours(args):
                 "d2h_bytes_per_step": int(e2e_stats["bytes_d2h"]),
                 "ms_h2d": round(e2e_stats["ms_h2d"], 3), "ms_d2h": round(e2e_stats["ms_d2h"], 3),
                 "ms_min": round(min(e2e_ms), 3), "ms_median": round(statistics.median(e2e_ms), 3),
-                "ms_max": round(max(e2e_ms), 3),
+                "ms_max": round(max(e2e_ms), 3), "ms_steps": [round(x, 2) for x in e2e_ms],
                 "inputs_pinned_fraction": round(pinned_in / max(in_bytes, 1), 4),
                 "outputs": "page-locked (cudaHostAlloc)"},
         "roofline": {"bound": "hbm", "kernel": "k_cheb_step<float> (fine-level Chebyshev step)",

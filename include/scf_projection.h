@@ -122,7 +122,10 @@ typedef struct scf_stats {
     double  ms_assemble;      /* coefficients + operator + rhs + hierarchy     */
     double  ms_solve;         /* CG (incl. V-cycles)                           */
     double  ms_correct;       /* scatter, velocity correction, BCs             */
-    double  ms_h2d, ms_d2h;   /* host<->device copies inside the call          */
+    double  ms_h2d, ms_d2h;   /* host<->device copies inside the call; in
+                                 scf_update_puvw ms_h2d covers the solve's
+                                 inputs (the correction's inputs are copied
+                                 on a second stream while the solve runs)    */
     double  ms_total;         /* device time of the whole call                 */
     int64_t bytes_h2d, bytes_d2h;
 } scf_stats;

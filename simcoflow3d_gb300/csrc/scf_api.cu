@@ -32,6 +32,9 @@ struct scf_ctx {
     Dims d;
     scf_opts opts;
     cudaStream_t st = nullptr;
+    cudaStream_t cst = nullptr;   // copies of the correction's inputs, overlapping the solve
+    cudaEvent_t corr_ready = nullptr;
+    bool corr_pending = false;    // st must wait for corr_ready before the correction
     char err[512] = {0};
     DevBuf mem, mgmem;
     // inputs (device)
@@ -678,6 +681,10 @@ int run(scf_ctx *ctx, bool with_correction, scf_stats *stats)
     ctx->solved = true;
     ctx->warm_ok = true;
     CorrArgs ca = corr_args(ctx);
+    if (ctx->corr_pending) {
+        CK(cudaStreamWaitEvent(ctx->st, ctx->corr_ready, 0));
+        ctx->corr_pending = false;
+    }
     launch_scatter(ca, ctx->st, &ctx->launches);
     if (with_correction) launch_correct(ca, ctx->st, &ctx->launches);
     cudaEventRecord(ctx->ev[3], ctx->st);
@@ -693,21 +700,25 @@ int run(scf_ctx *ctx, bool with_correction, scf_stats *stats)
 }
 
 template <typename P>
-int h2d(scf_ctx *ctx, P *dst, const P *src, size_t n, int64_t *bytes)
+int h2d(scf_ctx *ctx, P *dst, const P *src, size_t n, int64_t *bytes, cudaStream_t st)
 {
     if (!src) { set_err(ctx, "null input array"); return SCF_ERR_BAD_ARG; }
-    CK(cudaMemcpyAsync(dst, src, n * sizeof(P), cudaMemcpyHostToDevice, ctx->st));
+    CK(cudaMemcpyAsync(dst, src, n * sizeof(P), cudaMemcpyHostToDevice, st));
     *bytes += (int64_t)(n * sizeof(P));
     return SCF_OK;
 }
 #define H2D(dst, src, n)                                   \
     do {                                                   \
-        int rc_ = h2d(ctx, dst, src, (size_t)(n), &bytes); \
+        int rc_ = h2d(ctx, dst, src, (size_t)(n), &bytes, ctx->st); \
         if (rc_) return rc_;                               \
     } while (0)
 
+// defer_corr: the correction's inputs go to the device on the copy stream
+// and overlap the assembly and solve; run() orders the correction after
+// them.  Only for callers that keep the host arrays alive until the
+// projection has finished (scf_update_puvw).
 int stage(scf_ctx *ctx, const scf_poisson_in *in, const scf_correct_in *corr, const double *u, const double *v,
-          const double *w, const double *p, int64_t *bytes_out)
+          const double *w, const double *p, int64_t *bytes_out, bool defer_corr = false)
 {
     if (!in) { set_err(ctx, "null scf_poisson_in"); return SCF_ERR_BAD_ARG; }
     const Dims &d = ctx->d;
@@ -747,10 +758,25 @@ int stage(scf_ctx *ctx, const scf_poisson_in *in, const scf_correct_in *corr, co
             for (int q = 0; q < 6; ++q)
                 if (fl[f][q] != 0 && fl[f][q] != 1) { set_err(ctx, "velocity BC flag must be 0 or 1"); return SCF_ERR_BAD_ARG; }
         if ((u || v || w || p) && !(u && v && w && p)) { set_err(ctx, "null TVar array"); return SCF_ERR_BAD_ARG; }
-        H2D(ctx->umoex, corr->ucell_moexcell, d.n); H2D(ctx->uct, corr->ucell_cell_type, d.n);
-        H2D(ctx->vmoex, corr->vcell_moexcell, d.n); H2D(ctx->vct, corr->vcell_cell_type, d.n);
-        H2D(ctx->wmoex, corr->wcell_moexcell, d.n); H2D(ctx->wct, corr->wcell_cell_type, d.n);
-        if (u) { H2D(ctx->tu, u, d.ng); H2D(ctx->tv, v, d.ng); H2D(ctx->tw, w, d.ng); H2D(ctx->tp, p, d.ng); }
+        const cudaStream_t cs = defer_corr ? ctx->cst : ctx->st;
+#define H2DC(dst, src, n)                                               \
+    do {                                                                \
+        int rc_ = h2d(ctx, dst, src, (size_t)(n), &bytes, cs);          \
+        if (rc_) return rc_;                                            \
+    } while (0)
+        if (defer_corr) {   // the copy stream may not overwrite what a running call still reads
+            CK(cudaEventRecord(ctx->corr_ready, ctx->st));
+            CK(cudaStreamWaitEvent(ctx->cst, ctx->corr_ready, 0));
+        }
+        H2DC(ctx->umoex, corr->ucell_moexcell, d.n); H2DC(ctx->uct, corr->ucell_cell_type, d.n);
+        H2DC(ctx->vmoex, corr->vcell_moexcell, d.n); H2DC(ctx->vct, corr->vcell_cell_type, d.n);
+        H2DC(ctx->wmoex, corr->wcell_moexcell, d.n); H2DC(ctx->wct, corr->wcell_cell_type, d.n);
+        if (u) { H2DC(ctx->tu, u, d.ng); H2DC(ctx->tv, v, d.ng); H2DC(ctx->tw, w, d.ng); H2DC(ctx->tp, p, d.ng); }
+#undef H2DC
+        if (defer_corr) {
+            CK(cudaEventRecord(ctx->corr_ready, ctx->cst));
+            ctx->corr_pending = true;
+        }
         ctx->corr = *corr;
         ctx->have_corr = true;
     }
@@ -881,6 +907,8 @@ int scf_ctx_create(scf_ctx **out, int32_t imax, int32_t jmax, int32_t kmax, cons
     A(ctx->R.scal, S_NUM);
 #undef A
     if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) return fail(SCF_ERR_CUDA);
+    if (cudaStreamCreateWithFlags(&ctx->cst, cudaStreamNonBlocking) != cudaSuccess) return fail(SCF_ERR_CUDA);
+    if (cudaEventCreateWithFlags(&ctx->corr_ready, cudaEventDisableTiming) != cudaSuccess) return fail(SCF_ERR_CUDA);
     for (int e = 0; e < 8; ++e) cudaEventCreate(&ctx->ev[e]);
     if (cudaMallocHost(&ctx->h_scal, 64 * sizeof(double)) != cudaSuccess) return fail(SCF_ERR_OUT_OF_MEMORY);
     if (cudaMallocHost(&ctx->h_u32, 64 * sizeof(unsigned)) != cudaSuccess) return fail(SCF_ERR_OUT_OF_MEMORY);
@@ -906,6 +934,8 @@ int scf_ctx_destroy(scf_ctx *ctx)
     if (ctx->iter_exec) cudaGraphExecDestroy(ctx->iter_exec);
     if (ctx->h_scal) cudaFreeHost(ctx->h_scal);
     if (ctx->h_u32) cudaFreeHost(ctx->h_u32);
+    if (ctx->cst) { cudaStreamSynchronize(ctx->cst); cudaStreamDestroy(ctx->cst); }
+    if (ctx->corr_ready) cudaEventDestroy(ctx->corr_ready);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
     return SCF_OK;
@@ -987,11 +1017,16 @@ int scf_update_puvw(scf_ctx *ctx, const scf_poisson_in *in, const scf_correct_in
     auto t0 = std::chrono::steady_clock::now();
     int64_t bi = 0, bo = 0;
     cudaEventRecord(ctx->ev[6], ctx->st);
-    rc = stage(ctx, in, corr, u, v, w, p, &bi);
-    if (rc) return rc;
+    rc = stage(ctx, in, corr, u, v, w, p, &bi, true);
+    if (rc) { cudaStreamSynchronize(ctx->cst); ctx->corr_pending = false; return rc; }
     cudaEventRecord(ctx->ev[7], ctx->st);
     rc = run(ctx, true, stats);
-    if (rc && rc != SCF_ERR_NOT_CONVERGED) return rc;
+    if (rc && rc != SCF_ERR_NOT_CONVERGED) {
+        // the caller's arrays may go away on return: finish the copies first
+        cudaStreamSynchronize(ctx->cst);
+        ctx->corr_pending = false;
+        return rc;
+    }
     const int solve_rc = rc;
     float h2d_ms = 0.f;
     cudaEventElapsedTime(&h2d_ms, ctx->ev[6], ctx->ev[7]);
