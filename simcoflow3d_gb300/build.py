@@ -27,6 +27,7 @@ UNITS = {
     "scf_api.cu": [],
     "k_noalloc.cu": [],
     "k_adjoint.cu": [],
+    "k_cg_df.cu": [],
 }
 
 

@@ -305,6 +305,38 @@ __device__ __forceinline__ double term_memo(TermMemo &m, double p, double ar, do
     }
     return m.t;
 }
+// d - (double)hi rounded to FP32, where hi is d rounded to FP32: the lo part
+// of the double-float form of d.  Computed on the integer pipe (the
+// significands of d and hi aligned to d's exponent differ by less than
+// 2^29 units of d's last place); FP64 arithmetic is this GPU's scarcest
+// resource and this kernel is bound by it.  Zeros, subnormals and
+// non-finite values take the FP64 route.
+__device__ __forceinline__ float lo_part(double d, float hi)
+{
+    const long long db = __double_as_longlong(d);
+    const int ed = (int)((db >> 52) & 0x7ff);
+    const int hb = __float_as_int(hi);
+    const int eh8 = (hb >> 23) & 0xff;
+    if (ed != 0 && ed != 0x7ff && eh8 != 0 && eh8 != 0xff) {
+        const long long md = (db & 0xfffffffffffffLL) | (1LL << 52);
+        const long long mh = (long long)((hb & 0x7fffff) | 0x800000) << 29;
+        const int eh = eh8 - 127 + 1023;
+        long long diff;
+        bool ok = true;
+        if (eh == ed) diff = md - mh;
+        else if (eh == ed + 1) diff = md - (mh << 1);
+        else { diff = 0; ok = false; }
+        if (ok && diff > -(1LL << 30) && diff < (1LL << 30)) {
+            if (diff == 0) return 0.0f;
+            if (db < 0) diff = -diff;
+            const int fb = __float_as_int(__int2float_rn((int)diff));
+            const int ef = ((fb >> 23) & 0xff) + (ed - 1075);
+            if (ef >= 1 && ef <= 254) return __int_as_float((fb & ~(0xff << 23)) | (ef << 23));
+        }
+    }
+    return (float)(d - (double)hi);
+}
+
 // a*u with a == 1.0 short-cut (exact: 1.0*u == u)
 __device__ __forceinline__ double amul(double ar, double u) { return bits(ar) == 0x3ff0000000000000ull ? u : ar * u; }
 }  // namespace
@@ -341,6 +373,7 @@ __global__ void __launch_bounds__(128) k_operator(AsmArgs a, OpArgs o)
             o.extra[g] = 0.0; o.b[g] = 0.0; o.active[g] = 0;
             if (MIXED) {
                 o.diag32[g] = -1.0f; o.cE32[g] = 0.0f; o.cN32[g] = 0.0f; o.cT32[g] = 0.0f;
+                o.diag_lo[g] = 0.0f; o.cE_lo[g] = 0.0f; o.cN_lo[g] = 0.0f; o.cT_lo[g] = 0.0f;
                 o.extra32[g] = 0.0f;
             }
             continue;
@@ -417,7 +450,12 @@ __global__ void __launch_bounds__(128) k_operator(AsmArgs a, OpArgs o)
         o.active[g] = 1;
         if (MIXED) {
             o.diag32[g] = d32;
-            o.cE32[g] = (float)cE; o.cN32[g] = (float)cN; o.cT32[g] = (float)cT;
+            o.diag_lo[g] = lo_part(dg, d32);
+            const float e32 = (float)cE, n32 = (float)cN, t32 = (float)cT;
+            o.cE32[g] = e32; o.cN32[g] = n32; o.cT32[g] = t32;
+            o.cE_lo[g] = lo_part(cE, e32);
+            o.cN_lo[g] = lo_part(cN, n32);
+            o.cT_lo[g] = lo_part(cT, t32);
             o.extra32[g] = (float)ex;
         }
     }

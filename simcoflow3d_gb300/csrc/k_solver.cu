@@ -157,6 +157,12 @@ __global__ void __launch_bounds__(1024) k_reduce_alpha(const double *__restrict_
     }
 }
 
+void reduce_alpha(Reducer &R, int nblocks, bool singular, cudaStream_t st, int *launches)
+{
+    k_reduce_alpha<<<1, 1024, 0, st>>>(R.partials, nblocks, R.max_blocks, R.scal, singular ? 1 : 0);
+    *launches += 1;
+}
+
 void cg_spmv_dot(const LevelView<double> &A, const double *p, double *q, Reducer &R, bool singular,
                  cudaStream_t st, int *launches, KTimer *kt)
 {

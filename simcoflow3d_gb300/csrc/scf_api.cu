@@ -65,6 +65,7 @@ struct scf_ctx {
     double *diag, *dinv, *cE, *cN, *cT, *extra, *b;
     unsigned char *active;
     float *diag32, *cE32, *cN32, *cT32, *extra32;
+    float *diag_lo, *cE_lo, *cN_lo, *cT_lo;   // double-float remainders of the FP64 operator (mixed)
     // CG vectors
     double *x, *r, *p, *q;
     double *xbest;             // best round-end iterate of a solve that restarts
@@ -234,6 +235,10 @@ int ensure_mg(scf_ctx *ctx)
         DALLOC(ctx->mgmem, ctx->cN32, L0.tot);
         DALLOC(ctx->mgmem, ctx->cT32, L0.tot);
         DALLOC(ctx->mgmem, ctx->extra32, L0.tot);
+        DALLOC(ctx->mgmem, ctx->diag_lo, L0.tot);
+        DALLOC(ctx->mgmem, ctx->cE_lo, L0.tot);
+        DALLOC(ctx->mgmem, ctx->cN_lo, L0.tot);
+        DALLOC(ctx->mgmem, ctx->cT_lo, L0.tot);
         DALLOC(ctx->mgmem, L0.b, L0.tot);
         L0.diag = ctx->diag32; L0.dinv = nullptr; L0.cE = ctx->cE32; L0.cN = ctx->cN32; L0.cT = ctx->cT32;
         L0.extra = ctx->extra32; L0.active = ctx->active;
@@ -317,6 +322,7 @@ int assemble(scf_ctx *ctx)
     o.extra = ctx->extra; o.b = ctx->b; o.active = ctx->active;
     const bool mixed = ctx->opts.precision == SCF_PREC_MIXED;
     o.diag32 = ctx->diag32; o.cE32 = ctx->cE32; o.cN32 = ctx->cN32; o.cT32 = ctx->cT32;
+    o.diag_lo = ctx->diag_lo; o.cE_lo = ctx->cE_lo; o.cN_lo = ctx->cN_lo; o.cT_lo = ctx->cT_lo;
     o.extra32 = ctx->extra32;
     const double rho_ref = ctx->opts.rho_ref > 0.0 ? ctx->opts.rho_ref : ctx->opts.rho_l;
     int e = launch_assemble(a, o, mixed, ctx->use_rho ? ctx->adj_rho : nullptr, rho_ref, ctx->st, ctx->h_u32,
@@ -437,6 +443,45 @@ T *precondition(scf_ctx *ctx, MgLevel<T> *L, const ChebCoef &cc, bool first_done
                         ctx->st, &ctx->launches, ctx->kt.on ? &ctx->kt : nullptr);
 }
 
+// Fine operator of the mixed CG in double-float form.
+DfOp df_view(scf_ctx *ctx)
+{
+    DfOp D;
+    D.hi = ctx->L32[0].view();
+    D.dlo = ctx->diag_lo; D.elo = ctx->cE_lo; D.nlo = ctx->cN_lo; D.tlo = ctx->cT_lo;
+    return D;
+}
+
+// New search direction p = z + beta p: FP64 vectors, or (mixed) double-float
+// vectors held in the same buffers.
+template <typename T>
+void cg_direction(scf_ctx *ctx, const T *z, bool first)
+{
+    if constexpr (sizeof(T) == 4)
+        df_pupdate(df_view(ctx), z, (float2 *)ctx->p, ctx->R.scal, first, ctx->st, &ctx->launches);
+    else
+        cg_pupdate<double>(fine_view(ctx), z, ctx->p, ctx->R.scal, first, ctx->st, &ctx->launches);
+}
+
+// SpMV with (p, Ap) and the x/r update with (r, r); the update also writes
+// level 0's first smoothing step when fuse_first() holds.
+template <typename T>
+void cg_step(scf_ctx *ctx, MgLevel<T> *L, const ChebCoef &cc, bool singular, KTimer *kt)
+{
+    const bool fuse = fuse_first(ctx);
+    if constexpr (sizeof(T) == 4) {
+        const DfOp D = df_view(ctx);
+        df_spmv_dot(D, (const float2 *)ctx->p, (float2 *)ctx->q, ctx->R, singular, ctx->st, &ctx->launches, kt);
+        df_cg_update(D, (float2 *)ctx->x, (float2 *)ctx->r, (const float2 *)ctx->p, (const float2 *)ctx->q,
+                     L[0].b, fuse ? L[0].x : nullptr, cc.first, ctx->R, ctx->st, &ctx->launches, kt);
+    } else {
+        const LevelView<double> A = fine_view(ctx);
+        cg_spmv_dot(A, ctx->p, ctx->q, ctx->R, singular, ctx->st, &ctx->launches, kt);
+        cg_update<double>(A, ctx->x, ctx->r, ctx->p, ctx->q, nullptr, L[0].view(), fuse ? L[0].x : nullptr,
+                          cc.first, ctx->R, ctx->st, &ctx->launches, kt);
+    }
+}
+
 // The part of a CG iteration after the stopping test: precondition, new
 // search direction, SpMV with (p, Ap) and the x/r update with (r, r).  Its
 // kernel sequence is fixed for a context, so it is captured once as a CUDA
@@ -446,16 +491,11 @@ template <typename T>
 void iteration_kernels(scf_ctx *ctx, MgLevel<T> *L, const ChebCoef &cc, bool singular)
 {
     const LevelView<double> A = fine_view(ctx);
-    const bool mixed = sizeof(T) == 4;
-    float *rlow = mixed ? (float *)L[0].b : nullptr;
     KTimer *kt = ctx->kt.on ? &ctx->kt : nullptr;
     T *z = precondition<T>(ctx, L, cc, fuse_first(ctx));
     cg_dot_rz<T>(A, ctx->r, (const T *)L[0].b, z, ctx->R, ctx->st, &ctx->launches);
-    cg_pupdate<T>(A, z, ctx->p, ctx->R.scal, false, ctx->st, &ctx->launches);
-    cg_spmv_dot(A, ctx->p, ctx->q, ctx->R, singular, ctx->st, &ctx->launches, kt);
-    const bool fuse = fuse_first(ctx);
-    cg_update<T>(A, ctx->x, ctx->r, ctx->p, ctx->q, (T *)(mixed ? (void *)rlow : nullptr), L[0].view(),
-                 fuse ? L[0].x : nullptr, cc.first, ctx->R, ctx->st, &ctx->launches, kt);
+    cg_direction<T>(ctx, z, false);
+    cg_step<T>(ctx, L, cc, singular, kt);
 }
 
 template <typename T>
@@ -538,11 +578,17 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
     int restarts = 0;
     bool stalled = false, have_best = false;
     double best_rel = HUGE_VAL;
+    const int ng = ctx->d.ng;
     for (;;) {
-        if (mixed) copy_to_low(A, ctx->r, rlow, ctx->st, &ctx->launches);
+        if (mixed) {
+            // x and r (FP64 here) become double-float for the round
+            copy_to_low(A, ctx->r, rlow, ctx->st, &ctx->launches);
+            df_from_double(ctx->x, (float2 *)ctx->x, ng, ctx->st, &ctx->launches);
+            df_from_double(ctx->r, (float2 *)ctx->r, ng, ctx->st, &ctx->launches);
+        }
         T *z = precondition<T>(ctx, L, cc, false);
         cg_dot_rz<T>(A, ctx->r, (const T *)L[0].b, z, ctx->R, ctx->st, &ctx->launches);
-        cg_pupdate<T>(A, z, ctx->p, ctx->R.scal, true, ctx->st, &ctx->launches);
+        cg_direction<T>(ctx, z, true);
         bool conv = false;
         stalled = false;
         double best = HUGE_VAL;
@@ -550,13 +596,7 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
         bool replayed = false;
         if (its < ctx->opts.max_iter) {
             ++its;
-            KTimer *kt = ctx->kt.on ? &ctx->kt : nullptr;
-            cg_spmv_dot(A, ctx->p, ctx->q, ctx->R, singular, ctx->st, &ctx->launches, kt);
-            // the update also writes level 0's first smoothing step when the
-            // hierarchy has more than one level
-            const bool fuse = fuse_first(ctx);
-            cg_update<T>(A, ctx->x, ctx->r, ctx->p, ctx->q, (T *)(mixed ? (void *)rlow : nullptr), L[0].view(),
-                         fuse ? L[0].x : nullptr, cc.first, ctx->R, ctx->st, &ctx->launches, kt);
+            cg_step<T>(ctx, L, cc, singular, ctx->kt.on ? &ctx->kt : nullptr);
         }
         while (true) {
             const double rr = read_scal(ctx, S_RR);
@@ -582,6 +622,7 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
         }
         // true FP64 residual (the refinement check); for an all-Neumann
         // system also the mean of x, removed below
+        if (mixed) df_to_double((const float2 *)ctx->x, ctx->x, ng, ctx->st, &ctx->launches);
         final_residual(A, ctx->active, ctx->b, ctx->x, ctx->r, singular, ctx->R, ctx->st, &ctx->launches);
         rel = std::sqrt(read_scal(ctx, S_RR)) / bn;
         if (rel <= tol || !(conv || stalled) || its >= ctx->opts.max_iter || restarts >= ctx->opts.max_rounds)
@@ -1257,7 +1298,14 @@ int scf_debug_time_kernel(scf_ctx *ctx, int kernel, int reps, double *ms_per_lau
         case SCF_K_SMOOTH:
             if (mixed) probe_smooth<float>(ctx->L32[0], cc, ctx->st); else probe_smooth<double>(ctx->L64[0], cc, ctx->st);
             break;
-        case SCF_K_SPMV: probe_spmv(fine_view(ctx), ctx->p, ctx->q, ctx->R, ctx->st); break;
+        case SCF_K_SPMV:
+            if (mixed) {
+                int dummy = 0;
+                df_spmv_dot(df_view(ctx), (const float2 *)ctx->p, (float2 *)ctx->q, ctx->R, false, ctx->st, &dummy);
+            } else {
+                probe_spmv(fine_view(ctx), ctx->p, ctx->q, ctx->R, ctx->st);
+            }
+            break;
         case SCF_K_RESTRICT:
             if (mixed) probe_restrict<float>(ctx->L32[0], ctx->L32[1], ctx->st);
             else probe_restrict<double>(ctx->L64[0], ctx->L64[1], ctx->st);
@@ -1269,8 +1317,8 @@ int scf_debug_time_kernel(scf_ctx *ctx, int kernel, int reps, double *ms_per_lau
         default: {
             int dummy = 0;
             if (mixed)
-                cg_update<float>(fine_view(ctx), ctx->x, ctx->r, ctx->p, ctx->q, ctx->L32[0].b, ctx->L32[0].view(),
-                                 ctx->L32[0].x, cc.first, ctx->R, ctx->st, &dummy);
+                df_cg_update(df_view(ctx), (float2 *)ctx->x, (float2 *)ctx->r, (const float2 *)ctx->p,
+                             (const float2 *)ctx->q, ctx->L32[0].b, ctx->L32[0].x, cc.first, ctx->R, ctx->st, &dummy);
             else
                 cg_update<double>(fine_view(ctx), ctx->x, ctx->r, ctx->p, ctx->q, nullptr, ctx->L64[0].view(),
                                   ctx->L64[0].x, cc.first, ctx->R, ctx->st, &dummy);

@@ -35,6 +35,7 @@ struct OpArgs {
     double *diag, *dinv, *cE, *cN, *cT, *extra, *b;
     unsigned char *active;
     float *diag32, *cE32, *cN32, *cT32, *extra32;  // mixed only (FP32 levels derive 1/diag)
+    float *diag_lo, *cE_lo, *cN_lo, *cT_lo;        // mixed only: v - (double)(float)v
 };
 
 // rho: per-cell densities (ghosted) or nullptr for the reference's two-phase
@@ -146,6 +147,24 @@ void probe_restrict(MgLevel<T> &F, MgLevel<T> &C, cudaStream_t st);
 template <typename T>
 void probe_prolong(MgLevel<T> &F, MgLevel<T> &C, const ChebCoef &cc, cudaStream_t st);
 void probe_spmv(const LevelView<double> &A, const double *p, double *q, Reducer &R, cudaStream_t st);
+
+// Fine operator of the mixed solver's CG in double-float form: hi parts are
+// the FP32 level-0 copy, lo parts the rounding remainders written by the
+// assembly (diag, cE, cN, cT).
+struct DfOp {
+    LevelView<float> hi;
+    const float *dlo, *elo, *nlo, *tlo;
+};
+void df_spmv_dot(const DfOp &A, const float2 *p, float2 *q, Reducer &R, bool singular, cudaStream_t st,
+                 int *launches, KTimer *kt = nullptr);
+void df_cg_update(const DfOp &A, float2 *x, float2 *r, const float2 *p, const float2 *q, float *rlow, float *x0,
+                  double first, Reducer &R, cudaStream_t st, int *launches, KTimer *kt = nullptr);
+void df_pupdate(const DfOp &A, const float *z, float2 *p, const double *scal, bool first, cudaStream_t st,
+                int *launches);
+void df_from_double(const double *src, float2 *dst, int n, cudaStream_t st, int *launches);
+void df_to_double(const float2 *src, double *dst, int n, cudaStream_t st, int *launches);
+// alpha and the mean of A p from the two-lane partials of an SpMV
+void reduce_alpha(Reducer &R, int nblocks, bool singular, cudaStream_t st, int *launches);
 
 // CG building blocks on the fine level (FP64 vectors, ghosted layout).
 void cg_spmv_dot(const LevelView<double> &A, const double *p, double *q, Reducer &R, bool singular,
