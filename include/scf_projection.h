@@ -59,9 +59,10 @@ enum scf_status {
 /* ---- options ------------------------------------------------------------ */
 enum scf_precision {
     SCF_PREC_FP64 = 0,   /* FP64 CG with an FP64 multigrid preconditioner     */
-    SCF_PREC_MIXED = 1   /* FP64 CG (vectors, operator, dot products, true
-                            residual) with an FP32 multigrid V-cycle as the
-                            preconditioner; FP64 coarsest solve              */
+    SCF_PREC_MIXED = 1   /* CG in double-float arithmetic (FP32 pairs, about
+                            48 significand bits; FP64 true residual at the end
+                            of each round) with an FP32 multigrid V-cycle as
+                            the preconditioner; FP64 coarsest solve           */
 };
 
 typedef struct scf_opts {
