@@ -98,6 +98,24 @@ struct CoefMemo {
     bool valid;
 };
 
+// The FP64 work of a memo miss lives in functions that are never inlined:
+// a call cannot be executed speculatively, while inline code in a short
+// branch is often turned into unconditional arithmetic plus a select -- on
+// this GPU that put every division and product back on every cell.
+__device__ __noinline__ double coef_slow(double dp, double dg, double betap, double betam, double beta)
+{
+    return coef_expr(dp, dg, betap, betam, beta);
+}
+
+// GFM beta of a wet-dry face (ProjectionP.f90:155-156,176,218)
+__device__ __noinline__ double beta_interface(double phic, double phin, double tol, int pc, double betap,
+                                              double betam)
+{
+    const double x = fabs(phic), y = fabs(phin);
+    const double lam = x / ((x + y) + tol);
+    return pc == 1 ? lam * betam + (1.0 - lam) * betap : lam * betap + (1.0 - lam) * betam;
+}
+
 __device__ __forceinline__ double coef_memo(CoefMemo &m, double dp, double dg, double beta, double betap,
                                             double betam)
 {
@@ -105,7 +123,7 @@ __device__ __forceinline__ double coef_memo(CoefMemo &m, double dp, double dg, d
                              c = __double_as_longlong(beta);
     if (!m.valid || a != m.dp || b != m.dg || c != m.beta) {
         m.dp = a; m.dg = b; m.beta = c; m.valid = true;
-        m.coef = coef_expr(dp, dg, betap, betam, beta);
+        m.coef = coef_slow(dp, dg, betap, betam, beta);
     }
     return m.coef;
 }
@@ -163,8 +181,7 @@ __global__ void __launch_bounds__(128) k_pocoef(AsmArgs a)
                 if (pn == pc) {
                     beta = pc == 1 ? a.betam : a.betap;
                 } else if (pn != 0) {
-                    const double lam = lamda_of(a, gc, gn);
-                    beta = pc == 1 ? lam * a.betam + (1.0 - lam) * a.betap : lam * a.betap + (1.0 - lam) * a.betam;
+                    beta = beta_interface(a.phil[gc], a.phil[gn], a.tol, pc, a.betap, a.betam);
                 } else if (pc == 1 ? (maskW >> f) & 1u : (maskD >> f) & 1u) {
                     beta = pc == 1 ? carryW[f] : carryD[f];
                     pn = -1;   // carried, not assigned
@@ -297,13 +314,39 @@ struct TermMemo {
     double t;
     bool valid;
 };
+__device__ __noinline__ double prod4(double p, double ar, double d1, double d2) { return p * ar * d1 * d2; }
+__device__ __noinline__ double mul_slow(double a, double b) { return a * b; }
 __device__ __forceinline__ double term_memo(TermMemo &m, double p, double ar, double d1, double d2)
 {
     if (!m.valid || bits(p) != m.p || bits(ar) != m.ar || bits(d1) != m.d1 || bits(d2) != m.d2) {
         m.p = bits(p); m.ar = bits(ar); m.d1 = bits(d1); m.d2 = bits(d2); m.valid = true;
-        m.t = p * ar * d1 * d2;
+        m.t = prod4(p, ar, d1, d2);
     }
     return m.t;
+}
+// The diagonal of a row: the six own-side terms minus those of Neumann
+// boundary faces (bit f of nb set) (ProjectionP.f90:378-430).
+__device__ __noinline__ double row_diag(double t1, double t2, double t3, double t4, double t5, double t6, int nb)
+{
+    double v = t1 + t2 + t3 + t4 + t5 + t6;
+    if (nb & 1) v = v - t1;
+    if (nb & 2) v = v - t2;
+    if (nb & 4) v = v - t3;
+    if (nb & 8) v = v - t4;
+    if (nb & 16) v = v - t5;
+    if (nb & 32) v = v - t6;
+    return v;
+}
+__device__ __noinline__ double recip_slow(double v) { return v > 0.0 ? 1.0 / v : 0.0; }
+// -dy*dz, dx*dz, dx*dy of the rhs (ProjectionP.f90:521-526)
+__device__ __noinline__ double3 spacing_products(double dx, double dy, double dz)
+{
+    return make_double3(-dy * dz, dx * dz, dx * dy);
+}
+// (vof - vofO)*dx*dy*dz/dt (ProjectionP.f90:527)
+__device__ __noinline__ double vof_term(double vf, double vo, double dx, double dy, double dz, double dt)
+{
+    return (vf - vo) * dx * dy * dz / dt;
 }
 // d - (double)hi rounded to FP32, where hi is d rounded to FP32: the lo part
 // of the double-float form of d.  Computed on the integer pipe (the
@@ -338,7 +381,10 @@ __device__ __forceinline__ float lo_part(double d, float hi)
 }
 
 // a*u with a == 1.0 short-cut (exact: 1.0*u == u)
-__device__ __forceinline__ double amul(double ar, double u) { return bits(ar) == 0x3ff0000000000000ull ? u : ar * u; }
+__device__ __forceinline__ double amul(double ar, double u)
+{
+    return bits(ar) == 0x3ff0000000000000ull ? u : mul_slow(ar, u);
+}
 }  // namespace
 
 template <bool MIXED>
@@ -390,15 +436,11 @@ __global__ void __launch_bounds__(128) k_operator(AsmArgs a, OpArgs o)
         const bool bnd = i == 1 || j == 1 || k == 1 || i == d.I || j == d.J || k == d.K;
         if (bnd || !rvalid || bits(t1) != rt[0] || bits(t2) != rt[1] || bits(t3) != rt[2] || bits(t4) != rt[3] ||
             bits(t5) != rt[4] || bits(t6) != rt[5]) {
-            double v = t1 + t2 + t3 + t4 + t5 + t6;
-            if (fl[0] == 1 && i == 1) v = v - t1;
-            if (fl[2] == 1 && j == 1) v = v - t2;
-            if (fl[4] == 1 && k == 1) v = v - t3;
-            if (fl[1] == 1 && i == d.I) v = v - t4;
-            if (fl[3] == 1 && j == d.J) v = v - t5;
-            if (fl[5] == 1 && k == d.K) v = v - t6;
-            dg = v;
-            if (!MIXED) dinv = dg > 0.0 ? 1.0 / dg : 0.0;
+            const int nb = (fl[0] == 1 && i == 1 ? 1 : 0) | (fl[2] == 1 && j == 1 ? 2 : 0) |
+                           (fl[4] == 1 && k == 1 ? 4 : 0) | (fl[1] == 1 && i == d.I ? 8 : 0) |
+                           (fl[3] == 1 && j == d.J ? 16 : 0) | (fl[5] == 1 && k == d.K ? 32 : 0);
+            dg = row_diag(t1, t2, t3, t4, t5, t6, nb);
+            if (!MIXED) dinv = recip_slow(dg);
             if (MIXED) d32 = (float)dg;
             // a boundary row is never reused by an interior one
             rvalid = !bnd;
@@ -416,7 +458,8 @@ __global__ void __launch_bounds__(128) k_operator(AsmArgs a, OpArgs o)
         // Fortran expression: -dy*dz*(A) - dx*dz*(B) - dx*dy*(C)
         if (!pvalid || bits(dx) != pdx || bits(dy) != pdy || bits(dz) != pdz) {
             pdx = bits(dx); pdy = bits(dy); pdz = bits(dz); pvalid = true;
-            dydz = -dy * dz; dxdz = dx * dz; dxdy = dx * dy;
+            const double3 sp = spacing_products(dx, dy, dz);
+            dydz = sp.x; dxdz = sp.y; dxdy = sp.z;
         }
         const double A = amul(eE, a.us[g]) - amul(eW, a.us[g - 1]);
         const double B = amul(nN, a.vs[g]) - amul(nS, a.vs[g - sy]);
@@ -426,7 +469,7 @@ __global__ void __launch_bounds__(128) k_operator(AsmArgs a, OpArgs o)
         if (bits(vf) == bits(vo) && finite_bits(vf)) {
             r = r + 0.0;   // (vof - vofO)*dx*dy*dz/dt is +0 exactly
         } else {
-            r = r + (vf - vo) * dx * dy * dz / a.dt;
+            r = r + vof_term(vf, vo, dx, dy, dz, a.dt);
         }
         if (bnd) {
             if (fl[0] == 0 && i == 1) r = r + p1 * a.bvar[0][(j - 1) + d.J * (k - 1)];
