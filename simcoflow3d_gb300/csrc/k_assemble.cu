@@ -136,6 +136,35 @@ __global__ void __launch_bounds__(256) k_phase(AsmArgs a)
         a.phase[g] = (unsigned char)phase_of(a.vofl[g], a.vof[g], a.phil[g], a.epsi);
 }
 
+// Inputs of the six faces of one cell: phases of the cell and of its
+// neighbours W,S,B,E,N,T, and the Dp / DGrid pair of each face.
+struct FaceIn {
+    int ph[7];        // 0..5 neighbours in face order, 6 the cell
+    double dp[6], dg[6];
+};
+
+// Loads of the cell (i,j,k) except the B face, whose inputs are those of the
+// T face of (i,j,k-1) and are carried by the caller.
+__device__ __forceinline__ void load_face_in(const AsmArgs &a, int i, int j, int k, int im, int jm, FaceIn &v)
+{
+    const Dims &d = a.d;
+    const int sy = d.gx, sz = d.gx * d.gy;
+    const int gc = gidx(d, i, j, k), nc = nidx(d, i, j, k);
+    v.ph[6] = a.phase[gc];
+    v.ph[0] = a.phase[gc - 1]; v.ph[1] = a.phase[gc - sy];
+    v.ph[3] = a.phase[gc + 1]; v.ph[4] = a.phase[gc + sy]; v.ph[5] = a.phase[gc + sz];
+    // Dp(im,jm,km) and DGrid(max(im,1),...) (ProjectionP.f90:145-153)
+    v.dp[0] = a.dpu[gc - 1];  v.dg[0] = a.udx[nidx(d, im, j, k)];
+    v.dp[1] = a.dpv[gc - sy]; v.dg[1] = a.vdy[nidx(d, i, jm, k)];
+    v.dp[3] = a.dpu[gc];      v.dg[3] = a.udx[nc];
+    v.dp[4] = a.dpv[gc];      v.dg[4] = a.vdy[nc];
+    v.dp[5] = a.dpw[gc];      v.dg[5] = a.wdz[nc];
+}
+
+// Each thread marches one k segment of one (i,j) column.  The inputs of the
+// next cell are loaded before the current one is processed (their latency
+// overlaps its work), and the B face reuses the T-face inputs of the cell
+// below.
 __global__ void __launch_bounds__(128) k_pocoef(AsmArgs a)
 {
     const Dims &d = a.d;
@@ -157,31 +186,30 @@ __global__ void __launch_bounds__(128) k_pocoef(AsmArgs a)
         memo[f].valid = false; memo[f].dp = memo[f].dg = memo[f].beta = 0ull; memo[f].coef = 0.0;
     }
     const int im = i > 1 ? i - 1 : 1, jm = j > 1 ? j - 1 : 1;
+    FaceIn cur, nxt;
+    load_face_in(a, i, j, kbeg, im, jm, cur);
+    {   // B face of the first cell: Dp(i,j,kbeg-1), DGrid(i,j,max(kbeg-1,1))
+        const int gc = gidx(d, i, j, kbeg);
+        cur.ph[2] = a.phase[gc - sz];
+        cur.dp[2] = a.dpw[gc - sz];
+        cur.dg[2] = a.wdz[nidx(d, i, j, kbeg > 1 ? kbeg - 1 : 1)];
+    }
     for (int k = kbeg; k <= kend; ++k) {
+        if (k < kend) load_face_in(a, i, j, k + 1, im, jm, nxt);
         const int gc = gidx(d, i, j, k), nc = nidx(d, i, j, k);
-        const int pc = a.phase[gc];
-        const int km = k > 1 ? k - 1 : 1;
+        const int pc = cur.ph[6];
 #pragma unroll
         for (int f = 0; f < 6; ++f) {
             double coef = 0.0;
             if (pc != 0) {
-                const int gn = gc + goff[f];
-                int pn = a.phase[gn];
-                double dp, dg;
-                switch (f) {   // Dp(im,jm,km) and DGrid(max(im,1),...) (ProjectionP.f90:145-153)
-                case 0: dp = a.dpu[gc - 1];  dg = a.udx[nidx(d, im, j, k)]; break;
-                case 1: dp = a.dpv[gc - sy]; dg = a.vdy[nidx(d, i, jm, k)]; break;
-                case 2: dp = a.dpw[gc - sz]; dg = a.wdz[nidx(d, i, j, km)]; break;
-                case 3: dp = a.dpu[gc];      dg = a.udx[nc]; break;
-                case 4: dp = a.dpv[gc];      dg = a.vdy[nc]; break;
-                default: dp = a.dpw[gc];     dg = a.wdz[nc]; break;
-                }
+                int pn = cur.ph[f];
+                const double dp = cur.dp[f], dg = cur.dg[f];
                 double beta;
                 bool have = true;
                 if (pn == pc) {
                     beta = pc == 1 ? a.betam : a.betap;
                 } else if (pn != 0) {
-                    beta = beta_interface(a.phil[gc], a.phil[gn], a.tol, pc, a.betap, a.betam);
+                    beta = beta_interface(a.phil[gc], a.phil[gc + goff[f]], a.tol, pc, a.betap, a.betam);
                 } else if (pc == 1 ? (maskW >> f) & 1u : (maskD >> f) & 1u) {
                     beta = pc == 1 ? carryW[f] : carryD[f];
                     pn = -1;   // carried, not assigned
@@ -204,6 +232,10 @@ __global__ void __launch_bounds__(128) k_pocoef(AsmArgs a)
                 }
             }
             a.pocoef[nc + (long long)d.n * f] = coef;
+        }
+        if (k < kend) {
+            nxt.ph[2] = pc; nxt.dp[2] = cur.dp[5]; nxt.dg[2] = cur.dg[5];
+            cur = nxt;
         }
     }
 #pragma unroll
@@ -337,6 +369,18 @@ __device__ __noinline__ double row_diag(double t1, double t2, double t3, double 
     if (nb & 32) v = v - t6;
     return v;
 }
+// 0 + the terms of the faces in mask m, in face order (ProjectionP.f90:378-430)
+__device__ __noinline__ double extra_sum(double t1, double t2, double t3, double t4, double t5, double t6, int m)
+{
+    double v = 0.0;
+    if (m & 1) v += t1;
+    if (m & 2) v += t2;
+    if (m & 4) v += t3;
+    if (m & 8) v += t4;
+    if (m & 16) v += t5;
+    if (m & 32) v += t6;
+    return v;
+}
 __device__ __noinline__ double recip_slow(double v) { return v > 0.0 ? 1.0 / v : 0.0; }
 // -dy*dz, dx*dz, dx*dy of the rhs (ProjectionP.f90:521-526)
 __device__ __noinline__ double3 spacing_products(double dx, double dy, double dz)
@@ -352,11 +396,12 @@ __device__ __noinline__ double vof_term(double vf, double vo, double dx, double 
 // of the double-float form of d.  Computed on the integer pipe (the
 // significands of d and hi aligned to d's exponent differ by less than
 // 2^29 units of d's last place); FP64 arithmetic is this GPU's scarcest
-// resource and this kernel is bound by it.  Zeros, subnormals and
+// resource and this kernel is bound by it.  Zeros give +0; subnormals and
 // non-finite values take the FP64 route.
 __device__ __forceinline__ float lo_part(double d, float hi)
 {
     const long long db = __double_as_longlong(d);
+    if (((unsigned long long)db << 1) == 0) return 0.0f;   // d - (double)hi = +0 for d = +-0
     const int ed = (int)((db >> 52) & 0x7ff);
     const int hb = __float_as_int(hi);
     const int eh8 = (hb >> 23) & 0xff;
@@ -380,6 +425,26 @@ __device__ __forceinline__ float lo_part(double d, float hi)
     return (float)(d - (double)hi);
 }
 
+// d rounded to FP32 (round to nearest even) on the integer pipe, for results
+// in FP32's normal range, and of zeros; the rest (subnormal or out-of-range
+// results, non-finite values) take the conversion instruction, which runs on
+// the FP64 pipe.
+__device__ __forceinline__ float to_f32(double d)
+{
+    const unsigned long long b = bits(d);
+    const int e = (int)((b >> 52) & 0x7ff);
+    if ((b << 1) == 0) return __uint_as_float((unsigned)(b >> 32));   // +-0
+    if (e >= 1023 - 126 && e <= 1023 + 127) {
+        const unsigned long long m = b & 0xfffffffffffffull;
+        const unsigned hi = (unsigned)(m >> 29), rem = (unsigned)(m & 0x1fffffffu);
+        unsigned r = ((unsigned)(e - 1023 + 127) << 23) | hi;
+        if (rem > 0x10000000u || (rem == 0x10000000u && (hi & 1u))) r += 1u;   // a carry rounds into the exponent
+        r |= (unsigned)(b >> 32) & 0x80000000u;
+        return __uint_as_float(r);
+    }
+    return (float)d;
+}
+
 // a*u with a == 1.0 short-cut (exact: 1.0*u == u)
 __device__ __forceinline__ double amul(double ar, double u)
 {
@@ -401,9 +466,10 @@ __global__ void __launch_bounds__(128) k_operator(AsmArgs a, OpArgs o)
     TermMemo tm[6];
 #pragma unroll
     for (int f = 0; f < 6; ++f) { tm[f].valid = false; tm[f].p = tm[f].ar = tm[f].d1 = tm[f].d2 = 0ull; tm[f].t = 0.0; }
-    // memo of the row (diag and dependants) on the six terms
+    // memo of the row (diag and dependants) on the six terms and the
+    // Neumann-face mask
     unsigned long long rt[6] = {0, 0, 0, 0, 0, 0};
-    bool rvalid = false;
+    int rnb = -1;
     double dg = 0.0, dinv = 0.0;
     float d32 = 0.f;
     // memo of the spacing products of the rhs
@@ -434,25 +500,28 @@ __global__ void __launch_bounds__(128) k_operator(AsmArgs a, OpArgs o)
         const double t3 = term_memo(tm[2], p3, tB, dx, dy), t4 = term_memo(tm[3], p4, eE, dy, dz);
         const double t5 = term_memo(tm[4], p5, nN, dx, dz), t6 = term_memo(tm[5], p6, tT, dx, dy);
         const bool bnd = i == 1 || j == 1 || k == 1 || i == d.I || j == d.J || k == d.K;
-        if (bnd || !rvalid || bits(t1) != rt[0] || bits(t2) != rt[1] || bits(t3) != rt[2] || bits(t4) != rt[3] ||
+        const int nb = (fl[0] == 1 && i == 1 ? 1 : 0) | (fl[2] == 1 && j == 1 ? 2 : 0) |
+                       (fl[4] == 1 && k == 1 ? 4 : 0) | (fl[1] == 1 && i == d.I ? 8 : 0) |
+                       (fl[3] == 1 && j == d.J ? 16 : 0) | (fl[5] == 1 && k == d.K ? 32 : 0);
+        if (nb != rnb || bits(t1) != rt[0] || bits(t2) != rt[1] || bits(t3) != rt[2] || bits(t4) != rt[3] ||
             bits(t5) != rt[4] || bits(t6) != rt[5]) {
-            const int nb = (fl[0] == 1 && i == 1 ? 1 : 0) | (fl[2] == 1 && j == 1 ? 2 : 0) |
-                           (fl[4] == 1 && k == 1 ? 4 : 0) | (fl[1] == 1 && i == d.I ? 8 : 0) |
-                           (fl[3] == 1 && j == d.J ? 16 : 0) | (fl[5] == 1 && k == d.K ? 32 : 0);
             dg = row_diag(t1, t2, t3, t4, t5, t6, nb);
             if (!MIXED) dinv = recip_slow(dg);
-            if (MIXED) d32 = (float)dg;
-            // a boundary row is never reused by an interior one
-            rvalid = !bnd;
+            if (MIXED) d32 = to_f32(dg);
+            rnb = nb;
             rt[0] = bits(t1); rt[1] = bits(t2); rt[2] = bits(t3); rt[3] = bits(t4); rt[4] = bits(t5); rt[5] = bits(t6);
         }
-        double cE = 0.0, cN = 0.0, cT = 0.0, ex = 0.0;
-        if (i == 1) { if (fl[0] == 0) ex += t1; } else if (a.pos[n - 1] == -1) ex += t1;
-        if (j == 1) { if (fl[2] == 0) ex += t2; } else if (a.pos[n - d.I] == -1) ex += t2;
-        if (k == 1) { if (fl[4] == 0) ex += t3; } else if (a.pos[n - d.I * d.J] == -1) ex += t3;
-        if (i == d.I) { if (fl[1] == 0) ex += t4; } else if (a.pos[n + 1] == -1) ex += t4; else cE = t4;
-        if (j == d.J) { if (fl[3] == 0) ex += t5; } else if (a.pos[n + d.I] == -1) ex += t5; else cN = t5;
-        if (k == d.K) { if (fl[5] == 0) ex += t6; } else if (a.pos[n + d.I * d.J] == -1) ex += t6; else cT = t6;
+        // faces whose term goes to the extra diagonal part: Dirichlet
+        // boundary faces and faces to solid cells (bit f, order W,S,B,E,N,T)
+        double cE = 0.0, cN = 0.0, cT = 0.0;
+        int xm = 0;
+        if (i == 1) { if (fl[0] == 0) xm |= 1; } else if (a.pos[n - 1] == -1) xm |= 1;
+        if (j == 1) { if (fl[2] == 0) xm |= 2; } else if (a.pos[n - d.I] == -1) xm |= 2;
+        if (k == 1) { if (fl[4] == 0) xm |= 4; } else if (a.pos[n - d.I * d.J] == -1) xm |= 4;
+        if (i == d.I) { if (fl[1] == 0) xm |= 8; } else if (a.pos[n + 1] == -1) xm |= 8; else cE = t4;
+        if (j == d.J) { if (fl[3] == 0) xm |= 16; } else if (a.pos[n + d.I] == -1) xm |= 16; else cN = t5;
+        if (k == d.K) { if (fl[5] == 0) xm |= 32; } else if (a.pos[n + d.I * d.J] == -1) xm |= 32; else cT = t6;
+        const double ex = xm ? extra_sum(t1, t2, t3, t4, t5, t6, xm) : 0.0;
 
         // right-hand side (ProjectionP.f90:521-546), same rounding as the
         // Fortran expression: -dy*dz*(A) - dx*dz*(B) - dx*dy*(C)
@@ -467,7 +536,9 @@ __global__ void __launch_bounds__(128) k_operator(AsmArgs a, OpArgs o)
         double r = dydz * A - dxdz * B - dxdy * Cc;
         const double vf = a.vof[g], vo = a.vofo[g];
         if (bits(vf) == bits(vo) && finite_bits(vf)) {
-            r = r + 0.0;   // (vof - vofO)*dx*dy*dz/dt is +0 exactly
+            // (vof - vofO)*dx*dy*dz/dt is +0 exactly, and r + 0.0 is r except
+            // that -0 becomes +0
+            if (bits(r) == 0x8000000000000000ull) r = 0.0;
         } else {
             r = r + vof_term(vf, vo, dx, dy, dz, a.dt);
         }
@@ -480,7 +551,7 @@ __global__ void __launch_bounds__(128) k_operator(AsmArgs a, OpArgs o)
             if (fl[5] == 0 && k == d.K) r = r + p6 * a.bvar[5][(i - 1) + d.I * (j - 1)];
         }
         if (!finite_bits(dg)) atomicOr(a.flags, FLAG_NONFINITE);
-        else if (!(dg > 0.0)) atomicOr(a.flags, FLAG_BAD_DIAG);
+        else if ((long long)bits(dg) <= 0) atomicOr(a.flags, FLAG_BAD_DIAG);   // dg <= 0 (finite)
         if (!finite_bits(r) || !finite_bits(cE) || !finite_bits(cN) || !finite_bits(cT) || !finite_bits(ex))
             atomicOr(a.flags, FLAG_NONFINITE);
         if (a.phase[g] == 0) atomicOr(a.flags, FLAG_NEITHER_ACTIVE);
@@ -494,12 +565,12 @@ __global__ void __launch_bounds__(128) k_operator(AsmArgs a, OpArgs o)
         if (MIXED) {
             o.diag32[g] = d32;
             o.diag_lo[g] = lo_part(dg, d32);
-            const float e32 = (float)cE, n32 = (float)cN, t32 = (float)cT;
+            const float e32 = to_f32(cE), n32 = to_f32(cN), t32 = to_f32(cT);
             o.cE32[g] = e32; o.cN32[g] = n32; o.cT32[g] = t32;
             o.cE_lo[g] = lo_part(cE, e32);
             o.cN_lo[g] = lo_part(cN, n32);
             o.cT_lo[g] = lo_part(cT, t32);
-            o.extra32[g] = (float)ex;
+            o.extra32[g] = to_f32(ex);
         }
     }
 }
