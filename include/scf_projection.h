@@ -251,6 +251,15 @@ int scf_debug_precondition(scf_ctx *ctx, const double *r, double *z);
  * the right-hand side b (interior, 0 on solid cells).  Any may be NULL.     */
 int scf_debug_operator(scf_ctx *ctx, double *diag, double *cpl_e,
                        double *cpl_n, double *cpl_t, double *rhs);
+/* FP32 forms of the device operator of a SCF_PREC_MIXED context (interior
+ * arrays, solid cells included): hi = FP32 rounding (to nearest) of diag,
+ * the E/N/T couplings and the extra diagonal part; lo = FP32 rounding of the
+ * FP64 value minus hi, for diag and couplings (the double-float operator of
+ * the CG); extra = the FP64 extra diagonal part (Dirichlet and solid-face
+ * terms).  Any output may be NULL.                                         */
+int scf_debug_operator_f32(scf_ctx *ctx, float *diag_hi, float *e_hi, float *n_hi,
+                           float *t_hi, float *extra_hi, float *diag_lo, float *e_lo,
+                           float *n_lo, float *t_lo, double *extra);
 
 /* Times `reps` back-to-back launches of one kernel class of the last run's
  * state with CUDA events on the context's stream and reports the mean device

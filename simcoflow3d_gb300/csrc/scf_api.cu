@@ -1284,6 +1284,38 @@ int scf_debug_operator(scf_ctx *ctx, double *diag, double *cpl_e, double *cpl_n,
     return SCF_OK;
 }
 
+int scf_debug_operator_f32(scf_ctx *ctx, float *diag_hi, float *e_hi, float *n_hi, float *t_hi, float *extra_hi,
+                           float *diag_lo, float *e_lo, float *n_lo, float *t_lo, double *extra)
+{
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (ctx->opts.precision != SCF_PREC_MIXED) { set_err(ctx, "not a mixed-precision context"); return SCF_ERR_BAD_ARG; }
+    if (!ctx->staged) { set_err(ctx, "no inputs staged"); return SCF_ERR_NO_SOLVE; }
+    if (!ctx->assembled) { ctx->launches = 0; rc = assemble(ctx); if (rc) return rc; }
+    const Dims &d = ctx->d;
+    std::vector<float> tmp(d.ng);
+    float *outs[9] = {diag_hi, e_hi, n_hi, t_hi, extra_hi, diag_lo, e_lo, n_lo, t_lo};
+    const float *srcs[9] = {ctx->diag32, ctx->cE32, ctx->cN32, ctx->cT32, ctx->extra32,
+                            ctx->diag_lo, ctx->cE_lo, ctx->cN_lo, ctx->cT_lo};
+    for (int q = 0; q < 9; ++q) {
+        if (!outs[q]) continue;
+        CK(cudaMemcpyAsync(tmp.data(), srcs[q], sizeof(float) * d.ng, cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        for (int k = 1; k <= d.K; ++k)
+            for (int j = 1; j <= d.J; ++j)
+                for (int i = 1; i <= d.I; ++i) outs[q][nidx(d, i, j, k)] = tmp[gidx(d, i, j, k)];
+    }
+    if (extra) {
+        std::vector<double> t64(d.ng);
+        CK(cudaMemcpyAsync(t64.data(), ctx->extra, sizeof(double) * d.ng, cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        for (int k = 1; k <= d.K; ++k)
+            for (int j = 1; j <= d.J; ++j)
+                for (int i = 1; i <= d.I; ++i) extra[nidx(d, i, j, k)] = t64[gidx(d, i, j, k)];
+    }
+    return SCF_OK;
+}
+
 int scf_debug_time_kernel(scf_ctx *ctx, int kernel, int reps, double *ms_per_launch, double *bytes_per_launch)
 {
     int rc = check_ctx(ctx);

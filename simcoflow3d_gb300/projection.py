@@ -56,6 +56,7 @@ def load_library(path: Optional[str] = None):
                                     capi.c_double_p, capi.c_double_p, capi.c_double_p, P(capi.ScfBcOut)]
     L.scf_debug_apply.argtypes = [C.c_void_p, capi.c_double_p, capi.c_double_p]
     L.scf_debug_operator.argtypes = [C.c_void_p] + [capi.c_double_p] * 5
+    L.scf_debug_operator_f32.argtypes = [C.c_void_p] + [C.POINTER(C.c_float)] * 9 + [capi.c_double_p]
     L.scf_debug_precondition.argtypes = [C.c_void_p, capi.c_double_p, capi.c_double_p]
     L.scf_status_string.argtypes = [C.c_int]
     L.scf_status_string.restype = C.c_char_p
@@ -248,3 +249,16 @@ class Projection:
         outs = [np.zeros((I, J, K), order="F") for _ in range(5)]
         self._check(self.L.scf_debug_operator(self.ctx, *(capi.dptr(o) for o in outs)))
         return dict(zip(("diag", "cpl_e", "cpl_n", "cpl_t", "rhs"), outs))
+
+    def debug_operator_f32(self):
+        """FP32 hi/lo forms of the operator of a mixed context and the FP64
+        extra diagonal part (interior arrays)."""
+        I, J, K = self.shape
+        names = ("diag_hi", "e_hi", "n_hi", "t_hi", "extra_hi", "diag_lo", "e_lo", "n_lo", "t_lo")
+        outs = [np.zeros((I, J, K), dtype=np.float32, order="F") for _ in names]
+        extra = np.zeros((I, J, K), order="F")
+        fp = lambda a: a.ctypes.data_as(C.POINTER(C.c_float))
+        self._check(self.L.scf_debug_operator_f32(self.ctx, *(fp(o) for o in outs), capi.dptr(extra)))
+        r = dict(zip(names, outs))
+        r["extra"] = extra
+        return r

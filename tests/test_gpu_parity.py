@@ -83,6 +83,39 @@ def test_operator_and_rhs_bit_exact(lib, name, n):
                 assert cpl[i, j, k] == -lookup[(r, int(pos[tuple(nb)]))]
 
 
+@pytest.mark.parametrize("name,n", CASES + [("dirichlet", 16)])
+def test_fp32_operator_forms_are_rounded_to_nearest(lib, name, n):
+    """The mixed context's FP32 operator: hi is the FP64 value rounded to
+    nearest FP32, lo the FP64 remainder rounded to FP32 (bit-exact against
+    numpy's IEEE conversion); the extra diagonal part matches the row sum."""
+    if name == "dirichlet":
+        w = _with_bcs(W.config("c1", n=n), bcp=(0, 1, 1, 1, 1, 0), consts=False)
+    else:
+        w = W.config(name, n=n)
+    p = _proj(w, precision=1)
+    p.stage(w, correction=False)
+    op = p.debug_operator()
+    f = p.debug_operator_f32()
+    bits = lambda a: np.ascontiguousarray(a).view(np.uint32)
+    for k64, khi, klo in (("diag", "diag_hi", "diag_lo"), ("cpl_e", "e_hi", "e_lo"),
+                          ("cpl_n", "n_hi", "n_lo"), ("cpl_t", "t_hi", "t_lo")):
+        v = op[k64]
+        hi = v.astype(np.float32)
+        lo = (v - hi.astype(np.float64)).astype(np.float32)
+        assert np.array_equal(bits(f[khi]), bits(hi)), k64
+        assert np.array_equal(bits(f[klo]), bits(lo)), k64
+    assert np.array_equal(bits(f["extra_hi"]), bits(f["extra"].astype(np.float32)))
+    act = w.arrays["posnu"] >= 0
+    if name == "dirichlet":   # Dirichlet faces put their terms in extra
+        assert (f["extra"][act] > 0).any()
+    # diag = couplings of the six faces + extra, up to the summation order
+    cw = np.zeros_like(op["cpl_e"]); cw[1:] = op["cpl_e"][:-1]
+    cs = np.zeros_like(op["cpl_n"]); cs[:, 1:] = op["cpl_n"][:, :-1]
+    cb = np.zeros_like(op["cpl_t"]); cb[:, :, 1:] = op["cpl_t"][:, :, :-1]
+    tot = op["cpl_e"] + op["cpl_n"] + op["cpl_t"] + cw + cs + cb + f["extra"]
+    assert np.allclose(tot[act], op["diag"][act], rtol=1e-12, atol=0)
+
+
 @pytest.mark.parametrize("name,n", CASES)
 def test_apply_matches_reference_matrix(lib, name, n):
     w = W.config(name, n=n)
