@@ -45,6 +45,8 @@ def lib():
         L.oracle_scatter.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(capi.ScfPoissonIn), dp, dp]
         L.oracle_correct.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(capi.ScfPoissonIn),
                                      C.POINTER(capi.ScfCorrectIn), dp, dp, dp, dp, dp, dp, dp, C.c_int]
+        L.oracle_grid_preprocess.argtypes = [C.c_int, C.c_int, C.c_int] + [C.POINTER(capi.ScfGeoCells)] * 4
+        L.oracle_face_geo_cal.argtypes = [C.c_double] * 7 + [dp, dp]
         L.oracle_csr_apply.argtypes = [C.c_int32, i64p, ip, dp, dp, dp]
         L.oracle_csr_pcg.argtypes = [C.c_int32, i64p, ip, dp, dp, dp, C.c_double, C.c_int, C.c_int,
                                      C.POINTER(C.c_double)]
@@ -214,3 +216,26 @@ def project(w, solver="gmg", rel_tol=1e-13, precision=0, north_mass_fix=0, **kw)
 
 def num_threads() -> int:
     return int(lib().oracle_num_threads())
+
+
+def face_geo_cal(d1, d2, n1, n2, n3, d3, phi):
+    """FaceGeoCal (CutCell.f90:883-981) of one face: (area, (c1, c2, c3))."""
+    area = C.c_double()
+    cent = (C.c_double * 3)()
+    lib().oracle_face_geo_cal(d1, d2, n1, n2, n3, d3, phi, C.byref(area), cent)
+    return area.value, tuple(cent)
+
+
+def grid_preprocess(g):
+    """GridPreprocess + DefineMomentumExchangeCell + NumberExternalCell x4
+    (Main.f90:203-214) on a copy of ``g`` (simcoflow3d_gb300.geometry.GeoInputs);
+    returns the copy."""
+    from simcoflow3d_gb300 import geometry as GM
+    out = g.copy()
+    ss = [out.fams[f].struct() for f in GM.FAMILIES]
+    rc = lib().oracle_grid_preprocess(out.imax, out.jmax, out.kmax, *(C.byref(s) for s in ss))
+    if rc != 0:
+        raise ValueError("grid too small")
+    for f, s in zip(GM.FAMILIES, ss):
+        out.fams[f].ext_cell = s.ext_cell
+    return out

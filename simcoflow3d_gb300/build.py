@@ -28,6 +28,8 @@ UNITS = {
     "k_noalloc.cu": [],
     "k_adjoint.cu": [],
     "k_cg_df.cu": [],
+    "k_geometry.cu": ["-fmad=false"],
+    "geo_api.cu": [],
 }
 
 
@@ -43,6 +45,7 @@ def _compile(unit: str, extra, verbose: bool):
     obj = os.path.join(OUT, unit.replace(".cu", ".o"))
     deps = [src] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
     deps.append(os.path.join(HERE, "..", "include", "scf_projection.h"))
+    deps.append(os.path.join(HERE, "..", "include", "scf_geometry.h"))
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
         return obj
     cmd = [nvcc(), "-c", src, "-o", obj] + ARCH + COMMON + list(extra)

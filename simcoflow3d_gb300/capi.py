@@ -119,6 +119,29 @@ class ScfBcOut(C.Structure):
     _fields_ = [("var", (c_double_p * 6) * 4)]
 
 
+class ScfGeoCells(C.Structure):
+    """scf_geo_cells of include/scf_geometry.h: one cell family."""
+    _fields_ = [
+        ("dx", c_double_p), ("dy", c_double_p), ("dz", c_double_p),
+        ("phi", c_double_p), ("nx", c_double_p), ("ny", c_double_p), ("nz", c_double_p),
+        ("vof", c_double_p), ("vofl", c_double_p),
+        ("cell_type", c_int32_p),
+        ("eearea", c_double_p), ("nearea", c_double_p), ("tearea", c_double_p),
+        ("fce", c_double_p), ("fcn", c_double_p), ("fct", c_double_p),
+        ("cell_cent", c_double_p), ("wllh", c_double_p), ("delh", c_double_p),
+        ("moexcell", c_int32_p), ("posnu", c_int32_p),
+        ("ext_cell", C.c_int32),
+    ]
+
+
+class ScfGeoStats(C.Structure):
+    _fields_ = [
+        ("gpu_launches", C.c_int32), ("exact_faces", C.c_int32),
+        ("ms_h2d", C.c_double), ("ms_device", C.c_double), ("ms_d2h", C.c_double), ("ms_total", C.c_double),
+        ("bytes_h2d", C.c_int64), ("bytes_d2h", C.c_int64),
+    ]
+
+
 def dptr(a: Optional[np.ndarray]):
     if a is None:
         return c_double_p()

@@ -71,6 +71,14 @@ def load_library(path: Optional[str] = None):
     L.scf_loss_forward.argtypes = [C.c_void_p, P(capi.ScfPoissonIn), P(capi.ScfCorrectIn), capi.c_double_p,
                                    capi.c_double_p, capi.c_double_p, P(capi.ScfStats)]
     L.scf_loss_backward.argtypes = [C.c_void_p] + [capi.c_double_p] * 4 + [P(capi.ScfStats)]
+    P_G = P(capi.ScfGeoCells)
+    L.scf_geo_create.argtypes = [P(C.c_void_p), C.c_int32, C.c_int32, C.c_int32, C.c_int32]
+    L.scf_geo_destroy.argtypes = [C.c_void_p]
+    L.scf_grid_preprocess.argtypes = [C.c_void_p, P_G, P_G, P_G, P_G, P(capi.ScfGeoStats)]
+    L.scf_geo_stage.argtypes = [C.c_void_p, P_G, P_G, P_G, P_G]
+    L.scf_geo_run.argtypes = [C.c_void_p, P(capi.ScfGeoStats)]
+    L.scf_geo_fetch.argtypes = [C.c_void_p, P_G, P_G, P_G, P_G]
+    L.scf_geo_last_error.argtypes = [C.c_void_p, C.c_char_p, C.c_size_t]
     L.scf_apply_operator_noalloc.argtypes = [C.c_int32, C.c_int32, C.c_int32] + [C.c_void_p] * 8
     _lib = L
     return L

@@ -11,12 +11,15 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "scf_projection.h")
+GEO_HEADER = os.path.join(ROOT, "include", "scf_geometry.h")
 
 
 def declared_functions():
-    src = open(HEADER).read()
-    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b(scf_[a-z0-9_]+)\s*\(", src)))
+    names = set()
+    for h in (HEADER, GEO_HEADER):
+        src = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        names |= set(re.findall(r"\b(scf_[a-z0-9_]+)\s*\(", src))
+    return sorted(names)
 
 
 @pytest.fixture(scope="module")
@@ -28,7 +31,8 @@ def lib_path():
 def test_library_exports_every_declared_function(lib_path):
     lib = C.CDLL(lib_path)
     names = declared_functions()
-    assert len(names) >= 18
+    assert len(names) >= 25
+    assert "scf_grid_preprocess" in names and "scf_geo_create" in names
     for n in names:
         assert hasattr(lib, n), n
     assert lib.scf_abi_version() == 2
@@ -81,3 +85,36 @@ def test_product_does_not_reach_the_oracle():
                 txt = open(os.path.join(dp, fn)).read()
                 for pat in ("import oracle", "from oracle", "liboracle", "oracle/"):
                     assert pat not in txt, (fn, pat)
+
+
+def test_geometry_struct_layouts_match_header():
+    from simcoflow3d_gb300 import capi
+    prog = r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "scf_geometry.h"
+#define P(T, f) printf(#T " " #f " %zu\n", offsetof(T, f));
+int main(void) {
+  printf("scf_geo_cells size %zu\n", sizeof(scf_geo_cells));
+  printf("scf_geo_stats size %zu\n", sizeof(scf_geo_stats));
+  P(scf_geo_cells, vof) P(scf_geo_cells, cell_type) P(scf_geo_cells, fce) P(scf_geo_cells, moexcell)
+  P(scf_geo_cells, posnu) P(scf_geo_cells, ext_cell)
+  P(scf_geo_stats, exact_faces) P(scf_geo_stats, ms_h2d) P(scf_geo_stats, bytes_d2h)
+  return 0;
+}
+'''
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "g.c")
+        open(c, "w").write(prog)
+        exe = os.path.join(d, "g")
+        subprocess.run(["gcc", "-I", os.path.dirname(GEO_HEADER), c, "-o", exe], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout
+    m = {"scf_geo_cells": capi.ScfGeoCells, "scf_geo_stats": capi.ScfGeoStats}
+    lines = out.splitlines()
+    assert len(lines) == 11
+    for line in lines:
+        t, f, v = line.split()
+        if f == "size":
+            assert C.sizeof(m[t]) == int(v), (t, v)
+        else:
+            assert getattr(m[t], f).offset == int(v), (t, f, v)
