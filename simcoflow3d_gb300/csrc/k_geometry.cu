@@ -14,6 +14,12 @@
 namespace {
 
 __device__ __forceinline__ unsigned long long bits(double x) { return (unsigned long long)__double_as_longlong(x); }
+// -x (IEEE negation: the sign bit), on the 32-bit halves so that the
+// compiler does not turn it back into an FP64 instruction
+__device__ __forceinline__ double neg(double x)
+{
+    return __hiloint2double(__double2hiint(x) ^ (int)0x80000000, __double2loint(x));
+}
 constexpr unsigned long long ONE = 0x3ff0000000000000ull;
 constexpr double EPSI = 1.0e-3;    // CutCell.f90:11
 constexpr double TOL = 1.0e-20;    // CutCell.f90:396
@@ -63,15 +69,26 @@ __device__ __noinline__ Face face_exact(double d1, double d2, double n1, double 
     return f;
 }
 
+// x / 2 for normal x with a biased exponent above 1 (the exponent field
+// minus one); other values take the FP64 division.  Both are exact.
+__device__ __noinline__ double half_slow(double x) { return x / 2.0; }
+__device__ __forceinline__ double half(double x)
+{
+    const unsigned long long b = bits(x), e = (b >> 52) & 0x7ff;
+    return (e > 1 && e < 0x7ff) ? __longlong_as_double((long long)(b - (1ull << 52))) : half_slow(x);
+}
+
 // |x| truncated to FP32 on the integer pipe (|x|(1 - 2^-23) < result <= |x|);
 // ok is cleared for values outside FP32's normal range (zero is exact).
+// (Works on the 32-bit halves: a 64-bit mask of the sign bit is recognised
+// as fabs and issued on the FP64 pipe.)
 __device__ __forceinline__ float abs_f32_trunc(double x, bool &ok)
 {
-    const unsigned long long b = bits(x) & 0x7fffffffffffffffull;
-    if (b == 0ull) return 0.0f;
-    const int e = (int)(b >> 52) - 1023 + 127;
+    const unsigned hi = (unsigned)__double2hiint(x) & 0x7fffffffu, lo = (unsigned)__double2loint(x);
+    if ((hi | lo) == 0u) return 0.0f;
+    const int e = (int)(hi >> 20) - 1023 + 127;
     if (e < 1 || e > 254) { ok = false; return 0.0f; }
-    return __uint_as_float(((unsigned)e << 23) | (unsigned)((b >> 29) & 0x7fffffu));
+    return __uint_as_float(((unsigned)e << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
 }
 
 // 1: every corner of the face is open (n.x + phi > 0), -1: every corner is
@@ -90,7 +107,7 @@ __device__ __forceinline__ int face_class(double d1, double d2, double n1, doubl
     const float a3 = abs_f32_trunc(d3, ok) * abs_f32_trunc(n3, ok);
     const float p = abs_f32_trunc(phi, ok);
     if (!ok || !(p > (a1 + a2 + a3) * 1.0001f) || !(p > 1.0e-30f)) return 0;
-    return (bits(phi) >> 63) ? -1 : 1;
+    return __double2hiint(phi) < 0 ? -1 : 1;
 }
 
 // An open face: its result depends on d1, d2 only (the corners of the
@@ -128,35 +145,42 @@ __device__ __forceinline__ Face face_eval(FullMemo &mm, double d1, double d2, do
 struct Shared {
     double avg, fa, fb;
 };
-__device__ __noinline__ Shared share_slow(double w, double e, double na, double nb)
+// The FP64 work of share() is out of line: inline, the compiler evaluates
+// short branches unconditionally and selects, which put the products and
+// divisions on every face.
+__device__ __noinline__ Shared share_slow(double w, double e, double xa, double ya, double xb, double yb)
 {
     Shared s;
+    const double na = xa * w + ya * e, nb = xb * w + yb * e;
     const double den = w + e + TOL;
     s.avg = (w * w + e * e) / den;
     s.fa = na / den;
     s.fb = nb / den;
     return s;
 }
+// both sides open: den = 1 + 1 + 1e-20 = 2, avg = 2/2 = 1 and x*1 = x
+__device__ __noinline__ Shared share_open(double xa, double ya, double xb, double yb)
+{
+    Shared s;
+    s.avg = 1.0;
+    s.fa = (xa + ya) / 2.0;
+    s.fb = (xb + yb) / 2.0;
+    return s;
+}
 __device__ __forceinline__ Shared share(double w, double e, double xa, double ya, double xb, double yb)
 {
     Shared s;
-    if (bits(w) == ONE && bits(e) == ONE) {
-        // den = 1 + 1 + 1e-20 = 2 and avg = 2/2 exactly; x*1 = x
-        const double na = xa + ya, nb = xb + yb;
-        s.avg = 1.0;
-        s.fa = na / 2.0;
-        s.fb = nb / 2.0;
+    const bool zc = (bits(xa) | bits(ya) | bits(xb) | bits(yb)) == 0ull;   // all four centroid components +0
+    if (zc && ((bits(w) == ONE && bits(e) == ONE) || (bits(w) | bits(e)) == 0ull)) {
+        // both sides open: (1 + 1)/(1 + 1 + 1e-20) = 1 and (+0 + +0)/2 = +0;
+        // both closed: (0 + 0)/1e-20 = +0 and (+0*0 + +0*0)/1e-20 = +0
+        s.avg = bits(w) == ONE ? 1.0 : 0.0;
+        s.fa = 0.0;
+        s.fb = 0.0;
         return s;
     }
-    const double na = xa * w + ya * e, nb = xb * w + yb * e;
-    if (bits(w) == 0ull && bits(e) == 0ull && (bits(na) << 1) == 0ull && (bits(nb) << 1) == 0ull) {
-        // (0*0 + 0*0)/1e-20 = +0 and a signed zero over 1e-20 keeps its sign
-        s.avg = 0.0;
-        s.fa = na;
-        s.fb = nb;
-        return s;
-    }
-    return share_slow(w, e, na, nb);
+    if (bits(w) == ONE && bits(e) == ONE) return share_open(xa, ya, xb, yb);
+    return share_slow(w, e, xa, ya, xb, yb);
 }
 
 // sqrt(a^2 + b^2 + c^2) of CutCell.f90:455-462
@@ -209,27 +233,27 @@ __global__ void __launch_bounds__(128) k_geo_faces(GeoFam t, Dims d, int *exact_
     if (i > d.I || j > d.J) return;
     const int kbeg = blockIdx.z * GEO_KSEG + 1, kend = min(kbeg + GEO_KSEG - 1, d.K);
     const long long NG = d.ng, NN = d.n;
-    FullMemo mT, mB, mE, mW, mN, mS, mEn, mNn;
-    {
-        FullMemo z;
-        z.d1 = z.d2 = ~0ull; z.f.a = z.f.c1 = z.f.c2 = 0.0;
-        mT = mB = mE = mW = mN = mS = mEn = mNn = z;
-    }
+    // an open face's result depends on its edges (d1, d2) only, so the faces
+    // of one orientation share a memo: T/B (dx, dy), E/W (dy, dz), N/S (dz, dx)
+    FullMemo mXY, mYZ, mZX;
+    mXY.d1 = mXY.d2 = ~0ull; mXY.f.a = mXY.f.c1 = mXY.f.c2 = 0.0;
+    mYZ = mXY;
+    mZX = mXY;
     int exact = 0;
     Face prevT;
-    double prevdz = 0.0;
+    double prevhz = 0.0;
     prevT.a = prevT.c1 = prevT.c2 = 0.0;
     for (int k = kbeg; k <= kend; ++k) {
         const int g = gidx(d, i, j, k), n = nidx(d, i, j, k);
         const double dx = t.dx[n], dy = t.dy[n], dz = t.dz[n];
         const double nx = t.nx[g], ny = t.ny[g], nz = t.nz[g], phi = t.phi[g];
-        const double hx = dx / 2.0, hy = dy / 2.0, hz = dz / 2.0;
-        const Face T = face_eval(mT, dx, dy, nx, ny, nz, hz, phi, exact);
-        const Face B = face_eval(mB, dx, dy, nx, ny, nz, -hz, phi, exact);
-        const Face E = face_eval(mE, dy, dz, ny, nz, nx, hx, phi, exact);
-        const Face Wf = face_eval(mW, dy, dz, ny, nz, nx, -hx, phi, exact);
-        const Face N = face_eval(mN, dz, dx, nz, nx, ny, hy, phi, exact);
-        const Face S = face_eval(mS, dz, dx, nz, nx, ny, -hy, phi, exact);
+        const double hx = half(dx), hy = half(dy), hz = half(dz);
+        const Face T = face_eval(mXY, dx, dy, nx, ny, nz, hz, phi, exact);
+        const Face B = face_eval(mXY, dx, dy, nx, ny, nz, neg(hz), phi, exact);
+        const Face E = face_eval(mYZ, dy, dz, ny, nz, nx, hx, phi, exact);
+        const Face Wf = face_eval(mYZ, dy, dz, ny, nz, nx, neg(hx), phi, exact);
+        const Face N = face_eval(mZX, dz, dx, nz, nx, ny, hy, phi, exact);
+        const Face S = face_eval(mZX, dz, dx, nz, nx, ny, neg(hy), phi, exact);
         t.cent[n] = 0.0; t.cent[n + NN] = 0.0; t.cent[n + 2 * NN] = 0.0;
         const bool fin = ((bits(E.a) >> 52) & 0x7ff) != 0x7ff && ((bits(N.a) >> 52) & 0x7ff) != 0x7ff &&
                          ((bits(T.a) >> 52) & 0x7ff) != 0x7ff;
@@ -241,11 +265,12 @@ __global__ void __launch_bounds__(128) k_geo_faces(GeoFam t, Dims d, int *exact_
         if (i > 1) {
             const int gw = g - 1, nw = n - 1;
             const double dxw = t.dx[nw], dyw = t.dy[nw], dzw = t.dz[nw];
-            const Face Ew = face_eval(mEn, dyw, dzw, t.ny[gw], t.nz[gw], t.nx[gw], dxw / 2.0, t.phi[gw], exact);
+            const double hxw = half(dxw);
+            const Face Ew = face_eval(mYZ, dyw, dzw, t.ny[gw], t.nz[gw], t.nx[gw], hxw, t.phi[gw], exact);
             const Shared s = share(Wf.a, Ew.a, Wf.c1, Ew.c1, Wf.c2, Ew.c2);
             t.fce[gw + NG] = s.fa;
             t.fce[gw + 2 * NG] = s.fb;
-            t.fce[gw] = dxw / 2.0;
+            t.fce[gw] = hxw;
             t.ee[gw] = s.avg;
         }
         if (i == d.I) t.ee[g] = E.a;
@@ -253,11 +278,12 @@ __global__ void __launch_bounds__(128) k_geo_faces(GeoFam t, Dims d, int *exact_
         if (j > 1) {
             const int gs = g - d.gx, ns = n - d.I;
             const double dxs = t.dx[ns], dys = t.dy[ns], dzs = t.dz[ns];
-            const Face Ns = face_eval(mNn, dzs, dxs, t.nz[gs], t.nx[gs], t.ny[gs], dys / 2.0, t.phi[gs], exact);
+            const double hys = half(dys);
+            const Face Ns = face_eval(mZX, dzs, dxs, t.nz[gs], t.nx[gs], t.ny[gs], hys, t.phi[gs], exact);
             const Shared s = share(S.a, Ns.a, S.c2, Ns.c2, S.c1, Ns.c1);
             t.fcn[gs] = s.fa;
             t.fcn[gs + 2 * NG] = s.fb;
-            t.fcn[gs + NG] = dys / 2.0;
+            t.fcn[gs + NG] = hys;
             t.ne[gs] = s.avg;
         }
         if (j == d.J) t.ne[g] = N.a;
@@ -266,24 +292,21 @@ __global__ void __launch_bounds__(128) k_geo_faces(GeoFam t, Dims d, int *exact_
         if (k > 1) {
             const int gb = g - d.gx * d.gy;
             Face Tb = prevT;
-            double dzb = prevdz;
+            double hzb = prevhz;
             if (k == kbeg) {
                 const int nb = n - d.I * d.J;
-                const double dxb = t.dx[nb], dyb = t.dy[nb];
-                dzb = t.dz[nb];
-                FullMemo tmp;
-                tmp.d1 = tmp.d2 = ~0ull; tmp.f.a = tmp.f.c1 = tmp.f.c2 = 0.0;
-                Tb = face_eval(tmp, dxb, dyb, t.nx[gb], t.ny[gb], t.nz[gb], dzb / 2.0, t.phi[gb], exact);
+                hzb = half(t.dz[nb]);
+                Tb = face_eval(mXY, t.dx[nb], t.dy[nb], t.nx[gb], t.ny[gb], t.nz[gb], hzb, t.phi[gb], exact);
             }
             const Shared s = share(B.a, Tb.a, B.c1, Tb.c1, B.c1, Tb.c2);
             t.fct[gb] = s.fa;
             t.fct[gb + NG] = s.fb;
-            t.fct[gb + 2 * NG] = dzb / 2.0;
+            t.fct[gb + 2 * NG] = hzb;
             t.te[gb] = s.avg;
         }
         if (k == d.K) t.te[g] = T.a;
         prevT = T;
-        prevdz = dz;
+        prevhz = hz;
     }
     if (exact) atomicAdd(exact_count, exact);
 }
