@@ -431,13 +431,100 @@ def run_sequence(args):
     return 0
 
 
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
+# k_geo_faces on the PCell family, from the ncu capture summarised in
+# profiles/k_geo_faces_geometry_c2_128.md at 128^3, scaled to 256^3 by cells.
+GEO_FACES_TRAFFIC_128 = 132.545e6 + 222.457e6
+
+
+def run_geometry(args):
+    """The cut-cell geometry preprocessing (GridPreprocess +
+    DefineMomentumExchangeCell + NumberExternalCell x4) on the P/U/V/W cells of
+    the c2 geometry: device-resident time, the host-array call end to end,
+    the face kernel's live roofline and the oracle on the host cores.  One
+    JSON line."""
+    import numpy as np
+    from simcoflow3d_gb300 import geometry as GM
+    from simcoflow3d_gb300.projection import load_library
+    n = args.n or 256
+    g = GM.geometry_inputs("c2", n=n, seed=args.seed)
+    lib = load_library()
+    gp = GM.GridPreprocess(g.imax, g.jmax, g.kmax)
+    gp.stage(g)
+    for _ in range(args.warmup):
+        gp.run()
+    with ClockSampler(0) as cs:
+        runs = [gp.run() for _ in range(args.steps)]
+    clocks = cs.summary()
+    ms = [r["ms_device"] for r in runs]
+    ms_faces = [r["ms_faces"] / 4 for r in runs]
+    by_faces = runs[-1]["bytes_faces"] / 4
+    # end to end through scf_grid_preprocess with page-locked host arrays
+    pinned = []
+    for fam in g.fams.values():
+        for a in fam.arrays.values():
+            if a is not None and a.nbytes and lib.scf_host_register(a.ctypes.data, a.nbytes) == 0:
+                pinned.append(a)
+    e2e = [gp(g) for _ in range(max(3, args.steps // 4))]
+    unpin(lib, pinned)
+    peak, peak_kind = measured_peaks()
+    achieved = by_faces / (statistics.mean(ms_faces) * 1e-3) / 1e9
+    cpu = None
+    if not args.no_cpu:
+        threads = os.cpu_count() or 1
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+        from oracle import oracle as O
+        t0 = time.perf_counter()
+        O.grid_preprocess(g)
+        cpu = {"value": round((time.perf_counter() - t0) * 1e3, 1), "unit": "ms/call", "cores": threads,
+               "kind": "port", "sample": "one full call at %d^3 (oracle restatement of the four families' "
+                                        "GridPreprocess, DefineMomentumExchangeCell, NumberExternalCell), OpenMP" % n}
+    cells = g.imax * g.jmax * g.kmax
+    trf = None
+    if GEO_FACES_TRAFFIC_128 is not None:
+        trf = GEO_FACES_TRAFFIC_128 * cells / 128 ** 3
+    line = {
+        "metric": "ms per cut-cell geometry preprocessing call at %d^3 (GridPreprocess + "
+                  "DefineMomentumExchangeCell + NumberExternalCell x4, P/U/V/W cells)" % n,
+        "value": round(statistics.mean(ms), 4), "unit": "ms/call", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(statistics.mean(ms), 4), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (solid sphere level set, normals and fluid fractions of each family on its own "
+                "staggered grid; in/out arrays seeded)",
+        "config": {"workload": "geometry of c2: %d^3 unit cube, solid sphere r=0.15 at (0.5,0.5,0.3), "
+                               "liquid bubble r=0.1 at (0.5,0.5,0.65)" % n,
+                   "grid": [g.imax, g.jmax, g.kmax],
+                   "l2": "inputs larger than L2 (%.1f GB on the device)" % (e2e[-1]["bytes_h2d"] / 1e9)},
+        "exact_faces": runs[-1]["exact_faces"],
+        "e2e": {"value": round(statistics.mean(r["ms_total"] for r in e2e), 3), "unit": "ms/call",
+                "h2d_bytes_per_step": int(e2e[-1]["bytes_h2d"]), "d2h_bytes_per_step": int(e2e[-1]["bytes_d2h"]),
+                "ms_h2d": round(statistics.mean(r["ms_h2d"] for r in e2e), 3),
+                "ms_d2h": round(statistics.mean(r["ms_d2h"] for r in e2e), 3),
+                "inputs_pinned_fraction": round(sum(a.nbytes for a in pinned) /
+                                                max(1, sum(a.nbytes for f in g.fams.values()
+                                                           for a in f.arrays.values() if a is not None)), 4)},
+        "roofline": {"bound": "hbm", "kernel": "k_geo_faces (CellGeoCal faces of one family)",
+                     "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "peak_kind": peak_kind, "bytes_per_launch": by_faces,
+                     "ms_per_launch": round(statistics.mean(ms_faces), 5), "launches_timed": 4 * args.steps,
+                     "timing": "CUDA events around each face-kernel launch of the timed calls",
+                     "traffic": round(trf) if trf else None},
+        "clocks": clocks,
+        "gpu_launches": sum(r["gpu_launches"] for r in runs),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="c2")
+    ap.add_argument("--config", default="c2",
+                    help="c0..c4, or geometry (the cut-cell geometry preprocessing of the c2 geometry)")
     ap.add_argument("--tol", type=float, default=1e-8)
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--n", type=int, default=None, help="smaller grid (profiling captures only)")
@@ -454,6 +541,8 @@ def main():
         return run_reference(args)
     if args.sequence:
         return run_sequence(args)
+    if args.config == "geometry":
+        return run_geometry(args)
     return run_ours(args)
 
 

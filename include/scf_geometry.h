@@ -70,6 +70,10 @@ typedef struct scf_geo_stats {
     double  ms_d2h;           /* device->host copies                               */
     double  ms_total;         /* whole call                                        */
     int64_t bytes_h2d, bytes_d2h;
+    double  ms_faces;         /* CUDA-event time of the four CellGeoCal face
+                                 kernels (k_geo_faces), part of ms_device        */
+    int64_t bytes_faces;      /* their algorithmic bytes: each array they read
+                                 or write counted once per cell                 */
 } scf_geo_stats;
 
 typedef struct scf_geo_ctx scf_geo_ctx;

@@ -139,6 +139,7 @@ class ScfGeoStats(C.Structure):
         ("gpu_launches", C.c_int32), ("exact_faces", C.c_int32),
         ("ms_h2d", C.c_double), ("ms_device", C.c_double), ("ms_d2h", C.c_double), ("ms_total", C.c_double),
         ("bytes_h2d", C.c_int64), ("bytes_d2h", C.c_int64),
+        ("ms_faces", C.c_double), ("bytes_faces", C.c_int64),
     ]
 
 

@@ -17,6 +17,7 @@ struct scf_geo_ctx {
     int device = 0;
     cudaStream_t st = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t evf[8] = {};   // around the four face kernels
     std::vector<void *> mem;
     GeoFam fam[4];
     bool has_moex[4] = {false, false, false, false};
@@ -169,6 +170,8 @@ int scf_geo_create(scf_geo_ctx **out, int32_t imax, int32_t jmax, int32_t kmax, 
     if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) return fail(SCF_ERR_CUDA);
     if (cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess)
         return fail(SCF_ERR_CUDA);
+    for (int q = 0; q < 8; ++q)
+        if (cudaEventCreate(&ctx->evf[q]) != cudaSuccess) return fail(SCF_ERR_CUDA);
     const size_t n = d.n, g = d.ng;
     for (int f = 0; f < 4; ++f) {
         GeoFam &t = ctx->fam[f];
@@ -199,6 +202,8 @@ int scf_geo_destroy(scf_geo_ctx *ctx)
     for (void *p : ctx->mem) cudaFree(p);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    for (int q = 0; q < 8; ++q)
+        if (ctx->evf[q]) cudaEventDestroy(ctx->evf[q]);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
     return SCF_OK;
@@ -241,7 +246,7 @@ int scf_geo_run(scf_geo_ctx *ctx, scf_geo_stats *stats)
     }
     GK(cudaMemsetAsync(ctx->counters, 0, 8 * sizeof(int), ctx->st));
     GK(cudaEventRecord(ctx->ev0, ctx->st));
-    for (int f = 0; f < 4; ++f) launch_cell_geo(fam[f], d, ctx->counters + 4, ctx->st, &launches);
+    for (int f = 0; f < 4; ++f) launch_cell_geo(fam[f], d, ctx->counters + 4, ctx->st, &launches, ctx->evf + 2 * f);
     launch_grid_preprocess_tail(fam[0], fam[1], fam[2], fam[3], d, ctx->counters + 4, ctx->st, &launches);
     for (int f = 0; f < 4; ++f) launch_posnu(fam[f], d, ctx->colbuf, ctx->counters + f, ctx->st, &launches);
     GK(cudaGetLastError());
@@ -250,8 +255,13 @@ int scf_geo_run(scf_geo_ctx *ctx, scf_geo_stats *stats)
     GK(cudaMemcpyAsync(cnt, ctx->counters, sizeof(cnt), cudaMemcpyDeviceToHost, ctx->st));
     GK(cudaStreamSynchronize(ctx->st));
     for (int f = 0; f < 4; ++f) ctx->ext_cell[f] = cnt[f] - 1;
-    float ms = 0.f;
+    float ms = 0.f, msf = 0.f;
     GK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    for (int f = 0; f < 4; ++f) {
+        float m = 0.f;
+        GK(cudaEventElapsedTime(&m, ctx->evf[2 * f], ctx->evf[2 * f + 1]));
+        msf += m;
+    }
     ctx->ran = true;
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));
@@ -259,6 +269,10 @@ int scf_geo_run(scf_geo_ctx *ctx, scf_geo_stats *stats)
         stats->exact_faces = cnt[4];
         stats->ms_device = ms;
         stats->ms_total = ms;
+        stats->ms_faces = msf;
+        // per cell: dx, dy, dz, phi, nx, ny, nz read; EEArea, NEArea, TEArea,
+        // FCE, FCN, FCT (3 each), Cell_Cent (3) and WlLh written (FP64 each)
+        stats->bytes_faces = 4ll * (long long)d.n * 8 * (7 + 3 + 9 + 3 + 1);
     }
     return SCF_OK;
 }
@@ -297,6 +311,7 @@ int scf_grid_preprocess(scf_geo_ctx *ctx, scf_geo_cells *p, scf_geo_cells *u, sc
     if (rc) return rc;
     const double h2d = ms_since(t0);
     scf_geo_stats st;
+    std::memset(&st, 0, sizeof(st));
     if ((rc = scf_geo_run(ctx, &st))) return rc;
     const auto t1 = std::chrono::steady_clock::now();
     if ((rc = scf_geo_fetch(ctx, p, u, v, w))) return rc;

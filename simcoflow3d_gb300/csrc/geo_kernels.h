@@ -31,8 +31,10 @@ struct GeoFam {
                         (k = q_ / ((d).I * (d).J) + 1), true);                               \
          q_ += gridDim.x * blockDim.x)
 
-// DefineCell + CellGeoCal of one family.
-void launch_cell_geo(const GeoFam &t, const Dims &d, int *exact_count, cudaStream_t st, int *launches);
+// DefineCell + CellGeoCal of one family; when ev is given, ev[0] and ev[1]
+// are recorded around the face kernel.
+void launch_cell_geo(const GeoFam &t, const Dims &d, int *exact_count, cudaStream_t st, int *launches,
+                     cudaEvent_t *ev = nullptr);
 // The rest of GridPreprocess and DefineMomentumExchangeCell.
 void launch_grid_preprocess_tail(const GeoFam &P, const GeoFam &U, const GeoFam &V, const GeoFam &W, const Dims &d,
                                  int *exact_count, cudaStream_t st, int *launches);

@@ -218,21 +218,72 @@ __global__ void __launch_bounds__(256) k_geo_define(GeoFam t, Dims d)
     }
 }
 
+// Inputs of one FaceGeoCal call.
+struct FaceIn {
+    double d1, d2, n1, n2, n3, d3, phi;
+};
+
+// Faces whose corners are all open or all closed are resolved here; the
+// rest (cut faces) are put on the block's queue (slot >= 0) for a dense
+// evaluation, or evaluated in place when the queue is full (slot -1, -2
+// meaning resolved).
+__device__ __forceinline__ Face face_resolve(FullMemo &mm, const FaceIn &in, FaceIn *q_in, int *q_count, int cap,
+                                             int &slot, int &exact)
+{
+    Face f;
+    f.a = 0.0; f.c1 = 0.0; f.c2 = 0.0;
+    slot = -2;
+    const int c = face_class(in.d1, in.d2, in.n1, in.n2, in.n3, in.d3, in.phi);
+    if (c > 0) {
+        if (bits(in.d1) != mm.d1 || bits(in.d2) != mm.d2) {
+            mm.d1 = bits(in.d1); mm.d2 = bits(in.d2);
+            mm.f = face_full(in.d1, in.d2);
+        }
+        return mm.f;
+    }
+    if (c < 0) return f;
+    ++exact;
+    const int q = atomicAdd(q_count, 1);
+    if (q < cap) {
+        q_in[q] = in;
+        slot = q;
+        return f;
+    }
+    return face_exact(in.d1, in.d2, in.n1, in.n2, in.n3, in.d3, in.phi);
+}
+
 // CellGeoCal's face loop and shared-face averaging (CutCell.f90:402-531).
-// One thread marches a KSEG-cell segment of an (i,j) column.  For cell
-// (i,j,k) it evaluates its six faces (WlLh needs them all) and finishes the
-// three faces it shares with its lower neighbours: the W face with the E face
-// of (i-1,j,k), the S face with the N face of (i,j-1,k) (both evaluated here
-// again) and the B face with the T face of (i,j,k-1) (carried from the
-// previous cell of the march).  Faces on the upper boundary keep their own
-// value.  Every aperture and face centre is written by exactly one thread.
+// A block is 32 x 4 columns; each thread marches a GEO_KSEG-cell segment of
+// its (i,j) column.  For cell (i,j,k) it needs its six faces (WlLh takes
+// them all) and finishes the three faces it shares with its lower
+// neighbours: the W face with the E face of (i-1,j,k), the S face with the N
+// face of (i,j-1,k) (both evaluated here again) and the B face with the T
+// face of (i,j,k-1) (carried from the previous cell of the march).  Faces on
+// the upper boundary keep their own value.  Every aperture and face centre
+// is written by exactly one thread.
+//
+// Faces the solid surface cuts are rare and scattered: evaluated where they
+// occur, a warp would run the whole polygon (four FP64 divisions) for one
+// lane.  Each k step therefore queues them in shared memory, the block
+// evaluates the queue with one face per thread, and the threads pick their
+// results up.  The queue is double-buffered by k parity and reset by thread
+// 0 after its evaluation; a k step in which no thread queued anything takes
+// one barrier only.
+constexpr int GEO_QCAP = 256;
+
 __global__ void __launch_bounds__(128) k_geo_faces(GeoFam t, Dims d, int *exact_count)
 {
+    __shared__ FaceIn q_in[2][GEO_QCAP];
+    __shared__ Face q_out[2][GEO_QCAP];
+    __shared__ int q_count[2];
+    const int tid = threadIdx.x + 32 * threadIdx.y;
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    if (i > d.I || j > d.J) return;
+    const bool live = i <= d.I && j <= d.J;
     const int kbeg = blockIdx.z * GEO_KSEG + 1, kend = min(kbeg + GEO_KSEG - 1, d.K);
     const long long NG = d.ng, NN = d.n;
+    if (tid < 2) q_count[tid] = 0;
+    __syncthreads();
     // an open face's result depends on its edges (d1, d2) only, so the faces
     // of one orientation share a memo: T/B (dx, dy), E/W (dy, dz), N/S (dz, dx)
     FullMemo mXY, mYZ, mZX;
@@ -244,16 +295,71 @@ __global__ void __launch_bounds__(128) k_geo_faces(GeoFam t, Dims d, int *exact_
     double prevhz = 0.0;
     prevT.a = prevT.c1 = prevT.c2 = 0.0;
     for (int k = kbeg; k <= kend; ++k) {
-        const int g = gidx(d, i, j, k), n = nidx(d, i, j, k);
-        const double dx = t.dx[n], dy = t.dy[n], dz = t.dz[n];
-        const double nx = t.nx[g], ny = t.ny[g], nz = t.nz[g], phi = t.phi[g];
-        const double hx = half(dx), hy = half(dy), hz = half(dz);
-        const Face T = face_eval(mXY, dx, dy, nx, ny, nz, hz, phi, exact);
-        const Face B = face_eval(mXY, dx, dy, nx, ny, nz, neg(hz), phi, exact);
-        const Face E = face_eval(mYZ, dy, dz, ny, nz, nx, hx, phi, exact);
-        const Face Wf = face_eval(mYZ, dy, dz, ny, nz, nx, neg(hx), phi, exact);
-        const Face N = face_eval(mZX, dz, dx, nz, nx, ny, hy, phi, exact);
-        const Face S = face_eval(mZX, dz, dx, nz, nx, ny, neg(hy), phi, exact);
+        const int b = (k - kbeg) & 1;
+        // faces 0..5: T, B, E, W, N, S of this cell; 6: E of (i-1,j,k);
+        // 7: N of (i,j-1,k); 8: T of (i,j,k-1) at the segment start
+        Face F[9];
+        int slot[9];
+        double hx = 0.0, hy = 0.0, hz = 0.0, hxw = 0.0, hys = 0.0, hzb = prevhz;
+        int g = 0, n = 0;
+        double dx = 0.0, dy = 0.0, dz = 0.0;
+#pragma unroll
+        for (int f = 0; f < 9; ++f) { slot[f] = -2; F[f].a = F[f].c1 = F[f].c2 = 0.0; }
+        int queued = 0;
+        if (live) {
+            g = gidx(d, i, j, k); n = nidx(d, i, j, k);
+            dx = t.dx[n]; dy = t.dy[n]; dz = t.dz[n];
+            const double nx = t.nx[g], ny = t.ny[g], nz = t.nz[g], phi = t.phi[g];
+            hx = half(dx); hy = half(dy); hz = half(dz);
+            FaceIn in;
+            in.n1 = nx; in.n2 = ny; in.n3 = nz; in.phi = phi; in.d1 = dx; in.d2 = dy;
+            in.d3 = hz;      F[0] = face_resolve(mXY, in, q_in[b], &q_count[b], GEO_QCAP, slot[0], exact);
+            in.d3 = neg(hz); F[1] = face_resolve(mXY, in, q_in[b], &q_count[b], GEO_QCAP, slot[1], exact);
+            in.n1 = ny; in.n2 = nz; in.n3 = nx; in.d1 = dy; in.d2 = dz;
+            in.d3 = hx;      F[2] = face_resolve(mYZ, in, q_in[b], &q_count[b], GEO_QCAP, slot[2], exact);
+            in.d3 = neg(hx); F[3] = face_resolve(mYZ, in, q_in[b], &q_count[b], GEO_QCAP, slot[3], exact);
+            in.n1 = nz; in.n2 = nx; in.n3 = ny; in.d1 = dz; in.d2 = dx;
+            in.d3 = hy;      F[4] = face_resolve(mZX, in, q_in[b], &q_count[b], GEO_QCAP, slot[4], exact);
+            in.d3 = neg(hy); F[5] = face_resolve(mZX, in, q_in[b], &q_count[b], GEO_QCAP, slot[5], exact);
+            if (i > 1) {
+                const int gw = g - 1, nw = n - 1;
+                hxw = half(t.dx[nw]);
+                in.d1 = t.dy[nw]; in.d2 = t.dz[nw]; in.n1 = t.ny[gw]; in.n2 = t.nz[gw]; in.n3 = t.nx[gw];
+                in.d3 = hxw; in.phi = t.phi[gw];
+                F[6] = face_resolve(mYZ, in, q_in[b], &q_count[b], GEO_QCAP, slot[6], exact);
+            }
+            if (j > 1) {
+                const int gs = g - d.gx, ns = n - d.I;
+                hys = half(t.dy[ns]);
+                in.d1 = t.dz[ns]; in.d2 = t.dx[ns]; in.n1 = t.nz[gs]; in.n2 = t.nx[gs]; in.n3 = t.ny[gs];
+                in.d3 = hys; in.phi = t.phi[gs];
+                F[7] = face_resolve(mZX, in, q_in[b], &q_count[b], GEO_QCAP, slot[7], exact);
+            }
+            if (k > 1 && k == kbeg) {
+                const int gb = g - d.gx * d.gy, nb = n - d.I * d.J;
+                hzb = half(t.dz[nb]);
+                in.d1 = t.dx[nb]; in.d2 = t.dy[nb]; in.n1 = t.nx[gb]; in.n2 = t.ny[gb]; in.n3 = t.nz[gb];
+                in.d3 = hzb; in.phi = t.phi[gb];
+                F[8] = face_resolve(mXY, in, q_in[b], &q_count[b], GEO_QCAP, slot[8], exact);
+            }
+#pragma unroll
+            for (int f = 0; f < 9; ++f) queued |= slot[f] >= 0;
+        }
+        if (__syncthreads_count(queued)) {
+            const int nq = min(q_count[b], GEO_QCAP);
+            for (int q = tid; q < nq; q += 128) {
+                const FaceIn &in = q_in[b][q];
+                q_out[b][q] = face_exact(in.d1, in.d2, in.n1, in.n2, in.n3, in.d3, in.phi);
+            }
+            __syncthreads();
+            if (tid == 0) q_count[b] = 0;
+#pragma unroll
+            for (int f = 0; f < 9; ++f)
+                if (slot[f] >= 0) F[f] = q_out[b][slot[f]];
+        }
+        if (!live) continue;
+        if (!(k > 1 && k == kbeg)) F[8] = prevT;
+        const Face &T = F[0], &B = F[1], &E = F[2], &Wf = F[3], &N = F[4], &S = F[5];
         t.cent[n] = 0.0; t.cent[n + NN] = 0.0; t.cent[n + 2 * NN] = 0.0;
         const bool fin = ((bits(E.a) >> 52) & 0x7ff) != 0x7ff && ((bits(N.a) >> 52) & 0x7ff) != 0x7ff &&
                          ((bits(T.a) >> 52) & 0x7ff) != 0x7ff;
@@ -263,46 +369,33 @@ __global__ void __launch_bounds__(128) k_geo_faces(GeoFam t, Dims d, int *exact_
             t.wllh[n] = wllh_slow(E.a, Wf.a, N.a, S.a, T.a, B.a, dx, dy, dz);
         // W face (i-1 | i): CeW = (-dx/2, W.c1, W.c2), CeE(i-1) = (dx'/2, E'.c1, E'.c2)
         if (i > 1) {
-            const int gw = g - 1, nw = n - 1;
-            const double dxw = t.dx[nw], dyw = t.dy[nw], dzw = t.dz[nw];
-            const double hxw = half(dxw);
-            const Face Ew = face_eval(mYZ, dyw, dzw, t.ny[gw], t.nz[gw], t.nx[gw], hxw, t.phi[gw], exact);
-            const Shared s = share(Wf.a, Ew.a, Wf.c1, Ew.c1, Wf.c2, Ew.c2);
-            t.fce[gw + NG] = s.fa;
-            t.fce[gw + 2 * NG] = s.fb;
+            const int gw = g - 1;
+            const Shared sh = share(Wf.a, F[6].a, Wf.c1, F[6].c1, Wf.c2, F[6].c2);
+            t.fce[gw + NG] = sh.fa;
+            t.fce[gw + 2 * NG] = sh.fb;
             t.fce[gw] = hxw;
-            t.ee[gw] = s.avg;
+            t.ee[gw] = sh.avg;
         }
         if (i == d.I) t.ee[g] = E.a;
         // S face (j-1 | j): CeS = (S.c2, -dy/2, S.c1), CeN(j-1) = (N'.c2, dy'/2, N'.c1)
         if (j > 1) {
-            const int gs = g - d.gx, ns = n - d.I;
-            const double dxs = t.dx[ns], dys = t.dy[ns], dzs = t.dz[ns];
-            const double hys = half(dys);
-            const Face Ns = face_eval(mZX, dzs, dxs, t.nz[gs], t.nx[gs], t.ny[gs], hys, t.phi[gs], exact);
-            const Shared s = share(S.a, Ns.a, S.c2, Ns.c2, S.c1, Ns.c1);
-            t.fcn[gs] = s.fa;
-            t.fcn[gs + 2 * NG] = s.fb;
+            const int gs = g - d.gx;
+            const Shared sh = share(S.a, F[7].a, S.c2, F[7].c2, S.c1, F[7].c1);
+            t.fcn[gs] = sh.fa;
+            t.fcn[gs + 2 * NG] = sh.fb;
             t.fcn[gs + NG] = hys;
-            t.ne[gs] = s.avg;
+            t.ne[gs] = sh.avg;
         }
         if (j == d.J) t.ne[g] = N.a;
         // B face (k-1 | k): CeB = (B.c1, B.c2, -dz/2), CeT(k-1) = (T'.c1, T'.c2, dz'/2);
         // the second component weights CeB(...,1), as the reference does
         if (k > 1) {
             const int gb = g - d.gx * d.gy;
-            Face Tb = prevT;
-            double hzb = prevhz;
-            if (k == kbeg) {
-                const int nb = n - d.I * d.J;
-                hzb = half(t.dz[nb]);
-                Tb = face_eval(mXY, t.dx[nb], t.dy[nb], t.nx[gb], t.ny[gb], t.nz[gb], hzb, t.phi[gb], exact);
-            }
-            const Shared s = share(B.a, Tb.a, B.c1, Tb.c1, B.c1, Tb.c2);
-            t.fct[gb] = s.fa;
-            t.fct[gb + NG] = s.fb;
+            const Shared sh = share(B.a, F[8].a, B.c1, F[8].c1, B.c1, F[8].c2);
+            t.fct[gb] = sh.fa;
+            t.fct[gb + NG] = sh.fb;
             t.fct[gb + 2 * NG] = hzb;
-            t.te[gb] = s.avg;
+            t.te[gb] = sh.avg;
         }
         if (k == d.K) t.te[g] = T.a;
         prevT = T;
@@ -608,11 +701,14 @@ __global__ void __launch_bounds__(256) k_posnu_write(GeoFam t, Dims d, const int
 // host launchers
 static int grid_for(int n, int per_block) { return std::min((n + per_block - 1) / per_block, 152 * 16); }
 
-void launch_cell_geo(const GeoFam &t, const Dims &d, int *exact_count, cudaStream_t st, int *launches)
+void launch_cell_geo(const GeoFam &t, const Dims &d, int *exact_count, cudaStream_t st, int *launches,
+                     cudaEvent_t *ev)
 {
     k_geo_define<<<grid_for(d.ng, 256), 256, 0, st>>>(t, d);
     dim3 b(32, 4), g((d.I + 31) / 32, (d.J + 3) / 4, (d.K + GEO_KSEG - 1) / GEO_KSEG);
+    if (ev) cudaEventRecord(ev[0], st);
     k_geo_faces<<<g, b, 0, st>>>(t, d, exact_count);
+    if (ev) cudaEventRecord(ev[1], st);
     *launches += 2;
     if (!t.moex) {
         k_geo_maxface<<<grid_for(d.n, 256), 256, 0, st>>>(t, d);

@@ -99,7 +99,8 @@ int main(void) {
   printf("scf_geo_stats size %zu\n", sizeof(scf_geo_stats));
   P(scf_geo_cells, vof) P(scf_geo_cells, cell_type) P(scf_geo_cells, fce) P(scf_geo_cells, moexcell)
   P(scf_geo_cells, posnu) P(scf_geo_cells, ext_cell)
-  P(scf_geo_stats, exact_faces) P(scf_geo_stats, ms_h2d) P(scf_geo_stats, bytes_d2h)
+  P(scf_geo_stats, exact_faces) P(scf_geo_stats, ms_h2d) P(scf_geo_stats, bytes_d2h) P(scf_geo_stats, ms_faces)
+  P(scf_geo_stats, bytes_faces)
   return 0;
 }
 '''
@@ -111,7 +112,7 @@ int main(void) {
         out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout
     m = {"scf_geo_cells": capi.ScfGeoCells, "scf_geo_stats": capi.ScfGeoStats}
     lines = out.splitlines()
-    assert len(lines) == 11
+    assert len(lines) == 13
     for line in lines:
         t, f, v = line.split()
         if f == "size":
