@@ -74,7 +74,9 @@ typedef struct scf_opts {
                                  (when the recursive residual has drifted from
                                  it near the rounding floor), default 12       */
     double  inner_rtol;       /* reserved (default 1e-4; not used)             */
-    int32_t smoother_degree;  /* Chebyshev degree per pre/post smoothing (3)   */
+    int32_t smoother_degree;  /* Chebyshev degree per pre/post smoothing (3),
+                                 1..8; the polynomial damps the interval
+                                 [2/r, 2] of D^-1 A, r = max(6, 2 degree)     */
     int32_t coarse_max_cells; /* coarsen until a level has <= this many cells
                                  (default 64); solved densely in FP64          */
     double  rho_l, rho_g;     /* liquid/gas densities (StateVariables.f90:9)   */

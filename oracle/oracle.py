@@ -135,13 +135,20 @@ def csr_relres(A, b, x, singular_=False):
                                    _dp(np.ascontiguousarray(x, dtype=np.float64)), int(singular_))
 
 
-def gmg_solve(w, pc, b, precision=0, rel_tol=1e-13, max_iter=400, degree=2, ratio=6.0, coarse_max=64,
+def cheb_ratio(degree: int) -> float:
+    """lmax/lmin of the Chebyshev smoother for a degree: max(6, 2 degree), as
+    the library's smoother."""
+    return 2.0 * degree if degree > 3 else 6.0
+
+
+def gmg_solve(w, pc, b, precision=0, rel_tol=1e-13, max_iter=400, degree=2, ratio=None, coarse_max=64,
               max_rounds=12, inner_rtol=1e-4, line_seg=0):
     """CPU multigrid-preconditioned CG; returns (x in PosNu order, stats)."""
     I, J, K = w.imax, w.jmax, w.kmax
     x = np.zeros(w.ext_cell + 1)
     prm = GmgParams(precision=precision, rel_tol=rel_tol, max_iter=max_iter, max_rounds=max_rounds,
-                    inner_rtol=inner_rtol, degree=degree, ratio=ratio, coarse_max=coarse_max, line_seg=line_seg)
+                    inner_rtol=inner_rtol, degree=degree, ratio=ratio or cheb_ratio(degree), coarse_max=coarse_max,
+                    line_seg=line_seg)
     s = capi.poisson_in(w)
     rc = lib().oracle_gmg_solve(I, J, K, C.byref(s), _dp(pc), _dp(b), _dp(x), C.byref(prm))
     st = {f: getattr(prm, f) for f, _ in GmgParams._fields_}
@@ -149,12 +156,13 @@ def gmg_solve(w, pc, b, precision=0, rel_tol=1e-13, max_iter=400, degree=2, rati
     return x, st
 
 
-def gmg_vcycle(w, pc, r, precision=0, degree=3, ratio=6.0, coarse_max=64, line_seg=0):
+def gmg_vcycle(w, pc, r, precision=0, degree=3, ratio=None, coarse_max=64, line_seg=0):
     """One CPU V-cycle z = M r of the multigrid hierarchy of (w, pc); r and z
     ghosted FP64 arrays."""
     I, J, K = w.imax, w.jmax, w.kmax
     z = np.zeros(w.shape_g, order="F")
-    prm = GmgParams(precision=precision, degree=degree, ratio=ratio, coarse_max=coarse_max, line_seg=line_seg)
+    prm = GmgParams(precision=precision, degree=degree, ratio=ratio or cheb_ratio(degree), coarse_max=coarse_max,
+                    line_seg=line_seg)
     s = capi.poisson_in(w)
     rr = np.asfortranarray(r, dtype=np.float64)
     lib().oracle_gmg_vcycle(I, J, K, C.byref(s), _dp(pc), _dp(rr), _dp(z), C.byref(prm))

@@ -349,7 +349,9 @@ ChebCoef cheb_coef(int degree, int lines)
     if (degree < 1) degree = 1;
     if (degree > 8) degree = 8;
     cc.degree = degree;
-    const double lmax = 2.0, lmin = lmax / 6.0;
+    // interval [lmax/r, lmax]: lmax = 2 bounds the spectrum of D^-1 A
+    // (Gershgorin); higher degrees damp a wider band, r = max(6, 2 degree)
+    const double lmax = 2.0, lmin = lmax / (degree > 3 ? 2.0 * degree : 6.0);
     const double theta = 0.5 * (lmax + lmin), delta = 0.5 * (lmax - lmin), sigma = theta / delta;
     cc.first = 1.0 / theta;
     double rho = 1.0 / sigma;
