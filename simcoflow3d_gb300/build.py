@@ -30,6 +30,7 @@ UNITS = {
     "k_cg_df.cu": [],
     "k_geometry.cu": ["-fmad=false"],
     "geo_api.cu": [],
+    "k_output.cu": [],
 }
 
 
@@ -46,6 +47,7 @@ def _compile(unit: str, extra, verbose: bool):
     deps = [src] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
     deps.append(os.path.join(HERE, "..", "include", "scf_projection.h"))
     deps.append(os.path.join(HERE, "..", "include", "scf_geometry.h"))
+    deps.append(os.path.join(HERE, "..", "include", "scf_output.h"))
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
         return obj
     cmd = [nvcc(), "-c", src, "-o", obj] + ARCH + COMMON + list(extra)

@@ -143,6 +143,16 @@ class ScfGeoStats(C.Structure):
     ]
 
 
+class ScfVtrField(C.Structure):
+    """scf_vtr_field of include/scf_output.h."""
+    _fields_ = [("name", C.c_char_p), ("data", C.c_void_p), ("on_device", C.c_int32)]
+
+
+class ScfVtrStats(C.Structure):
+    _fields_ = [("ms_convert", C.c_double), ("ms_d2h", C.c_double), ("ms_write", C.c_double),
+                ("ms_total", C.c_double), ("bytes_file", C.c_int64), ("gpu_launches", C.c_int32)]
+
+
 def dptr(a: Optional[np.ndarray]):
     if a is None:
         return c_double_p()

@@ -1446,3 +1446,18 @@ int scf_host_unregister(void *ptr)
 int scf_abi_version(void) { return SCF_ABI_VERSION; }
 
 }  // extern "C"
+
+extern "C" int scf_ctx_device_fields(scf_ctx *ctx, const double **u, const double **v, const double **w,
+                                     const double **p, const double **phil, const double **vofl, const double **vof)
+{
+    int rc = check_ctx(ctx);
+    if (rc) return rc;
+    if (u) *u = ctx->tu;
+    if (v) *v = ctx->tv;
+    if (w) *w = ctx->tw;
+    if (p) *p = ctx->tp;
+    if (phil) *phil = ctx->phil;
+    if (vofl) *vofl = ctx->vofl;
+    if (vof) *vof = ctx->vof;
+    return SCF_OK;
+}

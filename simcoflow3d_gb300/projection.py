@@ -79,6 +79,9 @@ def load_library(path: Optional[str] = None):
     L.scf_geo_run.argtypes = [C.c_void_p, P(capi.ScfGeoStats)]
     L.scf_geo_fetch.argtypes = [C.c_void_p, P_G, P_G, P_G, P_G]
     L.scf_geo_last_error.argtypes = [C.c_void_p, C.c_char_p, C.c_size_t]
+    L.scf_write_vtr.argtypes = [C.c_char_p, C.c_int32, C.c_int32, C.c_int32] + [capi.c_double_p] * 6 + [
+        C.c_int32, P(capi.ScfVtrField), C.c_int32, P(capi.ScfVtrStats)]
+    L.scf_ctx_device_fields.argtypes = [C.c_void_p] + [P(C.c_void_p)] * 7
     L.scf_apply_operator_noalloc.argtypes = [C.c_int32, C.c_int32, C.c_int32] + [C.c_void_p] * 8
     _lib = L
     return L
@@ -257,6 +260,13 @@ class Projection:
         outs = [np.zeros((I, J, K), order="F") for _ in range(5)]
         self._check(self.L.scf_debug_operator(self.ctx, *(capi.dptr(o) for o in outs)))
         return dict(zip(("diag", "cpl_e", "cpl_n", "cpl_t", "rhs"), outs))
+
+    def device_fields(self) -> dict:
+        """Device pointers (ghosted FP64) of the context's u, v, w, p, phiL, vofL
+        and vof (scf_ctx_device_fields), for output without a host copy."""
+        ptrs = [C.c_void_p() for _ in range(7)]
+        self._check(self.L.scf_ctx_device_fields(self.ctx, *(C.byref(q) for q in ptrs)))
+        return dict(zip(("u", "v", "w", "p", "phil", "vofl", "vof"), (q.value for q in ptrs)))
 
     def debug_operator_f32(self):
         """FP32 hi/lo forms of the operator of a mixed context and the FP64

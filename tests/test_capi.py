@@ -12,11 +12,12 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "scf_projection.h")
 GEO_HEADER = os.path.join(ROOT, "include", "scf_geometry.h")
+OUT_HEADER = os.path.join(ROOT, "include", "scf_output.h")
 
 
 def declared_functions():
     names = set()
-    for h in (HEADER, GEO_HEADER):
+    for h in (HEADER, GEO_HEADER, OUT_HEADER):
         src = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
         names |= set(re.findall(r"\b(scf_[a-z0-9_]+)\s*\(", src))
     return sorted(names)
@@ -32,7 +33,7 @@ def test_library_exports_every_declared_function(lib_path):
     lib = C.CDLL(lib_path)
     names = declared_functions()
     assert len(names) >= 25
-    assert "scf_grid_preprocess" in names and "scf_geo_create" in names
+    assert "scf_grid_preprocess" in names and "scf_geo_create" in names and "scf_write_vtr" in names
     for n in names:
         assert hasattr(lib, n), n
     assert lib.scf_abi_version() == 2
