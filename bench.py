@@ -529,6 +529,75 @@ def run_geometry(args):
     return 0
 
 
+def run_output(args):
+    """PrintResultVTK's snapshot of a c2 projection (p, u, v, w, phiL, phi,
+    vofL, vof at 256^3) written by scf_write_vtr from the projection
+    context's device arrays (the solid level set from the host), against the
+    oracle's numpy writer from host arrays.  One JSON line."""
+    import numpy as np
+    from simcoflow3d_gb300 import output as OUT
+    from simcoflow3d_gb300.projection import Projection
+    w = make_workload("c2", args.seed, args.n)
+    proj = Projection.for_workload(w, precision=1, rel_tol=args.tol, smoother_degree=4)
+    u, v, ww, pp, _, _ = proj.update_puvw(w)
+    dev = proj.device_fields()
+    a = w.arrays
+    phi = np.zeros(w.shape_g, order="F")
+    phi[1:-1, 1:-1, 1:-1] = a["pcell_phi"]
+    dx, dy, dz = a["pgrid_dx"][:, 0, 0], a["pgrid_dy"][0, :, 0], a["pgrid_dz"][0, 0, :]
+    axes = (np.cumsum(dx) - dx / 2, dx, np.cumsum(dy) - dy / 2, dy, np.cumsum(dz) - dz / 2, dz)
+    names = OUT.PRINT_RESULT_VTK_FIELDS
+    fields = [(names[0], dev["p"]), (names[1], dev["u"]), (names[2], dev["v"]), (names[3], dev["w"]),
+              (names[4], dev["phil"]), (names[5], phi), (names[6], dev["vofl"]), (names[7], dev["vof"])]
+    shape = (w.imax, w.jmax, w.kmax)
+    d = tempfile.mkdtemp(prefix="scf_vtr_")
+    path = os.path.join(d, "PCell_3D.vtr")
+    for _ in range(args.warmup):
+        OUT.write_vtr(path, shape, axes, fields)
+    runs = [OUT.write_vtr(path, shape, axes, fields) for _ in range(args.steps)]
+    nbytes = runs[-1]["bytes_file"]
+    cpu = None
+    if not args.no_cpu:
+        from oracle import vtr as V
+        host = [(names[0], pp), (names[1], u), (names[2], v), (names[3], ww), (names[4], a["phil"]),
+                (names[5], phi), (names[6], a["vofl"]), (names[7], a["vof"])]
+        t0 = time.perf_counter()
+        V.write_vtr(path + ".ref", shape, axes, host)
+        cpu = {"value": round((time.perf_counter() - t0) * 1e3, 1), "unit": "ms/snapshot", "cores": 1,
+               "kind": "port", "sample": "one 256^3 snapshot of the 8 fields from host arrays (numpy restatement)"}
+        same = open(path, "rb").read() == open(path + ".ref", "rb").read()
+        os.unlink(path + ".ref")
+    else:
+        same = None
+    os.unlink(path)
+    os.rmdir(d)
+    mean = lambda k: statistics.mean(r[k] for r in runs)
+    n = w.imax * w.jmax * w.kmax
+    peak, peak_kind = measured_peaks()
+    conv_ms = mean("ms_convert") / 8
+    by = 12.0 * n     # one FP64 read and one FP32 write per cell and field
+    line = {
+        "metric": "ms per PrintResultVTK snapshot (8 fields, 256^3) from device-resident fields to a .vtr file",
+        "value": round(mean("ms_total"), 3), "unit": "ms/snapshot", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(mean("ms_total"), 3), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64->f32", "data": "a c2 projection's fields (synthetic)",
+        "config": {"workload": "c2 256^3 snapshot: p, u, v, w, phiL, phi, vofL, vof", "file_bytes": nbytes,
+                   "file_system": "tempfile.gettempdir() of the box"},
+        "breakdown_ms": {"convert": round(mean("ms_convert"), 3), "d2h": round(mean("ms_d2h"), 3),
+                         "write": round(mean("ms_write"), 3)},
+        "roofline": {"bound": "hbm", "kernel": "k_gather_f32 (gather + FP32 rounding of one field)",
+                     "achieved": round(by / (conv_ms * 1e-3) / 1e9, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(by / (conv_ms * 1e-3) / 1e9 / peak, 4), "peak_kind": peak_kind,
+                     "bytes_per_launch": by, "ms_per_launch": round(conv_ms, 5),
+                     "timing": "CUDA events around each conversion launch"},
+        "identical_to_oracle": same,
+        "gpu_launches": sum(r["gpu_launches"] for r in runs),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -536,7 +605,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c2",
-                    help="c0..c4, or geometry (the cut-cell geometry preprocessing of the c2 geometry)")
+                    help="c0..c4; geometry (the cut-cell geometry preprocessing of the c2 geometry); output "
+                         "(a PrintResultVTK snapshot of a c2 projection)")
     ap.add_argument("--tol", type=float, default=1e-8)
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--n", type=int, default=None, help="smaller grid (profiling captures only)")
@@ -555,6 +625,8 @@ def main():
         return run_sequence(args)
     if args.config == "geometry":
         return run_geometry(args)
+    if args.config == "output":
+        return run_output(args)
     return run_ours(args)
 
 

@@ -44,7 +44,9 @@ typedef struct scf_vtr_stats {
  * and widths along each axis (TGrid%x(:,1,1), TGrid%dx(:,1,1), ...).  The
  * node coordinates are Float32 of xc(i) - dx(i)/2, i = 1..I, and
  * xc(I) + dx(I)/2, as PrintResultVTK computes them.  Fields with
- * on_device = 1 must be on CUDA device `device`.                          */
+ * on_device = 1 must be on CUDA device `device`.  J and K are at most
+ * 65535.  Returns SCF_ERR_BAD_ARG for a bad name or size or a file that
+ * cannot be written.                                                      */
 int scf_write_vtr(const char *path, int32_t imax, int32_t jmax, int32_t kmax, const double *xc,
                   const double *dx, const double *yc, const double *dy, const double *zc, const double *dz,
                   int32_t nfields, const scf_vtr_field *fields, int32_t device, scf_vtr_stats *stats);

@@ -18,15 +18,16 @@
 
 namespace {
 
+// One block row of 256 cells along i of one (j, k) line per block:
+// grid (ceil(I/256), J, K), no index division.
 __global__ void __launch_bounds__(256) k_gather_f32(const double *__restrict__ src, float *__restrict__ dst, int I,
-                                                    int J, int K)
+                                                    int J)
 {
-    const long long n = (long long)I * J * K;
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        const int i = (int)(q % I), j = (int)((q / I) % J), k = (int)(q / ((long long)I * J));
-        const long long g = (i + 1) + (long long)(I + 2) * ((j + 1) + (long long)(J + 2) * (k + 1));
-        dst[q] = __double2float_rn(src[g]);
-    }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= I) return;
+    const int j = blockIdx.y, k = blockIdx.z;
+    const long long g = (i + 1) + (long long)(I + 2) * ((j + 1) + (long long)(J + 2) * (k + 1));
+    dst[i + (long long)I * (j + (long long)J * k)] = __double2float_rn(src[g]);
 }
 
 bool name_ok(const char *s)
@@ -75,7 +76,7 @@ extern "C" int scf_write_vtr(const char *path, int32_t imax, int32_t jmax, int32
                              int32_t nfields, const scf_vtr_field *fields, int32_t device, scf_vtr_stats *stats)
 {
     const auto t0 = std::chrono::steady_clock::now();
-    if (!path || imax < 1 || jmax < 1 || kmax < 1 || !xc || !dx || !yc || !dy || !zc || !dz || nfields < 0 ||
+    if (!path || imax < 1 || jmax < 1 || kmax < 1 || jmax > 65535 || kmax > 65535 || !xc || !dx || !yc || !dy || !zc || !dz || nfields < 0 ||
         (nfields > 0 && !fields))
         return SCF_ERR_BAD_ARG;
     for (int q = 0; q < nfields; ++q)
@@ -163,7 +164,7 @@ extern "C" int scf_write_vtr(const char *path, int32_t imax, int32_t jmax, int32
                 c.dev.push_back(p);
                 dsrc[s] = (double *)p;
             }
-        const int blocks = (int)std::min<long long>((n + 255) / 256, 152 * 16);
+        const dim3 grid((imax + 255) / 256, jmax, kmax);
         // field q on slot q%2: [host copy in] gather+round, D2H; the host
         // writes field q-1 while field q converts and copies
         auto issue = [&](int q) {
@@ -175,7 +176,7 @@ extern "C" int scf_write_vtr(const char *path, int32_t imax, int32_t jmax, int32
                 src = dsrc[s];
             }
             cudaEventRecord(c.ev[3 * s], st);
-            k_gather_f32<<<blocks, 256, 0, st>>>(src, dbuf[s], imax, jmax, kmax);
+            k_gather_f32<<<grid, 256, 0, st>>>(src, dbuf[s], imax, jmax);
             cudaEventRecord(c.ev[3 * s + 1], st);
             cudaMemcpyAsync(hbuf[s], dbuf[s], sizeof(float) * n, cudaMemcpyDeviceToHost, st);
             cudaEventRecord(c.ev[3 * s + 2], st);
