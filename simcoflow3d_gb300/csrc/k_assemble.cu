@@ -3,6 +3,8 @@
 // Compiled with -fmad=false: every product and sum is rounded on its own, in
 // the reference's evaluation order, so PoCoef, the operator and b are
 // bit-identical to a strict IEEE evaluation of the Fortran expressions.
+#include <cuda_pipeline.h>
+
 #include "scf_kernels.h"
 
 namespace {
@@ -452,16 +454,57 @@ __device__ __forceinline__ double amul(double ar, double u)
 }
 }  // namespace
 
-template <bool MIXED>
-__global__ void __launch_bounds__(128) k_operator(AsmArgs a, OpArgs o)
+// Staged inputs of one cell of k_operator: FP64 values and int32 values,
+// one smem column per thread (struct of arrays: consecutive threads hit
+// consecutive banks).
+enum OpVal { V_DX, V_DY, V_DZ, V_P1, V_P2, V_P3, V_P4, V_P5, V_P6, V_EW, V_EE, V_NS, V_NN, V_TB, V_TT,
+             V_UW, V_UE, V_VS, V_VN, V_WB, V_WT, V_VF, V_VO, V_COUNT };
+enum OpInt { I_CT, I_POS, I_PW, I_PE, I_PS, I_PN, I_PB, I_PT, I_COUNT };
+constexpr int OP_THREADS = 128;
+constexpr size_t OP_SMEM = 2 * (sizeof(double) * V_COUNT + sizeof(int) * I_COUNT) * OP_THREADS;
+
+// Asynchronous copies (cp.async) of cell (i,j,k)'s inputs into stage `st`:
+// the loads of the next cell are in flight while the current one is
+// computed, without holding registers.  Neighbour PosNu entries that the
+// cell does not use read the cell's own entry (always in range).
+__device__ __forceinline__ void op_issue(const AsmArgs &a, double *sd, int *si, int tid, int i, int j, int k)
 {
     const Dims &d = a.d;
+    const int sy = d.gx, sz = d.gx * d.gy;
+    const int g = gidx(d, i, j, k), n = nidx(d, i, j, k);
+    const long long N = d.n;
+    const double *src[V_COUNT] = {a.pdx + n, a.pdy + n, a.pdz + n, a.pocoef + n, a.pocoef + n + N,
+                                  a.pocoef + n + 2 * N, a.pocoef + n + 3 * N, a.pocoef + n + 4 * N,
+                                  a.pocoef + n + 5 * N, a.ee + g - 1, a.ee + g, a.ne + g - sy, a.ne + g,
+                                  a.te + g - sz, a.te + g, a.us + g - 1, a.us + g, a.vs + g - sy, a.vs + g,
+                                  a.ws + g - sz, a.ws + g, a.vof + g, a.vofo + g};
+#pragma unroll
+    for (int v = 0; v < V_COUNT; ++v) __pipeline_memcpy_async(sd + v * OP_THREADS + tid, src[v], sizeof(double));
+    const int IJ = d.I * d.J;
+    const int *isrc[I_COUNT] = {a.ct + n, a.pos + n, a.pos + (i > 1 ? n - 1 : n), a.pos + (i < d.I ? n + 1 : n),
+                                a.pos + (j > 1 ? n - d.I : n), a.pos + (j < d.J ? n + d.I : n),
+                                a.pos + (k > 1 ? n - IJ : n), a.pos + (k < d.K ? n + IJ : n)};
+#pragma unroll
+    for (int v = 0; v < I_COUNT; ++v) __pipeline_memcpy_async(si + v * OP_THREADS + tid, isrc[v], sizeof(int));
+    __pipeline_commit();
+}
+
+// Matrix rows, FP32 copies and right-hand side of each cell (a block is
+// 32 x 4 columns, each thread marches one KSEG segment along k).  The
+// inputs of cell k+1 are copied into shared memory while cell k is
+// computed (two stages).
+template <bool MIXED>
+__global__ void __launch_bounds__(OP_THREADS) k_operator(AsmArgs a, OpArgs o)
+{
+    extern __shared__ __align__(16) unsigned char op_smem[];
+    double *sd0 = (double *)op_smem;
+    int *si0 = (int *)(sd0 + 2 * V_COUNT * OP_THREADS);
+    const Dims &d = a.d;
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     if (i > d.I || j > d.J) return;
     const int kbeg = blockIdx.z * KSEG + 1, kend = min(kbeg + KSEG - 1, d.K);
-    const int sy = d.gx, sz = d.gx * d.gy;
-    const long long N = d.n;
     const int *fl = a.flag;
     TermMemo tm[6];
 #pragma unroll
@@ -474,11 +517,26 @@ __global__ void __launch_bounds__(128) k_operator(AsmArgs a, OpArgs o)
     float d32 = 0.f;
     // memo of the spacing products of the rhs
     unsigned long long pdx = 0, pdy = 0, pdz = 0;
-    double dydz = 0.0, dxdz = 0.0, dxdy = 0.0, dxdydz = 0.0;
+    double dydz = 0.0, dxdz = 0.0, dxdy = 0.0;
     bool pvalid = false;
+    op_issue(a, sd0, si0, tid, i, j, kbeg);
+    unsigned char ph_next = a.phase[gidx(d, i, j, kbeg)];
     for (int k = kbeg; k <= kend; ++k) {
-        const int g = gidx(d, i, j, k), n = nidx(d, i, j, k);
-        const int ct = a.ct[n], pos = a.pos[n];
+        const int st = (k - kbeg) & 1;
+        const double *sd = sd0 + st * V_COUNT * OP_THREADS;
+        const int *si = si0 + st * I_COUNT * OP_THREADS;
+        const unsigned char ph = ph_next;
+        if (k < kend) {
+            op_issue(a, sd0 + (st ^ 1) * V_COUNT * OP_THREADS, si0 + (st ^ 1) * I_COUNT * OP_THREADS, tid, i, j, k + 1);
+            ph_next = a.phase[gidx(d, i, j, k + 1)];
+            __pipeline_wait_prior(1);
+        } else {
+            __pipeline_wait_prior(0);
+        }
+#define SV(v) sd[(v) * OP_THREADS + tid]
+#define SI(v) si[(v) * OP_THREADS + tid]
+        const int g = gidx(d, i, j, k);
+        const int ct = SI(I_CT), pos = SI(I_POS);
         if ((pos == -1) != (ct == 2) || pos > a.ext_cell || pos < -1) atomicOr(a.flags, FLAG_BAD_POSNU);
         if (ct == 2) {   // solid: identity-free row, marked by diag = -1 (x stays 0 there)
             o.diag[g] = -1.0; o.dinv[g] = 0.0; o.cE[g] = 0.0; o.cN[g] = 0.0; o.cT[g] = 0.0;
@@ -490,12 +548,12 @@ __global__ void __launch_bounds__(128) k_operator(AsmArgs a, OpArgs o)
             }
             continue;
         }
-        const double dx = a.pdx[n], dy = a.pdy[n], dz = a.pdz[n];
-        const double p1 = a.pocoef[n], p2 = a.pocoef[n + N], p3 = a.pocoef[n + 2 * N];
-        const double p4 = a.pocoef[n + 3 * N], p5 = a.pocoef[n + 4 * N], p6 = a.pocoef[n + 5 * N];
-        const double eW = a.ee[g - 1], eE = a.ee[g];
-        const double nS = a.ne[g - sy], nN = a.ne[g];
-        const double tB = a.te[g - sz], tT = a.te[g];
+        const double dx = SV(V_DX), dy = SV(V_DY), dz = SV(V_DZ);
+        const double p1 = SV(V_P1), p2 = SV(V_P2), p3 = SV(V_P3);
+        const double p4 = SV(V_P4), p5 = SV(V_P5), p6 = SV(V_P6);
+        const double eW = SV(V_EW), eE = SV(V_EE);
+        const double nS = SV(V_NS), nN = SV(V_NN);
+        const double tB = SV(V_TB), tT = SV(V_TT);
         const double t1 = term_memo(tm[0], p1, eW, dy, dz), t2 = term_memo(tm[1], p2, nS, dx, dz);
         const double t3 = term_memo(tm[2], p3, tB, dx, dy), t4 = term_memo(tm[3], p4, eE, dy, dz);
         const double t5 = term_memo(tm[4], p5, nN, dx, dz), t6 = term_memo(tm[5], p6, tT, dx, dy);
@@ -515,12 +573,12 @@ __global__ void __launch_bounds__(128) k_operator(AsmArgs a, OpArgs o)
         // boundary faces and faces to solid cells (bit f, order W,S,B,E,N,T)
         double cE = 0.0, cN = 0.0, cT = 0.0;
         int xm = 0;
-        if (i == 1) { if (fl[0] == 0) xm |= 1; } else if (a.pos[n - 1] == -1) xm |= 1;
-        if (j == 1) { if (fl[2] == 0) xm |= 2; } else if (a.pos[n - d.I] == -1) xm |= 2;
-        if (k == 1) { if (fl[4] == 0) xm |= 4; } else if (a.pos[n - d.I * d.J] == -1) xm |= 4;
-        if (i == d.I) { if (fl[1] == 0) xm |= 8; } else if (a.pos[n + 1] == -1) xm |= 8; else cE = t4;
-        if (j == d.J) { if (fl[3] == 0) xm |= 16; } else if (a.pos[n + d.I] == -1) xm |= 16; else cN = t5;
-        if (k == d.K) { if (fl[5] == 0) xm |= 32; } else if (a.pos[n + d.I * d.J] == -1) xm |= 32; else cT = t6;
+        if (i == 1) { if (fl[0] == 0) xm |= 1; } else if (SI(I_PW) == -1) xm |= 1;
+        if (j == 1) { if (fl[2] == 0) xm |= 2; } else if (SI(I_PS) == -1) xm |= 2;
+        if (k == 1) { if (fl[4] == 0) xm |= 4; } else if (SI(I_PB) == -1) xm |= 4;
+        if (i == d.I) { if (fl[1] == 0) xm |= 8; } else if (SI(I_PE) == -1) xm |= 8; else cE = t4;
+        if (j == d.J) { if (fl[3] == 0) xm |= 16; } else if (SI(I_PN) == -1) xm |= 16; else cN = t5;
+        if (k == d.K) { if (fl[5] == 0) xm |= 32; } else if (SI(I_PT) == -1) xm |= 32; else cT = t6;
         const double ex = xm ? extra_sum(t1, t2, t3, t4, t5, t6, xm) : 0.0;
 
         // right-hand side (ProjectionP.f90:521-546), same rounding as the
@@ -530,11 +588,13 @@ __global__ void __launch_bounds__(128) k_operator(AsmArgs a, OpArgs o)
             const double3 sp = spacing_products(dx, dy, dz);
             dydz = sp.x; dxdz = sp.y; dxdy = sp.z;
         }
-        const double A = amul(eE, a.us[g]) - amul(eW, a.us[g - 1]);
-        const double B = amul(nN, a.vs[g]) - amul(nS, a.vs[g - sy]);
-        const double Cc = amul(tT, a.ws[g]) - amul(tB, a.ws[g - sz]);
+        const double A = amul(eE, SV(V_UE)) - amul(eW, SV(V_UW));
+        const double B = amul(nN, SV(V_VN)) - amul(nS, SV(V_VS));
+        const double Cc = amul(tT, SV(V_WT)) - amul(tB, SV(V_WB));
         double r = dydz * A - dxdz * B - dxdy * Cc;
-        const double vf = a.vof[g], vo = a.vofo[g];
+        const double vf = SV(V_VF), vo = SV(V_VO);
+#undef SV
+#undef SI
         if (bits(vf) == bits(vo) && finite_bits(vf)) {
             // (vof - vofO)*dx*dy*dz/dt is +0 exactly, and r + 0.0 is r except
             // that -0 becomes +0
@@ -554,7 +614,7 @@ __global__ void __launch_bounds__(128) k_operator(AsmArgs a, OpArgs o)
         else if ((long long)bits(dg) <= 0) atomicOr(a.flags, FLAG_BAD_DIAG);   // dg <= 0 (finite)
         if (!finite_bits(r) || !finite_bits(cE) || !finite_bits(cN) || !finite_bits(cT) || !finite_bits(ex))
             atomicOr(a.flags, FLAG_NONFINITE);
-        if (a.phase[g] == 0) atomicOr(a.flags, FLAG_NEITHER_ACTIVE);
+        if (ph == 0) atomicOr(a.flags, FLAG_NEITHER_ACTIVE);
 
         o.diag[g] = dg;
         if (!MIXED) o.dinv[g] = dinv;
@@ -612,10 +672,14 @@ int launch_assemble(const AsmArgs &a, const OpArgs &o, bool mixed, const double 
         *launches += 1;
     }
     dim3 ob(32, 4), og((d.I + 31) / 32, (d.J + 3) / 4, (d.K + KSEG - 1) / KSEG);
+    // the staged inputs need more than the default 48 KB of dynamic shared
+    // memory (set per device, so on every call)
+    cudaFuncSetAttribute(k_operator<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OP_SMEM);
+    cudaFuncSetAttribute(k_operator<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)OP_SMEM);
     if (mixed)
-        k_operator<true><<<og, ob, 0, st>>>(a, o);
+        k_operator<true><<<og, ob, OP_SMEM, st>>>(a, o);
     else
-        k_operator<false><<<og, ob, 0, st>>>(a, o);
+        k_operator<false><<<og, ob, OP_SMEM, st>>>(a, o);
     *launches += 1;
     return (int)cudaGetLastError();
 }
