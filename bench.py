@@ -381,6 +381,7 @@ def run_ours(args):
                  "rel_residual": s64["rel_residual"]},
         "mixed": {"iterations": smx["iterations"], "rel_residual": smx["rel_residual"],
                   "smoother_degree": degree["mixed"],
+                  "ms_steps": [round(x, 3) for x in results["mixed"]["ms"]],
                   "ms_assemble": round(smx["ms_assemble"], 3), "ms_solve": round(smx["ms_solve"], 3),
                   "ms_correct": round(smx["ms_correct"], 3)},
         "speedup_mixed_vs_fp64": round(fp64 / value, 3),
