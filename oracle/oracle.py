@@ -55,6 +55,14 @@ def lib():
         L.oracle_gmg_solve.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(capi.ScfPoissonIn), dp, dp, dp,
                                        C.POINTER(GmgParams)]
         L.oracle_num_threads.restype = C.c_int
+        PM, PO = C.POINTER(capi.ScfMomIn), C.POINTER(capi.ScfMomOpts)
+        L.oracle_mom_system.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, PM, PO, i64p, ip, dp, dp, dp]
+        L.oracle_mom_system.restype = C.c_long
+        L.oracle_csr_bicgstab.argtypes = [C.c_long, i64p, ip, dp, dp, dp, C.c_double, C.c_int,
+                                          C.POINTER(C.c_double)]
+        L.oracle_csr_bicgstab.restype = C.c_int
+        L.oracle_mom_get_values.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, PM, dp, dp]
+        L.oracle_predict_tail.argtypes = [C.c_int, C.c_int, C.c_int, PM] + [dp] * 6
         _lib = L
     return _lib
 
@@ -247,3 +255,57 @@ def grid_preprocess(g):
     for f, s in zip(GM.FAMILIES, ss):
         out.fams[f].ext_cell = s.ext_cell
     return out
+
+
+def mom_system(inp, opts, comp: int, dp_arr=None):
+    """SetMatrix + SetVectors (PredictUVW.f90:856-1292) of component comp
+    (0 = u): (CSR (rowptr, cols, vals), rhs, dp).  ``dp_arr`` (ghosted) is
+    updated on the loop range like PUVW%Dp; a new zero array if None."""
+    I, J, K = inp.imax, inp.jmax, inp.kmax
+    n = inp.comps[comp].extcell + 1
+    rp = np.zeros(n + 1, np.int64)
+    ci = np.zeros(7 * max(n, 1), np.int32)
+    va = np.zeros(7 * max(n, 1))
+    rhs = np.zeros(max(n, 1))
+    dp_arr = np.zeros(inp.shape_g(), order="F") if dp_arr is None else dp_arr
+    st = inp.comps[comp].struct()
+    nnz = lib().oracle_mom_system(I, J, K, comp + 1, C.byref(st), C.byref(opts),
+                                  rp.ctypes.data_as(C.POINTER(C.c_int64)), ci.ctypes.data_as(capi.c_int32_p),
+                                  _dp(va), _dp(rhs), _dp(dp_arr))
+    if nnz < 0:
+        raise ValueError("PosNu numbering does not match Cell_Type / ExtCell")
+    return (rp, ci[:nnz], va[:nnz]), rhs[:n], dp_arr
+
+
+def csr_bicgstab(A, b, tol=1e-14, maxit=20000):
+    rp, ci, va = A
+    x = np.zeros_like(b)
+    rel = C.c_double()
+    it = lib().oracle_csr_bicgstab(rp.size - 1, rp.ctypes.data_as(C.POINTER(C.c_int64)),
+                                   ci.ctypes.data_as(capi.c_int32_p), _dp(va), _dp(b), _dp(x), tol, maxit,
+                                   C.byref(rel))
+    return x, it, rel.value
+
+
+def predict_solves(inp, opts, pred=None, dp=None, tol=1e-14):
+    """The solve part of PredictingUVW (PredictUVW.f90:691-802) on the CPU:
+    per component SetMatrix/SetVectors, a BiCGStab solve to ``tol`` (true
+    residual), DeltaGetValues; then the Dp ghost planes, the predictor's
+    velocity BCs and the solid cells.  ``pred``/``dp`` are updated in place
+    (new zero arrays if None).  Returns (pred, dp, info)."""
+    I, J, K = inp.imax, inp.jmax, inp.kmax
+    shp = inp.shape_g()
+    pred = pred if pred is not None else [np.zeros(shp, order="F") for _ in range(3)]
+    dp = dp if dp is not None else [np.zeros(shp, order="F") for _ in range(3)]
+    info = []
+    for c in range(3):
+        A, b, _ = mom_system(inp, opts, c, dp[c])
+        x, it, rel = csr_bicgstab(A, b, tol=tol)
+        if it < 0:
+            raise RuntimeError("oracle BiCGStab did not converge (component %d, rel %.3e)" % (c, rel))
+        st = inp.comps[c].struct()
+        lib().oracle_mom_get_values(I, J, K, c + 1, C.byref(st), _dp(x), _dp(pred[c]))
+        info.append({"iterations": it, "rel_residual": rel, "rows": b.size})
+    structs = inp.structs()
+    lib().oracle_predict_tail(I, J, K, structs, *(_dp(a) for a in pred), *(_dp(a) for a in dp))
+    return pred, dp, info

@@ -31,6 +31,9 @@ UNITS = {
     "k_geometry.cu": ["-fmad=false"],
     "geo_api.cu": [],
     "k_output.cu": [],
+    "k_predictor.cu": ["-fmad=false"],
+    "k_bicgstab.cu": [],
+    "pred_api.cu": [],
 }
 
 
@@ -48,6 +51,7 @@ def _compile(unit: str, extra, verbose: bool):
     deps.append(os.path.join(HERE, "..", "include", "scf_projection.h"))
     deps.append(os.path.join(HERE, "..", "include", "scf_geometry.h"))
     deps.append(os.path.join(HERE, "..", "include", "scf_output.h"))
+    deps.append(os.path.join(HERE, "..", "include", "scf_predictor.h"))
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
         return obj
     cmd = [nvcc(), "-c", src, "-o", obj] + ARCH + COMMON + list(extra)

@@ -153,6 +153,46 @@ class ScfVtrStats(C.Structure):
                 ("ms_total", C.c_double), ("bytes_file", C.c_int64), ("gpu_launches", C.c_int32)]
 
 
+class ScfMomIn(C.Structure):
+    """scf_mom_in of include/scf_predictor.h: one velocity component."""
+    _fields_ = [
+        ("grid_dx", c_double_p), ("grid_dy", c_double_p), ("grid_dz", c_double_p),
+        ("vof", c_double_p), ("vofl", c_double_p),
+        ("eta_e", c_double_p), ("eta_n", c_double_p), ("eta_t", c_double_p),
+        ("cell_type", c_int32_p), ("posnu", c_int32_p), ("extcell", C.c_int32),
+        ("vof_old", c_double_p),
+        ("df_ew", c_double_p), ("df_ns", c_double_p), ("df_tb", c_double_p),
+        ("edf_ew", c_double_p), ("edf_ns", c_double_p), ("edf_tb", c_double_p),
+        ("fric", c_double_p), ("flux_div", c_double_p), ("tvar", c_double_p),
+        ("bc_flag", C.c_int32 * 6), ("bc_var", c_double_p * 6),
+    ]
+
+
+class ScfMomOpts(C.Structure):
+    _fields_ = [
+        ("dt", C.c_double), ("rho_a_ref", C.c_double), ("rho_w_ref", C.c_double), ("fr", C.c_double),
+        ("gx", C.c_double), ("gy", C.c_double), ("gz", C.c_double), ("g", C.c_double),
+        ("beta_vis", C.c_double), ("rel_tol", C.c_double), ("max_iter", C.c_int32), ("precision", C.c_int32),
+    ]
+
+
+class ScfMomStats(C.Structure):
+    _fields_ = [
+        ("iterations", C.c_int32 * 3), ("rounds", C.c_int32 * 3), ("converged", C.c_int32 * 3),
+        ("rel_residual", C.c_double * 3),
+        ("ms_assemble", C.c_double), ("ms_solve", C.c_double), ("ms_tail", C.c_double),
+        ("ms_h2d", C.c_double), ("ms_d2h", C.c_double), ("ms_total", C.c_double),
+        ("bytes_h2d", C.c_int64), ("bytes_d2h", C.c_int64), ("gpu_launches", C.c_int32),
+    ]
+
+    def as_dict(self):
+        out = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            out[name] = list(v) if hasattr(v, "__len__") else v
+        return out
+
+
 def dptr(a: Optional[np.ndarray]):
     if a is None:
         return c_double_p()

@@ -1,0 +1,327 @@
+// k_predictor.cu -- assembly of the momentum systems and the tail of
+// PredictingUVW (src/PredictUVW.f90).  Compiled with -fmad=false: every
+// FP64 expression below is evaluated with the reference's operations in its
+// order, so Dp is bit-identical to the Fortran and the rows differ from
+// HYPRE's only by the Jacobi scaling.
+#include "pred_kernels.h"
+
+namespace pred {
+
+dim3 interior_block() { return dim3(32, 4, 2); }
+dim3 interior_grid(const Dims &d) { return dim3((d.I + 31) / 32, (d.J + 3) / 4, (d.K + 1) / 2); }
+
+namespace {
+
+__device__ __forceinline__ long long gidx(const Dims &d, int i, int j, int k) { return i + d.sy * j + d.sz * k; }
+
+// The inputs of one row of SetMatrix that do not depend on the velocity:
+// six conductances DF, six cut-face terms EDF, six interpolation weights
+// Eta, vof, vofL, dx, dy, dz, Fric, and which k-boundary the row touches.
+struct RowKey {
+    double v[24];
+    int kb;
+};
+
+// What a row's key determines: the scaled couplings a_d / aP, 1/aP, Dp,
+// the gravity term of the rhs, and the boundary coefficients CWE/CSN/CBT.
+struct RowMemo {
+    double m[6];   // W,S,B,E,N,T
+    double inv, dp, gterm;
+    double cb[6];  // W,E,S,N,B,T boundary coefficients (before the cut-cell terms)
+};
+
+enum { KDFE, KDFW, KDFN, KDFS, KDFT, KDFB, KEE, KEW, KEN, KES, KET, KEB, KETAE, KETAW, KETAN, KETAS, KETAT, KETAB,
+       KVOF, KVOFL, KDX, KDY, KDZ, KFRIC };
+
+// SetMatrix for one row (PredictUVW.f90:904-1040) with the reference's
+// operations in its order; called only when the key differs from the
+// previous row's (never inlined, so none of it runs speculatively).
+__device__ __noinline__ void mom_row(const RowKey &K, const MomParams &o, int comp, int ib, RowMemo &M)
+{
+    const int iu = comp == 1, iv = comp == 2, iw = comp == 3;
+    const double CoefEW = (double)iu + (double)iv / 2.0 + (double)iw / 2.0;
+    const double CoefNS = (double)iu / 2.0 + (double)iv + (double)iw / 2.0;
+    const double CoefTB = (double)iu / 2.0 + (double)iv / 2.0 + (double)iw;
+    const double omb = 1.0 - o.beta_vis;
+    const double *v = K.v;
+    const double vof = v[KVOF], vofl = v[KVOFL];
+    const double rho = vofl * o.rho_w + (vof - vofl) * o.rho_a;
+    double Dfe = omb * v[KDFE] / rho, Dfw = omb * v[KDFW] / rho;
+    double Dfn = omb * v[KDFN] / rho, Dfs = omb * v[KDFS] / rho;
+    double Dft = omb * v[KDFT] / rho, Dfb = omb * v[KDFB] / rho;
+    const double ee = v[KEE], ew = v[KEW], en = v[KEN], es = v[KES], et = v[KET], eb = v[KEB];
+    const double etaE = v[KETAE], etaW = v[KETAW], etaN = v[KETAN], etaS = v[KETAS], etaT = v[KETAT],
+                 etaB = v[KETAB];
+    double Fep = ee * (1.0 - etaE) / rho, Fem = ee * etaE / rho;
+    double Fwp = ew * etaW / rho, Fwm = ew * (1.0 - etaW) / rho;
+    double Fnp = en * (1.0 - etaN) / rho, Fnm = en * etaN / rho;
+    double Fsp = es * etaS / rho, Fsm = es * (1.0 - etaS) / rho;
+    double Ftp = et * (1.0 - etaT) / rho, Ftm = et * etaT / rho;
+    double Fbp = eb * etaB / rho, Fbm = eb * (1.0 - etaB) / rho;
+    // boundary faces (939-1009); ib bits: i = 1, i = ie, j = 1, j = je,
+    // k = 1, k = ke; flags 1 = Neumann
+    const int *fl = o.flags;
+    if (ib & 1) {
+        if (fl[0] == 1) { Dfw = 0.0; Fwp = 0.0; Fwm = 0.0; }
+        else { Dfw = Dfw * CoefEW; Fwp = Fwp * CoefEW; Fwm = Fwm * CoefEW; }
+    }
+    if (ib & 2) {
+        if (fl[1] == 1) { Dfe = 0.0; Fep = 0.0; Fem = 0.0; }
+        else { Dfe = Dfe * CoefEW; Fep = Fep * CoefEW; Fem = Fem * CoefEW; }
+    }
+    if (ib & 4) {
+        if (fl[2] == 1) { Dfs = 0.0; Fsp = 0.0; Fsm = 0.0; }
+        else { Dfs = Dfs * CoefNS; Fsp = Fsp * CoefNS; Fsm = Fsm * CoefNS; }
+    }
+    if (ib & 8) {
+        if (fl[3] == 1) { Dfn = 0.0; Fnp = 0.0; Fnm = 0.0; }
+        else { Dfn = Dfn * CoefNS; Fnp = Fnp * CoefNS; Fnm = Fnm * CoefNS; }
+    }
+    if (ib & 16) {
+        if (fl[4] == 1) { Dfb = 0.0; Fbp = 0.0; Fbm = 0.0; }
+        else { Dfb = Dfb * CoefTB; Fbp = Fbp * CoefTB; Fbm = Fbm * CoefTB; }
+    }
+    if (ib & 32) {
+        if (fl[5] == 1) { Dft = 0.0; Ftp = 0.0; Ftm = 0.0; }
+        else { Dft = Dft * CoefTB; Ftp = Ftp * CoefTB; Ftm = Ftm * CoefTB; }
+    }
+    double aE = Dfe, aW = Dfw, aN = Dfn, aS = Dfs, aT = Dft, aB = Dfb;
+    M.cb[0] = aW; M.cb[1] = aE; M.cb[2] = aS; M.cb[3] = aN; M.cb[4] = aB; M.cb[5] = aT;   // CWE/CSN/CBT
+    const double dx = v[KDX], dy = v[KDY], dz = v[KDZ];
+    double aP = vof * dx * dy * dz / o.dt + aE + aW + aN + aS + aT + aB + v[KFRIC];
+    aP = aP + Fep - Fwp + Fnp - Fsp + Ftp - Fbp;
+    aE = aE - Fem;
+    aW = aW + Fwm;
+    aN = aN - Fnm;
+    aS = aS + Fsm;
+    aT = aT - Ftm;
+    aB = aB + Fbm;
+    const double dp0 = 1.0 / (aP - aE - aW - aN - aS - aT - aB);
+    M.dp = vof * dx * dy * dz * dp0;
+    const double G3 = o.gx * (double)iu + o.gy * (double)iv + o.gz * (double)iw;
+    M.gterm = 1.0 / (o.fr * o.fr) * vof * dx * dy * dz * G3 / o.g;
+    const double inv = 1.0 / aP;
+    M.inv = inv;
+    M.m[0] = aW * inv; M.m[1] = aS * inv; M.m[2] = aB * inv;
+    M.m[3] = aE * inv; M.m[4] = aN * inv; M.m[5] = aT * inv;
+}
+
+__device__ __forceinline__ bool same_key(const RowKey &a, const RowKey &b)
+{
+    bool eq = a.kb == b.kb;
+#pragma unroll
+    for (int q = 0; q < 24; ++q) eq = eq && __double_as_longlong(a.v[q]) == __double_as_longlong(b.v[q]);
+    return eq;
+}
+
+// One thread per (i, j) column, marching KZ cells along k.  Active cells of
+// the loop range (i <= I-iu, j <= J-iv, k <= K-iw, Cell_Type /= 2) get the
+// row of SetMatrix scaled by 1/aP and the rhs of SetVectors (1211-1251),
+// every other interior cell an identity row.  Dp: 0 on the loop range,
+// vof*dV/(aP - the neighbour coefficients) on its active cells (913, 1040,
+// 1226-1237).  Consecutive rows of a column with bit-identical keys (most
+// rows away from the interface and the solid) reuse the previous row's
+// memo, so the FP64 divisions run only where the inputs change.
+__global__ void __launch_bounds__(128) k_mom_assemble(MomDev in, MomParams o, int comp, Dims d, MomSys S,
+                                                      int want32, int kz)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k0 = blockIdx.z * kz + 1, k1 = min(k0 + kz - 1, d.K);
+    if (i > d.I || j > d.J) return;
+    const int iu = comp == 1, iv = comp == 2, iw = comp == 3;
+    const int ie = d.I - iu, je = d.J - iv, ke = d.K - iw;
+    const bool col_in = i <= ie && j <= je;
+    const int ibase = (i == 1 ? 1 : 0) | (i == ie ? 2 : 0) | (j == 1 ? 4 : 0) | (j == je ? 8 : 0);
+    const long long sns = d.I, stb = (long long)d.I * d.J;
+    const long long px = ie, pxy = (long long)ie * je;
+    RowKey key, prev;
+    RowMemo M;
+    bool have = false;
+    for (int k = k0; k <= k1; ++k) {
+        const long long c = gidx(d, i, j, k);
+        const long long n = (i - 1) + (long long)d.I * ((j - 1) + (long long)d.J * (k - 1));
+        double mw = 0.0, ms = 0.0, mb = 0.0, me = 0.0, mn = 0.0, mt = 0.0, bh = 0.0;
+        if (col_in && k <= ke) {
+            double dpv = 0.0;
+            if (in.cell_type[n] != 2) {
+                const long long few = i + (long long)(d.I + 2) * ((j - 1) + (long long)d.J * (k - 1));
+                const long long fns = (i - 1) + (long long)d.I * (j + (long long)(d.J + 2) * (k - 1));
+                const long long ftb = (i - 1) + (long long)d.I * ((j - 1) + (long long)d.J * k);
+                double *v = key.v;
+                v[KDFE] = in.df_ew[few + 1]; v[KDFW] = in.df_ew[few];
+                v[KDFN] = in.df_ns[fns + sns]; v[KDFS] = in.df_ns[fns];
+                v[KDFT] = in.df_tb[ftb + stb]; v[KDFB] = in.df_tb[ftb];
+                v[KEE] = in.edf_ew[few + 1]; v[KEW] = in.edf_ew[few];
+                v[KEN] = in.edf_ns[fns + sns]; v[KES] = in.edf_ns[fns];
+                v[KET] = in.edf_tb[ftb + stb]; v[KEB] = in.edf_tb[ftb];
+                v[KETAE] = in.eta_e[c]; v[KETAW] = in.eta_e[c - 1];
+                v[KETAN] = in.eta_n[c]; v[KETAS] = in.eta_n[c - d.sy];
+                v[KETAT] = in.eta_t[c]; v[KETAB] = in.eta_t[c - d.sz];
+                v[KVOF] = in.vof[c]; v[KVOFL] = in.vofl[c];
+                v[KDX] = in.dx[n]; v[KDY] = in.dy[n]; v[KDZ] = in.dz[n];
+                v[KFRIC] = in.fric[n];
+                key.kb = ibase | (k == 1 ? 16 : 0) | (k == ke ? 32 : 0);
+                if (!(have && same_key(key, prev))) {
+                    mom_row(key, o, comp, key.kb, M);
+                    prev = key;
+                    have = true;
+                }
+                dpv = M.dp;
+                // SetVectors: u.vof.dV/dt - u.dV.dvof/dt + gravity - flux +
+                // boundary values, in the reference's order
+                const double vof = key.v[KVOF], dx = key.v[KDX], dy = key.v[KDY], dz = key.v[KDZ];
+                const double U = in.tvar[c] + 0.0;
+                const double dv = vof - in.vof_old[c];
+                const double t1 = U * vof * dx * dy * dz / o.dt;
+                const double t2 = dv == 0.0 ? U * dv * dx * dy * dz : U * dv * dx * dy * dz / o.dt;
+                double rhs = t1 - t2 + M.gterm;
+                rhs = rhs - in.flux_div[n];
+                const int kb = key.kb;
+                if (kb & 1) rhs = rhs + M.cb[0] * in.bc[0][(j - 1) + (long long)d.J * (k - 1)];
+                if (kb & 2) rhs = rhs + M.cb[1] * in.bc[1][(j - 1) + (long long)d.J * (k - 1)];
+                if (kb & 4) rhs = rhs + M.cb[2] * in.bc[2][(i - 1) + (long long)d.I * (k - 1)];
+                if (kb & 8) rhs = rhs + M.cb[3] * in.bc[3][(i - 1) + (long long)d.I * (k - 1)];
+                if (kb & 16) rhs = rhs + M.cb[4] * in.bc[4][(i - 1) + (long long)d.I * (j - 1)];
+                if (kb & 32) rhs = rhs + M.cb[5] * in.bc[5][(i - 1) + (long long)d.I * (j - 1)];
+                // a neighbour couples when it is inside the loop range and
+                // numbered (PosNu /= -1, 1044-1097)
+                const long long pn = (i - 1) + px * (j - 1) + pxy * (k - 1);
+                if (i > 1 && in.posnu[pn - 1] != -1) mw = M.m[0];
+                if (j > 1 && in.posnu[pn - px] != -1) ms = M.m[1];
+                if (k > 1 && in.posnu[pn - pxy] != -1) mb = M.m[2];
+                if (i < ie && in.posnu[pn + 1] != -1) me = M.m[3];
+                if (j < je && in.posnu[pn + px] != -1) mn = M.m[4];
+                if (k < ke && in.posnu[pn + pxy] != -1) mt = M.m[5];
+                bh = rhs * M.inv;
+            }
+            S.dp[c] = dpv;
+        }
+        S.m[0][c] = mw; S.m[1][c] = ms; S.m[2][c] = mb;
+        S.m[3][c] = me; S.m[4][c] = mn; S.m[5][c] = mt;
+        S.b[c] = bh;
+        if (want32) {
+            S.m32[0][c] = (float)mw; S.m32[1][c] = (float)ms; S.m32[2][c] = (float)mb;
+            S.m32[3][c] = (float)me; S.m32[4][c] = (float)mn; S.m32[5][c] = (float)mt;
+        }
+    }
+}
+
+// counts[0]: active cells of the loop range; counts[1]: cells of the loop
+// range whose PosNu is -1 when active, or not -1 when solid.
+__global__ void __launch_bounds__(256) k_mom_numbering(MomDev in, int comp, Dims d, unsigned long long *counts)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z * blockDim.z + threadIdx.z + 1;
+    const int ie = d.I - (comp == 1), je = d.J - (comp == 2), ke = d.K - (comp == 3);
+    unsigned act = 0, bad = 0;
+    if (i <= ie && j <= je && k <= ke) {
+        const bool solid = in.cell_type[(i - 1) + (long long)d.I * ((j - 1) + (long long)d.J * (k - 1))] == 2;
+        const int32_t q = in.posnu[(i - 1) + (long long)ie * ((j - 1) + (long long)je * (k - 1))];
+        act = !solid;
+        bad = solid ? q != -1 : q < 0;
+    }
+    const unsigned a = __syncthreads_count(act), b = __syncthreads_count(bad);
+    if (threadIdx.x == 0 && threadIdx.y == 0 && threadIdx.z == 0) {
+        if (a) atomicAdd(counts, (unsigned long long)a);
+        if (b) atomicAdd(counts + 1, (unsigned long long)b);
+    }
+}
+
+// Dp ghost planes (PredictUVW.f90:766-788), one phase per axis; within a
+// phase each line along the axis is copied in the reference's order.
+// phase 0: lines along i over (j, k) in [0,J+1]x[0,K+1]; 1: along j; 2: along k.
+__global__ void k_dp_phase(double *dp, Dims d, int comp, int phase)
+{
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    const int b = blockIdx.y;
+    long long base, s;
+    int n;
+    if (phase == 0) {
+        if (a > d.J + 1) return;
+        base = d.sy * a + d.sz * b; s = 1; n = d.I;
+    } else if (phase == 1) {
+        if (a > d.I + 1) return;
+        base = a + d.sz * b; s = d.sy; n = d.J;
+    } else {
+        if (a > d.I + 1) return;
+        base = a + d.sy * b; s = d.sz; n = d.K;
+    }
+    double *p = dp + base;
+    p[0] = p[s];
+    if (comp == phase + 1) p[(long long)n * s] = p[(long long)(n - 1) * s];
+    p[(long long)(n + 1) * s] = p[(long long)n * s];
+}
+
+// PredictorVelocityBoundaryCondition (3796-3894) for the component's own
+// axis, then PredictorVelocityInternalCellCondition (3896-3914) on the one
+// plane the boundary condition writes inside 1..I (i = I for u, ...); the
+// loop-range cells of solid type already hold 0.
+__global__ void k_pred_bc(double *pred, MomDev in, Dims d, int comp)
+{
+    const int a = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int b = blockIdx.y + 1;
+    long long base, s;
+    int n, na, ct_idx;
+    const double *varlo, *varhi;
+    int flo, fhi;
+    long long bidx;
+    if (comp == 1) {   // a = j, b = k
+        if (a > d.J) return;
+        base = d.sy * a + d.sz * b; s = 1; n = d.I; na = d.J;
+        bidx = (a - 1) + (long long)d.J * (b - 1);
+        varlo = in.bc[0]; varhi = in.bc[1]; flo = in.flag[0]; fhi = in.flag[1];
+        ct_idx = (d.I - 1) + d.I * ((a - 1) + d.J * (b - 1));
+    } else if (comp == 2) {   // a = i, b = k
+        if (a > d.I) return;
+        base = a + d.sz * b; s = d.sy; n = d.J; na = d.I;
+        bidx = (a - 1) + (long long)d.I * (b - 1);
+        varlo = in.bc[2]; varhi = in.bc[3]; flo = in.flag[2]; fhi = in.flag[3];
+        ct_idx = (a - 1) + d.I * ((d.J - 1) + d.J * (b - 1));
+    } else {   // a = i, b = j
+        if (a > d.I) return;
+        base = a + d.sy * b; s = d.sz; n = d.K; na = d.I;
+        bidx = (a - 1) + (long long)d.I * (b - 1);
+        varlo = in.bc[4]; varhi = in.bc[5]; flo = in.flag[4]; fhi = in.flag[5];
+        ct_idx = (a - 1) + d.I * ((b - 1) + d.J * (d.K - 1));
+    }
+    (void)na;
+    double *p = pred + base;
+    p[0] = flo == 1 ? p[s] : varlo[bidx];
+    const double vh = varhi[bidx];
+    p[(long long)n * s] = fhi == 1 ? p[(long long)(n - 1) * s] : vh;
+    p[(long long)(n + 1) * s] = 2.0 * vh - p[(long long)(n - 1) * s];
+    if (in.cell_type[ct_idx] == 2) p[(long long)n * s] = 0.0;
+}
+
+}  // namespace
+
+void mom_assemble(const MomDev &in, const MomParams &o, int comp, const Dims &d, const MomSys &S, bool want32,
+                  cudaStream_t st)
+{
+    const int kz = 16;
+    const dim3 grid((d.I + 31) / 32, (d.J + 3) / 4, (d.K + kz - 1) / kz);
+    k_mom_assemble<<<grid, dim3(32, 4, 1), 0, st>>>(in, o, comp, d, S, want32 ? 1 : 0, kz);
+}
+
+void mom_check_numbering(const MomDev &in, int comp, const Dims &d, unsigned long long *counts, cudaStream_t st)
+{
+    k_mom_numbering<<<interior_grid(d), interior_block(), 0, st>>>(in, comp, d, counts);
+}
+
+void mom_tail(const MomDev in[3], const Dims &d, double *pred[3], double *dp[3], cudaStream_t st, int *launches)
+{
+    for (int c = 0; c < 3; ++c) {
+        k_dp_phase<<<dim3((d.J + 2 + 127) / 128, d.K + 2), 128, 0, st>>>(dp[c], d, c + 1, 0);
+        k_dp_phase<<<dim3((d.I + 2 + 127) / 128, d.K + 2), 128, 0, st>>>(dp[c], d, c + 1, 1);
+        k_dp_phase<<<dim3((d.I + 2 + 127) / 128, d.J + 2), 128, 0, st>>>(dp[c], d, c + 1, 2);
+        *launches += 3;
+    }
+    k_pred_bc<<<dim3((d.J + 127) / 128, d.K), 128, 0, st>>>(pred[0], in[0], d, 1);
+    k_pred_bc<<<dim3((d.I + 127) / 128, d.K), 128, 0, st>>>(pred[1], in[1], d, 2);
+    k_pred_bc<<<dim3((d.I + 127) / 128, d.J), 128, 0, st>>>(pred[2], in[2], d, 3);
+    *launches += 3;
+}
+
+}  // namespace pred

@@ -1,0 +1,89 @@
+// pred_kernels.h -- device-side types and launchers of the momentum
+// predictor's implicit solves (include/scf_predictor.h).
+//
+// Layout: every per-cell array of the solver lives on the ghosted grid of
+// the component, (I+2)(J+2)(K+2) cells, i fastest, so the 7-point stencil
+// needs no bounds checks.  Rows outside the reference's loop range
+// (i = I for u, j = J for v, k = K for w), rows of solid cells and the ghost
+// layer are identity rows with a zero right-hand side: their unknowns stay
+// exactly 0 and couple to nothing.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace pred {
+
+// Staged inputs of one component (device pointers; layouts of scf_mom_in).
+struct MomDev {
+    const double *dx, *dy, *dz;
+    const double *vof, *vofl, *eta_e, *eta_n, *eta_t, *vof_old, *tvar;
+    const double *df_ew, *df_ns, *df_tb, *edf_ew, *edf_ns, *edf_tb;
+    const double *fric, *flux_div;
+    const int32_t *cell_type, *posnu;
+    const double *bc[6];
+    int flag[6];
+};
+
+struct MomParams {
+    double dt, rho_a, rho_w, fr, gx, gy, gz, g, beta_vis;
+    int flags[6];   // the component's BC%flag (1 = Neumann)
+};
+
+// The Jacobi-scaled system of one component: row c reads
+//   x(c) - sum_d m_d(c) x(nb_d(c)) = b(c),   d = W,S,B,E,N,T,
+// with m_d = a_d / aP and b = rhs / aP (0 on identity rows).
+struct MomSys {
+    double *m[6];
+    float *m32[6];   // FP32 copies (mixed precision only; may be null)
+    double *b;
+    double *dp;      // PU/PV/PW%Dp, ghosted
+};
+
+struct Dims {
+    int I, J, K;          // interior sizes of the pressure grid
+    long long sy, sz, ng; // ghosted strides and size
+};
+
+// Scalars of one BiCGStab run, in device memory.
+struct BcgScalars {
+    double rho, alpha, omega, beta;
+    double rr, bb;        // ||r||^2 and ||b||^2
+    int breakdown;        // 1: r0.v = 0 or t.t = 0 in the last step
+    int pad;
+};
+
+// Assembly (k_predictor.cu, compiled without FMA contraction).
+void mom_assemble(const MomDev &in, const MomParams &o, int comp, const Dims &d, const MomSys &S, bool want32,
+                  cudaStream_t st);
+// Checks of the row numbering: counts[0] = active cells of the loop range,
+// counts[1] = cells whose PosNu is -1 exactly when they are solid is false.
+void mom_check_numbering(const MomDev &in, int comp, const Dims &d, unsigned long long *counts, cudaStream_t st);
+// Tail of PredictingUVW: Dp ghost planes, velocity BCs, solid cells.
+void mom_tail(const MomDev in[3], const Dims &d, double *pred[3], double *dp[3], cudaStream_t st, int *launches);
+
+// BiCGStab kernels (k_bicgstab.cu).  x, r, r0, p[2], v[2], t: ghosted T arrays.
+template <typename T>
+struct BcgVecs {
+    T *x, *r, *r0, *p[2], *v[2], *t;
+};
+struct Reduce {
+    double *partials;     // 4 per block
+    int nblocks;
+};
+template <typename T>
+void bcg_iteration(const Dims &d, const T *const m[6], BcgVecs<T> &V, int &pp, bool first, Reduce &R,
+                   BcgScalars *sc, cudaStream_t st);
+// r64 = b - A x (FP64 coefficients), ||r64||^2 into sc->rr, ||b||^2 into
+// sc->bb; xnew = x (+ e when e is given: the correction of a refinement
+// round).  With r32 given, r32 = (float) r64.
+void resid64(const Dims &d, const double *const m[6], const double *b, const double *x, const float *e,
+             double *xnew, double *r64, float *r32, Reduce &R, BcgScalars *sc, cudaStream_t st);
+// Launch shape of the per-cell kernels (assembly checks).
+dim3 interior_block();
+dim3 interior_grid(const Dims &d);
+// Launch shape of the solver kernels (KZ-cell column segments); Reduce
+// holds one partial per dot per block of this grid.
+dim3 solver_block();
+dim3 solver_grid(const Dims &d);
+
+}  // namespace pred

@@ -83,6 +83,16 @@ def load_library(path: Optional[str] = None):
         C.c_int32, P(capi.ScfVtrField), C.c_int32, P(capi.ScfVtrStats)]
     L.scf_ctx_device_fields.argtypes = [C.c_void_p] + [P(C.c_void_p)] * 7
     L.scf_apply_operator_noalloc.argtypes = [C.c_int32, C.c_int32, C.c_int32] + [C.c_void_p] * 8
+    P_M = P(capi.ScfMomIn)
+    L.scf_mom_create.argtypes = [P(C.c_void_p), C.c_int32, C.c_int32, C.c_int32, C.c_int32]
+    L.scf_mom_destroy.argtypes = [C.c_void_p]
+    L.scf_mom_stage.argtypes = [C.c_void_p, P_M]
+    L.scf_mom_run.argtypes = [C.c_void_p, P(capi.ScfMomOpts), P(capi.ScfMomStats)]
+    L.scf_mom_fetch.argtypes = [C.c_void_p] + [capi.c_double_p] * 6
+    L.scf_predict_solves.argtypes = [C.c_void_p, P_M, P(capi.ScfMomOpts)] + [capi.c_double_p] * 6 + [
+        P(capi.ScfMomStats)]
+    L.scf_mom_device_fields.argtypes = [C.c_void_p] + [P(C.c_void_p)] * 6
+    L.scf_mom_last_error.argtypes = [C.c_void_p, C.c_char_p, C.c_size_t]
     _lib = L
     return L
 

@@ -13,11 +13,12 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 HEADER = os.path.join(ROOT, "include", "scf_projection.h")
 GEO_HEADER = os.path.join(ROOT, "include", "scf_geometry.h")
 OUT_HEADER = os.path.join(ROOT, "include", "scf_output.h")
+PRED_HEADER = os.path.join(ROOT, "include", "scf_predictor.h")
 
 
 def declared_functions():
     names = set()
-    for h in (HEADER, GEO_HEADER, OUT_HEADER):
+    for h in (HEADER, GEO_HEADER, OUT_HEADER, PRED_HEADER):
         src = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
         names |= set(re.findall(r"\b(scf_[a-z0-9_]+)\s*\(", src))
     return sorted(names)
@@ -34,6 +35,7 @@ def test_library_exports_every_declared_function(lib_path):
     names = declared_functions()
     assert len(names) >= 25
     assert "scf_grid_preprocess" in names and "scf_geo_create" in names and "scf_write_vtr" in names
+    assert "scf_predict_solves" in names and "scf_mom_run" in names
     for n in names:
         assert hasattr(lib, n), n
     assert lib.scf_abi_version() == 2
@@ -114,6 +116,42 @@ int main(void) {
     m = {"scf_geo_cells": capi.ScfGeoCells, "scf_geo_stats": capi.ScfGeoStats}
     lines = out.splitlines()
     assert len(lines) == 13
+    for line in lines:
+        t, f, v = line.split()
+        if f == "size":
+            assert C.sizeof(m[t]) == int(v), (t, v)
+        else:
+            assert getattr(m[t], f).offset == int(v), (t, f, v)
+
+
+def test_predictor_struct_layouts_match_header():
+    from simcoflow3d_gb300 import capi
+    prog = r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "scf_predictor.h"
+#define P(T, f) printf(#T " " #f " %zu\n", offsetof(T, f));
+int main(void) {
+  printf("scf_mom_in size %zu\n", sizeof(scf_mom_in));
+  printf("scf_mom_opts size %zu\n", sizeof(scf_mom_opts));
+  printf("scf_mom_stats size %zu\n", sizeof(scf_mom_stats));
+  P(scf_mom_in, cell_type) P(scf_mom_in, extcell) P(scf_mom_in, vof_old) P(scf_mom_in, tvar)
+  P(scf_mom_in, bc_flag) P(scf_mom_in, bc_var)
+  P(scf_mom_opts, beta_vis) P(scf_mom_opts, max_iter) P(scf_mom_opts, precision)
+  P(scf_mom_stats, rel_residual) P(scf_mom_stats, ms_assemble) P(scf_mom_stats, bytes_d2h)
+  P(scf_mom_stats, gpu_launches)
+  return 0;
+}
+'''
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "m.c")
+        open(c, "w").write(prog)
+        exe = os.path.join(d, "m")
+        subprocess.run(["gcc", "-I", os.path.dirname(PRED_HEADER), c, "-o", exe], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout
+    m = {"scf_mom_in": capi.ScfMomIn, "scf_mom_opts": capi.ScfMomOpts, "scf_mom_stats": capi.ScfMomStats}
+    lines = out.splitlines()
+    assert len(lines) == 16
     for line in lines:
         t, f, v = line.split()
         if f == "size":
