@@ -530,6 +530,112 @@ def run_geometry(args):
     return 0
 
 
+# Algorithmic bytes per cell of one BiCGStab iteration's passes in FP32
+# (s = 4): U reads r, p, v, writes p (4 s); P reads p, r0 and the six
+# couplings, writes v (9 s); S reads r, v and the couplings, writes t (9 s);
+# X reads x, r, r0, p, v, t, writes x, r (8 s).
+BCG_BYTES_F32 = {"U": 16, "P": 36, "S": 36, "X": 32}
+
+
+def run_predictor(args):
+    """The implicit solves of the momentum predictor (SetMatrix + SetVectors
+    + solve + DeltaGetValues for u, v, w, then the tail of PredictingUVW) on
+    the c2 geometry at 256^3 with dam-break viscosity (Rey = 300): device
+    time with the inputs resident (FP32 BiCGStab inside FP64 refinement, and
+    FP64 BiCGStab), the host-array call end to end, the live roofline of the
+    largest BiCGStab kernel, and the oracle on the host cores.  One JSON line."""
+    import numpy as np
+    from simcoflow3d_gb300 import capi, geometry as GM, predictor as PR
+    from simcoflow3d_gb300.projection import load_library
+    n = args.n or 256
+    g = GM.geometry_inputs("c2", n=n, seed=args.seed)
+    GM.GridPreprocess(n, n, n)(g)
+    inp = PR.momentum_inputs(g, seed=args.seed)
+    lib = load_library()
+    ps = PR.PredictSolves(n, n, n)
+    ps.stage(inp)
+    tol = 1e-10   # the reference's PCG tolerance (PredictUVW.f90:830)
+    opts = PR.default_opts(precision=capi.SCF_PREC_MIXED, rel_tol=tol)
+    for _ in range(args.warmup):
+        ps.run(opts)
+    with ClockSampler(0) as cs:
+        runs = [ps.run(opts) for _ in range(args.steps)]
+    clocks = cs.summary()
+    topts = PR.default_opts(precision=capi.SCF_PREC_MIXED, rel_tol=tol)
+    topts.kernel_timing = 1
+    timed = [ps.run(topts) for _ in range(2)]
+    o64 = PR.default_opts(precision=capi.SCF_PREC_FP64, rel_tol=tol)
+    runs64 = [ps.run(o64) for _ in range(3)]
+    # end to end through scf_predict_solves with page-locked host arrays
+    pred, dpo = PR.new_outputs(inp)
+    pinned = []
+    for arr in [a for c in inp.comps for a in list(c.arrays.values()) + c.bc_var] + pred + dpo:
+        if arr.nbytes and lib.scf_host_register(arr.ctypes.data, arr.nbytes) == 0:
+            pinned.append(arr)
+    e2e = [ps(inp, opts, pred, dpo)[2] for _ in range(max(3, args.steps // 4))]
+    unpin(lib, pinned)
+    cells = n ** 3
+    it = sum(t["timed_iterations"] for t in timed)
+    kms = {k: sum(t["ms_kernels"][q] for t in timed) / it for q, k in enumerate(("U", "P", "S", "X"))}
+    kb = {k: BCG_BYTES_F32[k] * cells for k in kms}
+    top = max(("P", "S"), key=lambda k: kms[k])
+    achieved = kb[top] / (kms[top] * 1e-3) / 1e9
+    peak, peak_kind = measured_peaks()
+    cpu = None
+    if not args.no_cpu:
+        threads = os.cpu_count() or 1
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+        from oracle import oracle as O
+        o_cpu = PR.default_opts(rel_tol=tol)
+        t0 = time.perf_counter()
+        A, b, _ = O.mom_system(inp, o_cpu, 0)
+        x, its, _ = O.csr_bicgstab(A, b, tol=tol)
+        sec = time.perf_counter() - t0
+        cpu = {"value": round(3 * sec * 1e3, 1), "unit": "ms/call", "cores": threads, "kind": "port",
+               "sample": "the u system at %d^3 (oracle SetMatrix + SetVectors, then Jacobi BiCGStab with OpenMP "
+                         "to the same tolerance, %d iterations) timed once, times 3 components" % (n, its)}
+    ms = [r["ms_total"] for r in runs]
+    line = {
+        "metric": "ms per momentum-predictor solve call at %d^3 (SetMatrix + SetVectors + solve + "
+                  "DeltaGetValues for u, v, w, Dp ghosts and predictor BCs)" % n,
+        "value": round(statistics.mean(ms), 3), "unit": "ms/call", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(statistics.mean(ms), 3), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 BiCGStab inside f64 refinement; f64 rows and Dp",
+        "data": "synthetic (c2 cut-cell geometry from GridPreprocess; viscous conductances from the apertures and "
+                "the liquid fraction, Rey = 300; cut-face terms, wall friction and fluxes seeded)",
+        "config": {"workload": "momentum systems of c2: %d^3 unit cube, solid sphere, liquid bubble, dt = 1e-3, "
+                               "Rey = 300, rel. tol 1e-10" % n,
+                   "grid": [n, n, n],
+                   "l2": "inputs larger than L2 (%.1f GB staged)" % (e2e[-1]["bytes_h2d"] / 1e9)},
+        "iterations": runs[-1]["iterations"], "rounds": runs[-1]["rounds"],
+        "rel_residual": runs[-1]["rel_residual"],
+        "ms_assemble": round(statistics.mean(r["ms_assemble"] for r in runs), 3),
+        "ms_solve": round(statistics.mean(r["ms_solve"] for r in runs), 3),
+        "ms_tail": round(statistics.mean(r["ms_tail"] for r in runs), 3),
+        "fp64": {"value": round(statistics.mean(r["ms_total"] for r in runs64), 3), "unit": "ms/call",
+                 "iterations": runs64[-1]["iterations"], "ms_solve": round(statistics.mean(r["ms_solve"] for r in runs64), 3)},
+        "e2e": {"value": round(statistics.mean(r["ms_total"] for r in e2e), 3), "unit": "ms/call",
+                "h2d_bytes_per_step": int(e2e[-1]["bytes_h2d"]), "d2h_bytes_per_step": int(e2e[-1]["bytes_d2h"]),
+                "ms_h2d": round(statistics.mean(r["ms_h2d"] for r in e2e), 3),
+                "ms_d2h": round(statistics.mean(r["ms_d2h"] for r in e2e), 3)},
+        "roofline": {"bound": "hbm",
+                     "kernel": {"P": "k_bcg_p<float> (v = A p, r0.v)", "S": "k_bcg_s<float> (t = A s, t.s, t.t)"}[top]
+                               + ", 16-cell column segments",
+                     "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "peak_kind": peak_kind, "bytes_per_launch": kb[top],
+                     "ms_per_launch": round(kms[top], 5), "launches_timed": it,
+                     "passes": {k: {"ms_per_launch": round(kms[k], 5), "bytes_per_launch": kb[k],
+                                    "GB/s": round(kb[k] / (kms[k] * 1e-3) / 1e9, 1)} for k in kms},
+                     "timing": "CUDA events around each stencil kernel of the BiCGStab iterations of 2 calls",
+                     "traffic": None},
+        "clocks": clocks,
+        "gpu_launches": sum(r["gpu_launches"] for r in runs),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_output(args):
     """PrintResultVTK's snapshot of a c2 projection (p, u, v, w, phiL, phi,
     vofL, vof at 256^3) written by scf_write_vtr from the projection
@@ -607,7 +713,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c2",
                     help="c0..c4; geometry (the cut-cell geometry preprocessing of the c2 geometry); output "
-                         "(a PrintResultVTK snapshot of a c2 projection)")
+                         "(a PrintResultVTK snapshot of a c2 projection); predictor (the momentum predictor's "
+                         "implicit solves on the c2 geometry)")
     ap.add_argument("--tol", type=float, default=1e-8)
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--n", type=int, default=None, help="smaller grid (profiling captures only)")
@@ -628,6 +735,8 @@ def main():
         return run_geometry(args)
     if args.config == "output":
         return run_output(args)
+    if args.config == "predictor":
+        return run_predictor(args)
     return run_ours(args)
 
 

@@ -69,6 +69,8 @@ typedef struct scf_mom_opts {
     double  rel_tol;                /* stopping test, scaled FP64 residual             */
     int32_t max_iter;               /* BiCGStab iterations (all refinement rounds)     */
     int32_t precision;              /* SCF_PREC_FP64 or SCF_PREC_MIXED                 */
+    int32_t kernel_timing;          /* 1: CUDA events around each BiCGStab stencil
+                                       kernel (stats.ms_kernels)                       */
 } scf_mom_opts;
 
 typedef struct scf_mom_stats {
@@ -82,6 +84,11 @@ typedef struct scf_mom_stats {
     double  ms_h2d, ms_d2h, ms_total;
     int64_t bytes_h2d, bytes_d2h;
     int32_t gpu_launches;
+    /* with kernel_timing: summed device time of the four passes of the
+     * BiCGStab iterations (U: p update; P: v = A p; S: t = A s; X: x and r),
+     * and how many iterations they cover                                    */
+    int32_t timed_iterations;
+    double  ms_kernels[4];
 } scf_mom_stats;
 
 typedef struct scf_mom_ctx scf_mom_ctx;

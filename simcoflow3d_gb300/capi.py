@@ -173,6 +173,7 @@ class ScfMomOpts(C.Structure):
         ("dt", C.c_double), ("rho_a_ref", C.c_double), ("rho_w_ref", C.c_double), ("fr", C.c_double),
         ("gx", C.c_double), ("gy", C.c_double), ("gz", C.c_double), ("g", C.c_double),
         ("beta_vis", C.c_double), ("rel_tol", C.c_double), ("max_iter", C.c_int32), ("precision", C.c_int32),
+        ("kernel_timing", C.c_int32),
     ]
 
 
@@ -183,6 +184,7 @@ class ScfMomStats(C.Structure):
         ("ms_assemble", C.c_double), ("ms_solve", C.c_double), ("ms_tail", C.c_double),
         ("ms_h2d", C.c_double), ("ms_d2h", C.c_double), ("ms_total", C.c_double),
         ("bytes_h2d", C.c_int64), ("bytes_d2h", C.c_int64), ("gpu_launches", C.c_int32),
+        ("timed_iterations", C.c_int32), ("ms_kernels", C.c_double * 4),
     ]
 
     def as_dict(self):

@@ -2,12 +2,12 @@
 // 1992) on the Jacobi-scaled momentum systems of the predictor, templated on
 // the vector type (FP64, or FP32 inside FP64 iterative refinement).
 //
-// One iteration is three stencil passes and three one-block reductions:
-//   P: p = r + beta (p - omega v), formed at the 7 points it is needed
-//      (the first step of a run takes p = r); v = A p; r0.v
+// One iteration is four passes and three one-block reductions:
+//   U: p = r + beta (p - omega v) in place (the first step of a run takes
+//      p = r)
+//   P: v = A p; r0.v
 //   S: s = r - alpha v, formed at the 7 points; t = A s; t.s, t.t
 //   X: s again, x += alpha p + omega s, r = s - omega t; r0.r, r.r
-// p and v are double-buffered (P reads the old ones at the neighbours);
 // s is never stored.  Each thread marches KZ cells of one (i, j) column and
 // keeps its share of the dot products in registers, so a block writes one
 // partial sum per dot for 128 x KZ cells; one block then sums the partials
@@ -73,21 +73,31 @@ __device__ __forceinline__ T apply_stencil(const M6<T> &m, const Dims &d, long l
 }
 
 template <typename T>
-__global__ void __launch_bounds__(NT) k_bcg_p(Dims d, M6<T> m, const T *__restrict__ r, const T *__restrict__ r0,
-                                              const T *__restrict__ pold, const T *__restrict__ vold,
-                                              T *__restrict__ pnew, T *__restrict__ vnew, const BcgScalars *sc,
-                                              int first, double *partials)
+__global__ void __launch_bounds__(NT) k_bcg_u(Dims d, const T *__restrict__ r, T *__restrict__ p,
+                                              const T *__restrict__ v, const BcgScalars *sc, int first)
+{
+    COLUMN
+    if (!in) return;
+    const T beta = (T)sc->beta, omega = (T)sc->omega;
+    long long c = c0;
+    if (first)
+        for (int k = k0; k <= k1; ++k, c += d.sz) p[c] = r[c];
+    else
+        for (int k = k0; k <= k1; ++k, c += d.sz) p[c] = r[c] + beta * (p[c] - omega * v[c]);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NT) k_bcg_p(Dims d, M6<T> m, const T *__restrict__ p, const T *__restrict__ r0,
+                                              T *__restrict__ v, double *partials)
 {
     COLUMN
     T acc[1] = {T(0)};
     if (in) {
-        const T beta = first ? T(0) : (T)sc->beta, omega = first ? T(0) : (T)sc->omega;
-        auto P = [&](long long q) { return first ? r[q] : r[q] + beta * (pold[q] - omega * vold[q]); };
+        auto P = [&](long long q) { return p[q]; };
         long long c = c0;
         for (int k = k0; k <= k1; ++k, c += d.sz) {
             const T y = apply_stencil(m, d, c, P);
-            pnew[c] = P(c);
-            vnew[c] = y;
+            v[c] = y;
             acc[0] += r0[c] * y;
         }
     }
@@ -260,18 +270,26 @@ dim3 solver_grid(const Dims &d) { return dim3((d.I + 31) / 32, (d.J + 3) / 4, (d
 
 template <typename T>
 void bcg_iteration(const Dims &d, const T *const m[6], BcgVecs<T> &V, int &pp, bool first, Reduce &R,
-                   BcgScalars *sc, cudaStream_t st)
+                   BcgScalars *sc, cudaStream_t st, cudaEvent_t *ev)
 {
     const dim3 g = solver_grid(d), b = solver_block();
     const M6<T> M = m6(m);
-    const int q = pp ^ 1;
-    k_bcg_p<T><<<g, b, 0, st>>>(d, M, V.r, V.r0, V.p[pp], V.v[pp], V.p[q], V.v[q], sc, first ? 1 : 0, R.partials);
+    (void)pp;
+    T *p = V.p[0], *v = V.v[0];
+    if (ev) cudaEventRecord(ev[0], st);
+    k_bcg_u<T><<<g, b, 0, st>>>(d, V.r, p, v, sc, first ? 1 : 0);
+    if (ev) cudaEventRecord(ev[1], st);
+    k_bcg_p<T><<<g, b, 0, st>>>(d, M, p, V.r0, v, R.partials);
+    if (ev) cudaEventRecord(ev[2], st);
     k_red_alpha<<<1, 1024, 0, st>>>(R.partials, R.nblocks, sc);
-    k_bcg_s<T><<<g, b, 0, st>>>(d, M, V.r, V.v[q], V.t, sc, R.partials);
+    if (ev) cudaEventRecord(ev[3], st);
+    k_bcg_s<T><<<g, b, 0, st>>>(d, M, V.r, v, V.t, sc, R.partials);
+    if (ev) cudaEventRecord(ev[4], st);
     k_red_omega<<<1, 1024, 0, st>>>(R.partials, R.nblocks, sc);
-    k_bcg_x<T><<<g, b, 0, st>>>(d, V.x, V.r, V.r0, V.p[q], V.v[q], V.t, sc, R.partials);
+    if (ev) cudaEventRecord(ev[5], st);
+    k_bcg_x<T><<<g, b, 0, st>>>(d, V.x, V.r, V.r0, p, v, V.t, sc, R.partials);
+    if (ev) cudaEventRecord(ev[6], st);
     k_red_rho<<<1, 1024, 0, st>>>(R.partials, R.nblocks, sc);
-    pp = q;
 }
 
 void resid64(const Dims &d, const double *const m[6], const double *b, const double *x, const float *e,
@@ -282,8 +300,8 @@ void resid64(const Dims &d, const double *const m[6], const double *b, const dou
 }
 
 template void bcg_iteration<double>(const Dims &, const double *const[6], BcgVecs<double> &, int &, bool, Reduce &,
-                                    BcgScalars *, cudaStream_t);
+                                    BcgScalars *, cudaStream_t, cudaEvent_t *);
 template void bcg_iteration<float>(const Dims &, const float *const[6], BcgVecs<float> &, int &, bool, Reduce &,
-                                   BcgScalars *, cudaStream_t);
+                                   BcgScalars *, cudaStream_t, cudaEvent_t *);
 
 }  // namespace pred

@@ -20,6 +20,7 @@ struct scf_mom_ctx {
     int device = 0;
     cudaStream_t st = nullptr;
     cudaEvent_t ev[4] = {};
+    cudaEvent_t kev[7] = {};   // around the BiCGStab passes (kernel_timing)
     std::vector<void *> mem;
     struct Comp {
         double *dx, *dy, *dz, *vof, *vofl, *eta_e, *eta_n, *eta_t, *vof_old, *tvar;
@@ -146,7 +147,21 @@ struct SolveOut {
     double rel = 0.0;
     const double *x = nullptr;
     int launches = 0;
+    int timed = 0;
+    double ms_k[4] = {0.0, 0.0, 0.0, 0.0};
 };
+
+float elapsed(cudaEvent_t a, cudaEvent_t b);
+
+// After a synchronised iteration: the three stencil kernels' times.
+void add_kernel_times(scf_mom_ctx *ctx, SolveOut &out)
+{
+    out.ms_k[0] += elapsed(ctx->kev[0], ctx->kev[1]);
+    out.ms_k[1] += elapsed(ctx->kev[1], ctx->kev[2]);
+    out.ms_k[2] += elapsed(ctx->kev[3], ctx->kev[4]);
+    out.ms_k[3] += elapsed(ctx->kev[5], ctx->kev[6]);
+    ++out.timed;
+}
 
 // FP64 BiCGStab on the scaled system, restarted from the true residual
 // when the recursive one says converged but the true one does not, or on a
@@ -174,11 +189,12 @@ int solve_fp64(scf_mom_ctx *ctx, const scf_mom_opts &o, SolveOut &out)
     bool first = true;
     int pp = 0;
     while (out.iterations < o.max_iter) {
-        bcg_iteration<double>(d, m, V, pp, first, ctx->R, ctx->sc, ctx->st);
+        bcg_iteration<double>(d, m, V, pp, first, ctx->R, ctx->sc, ctx->st, o.kernel_timing ? ctx->kev : nullptr);
         out.launches += 6;
         ++out.iterations;
         first = false;
         RS();
+        if (o.kernel_timing) add_kernel_times(ctx, out);
         rr = ctx->sc_host->rr;
         if (!std::isfinite(rr)) {
             mom_err(ctx, "non-finite residual after %d iterations", out.iterations);
@@ -230,11 +246,12 @@ int solve_mixed(scf_mom_ctx *ctx, const scf_mom_opts &o, SolveOut &out)
         bool first = true;
         int pp = 0;
         while (out.iterations < o.max_iter) {
-            bcg_iteration<float>(d, m32, V, pp, first, ctx->R, ctx->sc, ctx->st);
+            bcg_iteration<float>(d, m32, V, pp, first, ctx->R, ctx->sc, ctx->st, o.kernel_timing ? ctx->kev : nullptr);
             out.launches += 6;
             ++out.iterations;
             first = false;
             RS();
+            if (o.kernel_timing) add_kernel_times(ctx, out);
             const double r2 = ctx->sc_host->rr;
             if (!std::isfinite(r2)) {
                 mom_err(ctx, "non-finite FP32 residual after %d iterations", out.iterations);
@@ -288,6 +305,8 @@ extern "C" int scf_mom_create(scf_mom_ctx **out, int32_t imax, int32_t jmax, int
     if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) return fail(SCF_ERR_CUDA);
     for (auto &e : ctx->ev)
         if (cudaEventCreate(&e) != cudaSuccess) return fail(SCF_ERR_CUDA);
+    for (auto &e : ctx->kev)
+        if (cudaEventCreate(&e) != cudaSuccess) return fail(SCF_ERR_CUDA);
     const size_t n = (size_t)imax * jmax * kmax, ng = (size_t)d.ng;
     const size_t few = (size_t)(imax + 2) * jmax * kmax, fns = (size_t)imax * (jmax + 2) * kmax,
                  ftb = (size_t)imax * jmax * (kmax + 2);
@@ -337,6 +356,8 @@ extern "C" int scf_mom_destroy(scf_mom_ctx *ctx)
     if (ctx->sc_host) cudaFreeHost(ctx->sc_host);
     if (ctx->counts_host) cudaFreeHost(ctx->counts_host);
     for (auto e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    for (auto e : ctx->kev)
         if (e) cudaEventDestroy(e);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
@@ -434,6 +455,8 @@ extern "C" int scf_mom_run(scf_mom_ctx *ctx, const scf_mom_opts *opts, scf_mom_s
         s.converged[c] = so.converged;
         s.rel_residual[c] = so.rel;
         s.gpu_launches += so.launches;
+        s.timed_iterations += so.timed;
+        for (int q = 0; q < 4; ++q) s.ms_kernels[q] += so.ms_k[q];
     }
     MK(cudaEventRecord(ctx->ev[0], ctx->st));
     int tl = 0;

@@ -61,7 +61,8 @@ void mom_check_numbering(const MomDev &in, int comp, const Dims &d, unsigned lon
 // Tail of PredictingUVW: Dp ghost planes, velocity BCs, solid cells.
 void mom_tail(const MomDev in[3], const Dims &d, double *pred[3], double *dp[3], cudaStream_t st, int *launches);
 
-// BiCGStab kernels (k_bicgstab.cu).  x, r, r0, p[2], v[2], t: ghosted T arrays.
+// BiCGStab kernels (k_bicgstab.cu).  x, r, r0, p, v, t: ghosted T arrays
+// (p[0] and v[0] are used; p[1], v[1] are spare).
 template <typename T>
 struct BcgVecs {
     T *x, *r, *r0, *p[2], *v[2], *t;
@@ -70,9 +71,10 @@ struct Reduce {
     double *partials;     // 4 per block
     int nblocks;
 };
+// ev (optional, 7 events): recorded around the four passes U, P, S, X.
 template <typename T>
 void bcg_iteration(const Dims &d, const T *const m[6], BcgVecs<T> &V, int &pp, bool first, Reduce &R,
-                   BcgScalars *sc, cudaStream_t st);
+                   BcgScalars *sc, cudaStream_t st, cudaEvent_t *ev = nullptr);
 // r64 = b - A x (FP64 coefficients), ||r64||^2 into sc->rr, ||b||^2 into
 // sc->bb; xnew = x (+ e when e is given: the correction of a refinement
 // round).  With r32 given, r32 = (float) r64.

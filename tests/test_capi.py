@@ -139,7 +139,7 @@ int main(void) {
   P(scf_mom_in, bc_flag) P(scf_mom_in, bc_var)
   P(scf_mom_opts, beta_vis) P(scf_mom_opts, max_iter) P(scf_mom_opts, precision)
   P(scf_mom_stats, rel_residual) P(scf_mom_stats, ms_assemble) P(scf_mom_stats, bytes_d2h)
-  P(scf_mom_stats, gpu_launches)
+  P(scf_mom_stats, gpu_launches) P(scf_mom_stats, ms_kernels) P(scf_mom_opts, kernel_timing)
   return 0;
 }
 '''
@@ -151,7 +151,7 @@ int main(void) {
         out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout
     m = {"scf_mom_in": capi.ScfMomIn, "scf_mom_opts": capi.ScfMomOpts, "scf_mom_stats": capi.ScfMomStats}
     lines = out.splitlines()
-    assert len(lines) == 16
+    assert len(lines) == 18
     for line in lines:
         t, f, v = line.split()
         if f == "size":
