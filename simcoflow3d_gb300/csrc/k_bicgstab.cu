@@ -148,7 +148,8 @@ __global__ void __launch_bounds__(NT) k_bcg_x(Dims d, T *__restrict__ x, T *__re
 }
 
 // xc = x (+ e); r = b - A xc; ||r||^2 (FP64), ||r_T||^2 of the stored
-// vector, ||b||^2.
+// vector, ||b||^2.  x = NULL stands for x = 0: then r = b without the
+// stencil pass.
 __global__ void __launch_bounds__(NT) k_resid64(Dims d, M6<double> m, const double *__restrict__ b,
                                                 const double *__restrict__ x, const float *__restrict__ e,
                                                 double *__restrict__ xnew, double *__restrict__ r64,
@@ -160,8 +161,8 @@ __global__ void __launch_bounds__(NT) k_resid64(Dims d, M6<double> m, const doub
         auto X = [&](long long q) { return e ? x[q] + (double)e[q] : x[q]; };
         long long c = c0;
         for (int k = k0; k <= k1; ++k, c += d.sz) {
-            const double xc = X(c);
-            const double r = b[c] - apply_stencil(m, d, c, X);
+            const double xc = x ? X(c) : 0.0;
+            const double r = x ? b[c] - apply_stencil(m, d, c, X) : b[c];
             if (xnew) xnew[c] = xc;
             double rt = r;
             if (r64) r64[c] = r;

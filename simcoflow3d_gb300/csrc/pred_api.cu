@@ -173,7 +173,7 @@ int solve_fp64(scf_mom_ctx *ctx, const scf_mom_opts &o, SolveOut &out)
     const double *const *m = ctx->m;
     const size_t bytes = (size_t)d.ng * sizeof(double);
     MK(cudaMemsetAsync(V.x, 0, bytes, ctx->st));
-    resid64(d, m, ctx->b, V.x, nullptr, nullptr, V.r, nullptr, ctx->R, ctx->sc, ctx->st);
+    resid64(d, m, ctx->b, nullptr, nullptr, nullptr, V.r, nullptr, ctx->R, ctx->sc, ctx->st);
     MK(cudaMemcpyAsync(V.r0, V.r, bytes, cudaMemcpyDeviceToDevice, ctx->st));
     out.launches += 2;
     RS();
@@ -227,7 +227,7 @@ int solve_mixed(scf_mom_ctx *ctx, const scf_mom_opts &o, SolveOut &out)
     double *xa = ctx->V64.x, *xb = ctx->x64b;
     const size_t bytes32 = (size_t)d.ng * sizeof(float);
     MK(cudaMemsetAsync(xa, 0, (size_t)d.ng * sizeof(double), ctx->st));
-    resid64(d, m, ctx->b, xa, nullptr, nullptr, nullptr, V.r, ctx->R, ctx->sc, ctx->st);
+    resid64(d, m, ctx->b, nullptr, nullptr, nullptr, nullptr, V.r, ctx->R, ctx->sc, ctx->st);
     out.launches += 2;
     RS();
     const double bb = ctx->sc_host->bb, target = o.rel_tol * o.rel_tol * bb;

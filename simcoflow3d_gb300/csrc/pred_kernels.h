@@ -77,7 +77,7 @@ void bcg_iteration(const Dims &d, const T *const m[6], BcgVecs<T> &V, int &pp, b
                    BcgScalars *sc, cudaStream_t st, cudaEvent_t *ev = nullptr);
 // r64 = b - A x (FP64 coefficients), ||r64||^2 into sc->rr, ||b||^2 into
 // sc->bb; xnew = x (+ e when e is given: the correction of a refinement
-// round).  With r32 given, r32 = (float) r64.
+// round).  With r32 given, r32 = (float) r64.  x = NULL: x = 0 (r = b).
 void resid64(const Dims &d, const double *const m[6], const double *b, const double *x, const float *e,
              double *xnew, double *r64, float *r32, Reduce &R, BcgScalars *sc, cudaStream_t st);
 // Launch shape of the per-cell kernels (assembly checks).
