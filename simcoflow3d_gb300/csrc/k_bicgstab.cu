@@ -147,34 +147,40 @@ __global__ void __launch_bounds__(NT) k_bcg_x(Dims d, T *__restrict__ x, T *__re
     block_partials<2, T>(acc, partials);
 }
 
-// xc = x (+ e); r = b - A xc; ||r||^2 (FP64), ||r_T||^2 of the stored
-// vector, ||b||^2.  x = NULL stands for x = 0: then r = b without the
-// stencil pass.
+// x += e (the FP32 correction of a refinement round), pointwise.
+__global__ void __launch_bounds__(NT) k_xadd(Dims d, double *__restrict__ x, const float *__restrict__ e)
+{
+    COLUMN
+    if (!in) return;
+    long long c = c0;
+    for (int k = k0; k <= k1; ++k, c += d.sz) x[c] = x[c] + (double)e[c];
+}
+
+// r = b - A x in FP64 (x = NULL stands for x = 0: r = b without the stencil
+// pass); ||r||^2, ||r_T||^2 of the stored vector (r32 when given, summed in
+// FP32) and, with want_bb, ||b||^2.
 __global__ void __launch_bounds__(NT) k_resid64(Dims d, M6<double> m, const double *__restrict__ b,
-                                                const double *__restrict__ x, const float *__restrict__ e,
-                                                double *__restrict__ xnew, double *__restrict__ r64,
-                                                float *__restrict__ r32, double *partials)
+                                                const double *__restrict__ x, double *__restrict__ r64,
+                                                float *__restrict__ r32, int want_bb, double *partials)
 {
     COLUMN
     double acc[3] = {0.0, 0.0, 0.0};
     if (in) {
-        auto X = [&](long long q) { return e ? x[q] + (double)e[q] : x[q]; };
+        auto X = [&](long long q) { return x[q]; };
+        float rt2 = 0.f;
         long long c = c0;
         for (int k = k0; k <= k1; ++k, c += d.sz) {
-            const double xc = x ? X(c) : 0.0;
             const double r = x ? b[c] - apply_stencil(m, d, c, X) : b[c];
-            if (xnew) xnew[c] = xc;
-            double rt = r;
             if (r64) r64[c] = r;
             if (r32) {
                 const float f = (float)r;
                 r32[c] = f;
-                rt = (double)f;
+                rt2 += f * f;
             }
             acc[0] += r * r;
-            acc[1] += rt * rt;
-            acc[2] += b[c] * b[c];
+            if (want_bb) acc[2] += b[c] * b[c];
         }
+        acc[1] = r32 ? (double)rt2 : acc[0];
     }
     block_partials<3, double>(acc, partials);
 }
@@ -243,14 +249,14 @@ __global__ void __launch_bounds__(1024) k_red_rho(const double *partials, int nb
 }
 
 // after a residual: a fresh start (p = r on the next P)
-__global__ void __launch_bounds__(1024) k_red_resid(const double *partials, int nb, BcgScalars *sc)
+__global__ void __launch_bounds__(1024) k_red_resid(const double *partials, int nb, BcgScalars *sc, int want_bb)
 {
     double s[3];
     sum_partials<3>(partials, nb, s);
     if (threadIdx.x == 0) {
         sc->rr = s[0];
         sc->rho = s[1];
-        sc->bb = s[2];
+        if (want_bb) sc->bb = s[2];
         sc->alpha = 1.0;
         sc->omega = 1.0;
         sc->beta = 0.0;
@@ -293,11 +299,16 @@ void bcg_iteration(const Dims &d, const T *const m[6], BcgVecs<T> &V, int &pp, b
     k_red_rho<<<1, 1024, 0, st>>>(R.partials, R.nblocks, sc);
 }
 
-void resid64(const Dims &d, const double *const m[6], const double *b, const double *x, const float *e,
-             double *xnew, double *r64, float *r32, Reduce &R, BcgScalars *sc, cudaStream_t st)
+void resid64(const Dims &d, const double *const m[6], const double *b, const double *x, double *r64, float *r32,
+             bool want_bb, Reduce &R, BcgScalars *sc, cudaStream_t st)
 {
-    k_resid64<<<solver_grid(d), solver_block(), 0, st>>>(d, m6(m), b, x, e, xnew, r64, r32, R.partials);
-    k_red_resid<<<1, 1024, 0, st>>>(R.partials, R.nblocks, sc);
+    k_resid64<<<solver_grid(d), solver_block(), 0, st>>>(d, m6(m), b, x, r64, r32, want_bb ? 1 : 0, R.partials);
+    k_red_resid<<<1, 1024, 0, st>>>(R.partials, R.nblocks, sc, want_bb ? 1 : 0);
+}
+
+void xadd(const Dims &d, double *x, const float *e, cudaStream_t st)
+{
+    k_xadd<<<solver_grid(d), solver_block(), 0, st>>>(d, x, e);
 }
 
 template void bcg_iteration<double>(const Dims &, const double *const[6], BcgVecs<double> &, int &, bool, Reduce &,

@@ -106,14 +106,6 @@ __device__ __noinline__ void mom_row(const RowKey &K, const MomParams &o, int co
     M.m[3] = aE * inv; M.m[4] = aN * inv; M.m[5] = aT * inv;
 }
 
-__device__ __forceinline__ bool same_key(const RowKey &a, const RowKey &b)
-{
-    bool eq = a.kb == b.kb;
-#pragma unroll
-    for (int q = 0; q < 24; ++q) eq = eq && __double_as_longlong(a.v[q]) == __double_as_longlong(b.v[q]);
-    return eq;
-}
-
 // One thread per (i, j) column, marching KZ cells along k.  Active cells of
 // the loop range (i <= I-iu, j <= J-iv, k <= K-iw, Cell_Type /= 2) get the
 // row of SetMatrix scaled by 1/aP and the rhs of SetVectors (1211-1251),
@@ -121,10 +113,17 @@ __device__ __forceinline__ bool same_key(const RowKey &a, const RowKey &b)
 // vof*dV/(aP - the neighbour coefficients) on its active cells (913, 1040,
 // 1226-1237).  Consecutive rows of a column with bit-identical keys (most
 // rows away from the interface and the solid) reuse the previous row's
-// memo, so the FP64 divisions run only where the inputs change.
-__global__ void __launch_bounds__(128) k_mom_assemble(MomDev in, MomParams o, int comp, Dims d, MomSys S,
-                                                      int want32, int kz)
+// memo, so the FP64 divisions run only where the inputs change.  The key
+// being compared stays in registers, the previous one in shared memory (a
+// slot per thread), the memo in registers; only a miss goes through local
+// memory into mom_row.
+constexpr int ASM_NT = 128;
+__global__ void __launch_bounds__(ASM_NT, 4) k_mom_assemble(MomDev in, MomParams o, int comp, Dims d, MomSys S,
+                                                         int want32, int kz)
 {
+    __shared__ double sprev[24][ASM_NT];
+    __shared__ int skb[ASM_NT];
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
     const int k0 = blockIdx.z * kz + 1, k1 = min(k0 + kz - 1, d.K);
@@ -135,20 +134,23 @@ __global__ void __launch_bounds__(128) k_mom_assemble(MomDev in, MomParams o, in
     const int ibase = (i == 1 ? 1 : 0) | (i == ie ? 2 : 0) | (j == 1 ? 4 : 0) | (j == je ? 8 : 0);
     const long long sns = d.I, stb = (long long)d.I * d.J;
     const long long px = ie, pxy = (long long)ie * je;
-    RowKey key, prev;
-    RowMemo M;
+    double mm[6], minv = 0.0, mdp = 0.0, mg = 0.0, mcb[6];
+    float mf[6];   // the FP32 copies of mm
+#pragma unroll
+    for (int q = 0; q < 6; ++q) { mm[q] = mcb[q] = 0.0; mf[q] = 0.f; }
     bool have = false;
     for (int k = k0; k <= k1; ++k) {
         const long long c = gidx(d, i, j, k);
         const long long n = (i - 1) + (long long)d.I * ((j - 1) + (long long)d.J * (k - 1));
         double mw = 0.0, ms = 0.0, mb = 0.0, me = 0.0, mn = 0.0, mt = 0.0, bh = 0.0;
+        float fw = 0.f, fs = 0.f, fb = 0.f, fe = 0.f, fn = 0.f, ft = 0.f;
         if (col_in && k <= ke) {
             double dpv = 0.0;
             if (in.cell_type[n] != 2) {
                 const long long few = i + (long long)(d.I + 2) * ((j - 1) + (long long)d.J * (k - 1));
                 const long long fns = (i - 1) + (long long)d.I * (j + (long long)(d.J + 2) * (k - 1));
                 const long long ftb = (i - 1) + (long long)d.I * ((j - 1) + (long long)d.J * k);
-                double *v = key.v;
+                double v[24];
                 v[KDFE] = in.df_ew[few + 1]; v[KDFW] = in.df_ew[few];
                 v[KDFN] = in.df_ns[fns + sns]; v[KDFS] = in.df_ns[fns];
                 v[KDFT] = in.df_tb[ftb + stb]; v[KDFB] = in.df_tb[ftb];
@@ -161,39 +163,52 @@ __global__ void __launch_bounds__(128) k_mom_assemble(MomDev in, MomParams o, in
                 v[KVOF] = in.vof[c]; v[KVOFL] = in.vofl[c];
                 v[KDX] = in.dx[n]; v[KDY] = in.dy[n]; v[KDZ] = in.dz[n];
                 v[KFRIC] = in.fric[n];
-                key.kb = ibase | (k == 1 ? 16 : 0) | (k == ke ? 32 : 0);
-                if (!(have && same_key(key, prev))) {
-                    mom_row(key, o, comp, key.kb, M);
-                    prev = key;
+                const int kb = ibase | (k == 1 ? 16 : 0) | (k == ke ? 32 : 0);
+                bool hit = have && skb[tid] == kb;
+#pragma unroll
+                for (int q = 0; q < 24; ++q)
+                    hit &= __double_as_longlong(v[q]) == __double_as_longlong(sprev[q][tid]);
+                if (!hit) {
+                    RowKey key;
+                    RowMemo M;
+#pragma unroll
+                    for (int q = 0; q < 24; ++q) key.v[q] = v[q];
+                    key.kb = kb;
+                    mom_row(key, o, comp, kb, M);
+#pragma unroll
+                    for (int q = 0; q < 24; ++q) sprev[q][tid] = v[q];
+                    skb[tid] = kb;
+#pragma unroll
+                    for (int q = 0; q < 6; ++q) { mm[q] = M.m[q]; mcb[q] = M.cb[q]; mf[q] = (float)M.m[q]; }
+                    minv = M.inv; mdp = M.dp; mg = M.gterm;
                     have = true;
                 }
-                dpv = M.dp;
+                dpv = mdp;
                 // SetVectors: u.vof.dV/dt - u.dV.dvof/dt + gravity - flux +
                 // boundary values, in the reference's order
-                const double vof = key.v[KVOF], dx = key.v[KDX], dy = key.v[KDY], dz = key.v[KDZ];
+                const double vof = v[KVOF], dx = v[KDX], dy = v[KDY], dz = v[KDZ];
                 const double U = in.tvar[c] + 0.0;
                 const double dv = vof - in.vof_old[c];
                 const double t1 = U * vof * dx * dy * dz / o.dt;
                 const double t2 = dv == 0.0 ? U * dv * dx * dy * dz : U * dv * dx * dy * dz / o.dt;
-                double rhs = t1 - t2 + M.gterm;
+                double rhs = t1 - t2 + mg;
                 rhs = rhs - in.flux_div[n];
-                const int kb = key.kb;
-                if (kb & 1) rhs = rhs + M.cb[0] * in.bc[0][(j - 1) + (long long)d.J * (k - 1)];
-                if (kb & 2) rhs = rhs + M.cb[1] * in.bc[1][(j - 1) + (long long)d.J * (k - 1)];
-                if (kb & 4) rhs = rhs + M.cb[2] * in.bc[2][(i - 1) + (long long)d.I * (k - 1)];
-                if (kb & 8) rhs = rhs + M.cb[3] * in.bc[3][(i - 1) + (long long)d.I * (k - 1)];
-                if (kb & 16) rhs = rhs + M.cb[4] * in.bc[4][(i - 1) + (long long)d.I * (j - 1)];
-                if (kb & 32) rhs = rhs + M.cb[5] * in.bc[5][(i - 1) + (long long)d.I * (j - 1)];
+                if (kb & 1) rhs = rhs + mcb[0] * in.bc[0][(j - 1) + (long long)d.J * (k - 1)];
+                if (kb & 2) rhs = rhs + mcb[1] * in.bc[1][(j - 1) + (long long)d.J * (k - 1)];
+                if (kb & 4) rhs = rhs + mcb[2] * in.bc[2][(i - 1) + (long long)d.I * (k - 1)];
+                if (kb & 8) rhs = rhs + mcb[3] * in.bc[3][(i - 1) + (long long)d.I * (k - 1)];
+                if (kb & 16) rhs = rhs + mcb[4] * in.bc[4][(i - 1) + (long long)d.I * (j - 1)];
+                if (kb & 32) rhs = rhs + mcb[5] * in.bc[5][(i - 1) + (long long)d.I * (j - 1)];
                 // a neighbour couples when it is inside the loop range and
                 // numbered (PosNu /= -1, 1044-1097)
                 const long long pn = (i - 1) + px * (j - 1) + pxy * (k - 1);
-                if (i > 1 && in.posnu[pn - 1] != -1) mw = M.m[0];
-                if (j > 1 && in.posnu[pn - px] != -1) ms = M.m[1];
-                if (k > 1 && in.posnu[pn - pxy] != -1) mb = M.m[2];
-                if (i < ie && in.posnu[pn + 1] != -1) me = M.m[3];
-                if (j < je && in.posnu[pn + px] != -1) mn = M.m[4];
-                if (k < ke && in.posnu[pn + pxy] != -1) mt = M.m[5];
-                bh = rhs * M.inv;
+                if (i > 1 && in.posnu[pn - 1] != -1) { mw = mm[0]; fw = mf[0]; }
+                if (j > 1 && in.posnu[pn - px] != -1) { ms = mm[1]; fs = mf[1]; }
+                if (k > 1 && in.posnu[pn - pxy] != -1) { mb = mm[2]; fb = mf[2]; }
+                if (i < ie && in.posnu[pn + 1] != -1) { me = mm[3]; fe = mf[3]; }
+                if (j < je && in.posnu[pn + px] != -1) { mn = mm[4]; fn = mf[4]; }
+                if (k < ke && in.posnu[pn + pxy] != -1) { mt = mm[5]; ft = mf[5]; }
+                bh = rhs * minv;
             }
             S.dp[c] = dpv;
         }
@@ -201,11 +216,15 @@ __global__ void __launch_bounds__(128) k_mom_assemble(MomDev in, MomParams o, in
         S.m[3][c] = me; S.m[4][c] = mn; S.m[5][c] = mt;
         S.b[c] = bh;
         if (want32) {
-            S.m32[0][c] = (float)mw; S.m32[1][c] = (float)ms; S.m32[2][c] = (float)mb;
-            S.m32[3][c] = (float)me; S.m32[4][c] = (float)mn; S.m32[5][c] = (float)mt;
+            S.m32[0][c] = fw; S.m32[1][c] = fs; S.m32[2][c] = fb;
+            S.m32[3][c] = fe; S.m32[4][c] = fn; S.m32[5][c] = ft;
         }
     }
 }
+
+}  // namespace
+
+namespace {
 
 // counts[0]: active cells of the loop range; counts[1]: cells of the loop
 // range whose PosNu is -1 when active, or not -1 when solid.

@@ -36,7 +36,6 @@ struct scf_mom_ctx {
     double *pred[3] = {}, *dp[3] = {};
     BcgVecs<double> V64{};
     BcgVecs<float> V32{};
-    double *x64b = nullptr;
     Reduce R{};
     BcgScalars *sc = nullptr, *sc_host = nullptr;
     unsigned long long *counts = nullptr, *counts_host = nullptr;
@@ -173,7 +172,7 @@ int solve_fp64(scf_mom_ctx *ctx, const scf_mom_opts &o, SolveOut &out)
     const double *const *m = ctx->m;
     const size_t bytes = (size_t)d.ng * sizeof(double);
     MK(cudaMemsetAsync(V.x, 0, bytes, ctx->st));
-    resid64(d, m, ctx->b, nullptr, nullptr, nullptr, V.r, nullptr, ctx->R, ctx->sc, ctx->st);
+    resid64(d, m, ctx->b, nullptr, V.r, nullptr, true, ctx->R, ctx->sc, ctx->st);
     MK(cudaMemcpyAsync(V.r0, V.r, bytes, cudaMemcpyDeviceToDevice, ctx->st));
     out.launches += 2;
     RS();
@@ -201,7 +200,7 @@ int solve_fp64(scf_mom_ctx *ctx, const scf_mom_opts &o, SolveOut &out)
             return SCF_ERR_NONFINITE;
         }
         if (rr <= target || ctx->sc_host->breakdown) {
-            resid64(d, m, ctx->b, V.x, nullptr, nullptr, V.r, nullptr, ctx->R, ctx->sc, ctx->st);
+            resid64(d, m, ctx->b, V.x, V.r, nullptr, false, ctx->R, ctx->sc, ctx->st);
             out.launches += 2;
             RS();
             rr = ctx->sc_host->rr;
@@ -217,17 +216,18 @@ int solve_fp64(scf_mom_ctx *ctx, const scf_mom_opts &o, SolveOut &out)
 
 // FP32 BiCGStab inside FP64 iterative refinement: each round solves
 // A e = r (r the FP64 residual rounded to FP32) to a relative 1e-6, then
-// x += e and the residual is recomputed in FP64 from the FP64 rows.
+// x += e and the residual is recomputed in FP64 from the FP64 rows.  The
+// host reads the scalars only to stop.
 int solve_mixed(scf_mom_ctx *ctx, const scf_mom_opts &o, SolveOut &out)
 {
     const Dims &d = ctx->d;
     BcgVecs<float> &V = ctx->V32;
     const double *const *m = ctx->m;
     const float *const *m32 = ctx->m32;
-    double *xa = ctx->V64.x, *xb = ctx->x64b;
+    double *xa = ctx->V64.x;
     const size_t bytes32 = (size_t)d.ng * sizeof(float);
     MK(cudaMemsetAsync(xa, 0, (size_t)d.ng * sizeof(double), ctx->st));
-    resid64(d, m, ctx->b, nullptr, nullptr, nullptr, nullptr, V.r, ctx->R, ctx->sc, ctx->st);
+    resid64(d, m, ctx->b, nullptr, nullptr, V.r, true, ctx->R, ctx->sc, ctx->st);
     out.launches += 2;
     RS();
     const double bb = ctx->sc_host->bb, target = o.rel_tol * o.rel_tol * bb;
@@ -259,9 +259,9 @@ int solve_mixed(scf_mom_ctx *ctx, const scf_mom_opts &o, SolveOut &out)
             }
             if (r2 <= inner || ctx->sc_host->breakdown) break;
         }
-        resid64(d, m, ctx->b, xa, V.x, xb, nullptr, V.r, ctx->R, ctx->sc, ctx->st);
-        out.launches += 2;
-        std::swap(xa, xb);
+        xadd(d, xa, V.x, ctx->st);
+        resid64(d, m, ctx->b, xa, nullptr, V.r, false, ctx->R, ctx->sc, ctx->st);
+        out.launches += 3;
         ++out.rounds;
         RS();
         rr = ctx->sc_host->rr;
@@ -334,7 +334,6 @@ extern "C" int scf_mom_create(scf_mom_ctx **out, int32_t imax, int32_t jmax, int
     TRY(ctx->V64.p[0], ng) TRY(ctx->V64.p[1], ng) TRY(ctx->V64.v[0], ng) TRY(ctx->V64.v[1], ng)
     TRY(ctx->V32.x, ng) TRY(ctx->V32.r, ng) TRY(ctx->V32.r0, ng) TRY(ctx->V32.t, ng)
     TRY(ctx->V32.p[0], ng) TRY(ctx->V32.p[1], ng) TRY(ctx->V32.v[0], ng) TRY(ctx->V32.v[1], ng)
-    TRY(ctx->x64b, ng)
     ctx->R.nblocks = (int)(solver_grid(d).x * solver_grid(d).y * solver_grid(d).z);
     TRY(ctx->R.partials, 4 * (size_t)ctx->R.nblocks)
     TRY(ctx->sc, 1)

@@ -75,11 +75,13 @@ struct Reduce {
 template <typename T>
 void bcg_iteration(const Dims &d, const T *const m[6], BcgVecs<T> &V, int &pp, bool first, Reduce &R,
                    BcgScalars *sc, cudaStream_t st, cudaEvent_t *ev = nullptr);
-// r64 = b - A x (FP64 coefficients), ||r64||^2 into sc->rr, ||b||^2 into
-// sc->bb; xnew = x (+ e when e is given: the correction of a refinement
-// round).  With r32 given, r32 = (float) r64.  x = NULL: x = 0 (r = b).
-void resid64(const Dims &d, const double *const m[6], const double *b, const double *x, const float *e,
-             double *xnew, double *r64, float *r32, Reduce &R, BcgScalars *sc, cudaStream_t st);
+// r = b - A x with the FP64 couplings (x = NULL: x = 0, r = b) into r64
+// and/or r32 (rounded); ||r||^2 into sc->rr, the stored vector's norm^2 into
+// sc->rho, and with want_bb ||b||^2 into sc->bb; resets alpha, omega, beta.
+void resid64(const Dims &d, const double *const m[6], const double *b, const double *x, double *r64, float *r32,
+             bool want_bb, Reduce &R, BcgScalars *sc, cudaStream_t st);
+// x += e (FP32 correction), pointwise.
+void xadd(const Dims &d, double *x, const float *e, cudaStream_t st);
 // Launch shape of the per-cell kernels (assembly checks).
 dim3 interior_block();
 dim3 interior_grid(const Dims &d);
