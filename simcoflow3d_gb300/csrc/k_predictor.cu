@@ -329,18 +329,16 @@ void mom_check_numbering(const MomDev &in, int comp, const Dims &d, unsigned lon
     k_mom_numbering<<<interior_grid(d), interior_block(), 0, st>>>(in, comp, d, counts);
 }
 
-void mom_tail(const MomDev in[3], const Dims &d, double *pred[3], double *dp[3], cudaStream_t st, int *launches)
+void mom_tail_comp(const MomDev &in, const Dims &d, int c, double *pred, double *dp, cudaStream_t st,
+                   int *launches)
 {
-    for (int c = 0; c < 3; ++c) {
-        k_dp_phase<<<dim3((d.J + 2 + 127) / 128, d.K + 2), 128, 0, st>>>(dp[c], d, c + 1, 0);
-        k_dp_phase<<<dim3((d.I + 2 + 127) / 128, d.K + 2), 128, 0, st>>>(dp[c], d, c + 1, 1);
-        k_dp_phase<<<dim3((d.I + 2 + 127) / 128, d.J + 2), 128, 0, st>>>(dp[c], d, c + 1, 2);
-        *launches += 3;
-    }
-    k_pred_bc<<<dim3((d.J + 127) / 128, d.K), 128, 0, st>>>(pred[0], in[0], d, 1);
-    k_pred_bc<<<dim3((d.I + 127) / 128, d.K), 128, 0, st>>>(pred[1], in[1], d, 2);
-    k_pred_bc<<<dim3((d.I + 127) / 128, d.J), 128, 0, st>>>(pred[2], in[2], d, 3);
-    *launches += 3;
+    k_dp_phase<<<dim3((d.J + 2 + 127) / 128, d.K + 2), 128, 0, st>>>(dp, d, c + 1, 0);
+    k_dp_phase<<<dim3((d.I + 2 + 127) / 128, d.K + 2), 128, 0, st>>>(dp, d, c + 1, 1);
+    k_dp_phase<<<dim3((d.I + 2 + 127) / 128, d.J + 2), 128, 0, st>>>(dp, d, c + 1, 2);
+    if (c == 0) k_pred_bc<<<dim3((d.J + 127) / 128, d.K), 128, 0, st>>>(pred, in, d, 1);
+    else if (c == 1) k_pred_bc<<<dim3((d.I + 127) / 128, d.K), 128, 0, st>>>(pred, in, d, 2);
+    else k_pred_bc<<<dim3((d.I + 127) / 128, d.J), 128, 0, st>>>(pred, in, d, 3);
+    *launches += 4;
 }
 
 }  // namespace pred

@@ -8,6 +8,8 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <future>
+#include <thread>
 #include <vector>
 
 #include "../../include/scf_predictor.h"
@@ -19,6 +21,8 @@ struct scf_mom_ctx {
     Dims d{};
     int device = 0;
     cudaStream_t st = nullptr;
+    cudaStream_t cin = nullptr, cout = nullptr;   // copies in / out of the pipelined call
+    cudaEvent_t staged_ev[3] = {}, done_ev[3] = {};
     cudaEvent_t ev[4] = {};
     cudaEvent_t kev[7] = {};   // around the BiCGStab passes (kernel_timing)
     std::vector<void *> mem;
@@ -151,6 +155,7 @@ struct SolveOut {
 };
 
 float elapsed(cudaEvent_t a, cudaEvent_t b);
+int check_inputs(scf_mom_ctx *ctx, const scf_mom_in in[3]);
 
 // After a synchronised iteration: the three stencil kernels' times.
 void add_kernel_times(scf_mom_ctx *ctx, SolveOut &out)
@@ -302,7 +307,14 @@ extern "C" int scf_mom_create(scf_mom_ctx **out, int32_t imax, int32_t jmax, int
         scf_mom_destroy(ctx);
         return rc;
     };
-    if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) return fail(SCF_ERR_CUDA);
+    if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->cin, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->cout, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(SCF_ERR_CUDA);
+    for (int c = 0; c < 3; ++c)
+        if (cudaEventCreateWithFlags(&ctx->staged_ev[c], cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ctx->done_ev[c], cudaEventDisableTiming) != cudaSuccess)
+            return fail(SCF_ERR_CUDA);
     for (auto &e : ctx->ev)
         if (cudaEventCreate(&e) != cudaSuccess) return fail(SCF_ERR_CUDA);
     for (auto &e : ctx->kev)
@@ -358,6 +370,14 @@ extern "C" int scf_mom_destroy(scf_mom_ctx *ctx)
         if (e) cudaEventDestroy(e);
     for (auto e : ctx->kev)
         if (e) cudaEventDestroy(e);
+    for (int c = 0; c < 3; ++c) {
+        if (ctx->staged_ev[c]) cudaEventDestroy(ctx->staged_ev[c]);
+        if (ctx->done_ev[c]) cudaEventDestroy(ctx->done_ev[c]);
+    }
+    if (ctx->cin) cudaStreamSynchronize(ctx->cin);
+    if (ctx->cout) cudaStreamSynchronize(ctx->cout);
+    if (ctx->cin) cudaStreamDestroy(ctx->cin);
+    if (ctx->cout) cudaStreamDestroy(ctx->cout);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
     return SCF_OK;
@@ -367,17 +387,8 @@ extern "C" int scf_mom_stage(scf_mom_ctx *ctx, const scf_mom_in in[3])
 {
     if (!ctx || !in) return SCF_ERR_BAD_ARG;
     ctx->err[0] = 0;
-    for (int c = 0; c < 3; ++c) {
-        for (const Copy &cp : comp_copies(ctx, c, in[c]))
-            if (!cp.host) {
-                mom_err(ctx, "component %d: a required input array is NULL", c);
-                return SCF_ERR_BAD_ARG;
-            }
-        if (in[c].extcell < -1) {
-            mom_err(ctx, "component %d: ExtCell %d", c, in[c].extcell);
-            return SCF_ERR_BAD_ARG;
-        }
-    }
+    const int rc = check_inputs(ctx, in);
+    if (rc != SCF_OK) return rc;
     MK(cudaSetDevice(ctx->device));
     for (int c = 0; c < 3; ++c) {
         for (const Copy &cp : comp_copies(ctx, c, in[c]))
@@ -390,6 +401,137 @@ extern "C" int scf_mom_stage(scf_mom_ctx *ctx, const scf_mom_in in[3])
     return SCF_OK;
 }
 
+namespace {
+
+int check_opts(scf_mom_ctx *ctx, const scf_mom_opts &o)
+{
+    if (!(o.dt > 0.0) || !(o.rel_tol > 0.0) || o.max_iter < 1 || !(o.g != 0.0) || !(o.fr != 0.0) ||
+        (o.precision != SCF_PREC_FP64 && o.precision != SCF_PREC_MIXED)) {
+        mom_err(ctx, "bad options");
+        return SCF_ERR_BAD_ARG;
+    }
+    return SCF_OK;
+}
+
+int check_inputs(scf_mom_ctx *ctx, const scf_mom_in in[3])
+{
+    for (int c = 0; c < 3; ++c) {
+        for (const Copy &cp : comp_copies(ctx, c, in[c]))
+            if (!cp.host) {
+                mom_err(ctx, "component %d: a required input array is NULL", c);
+                return SCF_ERR_BAD_ARG;
+            }
+        if (in[c].extcell < -1) {
+            mom_err(ctx, "component %d: ExtCell %d", c, in[c].extcell);
+            return SCF_ERR_BAD_ARG;
+        }
+    }
+    return SCF_OK;
+}
+
+// The numbering DeltaGetValues relies on: PosNu = -1 exactly on solid
+// cells, ExtCell + 1 numbered cells.
+int check_numbering(scf_mom_ctx *ctx, int c, scf_mom_stats &s)
+{
+    MK(cudaMemsetAsync(ctx->counts, 0, 2 * sizeof(unsigned long long), ctx->st));
+    mom_check_numbering(dev_view(ctx->comp[c]), c + 1, ctx->d, ctx->counts, ctx->st);
+    MK(cudaMemcpyAsync(ctx->counts_host, ctx->counts, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                       ctx->st));
+    MK(cudaStreamSynchronize(ctx->st));
+    s.gpu_launches += 1;
+    if (ctx->counts_host[1] != 0 || (long long)ctx->counts_host[0] != (long long)ctx->comp[c].extcell + 1) {
+        mom_err(ctx, "component %d: %llu active cells for ExtCell %d, %llu PosNu/Cell_Type mismatches", c,
+                ctx->counts_host[0], ctx->comp[c].extcell, ctx->counts_host[1]);
+        return SCF_ERR_BAD_INPUT;
+    }
+    return SCF_OK;
+}
+
+// Assembly, solve, scatter and tail of component c on ctx->st.
+int run_component(scf_mom_ctx *ctx, int c, const scf_mom_opts &o, scf_mom_stats &s)
+{
+    const Dims &d = ctx->d;
+    MomParams P;
+    P.dt = o.dt; P.rho_a = o.rho_a_ref; P.rho_w = o.rho_w_ref; P.fr = o.fr;
+    P.gx = o.gx; P.gy = o.gy; P.gz = o.gz; P.g = o.g; P.beta_vis = o.beta_vis;
+    for (int f = 0; f < 6; ++f) P.flags[f] = ctx->comp[c].flag[f];
+    const bool mixed = o.precision == SCF_PREC_MIXED;
+    MomSys S;
+    for (int q = 0; q < 6; ++q) { S.m[q] = ctx->m[q]; S.m32[q] = ctx->m32[q]; }
+    S.b = ctx->b;
+    S.dp = ctx->dp[c];
+    const MomDev view = dev_view(ctx->comp[c]);
+    MK(cudaEventRecord(ctx->ev[0], ctx->st));
+    mom_assemble(view, P, c + 1, d, S, mixed, ctx->st);
+    MK(cudaGetLastError());
+    MK(cudaEventRecord(ctx->ev[1], ctx->st));
+    s.gpu_launches += 1;
+    SolveOut so;
+    const int rc = mixed ? solve_mixed(ctx, o, so) : solve_fp64(ctx, o, so);
+    if (rc != SCF_OK) return rc;
+    MK(cudaGetLastError());
+    MK(cudaMemcpyAsync(ctx->pred[c], so.x, (size_t)d.ng * sizeof(double), cudaMemcpyDeviceToDevice, ctx->st));
+    MK(cudaEventRecord(ctx->ev[2], ctx->st));
+    int tl = 0;
+    mom_tail_comp(view, d, c, ctx->pred[c], ctx->dp[c], ctx->st, &tl);
+    MK(cudaGetLastError());
+    MK(cudaEventRecord(ctx->ev[3], ctx->st));
+    MK(cudaEventSynchronize(ctx->ev[3]));
+    s.ms_assemble += elapsed(ctx->ev[0], ctx->ev[1]);
+    s.ms_solve += elapsed(ctx->ev[1], ctx->ev[2]);
+    s.ms_tail += elapsed(ctx->ev[2], ctx->ev[3]);
+    s.iterations[c] = so.iterations;
+    s.rounds[c] = so.rounds;
+    s.converged[c] = so.converged;
+    s.rel_residual[c] = so.rel;
+    s.gpu_launches += so.launches + tl;
+    s.timed_iterations += so.timed;
+    for (int q = 0; q < 4; ++q) s.ms_kernels[q] += so.ms_k[q];
+    return SCF_OK;
+}
+
+int converged_or_report(scf_mom_ctx *ctx, const scf_mom_stats &s)
+{
+    for (int c = 0; c < 3; ++c)
+        if (!s.converged[c]) {
+            mom_err(ctx, "component %d: relative residual %.3e after %d iterations", c, s.rel_residual[c],
+                    s.iterations[c]);
+            return SCF_ERR_NOT_CONVERGED;
+        }
+    return SCF_OK;
+}
+
+// Copies of component c's results to the host on stream st: Dp whole, Pred
+// on the box the reference writes (the loop range and the BC planes of the
+// component's own axis).
+cudaError_t fetch_component(scf_mom_ctx *ctx, int c, double *pred, double *dp, cudaStream_t st)
+{
+    const Dims &d = ctx->d;
+    if (dp) {
+        const cudaError_t e = cudaMemcpyAsync(dp, ctx->dp[c], (size_t)d.ng * sizeof(double), cudaMemcpyDeviceToHost, st);
+        if (e != cudaSuccess) return e;
+    }
+    if (!pred) return cudaSuccess;
+    const int x0 = c == 0 ? 0 : 1, y0 = c == 1 ? 0 : 1, z0 = c == 2 ? 0 : 1;
+    const int nx = c == 0 ? d.I + 2 : d.I, ny = c == 1 ? d.J + 2 : d.J, nz = c == 2 ? d.K + 2 : d.K;
+    cudaMemcpy3DParms p;
+    std::memset(&p, 0, sizeof p);
+    p.srcPtr = make_cudaPitchedPtr(ctx->pred[c], (size_t)(d.I + 2) * sizeof(double), d.I + 2, d.J + 2);
+    p.dstPtr = make_cudaPitchedPtr(pred, (size_t)(d.I + 2) * sizeof(double), d.I + 2, d.J + 2);
+    p.srcPos = make_cudaPos((size_t)x0 * sizeof(double), y0, z0);
+    p.dstPos = p.srcPos;
+    p.extent = make_cudaExtent((size_t)nx * sizeof(double), ny, nz);
+    p.kind = cudaMemcpyDeviceToHost;
+    return cudaMemcpy3DAsync(&p, st);
+}
+
+double ms_between(std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b)
+{
+    return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+}  // namespace
+
 extern "C" int scf_mom_run(scf_mom_ctx *ctx, const scf_mom_opts *opts, scf_mom_stats *stats)
 {
     if (!ctx || !opts) return SCF_ERR_BAD_ARG;
@@ -398,83 +540,19 @@ extern "C" int scf_mom_run(scf_mom_ctx *ctx, const scf_mom_opts *opts, scf_mom_s
         mom_err(ctx, "scf_mom_run before scf_mom_stage");
         return SCF_ERR_NO_SOLVE;
     }
-    const scf_mom_opts &o = *opts;
-    if (!(o.dt > 0.0) || !(o.rel_tol > 0.0) || o.max_iter < 1 || !(o.g != 0.0) || !(o.fr != 0.0) ||
-        (o.precision != SCF_PREC_FP64 && o.precision != SCF_PREC_MIXED)) {
-        mom_err(ctx, "bad options");
-        return SCF_ERR_BAD_ARG;
-    }
+    int rc = check_opts(ctx, *opts);
+    if (rc != SCF_OK) return rc;
     MK(cudaSetDevice(ctx->device));
-    const Dims &d = ctx->d;
     scf_mom_stats s;
     std::memset(&s, 0, sizeof s);
-    // the numbering DeltaGetValues relies on: PosNu = -1 exactly on solid
-    // cells, ExtCell + 1 numbered cells
-    for (int c = 0; c < 3; ++c) {
-        MK(cudaMemsetAsync(ctx->counts, 0, 2 * sizeof(unsigned long long), ctx->st));
-        mom_check_numbering(dev_view(ctx->comp[c]), c + 1, d, ctx->counts, ctx->st);
-        MK(cudaMemcpyAsync(ctx->counts_host, ctx->counts, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
-                           ctx->st));
-        MK(cudaStreamSynchronize(ctx->st));
-        s.gpu_launches += 1;
-        if (ctx->counts_host[1] != 0 || (long long)ctx->counts_host[0] != (long long)ctx->comp[c].extcell + 1) {
-            mom_err(ctx, "component %d: %llu active cells for ExtCell %d, %llu PosNu/Cell_Type mismatches", c,
-                    ctx->counts_host[0], ctx->comp[c].extcell, ctx->counts_host[1]);
-            return SCF_ERR_BAD_INPUT;
-        }
-    }
-    MomParams P;
-    P.dt = o.dt; P.rho_a = o.rho_a_ref; P.rho_w = o.rho_w_ref; P.fr = o.fr;
-    P.gx = o.gx; P.gy = o.gy; P.gz = o.gz; P.g = o.g; P.beta_vis = o.beta_vis;
-    const bool mixed = o.precision == SCF_PREC_MIXED;
-    MomSys S;
-    for (int q = 0; q < 6; ++q) { S.m[q] = ctx->m[q]; S.m32[q] = ctx->m32[q]; }
-    S.b = ctx->b;
-    MomDev views[3];
-    for (int c = 0; c < 3; ++c) {
-        views[c] = dev_view(ctx->comp[c]);
-        S.dp = ctx->dp[c];
-        for (int f = 0; f < 6; ++f) P.flags[f] = ctx->comp[c].flag[f];
-        MK(cudaEventRecord(ctx->ev[0], ctx->st));
-        mom_assemble(views[c], P, c + 1, d, S, mixed, ctx->st);
-        MK(cudaGetLastError());
-        MK(cudaEventRecord(ctx->ev[1], ctx->st));
-        s.gpu_launches += 1;
-        SolveOut so;
-        const int rc = mixed ? solve_mixed(ctx, o, so) : solve_fp64(ctx, o, so);
-        if (rc != SCF_OK) return rc;
-        MK(cudaGetLastError());
-        MK(cudaMemcpyAsync(ctx->pred[c], so.x, (size_t)d.ng * sizeof(double), cudaMemcpyDeviceToDevice, ctx->st));
-        MK(cudaEventRecord(ctx->ev[2], ctx->st));
-        MK(cudaEventSynchronize(ctx->ev[2]));
-        s.ms_assemble += elapsed(ctx->ev[0], ctx->ev[1]);
-        s.ms_solve += elapsed(ctx->ev[1], ctx->ev[2]);
-        s.iterations[c] = so.iterations;
-        s.rounds[c] = so.rounds;
-        s.converged[c] = so.converged;
-        s.rel_residual[c] = so.rel;
-        s.gpu_launches += so.launches;
-        s.timed_iterations += so.timed;
-        for (int q = 0; q < 4; ++q) s.ms_kernels[q] += so.ms_k[q];
-    }
-    MK(cudaEventRecord(ctx->ev[0], ctx->st));
-    int tl = 0;
-    mom_tail(views, d, ctx->pred, ctx->dp, ctx->st, &tl);
-    MK(cudaGetLastError());
-    MK(cudaEventRecord(ctx->ev[1], ctx->st));
-    MK(cudaEventSynchronize(ctx->ev[1]));
-    s.ms_tail = elapsed(ctx->ev[0], ctx->ev[1]);
-    s.gpu_launches += tl;
+    for (int c = 0; c < 3; ++c)
+        if ((rc = check_numbering(ctx, c, s)) != SCF_OK) return rc;
+    for (int c = 0; c < 3; ++c)
+        if ((rc = run_component(ctx, c, *opts, s)) != SCF_OK) return rc;
     s.ms_total = s.ms_assemble + s.ms_solve + s.ms_tail;
     ctx->ran = true;
     if (stats) *stats = s;
-    for (int c = 0; c < 3; ++c)
-        if (!s.converged[c]) {
-            mom_err(ctx, "component %d: relative residual %.3e after %d iterations", c, s.rel_residual[c],
-                    s.iterations[c]);
-            return SCF_ERR_NOT_CONVERGED;
-        }
-    return SCF_OK;
+    return converged_or_report(ctx, s);
 }
 
 extern "C" int scf_mom_fetch(scf_mom_ctx *ctx, double *pred_u, double *pred_v, double *pred_w, double *pu_dp,
@@ -486,67 +564,113 @@ extern "C" int scf_mom_fetch(scf_mom_ctx *ctx, double *pred_u, double *pred_v, d
         return SCF_ERR_NO_SOLVE;
     }
     MK(cudaSetDevice(ctx->device));
-    const Dims &d = ctx->d;
     double *preds[3] = {pred_u, pred_v, pred_w}, *dps[3] = {pu_dp, pv_dp, pw_dp};
-    for (int c = 0; c < 3; ++c) {
-        if (dps[c])
-            MK(cudaMemcpyAsync(dps[c], ctx->dp[c], (size_t)d.ng * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
-        if (!preds[c]) continue;
-        // the box of Pred the reference writes: the loop range and the
-        // boundary planes of the component's own axis
-        const int x0 = c == 0 ? 0 : 1, y0 = c == 1 ? 0 : 1, z0 = c == 2 ? 0 : 1;
-        const int nx = c == 0 ? d.I + 2 : d.I, ny = c == 1 ? d.J + 2 : d.J, nz = c == 2 ? d.K + 2 : d.K;
-        cudaMemcpy3DParms p;
-        std::memset(&p, 0, sizeof p);
-        p.srcPtr = make_cudaPitchedPtr(ctx->pred[c], (size_t)(d.I + 2) * sizeof(double), d.I + 2, d.J + 2);
-        p.dstPtr = make_cudaPitchedPtr(preds[c], (size_t)(d.I + 2) * sizeof(double), d.I + 2, d.J + 2);
-        p.srcPos = make_cudaPos((size_t)x0 * sizeof(double), y0, z0);
-        p.dstPos = p.srcPos;
-        p.extent = make_cudaExtent((size_t)nx * sizeof(double), ny, nz);
-        p.kind = cudaMemcpyDeviceToHost;
-        MK(cudaMemcpy3DAsync(&p, ctx->st));
-    }
+    for (int c = 0; c < 3; ++c) MK(fetch_component(ctx, c, preds[c], dps[c], ctx->st));
     MK(cudaStreamSynchronize(ctx->st));
     return SCF_OK;
 }
 
+// The drop-in call, pipelined over the three components: a helper thread
+// copies component c+1's inputs in (stream cin) while component c is
+// assembled and solved, and a second one copies component c's results out
+// (stream cout) while the next component runs.  Each component's tail
+// touches only its own arrays, so it runs right after its solve; the
+// results equal those of stage + run + fetch.
 extern "C" int scf_predict_solves(scf_mom_ctx *ctx, const scf_mom_in in[3], const scf_mom_opts *opts,
                                   double *pred_u, double *pred_v, double *pred_w, double *pu_dp, double *pv_dp,
                                   double *pw_dp, scf_mom_stats *stats)
 {
-    if (!ctx) return SCF_ERR_BAD_ARG;
-    const auto t0 = std::chrono::steady_clock::now();
-    int rc = scf_mom_stage(ctx, in);
+    if (!ctx || !in || !opts) return SCF_ERR_BAD_ARG;
+    ctx->err[0] = 0;
+    int rc = check_inputs(ctx, in);
+    if (rc == SCF_OK) rc = check_opts(ctx, *opts);
     if (rc != SCF_OK) return rc;
-    const auto t1 = std::chrono::steady_clock::now();
+    MK(cudaSetDevice(ctx->device));
+    const auto t0 = std::chrono::steady_clock::now();
+    double *preds[3] = {pred_u, pred_v, pred_w}, *dps[3] = {pu_dp, pv_dp, pw_dp};
+    std::promise<cudaError_t> staged[3];
+    std::promise<bool> done[3];
+    std::future<cudaError_t> staged_f[3];
+    std::future<bool> done_f[3];
+    for (int c = 0; c < 3; ++c) {
+        staged_f[c] = staged[c].get_future();
+        done_f[c] = done[c].get_future();
+    }
+    std::chrono::steady_clock::time_point t_in_end = t0, t_out_end = t0;
+    cudaError_t out_err = cudaSuccess;
+    std::thread stager([&] {
+        cudaError_t e = cudaSetDevice(ctx->device);
+        for (int c = 0; c < 3; ++c) {
+            if (e == cudaSuccess)
+                for (const Copy &cp : comp_copies(ctx, c, in[c])) {
+                    e = cudaMemcpyAsync(cp.dev, cp.host, cp.bytes, cudaMemcpyHostToDevice, ctx->cin);
+                    if (e != cudaSuccess) break;
+                }
+            if (e == cudaSuccess) e = cudaEventRecord(ctx->staged_ev[c], ctx->cin);
+            staged[c].set_value(e);
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->cin);
+        t_in_end = std::chrono::steady_clock::now();
+    });
+    std::thread fetcher([&] {
+        cudaError_t e = cudaSetDevice(ctx->device);
+        for (int c = 0; c < 3; ++c) {
+            if (!done_f[c].get() || e != cudaSuccess) continue;
+            e = cudaStreamWaitEvent(ctx->cout, ctx->done_ev[c], 0);
+            if (e == cudaSuccess) e = fetch_component(ctx, c, preds[c], dps[c], ctx->cout);
+        }
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->cout);
+        out_err = e;
+        t_out_end = std::chrono::steady_clock::now();
+    });
     scf_mom_stats s;
     std::memset(&s, 0, sizeof s);
-    rc = scf_mom_run(ctx, opts, &s);
-    if (rc != SCF_OK && rc != SCF_ERR_NOT_CONVERGED) {
-        if (stats) *stats = s;
-        return rc;
+    int next = 0;   // components whose results were handed to the fetcher
+    for (int c = 0; c < 3 && rc == SCF_OK; ++c) {
+        const cudaError_t e = staged_f[c].get();
+        if (e != cudaSuccess) {
+            mom_err(ctx, "copy of component %d's inputs: %s", c, cudaGetErrorString(e));
+            rc = SCF_ERR_CUDA;
+            break;
+        }
+        if (cudaStreamWaitEvent(ctx->st, ctx->staged_ev[c], 0) != cudaSuccess) { rc = SCF_ERR_CUDA; break; }
+        for (int f = 0; f < 6; ++f) ctx->comp[c].flag[f] = in[c].bc_flag[f];
+        ctx->comp[c].extcell = in[c].extcell;
+        if ((rc = check_numbering(ctx, c, s)) != SCF_OK) break;
+        if ((rc = run_component(ctx, c, *opts, s)) != SCF_OK) break;
+        if (cudaEventRecord(ctx->done_ev[c], ctx->st) != cudaSuccess) { rc = SCF_ERR_CUDA; break; }
+        done[c].set_value(true);
+        next = c + 1;
     }
-    const auto t2 = std::chrono::steady_clock::now();
-    const int rc2 = scf_mom_fetch(ctx, pred_u, pred_v, pred_w, pu_dp, pv_dp, pw_dp);
-    const auto t3 = std::chrono::steady_clock::now();
+    const auto t_dev_end = std::chrono::steady_clock::now();
+    for (int c = next; c < 3; ++c) done[c].set_value(false);
+    for (int c = 0; c < 3; ++c)   // a failed component: let the stager finish
+        if (c >= next && staged_f[c].valid()) staged_f[c].wait();
+    stager.join();
+    fetcher.join();
+    const auto t1 = std::chrono::steady_clock::now();
+    ctx->staged = rc == SCF_OK;
+    ctx->ran = rc == SCF_OK;
+    if (rc == SCF_OK && out_err != cudaSuccess) {
+        mom_err(ctx, "copy of the results: %s", cudaGetErrorString(out_err));
+        rc = SCF_ERR_CUDA;
+    }
     const Dims &d = ctx->d;
-    long long h2d = 0;
-    for (int c = 0; c < 3; ++c)
-        for (const Copy &cp : comp_copies(ctx, c, in[c])) h2d += (long long)cp.bytes;
-    long long d2h = 0;
-    const double *preds[3] = {pred_u, pred_v, pred_w}, *dps[3] = {pu_dp, pv_dp, pw_dp};
+    long long h2d = 0, d2h = 0;
     for (int c = 0; c < 3; ++c) {
+        for (const Copy &cp : comp_copies(ctx, c, in[c])) h2d += (long long)cp.bytes;
         if (dps[c]) d2h += (long long)d.ng * 8;
         if (preds[c])
             d2h += 8LL * (c == 0 ? d.I + 2 : d.I) * (c == 1 ? d.J + 2 : d.J) * (c == 2 ? d.K + 2 : d.K);
     }
     s.bytes_h2d = h2d;
     s.bytes_d2h = d2h;
-    s.ms_h2d = std::chrono::duration<double, std::milli>(t1 - t0).count();
-    s.ms_d2h = std::chrono::duration<double, std::milli>(t3 - t2).count();
-    s.ms_total = std::chrono::duration<double, std::milli>(t3 - t0).count();
+    s.ms_h2d = ms_between(t0, t_in_end);
+    s.ms_d2h = ms_between(t_dev_end, t_out_end > t_dev_end ? t_out_end : t_dev_end);
+    s.ms_total = ms_between(t0, t1);
     if (stats) *stats = s;
-    return rc2 != SCF_OK ? rc2 : rc;
+    if (rc != SCF_OK) return rc;
+    return converged_or_report(ctx, s);
 }
 
 extern "C" int scf_mom_device_fields(scf_mom_ctx *ctx, const double **pred_u, const double **pred_v,

@@ -58,8 +58,12 @@ void mom_assemble(const MomDev &in, const MomParams &o, int comp, const Dims &d,
 // Checks of the row numbering: counts[0] = active cells of the loop range,
 // counts[1] = cells whose PosNu is -1 exactly when they are solid is false.
 void mom_check_numbering(const MomDev &in, int comp, const Dims &d, unsigned long long *counts, cudaStream_t st);
-// Tail of PredictingUVW: Dp ghost planes, velocity BCs, solid cells.
-void mom_tail(const MomDev in[3], const Dims &d, double *pred[3], double *dp[3], cudaStream_t st, int *launches);
+// Tail of PredictingUVW for component c (0 = u): its Dp ghost planes, its
+// velocity BC planes and the solid cells of the plane the BC writes.  Each
+// component's tail touches only its own arrays, so it may run right after
+// that component's solve.
+void mom_tail_comp(const MomDev &in, const Dims &d, int c, double *pred, double *dp, cudaStream_t st,
+                   int *launches);
 
 // BiCGStab kernels (k_bicgstab.cu).  x, r, r0, p, v, t: ghosted T arrays
 // (p[0] and v[0] are used; p[1], v[1] are spare).
