@@ -2,17 +2,23 @@
 // 1992) on the Jacobi-scaled momentum systems of the predictor, templated on
 // the vector type (FP64, or FP32 inside FP64 iterative refinement).
 //
-// One iteration is four passes and three one-block reductions:
+// One iteration is four passes:
 //   U: p = r + beta (p - omega v) in place (the first step of a run takes
 //      p = r)
-//   P: v = A p; r0.v
-//   S: s = r - alpha v, formed at the 7 points; t = A s; t.s, t.t
-//   X: s again, x += alpha p + omega s, r = s - omega t; r0.r, r.r
+//   P: v = A p; r0.v; then alpha
+//   S: s = r - alpha v, formed at the 7 points; t = A s; t.s, t.t; omega
+//   X: s again, x += alpha p + omega s, r = s - omega t; r0.r, r.r; beta,
+//      and the stopping test
 // s is never stored.  Each thread marches KZ cells of one (i, j) column and
 // keeps its share of the dot products in registers, so a block writes one
-// partial sum per dot for 128 x KZ cells; one block then sums the partials
-// in a fixed order, so every run is bitwise reproducible.  The scalars stay
-// in device memory; the host reads only ||r||^2 and the breakdown flag.
+// partial sum per dot for 128 x KZ cells; after each of P, S and X one
+// block of 1024 threads sums the partials in a fixed order (so every run is
+// bitwise reproducible) and updates the scalars, which stay in device
+// memory.  (Summing them in the last block of the pass instead was slower:
+// 128 threads on one SM add 8192 partials.)  The reduction after X sets
+// `done` when ||r||^2 <= target or on a breakdown, and every kernel after
+// that returns at once, so the host enqueues several iterations and reads
+// the scalars once per batch.
 #include "pred_kernels.h"
 
 namespace pred {
@@ -50,6 +56,8 @@ __device__ __forceinline__ void block_partials(A (&v)[Q], double *partials)
     }
 }
 
+__device__ __forceinline__ bool finite_nonzero(double a) { return a != 0.0 && isfinite(a); }
+
 template <typename T>
 struct M6 {
     const T *w, *s, *b, *e, *n, *t;
@@ -76,6 +84,7 @@ template <typename T>
 __global__ void __launch_bounds__(NT) k_bcg_u(Dims d, const T *__restrict__ r, T *__restrict__ p,
                                               const T *__restrict__ v, const BcgScalars *sc, int first)
 {
+    if (sc->done) return;
     COLUMN
     if (!in) return;
     const T beta = (T)sc->beta, omega = (T)sc->omega;
@@ -88,8 +97,9 @@ __global__ void __launch_bounds__(NT) k_bcg_u(Dims d, const T *__restrict__ r, T
 
 template <typename T>
 __global__ void __launch_bounds__(NT) k_bcg_p(Dims d, M6<T> m, const T *__restrict__ p, const T *__restrict__ r0,
-                                              T *__restrict__ v, double *partials)
+                                              T *__restrict__ v, const BcgScalars *sc, double *partials)
 {
+    if (sc->done) return;
     COLUMN
     T acc[1] = {T(0)};
     if (in) {
@@ -108,6 +118,7 @@ template <typename T>
 __global__ void __launch_bounds__(NT) k_bcg_s(Dims d, M6<T> m, const T *__restrict__ r, const T *__restrict__ v,
                                               T *__restrict__ t, const BcgScalars *sc, double *partials)
 {
+    if (sc->done) return;
     COLUMN
     T acc[2] = {T(0), T(0)};
     if (in) {
@@ -130,6 +141,7 @@ __global__ void __launch_bounds__(NT) k_bcg_x(Dims d, T *__restrict__ x, T *__re
                                               const T *__restrict__ v, const T *__restrict__ t, const BcgScalars *sc,
                                               double *partials)
 {
+    if (sc->done) return;
     COLUMN
     T acc[2] = {T(0), T(0)};
     if (in) {
@@ -209,23 +221,23 @@ __device__ __forceinline__ void sum_partials(const double *partials, int nb, dou
     for (int q = 0; q < Q; ++q) out[q] = sh[0][q];
 }
 
-__device__ __forceinline__ bool finite_nonzero(double a) { return a != 0.0 && isfinite(a); }
-
 // after P: alpha = rho / (r0.v)
 __global__ void __launch_bounds__(1024) k_red_alpha(const double *partials, int nb, BcgScalars *sc)
 {
+    if (sc->done) return;
     double s[1];
     sum_partials<1>(partials, nb, s);
     if (threadIdx.x == 0) {
         const double a = sc->rho / s[0];
         if (finite_nonzero(s[0]) && isfinite(a)) sc->alpha = a;
-        else { sc->alpha = 0.0; sc->breakdown = 1; }
+        else { sc->alpha = 0.0; sc->breakdown = 1; sc->done = 1; }
     }
 }
 
 // after S: omega = (t.s) / (t.t); t.t = 0 means s = 0 (omega = 0 finishes)
 __global__ void __launch_bounds__(1024) k_red_omega(const double *partials, int nb, BcgScalars *sc)
 {
+    if (sc->done) return;
     double s[2];
     sum_partials<2>(partials, nb, s);
     if (threadIdx.x == 0) {
@@ -234,17 +246,21 @@ __global__ void __launch_bounds__(1024) k_red_omega(const double *partials, int 
     }
 }
 
-// after X: beta = (rho_new / rho) (alpha / omega), rho = rho_new, rr
+// after X: beta = (rho_new / rho) (alpha / omega), rho = rho_new, rr, and
+// the stopping test
 __global__ void __launch_bounds__(1024) k_red_rho(const double *partials, int nb, BcgScalars *sc)
 {
+    if (sc->done) return;
     double s[2];
     sum_partials<2>(partials, nb, s);
     if (threadIdx.x == 0) {
         sc->rr = s[1];
+        sc->iters += 1;
         const double b = (s[0] / sc->rho) * (sc->alpha / sc->omega);
         if (finite_nonzero(s[0]) && sc->omega != 0.0 && isfinite(b)) sc->beta = b;
-        else { sc->beta = 0.0; sc->breakdown = 1; }
+        else { sc->beta = 0.0; sc->breakdown = 1; sc->done = 1; }
         sc->rho = s[0];
+        if (!(s[1] > sc->target)) sc->done = 1;   // converged (or NaN: the host checks)
     }
 }
 
@@ -261,7 +277,16 @@ __global__ void __launch_bounds__(1024) k_red_resid(const double *partials, int 
         sc->omega = 1.0;
         sc->beta = 0.0;
         sc->breakdown = 0;
+        sc->done = 0;
+        sc->iters = 0;
     }
+}
+
+__global__ void k_set_target(BcgScalars *sc, double target)
+{
+    sc->target = target;
+    sc->done = 0;
+    sc->iters = 0;
 }
 
 template <typename T>
@@ -286,7 +311,7 @@ void bcg_iteration(const Dims &d, const T *const m[6], BcgVecs<T> &V, int &pp, b
     if (ev) cudaEventRecord(ev[0], st);
     k_bcg_u<T><<<g, b, 0, st>>>(d, V.r, p, v, sc, first ? 1 : 0);
     if (ev) cudaEventRecord(ev[1], st);
-    k_bcg_p<T><<<g, b, 0, st>>>(d, M, p, V.r0, v, R.partials);
+    k_bcg_p<T><<<g, b, 0, st>>>(d, M, p, V.r0, v, sc, R.partials);
     if (ev) cudaEventRecord(ev[2], st);
     k_red_alpha<<<1, 1024, 0, st>>>(R.partials, R.nblocks, sc);
     if (ev) cudaEventRecord(ev[3], st);
@@ -304,6 +329,11 @@ void resid64(const Dims &d, const double *const m[6], const double *b, const dou
 {
     k_resid64<<<solver_grid(d), solver_block(), 0, st>>>(d, m6(m), b, x, r64, r32, want_bb ? 1 : 0, R.partials);
     k_red_resid<<<1, 1024, 0, st>>>(R.partials, R.nblocks, sc, want_bb ? 1 : 0);
+}
+
+void set_target(BcgScalars *sc, double target, cudaStream_t st)
+{
+    k_set_target<<<1, 1, 0, st>>>(sc, target);
 }
 
 void xadd(const Dims &d, double *x, const float *e, cudaStream_t st)

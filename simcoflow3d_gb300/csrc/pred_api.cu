@@ -167,6 +167,42 @@ void add_kernel_times(scf_mom_ctx *ctx, SolveOut &out)
     ++out.timed;
 }
 
+// Iterations enqueued between two reads of the device scalars (the passes
+// after convergence return at once, so a batch costs at most a few empty
+// launches); 1 with kernel timing, whose events are read per iteration.
+constexpr int BATCH = 4;
+
+// Runs BiCGStab iterations on V until the device-side test stops them (done)
+// or `cap` iterations ran; returns the iterations run.  `first`: the first
+// one starts with p = r.
+template <typename T>
+int run_batches(scf_mom_ctx *ctx, const scf_mom_opts &o, const T *const m[6], BcgVecs<T> &V, bool first, int cap,
+                SolveOut &out, int &rc)
+{
+    const Dims &d = ctx->d;
+    const int batch = o.kernel_timing ? 1 : BATCH;
+    int done_its = 0, pp = 0;
+    rc = SCF_OK;
+    while (done_its < cap) {
+        const int nb = std::min(batch, cap - done_its);
+        for (int q = 0; q < nb; ++q)
+            bcg_iteration<T>(d, m, V, pp, first && q == 0, ctx->R, ctx->sc, ctx->st,
+                             o.kernel_timing ? ctx->kev : nullptr);
+        first = false;
+        out.launches += 7 * nb;
+        if ((rc = read_scalars(ctx)) != SCF_OK) return done_its;
+        done_its = ctx->sc_host->iters;
+        if (o.kernel_timing) add_kernel_times(ctx, out);
+        if (!std::isfinite(ctx->sc_host->rr)) {
+            mom_err(ctx, "non-finite residual after %d iterations", out.iterations + done_its);
+            rc = SCF_ERR_NONFINITE;
+            return done_its;
+        }
+        if (ctx->sc_host->done) break;
+    }
+    return done_its;
+}
+
 // FP64 BiCGStab on the scaled system, restarted from the true residual
 // when the recursive one says converged but the true one does not, or on a
 // breakdown.
@@ -190,30 +226,21 @@ int solve_fp64(scf_mom_ctx *ctx, const scf_mom_opts &o, SolveOut &out)
         out.rel = bb == 0.0 ? 0.0 : std::sqrt(rr / bb);
         return SCF_OK;
     }
-    bool first = true;
-    int pp = 0;
     while (out.iterations < o.max_iter) {
-        bcg_iteration<double>(d, m, V, pp, first, ctx->R, ctx->sc, ctx->st, o.kernel_timing ? ctx->kev : nullptr);
-        out.launches += 6;
-        ++out.iterations;
-        first = false;
+        set_target(ctx->sc, target, ctx->st);
+        int rc = SCF_OK;
+        out.iterations += run_batches<double>(ctx, o, m, V, true, o.max_iter - out.iterations, out, rc);
+        if (rc != SCF_OK) return rc;
+        if (!ctx->sc_host->done) break;   // iteration cap
+        // converged by the recursive residual, or broken down: check the
+        // true residual and restart from it if needed
+        resid64(d, m, ctx->b, V.x, V.r, nullptr, false, ctx->R, ctx->sc, ctx->st);
+        out.launches += 2;
         RS();
-        if (o.kernel_timing) add_kernel_times(ctx, out);
         rr = ctx->sc_host->rr;
-        if (!std::isfinite(rr)) {
-            mom_err(ctx, "non-finite residual after %d iterations", out.iterations);
-            return SCF_ERR_NONFINITE;
-        }
-        if (rr <= target || ctx->sc_host->breakdown) {
-            resid64(d, m, ctx->b, V.x, V.r, nullptr, false, ctx->R, ctx->sc, ctx->st);
-            out.launches += 2;
-            RS();
-            rr = ctx->sc_host->rr;
-            if (rr <= target) { out.converged = 1; break; }
-            MK(cudaMemcpyAsync(V.r0, V.r, bytes, cudaMemcpyDeviceToDevice, ctx->st));
-            first = true;
-            ++out.rounds;
-        }
+        if (rr <= target) { out.converged = 1; break; }
+        MK(cudaMemcpyAsync(V.r0, V.r, bytes, cudaMemcpyDeviceToDevice, ctx->st));
+        ++out.rounds;
     }
     out.rel = std::sqrt(rr / bb);
     return SCF_OK;
@@ -248,22 +275,10 @@ int solve_mixed(scf_mom_ctx *ctx, const scf_mom_opts &o, SolveOut &out)
         const double inner = std::max(1e-12 * rho0, 0.25 * target);
         MK(cudaMemcpyAsync(V.r0, V.r, bytes32, cudaMemcpyDeviceToDevice, ctx->st));
         MK(cudaMemsetAsync(V.x, 0, bytes32, ctx->st));
-        bool first = true;
-        int pp = 0;
-        while (out.iterations < o.max_iter) {
-            bcg_iteration<float>(d, m32, V, pp, first, ctx->R, ctx->sc, ctx->st, o.kernel_timing ? ctx->kev : nullptr);
-            out.launches += 6;
-            ++out.iterations;
-            first = false;
-            RS();
-            if (o.kernel_timing) add_kernel_times(ctx, out);
-            const double r2 = ctx->sc_host->rr;
-            if (!std::isfinite(r2)) {
-                mom_err(ctx, "non-finite FP32 residual after %d iterations", out.iterations);
-                return SCF_ERR_NONFINITE;
-            }
-            if (r2 <= inner || ctx->sc_host->breakdown) break;
-        }
+        set_target(ctx->sc, inner, ctx->st);
+        int rc = SCF_OK;
+        out.iterations += run_batches<float>(ctx, o, m32, V, true, o.max_iter - out.iterations, out, rc);
+        if (rc != SCF_OK) return rc;
         xadd(d, xa, V.x, ctx->st);
         resid64(d, m, ctx->b, xa, nullptr, V.r, false, ctx->R, ctx->sc, ctx->st);
         out.launches += 3;

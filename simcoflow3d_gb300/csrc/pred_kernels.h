@@ -48,7 +48,10 @@ struct Dims {
 struct BcgScalars {
     double rho, alpha, omega, beta;
     double rr, bb;        // ||r||^2 and ||b||^2
-    int breakdown;        // 1: r0.v = 0 or t.t = 0 in the last step
+    double target;        // stop when rr <= target (the device-side stopping test)
+    int breakdown;        // 1: r0.v = 0 or an invalid beta in the last step
+    int done;             // 1: converged or broken down; later passes return at once
+    int iters;            // iterations run since the last set_target / residual
     int pad;
 };
 
@@ -86,6 +89,8 @@ void resid64(const Dims &d, const double *const m[6], const double *b, const dou
              bool want_bb, Reduce &R, BcgScalars *sc, cudaStream_t st);
 // x += e (FP32 correction), pointwise.
 void xadd(const Dims &d, double *x, const float *e, cudaStream_t st);
+// sc->target = target; clears done and iters.
+void set_target(BcgScalars *sc, double target, cudaStream_t st);
 // Launch shape of the per-cell kernels (assembly checks).
 dim3 interior_block();
 dim3 interior_grid(const Dims &d);
