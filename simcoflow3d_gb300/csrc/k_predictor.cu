@@ -33,31 +33,68 @@ struct RowMemo {
 enum { KDFE, KDFW, KDFN, KDFS, KDFT, KDFB, KEE, KEW, KEN, KES, KET, KEB, KETAE, KETAW, KETAN, KETAS, KETAT, KETAB,
        KVOF, KVOFL, KDX, KDY, KDZ, KFRIC };
 
+// The 18 quotients by the cell density (Dfe..Dfb, Fep..Fbm before the
+// boundary scaling) depend only on the first 20 key values (DF, EDF, Eta,
+// vof, vofL).  A row whose spacing or friction differs from the previous
+// one (a stretched grid, or spacings that are not exact in binary) still
+// reuses them, so it costs three divisions instead of 24.
+constexpr int RHO_KEYS = 20;
+struct RhoMemo {
+    double key[RHO_KEYS];
+    double f[18];   // Dfe, Dfw, Dfn, Dfs, Dft, Dfb, Fep, Fem, Fwp, Fwm, Fnp, Fnm, Fsp, Fsm, Ftp, Ftm, Fbp, Fbm
+    bool valid;
+};
+
 // SetMatrix for one row (PredictUVW.f90:904-1040) with the reference's
 // operations in its order; called only when the key differs from the
 // previous row's (never inlined, so none of it runs speculatively).
-__device__ __noinline__ void mom_row(const RowKey &K, const MomParams &o, int comp, int ib, RowMemo &M)
+__device__ __noinline__ void mom_row(const RowKey &K, const MomParams &o, int comp, int ib, RowMemo &M, RhoMemo &R)
 {
     const int iu = comp == 1, iv = comp == 2, iw = comp == 3;
     const double CoefEW = (double)iu + (double)iv / 2.0 + (double)iw / 2.0;
     const double CoefNS = (double)iu / 2.0 + (double)iv + (double)iw / 2.0;
     const double CoefTB = (double)iu / 2.0 + (double)iv / 2.0 + (double)iw;
-    const double omb = 1.0 - o.beta_vis;
     const double *v = K.v;
-    const double vof = v[KVOF], vofl = v[KVOFL];
-    const double rho = vofl * o.rho_w + (vof - vofl) * o.rho_a;
-    double Dfe = omb * v[KDFE] / rho, Dfw = omb * v[KDFW] / rho;
-    double Dfn = omb * v[KDFN] / rho, Dfs = omb * v[KDFS] / rho;
-    double Dft = omb * v[KDFT] / rho, Dfb = omb * v[KDFB] / rho;
-    const double ee = v[KEE], ew = v[KEW], en = v[KEN], es = v[KES], et = v[KET], eb = v[KEB];
-    const double etaE = v[KETAE], etaW = v[KETAW], etaN = v[KETAN], etaS = v[KETAS], etaT = v[KETAT],
-                 etaB = v[KETAB];
-    double Fep = ee * (1.0 - etaE) / rho, Fem = ee * etaE / rho;
-    double Fwp = ew * etaW / rho, Fwm = ew * (1.0 - etaW) / rho;
-    double Fnp = en * (1.0 - etaN) / rho, Fnm = en * etaN / rho;
-    double Fsp = es * etaS / rho, Fsm = es * (1.0 - etaS) / rho;
-    double Ftp = et * (1.0 - etaT) / rho, Ftm = et * etaT / rho;
-    double Fbp = eb * etaB / rho, Fbm = eb * (1.0 - etaB) / rho;
+    const double vof = v[KVOF];
+    bool same = R.valid;
+    for (int q = 0; q < RHO_KEYS; ++q) same = same && __double_as_longlong(v[q]) == __double_as_longlong(R.key[q]);
+    if (!same) {
+        const double omb = 1.0 - o.beta_vis;
+        const double vofl = v[KVOFL];
+        const double rho = vofl * o.rho_w + (vof - vofl) * o.rho_a;
+        // x / rho without a division where that is exact: rho a power of
+        // two (the liquid's 1.0 with the water reference density) gives the
+        // same rounding as x * (1/rho) (the two real quotients are equal),
+        // and x = +-0 over a finite non-zero rho gives the signed zero.
+        const long long rb = __double_as_longlong(rho);
+        const int rexp = (int)((rb >> 52) & 0x7ff);
+        const bool pow2 = (rb & 0xfffffffffffffLL) == 0 && rexp > 0 && rexp < 0x7fe;
+        const bool finite_nz = rexp > 0 && rexp < 0x7ff;
+        const double rinv = pow2 ? 1.0 / rho : 0.0;
+        auto q = [&](double x) {
+            if (pow2) return x * rinv;
+            if (x == 0.0 && finite_nz) return rho > 0.0 ? x : -x;
+            return x / rho;
+        };
+        double *f = R.f;
+        f[0] = q(omb * v[KDFE]); f[1] = q(omb * v[KDFW]);
+        f[2] = q(omb * v[KDFN]); f[3] = q(omb * v[KDFS]);
+        f[4] = q(omb * v[KDFT]); f[5] = q(omb * v[KDFB]);
+        const double ee = v[KEE], ew = v[KEW], en = v[KEN], es = v[KES], et = v[KET], eb = v[KEB];
+        const double etaE = v[KETAE], etaW = v[KETAW], etaN = v[KETAN], etaS = v[KETAS], etaT = v[KETAT],
+                     etaB = v[KETAB];
+        f[6] = q(ee * (1.0 - etaE)); f[7] = q(ee * etaE);
+        f[8] = q(ew * etaW); f[9] = q(ew * (1.0 - etaW));
+        f[10] = q(en * (1.0 - etaN)); f[11] = q(en * etaN);
+        f[12] = q(es * etaS); f[13] = q(es * (1.0 - etaS));
+        f[14] = q(et * (1.0 - etaT)); f[15] = q(et * etaT);
+        f[16] = q(eb * etaB); f[17] = q(eb * (1.0 - etaB));
+        for (int q = 0; q < RHO_KEYS; ++q) R.key[q] = v[q];
+        R.valid = true;
+    }
+    double Dfe = R.f[0], Dfw = R.f[1], Dfn = R.f[2], Dfs = R.f[3], Dft = R.f[4], Dfb = R.f[5];
+    double Fep = R.f[6], Fem = R.f[7], Fwp = R.f[8], Fwm = R.f[9], Fnp = R.f[10], Fnm = R.f[11];
+    double Fsp = R.f[12], Fsm = R.f[13], Ftp = R.f[14], Ftm = R.f[15], Fbp = R.f[16], Fbm = R.f[17];
     // boundary faces (939-1009); ib bits: i = 1, i = ie, j = 1, j = je,
     // k = 1, k = ke; flags 1 = Neumann
     const int *fl = o.flags;
@@ -99,7 +136,7 @@ __device__ __noinline__ void mom_row(const RowKey &K, const MomParams &o, int co
     const double dp0 = 1.0 / (aP - aE - aW - aN - aS - aT - aB);
     M.dp = vof * dx * dy * dz * dp0;
     const double G3 = o.gx * (double)iu + o.gy * (double)iv + o.gz * (double)iw;
-    M.gterm = 1.0 / (o.fr * o.fr) * vof * dx * dy * dz * G3 / o.g;
+    M.gterm = o.rfr2 * vof * dx * dy * dz * G3 / o.g;   // rfr2 = 1.d0/Fr**2.d0, formed once
     const double inv = 1.0 / aP;
     M.inv = inv;
     M.m[0] = aW * inv; M.m[1] = aS * inv; M.m[2] = aB * inv;
@@ -134,6 +171,8 @@ __global__ void __launch_bounds__(ASM_NT, 4) k_mom_assemble(MomDev in, MomParams
     const int ibase = (i == 1 ? 1 : 0) | (i == ie ? 2 : 0) | (j == 1 ? 4 : 0) | (j == je ? 8 : 0);
     const long long sns = d.I, stb = (long long)d.I * d.J;
     const long long px = ie, pxy = (long long)ie * je;
+    RhoMemo rmemo;
+    rmemo.valid = false;
     double mm[6], minv = 0.0, mdp = 0.0, mg = 0.0, mcb[6];
     float mf[6];   // the FP32 copies of mm
 #pragma unroll
@@ -174,7 +213,7 @@ __global__ void __launch_bounds__(ASM_NT, 4) k_mom_assemble(MomDev in, MomParams
 #pragma unroll
                     for (int q = 0; q < 24; ++q) key.v[q] = v[q];
                     key.kb = kb;
-                    mom_row(key, o, comp, kb, M);
+                    mom_row(key, o, comp, kb, M, rmemo);
 #pragma unroll
                     for (int q = 0; q < 24; ++q) sprev[q][tid] = v[q];
                     skb[tid] = kb;

@@ -469,6 +469,7 @@ int run_component(scf_mom_ctx *ctx, int c, const scf_mom_opts &o, scf_mom_stats 
     MomParams P;
     P.dt = o.dt; P.rho_a = o.rho_a_ref; P.rho_w = o.rho_w_ref; P.fr = o.fr;
     P.gx = o.gx; P.gy = o.gy; P.gz = o.gz; P.g = o.g; P.beta_vis = o.beta_vis;
+    P.rfr2 = 1.0 / (o.fr * o.fr);
     for (int f = 0; f < 6; ++f) P.flags[f] = ctx->comp[c].flag[f];
     const bool mixed = o.precision == SCF_PREC_MIXED;
     MomSys S;

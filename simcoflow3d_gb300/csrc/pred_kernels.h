@@ -26,6 +26,7 @@ struct MomDev {
 
 struct MomParams {
     double dt, rho_a, rho_w, fr, gx, gy, gz, g, beta_vis;
+    double rfr2;    // 1 / (fr * fr), the same IEEE quotient the rows would form
     int flags[6];   // the component's BC%flag (1 = Neumann)
 };
 

@@ -121,3 +121,25 @@ def test_not_converged_is_reported(lib):
     with pytest.raises(ScfError) as e:
         ps(inp, o)
     assert e.value.status == capi.SCF_ERR_NOT_CONVERGED
+
+
+@pytest.mark.parametrize("prec", [capi.SCF_PREC_FP64, capi.SCF_PREC_MIXED], ids=["fp64", "mixed"])
+def test_dirichlet_faces_and_tiny_grid(lib, prec):
+    """All six faces Dirichlet with seeded boundary values (and stronger
+    cut-face terms) on the sphere, and the smallest box: Dp bit for bit,
+    Pred within tolerance."""
+    rng = np.random.default_rng(11)
+    cases = [PR.momentum_inputs(O.grid_preprocess(GM.geometry_inputs("c1", n=12)), vof_old_noise=0.02, edf=0.5),
+             PR.momentum_inputs(O.grid_preprocess(GM.geometry_inputs("box", shape=(3, 2, 4), solid=None)))]
+    for c in cases[0].comps:
+        c.bc_flag[:] = [0] * 6
+        c.bc_var[:] = [np.asfortranarray(rng.normal(size=v.shape)) for v in c.bc_var]
+    for inp in cases:
+        opts = PR.default_opts(precision=prec, rel_tol=1e-12)
+        init, (po, do), (pg, dg), st = _run_both(inp, opts)
+        assert all(st["converged"])
+        for c in range(3):
+            assert np.array_equal(dg[c].view(np.int64), do[c].view(np.int64)), c
+            t = _touched(c, inp.imax, inp.jmax, inp.kmax)
+            assert np.array_equal(pg[c][~t], init[c][~t])
+            assert np.abs(pg[c][t] - po[c][t]).max() <= 1e-9 * np.abs(po[c][t]).max()
