@@ -301,13 +301,12 @@ dim3 solver_block() { return dim3(32, 4, 1); }
 dim3 solver_grid(const Dims &d) { return dim3((d.I + 31) / 32, (d.J + 3) / 4, (d.K + KZ - 1) / KZ); }
 
 template <typename T>
-void bcg_iteration(const Dims &d, const T *const m[6], BcgVecs<T> &V, int &pp, bool first, Reduce &R,
+void bcg_iteration(const Dims &d, const T *const m[6], BcgVecs<T> &V, bool first, Reduce &R,
                    BcgScalars *sc, cudaStream_t st, cudaEvent_t *ev)
 {
     const dim3 g = solver_grid(d), b = solver_block();
     const M6<T> M = m6(m);
-    (void)pp;
-    T *p = V.p[0], *v = V.v[0];
+    T *p = V.p, *v = V.v;
     if (ev) cudaEventRecord(ev[0], st);
     k_bcg_u<T><<<g, b, 0, st>>>(d, V.r, p, v, sc, first ? 1 : 0);
     if (ev) cudaEventRecord(ev[1], st);
@@ -341,9 +340,9 @@ void xadd(const Dims &d, double *x, const float *e, cudaStream_t st)
     k_xadd<<<solver_grid(d), solver_block(), 0, st>>>(d, x, e);
 }
 
-template void bcg_iteration<double>(const Dims &, const double *const[6], BcgVecs<double> &, int &, bool, Reduce &,
+template void bcg_iteration<double>(const Dims &, const double *const[6], BcgVecs<double> &, bool, Reduce &,
                                     BcgScalars *, cudaStream_t, cudaEvent_t *);
-template void bcg_iteration<float>(const Dims &, const float *const[6], BcgVecs<float> &, int &, bool, Reduce &,
+template void bcg_iteration<float>(const Dims &, const float *const[6], BcgVecs<float> &, bool, Reduce &,
                                    BcgScalars *, cudaStream_t, cudaEvent_t *);
 
 }  // namespace pred

@@ -83,12 +83,6 @@ int malloc0(scf_mom_ctx *ctx, P **ptr, size_t count)
     return SCF_OK;
 }
 
-#define ALLOC(ptr, count)                                  \
-    do {                                                   \
-        const int rc_ = malloc0(ctx, &(ptr), (count));     \
-        if (rc_ != SCF_OK) return rc_;                     \
-    } while (0)
-
 struct Copy {
     void *dev;
     const void *host;
@@ -181,12 +175,12 @@ int run_batches(scf_mom_ctx *ctx, const scf_mom_opts &o, const T *const m[6], Bc
 {
     const Dims &d = ctx->d;
     const int batch = o.kernel_timing ? 1 : BATCH;
-    int done_its = 0, pp = 0;
+    int done_its = 0;
     rc = SCF_OK;
     while (done_its < cap) {
         const int nb = std::min(batch, cap - done_its);
         for (int q = 0; q < nb; ++q)
-            bcg_iteration<T>(d, m, V, pp, first && q == 0, ctx->R, ctx->sc, ctx->st,
+            bcg_iteration<T>(d, m, V, first && q == 0, ctx->R, ctx->sc, ctx->st,
                              o.kernel_timing ? ctx->kev : nullptr);
         first = false;
         out.launches += 7 * nb;
@@ -358,9 +352,9 @@ extern "C" int scf_mom_create(scf_mom_ctx **out, int32_t imax, int32_t jmax, int
     for (int q = 0; q < 6; ++q) { TRY(ctx->m[q], ng) TRY(ctx->m32[q], ng) }
     TRY(ctx->b, ng)
     TRY(ctx->V64.x, ng) TRY(ctx->V64.r, ng) TRY(ctx->V64.r0, ng) TRY(ctx->V64.t, ng)
-    TRY(ctx->V64.p[0], ng) TRY(ctx->V64.p[1], ng) TRY(ctx->V64.v[0], ng) TRY(ctx->V64.v[1], ng)
+    TRY(ctx->V64.p, ng) TRY(ctx->V64.v, ng)
     TRY(ctx->V32.x, ng) TRY(ctx->V32.r, ng) TRY(ctx->V32.r0, ng) TRY(ctx->V32.t, ng)
-    TRY(ctx->V32.p[0], ng) TRY(ctx->V32.p[1], ng) TRY(ctx->V32.v[0], ng) TRY(ctx->V32.v[1], ng)
+    TRY(ctx->V32.p, ng) TRY(ctx->V32.v, ng)
     ctx->R.nblocks = (int)(solver_grid(d).x * solver_grid(d).y * solver_grid(d).z);
     TRY(ctx->R.partials, 4 * (size_t)ctx->R.nblocks)
     TRY(ctx->sc, 1)

@@ -69,11 +69,10 @@ void mom_check_numbering(const MomDev &in, int comp, const Dims &d, unsigned lon
 void mom_tail_comp(const MomDev &in, const Dims &d, int c, double *pred, double *dp, cudaStream_t st,
                    int *launches);
 
-// BiCGStab kernels (k_bicgstab.cu).  x, r, r0, p, v, t: ghosted T arrays
-// (p[0] and v[0] are used; p[1], v[1] are spare).
+// BiCGStab kernels (k_bicgstab.cu).  x, r, r0, p, v, t: ghosted T arrays.
 template <typename T>
 struct BcgVecs {
-    T *x, *r, *r0, *p[2], *v[2], *t;
+    T *x, *r, *r0, *p, *v, *t;
 };
 struct Reduce {
     double *partials;     // 4 per block
@@ -81,8 +80,8 @@ struct Reduce {
 };
 // ev (optional, 7 events): recorded around the four passes U, P, S, X.
 template <typename T>
-void bcg_iteration(const Dims &d, const T *const m[6], BcgVecs<T> &V, int &pp, bool first, Reduce &R,
-                   BcgScalars *sc, cudaStream_t st, cudaEvent_t *ev = nullptr);
+void bcg_iteration(const Dims &d, const T *const m[6], BcgVecs<T> &V, bool first, Reduce &R, BcgScalars *sc,
+                   cudaStream_t st, cudaEvent_t *ev = nullptr);
 // r = b - A x with the FP64 couplings (x = NULL: x = 0, r = b) into r64
 // and/or r32 (rounded); ||r||^2 into sc->rr, the stored vector's norm^2 into
 // sc->rho, and with want_bb ||b||^2 into sc->bb; resets alpha, omega, beta.
