@@ -547,12 +547,13 @@ def run_predictor(args):
     import numpy as np
     from simcoflow3d_gb300 import capi, geometry as GM, predictor as PR
     from simcoflow3d_gb300.projection import load_library
+    geo = args.pred_geometry
     n = args.n or 256
-    g = GM.geometry_inputs("c2", n=n, seed=args.seed)
-    GM.GridPreprocess(n, n, n)(g)
+    g = GM.geometry_inputs(geo, n=n, seed=args.seed)
+    GM.GridPreprocess(g.imax, g.jmax, g.kmax)(g)
     inp = PR.momentum_inputs(g, seed=args.seed)
     lib = load_library()
-    ps = PR.PredictSolves(n, n, n)
+    ps = PR.PredictSolves(g.imax, g.jmax, g.kmax)
     ps.stage(inp)
     tol = 1e-10   # the reference's PCG tolerance (PredictUVW.f90:830)
     opts = PR.default_opts(precision=capi.SCF_PREC_MIXED, rel_tol=tol)
@@ -574,7 +575,7 @@ def run_predictor(args):
             pinned.append(arr)
     e2e = [ps(inp, opts, pred, dpo)[2] for _ in range(max(3, args.steps // 4))]
     unpin(lib, pinned)
-    cells = n ** 3
+    cells = g.imax * g.jmax * g.kmax
     it = sum(t["timed_iterations"] for t in timed)
     kms = {k: sum(t["ms_kernels"][q] for t in timed) / it for q, k in enumerate(("U", "P", "S", "X"))}
     kb = {k: BCG_BYTES_F32[k] * cells for k in kms}
@@ -592,20 +593,24 @@ def run_predictor(args):
         x, its, _ = O.csr_bicgstab(A, b, tol=tol)
         sec = time.perf_counter() - t0
         cpu = {"value": round(3 * sec * 1e3, 1), "unit": "ms/call", "cores": threads, "kind": "port",
-               "sample": "the u system at %d^3 (oracle SetMatrix + SetVectors, then Jacobi BiCGStab with OpenMP "
-                         "to the same tolerance, %d iterations) timed once, times 3 components" % (n, its)}
+               "sample": "the u system at %dx%dx%d (oracle SetMatrix + SetVectors, then Jacobi BiCGStab with OpenMP "
+                         "to the same tolerance, %d iterations) timed once, times 3 components"
+                         % (g.imax, g.jmax, g.kmax, its)}
     ms = [r["ms_total"] for r in runs]
     line = {
-        "metric": "ms per momentum-predictor solve call at %d^3 (SetMatrix + SetVectors + solve + "
-                  "DeltaGetValues for u, v, w, Dp ghosts and predictor BCs)" % n,
+        "metric": "ms per momentum-predictor solve call at %dx%dx%d (SetMatrix + SetVectors + solve + "
+                  "DeltaGetValues for u, v, w, Dp ghosts and predictor BCs)" % (g.imax, g.jmax, g.kmax),
         "value": round(statistics.mean(ms), 3), "unit": "ms/call", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(statistics.mean(ms), 3), "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 BiCGStab inside f64 refinement; f64 rows and Dp",
-        "data": "synthetic (c2 cut-cell geometry from GridPreprocess; viscous conductances from the apertures and "
-                "the liquid fraction, Rey = 300; cut-face terms, wall friction and fluxes seeded)",
-        "config": {"workload": "momentum systems of c2: %d^3 unit cube, solid sphere, liquid bubble, dt = 1e-3, "
-                               "Rey = 300, rel. tol 1e-10" % n,
-                   "grid": [n, n, n],
+        "data": "synthetic (%s cut-cell geometry from GridPreprocess; viscous conductances from the apertures and "
+                "the liquid fraction, Rey = 300; cut-face terms, wall friction and fluxes seeded)" % geo,
+        "config": {"workload": ("momentum systems of c2: %d^3 unit cube, solid sphere, liquid bubble" % n
+                                if geo == "c2" else
+                                "momentum systems of c4: %dx%dx%d wave tank on [0,4]x[0,1]x[0,1], z-stretched "
+                                "(ratio 1.02), vertical cylinder" % (g.imax, g.jmax, g.kmax))
+                               + ", dt = 1e-3, Rey = 300, rel. tol 1e-10",
+                   "grid": [g.imax, g.jmax, g.kmax],
                    "l2": "inputs larger than L2 (%.1f GB staged)" % (e2e[-1]["bytes_h2d"] / 1e9)},
         "iterations": runs[-1]["iterations"], "rounds": runs[-1]["rounds"],
         "rel_residual": runs[-1]["rel_residual"],
@@ -723,6 +728,8 @@ def main():
     ap.add_argument("--only", choices=["mixed", "fp64"], default=None,
                     help="time one precision device-resident only (profiling captures)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--pred-geometry", choices=["c2", "c4"], default="c2",
+                    help="geometry of --config predictor (c4: the z-stretched wave tank, 512x256x256)")
     ap.add_argument("--max-cpu-s", type=float, default=150.0, help="stop the reference arm after this many s")
     args = ap.parse_args()
     if args.warmup < 3:
