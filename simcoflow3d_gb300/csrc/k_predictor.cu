@@ -14,87 +14,57 @@ namespace {
 
 __device__ __forceinline__ long long gidx(const Dims &d, int i, int j, int k) { return i + d.sy * j + d.sz * k; }
 
-// The inputs of one row of SetMatrix that do not depend on the velocity:
-// six conductances DF, six cut-face terms EDF, six interpolation weights
-// Eta, vof, vofL, dx, dy, dz, Fric, and which k-boundary the row touches.
-struct RowKey {
-    double v[24];
-    int kb;
-};
-
-// What a row's key determines: the scaled couplings a_d / aP, 1/aP, Dp,
-// the gravity term of the rhs, and the boundary coefficients CWE/CSN/CBT.
-struct RowMemo {
-    double m[6];   // W,S,B,E,N,T
-    double inv, dp, gterm;
-    double cb[6];  // W,E,S,N,B,T boundary coefficients (before the cut-cell terms)
-};
-
+// The inputs of one row of SetMatrix that do not depend on the velocity
+// (the row key): six conductances DF, six cut-face terms EDF, six
+// interpolation weights Eta, vof, vofL, dx, dy, dz, Fric; plus which
+// boundaries the row touches.
 enum { KDFE, KDFW, KDFN, KDFS, KDFT, KDFB, KEE, KEW, KEN, KES, KET, KEB, KETAE, KETAW, KETAN, KETAS, KETAT, KETAB,
-       KVOF, KVOFL, KDX, KDY, KDZ, KFRIC };
-
-// The 18 quotients by the cell density (Dfe..Dfb, Fep..Fbm before the
-// boundary scaling) depend only on the first 20 key values (DF, EDF, Eta,
-// vof, vofL).  A row whose spacing or friction differs from the previous
-// one (a stretched grid, or spacings that are not exact in binary) still
-// reuses them, so it costs three divisions instead of 24.
-constexpr int RHO_KEYS = 20;
-struct RhoMemo {
-    double key[RHO_KEYS];
-    double f[18];   // Dfe, Dfw, Dfn, Dfs, Dft, Dfb, Fep, Fem, Fwp, Fwm, Fnp, Fnm, Fsp, Fsm, Ftp, Ftm, Fbp, Fbm
-    bool valid;
-};
+       KVOF, KVOFL, KDX, KDY, KDZ, KFRIC, NKEY };
+// What a row's key determines (the memo): the scaled couplings a_d / aP
+// (W,S,B,E,N,T), 1/aP, Dp, the gravity term of the rhs, and the boundary
+// coefficients CWE/CSN/CBT before the cut-cell terms (W,E,S,N,B,T).
+enum { MW, MS, MB, ME, MN, MT, MINV, MDP, MG, MCW, MCE, MCS, MCN, MCB, MCT, NMEMO };
+constexpr int ASM_NT = 128;   // threads of an assembly block; the stride of the shared-memory slots
 
 // SetMatrix for one row (PredictUVW.f90:904-1040) with the reference's
 // operations in its order; called only when the key differs from the
 // previous row's (never inlined, so none of it runs speculatively).
-__device__ __noinline__ void mom_row(const RowKey &K, const MomParams &o, int comp, int ib, RowMemo &M, RhoMemo &R)
+__device__ __noinline__ void mom_row(const double *k, const MomParams &o, int comp, int ib, double *mo)
 {
     const int iu = comp == 1, iv = comp == 2, iw = comp == 3;
     const double CoefEW = (double)iu + (double)iv / 2.0 + (double)iw / 2.0;
     const double CoefNS = (double)iu / 2.0 + (double)iv + (double)iw / 2.0;
     const double CoefTB = (double)iu / 2.0 + (double)iv / 2.0 + (double)iw;
-    const double *v = K.v;
-    const double vof = v[KVOF];
-    bool same = R.valid;
-    for (int q = 0; q < RHO_KEYS; ++q) same = same && __double_as_longlong(v[q]) == __double_as_longlong(R.key[q]);
-    if (!same) {
-        const double omb = 1.0 - o.beta_vis;
-        const double vofl = v[KVOFL];
-        const double rho = vofl * o.rho_w + (vof - vofl) * o.rho_a;
-        // x / rho without a division where that is exact: rho a power of
-        // two (the liquid's 1.0 with the water reference density) gives the
-        // same rounding as x * (1/rho) (the two real quotients are equal),
-        // and x = +-0 over a finite non-zero rho gives the signed zero.
-        const long long rb = __double_as_longlong(rho);
-        const int rexp = (int)((rb >> 52) & 0x7ff);
-        const bool pow2 = (rb & 0xfffffffffffffLL) == 0 && rexp > 0 && rexp < 0x7fe;
-        const bool finite_nz = rexp > 0 && rexp < 0x7ff;
-        const double rinv = pow2 ? 1.0 / rho : 0.0;
-        auto q = [&](double x) {
-            if (pow2) return x * rinv;
-            if (x == 0.0 && finite_nz) return rho > 0.0 ? x : -x;
-            return x / rho;
-        };
-        double *f = R.f;
-        f[0] = q(omb * v[KDFE]); f[1] = q(omb * v[KDFW]);
-        f[2] = q(omb * v[KDFN]); f[3] = q(omb * v[KDFS]);
-        f[4] = q(omb * v[KDFT]); f[5] = q(omb * v[KDFB]);
-        const double ee = v[KEE], ew = v[KEW], en = v[KEN], es = v[KES], et = v[KET], eb = v[KEB];
-        const double etaE = v[KETAE], etaW = v[KETAW], etaN = v[KETAN], etaS = v[KETAS], etaT = v[KETAT],
-                     etaB = v[KETAB];
-        f[6] = q(ee * (1.0 - etaE)); f[7] = q(ee * etaE);
-        f[8] = q(ew * etaW); f[9] = q(ew * (1.0 - etaW));
-        f[10] = q(en * (1.0 - etaN)); f[11] = q(en * etaN);
-        f[12] = q(es * etaS); f[13] = q(es * (1.0 - etaS));
-        f[14] = q(et * (1.0 - etaT)); f[15] = q(et * etaT);
-        f[16] = q(eb * etaB); f[17] = q(eb * (1.0 - etaB));
-        for (int q = 0; q < RHO_KEYS; ++q) R.key[q] = v[q];
-        R.valid = true;
-    }
-    double Dfe = R.f[0], Dfw = R.f[1], Dfn = R.f[2], Dfs = R.f[3], Dft = R.f[4], Dfb = R.f[5];
-    double Fep = R.f[6], Fem = R.f[7], Fwp = R.f[8], Fwm = R.f[9], Fnp = R.f[10], Fnm = R.f[11];
-    double Fsp = R.f[12], Fsm = R.f[13], Ftp = R.f[14], Ftm = R.f[15], Fbp = R.f[16], Fbm = R.f[17];
+    auto K = [&](int q) { return k[q * ASM_NT]; };
+    const double omb = 1.0 - o.beta_vis;
+    const double vof = K(KVOF), vofl = K(KVOFL);
+    const double rho = vofl * o.rho_w + (vof - vofl) * o.rho_a;
+    // x / rho without a division where that is exact: rho a power of two
+    // (the liquid's 1.0 with the water reference density) gives the same
+    // rounding as x * (1/rho) (the two real quotients are equal), and
+    // x = +-0 over a finite non-zero rho gives the signed zero.
+    const long long rb = __double_as_longlong(rho);
+    const int rexp = (int)((rb >> 52) & 0x7ff);
+    const bool pow2 = (rb & 0xfffffffffffffLL) == 0 && rexp > 0 && rexp < 0x7fe;
+    const bool finite_nz = rexp > 0 && rexp < 0x7ff;
+    const double rinv = pow2 ? 1.0 / rho : 0.0;
+    auto q = [&](double x) {
+        if (pow2) return x * rinv;
+        if (x == 0.0 && finite_nz) return rho > 0.0 ? x : -x;
+        return x / rho;
+    };
+    double Dfe = q(omb * K(KDFE)), Dfw = q(omb * K(KDFW));
+    double Dfn = q(omb * K(KDFN)), Dfs = q(omb * K(KDFS));
+    double Dft = q(omb * K(KDFT)), Dfb = q(omb * K(KDFB));
+    const double ee = K(KEE), ew = K(KEW), en = K(KEN), es = K(KES), et = K(KET), eb = K(KEB);
+    const double etaE = K(KETAE), etaW = K(KETAW), etaN = K(KETAN), etaS = K(KETAS), etaT = K(KETAT),
+                 etaB = K(KETAB);
+    double Fep = q(ee * (1.0 - etaE)), Fem = q(ee * etaE);
+    double Fwp = q(ew * etaW), Fwm = q(ew * (1.0 - etaW));
+    double Fnp = q(en * (1.0 - etaN)), Fnm = q(en * etaN);
+    double Fsp = q(es * etaS), Fsm = q(es * (1.0 - etaS));
+    double Ftp = q(et * (1.0 - etaT)), Ftm = q(et * etaT);
+    double Fbp = q(eb * etaB), Fbm = q(eb * (1.0 - etaB));
     // boundary faces (939-1009); ib bits: i = 1, i = ie, j = 1, j = je,
     // k = 1, k = ke; flags 1 = Neumann
     const int *fl = o.flags;
@@ -123,9 +93,10 @@ __device__ __noinline__ void mom_row(const RowKey &K, const MomParams &o, int co
         else { Dft = Dft * CoefTB; Ftp = Ftp * CoefTB; Ftm = Ftm * CoefTB; }
     }
     double aE = Dfe, aW = Dfw, aN = Dfn, aS = Dfs, aT = Dft, aB = Dfb;
-    M.cb[0] = aW; M.cb[1] = aE; M.cb[2] = aS; M.cb[3] = aN; M.cb[4] = aB; M.cb[5] = aT;   // CWE/CSN/CBT
-    const double dx = v[KDX], dy = v[KDY], dz = v[KDZ];
-    double aP = vof * dx * dy * dz / o.dt + aE + aW + aN + aS + aT + aB + v[KFRIC];
+    auto M = [&](int r, double val) { mo[r * ASM_NT] = val; };
+    M(MCW, aW); M(MCE, aE); M(MCS, aS); M(MCN, aN); M(MCB, aB); M(MCT, aT);   // CWE/CSN/CBT
+    const double dx = K(KDX), dy = K(KDY), dz = K(KDZ);
+    double aP = vof * dx * dy * dz / o.dt + aE + aW + aN + aS + aT + aB + K(KFRIC);
     aP = aP + Fep - Fwp + Fnp - Fsp + Ftp - Fbp;
     aE = aE - Fem;
     aW = aW + Fwm;
@@ -134,13 +105,13 @@ __device__ __noinline__ void mom_row(const RowKey &K, const MomParams &o, int co
     aT = aT - Ftm;
     aB = aB + Fbm;
     const double dp0 = 1.0 / (aP - aE - aW - aN - aS - aT - aB);
-    M.dp = vof * dx * dy * dz * dp0;
+    M(MDP, vof * dx * dy * dz * dp0);
     const double G3 = o.gx * (double)iu + o.gy * (double)iv + o.gz * (double)iw;
-    M.gterm = o.rfr2 * vof * dx * dy * dz * G3 / o.g;   // rfr2 = 1.d0/Fr**2.d0, formed once
+    M(MG, o.rfr2 * vof * dx * dy * dz * G3 / o.g);   // rfr2 = 1.d0/Fr**2.d0, formed once
     const double inv = 1.0 / aP;
-    M.inv = inv;
-    M.m[0] = aW * inv; M.m[1] = aS * inv; M.m[2] = aB * inv;
-    M.m[3] = aE * inv; M.m[4] = aN * inv; M.m[5] = aT * inv;
+    M(MINV, inv);
+    M(MW, aW * inv); M(MS, aS * inv); M(MB, aB * inv);
+    M(ME, aE * inv); M(MN, aN * inv); M(MT, aT * inv);
 }
 
 // One thread per (i, j) column, marching KZ cells along k.  Active cells of
@@ -151,14 +122,13 @@ __device__ __noinline__ void mom_row(const RowKey &K, const MomParams &o, int co
 // 1226-1237).  Consecutive rows of a column with bit-identical keys (most
 // rows away from the interface and the solid) reuse the previous row's
 // memo, so the FP64 divisions run only where the inputs change.  The key
-// being compared stays in registers, the previous one in shared memory (a
-// slot per thread), the memo in registers; only a miss goes through local
-// memory into mom_row.
-constexpr int ASM_NT = 128;
+// being compared is in registers; the previous key and the memo live in the
+// thread's shared-memory slots, which a miss hands to mom_row.
 __global__ void __launch_bounds__(ASM_NT, 4) k_mom_assemble(MomDev in, MomParams o, int comp, Dims d, MomSys S,
                                                          int want32, int kz)
 {
-    __shared__ double sprev[24][ASM_NT];
+    __shared__ double sprev[NKEY][ASM_NT];
+    __shared__ double smemo[NMEMO][ASM_NT];
     __shared__ int skb[ASM_NT];
     const int tid = threadIdx.x + blockDim.x * threadIdx.y;
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
@@ -171,8 +141,6 @@ __global__ void __launch_bounds__(ASM_NT, 4) k_mom_assemble(MomDev in, MomParams
     const int ibase = (i == 1 ? 1 : 0) | (i == ie ? 2 : 0) | (j == 1 ? 4 : 0) | (j == je ? 8 : 0);
     const long long sns = d.I, stb = (long long)d.I * d.J;
     const long long px = ie, pxy = (long long)ie * je;
-    RhoMemo rmemo;
-    rmemo.valid = false;
     double mm[6], minv = 0.0, mdp = 0.0, mg = 0.0, mcb[6];
     float mf[6];   // the FP32 copies of mm
 #pragma unroll
@@ -189,7 +157,7 @@ __global__ void __launch_bounds__(ASM_NT, 4) k_mom_assemble(MomDev in, MomParams
                 const long long few = i + (long long)(d.I + 2) * ((j - 1) + (long long)d.J * (k - 1));
                 const long long fns = (i - 1) + (long long)d.I * (j + (long long)(d.J + 2) * (k - 1));
                 const long long ftb = (i - 1) + (long long)d.I * ((j - 1) + (long long)d.J * k);
-                double v[24];
+                double v[NKEY];
                 v[KDFE] = in.df_ew[few + 1]; v[KDFW] = in.df_ew[few];
                 v[KDFN] = in.df_ns[fns + sns]; v[KDFS] = in.df_ns[fns];
                 v[KDFT] = in.df_tb[ftb + stb]; v[KDFB] = in.df_tb[ftb];
@@ -205,21 +173,20 @@ __global__ void __launch_bounds__(ASM_NT, 4) k_mom_assemble(MomDev in, MomParams
                 const int kb = ibase | (k == 1 ? 16 : 0) | (k == ke ? 32 : 0);
                 bool hit = have && skb[tid] == kb;
 #pragma unroll
-                for (int q = 0; q < 24; ++q)
+                for (int q = 0; q < NKEY; ++q)
                     hit &= __double_as_longlong(v[q]) == __double_as_longlong(sprev[q][tid]);
                 if (!hit) {
-                    RowKey key;
-                    RowMemo M;
 #pragma unroll
-                    for (int q = 0; q < 24; ++q) key.v[q] = v[q];
-                    key.kb = kb;
-                    mom_row(key, o, comp, kb, M, rmemo);
-#pragma unroll
-                    for (int q = 0; q < 24; ++q) sprev[q][tid] = v[q];
+                    for (int q = 0; q < NKEY; ++q) sprev[q][tid] = v[q];
                     skb[tid] = kb;
+                    mom_row(&sprev[0][tid], o, comp, kb, &smemo[0][tid]);
 #pragma unroll
-                    for (int q = 0; q < 6; ++q) { mm[q] = M.m[q]; mcb[q] = M.cb[q]; mf[q] = (float)M.m[q]; }
-                    minv = M.inv; mdp = M.dp; mg = M.gterm;
+                    for (int q = 0; q < 6; ++q) {
+                        mm[q] = smemo[MW + q][tid];
+                        mcb[q] = smemo[MCW + q][tid];
+                        mf[q] = (float)mm[q];
+                    }
+                    minv = smemo[MINV][tid]; mdp = smemo[MDP][tid]; mg = smemo[MG][tid];
                     have = true;
                 }
                 dpv = mdp;
