@@ -608,7 +608,7 @@ extern "C" int scf_predict_solves(scf_mom_ctx *ctx, const scf_mom_in in[3], cons
     }
     std::chrono::steady_clock::time_point t_in_end = t0, t_out_end = t0;
     cudaError_t out_err = cudaSuccess;
-    std::thread stager([&] {
+    auto stage_all = [&] {
         cudaError_t e = cudaSetDevice(ctx->device);
         for (int c = 0; c < 3; ++c) {
             if (e == cudaSuccess)
@@ -621,8 +621,8 @@ extern "C" int scf_predict_solves(scf_mom_ctx *ctx, const scf_mom_in in[3], cons
         }
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->cin);
         t_in_end = std::chrono::steady_clock::now();
-    });
-    std::thread fetcher([&] {
+    };
+    auto fetch_all = [&] {
         cudaError_t e = cudaSetDevice(ctx->device);
         for (int c = 0; c < 3; ++c) {
             if (!done_f[c].get() || e != cudaSuccess) continue;
@@ -632,7 +632,18 @@ extern "C" int scf_predict_solves(scf_mom_ctx *ctx, const scf_mom_in in[3], cons
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->cout);
         out_err = e;
         t_out_end = std::chrono::steady_clock::now();
-    });
+    };
+    // the helper threads; an exception must not leave this C entry point
+    std::thread stager, fetcher;
+    try {
+        stager = std::thread(stage_all);
+        fetcher = std::thread(fetch_all);
+    } catch (...) {
+        if (stager.joinable()) stager.join();   // finishes on its own
+        ctx->staged = ctx->ran = false;
+        mom_err(ctx, "could not start the copy threads");
+        return SCF_ERR_CUDA;
+    }
     scf_mom_stats s;
     std::memset(&s, 0, sizeof s);
     int next = 0;   // components whose results were handed to the fetcher
