@@ -1,9 +1,16 @@
 """Python front end of the oracle (test infrastructure only).
 
-The oracle is the CPU restatement of SIMCOFlow's projection path in
-``oracle.c`` (coefficients, literal CSR matrix, rhs, scatter, correction,
-boundary conditions) plus the CPU multigrid-preconditioned CG of ``gmg.cpp``.
-Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+The oracle is the CPU restatement of the SIMCOFlow routines this repository
+rebuilds:
+- ``oracle.c``: the projection path (coefficients, literal CSR matrix, rhs,
+  scatter, correction, boundary conditions), with the CPU
+  multigrid-preconditioned CG of ``gmg.cpp``;
+- ``geometry.c``: the cut-cell geometry preprocessing;
+- ``predictor.c``: the momentum predictor's SetMatrix / SetVectors,
+  DeltaGetValues and the tail of PredictingUVW, with a Jacobi BiCGStab;
+- ``vtr.py``: the VTK RectilinearGrid writer.
+
+Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline legs of
 ``bench.py`` use it, and only as the checker or the timed CPU path.
 """
 from __future__ import annotations
