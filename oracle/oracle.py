@@ -8,7 +8,9 @@ rebuilds:
 - ``geometry.c``: the cut-cell geometry preprocessing;
 - ``predictor.c``: the momentum predictor's SetMatrix / SetVectors,
   DeltaGetValues and the tail of PredictingUVW, with a Jacobi BiCGStab;
-- ``vtr.py``: the VTK RectilinearGrid writer.
+- ``vtr.py``: the VTK RectilinearGrid writer;
+- ``clsvof.c``: ComputeUVWLiquidField, the first piece of the CLSVOF module
+  (no GPU counterpart yet).
 
 Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline legs of
 ``bench.py`` use it, and only as the checker or the timed CPU path.
@@ -70,6 +72,12 @@ def lib():
         L.oracle_csr_bicgstab.restype = C.c_int
         L.oracle_mom_get_values.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, PM, dp, dp]
         L.oracle_predict_tail.argtypes = [C.c_int, C.c_int, C.c_int, PM] + [dp] * 6
+        L.oracle_volume_fraction_calc.argtypes = [C.c_double] * 7
+        L.oracle_volume_fraction_calc.restype = C.c_double
+        L.oracle_convert_coord.argtypes = [C.c_double] * 7
+        L.oracle_convert_coord.restype = C.c_double
+        DP3 = dp * 3
+        L.oracle_uvw_liquid_field.argtypes = [C.c_int, C.c_int, C.c_int] + [dp] * 8 + [DP3] * 9
         _lib = L
     return _lib
 
@@ -316,3 +324,24 @@ def predict_solves(inp, opts, pred=None, dp=None, tol=1e-14):
     structs = inp.structs()
     lib().oracle_predict_tail(I, J, K, structs, *(_dp(a) for a in pred), *(_dp(a) for a in dp))
     return pred, dp, info
+
+
+def volume_fraction_calc(dx, dy, dz, nx, ny, nz, s):
+    """Volume_Fraction_Calc (Clsvof.f90:1475-1550) of one box."""
+    return lib().oracle_volume_fraction_calc(dx, dy, dz, nx, ny, nz, s)
+
+
+def uvw_liquid_field(pgrid, pcell, vgrids, vcells):
+    """ComputeUVWLiquidField (Clsvof.f90:174-298).  ``pgrid``: (dx, dy, dz)
+    interior arrays of the P grid; ``pcell``: dict of ghosted phil, nxl, nyl,
+    nzl, vofl; ``vgrids``: three (dx, dy, dz) of the U, V, W grids;
+    ``vcells``: three dicts with ghosted phil, nxl, nyl, nzl, vofl (updated
+    in place) and vof."""
+    I, J, K = pgrid[0].shape
+    P = lambda a: _dp(a)
+    arr3 = lambda key: (capi.c_double_p * 3)(*(P(c[key]) for c in vcells))
+    g3 = lambda q: (capi.c_double_p * 3)(*(P(g[q]) for g in vgrids))
+    lib().oracle_uvw_liquid_field(I, J, K, P(pgrid[0]), P(pgrid[1]), P(pgrid[2]), P(pcell["phil"]),
+                                  P(pcell["nxl"]), P(pcell["nyl"]), P(pcell["nzl"]), P(pcell["vofl"]),
+                                  g3(0), g3(1), g3(2), arr3("phil"), arr3("nxl"), arr3("nyl"), arr3("nzl"),
+                                  arr3("vofl"), arr3("vof"))
