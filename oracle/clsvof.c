@@ -1,18 +1,22 @@
 /*
- * clsvof.c -- CPU restatement of ComputeUVWLiquidField, the step of
- * SIMCOFlow's CLSVOF module (src/Clsvof.f90) that derives the liquid
+ * clsvof.c -- CPU restatement of the first pieces of SIMCOFlow's CLSVOF
+ * module (src/Clsvof.f90): ComputeUVWLiquidField, which derives the liquid
  * fraction and level set of the U, V, W cells from the pressure cells after
- * each interface advection (called from src/Solver.f90:209).
+ * each interface advection (called from src/Solver.f90:209), and
+ * Interface_Reconstruct, the normals and plane distances every sweep of
+ * Clsvof_Scheme starts from.
  *
  * TEST INFRASTRUCTURE ONLY: the checker for a future GPU restatement;
  * nothing in the product links or calls it.  Parity status: the reference
  * (Fortran) cannot be built on this machine and its tests hold no golden
- * values for this routine, so the restatement is pinned by known-answer
+ * values for these routines, so the restatement is pinned by known-answer
  * tests in tests/ (a horizontal interface seen by the U cells, the direction
- * averages written through the reference's index shift) and by an
- * independent vectorised restatement of Volume_Fraction_Calc
+ * averages written through the reference's index shift, a planar interface
+ * reconstructed exactly, Find_Distance inverting Volume_Fraction_Calc) and
+ * by an independent vectorised restatement of Volume_Fraction_Calc
  * (simcoflow3d_gb300/workloads.py volume_fraction_calc), not by reference
- * outputs.
+ * outputs.  Newton_Raphson is capped at 200 steps (the reference loops
+ * without a cap).
  *
  * Loops and expressions keep the reference's order; built with
  * -ffp-contract=off.  Fortran x**2.d0 is x*x (gfortran folds it exactly) and
@@ -213,4 +217,190 @@ void oracle_uvw_liquid_field(int imax, int jmax, int kmax, const double *pdx, co
             }
             vel_vofl[2][G(i, j, K)] = vofl[G(i, j, K)];
         }
+}
+
+/* ---- interface reconstruction (Clsvof.f90:801-815, 1216-1473, 2361-2456) -- */
+
+static const double VOFEPS = 1.0e-14;   /* Clsvof.f90:32 */
+static const double ETA = 0.075;        /* Clsvof.f90:32 */
+static const double TOLPAR = 1.0e-14;   /* Clsvof.f90:35 */
+
+/* Newton_Raphson (Clsvof.f90:1462-1473) on a3 s^3 + a2 s^2 + a1 s + a0.  The
+ * reference loops until the step is below 1e-6 |s|; here at most 200 steps
+ * (the reference has no cap).                                              */
+static double newton_raphson(double a3, double a2, double a1, double a0, double sc)
+{
+    const double tol = 1.0e-6;
+    double delvar = 1.0e6;
+    for (int it = 0; it < 200 && fabs(delvar) > tol * fabs(sc); ++it) {
+        delvar = (a3 * pow(sc, 3.0) + a2 * (sc * sc) + a1 * sc + a0) / (3.0 * a3 * (sc * sc) + 2.0 * a2 * sc + a1);
+        sc = sc - delvar;
+    }
+    return sc;
+}
+
+/* Cubic_Equation_Solve (1380-1398); case2 selects the first form.          */
+static double cubic_solve(double fc, double dx1, double dy1, double dz1, double sc, int case2)
+{
+    if (case2)
+        return newton_raphson(1.0, -3.0 * (dy1 + dz1), 3.0 * (dy1 * dy1 + dz1 * dz1),
+                              6.0 * fc * dx1 * dy1 * dz1 - (pow(dy1, 3.0) + pow(dz1, 3.0)), sc);
+    return newton_raphson(2.0, -3.0 * (dx1 + dy1 + dz1), 3.0 * (dx1 * dx1 + dy1 * dy1 + dz1 * dz1),
+                          6.0 * fc * dx1 * dy1 * dz1 - (pow(dx1, 3.0) + pow(dy1, 3.0) + pow(dz1, 3.0)), sc);
+}
+
+static double final_distance(double f, double sc, double sm) { return f <= 0.5 ? sc : sm - sc; }
+
+/* Find_Distance (1311-1378): the distance s from the box's corner along
+ * the normal at which the plane cuts the liquid fraction f off the box.    */
+double oracle_find_distance(double dx, double dy, double dz, double nxx, double nyy, double nzz, double f)
+{
+    const double nx1 = fabs(nxx), ny1 = fabs(nyy), nz1 = fabs(nzz);
+    const double dx1 = max3(nx1 * dx, ny1 * dy, nz1 * dz);
+    double dz1 = min3(nx1 * dx, ny1 * dy, nz1 * dz);
+    if (fabs(dz1) < TOLPAR) dz1 = 0.0;
+    double dy1 = nx1 * dx + ny1 * dy + nz1 * dz - dx1 - dz1;
+    if (fabs(dy1) < TOLPAR) dy1 = 0.0;
+    const double fc = f < 1.0 - f ? f : 1.0 - f;
+    const double sm = dx1 + dy1 + dz1;
+    double sc = 6.0 * fc * dx1 * dy1 * dz1;
+    sc = copysign(1.0, sc) * pow(fabs(sc), 1.0 / 3.0);
+    if (sc < dz1) return final_distance(f, sc, sm);
+    sc = 0.5 * dz1 + sqrt(2.0 * fc * dx1 * dy1 - dz1 * dz1 / 12.0);
+    if (sc < dy1) return final_distance(f, sc, sm);
+    if (dx1 >= dy1 + dz1) {
+        sc = fc * dx1 + (dy1 + dz1) / 2.0;
+        if (sc >= dy1 + dz1) return final_distance(f, sc, sm);
+        sc = cubic_solve(fc, dx1, dy1, dz1, sc, 1);
+        return final_distance(f, sc, sm);
+    }
+    sc = fc * dx1 + (dy1 + dz1) / 2.0;
+    if (sc >= dx1) {
+        sc = cubic_solve(fc, dx1, dy1, dz1, sc, 0);
+        if (sc < dx1) sc = cubic_solve(fc, dx1, dy1, dz1, sc, 1);
+        return final_distance(f, sc, sm);
+    }
+    sc = cubic_solve(fc, dx1, dy1, dz1, sc, 1);
+    return final_distance(f, sc, sm);
+}
+
+/* Isinterface (801-815): a partly filled cell, or a full/empty cell next to
+ * its opposite.  vfl ghosted.                                              */
+static int is_interface(const double *vfl, int i, int j, int k)
+{
+    const double v = vfl[G(i, j, k)];
+    const double jump = 1.0 - 2.1 * VOFEPS;
+    int flag = v > VOFEPS && v < 1.0 - VOFEPS;
+    if (fabs(vfl[G(i - 1, j, k)] - v) >= jump) flag = 1;
+    if (fabs(vfl[G(i + 1, j, k)] - v) >= jump) flag = 1;
+    if (fabs(vfl[G(i, j - 1, k)] - v) >= jump) flag = 1;
+    if (fabs(vfl[G(i, j + 1, k)] - v) >= jump) flag = 1;
+    if (fabs(vfl[G(i, j, k - 1)] - v) >= jump) flag = 1;
+    if (fabs(vfl[G(i, j, k + 1)] - v) >= jump) flag = 1;
+    return flag;
+}
+
+/* Normal_Vector_Irre (2361-2456): per direction, a one-sided difference of
+ * phi towards the side whose neighbour has |grad phi| within ETA of 1 when
+ * the other side's does not, else the central difference.  x, y, z: cell
+ * centres (interior arrays); phi ghosted; only called with 1 < i < I etc. */
+static void normal_vector_irre(const double *x, const double *y, const double *z, const double *phi, int i, int j,
+                               int k, double *nxx, double *nyy, double *nzz)
+{
+#define P(a, b, c) phi[G(a, b, c)]
+#define X(a, b, c) x[N(a, b, c)]
+#define Y(a, b, c) y[N(a, b, c)]
+#define Z(a, b, c) z[N(a, b, c)]
+    double vx, vy, vz, qm, qp;
+    int dx, dy, dz;
+    if (i >= 3) vx = (P(i, j, k) - P(i - 2, j, k)) / (X(i, j, k) - X(i - 2, j, k));
+    else vx = (P(i, j, k) - P(i - 1, j, k)) / (X(i, j, k) - X(i - 1, j, k));
+    vy = (P(i - 1, j + 1, k) - P(i - 1, j - 1, k)) / (Y(i - 1, j + 1, k) - Y(i - 1, j - 1, k));
+    vz = (P(i - 1, j, k + 1) - P(i - 1, j, k - 1)) / (Z(i - 1, j, k + 1) - Z(i - 1, j, k - 1));
+    qm = fabs(1.0 - sqrt(vx * vx + vy * vy + vz * vz));
+    if (i <= I - 2) vx = (P(i + 2, j, k) - P(i, j, k)) / (X(i + 2, j, k) - X(i, j, k));
+    else vx = (P(i + 1, j, k) - P(i, j, k)) / (X(i + 1, j, k) - X(i, j, k));
+    vy = (P(i + 1, j + 1, k) - P(i + 1, j - 1, k)) / (Y(i + 1, j + 1, k) - Y(i + 1, j - 1, k));
+    vz = (P(i + 1, j, k + 1) - P(i + 1, j, k - 1)) / (Z(i + 1, j, k + 1) - Z(i + 1, j, k - 1));
+    qp = fabs(1.0 - sqrt(vx * vx + vy * vy + vz * vz));
+    dx = (qm < ETA && qp >= ETA) ? -1 : (qm >= ETA && qp < ETA) ? 1 : 0;
+    if (j >= 3) vy = (P(i, j, k) - P(i, j - 2, k)) / (Y(i, j, k) - Y(i, j - 2, k));
+    else vy = (P(i, j, k) - P(i, j - 1, k)) / (Y(i, j, k) - Y(i, j - 1, k));
+    vx = (P(i + 1, j - 1, k) - P(i - 1, j - 1, k)) / (X(i + 1, j - 1, k) - X(i - 1, j - 1, k));
+    vz = (P(i, j - 1, k + 1) - P(i, j - 1, k - 1)) / (Z(i, j - 1, k + 1) - Z(i, j - 1, k - 1));
+    qm = fabs(1.0 - sqrt(vx * vx + vy * vy + vz * vz));
+    vx = (P(i + 1, j + 1, k) - P(i - 1, j + 1, k)) / (X(i + 1, j + 1, k) - X(i - 1, j + 1, k));
+    if (j <= J - 2) vy = (P(i, j + 2, k) - P(i, j, k)) / (Y(i, j + 2, k) - Y(i, j, k));
+    else vy = (P(i, j + 1, k) - P(i, j, k)) / (Y(i, j + 1, k) - Y(i, j, k));
+    vz = (P(i, j + 1, k + 1) - P(i, j + 1, k - 1)) / (Z(i, j + 1, k + 1) - Z(i, j + 1, k - 1));
+    qp = fabs(1.0 - sqrt(vx * vx + vy * vy + vz * vz));
+    dy = (qm < ETA && qp >= ETA) ? -1 : (qm >= ETA && qp < ETA) ? 1 : 0;
+    vx = (P(i + 1, j, k - 1) - P(i - 1, j, k - 1)) / (X(i + 1, j, k - 1) - X(i - 1, j, k - 1));
+    vy = (P(i, j + 1, k - 1) - P(i, j - 1, k - 1)) / (Y(i, j + 1, k - 1) - Y(i, j - 1, k - 1));
+    if (k >= 3) vz = (P(i, j, k) - P(i, j, k - 2)) / (Z(i, j, k) - Z(i, j, k - 2));
+    else vz = (P(i, j, k) - P(i, j, k - 1)) / (Z(i, j, k) - Z(i, j, k - 1));
+    qm = fabs(1.0 - sqrt(vx * vx + vy * vy + vz * vz));
+    vx = (P(i + 1, j, k + 1) - P(i - 1, j, k + 1)) / (X(i + 1, j, k + 1) - X(i - 1, j, k + 1));
+    vy = (P(i, j + 1, k + 1) - P(i, j - 1, k + 1)) / (Y(i, j + 1, k + 1) - Y(i, j - 1, k + 1));
+    if (k <= K - 2) vz = (P(i, j, k + 2) - P(i, j, k)) / (Z(i, j, k + 2) - Z(i, j, k));
+    else vz = (P(i, j, k + 1) - P(i, j, k)) / (Z(i, j, k + 1) - Z(i, j, k));
+    qp = fabs(1.0 - sqrt(vx * vx + vy * vy + vz * vz));
+    dz = (qm < ETA && qp >= ETA) ? -1 : (qm >= ETA && qp < ETA) ? 1 : 0;
+    if (dx == -1) *nxx = (P(i, j, k) - P(i - 1, j, k)) / (X(i, j, k) - X(i - 1, j, k));
+    if (dx == 1) *nxx = (P(i + 1, j, k) - P(i, j, k)) / (X(i + 1, j, k) - X(i, j, k));
+    if (dx == 0) *nxx = (P(i + 1, j, k) - P(i - 1, j, k)) / (X(i + 1, j, k) - X(i - 1, j, k));
+    if (dy == -1) *nyy = (P(i, j, k) - P(i, j - 1, k)) / (Y(i, j, k) - Y(i, j - 1, k));
+    if (dy == 1) *nyy = (P(i, j + 1, k) - P(i, j, k)) / (Y(i, j + 1, k) - Y(i, j, k));
+    if (dy == 0) *nyy = (P(i, j + 1, k) - P(i, j - 1, k)) / (Y(i, j + 1, k) - Y(i, j - 1, k));
+    if (dz == -1) *nzz = (P(i, j, k) - P(i, j, k - 1)) / (Z(i, j, k) - Z(i, j, k - 1));
+    if (dz == 1) *nzz = (P(i, j, k + 1) - P(i, j, k)) / (Z(i, j, k + 1) - Z(i, j, k));
+    if (dz == 0) *nzz = (P(i, j, k + 1) - P(i, j, k - 1)) / (Z(i, j, k + 1) - Z(i, j, k - 1));
+#undef P
+#undef X
+#undef Y
+#undef Z
+}
+
+/* Interface_Reconstruct (1216-1309): for every interface cell the unit
+ * normal of phi (Normal_Vector_Irre inside, clamped central differences
+ * near the walls, +z when the gradient vanishes) and Find_Distance of its
+ * liquid fraction; every other cell gets 0.  x, y, z, dx, dy, dz interior;
+ * vfl, phi, nxx, nyy, nzz, diss ghosted (nxx, nyy, nzz zeroed whole first,
+ * diss written on the interior only).                                      */
+void oracle_interface_reconstruct(int imax, int jmax, int kmax, const double *x, const double *y, const double *z,
+                                  const double *dx, const double *dy, const double *dz, const double *vfl,
+                                  const double *phi, double *nxx, double *nyy, double *nzz, double *diss)
+{
+    I = imax; J = jmax; K = kmax;
+    const size_t ng = (size_t)(I + 2) * (J + 2) * (K + 2);
+    for (size_t q = 0; q < ng; ++q) nxx[q] = nyy[q] = nzz[q] = 0.0;
+    for (int i = 1; i <= I; ++i)
+        for (int j = 1; j <= J; ++j)
+            for (int k = 1; k <= K; ++k) {
+                double n1 = 0.0, n2 = 0.0, n3 = 0.0, d1 = 0.0;
+                if (is_interface(vfl, i, j, k)) {
+                    if (i > 1 && i < I && j > 1 && j < J && k > 1 && k < K) {
+                        normal_vector_irre(x, y, z, phi, i, j, k, &n1, &n2, &n3);
+                    } else {
+                        const int ip = i + 1 < I ? i + 1 : I, im = i - 1 > 1 ? i - 1 : 1;
+                        const int jp = j + 1 < J ? j + 1 : J, jm = j - 1 > 1 ? j - 1 : 1;
+                        const int kp = k + 1 < K ? k + 1 : K, km = k - 1 > 1 ? k - 1 : 1;
+                        n1 = (phi[G(ip, j, k)] - phi[G(im, j, k)]) / (x[N(ip, j, k)] - x[N(im, j, k)]);
+                        n2 = (phi[G(i, jp, k)] - phi[G(i, jm, k)]) / (y[N(i, jp, k)] - y[N(i, jm, k)]);
+                        n3 = (phi[G(i, j, kp)] - phi[G(i, j, km)]) / (z[N(i, j, kp)] - z[N(i, j, km)]);
+                    }
+                    const double temp = sqrt(n1 * n1 + n2 * n2 + n3 * n3);
+                    if (temp < 1.0e-14) {
+                        n1 = 0.0; n2 = 0.0; n3 = 1.0;
+                    } else {
+                        n1 = n1 / temp; n2 = n2 / temp; n3 = n3 / temp;
+                    }
+                    d1 = oracle_find_distance(dx[N(i, j, k)], dy[N(i, j, k)], dz[N(i, j, k)], n1, n2, n3,
+                                              vfl[G(i, j, k)]);
+                }
+                nxx[G(i, j, k)] = n1;
+                nyy[G(i, j, k)] = n2;
+                nzz[G(i, j, k)] = n3;
+                diss[G(i, j, k)] = d1;
+            }
 }

@@ -9,8 +9,8 @@ rebuilds:
 - ``predictor.c``: the momentum predictor's SetMatrix / SetVectors,
   DeltaGetValues and the tail of PredictingUVW, with a Jacobi BiCGStab;
 - ``vtr.py``: the VTK RectilinearGrid writer;
-- ``clsvof.c``: ComputeUVWLiquidField, the first piece of the CLSVOF module
-  (no GPU counterpart yet).
+- ``clsvof.c``: ComputeUVWLiquidField and Interface_Reconstruct, the first
+  pieces of the CLSVOF module (no GPU counterpart yet).
 
 Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline legs of
 ``bench.py`` use it, and only as the checker or the timed CPU path.
@@ -78,6 +78,9 @@ def lib():
         L.oracle_convert_coord.restype = C.c_double
         DP3 = dp * 3
         L.oracle_uvw_liquid_field.argtypes = [C.c_int, C.c_int, C.c_int] + [dp] * 8 + [DP3] * 9
+        L.oracle_find_distance.argtypes = [C.c_double] * 7
+        L.oracle_find_distance.restype = C.c_double
+        L.oracle_interface_reconstruct.argtypes = [C.c_int, C.c_int, C.c_int] + [dp] * 12
         _lib = L
     return _lib
 
@@ -345,3 +348,20 @@ def uvw_liquid_field(pgrid, pcell, vgrids, vcells):
                                   P(pcell["nxl"]), P(pcell["nyl"]), P(pcell["nzl"]), P(pcell["vofl"]),
                                   g3(0), g3(1), g3(2), arr3("phil"), arr3("nxl"), arr3("nyl"), arr3("nzl"),
                                   arr3("vofl"), arr3("vof"))
+
+
+def find_distance(dx, dy, dz, nx, ny, nz, f):
+    """Find_Distance (Clsvof.f90:1311-1378) of one box."""
+    return lib().oracle_find_distance(dx, dy, dz, nx, ny, nz, f)
+
+
+def interface_reconstruct(centres, spacings, vfl, phi):
+    """Interface_Reconstruct (Clsvof.f90:1216-1309).  ``centres``: the P
+    grid's x, y, z; ``spacings``: dx, dy, dz (interior arrays); ``vfl``,
+    ``phi`` ghosted.  Returns the ghosted nx, ny, nz, dis."""
+    I, J, K = spacings[0].shape
+    shp = (I + 2, J + 2, K + 2)
+    out = [np.zeros(shp, order="F") for _ in range(4)]
+    lib().oracle_interface_reconstruct(I, J, K, *(_dp(a) for a in centres), *(_dp(a) for a in spacings),
+                                       _dp(vfl), _dp(phi), *(_dp(a) for a in out))
+    return out

@@ -137,3 +137,52 @@ def test_v_and_w_cells_follow_the_reference_lines(fam):
             right = dx * dy * dc - vf(dx, dy, dc, *n1, _conv(dx, dy, dc, *n1, phn))
         want = (left + right) / dx / dy / dz
         assert got[i, j, k] == want, (fam, i, j, k)
+
+
+def test_find_distance_inverts_volume_fraction():
+    """Find_Distance (with its cube root and Newton steps) returns the
+    corner distance at which Volume_Fraction_Calc gives back the fraction."""
+    rng = np.random.default_rng(5)
+    worst = 0.0
+    for _ in range(3000):
+        n = rng.normal(size=3)
+        n /= np.linalg.norm(n)
+        d = rng.uniform(0.5, 2.0, 3)
+        f = rng.uniform(0.001, 0.999)
+        s = O.find_distance(*d, *n, f)
+        worst = max(worst, abs(O.volume_fraction_calc(*d, *n, s) / np.prod(d) - f))
+    assert worst < 1e-10
+
+
+def test_interface_reconstruct_recovers_a_plane():
+    """A planar liquid surface: every interface cell gets the plane's unit
+    normal (phi is linear, so every difference Normal_Vector_Irre may pick
+    is exact to rounding) and a distance whose cut volume is its liquid
+    fraction; the other cells get zeros."""
+    I = J = K = 10
+    h = 1.0 / I
+    c = (np.arange(I) + 0.5) * h
+    X, Y, Z = np.meshgrid(c, c, c, indexing="ij")
+    centres = tuple(np.asfortranarray(a) for a in (X, Y, Z))
+    spacings = tuple(np.full((I, J, K), h, order="F") for _ in range(3))
+    n = np.array([0.3, -0.5, 0.81])
+    n /= np.linalg.norm(n)
+    cg = (np.arange(I + 2) - 0.5) * h
+    Xg, Yg, Zg = np.meshgrid(cg, cg, cg, indexing="ij")
+    phi = np.asfortranarray(n[0] * (Xg - 0.52) + n[1] * (Yg - 0.47) + n[2] * (Zg - 0.55))
+    # liquid (phi < 0) fraction of each cell, from the corner distance
+    s = phi + 0.5 * h * np.abs(n).sum()
+    vfl = np.asfortranarray(1.0 - W.volume_fraction_calc(h, h, h, n[0], n[1], n[2], s) / h ** 3)
+    nx, ny, nz, dis = O.interface_reconstruct(centres, spacings, vfl, phi)
+    part = (vfl > 1e-14) & (vfl < 1.0 - 1e-14)
+    inner = np.zeros_like(part)
+    inner[1:-1, 1:-1, 1:-1] = part[1:-1, 1:-1, 1:-1]
+    assert inner.sum() > 50
+    for q, a in enumerate((nx, ny, nz)):
+        np.testing.assert_allclose(a[inner], n[q], atol=1e-12)
+    for (i, j, k) in np.argwhere(inner)[:40]:
+        got = O.volume_fraction_calc(h, h, h, nx[i, j, k], ny[i, j, k], nz[i, j, k], dis[i, j, k]) / h ** 3
+        assert abs(got - vfl[i, j, k]) < 1e-10
+    far = np.zeros_like(part)
+    far[1:-1, 1:-1, 1:-1] = (vfl[1:-1, 1:-1, 1:-1] == 0.0) & (np.abs(phi[1:-1, 1:-1, 1:-1]) > 3 * h)
+    assert (nx[far] == 0).all() and (dis[far] == 0).all()
