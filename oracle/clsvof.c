@@ -2,9 +2,11 @@
  * clsvof.c -- CPU restatement of the first pieces of SIMCOFlow's CLSVOF
  * module (src/Clsvof.f90): ComputeUVWLiquidField, which derives the liquid
  * fraction and level set of the U, V, W cells from the pressure cells after
- * each interface advection (called from src/Solver.f90:209), and
+ * each interface advection (called from src/Solver.f90:209);
  * Interface_Reconstruct, the normals and plane distances every sweep of
- * Clsvof_Scheme starts from.
+ * Clsvof_Scheme starts from; and the directional sweeps X_Sweep, Y_Sweep,
+ * Z_Sweep with their geometric face fluxes, which advance the liquid
+ * fraction and the level set along one axis.
  *
  * TEST INFRASTRUCTURE ONLY: the checker for a future GPU restatement;
  * nothing in the product links or calls it.  Parity status: the reference
@@ -12,7 +14,9 @@
  * values for these routines, so the restatement is pinned by known-answer
  * tests in tests/ (a horizontal interface seen by the U cells, the direction
  * averages written through the reference's index shift, a planar interface
- * reconstructed exactly, Find_Distance inverting Volume_Fraction_Calc) and
+ * reconstructed exactly, Find_Distance inverting Volume_Fraction_Calc, a
+ * plane carried exactly by each sweep, the liquid of every line conserved
+ * up to its wall fluxes, closed forms of the sweeps' boundary faces) and
  * by an independent vectorised restatement of Volume_Fraction_Calc
  * (simcoflow3d_gb300/workloads.py volume_fraction_calc), not by reference
  * outputs.  Newton_Raphson is capped at 200 steps (the reference loops
@@ -403,4 +407,167 @@ void oracle_interface_reconstruct(int imax, int jmax, int kmax, const double *x,
                 nzz[G(i, j, k)] = n3;
                 diss[G(i, j, k)] = d1;
             }
+}
+
+/* ---- the directional sweeps (Clsvof.f90:817-1214, fluxes 1553-1688) ------ */
+
+/* East_Flux / West_Flux / North_Flux / South_Flux / Top_Flux / Bottom_Flux
+ * (1553-1688) in one: the liquid volume per unit face area that crosses the
+ * face in one step, from the cell upstream.  axis 0/1/2 = x/y/z; side +1
+ * the east/north/top face (the plane's normal component <= 0 takes the
+ * slab next to the face), -1 the west/south/bottom face (>= 0 does).      */
+static double face_flux(int axis, int side, double nxx, double nyy, double nzz, double diss, double volf, double dx,
+                        double dy, double dz, double wdt)
+{
+    if (wdt == 0.0) return 0.0;
+    const double nn = axis == 0 ? nxx : axis == 1 ? nyy : nzz;
+    const int thin = side > 0 ? nn <= 0.0 : nn >= 0.0;
+    double flux;
+    if (axis == 0) {
+        if (thin) flux = oracle_volume_fraction_calc(wdt, dy, dz, nxx, nyy, nzz, diss) / (wdt * dy * dz);
+        else flux = (volf * dx * dy * dz - oracle_volume_fraction_calc(dx - wdt, dy, dz, nxx, nyy, nzz, diss)) /
+                    (wdt * dy * dz);
+    } else if (axis == 1) {
+        if (thin) flux = oracle_volume_fraction_calc(dx, wdt, dz, nxx, nyy, nzz, diss) / (dx * wdt * dz);
+        else flux = (volf * dx * dy * dz - oracle_volume_fraction_calc(dx, dy - wdt, dz, nxx, nyy, nzz, diss)) /
+                    (dx * wdt * dz);
+    } else {
+        if (thin) flux = oracle_volume_fraction_calc(dx, dy, wdt, nxx, nyy, nzz, diss) / (dx * dy * wdt);
+        else flux = (volf * dx * dy * dz - oracle_volume_fraction_calc(dx, dy, dz - wdt, nxx, nyy, nzz, diss)) /
+                    (dx * dy * wdt);
+    }
+    return flux * wdt;
+}
+
+/* X_Sweep, Y_Sweep, Z_Sweep along `axis`, after Interface_Reconstruct:
+ *   temvf -= the divergence of the geometric VOF fluxes (a full or empty
+ *   upstream cell sends vfl*u*dt), temls -= the divergence of the level-set
+ *   fluxes u*phi_face*dt, phi_face extrapolated half a step upstream.
+ * Arrays ghosted except the spacings d* and the centres c* (interior).
+ * vel: the velocity of the axis (ghosted; vel(i) at the + face of cell i,
+ * vel(0) at the wall).  bc_vel, bc_lvs: the wall values at the - face
+ * (BCu%VarW and BCLvs%VarW for x, the S and B planes for y and z).  Each
+ * line along the axis is independent; within it the updates run in the
+ * reference's order.  Quirks kept: the VOF branch tests vel > 0 for x and
+ * y but vel >= 0 for z; at the first face, x's backward level-set
+ * difference is (phi(3)-phi(1))/2*dx(2) and z's adds where x and y
+ * subtract; at the last face z scales by dy where x and y use their own
+ * spacing.  (The operand orders of the reference's flux products, ue*lse
+ * against lsn*ve, are single commutative products and round the same.)    */
+static void sweep(int axis, const double *dx, const double *dy, const double *dz, const double *cx, const double *cy,
+                  const double *cz, const double *vfl, const double *phi, const double *nxx, const double *nyy,
+                  const double *nzz, const double *diss, const double *vel, const double *bc_vel, const double *bc_lvs,
+                  double dtv, double *temvf, double *temls)
+{
+    const int n = axis == 0 ? I : axis == 1 ? J : K;
+    const int na = axis == 0 ? J : I, nb = axis == 2 ? J : K;
+    const double *d = axis == 0 ? dx : axis == 1 ? dy : dz;
+    const double *cc = axis == 0 ? cx : axis == 1 ? cy : cz;
+    for (int a = 1; a <= na; ++a)
+        for (int b = 1; b <= nb; ++b) {
+            /* cell m of the line (a, b): x lines are (j, k), y lines (i, k),
+             * z lines (i, j) */
+#define CI(m) (axis == 0 ? (m) : a)
+#define CJ(m) (axis == 1 ? (m) : (axis == 0 ? a : b))
+#define CK(m) (axis == 2 ? (m) : b)
+#define GP(m) G(CI(m), CJ(m), CK(m))
+#define NP(m) N(CI(m), CJ(m), CK(m))
+            /* VOF */
+            for (int m = 1; m <= n - 1; ++m) {
+                const size_t g0 = GP(m), g1 = GP(m + 1), n0 = NP(m), n1 = NP(m + 1);
+                const double w = vel[g0];
+                const int down = axis == 2 ? w >= 0.0 : w > 0.0;
+                double flux;
+                if (down) {
+                    if (vfl[g0] >= 1.0 - VOFEPS || vfl[g0] <= VOFEPS) flux = vfl[g0] * w * dtv;
+                    else flux = face_flux(axis, +1, nxx[g0], nyy[g0], nzz[g0], diss[g0], vfl[g0], dx[n0], dy[n0],
+                                          dz[n0], w * dtv);
+                } else {
+                    if (vfl[g1] >= 1.0 - VOFEPS || vfl[g1] <= VOFEPS) flux = vfl[g1] * w * dtv;
+                    else flux = -face_flux(axis, -1, nxx[g1], nyy[g1], nzz[g1], diss[g1], vfl[g1], dx[n1], dy[n1],
+                                           dz[n1], -w * dtv);
+                }
+                temvf[g0] = temvf[g0] - flux / d[n0];
+                temvf[g1] = temvf[g1] + flux / d[n1];
+            }
+            {
+                const size_t g1 = GP(1), gn = GP(n);
+                const size_t gw = G(axis == 0 ? 0 : CI(1), axis == 1 ? 0 : CJ(1), axis == 2 ? 0 : CK(1));
+                double flux = vfl[g1] * vel[gw] * dtv;
+                temvf[g1] = temvf[g1] + flux / d[NP(1)];
+                flux = vfl[gn] * vel[gn] * dtv;
+                temvf[gn] = temvf[gn] - flux / d[NP(n)];
+            }
+            /* level set, the faces between cells 2..n */
+            for (int m = 2; m <= n - 1; ++m) {
+                const double w = vel[GP(m)], dm = d[NP(m)];
+                double ls;
+                if (w >= 0.0)
+                    ls = phi[GP(m)] + dm / 2.0 * (1.0 - w * dtv / dm) * (phi[GP(m + 1)] - phi[GP(m - 1)]) / (2.0 * dm);
+                else if (m <= n - 2)
+                    ls = phi[GP(m + 1)] - dm / 2.0 * (1.0 + w * dtv / dm) * (phi[GP(m + 2)] - phi[GP(m)]) / (2.0 * dm);
+                else
+                    ls = phi[GP(m + 1)] - dm / 2.0 * (1.0 + w * dtv / dm) * (phi[GP(m + 1)] - phi[GP(m)]) / dm;
+                const double flux = w * ls * dtv;
+                temls[GP(m)] = temls[GP(m)] - flux / d[NP(m)];
+                temls[GP(m + 1)] = temls[GP(m + 1)] + flux / d[NP(m + 1)];
+            }
+            /* the face between cells 1 and 2, and the wall flux */
+            {
+                const double w = vel[GP(1)];
+                double ls;
+                if (w >= 0.0) {
+                    const double den = axis == 0 ? d[NP(1)] : cc[NP(2)] - cc[NP(1)];
+                    ls = phi[GP(1)] + d[NP(1)] / 2.0 * (1.0 - w * dtv / d[NP(1)]) * (phi[GP(2)] - phi[GP(1)]) / den;
+                } else if (axis == 0) {
+                    ls = phi[GP(2)] - d[NP(2)] / 2.0 * (1.0 + w * dtv / d[NP(2)]) * (phi[GP(3)] - phi[GP(1)]) / 2.0 *
+                                          d[NP(2)];
+                } else if (axis == 1) {
+                    ls = phi[GP(2)] - d[NP(2)] / 2.0 * (1.0 + w * dtv / d[NP(2)]) * (phi[GP(3)] - phi[GP(1)]) /
+                                          (cc[NP(3)] - cc[NP(1)]);
+                } else {
+                    ls = phi[GP(2)] + d[NP(2)] / 2.0 * (1.0 + w * dtv / d[NP(2)]) * (phi[GP(3)] - phi[GP(1)]) /
+                                          (cc[NP(3)] - cc[NP(1)]);
+                }
+                double flux = ls * w * dtv;
+                temls[GP(1)] = temls[GP(1)] - flux / d[NP(1)];
+                temls[GP(2)] = temls[GP(2)] + flux / d[NP(2)];
+                const size_t bw = (size_t)(a - 1) + (size_t)(axis == 0 ? J : I) * (size_t)(b - 1);
+                flux = bc_vel[bw] * bc_lvs[bw] * dtv;
+                temls[GP(1)] = temls[GP(1)] + flux / d[NP(1)];
+            }
+            /* the last face */
+            {
+                const double w = vel[GP(n)];
+                double ls;
+                if (w > 0.0) {
+                    ls = phi[GP(n)] + d[NP(n)] / 2.0 * (1.0 - w * dtv / d[NP(n)]) * (phi[GP(n)] - phi[GP(n - 1)]) /
+                                          (cc[NP(n)] - cc[NP(n - 1)]);
+                } else {
+                    const double scale = axis == 2 ? dy[NP(n - 1)] : d[NP(n - 1)];
+                    ls = phi[GP(n)] - d[NP(n - 1)] / 2.0 * (1.0 + w * dtv / scale) * (phi[GP(n)] - phi[GP(n - 1)]) /
+                                          (cc[NP(n)] - cc[NP(n - 1)]);
+                }
+                const double flux = ls * w * dtv;
+                temls[GP(n)] = temls[GP(n)] - flux / d[NP(n)];
+            }
+#undef CI
+#undef CJ
+#undef CK
+#undef GP
+#undef NP
+        }
+}
+
+/* One sweep as Clsvof_Scheme calls it: Interface_Reconstruct of vfl, phi
+ * into the normals and distances, then the sweep of `axis` into temvf,
+ * temls (which hold the copies of vfl, phi on entry).                      */
+void oracle_clsvof_sweep(int imax, int jmax, int kmax, int axis, const double *x, const double *y, const double *z,
+                         const double *dx, const double *dy, const double *dz, const double *vfl, const double *phi,
+                         const double *vel, const double *bc_vel, const double *bc_lvs, double dtv, double *nxx,
+                         double *nyy, double *nzz, double *diss, double *temvf, double *temls)
+{
+    oracle_interface_reconstruct(imax, jmax, kmax, x, y, z, dx, dy, dz, vfl, phi, nxx, nyy, nzz, diss);
+    I = imax; J = jmax; K = kmax;
+    sweep(axis, dx, dy, dz, x, y, z, vfl, phi, nxx, nyy, nzz, diss, vel, bc_vel, bc_lvs, dtv, temvf, temls);
 }

@@ -9,8 +9,9 @@ rebuilds:
 - ``predictor.c``: the momentum predictor's SetMatrix / SetVectors,
   DeltaGetValues and the tail of PredictingUVW, with a Jacobi BiCGStab;
 - ``vtr.py``: the VTK RectilinearGrid writer;
-- ``clsvof.c``: ComputeUVWLiquidField and Interface_Reconstruct, the first
-  pieces of the CLSVOF module (no GPU counterpart yet).
+- ``clsvof.c``: ComputeUVWLiquidField, Interface_Reconstruct and the
+  directional sweeps X_Sweep / Y_Sweep / Z_Sweep, the first pieces of the
+  CLSVOF module (no GPU counterpart yet).
 
 Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline legs of
 ``bench.py`` use it, and only as the checker or the timed CPU path.
@@ -81,6 +82,7 @@ def lib():
         L.oracle_find_distance.argtypes = [C.c_double] * 7
         L.oracle_find_distance.restype = C.c_double
         L.oracle_interface_reconstruct.argtypes = [C.c_int, C.c_int, C.c_int] + [dp] * 12
+        L.oracle_clsvof_sweep.argtypes = [C.c_int] * 4 + [dp] * 11 + [C.c_double] + [dp] * 6
         _lib = L
     return _lib
 
@@ -365,3 +367,22 @@ def interface_reconstruct(centres, spacings, vfl, phi):
     lib().oracle_interface_reconstruct(I, J, K, *(_dp(a) for a in centres), *(_dp(a) for a in spacings),
                                        _dp(vfl), _dp(phi), *(_dp(a) for a in out))
     return out
+
+
+def clsvof_sweep(axis, centres, spacings, vfl, phi, vel, bc_vel, bc_lvs, dtv):
+    """One directional sweep of Clsvof_Scheme: Interface_Reconstruct, then
+    X_Sweep / Y_Sweep / Z_Sweep (Clsvof.f90:817-1214) for ``axis`` 0/1/2.
+    ``vfl``, ``phi``, ``vel`` ghosted; ``bc_vel``, ``bc_lvs`` the wall planes
+    at the low face of the axis ((J, K) for x, (I, K) for y, (I, J) for z).
+    Returns the swept (temvf, temls), ghosted, and the normals nx, ny, nz,
+    dis the sweep used."""
+    I, J, K = spacings[0].shape
+    shp = (I + 2, J + 2, K + 2)
+    rec = [np.zeros(shp, order="F") for _ in range(4)]
+    temvf = np.array(vfl, order="F", copy=True)
+    temls = np.array(phi, order="F", copy=True)
+    args = [np.asfortranarray(a, dtype=np.float64) for a in (vel, bc_vel, bc_lvs)]
+    lib().oracle_clsvof_sweep(I, J, K, int(axis), *(_dp(a) for a in centres), *(_dp(a) for a in spacings),
+                              _dp(vfl), _dp(phi), *(_dp(a) for a in args), float(dtv),
+                              *(_dp(a) for a in rec), _dp(temvf), _dp(temls))
+    return temvf, temls, rec

@@ -1,7 +1,9 @@
-"""The oracle of ComputeUVWLiquidField (oracle/clsvof.c), the first piece of
-the CLSVOF module, against closed forms, an independent vectorised
-Volume_Fraction_Calc, and the reference's index shift of the velocity cells'
-direction averages.  CPU only (no GPU counterpart yet)."""
+"""The oracle of the first pieces of the CLSVOF module (oracle/clsvof.c):
+ComputeUVWLiquidField, Interface_Reconstruct and the directional sweeps,
+against closed forms, an independent vectorised Volume_Fraction_Calc, the
+reference's index shift of the velocity cells' direction averages, exact
+translation of a plane and conservation along each swept line.  CPU only
+(no GPU counterpart yet)."""
 import numpy as np
 import pytest
 
@@ -186,3 +188,131 @@ def test_interface_reconstruct_recovers_a_plane():
     far = np.zeros_like(part)
     far[1:-1, 1:-1, 1:-1] = (vfl[1:-1, 1:-1, 1:-1] == 0.0) & (np.abs(phi[1:-1, 1:-1, 1:-1]) > 3 * h)
     assert (nx[far] == 0).all() and (dis[far] == 0).all()
+
+
+# ---- the directional sweeps (X_Sweep / Y_Sweep / Z_Sweep) ----------------
+
+_SHAPE = (12, 9, 10)
+
+
+def _plane_case(axis, n, x0, shape=_SHAPE):
+    """Cells of the unit box (spacing 1/I, 1/J, 1/K) cut by the plane
+    n.(x - x0 e_axis) = 0, liquid on the phi < 0 side: centres, spacings,
+    the ghosted phi and the exact liquid fractions."""
+    I, J, K = shape
+    h = np.array([1.0 / I, 1.0 / J, 1.0 / K])
+    n = np.asarray(n, float) / np.linalg.norm(n)
+    cs = [(np.arange(m) + 0.5) * hq for m, hq in zip(shape, h)]
+    cg = [(np.arange(m + 2) - 0.5) * hq for m, hq in zip(shape, h)]
+    centres = tuple(np.asfortranarray(a) for a in np.meshgrid(*cs, indexing="ij"))
+    spacings = tuple(np.full(shape, hq, order="F") for hq in h)
+    Xg = np.meshgrid(*cg, indexing="ij")
+    off = np.zeros(3)
+    off[axis] = x0
+
+    def phi_at(shift):
+        return np.asfortranarray(sum(n[q] * (Xg[q] - off[q] - (shift if q == axis else 0.0)) for q in range(3)))
+
+    def fractions(phi):
+        s = phi + 0.5 * (np.abs(n) * h).sum()
+        return np.asfortranarray(1.0 - W.volume_fraction_calc(h[0], h[1], h[2], n[0], n[1], n[2], s) / h.prod())
+
+    return centres, spacings, h, n, phi_at, fractions
+
+
+def _wall(a, axis):
+    """The ghost plane at the low wall of ``axis``, interior in the others."""
+    idx = [slice(1, -1)] * 3
+    idx[axis] = 0
+    return np.asfortranarray(a[tuple(idx)])
+
+
+@pytest.mark.parametrize("axis", [0, 1, 2])
+@pytest.mark.parametrize("tilt", [False, True])
+def test_sweep_translates_a_plane(axis, tilt):
+    """A uniform velocity along the axis carries a plane exactly: the
+    geometric fluxes cut the upstream cells by the reconstructed plane, so
+    each new liquid fraction is the fraction of the plane moved by u dt;
+    the level set, linear, drops by u dt times its slope in every cell when
+    the wall value is the level set at the wall half a step upstream."""
+    n = [0.0, 0.0, 0.0]
+    n[axis] = 1.0
+    if tilt:
+        n[(axis + 1) % 3], n[(axis + 2) % 3] = 0.15, -0.1
+    centres, spacings, h, nu, phi_at, fractions = _plane_case(axis, n, 0.57)
+    u, dt = 0.7, 0.35 * h[axis] / 0.7
+    phi = phi_at(0.0)
+    vfl = fractions(phi)
+    vel = np.full(phi.shape, u, order="F")
+    bc_vel = _wall(vel, axis)
+    wall_phi = _wall(phi, axis) + 0.5 * h[axis] * nu[axis]
+    bc_lvs = np.asfortranarray(wall_phi - nu[axis] * u * dt / 2.0)
+    temvf, temls, _ = O.clsvof_sweep(axis, centres, spacings, vfl, phi, vel, bc_vel, bc_lvs, dt)
+    moved = phi_at(u * dt)
+    inner = (slice(1, -1),) * 3
+    part = (vfl[inner] > 0.0) & (vfl[inner] < 1.0)
+    assert part.sum() > 20
+    np.testing.assert_allclose(temvf[inner], fractions(moved)[inner], atol=1e-12)
+    np.testing.assert_allclose(temls[inner], moved[inner], atol=1e-13)
+
+
+@pytest.mark.parametrize("axis", [0, 1, 2])
+def test_sweep_conserves_liquid_along_each_line(axis):
+    """Every interior face's VOF flux leaves one cell and enters the next,
+    so along a line the liquid changes only by the two wall fluxes
+    vfl(1) u(0) dt and vfl(n) u(n) dt, whatever the velocities (both signs
+    here, so the east and the west cuts both run)."""
+    centres, spacings, h, _, phi_at, fractions = _plane_case(axis, [0.45, -0.6, 0.66], 0.5)
+    phi = phi_at(0.0)
+    vfl = fractions(phi)
+    rng = np.random.default_rng(5 + axis)
+    vel = np.asfortranarray(rng.uniform(-1.0, 1.0, phi.shape))
+    dt = 0.4 * h.min()
+    wall = np.zeros(_wall(vel, axis).shape, order="F")
+    temvf, _, _ = O.clsvof_sweep(axis, centres, spacings, vfl, phi, vel, wall, wall, dt)
+    inner = (slice(1, -1),) * 3
+    gained = np.moveaxis((temvf - vfl)[inner], axis, 0).sum(axis=0) * h[axis]
+    vm = np.moveaxis(vel, axis, 0)
+    fm = np.moveaxis(vfl, axis, 0)
+    # the other two axes keep their interior order after moveaxis
+    lo = fm[1, 1:-1, 1:-1] * vm[0, 1:-1, 1:-1] * dt
+    hi = fm[-2, 1:-1, 1:-1] * vm[-2, 1:-1, 1:-1] * dt
+    np.testing.assert_allclose(gained, lo - hi, atol=1e-14)
+    assert ((vfl[inner] > 0) & (vfl[inner] < 1)).sum() > 20
+
+
+@pytest.mark.parametrize("axis", [0, 1, 2])
+def test_sweep_backward_level_set_keeps_the_reference_faces(axis):
+    """u < 0 on a level set of unit slope along the axis: the faces between
+    cells 2..n take the upwind value exactly, the first face takes the
+    reference's x / y / z forms (x divides by 2 and multiplies by dx(2), y
+    is the exact upwind value, z adds the correction), and the last face
+    extrapolates from the face below, which leaves cell n as it was when
+    its spacings are all equal (x, y) and scales by dy for z."""
+    n = [0.0, 0.0, 0.0]
+    n[axis] = 1.0
+    centres, spacings, h, _, phi_at, fractions = _plane_case(axis, n, 0.57)
+    u = -0.8
+    dt = 0.3 * h.min() / 0.8
+    phi = phi_at(0.0)
+    vfl = fractions(phi)
+    vel = np.full(phi.shape, u, order="F")
+    bc_lvs = np.asfortranarray(_wall(phi, axis) * 0.0 + 0.25)
+    _, temls, _ = O.clsvof_sweep(axis, centres, spacings, vfl, phi, vel, _wall(vel, axis), bc_lvs, dt)
+    hd = h[axis]
+    p = np.moveaxis(phi, axis, 0)[1:-1, 1:-1, 1:-1]
+    t = np.moveaxis(temls, axis, 0)[1:-1, 1:-1, 1:-1]
+    m = p.shape[0]
+    a = hd / 2.0 * (1.0 + u * dt / hd)
+    face = {q: p[q + 1] - a for q in range(1, m - 1)}   # 0-based: the face between cells q and q+1
+    first = {0: p[1] - a * hd * hd, 1: p[1] - a, 2: p[1] + a}[axis]
+    scale = h[1] if axis == 2 else hd
+    last = p[m - 1] - hd / 2.0 * (1.0 + u * dt / scale)
+    f = lambda ls: u * ls * dt / hd
+    np.testing.assert_allclose(t[0], p[0] - f(first) + u * 0.25 * dt / hd, atol=1e-13)
+    np.testing.assert_allclose(t[1], p[1] + f(first) - f(face[1]), atol=1e-13)
+    for q in range(2, m - 1):
+        np.testing.assert_allclose(t[q], p[q] - u * dt, atol=1e-13)
+    np.testing.assert_allclose(t[m - 1], p[m - 1] + f(face[m - 2]) - f(last), atol=1e-13)
+    if axis != 2:
+        np.testing.assert_allclose(t[m - 1], p[m - 1], atol=1e-13)
