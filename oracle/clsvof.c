@@ -4,9 +4,11 @@
  * fraction and level set of the U, V, W cells from the pressure cells after
  * each interface advection (called from src/Solver.f90:209);
  * Interface_Reconstruct, the normals and plane distances every sweep of
- * Clsvof_Scheme starts from; and the directional sweeps X_Sweep, Y_Sweep,
+ * Clsvof_Scheme starts from; the directional sweeps X_Sweep, Y_Sweep,
  * Z_Sweep with their geometric face fluxes, which advance the liquid
- * fraction and the level set along one axis.
+ * fraction and the level set along one axis; BoundaryConditionLvsVof;
+ * Redistance_Levelset; and Clsvof_Scheme itself, the six split sub-steps
+ * of one time step.
  *
  * TEST INFRASTRUCTURE ONLY: the checker for a future GPU restatement;
  * nothing in the product links or calls it.  Parity status: the reference
@@ -16,11 +18,14 @@
  * averages written through the reference's index shift, a planar interface
  * reconstructed exactly, Find_Distance inverting Volume_Fraction_Calc, a
  * plane carried exactly by each sweep, the liquid of every line conserved
- * up to its wall fluxes, closed forms of the sweeps' boundary faces) and
- * by an independent vectorised restatement of Volume_Fraction_Calc
- * (simcoflow3d_gb300/workloads.py volume_fraction_calc), not by reference
- * outputs.  Newton_Raphson is capped at 200 steps (the reference loops
- * without a cap).
+ * up to its wall fluxes, closed forms of the sweeps' boundary faces, a
+ * plane carried through a whole step, a drop's volume kept in a shear) and
+ * by independent restatements: a vectorised Volume_Fraction_Calc
+ * (simcoflow3d_gb300/workloads.py volume_fraction_calc), a gather form of
+ * Redistance_Levelset and a numpy BoundaryConditionLvsVof (tests/), which
+ * the oracle matches bit for bit where the arithmetic is alike.  Not by
+ * reference outputs.  Newton_Raphson is capped at 200 steps (the reference
+ * loops without a cap).
  *
  * Loops and expressions keep the reference's order; built with
  * -ffp-contract=off.  Fortran x**2.d0 is x*x (gfortran folds it exactly) and
@@ -39,12 +44,19 @@
  *    the U cells' shifts by -dx/2 (208-209).
  *  - ComputeVelocityCellLiquidField's clamp of vof + vofL <= 1 (314-322)
  *    acts on the previous vofL, which the loops then overwrite.
+ *  - The sweeps' own quirks are listed above sweep(); Shortest_Point_2d's
+ *    y-face case divides by |nzz| where it solves for x (2026), which can
+ *    put band cells under their true distance; BoundaryConditionLvsVof
+ *    builds the ghost level set from the fluid normals (PCell%nx, not
+ *    nxL), the north ghost subtracting like the south (2142-2143).
  *
  * Indexing (column-major, i fastest): ghosted (0:I+1,0:J+1,0:K+1), interior
  * (1:I,1:J,1:K).
  */
 #include <math.h>
 #include <stddef.h>
+#include <stdlib.h>
+#include <string.h>
 
 static int I, J, K;
 #define G(i, j, k) ((size_t)(i) + (size_t)(I + 2) * ((size_t)(j) + (size_t)(J + 2) * (size_t)(k)))
@@ -570,4 +582,402 @@ void oracle_clsvof_sweep(int imax, int jmax, int kmax, int axis, const double *x
     oracle_interface_reconstruct(imax, jmax, kmax, x, y, z, dx, dy, dz, vfl, phi, nxx, nyy, nzz, diss);
     I = imax; J = jmax; K = kmax;
     sweep(axis, dx, dy, dz, x, y, z, vfl, phi, nxx, nyy, nzz, diss, vel, bc_vel, bc_lvs, dtv, temvf, temls);
+}
+
+/* ---- redistancing (Clsvof.f90:1689-1889, helpers 1904-1959, 1961-2060) --- */
+
+static const int BAND_WIDTH = 4;   /* Clsvof.f90:31 */
+static const int NV = 6;           /* Clsvof.f90:31 */
+
+static double sgn(double a) { return copysign(1.0, a); }   /* dsign(1.d0, a) */
+
+/* Isinsidecell (1904-1916) and Isinsiderect (1918-1927). */
+static int inside_cell(double xp, double yp, double zp, double dx, double dy, double dz)
+{
+    return -0.5 * dx <= xp && xp <= 0.5 * dx && -0.5 * dy <= yp && yp <= 0.5 * dy && -0.5 * dz <= zp &&
+           zp <= 0.5 * dz;
+}
+static int inside_rect(double d1, double d2, double r10, double r11, double r20, double r21)
+{
+    return r10 <= d1 && d1 <= r11 && r20 <= d2 && d2 <= r21;
+}
+
+/* Iscutface (1929-1959): does the plane cross the face at `fp` normal to
+ * axis `cas` (its four corners not all on one side). */
+static int cut_face(double fp, double nxx, double nyy, double nzz, double diss, double dx, double dy, double dz,
+                    int cas)
+{
+    double p1, p2, p3, p4;
+    if (cas == 1) {
+        p1 = fp * nxx - 0.5 * dy * nyy - 0.5 * dz * nzz + diss;
+        p2 = fp * nxx - 0.5 * dy * nyy + 0.5 * dz * nzz + diss;
+        p3 = fp * nxx + 0.5 * dy * nyy + 0.5 * dz * nzz + diss;
+        p4 = fp * nxx + 0.5 * dy * nyy - 0.5 * dz * nzz + diss;
+    } else if (cas == 2) {
+        p1 = -0.5 * dx * nxx + fp * nyy - 0.5 * dz * nzz + diss;
+        p2 = -0.5 * dx * nxx + fp * nyy + 0.5 * dz * nzz + diss;
+        p3 = 0.5 * dx * nxx + fp * nyy + 0.5 * dz * nzz + diss;
+        p4 = 0.5 * dx * nxx + fp * nyy - 0.5 * dz * nzz + diss;
+    } else {
+        p1 = -0.5 * dx * nxx - 0.5 * dy * nyy + fp * nzz + diss;
+        p2 = -0.5 * dx * nxx + 0.5 * dy * nyy + fp * nzz + diss;
+        p3 = 0.5 * dx * nxx + 0.5 * dy * nyy + fp * nzz + diss;
+        p4 = 0.5 * dx * nxx - 0.5 * dy * nyy + fp * nzz + diss;
+    }
+    return !(p1 * p2 >= 0.0 && p2 * p3 >= 0.0 && p3 * p4 >= 0.0 && p4 * p1 >= 0.0);
+}
+
+/* Shortest_Point_2d (1961-2060): the point of the plane's trace on the face
+ * normal to axis `cas` (whose coordinate the caller has set) nearest the
+ * centre of the cell (ii, jj, kk) away; the other two coordinates are
+ * written.  Kept: the y-face case divides by |nzz| where it solves for x. */
+static void shortest_point_2d(double nx1, double ny1, double nz1, double dis1, int ii, int jj, int kk, int cas,
+                              double dx, double dy, double dz, double *xs, double *ys, double *zs)
+{
+    const double epsi = 1.0e-30;
+    if (cas == 1) {
+        const double temp = sqrt(ny1 * ny1 + nz1 * nz1 + epsi * epsi);
+        const double nyy = ny1 / temp, nzz = nz1 / temp, diss = dis1 / temp;
+        const double dij1 = nyy * dy * (double)jj + nzz * dz * (double)kk + diss;
+        const double yp = dy * (double)jj - dij1 * nyy, zp = dz * (double)kk - dij1 * nzz;
+        if (inside_rect(yp, zp, -0.5 * dy, 0.5 * dy, -0.5 * dz, 0.5 * dz)) {
+            *ys = yp;
+            *zs = zp;
+            return;
+        }
+        const double yoff = fmax(fabs(yp) - 0.5 * dy, 0.0), zoff = fmax(fabs(zp) - 0.5 * dz, 0.0);
+        const double yfc = sgn(yp) * 0.5 * dy, zfc = sgn(zp) * 0.5 * dz;
+        if (yoff * fabs(nyy) > zoff * fabs(nzz)) {
+            *ys = yfc;
+            *zs = (diss + nyy * *ys) / (sgn(-nzz) * fmax(fabs(nzz), TOLPAR));
+        } else {
+            *zs = zfc;
+            *ys = (diss + nzz * *zs) / (sgn(-nyy) * fmax(fabs(nyy), TOLPAR));
+        }
+    } else if (cas == 2) {
+        const double temp = sqrt(nx1 * nx1 + nz1 * nz1 + epsi * epsi);
+        const double nxx = nx1 / temp, nzz = nz1 / temp, diss = dis1 / temp;
+        const double dij1 = nxx * dx * (double)ii + nzz * dz * (double)kk + diss;
+        const double xp = dx * (double)ii - dij1 * nxx, zp = dz * (double)kk - dij1 * nzz;
+        if (inside_rect(xp, zp, -0.5 * dx, 0.5 * dx, -0.5 * dz, 0.5 * dz)) {
+            *xs = xp;
+            *zs = zp;
+            return;
+        }
+        const double xoff = fmax(fabs(xp) - 0.5 * dx, 0.0), zoff = fmax(fabs(zp) - 0.5 * dz, 0.0);
+        const double xfc = sgn(xp) * 0.5 * dx, zfc = sgn(zp) * 0.5 * dz;
+        if (xoff * fabs(nxx) > zoff * fabs(nzz)) {
+            *xs = xfc;
+            *zs = (diss + nxx * *xs) / (sgn(-nzz) * fmax(fabs(nzz), TOLPAR));
+        } else {
+            *zs = zfc;
+            *xs = (diss + nzz * *zs) / (sgn(-nxx) * fmax(fabs(nzz), TOLPAR));
+        }
+    } else {
+        const double temp = sqrt(nx1 * nx1 + ny1 * ny1 + epsi * epsi);
+        const double nxx = nx1 / temp, nyy = ny1 / temp, diss = dis1 / temp;
+        const double dij1 = nxx * dx * (double)ii + nyy * dy * (double)jj + diss;
+        const double xp = dx * (double)ii - dij1 * nxx, yp = dy * (double)jj - dij1 * nyy;
+        if (inside_rect(xp, yp, -0.5 * dx, 0.5 * dx, -0.5 * dy, 0.5 * dy)) {
+            *xs = xp;
+            *ys = yp;
+            return;
+        }
+        const double xoff = fmax(fabs(xp) - 0.5 * dx, 0.0), yoff = fmax(fabs(yp) - 0.5 * dy, 0.0);
+        const double xfc = sgn(xp) * 0.5 * dx, yfc = sgn(yp) * 0.5 * dy;
+        if (xoff * fabs(nxx) > yoff * fabs(nyy)) {
+            *xs = xfc;
+            *ys = (diss + nxx * *xs) / (sgn(-nyy) * fmax(fabs(nyy), TOLPAR));
+        } else {
+            *ys = yfc;
+            *xs = (diss + nyy * *ys) / (sgn(-nxx) * fmax(fabs(nxx), TOLPAR));
+        }
+    }
+}
+
+/* The distance from the centre of the cell (ii, jj, kk) away to the plane
+ * piece n.x + diss = 0 of an interface cell, as the band loop of
+ * Redistance_Levelset measures it (1740-1861): the facing boundary point
+ * when it lies across the plane from that centre, else the foot of the
+ * perpendicular when it falls inside the cell, else the nearest point of
+ * the plane's trace on the face it leaves through.  `side` is phi at the
+ * target centre. */
+static double band_distance(double nxx, double nyy, double nzz, double diss, int ii, int jj, int kk, double dx,
+                            double dy, double dz, double side)
+{
+    const int l = ii < -1 ? -1 : ii > 1 ? 1 : ii;
+    const int m = jj < -1 ? -1 : jj > 1 ? 1 : jj;
+    const int n = kk < -1 ? -1 : kk > 1 ? 1 : kk;
+    const double xv = dx * (double)l / 2.0, yv = dy * (double)m / 2.0, zv = dz * (double)n / 2.0;
+    const double dv = nxx * xv + nyy * yv + nzz * zv + diss;
+    const double X = dx * (double)ii, Y = dy * (double)jj, Z = dz * (double)kk;
+    if (dv * sgn(side) <= 0.0) return sqrt((X - xv) * (X - xv) + (Y - yv) * (Y - yv) + (Z - zv) * (Z - zv));
+    const double dij1 = nxx * dx * (double)ii + nyy * dy * (double)jj + nzz * dz * (double)kk + diss;
+    const double xp = X - dij1 * nxx, yp = Y - dij1 * nyy, zp = Z - dij1 * nzz;
+    if (inside_cell(xp, yp, zp, dx, dy, dz))
+        return sqrt((X - xp) * (X - xp) + (Y - yp) * (Y - yp) + (Z - zp) * (Z - zp));
+    const double xoff = fmax(fabs(xp) - 0.5 * dx, 0.0);
+    const double yoff = fmax(fabs(yp) - 0.5 * dy, 0.0);
+    const double zoff = fmax(fabs(zp) - 0.5 * dz, 0.0);
+    const double xfc = sgn(xp) * 0.5 * dx, yfc = sgn(yp) * 0.5 * dy, zfc = sgn(zp) * 0.5 * dz;
+    const double ax = xoff * fabs(nxx), ay = yoff * fabs(nyy), az = zoff * fabs(nzz);
+    double xs = 0.0, ys = 0.0, zs = 0.0, diss1;
+    int cas;
+    if (ax >= ay && ax >= az) {
+        if (cut_face(xfc, nxx, nyy, nzz, diss, dx, dy, dz, 1)) {
+            xs = xfc; diss1 = nxx * xs + diss; cas = 1;
+        } else if (ay > az) {
+            ys = yfc; diss1 = nyy * ys + diss; cas = 2;
+        } else {
+            zs = zfc; diss1 = nzz * zs + diss; cas = 3;
+        }
+        shortest_point_2d(nxx, nyy, nzz, diss1, ii, jj, kk, cas, dx, dy, dz, &xs, &ys, &zs);
+    }
+    if (ay >= ax && ay >= az) {
+        if (cut_face(yfc, nxx, nyy, nzz, diss, dx, dy, dz, 2)) {
+            ys = yfc; diss1 = nyy * ys + diss; cas = 2;
+        } else if (ax > az) {
+            xs = xfc; diss1 = nxx * xs + diss; cas = 1;
+        } else {
+            zs = zfc; diss1 = nzz * zs + diss; cas = 3;
+        }
+        shortest_point_2d(nxx, nyy, nzz, diss1, ii, jj, kk, cas, dx, dy, dz, &xs, &ys, &zs);
+    }
+    if (az >= ax && az >= ay) {
+        if (cut_face(zfc, nxx, nyy, nzz, diss, dx, dy, dz, 3)) {
+            zs = zfc; diss1 = nzz * zs + diss; cas = 3;
+        } else if (ax > ay) {
+            xs = xfc; diss1 = nxx * xs + diss; cas = 1;
+        } else {
+            ys = yfc; diss1 = nyy * ys + diss; cas = 2;
+        }
+        shortest_point_2d(nxx, nyy, nzz, diss1, ii, jj, kk, cas, dx, dy, dz, &xs, &ys, &zs);
+    }
+    return sqrt((X - xs) * (X - xs) + (Y - ys) * (Y - ys) + (Z - zs) * (Z - zs));
+}
+
+/* Redistance_Levelset (1689-1889).  Each interface cell (1e-15 < vfl <
+ * 1-1e-15) takes sign(0.5-vfl)|dis| (dis from its centre); each full or
+ * empty cell within BAND_WIDTH cells of an interface cell (in every index)
+ * takes sign(0.5-vfl) times the least band_distance over those interface
+ * cells; every other cell sign(0.5-vfl)(BAND_WIDTH+1) dx sqrt(3).  A full or
+ * empty cell is never an interface cell and only its running minimum is
+ * written, so the result does not depend on the loop order (the reference
+ * loops i, j, k over the interface cells and ii, jj, kk over the band).
+ * The distances use the interface cell's spacings.  phi is read (its sign
+ * at the target) before any of it is written.                               */
+static void redistance(const double *dx, const double *dy, const double *dz, const double *vfl, double *phi,
+                       const double *nxx, const double *nyy, const double *nzz, const double *dis, double *aux,
+                       int *fix)
+{
+    const double epsi = 1.0e-15;
+    const size_t nin = (size_t)I * J * K;
+    for (size_t q = 0; q < nin; ++q) { aux[q] = 1.0e4; fix[q] = 0; }
+    for (int i = 1; i <= I; ++i)
+        for (int j = 1; j <= J; ++j)
+            for (int k = 1; k <= K; ++k) {
+                const size_t g = G(i, j, k), c = N(i, j, k);
+                if (!(0.0 + epsi < vfl[g] && vfl[g] < 1.0 - epsi)) continue;
+                aux[c] = sgn(0.5 - vfl[g]) * fabs(dis[g]);
+                fix[c] = 1;
+                for (int ii = -BAND_WIDTH; ii <= BAND_WIDTH; ++ii)
+                    for (int jj = -BAND_WIDTH; jj <= BAND_WIDTH; ++jj)
+                        for (int kk = -BAND_WIDTH; kk <= BAND_WIDTH; ++kk) {
+                            const int ti = i + ii, tj = j + jj, tk = k + kk;
+                            if (!(1 <= ti && ti <= I && 1 <= tj && tj <= J && 1 <= tk && tk <= K)) continue;
+                            const size_t tg = G(ti, tj, tk), tc = N(ti, tj, tk);
+                            if (!(vfl[tg] < 0.0 + epsi || vfl[tg] > 1.0 - epsi)) continue;
+                            fix[tc] = 1;
+                            const double deuc = band_distance(nxx[g], nyy[g], nzz[g], dis[g], ii, jj, kk, dx[c],
+                                                              dy[c], dz[c], phi[tg]);
+                            const double cur = fabs(aux[tc]);
+                            aux[tc] = sgn(0.5 - vfl[tg]) * (deuc < cur ? deuc : cur);
+                        }
+            }
+    for (int i = 1; i <= I; ++i)
+        for (int j = 1; j <= J; ++j)
+            for (int k = 1; k <= K; ++k) {
+                const size_t g = G(i, j, k), c = N(i, j, k);
+                if (fix[c] == 1) phi[g] = aux[c];
+                else phi[g] = (double)(BAND_WIDTH + 1) * dx[c] * sqrt(3.0) * sgn(0.5 - vfl[g]);
+            }
+}
+
+/* ---- the boundary planes and the scheme (Clsvof.f90:355-798, 2087-2221) -- */
+
+/* One CLSVOF time step, Clsvof_Scheme's arguments flattened.  Arrays:
+ * x..dz interior; vofl, phil, nxl, nyl, nzl, nx, ny, nz, u, v, w ghosted;
+ * the wall planes face by face W, E, S, N, B, T, (J,K) for W/E, (I,K) for
+ * S/N, (I,J) for B/T, numbered like the sweeps' bc planes.                  */
+struct oracle_clsvof_args {
+    int imax, jmax, kmax;
+    const double *x, *y, *z, *dx, *dy, *dz;
+    double *vofl, *phil;                 /* in/out */
+    double *nxl, *nyl, *nzl;             /* in/out: the liquid normals */
+    const double *nx, *ny, *nz;          /* the fluid normals (the ghost level set uses them) */
+    const double *u, *v, *w;             /* face velocities */
+    const double *bc_vel[3];             /* BCu%VarW, BCv%VarS, BCw%VarB */
+    double *lvs_bc[6];                   /* BCLvs%Var*: in (W, S, B feed the sweeps) and out */
+    double *vof_bc[6];                   /* BCVof%Var*: out */
+    int lvs_flag[6], vof_flag[6];        /* 0 Dirichlet, else Neumann */
+    double lvs_const[6], vof_const[6];
+    double dt;
+};
+
+/* TypicalBC (BoundaryFunction.f90) over one face: Dirichlet const, else the
+ * inner value less const*d/2 (d negative on the E, N, T faces). */
+static double typical_bc(int flag, double cst, double var, double d)
+{
+    return flag == 0 ? cst : var - cst * d / 2.0;
+}
+
+/* BoundaryConditionLvsVof (2087-2221).  The level-set planes: W and E take
+ * LvSBoundaryCondition, phiL - nxL*d/2 with d = +dx, -dx (BCLvsW/E are
+ * passed the liquid normals), S, N, B, T take TypicalBC; the level-set
+ * ghosts are phiL -/+ the FLUID normal times the spacing, and the N ghost
+ * subtracts like S (kept).  Then the VOF planes (TypicalBC) and the VOF
+ * ghosts (copies).  Ghost edges and corners are not touched.               */
+static void boundary_lvs_vof(const struct oracle_clsvof_args *a)
+{
+    double *phil = a->phil, *vofl = a->vofl;
+    for (int pass = 0; pass < 2; ++pass) {
+        double *f = pass == 0 ? phil : vofl;
+        double *const *bc = pass == 0 ? a->lvs_bc : a->vof_bc;
+        const int *flag = pass == 0 ? a->lvs_flag : a->vof_flag;
+        const double *cst = pass == 0 ? a->lvs_const : a->vof_const;
+        for (int j = 1; j <= J; ++j)
+            for (int k = 1; k <= K; ++k) {
+                const size_t b = (size_t)(j - 1) + (size_t)J * (k - 1);
+                const size_t g1 = G(1, j, k), gI = G(I, j, k);
+                const double d1 = a->dx[N(1, j, k)], dI = a->dx[N(I, j, k)];
+                bc[0][b] = typical_bc(flag[0], cst[0], f[g1], d1);
+                if (pass == 0) bc[0][b] = f[g1] - a->nxl[g1] * d1 / 2.0;
+                f[G(0, j, k)] = pass == 0 ? f[g1] - a->nx[g1] * d1 : f[g1];
+                bc[1][b] = typical_bc(flag[1], cst[1], f[gI], -dI);
+                if (pass == 0) bc[1][b] = f[gI] - a->nxl[gI] * (-dI) / 2.0;
+                f[G(I + 1, j, k)] = pass == 0 ? f[gI] + a->nx[gI] * dI : f[gI];
+            }
+        for (int i = 1; i <= I; ++i)
+            for (int k = 1; k <= K; ++k) {
+                const size_t b = (size_t)(i - 1) + (size_t)I * (k - 1);
+                const size_t g1 = G(i, 1, k), gJ = G(i, J, k);
+                const double d1 = a->dy[N(i, 1, k)], dJ = a->dy[N(i, J, k)];
+                bc[2][b] = typical_bc(flag[2], cst[2], f[g1], d1);
+                f[G(i, 0, k)] = pass == 0 ? f[g1] - a->ny[g1] * d1 : f[g1];
+                bc[3][b] = typical_bc(flag[3], cst[3], f[gJ], -dJ);
+                f[G(i, J + 1, k)] = pass == 0 ? f[gJ] - a->ny[gJ] * dJ : f[gJ];
+            }
+        for (int i = 1; i <= I; ++i)
+            for (int j = 1; j <= J; ++j) {
+                const size_t b = (size_t)(i - 1) + (size_t)I * (j - 1);
+                const size_t g1 = G(i, j, 1), gK = G(i, j, K);
+                const double d1 = a->dz[N(i, j, 1)], dK = a->dz[N(i, j, K)];
+                bc[4][b] = typical_bc(flag[4], cst[4], f[g1], d1);
+                f[G(i, j, 0)] = pass == 0 ? f[g1] - a->nz[g1] * d1 : f[g1];
+                bc[5][b] = typical_bc(flag[5], cst[5], f[gK], -dK);
+                f[G(i, j, K + 1)] = pass == 0 ? f[gK] + a->nz[gK] * dK : f[gK];
+            }
+    }
+}
+
+/* Clsvof_Scheme (355-798): NV sub-steps of dt/NV.  Sub-step kk sweeps
+ * y, z, x when kk mod 3 = 1, z, x, y when 2, x, y, z when 0.  The first
+ * sweep divides its fields by 1 - dtv/d (u_i - u_{i-1}); the later two add
+ * dtv/d times the first sweep's fields times their own velocity
+ * difference; the VOF is clipped to 0 and 1 within 1e-14 after each sweep.
+ * Then the boundary planes, Interface_Reconstruct, the liquid normals, the
+ * plane distances from the cell centres, and Redistance_Levelset.
+ * Returns 0, or -1 when out of memory.                                      */
+int oracle_clsvof_scheme(const struct oracle_clsvof_args *a)
+{
+    I = a->imax; J = a->jmax; K = a->kmax;
+    const size_t ng = (size_t)(I + 2) * (J + 2) * (K + 2), nin = (size_t)I * J * K;
+    double *buf = calloc(10 * ng + nin, sizeof(double));
+    int *fix = calloc(nin, sizeof(int));
+    if (!buf || !fix) { free(buf); free(fix); return -1; }
+    double *nxx = buf, *nyy = buf + ng, *nzz = buf + 2 * ng, *dis = buf + 3 * ng;
+    double *tvf[3] = {buf + 4 * ng, buf + 5 * ng, buf + 6 * ng};
+    double *tls[3] = {buf + 7 * ng, buf + 8 * ng, buf + 9 * ng};
+    double *aux = buf + 10 * ng;
+    double *vfl = a->vofl, *phi = a->phil;
+    const double *d[3] = {a->dx, a->dy, a->dz};
+    const double *vel[3] = {a->u, a->v, a->w};
+    const double *lvs_lo[3] = {a->lvs_bc[0], a->lvs_bc[2], a->lvs_bc[4]};
+    const double dtv = a->dt / (double)NV;
+    for (int kk = 1; kk <= NV; ++kk) {
+        const int first = kk % 3 == 0 ? 0 : kk % 3 == 1 ? 1 : 2;
+        for (int s = 0; s < 3; ++s) {
+            const int ax = (first + s) % 3;
+            memcpy(tvf[ax], vfl, ng * sizeof(double));
+            memcpy(tls[ax], phi, ng * sizeof(double));
+            oracle_interface_reconstruct(I, J, K, a->x, a->y, a->z, a->dx, a->dy, a->dz, vfl, phi, nxx, nyy, nzz,
+                                         dis);
+            sweep(ax, a->dx, a->dy, a->dz, a->x, a->y, a->z, vfl, phi, nxx, nyy, nzz, dis, vel[ax], a->bc_vel[ax],
+                  lvs_lo[ax], dtv, tvf[ax], tls[ax]);
+            for (int i = 1; i <= I; ++i)
+                for (int j = 1; j <= J; ++j)
+                    for (int k = 1; k <= K; ++k) {
+                        const size_t g = G(i, j, k);
+                        const size_t gm = G(i - (ax == 0), j - (ax == 1), k - (ax == 2));
+                        const double dd = d[ax][N(i, j, k)], du = vel[ax][g] - vel[ax][gm];
+                        if (s == 0) {
+                            tvf[ax][g] = tvf[ax][g] / (1.0 - dtv / dd * du);
+                            tls[ax][g] = tls[ax][g] / (1.0 - dtv / dd * du);
+                        } else {
+                            tvf[ax][g] = tvf[ax][g] + dtv / dd * tvf[first][g] * du;
+                            tls[ax][g] = tls[ax][g] + dtv / dd * tls[first][g] * du;
+                        }
+                        if (tvf[ax][g] <= VOFEPS) tvf[ax][g] = 0.0;
+                        if (tvf[ax][g] >= 1.0 - VOFEPS) tvf[ax][g] = 1.0;
+                        vfl[g] = tvf[ax][g];
+                        phi[g] = tls[ax][g];
+                    }
+        }
+        boundary_lvs_vof(a);
+        oracle_interface_reconstruct(I, J, K, a->x, a->y, a->z, a->dx, a->dy, a->dz, vfl, phi, nxx, nyy, nzz, dis);
+        for (int i = 1; i <= I; ++i)
+            for (int j = 1; j <= J; ++j)
+                for (int k = 1; k <= K; ++k) {
+                    const size_t g = G(i, j, k), c = N(i, j, k);
+                    a->nxl[g] = nxx[g];
+                    a->nyl[g] = nyy[g];
+                    a->nzl[g] = nzz[g];
+                    dis[g] = (0.5 * a->dx[c] * fabs(nxx[g]) + 0.5 * a->dy[c] * fabs(nyy[g]) +
+                              0.5 * a->dz[c] * fabs(nzz[g])) - dis[g];
+                }
+        redistance(a->dx, a->dy, a->dz, vfl, phi, nxx, nyy, nzz, dis, aux, fix);
+    }
+    free(buf);
+    free(fix);
+    return 0;
+}
+
+/* The tail of one sub-step alone: Interface_Reconstruct, the liquid
+ * normals, the centre distances and Redistance_Levelset (Clsvof.f90:767-780).
+ * Returns 0, or -1 when out of memory. */
+int oracle_clsvof_redistance(int imax, int jmax, int kmax, const double *x, const double *y, const double *z,
+                             const double *dx, const double *dy, const double *dz, const double *vfl, double *phi,
+                             double *nxl, double *nyl, double *nzl)
+{
+    I = imax; J = jmax; K = kmax;
+    const size_t ng = (size_t)(I + 2) * (J + 2) * (K + 2), nin = (size_t)I * J * K;
+    double *buf = calloc(4 * ng + nin, sizeof(double));
+    int *fix = calloc(nin, sizeof(int));
+    if (!buf || !fix) { free(buf); free(fix); return -1; }
+    double *nxx = buf, *nyy = buf + ng, *nzz = buf + 2 * ng, *dis = buf + 3 * ng, *aux = buf + 4 * ng;
+    oracle_interface_reconstruct(I, J, K, x, y, z, dx, dy, dz, vfl, phi, nxx, nyy, nzz, dis);
+    for (int i = 1; i <= I; ++i)
+        for (int j = 1; j <= J; ++j)
+            for (int k = 1; k <= K; ++k) {
+                const size_t g = G(i, j, k), c = N(i, j, k);
+                nxl[g] = nxx[g];
+                nyl[g] = nyy[g];
+                nzl[g] = nzz[g];
+                dis[g] = (0.5 * dx[c] * fabs(nxx[g]) + 0.5 * dy[c] * fabs(nyy[g]) + 0.5 * dz[c] * fabs(nzz[g])) -
+                         dis[g];
+            }
+    redistance(dx, dy, dz, vfl, phi, nxx, nyy, nzz, dis, aux, fix);
+    free(buf);
+    free(fix);
+    return 0;
 }

@@ -9,9 +9,9 @@ rebuilds:
 - ``predictor.c``: the momentum predictor's SetMatrix / SetVectors,
   DeltaGetValues and the tail of PredictingUVW, with a Jacobi BiCGStab;
 - ``vtr.py``: the VTK RectilinearGrid writer;
-- ``clsvof.c``: ComputeUVWLiquidField, Interface_Reconstruct and the
-  directional sweeps X_Sweep / Y_Sweep / Z_Sweep, the first pieces of the
-  CLSVOF module (no GPU counterpart yet).
+- ``clsvof.c``: the CLSVOF interface transport: Clsvof_Scheme with its
+  directional sweeps, Interface_Reconstruct, BoundaryConditionLvsVof and
+  Redistance_Levelset, and ComputeUVWLiquidField (no GPU counterpart yet).
 
 Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline legs of
 ``bench.py`` use it, and only as the checker or the timed CPU path.
@@ -83,8 +83,20 @@ def lib():
         L.oracle_find_distance.restype = C.c_double
         L.oracle_interface_reconstruct.argtypes = [C.c_int, C.c_int, C.c_int] + [dp] * 12
         L.oracle_clsvof_sweep.argtypes = [C.c_int] * 4 + [dp] * 11 + [C.c_double] + [dp] * 6
+        L.oracle_clsvof_scheme.argtypes = [C.POINTER(ClsvofArgs)]
+        L.oracle_clsvof_redistance.argtypes = [C.c_int] * 3 + [dp] * 11
         _lib = L
     return _lib
+
+
+class ClsvofArgs(C.Structure):
+    """struct oracle_clsvof_args (oracle/clsvof.c)."""
+    _fields_ = [("imax", C.c_int), ("jmax", C.c_int), ("kmax", C.c_int)] + [
+        (n, capi.c_double_p) for n in ("x", "y", "z", "dx", "dy", "dz", "vofl", "phil", "nxl", "nyl", "nzl",
+                                       "nx", "ny", "nz", "u", "v", "w")] + [
+        ("bc_vel", capi.c_double_p * 3), ("lvs_bc", capi.c_double_p * 6), ("vof_bc", capi.c_double_p * 6),
+        ("lvs_flag", C.c_int * 6), ("vof_flag", C.c_int * 6), ("lvs_const", C.c_double * 6),
+        ("vof_const", C.c_double * 6), ("dt", C.c_double)]
 
 
 class GmgParams(C.Structure):
@@ -386,3 +398,50 @@ def clsvof_sweep(axis, centres, spacings, vfl, phi, vel, bc_vel, bc_lvs, dtv):
                               _dp(vfl), _dp(phi), *(_dp(a) for a in args), float(dtv),
                               *(_dp(a) for a in rec), _dp(temvf), _dp(temls))
     return temvf, temls, rec
+
+
+def clsvof_redistance(centres, spacings, vfl, phi):
+    """The tail of a CLSVOF sub-step (Clsvof.f90:767-780): reconstruct the
+    interface from ``vfl`` and ``phi`` (ghosted), then Redistance_Levelset.
+    Returns the redistanced phi (ghosts as given) and the liquid normals."""
+    I, J, K = spacings[0].shape
+    out = np.array(phi, order="F", copy=True)
+    nl = [np.zeros((I + 2, J + 2, K + 2), order="F") for _ in range(3)]
+    rc = lib().oracle_clsvof_redistance(I, J, K, *(_dp(a) for a in centres), *(_dp(a) for a in spacings),
+                                        _dp(vfl), _dp(out), *(_dp(a) for a in nl))
+    if rc != 0:
+        raise MemoryError("oracle_clsvof_redistance")
+    return out, nl
+
+
+def clsvof_scheme(centres, spacings, state, vel, fluid_normals, bc_vel, lvs_bc, dt, lvs_flag=(1,) * 6,
+                  lvs_const=(0.0,) * 6, vof_flag=(1,) * 6, vof_const=(0.0,) * 6):
+    """One Clsvof_Scheme step (Clsvof.f90:355-798).  ``state``: dict of the
+    ghosted vofl, phil, nxl, nyl, nzl, updated in place; ``vel``: the
+    ghosted u, v, w; ``fluid_normals``: the ghosted nx, ny, nz of the fluid;
+    ``bc_vel``: the wall velocities BCu%VarW, BCv%VarS, BCw%VarB; ``lvs_bc``:
+    the six level-set wall planes W, E, S, N, B, T, updated in place.
+    Returns the six VOF wall planes."""
+    I, J, K = spacings[0].shape
+    shapes = [(J, K), (J, K), (I, K), (I, K), (I, J), (I, J)]
+    for q, a in enumerate(lvs_bc):
+        assert a.shape == shapes[q] and a.flags.f_contiguous and a.dtype == np.float64
+    for key in ("vofl", "phil", "nxl", "nyl", "nzl"):
+        assert state[key].flags.f_contiguous and state[key].dtype == np.float64
+    vof_bc = [np.zeros(sh, order="F") for sh in shapes]
+    keep = [np.asfortranarray(a, dtype=np.float64) for a in (*centres, *spacings, *fluid_normals, *vel, *bc_vel)]
+    cx, cy, cz, dx, dy, dz, nx, ny, nz, u, v, w, bu, bv, bw = keep
+    args = ClsvofArgs(I, J, K, _dp(cx), _dp(cy), _dp(cz), _dp(dx), _dp(dy), _dp(dz), _dp(state["vofl"]),
+                      _dp(state["phil"]), _dp(state["nxl"]), _dp(state["nyl"]), _dp(state["nzl"]), _dp(nx),
+                      _dp(ny), _dp(nz), _dp(u), _dp(v), _dp(w))
+    args.bc_vel[:] = [_dp(bu), _dp(bv), _dp(bw)]
+    args.lvs_bc[:] = [_dp(a) for a in lvs_bc]
+    args.vof_bc[:] = [_dp(a) for a in vof_bc]
+    args.lvs_flag[:] = list(lvs_flag)
+    args.vof_flag[:] = list(vof_flag)
+    args.lvs_const[:] = list(lvs_const)
+    args.vof_const[:] = list(vof_const)
+    args.dt = float(dt)
+    if lib().oracle_clsvof_scheme(C.byref(args)) != 0:
+        raise MemoryError("oracle_clsvof_scheme")
+    return vof_bc

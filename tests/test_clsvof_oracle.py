@@ -1,9 +1,13 @@
-"""The oracle of the first pieces of the CLSVOF module (oracle/clsvof.c):
-ComputeUVWLiquidField, Interface_Reconstruct and the directional sweeps,
-against closed forms, an independent vectorised Volume_Fraction_Calc, the
-reference's index shift of the velocity cells' direction averages, exact
-translation of a plane and conservation along each swept line.  CPU only
-(no GPU counterpart yet)."""
+"""The oracle of the CLSVOF module (oracle/clsvof.c): ComputeUVWLiquidField,
+Interface_Reconstruct, the directional sweeps, Redistance_Levelset,
+BoundaryConditionLvsVof and Clsvof_Scheme, against closed forms, an
+independent vectorised Volume_Fraction_Calc, the reference's index shift of
+the velocity cells' direction averages, exact translation of a plane,
+conservation along each swept line and in a shear, and independent
+restatements of the redistancing (as a gather) and of the boundary planes,
+matched bit for bit.  CPU only (no GPU counterpart yet)."""
+import math
+
 import numpy as np
 import pytest
 
@@ -316,3 +320,272 @@ def test_sweep_backward_level_set_keeps_the_reference_faces(axis):
     np.testing.assert_allclose(t[m - 1], p[m - 1] + f(face[m - 2]) - f(last), atol=1e-13)
     if axis != 2:
         np.testing.assert_allclose(t[m - 1], p[m - 1], atol=1e-13)
+
+
+# ---- redistancing (Redistance_Levelset) -----------------------------------
+
+def _sg(a):
+    return math.copysign(1.0, a)
+
+
+def _shortest_point_2d(n, d1, off, cas, h, s):
+    """Shortest_Point_2d (Clsvof.f90:1961-2060) on the face normal to axis
+    ``cas`` (0, 1, 2): writes the two other coordinates of ``s``.  The y
+    face solves for x by dividing by |nz| (the reference's)."""
+    a, b = [q for q in range(3) if q != cas]
+    t = math.sqrt(n[a] * n[a] + n[b] * n[b] + 1e-30 * 1e-30)
+    na, nb, d = n[a] / t, n[b] / t, d1 / t
+    dij = na * h[a] * off[a] + nb * h[b] * off[b] + d
+    pa, pb = h[a] * off[a] - dij * na, h[b] * off[b] - dij * nb
+    if -0.5 * h[a] <= pa <= 0.5 * h[a] and -0.5 * h[b] <= pb <= 0.5 * h[b]:
+        s[a], s[b] = pa, pb
+        return
+    oa, ob = max(abs(pa) - 0.5 * h[a], 0.0), max(abs(pb) - 0.5 * h[b], 0.0)
+    if oa * abs(na) > ob * abs(nb):
+        s[a] = _sg(pa) * 0.5 * h[a]
+        s[b] = (d + na * s[a]) / (_sg(-nb) * max(abs(nb), 1e-14))
+    else:
+        s[b] = _sg(pb) * 0.5 * h[b]
+        div = abs(nb) if cas == 1 else abs(na)
+        s[a] = (d + nb * s[b]) / (_sg(-na) * max(div, 1e-14))
+
+
+def _band_distance(n, dc, off, h, side):
+    """The distance Redistance_Levelset (Clsvof.f90:1740-1861) measures from
+    the centre ``off`` cells away to an interface cell's plane n.x + dc = 0."""
+    X = [h[q] * off[q] for q in range(3)]
+    xv = [h[q] * max(-1, min(1, off[q])) / 2.0 for q in range(3)]
+    dv = n[0] * xv[0] + n[1] * xv[1] + n[2] * xv[2] + dc
+    dist = lambda p: math.sqrt((X[0] - p[0]) * (X[0] - p[0]) + (X[1] - p[1]) * (X[1] - p[1]) +
+                               (X[2] - p[2]) * (X[2] - p[2]))
+    if dv * _sg(side) <= 0.0:
+        return dist(xv)
+    dij = n[0] * h[0] * off[0] + n[1] * h[1] * off[1] + n[2] * h[2] * off[2] + dc
+    p = [X[q] - dij * n[q] for q in range(3)]
+    if all(-0.5 * h[q] <= p[q] <= 0.5 * h[q] for q in range(3)):
+        return dist(p)
+    w = [max(abs(p[q]) - 0.5 * h[q], 0.0) * abs(n[q]) for q in range(3)]
+    fc = [_sg(p[q]) * 0.5 * h[q] for q in range(3)]
+    s = [0.0, 0.0, 0.0]
+    for c in range(3):
+        o1, o2 = [q for q in range(3) if q != c]
+        if not (w[c] >= w[o1] and w[c] >= w[o2]):
+            continue
+        corners = []      # Iscutface's point1..point4, around the face
+        for sa, sb in ((-0.5, -0.5), (-0.5, 0.5), (0.5, 0.5), (0.5, -0.5)):
+            v = [0.0, 0.0, 0.0]
+            v[c], v[o1], v[o2] = fc[c], sa * h[o1], sb * h[o2]
+            corners.append(n[0] * v[0] + n[1] * v[1] + n[2] * v[2] + dc)
+        cut = not all(corners[q] * corners[(q + 1) % 4] >= 0.0 for q in range(4))
+        if cut:
+            cas = c
+        else:
+            cas = o1 if w[o1] > w[o2] else o2
+        s[cas] = fc[cas]
+        _shortest_point_2d(n, n[cas] * s[cas] + dc, off, cas, h, s)
+    return dist(s)
+
+
+def _redistance_gather(h, vfl, phi, nx, ny, nz, dis):
+    """Redistance_Levelset restated as a gather: each full or empty cell
+    takes the least band distance over the interface cells around it."""
+    I, J, K = (m - 2 for m in vfl.shape)
+    inner = (slice(1, -1),) * 3
+    part = (vfl[inner] > 1e-15) & (vfl[inner] < 1.0 - 1e-15)
+    iface = [tuple(int(v) + 1 for v in c) for c in np.argwhere(part)]
+    out = np.array(phi, copy=True)
+
+    def centre_distance(a, b, c):
+        n = (nx[a, b, c], ny[a, b, c], nz[a, b, c])
+        return n, (0.5 * h[0] * abs(n[0]) + 0.5 * h[1] * abs(n[1]) + 0.5 * h[2] * abs(n[2])) - dis[a, b, c]
+
+    for i in range(1, I + 1):
+        for j in range(1, J + 1):
+            for k in range(1, K + 1):
+                f = vfl[i, j, k]
+                if part[i - 1, j - 1, k - 1]:
+                    out[i, j, k] = _sg(0.5 - f) * abs(centre_distance(i, j, k)[1])
+                    continue
+                best = None
+                if f < 1e-15 or f > 1.0 - 1e-15:
+                    for (a, b, c) in iface:
+                        off = (i - a, j - b, k - c)
+                        if max(abs(q) for q in off) > 4:
+                            continue
+                        n, dc = centre_distance(a, b, c)
+                        d = _band_distance(n, dc, off, h, phi[i, j, k])
+                        best = d if best is None or d < best else best
+                out[i, j, k] = _sg(0.5 - f) * (min(best, 1.0e4) if best is not None else 5 * h[0] * math.sqrt(3.0))
+    return out
+
+
+@pytest.mark.parametrize("n", [[1.0, 0.0, 0.0], [1.0, 0.15, 0.0], [1.0, 0.15, -0.1]])
+def test_redistance_matches_a_gather_restatement(n):
+    """The oracle's Redistance_Levelset (a scatter of running minima over
+    the band of each interface cell, as the reference loops) equals, bit for
+    bit, an independent gather over the interface cells around each cell.
+    An axis-normal plane comes back as its exact signed distance; a tilted
+    one is never under the true distance where the reference's y-face
+    division by |nz| cannot act (nz = 0), and with nz != 0 that division
+    puts some band cells well under it."""
+    centres, spacings, h, nu, phi_at, fractions = _plane_case(0, n, 0.53, (12, 9, 10))
+    phi = phi_at(0.0)
+    vfl = fractions(phi)
+    got, nl = O.clsvof_redistance(centres, spacings, vfl, 2.5 * phi)
+    nx, ny, nz, dis = O.interface_reconstruct(centres, spacings, vfl, 2.5 * phi)
+    ref = _redistance_gather(h, vfl, 2.5 * phi, nx, ny, nz, dis)
+    np.testing.assert_array_equal(got, ref)
+    for q, a in enumerate(nl):
+        np.testing.assert_array_equal(a[1:-1, 1:-1, 1:-1], (nx, ny, nz)[q][1:-1, 1:-1, 1:-1])
+    inner = (slice(1, -1),) * 3
+    assert (np.sign(got[inner]) == np.where(vfl[inner] > 0.5, -1.0, 1.0)).all()
+    far = np.abs(got[inner]) == 5 * h[0] * math.sqrt(3.0)
+    under = np.abs(got[inner][~far]) - np.abs(phi[inner][~far])
+    if n[1] == 0.0 and n[2] == 0.0:
+        assert np.abs(under).max() < 1e-14
+    elif n[2] == 0.0:
+        assert under.min() > -1e-14 and (np.abs(under) < 1e-13).mean() > 0.6
+    else:
+        assert under.min() < -h[0]
+
+
+# ---- one Clsvof_Scheme step ---------------------------------------------
+
+def _clip(v):
+    return np.where(v <= 1e-14, 0.0, np.where(v >= 1.0 - 1e-14, 1.0, v))
+
+
+def _bc_lvs_vof(phi, vof, nxl, nf, h, lvs, vof_bc):
+    """BoundaryConditionLvsVof restated on numpy planes: ``lvs`` and
+    ``vof_bc`` are (flags, consts) pairs; fills the ghosts of phi and vof
+    and returns the 12 wall planes W, E, S, N, B, T of each."""
+    def typical(flag, cst, var, d):
+        return np.full(var.shape, cst) if flag == 0 else var - cst * d / 2.0
+    out = []
+    for f, (flags, consts) in ((phi, lvs), (vof, vof_bc)):
+        lvl = f is phi
+        planes = []
+        for ax in range(3):
+            for hi in (False, True):
+                q = 2 * ax + hi
+                cell = [slice(1, -1)] * 3
+                ghost = [slice(1, -1)] * 3
+                cell[ax] = -2 if hi else 1
+                ghost[ax] = -1 if hi else 0
+                var = f[tuple(cell)].copy()
+                d = -h[ax] if hi else h[ax]
+                plane = typical(flags[q], consts[q], var, np.full(var.shape, d))
+                if lvl and ax == 0:
+                    plane = var - nxl[tuple(cell)] * d / 2.0
+                planes.append(np.asfortranarray(plane))
+                if lvl:
+                    step = nf[ax][tuple(cell)] * h[ax]
+                    f[tuple(ghost)] = var + step if hi and ax != 1 else var - step
+                else:
+                    f[tuple(ghost)] = var
+        out.append(planes)
+    return out
+
+
+def _scheme_inputs(n, x0, shape=(12, 9, 10)):
+    centres, spacings, h, nu, phi_at, fractions = _plane_case(0, n, x0, shape)
+    g = (shape[0] + 2, shape[1] + 2, shape[2] + 2)
+    state = {"phil": phi_at(0.0), "vofl": np.asfortranarray(_clip(fractions(phi_at(0.0))))}
+    for key in ("nxl", "nyl", "nzl"):
+        state[key] = np.zeros(g, order="F")
+    nf = [np.full(g, nu[q], order="F") for q in range(3)]
+    lvs_bc = [np.zeros(sh, order="F") for sh in [shape[1:]] * 2 + [(shape[0], shape[2])] * 2 + [shape[:2]] * 2]
+    return centres, spacings, h, nu, phi_at, fractions, state, nf, lvs_bc
+
+
+def test_scheme_at_rest_is_six_redistancings():
+    """With no velocity the sweeps move nothing, so a step is six rounds of
+    the boundary planes and ghosts (W/E planes from the liquid normals, the
+    others TypicalBC; ghost level set from the fluid normals, the north one
+    subtracting like the south) followed by the redistancing; the liquid
+    fractions stay as they are, bit for bit."""
+    centres, spacings, h, nu, phi_at, fractions, state, nf, lvs_bc = _scheme_inputs([1.0, 0.15, -0.1], 0.53)
+    state["phil"] = np.asfortranarray(2.5 * state["phil"])
+    lvs = ((1, 1, 0, 1, 1, 1), (0.0, 0.0, 0.7, 0.3, 0.0, 0.0))
+    vofb = ((1, 1, 1, 1, 0, 1), (0.0, 0.0, 0.0, 0.0, 0.25, 0.1))
+    vel = [np.zeros_like(state["phil"]) for _ in range(3)]
+    bc_vel = [np.zeros(a.shape, order="F") for a in (lvs_bc[0], lvs_bc[2], lvs_bc[4])]
+    phi = state["phil"].copy(order="F")
+    vof = state["vofl"].copy(order="F")
+    nxl = state["nxl"].copy(order="F")
+    for _ in range(6):
+        planes = _bc_lvs_vof(phi, vof, nxl, nf, h, lvs, vofb)
+        phi, nl = O.clsvof_redistance(centres, spacings, vof, phi)
+        nxl = nl[0]
+    vof_bc = O.clsvof_scheme(centres, spacings, state, vel, nf, bc_vel, lvs_bc, 0.01, lvs_flag=lvs[0],
+                             lvs_const=lvs[1], vof_flag=vofb[0], vof_const=vofb[1])
+    np.testing.assert_array_equal(state["phil"], phi)
+    np.testing.assert_array_equal(state["vofl"], vof)
+    np.testing.assert_array_equal(state["nxl"][1:-1, 1:-1, 1:-1], nl[0][1:-1, 1:-1, 1:-1])
+    np.testing.assert_array_equal(state["nyl"][1:-1, 1:-1, 1:-1], nl[1][1:-1, 1:-1, 1:-1])
+    for q in range(6):
+        np.testing.assert_array_equal(lvs_bc[q], planes[0][q])
+        np.testing.assert_array_equal(vof_bc[q], planes[1][q])
+    assert (lvs_bc[2] == 0.7).all() and (vof_bc[4] == 0.25).all()
+
+
+def test_scheme_carries_a_plane_one_step():
+    """A uniform velocity along x carries a tilted plane through the six
+    sub-steps: the liquid fractions are those of the moved plane, and the
+    interface cells' level set and normals are the moved plane's."""
+    n = [1.0, 0.0, 0.15]
+    centres, spacings, h, nu, phi_at, fractions, state, nf, lvs_bc = _scheme_inputs(n, 0.47)
+    u, dt = 0.9, 0.45 * h[0] / 0.9
+    g = state["phil"].shape
+    vel = [np.full(g, u, order="F"), np.zeros(g, order="F"), np.zeros(g, order="F")]
+    bc_vel = [np.full(lvs_bc[0].shape, u, order="F"), np.zeros(lvs_bc[2].shape, order="F"),
+              np.zeros(lvs_bc[4].shape, order="F")]
+    O.clsvof_scheme(centres, spacings, state, vel, nf, bc_vel, lvs_bc, dt)
+    moved = phi_at(u * dt)
+    inner = (slice(1, -1),) * 3
+    want = _clip(fractions(moved))[inner]
+    part = (want > 0) & (want < 1)
+    assert part.sum() > 50
+    np.testing.assert_allclose(state["vofl"][inner], want, atol=1e-12)
+    np.testing.assert_allclose(state["phil"][inner][part], moved[inner][part], atol=1e-12)
+    for q, key in enumerate(("nxl", "nyl", "nzl")):
+        np.testing.assert_allclose(state[key][inner][part], nu[q], atol=1e-12)
+
+
+def test_scheme_keeps_the_liquid_volume_in_a_shear():
+    """u = u(y), v = w = 0 is divergence-free along every x line, so the
+    first sweep's division and the later corrections are exact no-ops and a
+    drop away from the walls keeps its liquid volume to rounding."""
+    I = J = K = 14
+    h = 1.0 / I
+    c = (np.arange(I) + 0.5) * h
+    cg = (np.arange(I + 2) - 0.5) * h
+    centres = tuple(np.asfortranarray(a) for a in np.meshgrid(c, c, c, indexing="ij"))
+    spacings = tuple(np.full((I, J, K), h, order="F") for _ in range(3))
+    Xg, Yg, Zg = np.meshgrid(cg, cg, cg, indexing="ij")
+    r = np.sqrt((Xg - 0.48) ** 2 + (Yg - 0.52) ** 2 + (Zg - 0.5) ** 2)
+    phi = np.asfortranarray(r - 0.23)
+    sub = (np.arange(6) + 0.5) / 6 - 0.5
+    vof = np.zeros_like(phi)
+    for a in sub:
+        for b in sub:
+            for d in sub:
+                vof += (np.sqrt((Xg + a * h - 0.48) ** 2 + (Yg + b * h - 0.52) ** 2 + (Zg + d * h - 0.5) ** 2)
+                        < 0.23)
+    vof = np.asfortranarray(_clip(vof / 216.0))
+    g = phi.shape
+    state = {"phil": phi, "vofl": vof}
+    for key in ("nxl", "nyl", "nzl"):
+        state[key] = np.zeros(g, order="F")
+    nf = [np.zeros(g, order="F") for _ in range(3)]
+    vel = [np.asfortranarray(0.6 * np.sin(2 * np.pi * Yg) + np.zeros(g)), np.zeros(g, order="F"),
+           np.zeros(g, order="F")]
+    lvs_bc = [np.zeros(sh, order="F") for sh in [(J, K)] * 2 + [(I, K)] * 2 + [(I, J)] * 2]
+    bc_vel = [np.asfortranarray(vel[0][0, 1:-1, 1:-1]), np.zeros((I, K), order="F"), np.zeros((I, J), order="F")]
+    vof0 = vof[1:-1, 1:-1, 1:-1].copy()
+    before = vof0.sum()
+    O.clsvof_scheme(centres, spacings, state, vel, nf, bc_vel, lvs_bc, 0.4 * h / 0.6)
+    after = state["vofl"][1:-1, 1:-1, 1:-1]
+    assert ((after > 0) & (after < 1)).sum() > 100
+    assert abs(after.sum() - before) < 1e-11 * before
+    assert np.abs(after - vof0).max() > 0.05
