@@ -34,6 +34,7 @@ UNITS = {
     "k_predictor.cu": ["-fmad=false"],
     "k_bicgstab.cu": [],
     "pred_api.cu": [],
+    "k_transport.cu": ["-fmad=false"],
 }
 
 
@@ -52,6 +53,7 @@ def _compile(unit: str, extra, verbose: bool):
     deps.append(os.path.join(HERE, "..", "include", "scf_geometry.h"))
     deps.append(os.path.join(HERE, "..", "include", "scf_output.h"))
     deps.append(os.path.join(HERE, "..", "include", "scf_predictor.h"))
+    deps.append(os.path.join(HERE, "..", "include", "scf_clsvof.h"))
     if os.path.exists(obj) and all(os.path.getmtime(obj) >= os.path.getmtime(d) for d in deps):
         return obj
     cmd = [nvcc(), "-c", src, "-o", obj] + ARCH + COMMON + list(extra)

@@ -195,6 +195,29 @@ class ScfMomStats(C.Structure):
         return out
 
 
+class ScfClsvofIn(C.Structure):
+    """scf_clsvof_in of include/scf_clsvof.h."""
+    _fields_ = [(n, c_double_p) for n in ("x", "y", "z", "dx", "dy", "dz", "u", "v", "w", "nx", "ny", "nz",
+                                          "bc_u_w", "bc_v_s", "bc_w_b")] + [
+        ("lvs_flag", C.c_int32 * 6), ("vof_flag", C.c_int32 * 6), ("lvs_const", C.c_double * 6),
+        ("vof_const", C.c_double * 6), ("dt", C.c_double)]
+
+
+class ScfClsvofState(C.Structure):
+    """scf_clsvof_state of include/scf_clsvof.h."""
+    _fields_ = [(n, c_double_p) for n in ("vofl", "phil", "nxl", "nyl", "nzl")] + [
+        ("lvs_bc", c_double_p * 6), ("vof_bc", c_double_p * 6)]
+
+
+class ScfClsvofStats(C.Structure):
+    _fields_ = [("ms_h2d", C.c_double), ("ms_run", C.c_double), ("ms_d2h", C.c_double), ("ms_total", C.c_double),
+                ("bytes_h2d", C.c_int64), ("bytes_d2h", C.c_int64), ("steps", C.c_int32),
+                ("gpu_launches", C.c_int32)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 def dptr(a: Optional[np.ndarray]):
     if a is None:
         return c_double_p()

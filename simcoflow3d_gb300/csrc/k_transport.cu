@@ -1,0 +1,486 @@
+// k_transport.cu -- the CLSVOF interface transport on the device and its C
+// ABI (include/scf_clsvof.h).
+//
+// One time step is six sub-steps; a sub-step is
+//   3 x (k_reconstruct, k_sweep)   the split sweeps, each cell gathering its
+//                                  own face fluxes (no scatter, no atomics)
+//                                  with the divergence term fused in;
+//   k_walls                        the wall planes and ghosts;
+//   k_reconstruct (tail)           normals, liquid normals, centre distances;
+//   k_band_reset, k_band_scatter,  the redistancing: every interface cell
+//   k_band_value                   sends its band distances with a 64-bit
+//                                  atomicMin (non-negative doubles order like
+//                                  their bits), so the result is the
+//                                  reference's running minimum whatever the
+//                                  order.
+// The VOF and level set ping-pong through three buffers (the sub-step's
+// input, its first sweep's result, which the later sweeps' divergence terms
+// read, and the second sweep's result); every sub-step ends in buffer 0.
+// Built with -fmad=false: the bodies round like the reference's Fortran.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "../../include/scf_clsvof.h"
+#include "transport_body.cuh"
+
+using tr::Dims;
+using tr::Geo;
+
+struct scf_clsvof_ctx {
+    Dims D{};
+    int device = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev[4] = {};
+    std::vector<void *> mem;
+    double *geo[6] = {};                 // x, y, z, dx, dy, dz
+    double *vf[3] = {}, *ls[3] = {};     // ghosted ping-pong
+    double *nx = nullptr, *ny = nullptr, *nz = nullptr, *dis = nullptr;
+    double *nxl = nullptr, *nyl = nullptr, *nzl = nullptr;
+    double *fn[3] = {};                  // fluid normals
+    double *vel[3] = {};
+    double *bc_vel[3] = {};              // W, S, B planes of u, v, w
+    double *lvs_bc[6] = {}, *vof_bc[6] = {};
+    unsigned long long *key = nullptr;
+    uint8_t *fix = nullptr;
+    int lvs_flag[6] = {}, vof_flag[6] = {};
+    double lvs_const[6] = {}, vof_const[6] = {};
+    double dt = 0.0;
+    bool staged = false;
+    char err[512] = {0};
+};
+
+namespace {
+
+constexpr int NT = 256;
+
+void tr_err(scf_clsvof_ctx *c, const char *fmt, ...)
+{
+    if (!c) return;
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(c->err, sizeof(c->err), fmt, ap);
+    va_end(ap);
+}
+
+#define TK(call)                                                                            \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess) {                                                            \
+            tr_err(ctx, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return e_ == cudaErrorMemoryAllocation ? SCF_ERR_OUT_OF_MEMORY : SCF_ERR_CUDA;   \
+        }                                                                                   \
+    } while (0)
+
+int blocks_for(size_t n)
+{
+    const size_t b = (n + NT - 1) / NT;
+    return (int)std::min<size_t>(std::max<size_t>(b, 1), (size_t)152 * 64);
+}
+
+Geo geo_of(const scf_clsvof_ctx *c)
+{
+    return Geo{c->geo[0], c->geo[1], c->geo[2], c->geo[3], c->geo[4], c->geo[5]};
+}
+
+// ---- kernels -------------------------------------------------------------
+
+// Interface_Reconstruct over the interior; with `tail` also the liquid
+// normals and the distance from the cell centre (Clsvof_Scheme 767-778).
+__global__ void k_reconstruct(Dims D, Geo G, const double *__restrict__ vfl, const double *__restrict__ phi,
+                              double *nx, double *ny, double *nz, double *dis, int tail, double *nxl, double *nyl,
+                              double *nzl)
+{
+    const size_t nin = D.interior();
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nin; t += (size_t)gridDim.x * blockDim.x) {
+        int i, j, k;
+        D.cell_of(t, i, j, k);
+        double n1, n2, n3, d1;
+        tr::reconstruct(D, G, vfl, phi, i, j, k, n1, n2, n3, d1);
+        const size_t g = D.g(i, j, k);
+        nx[g] = n1;
+        ny[g] = n2;
+        nz[g] = n3;
+        if (tail) {
+            nxl[g] = n1;
+            nyl[g] = n2;
+            nzl[g] = n3;
+            d1 = (0.5 * G.dx[t] * fabs(n1) + 0.5 * G.dy[t] * fabs(n2) + 0.5 * G.dz[t] * fabs(n3)) - d1;
+        }
+        dis[g] = d1;
+    }
+}
+
+// One directional sweep over the ghosted grid: interior cells take their
+// swept values, ghost cells are carried over.
+__global__ void k_sweep(Dims D, Geo G, tr::SweepIn S, double *__restrict__ vf_out, double *__restrict__ ls_out)
+{
+    const size_t ng = D.ghosted();
+    const int gi = D.I + 2, gj = D.J + 2;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < ng; t += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(t % (size_t)gi), j = (int)((t / (size_t)gi) % (size_t)gj), k = (int)(t / ((size_t)gi * gj));
+        if (i < 1 || i > D.I || j < 1 || j > D.J || k < 1 || k > D.K) {
+            vf_out[t] = S.vfl[t];
+            ls_out[t] = S.phi[t];
+            continue;
+        }
+        double a, b;
+        tr::sweep_cell(D, G, S, i, j, k, a, b);
+        vf_out[t] = a;
+        ls_out[t] = b;
+    }
+}
+
+// BoundaryConditionLvsVof: blockIdx.y is the axis, x strides its planes.
+__global__ void k_walls(Dims D, Geo G, tr::WallIn W)
+{
+    const int axis = blockIdx.y;
+    const size_t np = D.plane_size(axis);
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < np; t += (size_t)gridDim.x * blockDim.x)
+        tr::wall_point(D, G, W, axis, t);
+}
+
+__global__ void k_band_reset(size_t nin, unsigned long long *key, uint8_t *fix)
+{
+    const unsigned long long far = (unsigned long long)tr::key_of(1.0e4);
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nin; t += (size_t)gridDim.x * blockDim.x) {
+        key[t] = far;
+        fix[t] = 0;
+    }
+}
+
+__global__ void k_band_scatter(Dims D, Geo G, const double *__restrict__ vfl, const double *__restrict__ phi,
+                               const double *__restrict__ nx, const double *__restrict__ ny,
+                               const double *__restrict__ nz, const double *__restrict__ dis,
+                               unsigned long long *key, uint8_t *fix)
+{
+    const size_t nin = D.interior();
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nin; t += (size_t)gridDim.x * blockDim.x) {
+        int i, j, k;
+        D.cell_of(t, i, j, k);
+        tr::band_scatter(D, G, vfl, phi, nx, ny, nz, dis, i, j, k, key, fix);
+    }
+}
+
+__global__ void k_band_value(Dims D, Geo G, const double *__restrict__ vfl, const double *__restrict__ dis,
+                             const unsigned long long *__restrict__ key, const uint8_t *__restrict__ fix,
+                             double *phi)
+{
+    const size_t nin = D.interior();
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nin; t += (size_t)gridDim.x * blockDim.x) {
+        int i, j, k;
+        D.cell_of(t, i, j, k);
+        phi[D.g(i, j, k)] = tr::band_value(D, G, vfl, dis, i, j, k, key, fix);
+    }
+}
+
+// ---- one time step ---------------------------------------------------------
+
+int launch_check(scf_clsvof_ctx *ctx, const char *what)
+{
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        tr_err(ctx, "%s launch: %s", what, cudaGetErrorString(e));
+        return SCF_ERR_CUDA;
+    }
+    return SCF_OK;
+}
+
+// Clsvof_Scheme (Clsvof.f90:355-798) on the staged state; counts launches.
+int scheme_step(scf_clsvof_ctx *ctx, int &launches)
+{
+    const Dims D = ctx->D;
+    const Geo G = geo_of(ctx);
+    const size_t nin = D.interior(), ng = D.ghosted();
+    const double dtv = ctx->dt / (double)tr::NSUB;
+    const int bi = blocks_for(nin), bg = blocks_for(ng);
+    size_t pmax = std::max(D.plane_size(0), std::max(D.plane_size(1), D.plane_size(2)));
+    int rc;
+    for (int kk = 1; kk <= tr::NSUB; ++kk) {
+        const int first = kk % 3 == 0 ? 0 : kk % 3 == 1 ? 1 : 2;
+        int cur = 0;
+        for (int s = 0; s < 3; ++s) {
+            const int ax = (first + s) % 3, out = s == 0 ? 1 : s == 1 ? 2 : 0;
+            k_reconstruct<<<bi, NT, 0, ctx->st>>>(D, G, ctx->vf[cur], ctx->ls[cur], ctx->nx, ctx->ny, ctx->nz,
+                                                  ctx->dis, 0, nullptr, nullptr, nullptr);
+            if ((rc = launch_check(ctx, "k_reconstruct")) != SCF_OK) return rc;
+            tr::SweepIn S;
+            S.vfl = ctx->vf[cur];
+            S.phi = ctx->ls[cur];
+            S.nx = ctx->nx;
+            S.ny = ctx->ny;
+            S.nz = ctx->nz;
+            S.dis = ctx->dis;
+            S.vel = ctx->vel[ax];
+            S.bc_vel = ctx->bc_vel[ax];
+            S.bc_lvs = ctx->lvs_bc[2 * ax];
+            S.vf_first = ctx->vf[1];
+            S.ls_first = ctx->ls[1];
+            S.dtv = dtv;
+            S.axis = ax;
+            S.stage = s;
+            k_sweep<<<bg, NT, 0, ctx->st>>>(D, G, S, ctx->vf[out], ctx->ls[out]);
+            if ((rc = launch_check(ctx, "k_sweep")) != SCF_OK) return rc;
+            launches += 2;
+            cur = out;
+        }
+        tr::WallIn W;
+        W.phil = ctx->ls[0];
+        W.vofl = ctx->vf[0];
+        W.nxl = ctx->nxl;
+        W.nx = ctx->fn[0];
+        W.ny = ctx->fn[1];
+        W.nz = ctx->fn[2];
+        for (int f = 0; f < 6; ++f) {
+            W.lvs_bc[f] = ctx->lvs_bc[f];
+            W.vof_bc[f] = ctx->vof_bc[f];
+            W.lvs_flag[f] = ctx->lvs_flag[f];
+            W.vof_flag[f] = ctx->vof_flag[f];
+            W.lvs_const[f] = ctx->lvs_const[f];
+            W.vof_const[f] = ctx->vof_const[f];
+        }
+        k_walls<<<dim3(blocks_for(pmax), 3), NT, 0, ctx->st>>>(D, G, W);
+        if ((rc = launch_check(ctx, "k_walls")) != SCF_OK) return rc;
+        k_reconstruct<<<bi, NT, 0, ctx->st>>>(D, G, ctx->vf[0], ctx->ls[0], ctx->nx, ctx->ny, ctx->nz, ctx->dis, 1,
+                                              ctx->nxl, ctx->nyl, ctx->nzl);
+        if ((rc = launch_check(ctx, "k_reconstruct")) != SCF_OK) return rc;
+        k_band_reset<<<bi, NT, 0, ctx->st>>>(nin, ctx->key, ctx->fix);
+        if ((rc = launch_check(ctx, "k_band_reset")) != SCF_OK) return rc;
+        k_band_scatter<<<bi, NT, 0, ctx->st>>>(D, G, ctx->vf[0], ctx->ls[0], ctx->nx, ctx->ny, ctx->nz, ctx->dis,
+                                               ctx->key, ctx->fix);
+        if ((rc = launch_check(ctx, "k_band_scatter")) != SCF_OK) return rc;
+        k_band_value<<<bi, NT, 0, ctx->st>>>(D, G, ctx->vf[0], ctx->dis, ctx->key, ctx->fix, ctx->ls[0]);
+        if ((rc = launch_check(ctx, "k_band_value")) != SCF_OK) return rc;
+        launches += 5;
+    }
+    return SCF_OK;
+}
+
+template <typename P>
+int alloc(scf_clsvof_ctx *ctx, P **ptr, size_t count)
+{
+    void *p = nullptr;
+    const size_t bytes = std::max<size_t>(count * sizeof(P), 16);
+    const cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) {
+        tr_err(ctx, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
+        return SCF_ERR_OUT_OF_MEMORY;
+    }
+    ctx->mem.push_back(p);
+    *ptr = (P *)p;
+    return cudaMemset(p, 0, bytes) == cudaSuccess ? SCF_OK : SCF_ERR_CUDA;
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b)
+{
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+}
+
+}  // namespace
+
+extern "C" int scf_clsvof_create(scf_clsvof_ctx **out, int32_t imax, int32_t jmax, int32_t kmax, int32_t device)
+{
+    if (!out) return SCF_ERR_BAD_ARG;
+    *out = nullptr;
+    if (imax < 3 || jmax < 3 || kmax < 3 || imax > 65533 || jmax > 65533 || kmax > 65533) return SCF_ERR_BAD_ARG;
+    if (cudaSetDevice(device) != cudaSuccess) return SCF_ERR_NO_DEVICE;
+    scf_clsvof_ctx *ctx = new scf_clsvof_ctx();
+    ctx->device = device;
+    ctx->D = Dims{imax, jmax, kmax};
+    auto fail = [&](int rc) {
+        scf_clsvof_destroy(ctx);
+        return rc;
+    };
+    if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) return fail(SCF_ERR_CUDA);
+    for (auto &e : ctx->ev)
+        if (cudaEventCreate(&e) != cudaSuccess) return fail(SCF_ERR_CUDA);
+    const size_t nin = ctx->D.interior(), ng = ctx->D.ghosted();
+    int rc;
+#define TRY(ptr, count)                                         \
+    if ((rc = alloc(ctx, &(ptr), (count))) != SCF_OK) return fail(rc);
+    for (auto &p : ctx->geo) TRY(p, nin)
+    for (int b = 0; b < 3; ++b) { TRY(ctx->vf[b], ng) TRY(ctx->ls[b], ng) }
+    TRY(ctx->nx, ng) TRY(ctx->ny, ng) TRY(ctx->nz, ng) TRY(ctx->dis, ng)
+    TRY(ctx->nxl, ng) TRY(ctx->nyl, ng) TRY(ctx->nzl, ng)
+    for (auto &p : ctx->fn) TRY(p, ng)
+    for (auto &p : ctx->vel) TRY(p, ng)
+    for (int a = 0; a < 3; ++a) TRY(ctx->bc_vel[a], ctx->D.plane_size(a))
+    for (int f = 0; f < 6; ++f) { TRY(ctx->lvs_bc[f], ctx->D.plane_size(f / 2)) TRY(ctx->vof_bc[f], ctx->D.plane_size(f / 2)) }
+    TRY(ctx->key, nin) TRY(ctx->fix, nin)
+#undef TRY
+    *out = ctx;
+    return SCF_OK;
+}
+
+extern "C" int scf_clsvof_destroy(scf_clsvof_ctx *ctx)
+{
+    if (!ctx) return SCF_ERR_BAD_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->st) cudaStreamSynchronize(ctx->st);
+    for (void *p : ctx->mem) cudaFree(p);
+    for (auto &e : ctx->ev)
+        if (e) cudaEventDestroy(e);
+    if (ctx->st) cudaStreamDestroy(ctx->st);
+    delete ctx;
+    return SCF_OK;
+}
+
+extern "C" int scf_clsvof_stage(scf_clsvof_ctx *ctx, const scf_clsvof_in *in, const scf_clsvof_state *s)
+{
+    if (!ctx || !in || !s) return SCF_ERR_BAD_ARG;
+    const double *need[] = {in->x, in->y, in->z, in->dx, in->dy, in->dz, in->u, in->v, in->w, in->nx, in->ny,
+                            in->nz, in->bc_u_w, in->bc_v_s, in->bc_w_b, s->vofl, s->phil, s->nxl, s->nyl, s->nzl};
+    for (const double *p : need)
+        if (!p) {
+            tr_err(ctx, "scf_clsvof_stage: a required array is null");
+            return SCF_ERR_BAD_ARG;
+        }
+    for (int f = 0; f < 6; ++f)
+        if (!s->lvs_bc[f]) {
+            tr_err(ctx, "scf_clsvof_stage: lvs_bc[%d] is null", f);
+            return SCF_ERR_BAD_ARG;
+        }
+    if (!(in->dt >= 0.0) || !std::isfinite(in->dt)) {
+        tr_err(ctx, "scf_clsvof_stage: dt must be finite and >= 0");
+        return SCF_ERR_BAD_ARG;
+    }
+    cudaSetDevice(ctx->device);
+    const size_t nin = ctx->D.interior(), ng = ctx->D.ghosted();
+    const size_t bi = nin * sizeof(double), bg = ng * sizeof(double);
+    const double *geo[6] = {in->x, in->y, in->z, in->dx, in->dy, in->dz};
+    for (int q = 0; q < 6; ++q) TK(cudaMemcpyAsync(ctx->geo[q], geo[q], bi, cudaMemcpyHostToDevice, ctx->st));
+    const double *vel[3] = {in->u, in->v, in->w}, *fn[3] = {in->nx, in->ny, in->nz};
+    const double *bcv[3] = {in->bc_u_w, in->bc_v_s, in->bc_w_b};
+    for (int a = 0; a < 3; ++a) {
+        TK(cudaMemcpyAsync(ctx->vel[a], vel[a], bg, cudaMemcpyHostToDevice, ctx->st));
+        TK(cudaMemcpyAsync(ctx->fn[a], fn[a], bg, cudaMemcpyHostToDevice, ctx->st));
+        TK(cudaMemcpyAsync(ctx->bc_vel[a], bcv[a], ctx->D.plane_size(a) * sizeof(double), cudaMemcpyHostToDevice,
+                           ctx->st));
+    }
+    TK(cudaMemcpyAsync(ctx->vf[0], s->vofl, bg, cudaMemcpyHostToDevice, ctx->st));
+    TK(cudaMemcpyAsync(ctx->ls[0], s->phil, bg, cudaMemcpyHostToDevice, ctx->st));
+    TK(cudaMemcpyAsync(ctx->nxl, s->nxl, bg, cudaMemcpyHostToDevice, ctx->st));
+    TK(cudaMemcpyAsync(ctx->nyl, s->nyl, bg, cudaMemcpyHostToDevice, ctx->st));
+    TK(cudaMemcpyAsync(ctx->nzl, s->nzl, bg, cudaMemcpyHostToDevice, ctx->st));
+    for (int f = 0; f < 6; ++f)
+        TK(cudaMemcpyAsync(ctx->lvs_bc[f], s->lvs_bc[f], ctx->D.plane_size(f / 2) * sizeof(double),
+                           cudaMemcpyHostToDevice, ctx->st));
+    for (int f = 0; f < 6; ++f) {
+        ctx->lvs_flag[f] = in->lvs_flag[f];
+        ctx->vof_flag[f] = in->vof_flag[f];
+        ctx->lvs_const[f] = in->lvs_const[f];
+        ctx->vof_const[f] = in->vof_const[f];
+    }
+    ctx->dt = in->dt;
+    TK(cudaStreamSynchronize(ctx->st));
+    ctx->staged = true;
+    return SCF_OK;
+}
+
+extern "C" int scf_clsvof_run(scf_clsvof_ctx *ctx, int32_t steps, scf_clsvof_stats *stats)
+{
+    if (!ctx || steps < 0) return SCF_ERR_BAD_ARG;
+    if (!ctx->staged) {
+        tr_err(ctx, "scf_clsvof_run: nothing staged");
+        return SCF_ERR_BAD_ARG;
+    }
+    cudaSetDevice(ctx->device);
+    int launches = 0, rc;
+    TK(cudaEventRecord(ctx->ev[0], ctx->st));
+    for (int n = 0; n < steps; ++n)
+        if ((rc = scheme_step(ctx, launches)) != SCF_OK) return rc;
+    TK(cudaEventRecord(ctx->ev[1], ctx->st));
+    TK(cudaStreamSynchronize(ctx->st));
+    if (stats) {
+        stats->ms_run = elapsed(ctx->ev[0], ctx->ev[1]);
+        stats->steps = steps;
+        stats->gpu_launches = launches;
+    }
+    return SCF_OK;
+}
+
+extern "C" int scf_clsvof_fetch(scf_clsvof_ctx *ctx, scf_clsvof_state *s, scf_clsvof_stats *stats)
+{
+    if (!ctx || !s) return SCF_ERR_BAD_ARG;
+    if (!ctx->staged) {
+        tr_err(ctx, "scf_clsvof_fetch: nothing staged");
+        return SCF_ERR_BAD_ARG;
+    }
+    double *need[] = {s->vofl, s->phil, s->nxl, s->nyl, s->nzl};
+    for (double *p : need)
+        if (!p) return SCF_ERR_BAD_ARG;
+    for (int f = 0; f < 6; ++f)
+        if (!s->lvs_bc[f] || !s->vof_bc[f]) return SCF_ERR_BAD_ARG;
+    cudaSetDevice(ctx->device);
+    const size_t bg = ctx->D.ghosted() * sizeof(double);
+    TK(cudaEventRecord(ctx->ev[2], ctx->st));
+    TK(cudaMemcpyAsync(s->vofl, ctx->vf[0], bg, cudaMemcpyDeviceToHost, ctx->st));
+    TK(cudaMemcpyAsync(s->phil, ctx->ls[0], bg, cudaMemcpyDeviceToHost, ctx->st));
+    TK(cudaMemcpyAsync(s->nxl, ctx->nxl, bg, cudaMemcpyDeviceToHost, ctx->st));
+    TK(cudaMemcpyAsync(s->nyl, ctx->nyl, bg, cudaMemcpyDeviceToHost, ctx->st));
+    TK(cudaMemcpyAsync(s->nzl, ctx->nzl, bg, cudaMemcpyDeviceToHost, ctx->st));
+    int64_t planes = 0;
+    for (int f = 0; f < 6; ++f) {
+        const size_t pb = ctx->D.plane_size(f / 2) * sizeof(double);
+        TK(cudaMemcpyAsync(s->lvs_bc[f], ctx->lvs_bc[f], pb, cudaMemcpyDeviceToHost, ctx->st));
+        TK(cudaMemcpyAsync(s->vof_bc[f], ctx->vof_bc[f], pb, cudaMemcpyDeviceToHost, ctx->st));
+        planes += 2 * (int64_t)pb;
+    }
+    TK(cudaEventRecord(ctx->ev[3], ctx->st));
+    TK(cudaStreamSynchronize(ctx->st));
+    if (stats) {
+        stats->ms_d2h = elapsed(ctx->ev[2], ctx->ev[3]);
+        stats->bytes_d2h = 5 * (int64_t)bg + planes;
+    }
+    return SCF_OK;
+}
+
+extern "C" int scf_clsvof_step(scf_clsvof_ctx *ctx, const scf_clsvof_in *in, scf_clsvof_state *s,
+                               scf_clsvof_stats *stats)
+{
+    if (!ctx) return SCF_ERR_BAD_ARG;
+    scf_clsvof_stats local{};
+    scf_clsvof_stats *st = stats ? stats : &local;
+    *st = scf_clsvof_stats{};
+    cudaSetDevice(ctx->device);
+    cudaEvent_t t0 = nullptr, t1 = nullptr;
+    TK(cudaEventCreate(&t0));
+    TK(cudaEventCreate(&t1));
+    int rc = SCF_OK;
+    cudaEventRecord(t0, ctx->st);
+    if ((rc = scf_clsvof_stage(ctx, in, s)) == SCF_OK) {
+        cudaEventRecord(t1, ctx->st);
+        cudaEventSynchronize(t1);
+        st->ms_h2d = elapsed(t0, t1);
+        const size_t nin = ctx->D.interior(), ng = ctx->D.ghosted();
+        int64_t planes = 0;
+        for (int a = 0; a < 3; ++a) planes += (int64_t)ctx->D.plane_size(a) * 3;   // bc_vel + two lvs planes
+        st->bytes_h2d = (int64_t)(6 * nin + 11 * ng) * 8 + planes * 8;
+        if ((rc = scf_clsvof_run(ctx, 1, st)) == SCF_OK) rc = scf_clsvof_fetch(ctx, s, st);
+    }
+    cudaEventRecord(t1, ctx->st);
+    cudaEventSynchronize(t1);
+    st->ms_total = elapsed(t0, t1);
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    return rc;
+}
+
+extern "C" int scf_clsvof_device_fields(scf_clsvof_ctx *ctx, double **vofl, double **phil)
+{
+    if (!ctx || !vofl || !phil) return SCF_ERR_BAD_ARG;
+    *vofl = ctx->staged ? ctx->vf[0] : nullptr;
+    *phil = ctx->staged ? ctx->ls[0] : nullptr;
+    return SCF_OK;
+}
+
+extern "C" int scf_clsvof_last_error(scf_clsvof_ctx *ctx, char *buf, size_t n)
+{
+    if (!ctx || !buf || n == 0) return SCF_ERR_BAD_ARG;
+    snprintf(buf, n, "%s", ctx->err);
+    return SCF_OK;
+}

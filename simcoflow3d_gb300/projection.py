@@ -93,6 +93,15 @@ def load_library(path: Optional[str] = None):
         P(capi.ScfMomStats)]
     L.scf_mom_device_fields.argtypes = [C.c_void_p] + [P(C.c_void_p)] * 6
     L.scf_mom_last_error.argtypes = [C.c_void_p, C.c_char_p, C.c_size_t]
+    L.scf_clsvof_create.argtypes = [P(C.c_void_p), C.c_int32, C.c_int32, C.c_int32, C.c_int32]
+    L.scf_clsvof_destroy.argtypes = [C.c_void_p]
+    L.scf_clsvof_stage.argtypes = [C.c_void_p, P(capi.ScfClsvofIn), P(capi.ScfClsvofState)]
+    L.scf_clsvof_run.argtypes = [C.c_void_p, C.c_int32, P(capi.ScfClsvofStats)]
+    L.scf_clsvof_fetch.argtypes = [C.c_void_p, P(capi.ScfClsvofState), P(capi.ScfClsvofStats)]
+    L.scf_clsvof_step.argtypes = [C.c_void_p, P(capi.ScfClsvofIn), P(capi.ScfClsvofState),
+                                  P(capi.ScfClsvofStats)]
+    L.scf_clsvof_device_fields.argtypes = [C.c_void_p, P(C.c_void_p), P(C.c_void_p)]
+    L.scf_clsvof_last_error.argtypes = [C.c_void_p, C.c_char_p, C.c_size_t]
     _lib = L
     return L
 

@@ -14,11 +14,12 @@ HEADER = os.path.join(ROOT, "include", "scf_projection.h")
 GEO_HEADER = os.path.join(ROOT, "include", "scf_geometry.h")
 OUT_HEADER = os.path.join(ROOT, "include", "scf_output.h")
 PRED_HEADER = os.path.join(ROOT, "include", "scf_predictor.h")
+CLSVOF_HEADER = os.path.join(ROOT, "include", "scf_clsvof.h")
 
 
 def declared_functions():
     names = set()
-    for h in (HEADER, GEO_HEADER, OUT_HEADER, PRED_HEADER):
+    for h in (HEADER, GEO_HEADER, OUT_HEADER, PRED_HEADER, CLSVOF_HEADER):
         src = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
         names |= set(re.findall(r"\b(scf_[a-z0-9_]+)\s*\(", src))
     return sorted(names)
@@ -36,6 +37,7 @@ def test_library_exports_every_declared_function(lib_path):
     assert len(names) >= 25
     assert "scf_grid_preprocess" in names and "scf_geo_create" in names and "scf_write_vtr" in names
     assert "scf_predict_solves" in names and "scf_mom_run" in names
+    assert "scf_clsvof_step" in names and "scf_clsvof_run" in names
     for n in names:
         assert hasattr(lib, n), n
     assert lib.scf_abi_version() == 2
@@ -152,6 +154,42 @@ int main(void) {
     m = {"scf_mom_in": capi.ScfMomIn, "scf_mom_opts": capi.ScfMomOpts, "scf_mom_stats": capi.ScfMomStats}
     lines = out.splitlines()
     assert len(lines) == 18
+    for line in lines:
+        t, f, v = line.split()
+        if f == "size":
+            assert C.sizeof(m[t]) == int(v), (t, v)
+        else:
+            assert getattr(m[t], f).offset == int(v), (t, f, v)
+
+
+def test_clsvof_struct_layouts_match_header():
+    from simcoflow3d_gb300 import capi
+    prog = r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "scf_clsvof.h"
+#define P(T, f) printf(#T " " #f " %zu\n", offsetof(T, f));
+int main(void) {
+  printf("scf_clsvof_in size %zu\n", sizeof(scf_clsvof_in));
+  printf("scf_clsvof_state size %zu\n", sizeof(scf_clsvof_state));
+  printf("scf_clsvof_stats size %zu\n", sizeof(scf_clsvof_stats));
+  P(scf_clsvof_in, u) P(scf_clsvof_in, bc_w_b) P(scf_clsvof_in, lvs_flag) P(scf_clsvof_in, vof_flag)
+  P(scf_clsvof_in, lvs_const) P(scf_clsvof_in, vof_const) P(scf_clsvof_in, dt)
+  P(scf_clsvof_state, nzl) P(scf_clsvof_state, lvs_bc) P(scf_clsvof_state, vof_bc)
+  P(scf_clsvof_stats, bytes_h2d) P(scf_clsvof_stats, steps) P(scf_clsvof_stats, gpu_launches)
+  return 0;
+}
+'''
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "m.c")
+        open(c, "w").write(prog)
+        exe = os.path.join(d, "m")
+        subprocess.run(["gcc", "-I", os.path.dirname(CLSVOF_HEADER), c, "-o", exe], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout
+    m = {"scf_clsvof_in": capi.ScfClsvofIn, "scf_clsvof_state": capi.ScfClsvofState,
+         "scf_clsvof_stats": capi.ScfClsvofStats}
+    lines = out.splitlines()
+    assert len(lines) == 16
     for line in lines:
         t, f, v = line.split()
         if f == "size":

@@ -1,0 +1,136 @@
+"""The CLSVOF transport kernels' bodies (simcoflow3d_gb300/csrc/
+transport_body.cuh) compiled for the host with every index range-checked
+(tests/transport_host.cpp drives them over the kernels' thread indices),
+against the oracle's Clsvof_Scheme, bit for bit.  The host build computes
+x**3 and x**(1/3) with the C library's pow like the oracle, so any
+difference is a difference in the kernels' logic or index arithmetic.  CPU
+only; the device run is checked in test_gpu_vof_transport.py."""
+import ctypes as C
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+
+
+@pytest.fixture(scope="module")
+def host_lib(tmp_path_factory):
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("g++ not found")
+    out = str(tmp_path_factory.mktemp("transport_host") / "libtransport_host.so")
+    cmd = [cxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-ffp-contract=off",
+           "-I" + os.path.join(ROOT, "simcoflow3d_gb300", "csrc"), os.path.join(HERE, "transport_host.cpp"), "-o", out]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    L = C.CDLL(out)
+    dp = C.POINTER(C.c_double)
+    L.host_clsvof_step.argtypes = [C.c_int] * 3 + [dp * 6, dp, dp, dp, dp, dp, dp * 3, dp * 3, dp * 3, dp * 6,
+                                                    dp * 6, C.c_int * 6, C.c_double * 6, C.c_int * 6,
+                                                    C.c_double * 6, C.c_double]
+    return L
+
+
+def _p(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def host_step(L, centres, spacings, state, vel, fn, bc_vel, lvs_bc, dt, lvs=((1,) * 6, (0.0,) * 6),
+              vofb=((1,) * 6, (0.0,) * 6)):
+    I, J, K = spacings[0].shape
+    keep = [np.asfortranarray(a, dtype=np.float64) for a in (*centres, *spacings, *fn, *vel, *bc_vel)]
+    dp = C.POINTER(C.c_double)
+    shapes = [(J, K), (J, K), (I, K), (I, K), (I, J), (I, J)]
+    vof_bc = [np.zeros(sh, order="F") for sh in shapes]
+    rc = L.host_clsvof_step(I, J, K, (dp * 6)(*[_p(a) for a in keep[:6]]), _p(state["vofl"]), _p(state["phil"]),
+                            _p(state["nxl"]), _p(state["nyl"]), _p(state["nzl"]),
+                            (dp * 3)(*[_p(a) for a in keep[6:9]]), (dp * 3)(*[_p(a) for a in keep[9:12]]),
+                            (dp * 3)(*[_p(a) for a in keep[12:15]]), (dp * 6)(*[_p(a) for a in lvs_bc]),
+                            (dp * 6)(*[_p(a) for a in vof_bc]), (C.c_int * 6)(*lvs[0]), (C.c_double * 6)(*lvs[1]),
+                            (C.c_int * 6)(*vofb[0]), (C.c_double * 6)(*vofb[1]), float(dt))
+    assert rc == 0
+    return vof_bc
+
+
+def _case(kind):
+    """Inputs of one Clsvof_Scheme call: a tilted plane in a uniform
+    stream, a drop in a shear, a plane at rest with Dirichlet planes, or a
+    drop in a random (divergent) velocity field."""
+    I, J, K = (12, 9, 10) if kind in ("plane", "rest") else (13, 12, 11)
+    h = np.array([1.0 / I, 1.0 / J, 1.0 / K])
+    cs = [(np.arange(m) + 0.5) * hq for m, hq in zip((I, J, K), h)]
+    cg = [(np.arange(m + 2) - 0.5) * hq for m, hq in zip((I, J, K), h)]
+    centres = tuple(np.asfortranarray(a) for a in np.meshgrid(*cs, indexing="ij"))
+    spacings = tuple(np.full((I, J, K), hq, order="F") for hq in h)
+    Xg, Yg, Zg = np.meshgrid(*cg, indexing="ij")
+    g = Xg.shape
+    rng = np.random.default_rng({"plane": 1, "rest": 2, "shear": 3, "random": 4}[kind])
+    if kind in ("plane", "rest"):
+        n = np.array([1.0, 0.15, -0.1]) if kind == "rest" else np.array([1.0, 0.0, 0.15])
+        n /= np.linalg.norm(n)
+        phi = n[0] * (Xg - 0.5) + n[1] * (Yg - 0.5) + n[2] * (Zg - 0.5)
+        from simcoflow3d_gb300 import workloads as W
+        s = phi + 0.5 * (np.abs(n) * h).sum()
+        vof = 1.0 - W.volume_fraction_calc(h[0], h[1], h[2], n[0], n[1], n[2], s) / h.prod()
+        fn = [np.full(g, n[q]) for q in range(3)]
+    else:
+        r = np.sqrt((Xg - 0.48) ** 2 + (Yg - 0.52) ** 2 + (Zg - 0.5) ** 2)
+        phi = r - 0.24
+        sub = (np.arange(4) + 0.5) / 4 - 0.5
+        vof = np.zeros(g)
+        for a in sub:
+            for b in sub:
+                for d in sub:
+                    vof += np.sqrt((Xg + a * h[0] - 0.48) ** 2 + (Yg + b * h[1] - 0.52) ** 2 +
+                                   (Zg + d * h[2] - 0.5) ** 2) < 0.24
+        vof /= 64.0
+        fn = [rng.normal(size=g) for _ in range(3)]
+    vof = np.where(vof <= 1e-14, 0.0, np.where(vof >= 1 - 1e-14, 1.0, vof))
+    if kind == "plane":
+        vel = [np.full(g, 0.9), np.zeros(g), np.zeros(g)]
+    elif kind == "rest":
+        vel = [np.zeros(g) for _ in range(3)]
+    elif kind == "shear":
+        vel = [0.6 * np.sin(2 * np.pi * Yg), 0.3 * np.cos(2 * np.pi * Zg), 0.2 * np.sin(2 * np.pi * Xg)]
+    else:
+        vel = [rng.uniform(-0.8, 0.8, g) for _ in range(3)]
+    vel = [np.asfortranarray(v) for v in vel]
+    state = {"vofl": np.asfortranarray(vof), "phil": np.asfortranarray(phi)}
+    for key in ("nxl", "nyl", "nzl"):
+        state[key] = np.asfortranarray(rng.normal(size=g) * 0.1)
+    shapes = [(J, K), (J, K), (I, K), (I, K), (I, J), (I, J)]
+    lvs_bc = [np.asfortranarray(rng.normal(size=sh) * 0.1) for sh in shapes]
+    bc_vel = [np.asfortranarray(vel[0][0, 1:-1, 1:-1]), np.asfortranarray(vel[1][1:-1, 0, 1:-1]),
+              np.asfortranarray(vel[2][1:-1, 1:-1, 0])]
+    fn = [np.asfortranarray(a) for a in fn]
+    dt = 0.4 * h.min()
+    flags = ((1, 1, 0, 1, 1, 1), (0.0, 0.0, 0.7, 0.3, 0.0, 0.0)) if kind == "rest" else ((1,) * 6, (0.0,) * 6)
+    vflags = ((1, 1, 1, 1, 0, 1), (0.0, 0.0, 0.0, 0.0, 0.25, 0.1)) if kind == "rest" else ((1,) * 6, (0.0,) * 6)
+    return centres, spacings, state, vel, fn, bc_vel, lvs_bc, dt, flags, vflags
+
+
+def _copy(state, planes):
+    return {k: v.copy(order="F") for k, v in state.items()}, [p.copy(order="F") for p in planes]
+
+
+@pytest.mark.parametrize("kind", ["plane", "rest", "shear", "random"])
+def test_kernel_bodies_match_the_oracle(host_lib, kind):
+    centres, spacings, state, vel, fn, bc_vel, lvs_bc, dt, flags, vflags = _case(kind)
+    s_ref, p_ref = _copy(state, lvs_bc)
+    s_got, p_got = _copy(state, lvs_bc)
+    v_ref = O.clsvof_scheme(centres, spacings, s_ref, vel, fn, bc_vel, p_ref, dt, lvs_flag=flags[0],
+                            lvs_const=flags[1], vof_flag=vflags[0], vof_const=vflags[1])
+    v_got = host_step(host_lib, centres, spacings, s_got, vel, fn, bc_vel, p_got, dt, flags, vflags)
+    for key in ("vofl", "phil", "nxl", "nyl", "nzl"):
+        np.testing.assert_array_equal(s_got[key], s_ref[key], err_msg=key)
+    for q in range(6):
+        np.testing.assert_array_equal(p_got[q], p_ref[q], err_msg=f"lvs plane {q}")
+        np.testing.assert_array_equal(v_got[q], v_ref[q], err_msg=f"vof plane {q}")
+    inner = s_ref["vofl"][1:-1, 1:-1, 1:-1]
+    assert ((inner > 0) & (inner < 1)).sum() > 30

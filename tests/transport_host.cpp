@@ -1,0 +1,129 @@
+// transport_host.cpp -- the device bodies of the CLSVOF transport
+// (simcoflow3d_gb300/csrc/transport_body.cuh), compiled for the host with
+// every index range-checked, driven over the same thread indices as the
+// kernels of k_transport.cu, one after the other.  Test infrastructure: it
+// lets the CPU tests check the kernels' index arithmetic and arithmetic
+// against the oracle without a GPU.
+#define TR_HOST_CHECK 1
+#include <string.h>
+
+#include <vector>
+
+#include "transport_body.cuh"
+
+using tr::Dims;
+using tr::Geo;
+
+extern "C" int host_clsvof_step(int I, int J, int K, const double *const geo[6], double *vofl, double *phil,
+                                double *nxl, double *nyl, double *nzl, const double *const fn[3],
+                                const double *const vel[3], const double *const bc_vel[3], double *const lvs_bc[6],
+                                double *const vof_bc[6], const int lvs_flag[6], const double lvs_const[6],
+                                const int vof_flag[6], const double vof_const[6], double dt)
+{
+    const Dims D{I, J, K};
+    const Geo G{geo[0], geo[1], geo[2], geo[3], geo[4], geo[5]};
+    const size_t nin = D.interior(), ng = D.ghosted();
+    std::vector<double> vf[3], ls[3], nx(ng), ny(ng), nz(ng), dis(ng);
+    for (int b = 0; b < 3; ++b) {
+        vf[b].assign(ng, 0.0);
+        ls[b].assign(ng, 0.0);
+    }
+    std::vector<unsigned long long> key(nin);
+    std::vector<uint8_t> fix(nin);
+    memcpy(vf[0].data(), vofl, ng * sizeof(double));
+    memcpy(ls[0].data(), phil, ng * sizeof(double));
+    const double dtv = dt / (double)tr::NSUB;
+    auto reconstruct = [&](int cur, bool tail) {
+        for (size_t t = 0; t < nin; ++t) {   // k_reconstruct
+            int i, j, k;
+            D.cell_of(t, i, j, k);
+            double n1, n2, n3, d1;
+            tr::reconstruct(D, G, vf[cur].data(), ls[cur].data(), i, j, k, n1, n2, n3, d1);
+            const size_t g = D.g(i, j, k);
+            nx[g] = n1;
+            ny[g] = n2;
+            nz[g] = n3;
+            if (tail) {
+                nxl[g] = n1;
+                nyl[g] = n2;
+                nzl[g] = n3;
+                d1 = (0.5 * G.dx[t] * fabs(n1) + 0.5 * G.dy[t] * fabs(n2) + 0.5 * G.dz[t] * fabs(n3)) - d1;
+            }
+            dis[g] = d1;
+        }
+    };
+    for (int kk = 1; kk <= tr::NSUB; ++kk) {
+        const int first = kk % 3 == 0 ? 0 : kk % 3 == 1 ? 1 : 2;
+        int cur = 0;
+        for (int s = 0; s < 3; ++s) {
+            const int ax = (first + s) % 3, out = s == 0 ? 1 : s == 1 ? 2 : 0;
+            reconstruct(cur, false);
+            tr::SweepIn S;
+            S.vfl = vf[cur].data();
+            S.phi = ls[cur].data();
+            S.nx = nx.data();
+            S.ny = ny.data();
+            S.nz = nz.data();
+            S.dis = dis.data();
+            S.vel = vel[ax];
+            S.bc_vel = bc_vel[ax];
+            S.bc_lvs = lvs_bc[2 * ax];
+            S.vf_first = vf[1].data();
+            S.ls_first = ls[1].data();
+            S.dtv = dtv;
+            S.axis = ax;
+            S.stage = s;
+            const int gi = I + 2, gj = J + 2;
+            for (size_t t = 0; t < ng; ++t) {   // k_sweep
+                const int i = (int)(t % (size_t)gi), j = (int)((t / (size_t)gi) % (size_t)gj),
+                          k = (int)(t / ((size_t)gi * gj));
+                if (i < 1 || i > I || j < 1 || j > J || k < 1 || k > K) {
+                    vf[out][t] = S.vfl[t];
+                    ls[out][t] = S.phi[t];
+                    continue;
+                }
+                double a, b;
+                tr::sweep_cell(D, G, S, i, j, k, a, b);
+                vf[out][t] = a;
+                ls[out][t] = b;
+            }
+            cur = out;
+        }
+        tr::WallIn W;
+        W.phil = ls[0].data();
+        W.vofl = vf[0].data();
+        W.nxl = nxl;
+        W.nx = fn[0];
+        W.ny = fn[1];
+        W.nz = fn[2];
+        for (int f = 0; f < 6; ++f) {
+            W.lvs_bc[f] = lvs_bc[f];
+            W.vof_bc[f] = vof_bc[f];
+            W.lvs_flag[f] = lvs_flag[f];
+            W.vof_flag[f] = vof_flag[f];
+            W.lvs_const[f] = lvs_const[f];
+            W.vof_const[f] = vof_const[f];
+        }
+        for (int axis = 0; axis < 3; ++axis)   // k_walls
+            for (size_t t = 0; t < D.plane_size(axis); ++t) tr::wall_point(D, G, W, axis, t);
+        reconstruct(0, true);
+        for (size_t t = 0; t < nin; ++t) {   // k_band_reset
+            key[t] = (unsigned long long)tr::key_of(1.0e4);
+            fix[t] = 0;
+        }
+        for (size_t t = 0; t < nin; ++t) {   // k_band_scatter
+            int i, j, k;
+            D.cell_of(t, i, j, k);
+            tr::band_scatter(D, G, vf[0].data(), ls[0].data(), nx.data(), ny.data(), nz.data(), dis.data(), i, j, k,
+                             key.data(), fix.data());
+        }
+        for (size_t t = 0; t < nin; ++t) {   // k_band_value
+            int i, j, k;
+            D.cell_of(t, i, j, k);
+            ls[0][D.g(i, j, k)] = tr::band_value(D, G, vf[0].data(), dis.data(), i, j, k, key.data(), fix.data());
+        }
+    }
+    memcpy(vofl, vf[0].data(), ng * sizeof(double));
+    memcpy(phil, ls[0].data(), ng * sizeof(double));
+    return 0;
+}
