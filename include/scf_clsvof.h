@@ -9,6 +9,10 @@
  * order y z x, z x y, x y z, then BoundaryConditionLvsVof (2087-2221),
  * Interface_Reconstruct and Redistance_Levelset (1689-1889).
  *
+ * scf_clsvof_uvw_liquid_field replaces ComputeUVWLiquidField
+ * (src/Clsvof.f90:174-298), which derives the U, V, W cells' liquid fields
+ * from the P cells' after the transport.
+ *
  * Arrays are Fortran column-major (i fastest).  "ghosted" means
  * (0:I+1,0:J+1,0:K+1), "interior" (1:I,1:J,1:K); wall planes are (J,K) for
  * the W and E faces, (I,K) for S and N, (I,J) for B and T, in that face
@@ -75,6 +79,23 @@ int scf_clsvof_fetch(scf_clsvof_ctx *ctx, scf_clsvof_state *state, scf_clsvof_st
 /* stage + run(1) + fetch: one Clsvof_Scheme call with host arrays.         */
 int scf_clsvof_step(scf_clsvof_ctx *ctx, const scf_clsvof_in *in, scf_clsvof_state *state,
                     scf_clsvof_stats *stats);
+
+/* One velocity family's cells for ComputeUVWLiquidField.                  */
+typedef struct scf_clsvof_vcell {
+    const double *dx, *dy, *dz;    /* UGrid%dx ... (or V, W), interior          */
+    double *phil, *nxl, *nyl, *nzl;    /* UCell%phiL, %nxL, %nyL, %nzL, ghosted:
+                                      (0:I-1,0:J-1,0:K-1) is written             */
+    double *vofl;                  /* UCell%vofL, ghosted: the interior is written */
+} scf_clsvof_vcell;
+
+/* ComputeUVWLiquidField (src/Clsvof.f90:174-298), which Solver.f90:209 calls
+ * after Clsvof_Scheme: the U, V, W cells' liquid level set, normals and
+ * fraction from the P cells' state on the device (after the last run, or
+ * as staged).  cells[0..2] = U, V, W; their arrays are read (to keep what
+ * is not written) and written back.  The clamp vof + vofL <= 1 of
+ * ComputeVelocityCellLiquidField acts on values the loops then overwrite
+ * in the reference, so it is not applied.                                  */
+int scf_clsvof_uvw_liquid_field(scf_clsvof_ctx *ctx, const scf_clsvof_vcell cells[3], scf_clsvof_stats *stats);
 
 /* The device copies of vofL and phiL (ghosted) after the last run, for
  * callers that keep the fields on the GPU (0 if not staged).               */

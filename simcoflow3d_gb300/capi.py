@@ -209,6 +209,11 @@ class ScfClsvofState(C.Structure):
         ("lvs_bc", c_double_p * 6), ("vof_bc", c_double_p * 6)]
 
 
+class ScfClsvofVcell(C.Structure):
+    """scf_clsvof_vcell of include/scf_clsvof.h: one velocity family."""
+    _fields_ = [(n, c_double_p) for n in ("dx", "dy", "dz", "phil", "nxl", "nyl", "nzl", "vofl")]
+
+
 class ScfClsvofStats(C.Structure):
     _fields_ = [("ms_h2d", C.c_double), ("ms_run", C.c_double), ("ms_d2h", C.c_double), ("ms_total", C.c_double),
                 ("bytes_h2d", C.c_int64), ("bytes_d2h", C.c_int64), ("steps", C.c_int32),

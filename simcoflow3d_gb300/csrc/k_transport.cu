@@ -45,6 +45,8 @@ struct scf_clsvof_ctx {
     double *lvs_bc[6] = {}, *vof_bc[6] = {};
     unsigned long long *key = nullptr;
     uint8_t *fix = nullptr;
+    double *vgeo[3][3] = {};             // U, V, W grid spacings (allocated on first use)
+    double *vfld[3][5] = {};             // U, V, W: phiL, nxL, nyL, nzL, vofL
     int lvs_flag[6] = {}, vof_flag[6] = {};
     double lvs_const[6] = {}, vof_const[6] = {};
     double dt = 0.0;
@@ -173,6 +175,33 @@ __global__ void k_band_value(Dims D, Geo G, const double *__restrict__ vfl, cons
         int i, j, k;
         D.cell_of(t, i, j, k);
         phi[D.g(i, j, k)] = tr::band_value(D, G, vfl, dis, i, j, k, key, fix);
+    }
+}
+
+// ComputeUVWLiquidField for one family over its ghosted grid: the cells of
+// (0:I-1,0:J-1,0:K-1) take the direction averages, the interior cells the
+// liquid fraction.
+__global__ void k_uvw(Dims D, int fam, Geo G, const double *__restrict__ phil, const double *__restrict__ nxl,
+                      const double *__restrict__ nyl, const double *__restrict__ nzl, const double *__restrict__ vofl,
+                      const double *__restrict__ vdx, const double *__restrict__ vdy, const double *__restrict__ vdz,
+                      double *o_phil, double *o_nxl, double *o_nyl, double *o_nzl, double *o_vofl)
+{
+    const size_t ng = D.ghosted();
+    const int gi = D.I + 2, gj = D.J + 2;
+    const double *pin[4] = {phil, nxl, nyl, nzl};
+    const double *d = fam == 0 ? G.dx : fam == 1 ? G.dy : G.dz;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < ng; t += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(t % (size_t)gi), j = (int)((t / (size_t)gi) % (size_t)gj), k = (int)(t / ((size_t)gi * gj));
+        if (i < D.I && j < D.J && k < D.K) {
+            double av[4];
+            tr::family_average(D, fam, d, pin, i, j, k, av);
+            o_phil[t] = av[0];
+            o_nxl[t] = av[1];
+            o_nyl[t] = av[2];
+            o_nzl[t] = av[3];
+        }
+        if (i >= 1 && i <= D.I && j >= 1 && j <= D.J && k >= 1 && k <= D.K)
+            o_vofl[t] = tr::family_vofl(D, fam, G.dx, G.dy, G.dz, phil, nxl, nyl, nzl, vofl, vdx, vdy, vdz, i, j, k);
     }
 }
 
@@ -468,6 +497,70 @@ extern "C" int scf_clsvof_step(scf_clsvof_ctx *ctx, const scf_clsvof_in *in, scf
     cudaEventDestroy(t0);
     cudaEventDestroy(t1);
     return rc;
+}
+
+extern "C" int scf_clsvof_uvw_liquid_field(scf_clsvof_ctx *ctx, const scf_clsvof_vcell cells[3],
+                                           scf_clsvof_stats *stats)
+{
+    if (!ctx || !cells) return SCF_ERR_BAD_ARG;
+    if (!ctx->staged) {
+        tr_err(ctx, "scf_clsvof_uvw_liquid_field: nothing staged");
+        return SCF_ERR_BAD_ARG;
+    }
+    for (int f = 0; f < 3; ++f) {
+        const scf_clsvof_vcell &c = cells[f];
+        if (!c.dx || !c.dy || !c.dz || !c.phil || !c.nxl || !c.nyl || !c.nzl || !c.vofl) {
+            tr_err(ctx, "scf_clsvof_uvw_liquid_field: a required array of family %d is null", f);
+            return SCF_ERR_BAD_ARG;
+        }
+    }
+    cudaSetDevice(ctx->device);
+    const size_t nin = ctx->D.interior(), ng = ctx->D.ghosted();
+    int rc;
+    for (int f = 0; f < 3; ++f) {
+        for (auto &p : ctx->vgeo[f])
+            if (!p && (rc = alloc(ctx, &p, nin)) != SCF_OK) return rc;
+        for (auto &p : ctx->vfld[f])
+            if (!p && (rc = alloc(ctx, &p, ng)) != SCF_OK) return rc;
+    }
+    TK(cudaEventRecord(ctx->ev[0], ctx->st));
+    for (int f = 0; f < 3; ++f) {
+        const scf_clsvof_vcell &c = cells[f];
+        const double *g[3] = {c.dx, c.dy, c.dz};
+        double *h[5] = {c.phil, c.nxl, c.nyl, c.nzl, c.vofl};
+        for (int q = 0; q < 3; ++q)
+            TK(cudaMemcpyAsync(ctx->vgeo[f][q], g[q], nin * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+        for (int q = 0; q < 5; ++q)
+            TK(cudaMemcpyAsync(ctx->vfld[f][q], h[q], ng * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+    }
+    TK(cudaEventRecord(ctx->ev[1], ctx->st));
+    const Geo G = geo_of(ctx);
+    for (int f = 0; f < 3; ++f) {
+        k_uvw<<<blocks_for(ng), NT, 0, ctx->st>>>(ctx->D, f, G, ctx->ls[0], ctx->nxl, ctx->nyl, ctx->nzl, ctx->vf[0],
+                                                 ctx->vgeo[f][0], ctx->vgeo[f][1], ctx->vgeo[f][2], ctx->vfld[f][0],
+                                                 ctx->vfld[f][1], ctx->vfld[f][2], ctx->vfld[f][3], ctx->vfld[f][4]);
+        if ((rc = launch_check(ctx, "k_uvw")) != SCF_OK) return rc;
+    }
+    TK(cudaEventRecord(ctx->ev[2], ctx->st));
+    for (int f = 0; f < 3; ++f) {
+        const scf_clsvof_vcell &c = cells[f];
+        double *h[5] = {c.phil, c.nxl, c.nyl, c.nzl, c.vofl};
+        for (int q = 0; q < 5; ++q)
+            TK(cudaMemcpyAsync(h[q], ctx->vfld[f][q], ng * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+    }
+    TK(cudaEventRecord(ctx->ev[3], ctx->st));
+    TK(cudaStreamSynchronize(ctx->st));
+    if (stats) {
+        *stats = scf_clsvof_stats{};
+        stats->ms_h2d = elapsed(ctx->ev[0], ctx->ev[1]);
+        stats->ms_run = elapsed(ctx->ev[1], ctx->ev[2]);
+        stats->ms_d2h = elapsed(ctx->ev[2], ctx->ev[3]);
+        stats->ms_total = elapsed(ctx->ev[0], ctx->ev[3]);
+        stats->bytes_h2d = (int64_t)(3 * (3 * nin + 5 * ng)) * 8;
+        stats->bytes_d2h = (int64_t)(15 * ng) * 8;
+        stats->gpu_launches = 3;
+    }
+    return SCF_OK;
 }
 
 extern "C" int scf_clsvof_device_fields(scf_clsvof_ctx *ctx, double **vofl, double **phil)

@@ -679,4 +679,88 @@ TR_HD void wall_point(const Dims &D, const Geo &G, const WallIn &W, int axis, si
     W.vofl[gx] = vn;
 }
 
+// ---- the velocity cells' liquid fields (ComputeUVWLiquidField 174-353) ----
+
+// ConvertTheCoordinateSystem (2458-2465): phi measured from the corner.
+TR_HD double corner_level(double dx, double dy, double dz, double nx, double ny, double nz, double phi)
+{
+    return phi + 0.5 * (fabs(nx) * dx + fabs(ny) * dy + fabs(nz) * dz);
+}
+
+// The four averaged fields (phiL, nxL, nyL, nzL) of velocity family `fam`
+// (0 U, 1 V, 2 W) at its cell (p, q, r), 0 <= p < I, 0 <= q < J, 0 <= r < K.
+// DirectionAverageArray (328-353) writes the average of the P cells
+// (i, i+1) along the family's axis into VelCell(i-1, j-1, k-1) -- an
+// assumed-shape dummy numbered from 1 over arrays allocated from 0 -- and
+// copies the last one once more, so the cell gathers the P pair at
+// (p+1, q+1, r+1) with the axis index held at n-1.  d: the P spacing along
+// the axis.
+TR_HD void family_average(const Dims &D, int fam, const double *d, const double *const pin[4], int p, int q, int r,
+                          double out[4])
+{
+    int i = p + 1, j = q + 1, k = r + 1;
+    if (fam == 0 && i == D.I) i = D.I - 1;
+    if (fam == 1 && j == D.J) j = D.J - 1;
+    if (fam == 2 && k == D.K) k = D.K - 1;
+    const int i2 = i + (fam == 0), j2 = j + (fam == 1), k2 = k + (fam == 2);
+    const double lamda = d[D.n(i2, j2, k2)] / (d[D.n(i, j, k)] + d[D.n(i2, j2, k2)]);
+    const size_t a = D.g(i, j, k), b = D.g(i2, j2, k2);
+    for (int f = 0; f < 4; ++f) out[f] = lamda * pin[f][a] + (1.0 - lamda) * pin[f][b];
+}
+
+// The liquid fraction of velocity cell (i, j, k) of family `fam`: the
+// liquid in the half of P cell (i, j, k) on its high side plus the half of
+// the next P cell on its low side, over the velocity cell's volume; the
+// last cell of each line takes the P cell's own fraction (ComputeUVW-
+// LiquidField 186-297).  Kept as the reference computes them: the V cell's
+// low half cuts with the whole dy and the unshifted level set, its high
+// half starts from phiL(i,j,k) with the normal of (i,j+1,k); the W cell's
+// high half shifts by +dz/2 where the U cell's shifts by -dx/2.
+TR_HD double family_vofl(const Dims &D, int fam, const double *pdx, const double *pdy, const double *pdz,
+                         const double *phil, const double *nxl, const double *nyl, const double *nzl,
+                         const double *vofl, const double *vdx, const double *vdy, const double *vdz, int i, int j,
+                         int k)
+{
+    const int n = D.len(fam), m = fam == 0 ? i : fam == 1 ? j : k;
+    const size_t a = D.g(i, j, k), na = D.n(i, j, k);
+    if (m == n) return vofl[a];
+    const int i2 = i + (fam == 0), j2 = j + (fam == 1), k2 = k + (fam == 2);
+    const size_t b = D.g(i2, j2, k2), nb = D.n(i2, j2, k2);
+    double dcell, phinew, dist, left, right;
+    if (fam == 0) {
+        dcell = pdx[na] / 2.0;
+        phinew = phil[a] + dcell * nxl[a];
+        dist = corner_level(dcell, pdy[na], pdz[na], nxl[a], nyl[a], nzl[a], phinew);
+        left = volume_fraction(dcell, pdy[na], pdz[na], nxl[a], nyl[a], nzl[a], dist);
+        left = dcell * pdy[na] * pdz[na] - left;
+        dcell = pdx[nb] / 2.0;
+        phinew = phil[b] - dcell * nxl[b];
+        dist = corner_level(dcell, pdy[nb], pdz[nb], nxl[b], nyl[b], nzl[b], phinew);
+        right = volume_fraction(dcell, pdy[nb], pdz[nb], nxl[b], nyl[b], nzl[b], dist);
+        right = dcell * pdy[nb] * pdz[nb] - right;
+    } else if (fam == 1) {
+        dcell = pdy[na] / 2.0;
+        dist = corner_level(pdx[na], pdy[na], pdz[na], nxl[a], nyl[a], nzl[a], phil[a]);
+        left = volume_fraction(pdx[na], dcell, pdz[na], nxl[a], nyl[a], nzl[a], dist);
+        left = pdx[na] * dcell * pdz[na] - left;
+        dcell = pdy[nb] / 2.0;
+        phinew = phil[a] + dcell * nyl[b];
+        dist = corner_level(pdx[nb], dcell, pdz[nb], nxl[b], nyl[b], nzl[b], phinew);
+        right = volume_fraction(pdx[nb], dcell, pdz[nb], nxl[b], nyl[b], nzl[b], dist);
+        right = pdx[nb] * dcell * pdz[nb] - right;
+    } else {
+        dcell = pdz[na] / 2.0;
+        phinew = phil[a] + dcell * nzl[a];
+        dist = corner_level(pdx[na], pdy[na], dcell, nxl[a], nyl[a], nzl[a], phinew);
+        left = volume_fraction(pdx[na], pdy[na], dcell, nxl[a], nyl[a], nzl[a], dist);
+        left = pdx[na] * pdy[na] * dcell - left;
+        dcell = pdz[nb] / 2.0;
+        phinew = phil[b] + dcell * nzl[b];
+        dist = corner_level(pdx[nb], pdy[nb], dcell, nxl[b], nyl[b], nzl[b], phinew);
+        right = volume_fraction(pdx[nb], pdy[nb], dcell, nxl[b], nyl[b], nzl[b], dist);
+        right = pdx[nb] * pdy[nb] * dcell - right;
+    }
+    return (left + right) / vdx[na] / vdy[na] / vdz[na];
+}
+
 }  // namespace tr

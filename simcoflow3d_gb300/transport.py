@@ -136,6 +136,29 @@ class ClsvofScheme:
             self._err(rc)
         return vof_bc, st.as_dict()
 
+    def uvw_liquid_field(self, vgrids, vcells) -> dict:
+        """scf_clsvof_uvw_liquid_field (ComputeUVWLiquidField) from the P
+        cells' device state after the last run or stage.  ``vgrids``: three
+        (dx, dy, dz) interior arrays of the U, V, W grids; ``vcells``: three
+        dicts of ghosted phil, nxl, nyl, nzl, vofl, updated in place."""
+        I, J, K = self.shape
+        cells = (capi.ScfClsvofVcell * 3)()
+        keep = []
+        for f in range(3):
+            g = [_f64(a) for a in vgrids[f]]
+            c = [_f64(vcells[f][k]) for k in ("phil", "nxl", "nyl", "nzl", "vofl")]
+            for a in g:
+                assert a.shape == (I, J, K)
+            for a in c:
+                assert a.shape == (I + 2, J + 2, K + 2)
+            keep += g + c
+            cells[f] = capi.ScfClsvofVcell(*(capi.dptr(a) for a in g + c))
+        st = capi.ScfClsvofStats()
+        rc = self.L.scf_clsvof_uvw_liquid_field(self.ctx, cells, C.byref(st))
+        if rc != 0:
+            self._err(rc)
+        return st.as_dict()
+
     def device_fields(self):
         a, b = C.c_void_p(), C.c_void_p()
         rc = self.L.scf_clsvof_device_fields(self.ctx, C.byref(a), C.byref(b))

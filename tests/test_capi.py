@@ -177,6 +177,8 @@ int main(void) {
   P(scf_clsvof_in, lvs_const) P(scf_clsvof_in, vof_const) P(scf_clsvof_in, dt)
   P(scf_clsvof_state, nzl) P(scf_clsvof_state, lvs_bc) P(scf_clsvof_state, vof_bc)
   P(scf_clsvof_stats, bytes_h2d) P(scf_clsvof_stats, steps) P(scf_clsvof_stats, gpu_launches)
+  printf("scf_clsvof_vcell size %zu\n", sizeof(scf_clsvof_vcell));
+  P(scf_clsvof_vcell, phil) P(scf_clsvof_vcell, vofl)
   return 0;
 }
 '''
@@ -187,9 +189,9 @@ int main(void) {
         subprocess.run(["gcc", "-I", os.path.dirname(CLSVOF_HEADER), c, "-o", exe], check=True)
         out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout
     m = {"scf_clsvof_in": capi.ScfClsvofIn, "scf_clsvof_state": capi.ScfClsvofState,
-         "scf_clsvof_stats": capi.ScfClsvofStats}
+         "scf_clsvof_stats": capi.ScfClsvofStats, "scf_clsvof_vcell": capi.ScfClsvofVcell}
     lines = out.splitlines()
-    assert len(lines) == 16
+    assert len(lines) == 19
     for line in lines:
         t, f, v = line.split()
         if f == "size":

@@ -102,6 +102,38 @@ def test_gpu_shear_keeps_the_liquid_volume(lib):
     assert abs(after - before) < 1e-10 * before
 
 
+@pytest.mark.parametrize("seed", [5, 6])
+def test_gpu_uvw_liquid_field_matches_the_oracle(lib, seed):
+    """ComputeUVWLiquidField on the device from the staged P cells, against
+    the oracle: the direction averages bit for bit, the liquid fractions to
+    1e-12 (x**3 is the only difference in rounding)."""
+    from simcoflow3d_gb300.transport import ClsvofScheme
+    from test_transport_host import _uvw_case
+    pgrid, pcell, vgrids, vcells = _uvw_case(seed)
+    ref = [{k: v.copy(order="F") for k, v in c.items()} for c in vcells]
+    O.uvw_liquid_field(pgrid, pcell, vgrids, ref)
+    I, J, K = pgrid[0].shape
+    g = (I + 2, J + 2, K + 2)
+    zg = np.zeros(g, order="F")
+    centres = tuple(np.zeros((I, J, K), order="F") for _ in range(3))
+    state = {k: pcell[k].copy(order="F") for k in ("vofl", "phil", "nxl", "nyl", "nzl")}
+    planes = [np.zeros(sh, order="F") for sh in [(J, K)] * 2 + [(I, K)] * 2 + [(I, J)] * 2]
+    got = [{k: v.copy(order="F") for k, v in c.items()} for c in vcells]
+    sch = ClsvofScheme(I, J, K, lib=lib)
+    try:
+        sch.stage(centres, pgrid, state, [zg] * 3, [zg] * 3,
+                  [np.zeros((J, K), order="F"), np.zeros((I, K), order="F"), np.zeros((I, J), order="F")],
+                  planes, 0.0)
+        st = sch.uvw_liquid_field(vgrids, got)
+        assert st["gpu_launches"] == 3
+    finally:
+        sch.close()
+    for f in range(3):
+        for k in ("phil", "nxl", "nyl", "nzl"):
+            np.testing.assert_array_equal(got[f][k], ref[f][k], err_msg=f"family {f} {k}")
+        np.testing.assert_allclose(got[f]["vofl"], ref[f]["vofl"], rtol=0, atol=1e-12)
+
+
 def test_gpu_rejects_bad_arguments(lib):
     import ctypes as C
     from simcoflow3d_gb300.projection import ScfError

@@ -127,3 +127,32 @@ extern "C" int host_clsvof_step(int I, int J, int K, const double *const geo[6],
     memcpy(phil, ls[0].data(), ng * sizeof(double));
     return 0;
 }
+
+// ComputeUVWLiquidField: k_uvw for the three families over the ghosted grid.
+// pd: the P spacings (interior); pf: the P cells' phiL, nxL, nyL, nzL, vofL;
+// vg[f]: family f's spacings; vf[f]: its phiL, nxL, nyL, nzL, vofL (in/out).
+extern "C" int host_uvw(int I, int J, int K, const double *const pd[3], const double *const pf[5],
+                        const double *const vg[9], double *const vf[15])
+{
+    const Dims D{I, J, K};
+    const Geo G{nullptr, nullptr, nullptr, pd[0], pd[1], pd[2]};
+    const int gi = I + 2, gj = J + 2;
+    const double *pin[4] = {pf[0], pf[1], pf[2], pf[3]};
+    for (int fam = 0; fam < 3; ++fam) {
+        const double *d = fam == 0 ? G.dx : fam == 1 ? G.dy : G.dz;
+        double *const *o = vf + 5 * fam;
+        for (size_t t = 0; t < D.ghosted(); ++t) {
+            const int i = (int)(t % (size_t)gi), j = (int)((t / (size_t)gi) % (size_t)gj),
+                      k = (int)(t / ((size_t)gi * gj));
+            if (i < I && j < J && k < K) {
+                double av[4];
+                tr::family_average(D, fam, d, pin, i, j, k, av);
+                for (int q = 0; q < 4; ++q) o[q][t] = av[q];
+            }
+            if (i >= 1 && i <= I && j >= 1 && j <= J && k >= 1 && k <= K)
+                o[4][t] = tr::family_vofl(D, fam, G.dx, G.dy, G.dz, pf[0], pf[1], pf[2], pf[3], pf[4],
+                                          vg[3 * fam], vg[3 * fam + 1], vg[3 * fam + 2], i, j, k);
+        }
+    }
+    return 0;
+}
