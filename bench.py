@@ -226,6 +226,32 @@ def run_reference(args):
     if rank != 0:
         barrier(dist)
         return 0
+    if args.config == "clsvof":
+        n = args.n or 256
+        ms = []
+        for i in range(args.warmup + args.steps):
+            t, _ = clsvof_cpu_ms(n)
+            if i >= args.warmup:
+                ms.append(t)
+            if args.max_cpu_s and sum(ms) / 1e3 * 64 ** 3 / n ** 3 > args.max_cpu_s and len(ms) >= 1:
+                break
+        v = statistics.mean(ms)
+        line = {
+            "impl": "reference", "metric": "ms per Clsvof_Scheme step at %d^3 (6 sub-steps x 3 split sweeps, wall "
+                                           "planes, reconstruction, redistancing)" % n,
+            "value": round(v, 3), "unit": "ms/step", "n_gpus": ws, "steps": len(ms), "warmup": args.warmup,
+            "ms_per_step": round(v, 3), "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic: the 3-D deformation test of the reference's AdvectionTest at t = 0",
+            "config": {"workload": "CLSVOF transport: liquid sphere r=0.15 at (0.35,0.35,0.35) in the %d^3 unit "
+                                   "cube, LeVeque deformation field, CFL 0.15" % n, "grid": [n, n, n]},
+            "cpu_baseline": {"value": round(v, 3), "unit": "ms/step", "cores": 1, "kind": "port",
+                             "sample": "each step one oracle Clsvof_Scheme step at 64^3 (the reference test's own "
+                                       "grid), scaled by the cell count to %d^3" % n},
+            "e2e": {"value": round(v, 3), "unit": "ms/step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line), flush=True)
+        barrier(dist)
+        return 0
     threads = os.cpu_count() or 1
     os.environ["OMP_NUM_THREADS"] = str(threads)
     w = make_workload(args.config, args.seed, args.n)
@@ -641,6 +667,152 @@ def run_predictor(args):
     return 0
 
 
+def clsvof_workload(n: int):
+    """The 3-D deformation test of the reference's src/Test/AdvectionTest at
+    t = 0 on an n^3 unit cube: a liquid sphere r = 0.15 at (0.35, 0.35, 0.35)
+    (phiL its signed distance, vofL the cut of each cell by the sphere's
+    tangent plane), u = 2 sin^2(pi x) sin(2 pi y) sin(2 pi z) and its v, w
+    partners at the cell centres (zero in the ghosts), the fluid normals of
+    a sphere about (1000, 1000, 1000), Dirichlet zero walls, dt from CFL 0.15
+    capped at 0.15 h / 0.2 (AdvectionTest.f90:180-212)."""
+    import numpy as np
+    from simcoflow3d_gb300 import workloads as W
+    h = 1.0 / n
+    c = (np.arange(n) + 0.5) * h
+    cg = (np.arange(n + 2) - 0.5) * h
+    centres = tuple(np.asfortranarray(a) for a in np.meshgrid(c, c, c, indexing="ij"))
+    spacings = tuple(np.full((n, n, n), h, order="F") for _ in range(3))
+    X, Y, Z = np.meshgrid(cg, cg, cg, indexing="ij")
+    dx, dy, dz = X - 0.35, Y - 0.35, Z - 0.35
+    r = np.sqrt(dx * dx + dy * dy + dz * dz)
+    phi = np.asfortranarray(r - 0.15)
+    rn = np.maximum(r, 1e-300)
+    nx, ny, nz = dx / rn, dy / rn, dz / rn
+    s = phi + 0.5 * h * (np.abs(nx) + np.abs(ny) + np.abs(nz))
+    vof = 1.0 - W.volume_fraction_calc(h, h, h, nx, ny, nz, s) / h ** 3
+    vof = np.asfortranarray(np.where(vof <= 1e-14, 0.0, np.where(vof >= 1 - 1e-14, 1.0, vof)))
+    inner = (slice(1, -1),) * 3
+    vel = [np.zeros((n + 2,) * 3, order="F") for _ in range(3)]
+    sx, sy, sz = np.sin(np.pi * X), np.sin(np.pi * Y), np.sin(np.pi * Z)
+    s2x, s2y, s2z = np.sin(2 * np.pi * X), np.sin(2 * np.pi * Y), np.sin(2 * np.pi * Z)
+    vel[0][inner] = (2.0 * sx * sx * s2y * s2z)[inner]
+    vel[1][inner] = (-s2x * sy * sy * s2z)[inner]
+    vel[2][inner] = (-s2x * s2y * sz * sz)[inner]
+    fx, fy, fz = X - 1000.0, Y - 1000.0, Z - 1000.0
+    fr = np.sqrt(fx * fx + fy * fy + fz * fz)
+    fn = [np.zeros((n + 2,) * 3, order="F") for _ in range(3)]
+    for q, f in enumerate((fx, fy, fz)):
+        fn[q][inner] = (f / fr)[inner]
+    vmax = max(np.abs(v).max() for v in vel)
+    dt = min(0.15 * h / (vmax + 1e-30), 0.15 * h / 0.2)
+    state = {"vofl": vof, "phil": phi}
+    for key in ("nxl", "nyl", "nzl"):
+        state[key] = np.zeros((n + 2,) * 3, order="F")
+    shapes = [(n, n)] * 6
+    lvs_bc = [np.zeros(sh, order="F") for sh in shapes]
+    bc_vel = [np.zeros((n, n), order="F") for _ in range(3)]
+    flags = dict(lvs_flag=(0,) * 6, lvs_const=(0.0,) * 6, vof_flag=(0,) * 6, vof_const=(0.0,) * 6)
+    return centres, spacings, state, vel, fn, bc_vel, lvs_bc, dt, flags
+
+
+# algorithmic bytes per interior cell of one launch: the fields a kernel must
+# read and write once (neighbours come from cache)
+CLSVOF_BYTES = {"sweep_first": 40, "sweep_later": 56, "reconstruct": 40}
+
+
+def clsvof_cpu_ms(n_full: int, sample_n: int = 64):
+    """The oracle's Clsvof_Scheme step on the same test at sample_n^3 (the
+    reference test's own size), scaled to n_full^3 by the cell count."""
+    from oracle import oracle as O
+    centres, spacings, state, vel, fn, bc_vel, lvs_bc, dt, flags = clsvof_workload(sample_n)
+    t0 = time.perf_counter()
+    O.clsvof_scheme(centres, spacings, state, vel, fn, bc_vel, lvs_bc, dt, **flags)
+    sec = time.perf_counter() - t0
+    return sec * 1e3 * (n_full / sample_n) ** 3, sec
+
+
+def run_clsvof(args):
+    """One Clsvof_Scheme step (six sub-steps of three split sweeps, the wall
+    planes, the reconstruction and the redistancing) on the reference's
+    3-D deformation test scaled to 256^3: device time with the state
+    resident, the host-array call end to end, the live roofline of the
+    heaviest kernel kind, and the oracle on the host cores.  One JSON line."""
+    import numpy as np
+    from simcoflow3d_gb300.projection import load_library
+    from simcoflow3d_gb300.transport import ClsvofScheme
+    n = args.n or 256
+    centres, spacings, state, vel, fn, bc_vel, lvs_bc, dt, flags = clsvof_workload(n)
+    lib = load_library()
+    sch = ClsvofScheme(n, n, n, lib=lib)
+    work = {k: v.copy(order="F") for k, v in state.items()}
+    planes = [p.copy(order="F") for p in lvs_bc]
+    sch.stage(centres, spacings, work, vel, fn, bc_vel, planes, dt, **flags)
+    for _ in range(args.warmup):
+        sch.run(1)
+    with ClockSampler(0) as cs:
+        runs = [sch.run(1) for _ in range(args.steps)]
+    clocks = cs.summary()
+    sch.set_timing(True)
+    timed = [sch.run(1) for _ in range(2)]
+    sch.set_timing(False)
+    # end to end through scf_clsvof_step with page-locked host arrays
+    e_state = {k: v.copy(order="F") for k, v in state.items()}
+    e_planes = [p.copy(order="F") for p in lvs_bc]
+    pinned = []
+    for arr in list(e_state.values()) + e_planes + list(centres) + list(spacings) + vel + fn + bc_vel:
+        if arr.nbytes and lib.scf_host_register(arr.ctypes.data, arr.nbytes) == 0:
+            pinned.append(arr)
+    e2e = [sch(centres, spacings, e_state, vel, fn, bc_vel, e_planes, dt, **flags)[1]
+           for _ in range(max(3, args.steps // 4))]
+    unpin(lib, pinned)
+    sch.close()
+    cells = n ** 3
+    kinds = ("reconstruct", "sweep", "walls", "redistance")
+    kms = {k: sum(t["ms_kernels"][q] for t in timed) / len(timed) for q, k in enumerate(kinds)}
+    # per step: 18 sweeps (6 first, 12 later) and 24 reconstructions
+    sweep_bytes = 6 * cells * (CLSVOF_BYTES["sweep_first"] + 2 * CLSVOF_BYTES["sweep_later"])
+    rec_bytes = 24 * cells * CLSVOF_BYTES["reconstruct"]
+    top = max(("sweep", "reconstruct"), key=lambda k: kms[k])
+    tb = {"sweep": sweep_bytes, "reconstruct": rec_bytes}[top]
+    launches = {"sweep": 18, "reconstruct": 24}[top]
+    achieved = tb / (kms[top] * 1e-3) / 1e9
+    peak, peak_kind = measured_peaks()
+    cpu = None
+    if not args.no_cpu:
+        ms_cpu, sec = clsvof_cpu_ms(n)
+        cpu = {"value": round(ms_cpu, 1), "unit": "ms/step", "cores": 1, "kind": "port",
+               "sample": "one oracle Clsvof_Scheme step of the same test at 64^3 (the reference test's own grid), "
+                         "%.2f s, scaled by the cell count to %d^3" % (sec, n)}
+    ms = [r["ms_run"] for r in runs]
+    line = {
+        "metric": "ms per Clsvof_Scheme step at %d^3 (6 sub-steps x 3 split sweeps, wall planes, reconstruction, "
+                  "redistancing)" % n,
+        "value": round(statistics.mean(ms), 3), "unit": "ms/step", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(statistics.mean(ms), 3), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: the 3-D deformation test of the reference's AdvectionTest at t = 0",
+        "config": {"workload": "CLSVOF transport: liquid sphere r=0.15 at (0.35,0.35,0.35) in the %d^3 unit cube, "
+                               "LeVeque deformation field, CFL 0.15, dt = %.3e" % (n, dt),
+                   "grid": [n, n, n],
+                   "l2": "inputs larger than L2 (%.1f GB staged)" % (e2e[-1]["bytes_h2d"] / 1e9)},
+        "e2e": {"value": round(statistics.mean(r["ms_total"] for r in e2e), 3), "unit": "ms/step",
+                "h2d_bytes_per_step": int(e2e[-1]["bytes_h2d"]), "d2h_bytes_per_step": int(e2e[-1]["bytes_d2h"]),
+                "ms_h2d": round(statistics.mean(r["ms_h2d"] for r in e2e), 3),
+                "ms_d2h": round(statistics.mean(r["ms_d2h"] for r in e2e), 3)},
+        "roofline": {"bound": "hbm", "kernel": {"sweep": "k_sweep", "reconstruct": "k_reconstruct"}[top],
+                     "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "peak_kind": peak_kind, "bytes_per_launch": tb // launches,
+                     "ms_per_launch": round(kms[top] / launches, 5),
+                     "kinds_ms_per_step": {k: round(v, 4) for k, v in kms.items()},
+                     "timing": "CUDA events around every kernel of 2 steps", "traffic": None},
+        "clocks": clocks,
+        "gpu_launches": sum(r["gpu_launches"] for r in runs),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_output(args):
     """PrintResultVTK's snapshot of a c2 projection (p, u, v, w, phiL, phi,
     vofL, vof at 256^3) written by scf_write_vtr from the projection
@@ -719,7 +891,8 @@ def main():
     ap.add_argument("--config", default="c2",
                     help="c0..c4; geometry (the cut-cell geometry preprocessing of the c2 geometry); output "
                          "(a PrintResultVTK snapshot of a c2 projection); predictor (the momentum predictor's "
-                         "implicit solves on the c2 geometry)")
+                         "implicit solves on the c2 geometry); clsvof (one Clsvof_Scheme step of the "
+                         "reference's 3-D deformation test at 256^3)")
     ap.add_argument("--tol", type=float, default=1e-8)
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--n", type=int, default=None, help="smaller grid (profiling captures only)")
@@ -744,6 +917,8 @@ def main():
         return run_output(args)
     if args.config == "predictor":
         return run_predictor(args)
+    if args.config == "clsvof":
+        return run_clsvof(args)
     return run_ours(args)
 
 

@@ -63,6 +63,9 @@ typedef struct scf_clsvof_stats {
     int64_t bytes_h2d, bytes_d2h;
     int32_t steps;                 /* time steps run by the last call            */
     int32_t gpu_launches;          /* kernels launched by the last run           */
+    double ms_kernels[4];          /* with scf_clsvof_set_timing: the summed
+                                      times of k_reconstruct, k_sweep, k_walls
+                                      and the three redistancing kernels       */
 } scf_clsvof_stats;
 
 typedef struct scf_clsvof_ctx scf_clsvof_ctx;
@@ -76,6 +79,9 @@ int scf_clsvof_stage(scf_clsvof_ctx *ctx, const scf_clsvof_in *in, const scf_cls
 int scf_clsvof_run(scf_clsvof_ctx *ctx, int32_t steps, scf_clsvof_stats *stats);
 /* Copies the state back.                                                   */
 int scf_clsvof_fetch(scf_clsvof_ctx *ctx, scf_clsvof_state *state, scf_clsvof_stats *stats);
+/* With on != 0, scf_clsvof_run times every kernel with CUDA events (and
+ * synchronises after each step) to fill stats->ms_kernels.                 */
+int scf_clsvof_set_timing(scf_clsvof_ctx *ctx, int32_t on);
 /* stage + run(1) + fetch: one Clsvof_Scheme call with host arrays.         */
 int scf_clsvof_step(scf_clsvof_ctx *ctx, const scf_clsvof_in *in, scf_clsvof_state *state,
                     scf_clsvof_stats *stats);

@@ -217,10 +217,14 @@ class ScfClsvofVcell(C.Structure):
 class ScfClsvofStats(C.Structure):
     _fields_ = [("ms_h2d", C.c_double), ("ms_run", C.c_double), ("ms_d2h", C.c_double), ("ms_total", C.c_double),
                 ("bytes_h2d", C.c_int64), ("bytes_d2h", C.c_int64), ("steps", C.c_int32),
-                ("gpu_launches", C.c_int32)]
+                ("gpu_launches", C.c_int32), ("ms_kernels", C.c_double * 4)]
 
     def as_dict(self):
-        return {name: getattr(self, name) for name, _ in self._fields_}
+        out = {}
+        for name, _ in self._fields_:
+            v = getattr(self, name)
+            out[name] = list(v) if hasattr(v, "__len__") else v
+        return out
 
 
 def dptr(a: Optional[np.ndarray]):

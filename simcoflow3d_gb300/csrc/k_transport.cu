@@ -51,6 +51,9 @@ struct scf_clsvof_ctx {
     double lvs_const[6] = {}, vof_const[6] = {};
     double dt = 0.0;
     bool staged = false;
+    bool timing = false;
+    std::vector<cudaEvent_t> tev;        // 2 per launch of a step when timing
+    std::vector<int> tkind;              // kernel kind of each timed launch
     char err[512] = {0};
 };
 
@@ -217,8 +220,27 @@ int launch_check(scf_clsvof_ctx *ctx, const char *what)
     return SCF_OK;
 }
 
+// With timing on, an event pair around each launch, tagged with its kind
+// (0 reconstruct, 1 sweep, 2 walls, 3 redistancing).
+struct Timer {
+    scf_clsvof_ctx *ctx;
+    int n = 0;
+    void before(int kind)
+    {
+        if (!ctx->timing) return;
+        cudaEventRecord(ctx->tev[2 * n], ctx->st);
+        ctx->tkind[n] = kind;
+    }
+    void after()
+    {
+        if (!ctx->timing) return;
+        cudaEventRecord(ctx->tev[2 * n + 1], ctx->st);
+        ++n;
+    }
+};
+
 // Clsvof_Scheme (Clsvof.f90:355-798) on the staged state; counts launches.
-int scheme_step(scf_clsvof_ctx *ctx, int &launches)
+int scheme_step(scf_clsvof_ctx *ctx, int &launches, Timer &T)
 {
     const Dims D = ctx->D;
     const Geo G = geo_of(ctx);
@@ -232,8 +254,10 @@ int scheme_step(scf_clsvof_ctx *ctx, int &launches)
         int cur = 0;
         for (int s = 0; s < 3; ++s) {
             const int ax = (first + s) % 3, out = s == 0 ? 1 : s == 1 ? 2 : 0;
+            T.before(0);
             k_reconstruct<<<bi, NT, 0, ctx->st>>>(D, G, ctx->vf[cur], ctx->ls[cur], ctx->nx, ctx->ny, ctx->nz,
                                                   ctx->dis, 0, nullptr, nullptr, nullptr);
+            T.after();
             if ((rc = launch_check(ctx, "k_reconstruct")) != SCF_OK) return rc;
             tr::SweepIn S;
             S.vfl = ctx->vf[cur];
@@ -250,7 +274,9 @@ int scheme_step(scf_clsvof_ctx *ctx, int &launches)
             S.dtv = dtv;
             S.axis = ax;
             S.stage = s;
+            T.before(1);
             k_sweep<<<bg, NT, 0, ctx->st>>>(D, G, S, ctx->vf[out], ctx->ls[out]);
+            T.after();
             if ((rc = launch_check(ctx, "k_sweep")) != SCF_OK) return rc;
             launches += 2;
             cur = out;
@@ -270,17 +296,27 @@ int scheme_step(scf_clsvof_ctx *ctx, int &launches)
             W.lvs_const[f] = ctx->lvs_const[f];
             W.vof_const[f] = ctx->vof_const[f];
         }
+        T.before(2);
         k_walls<<<dim3(blocks_for(pmax), 3), NT, 0, ctx->st>>>(D, G, W);
+        T.after();
         if ((rc = launch_check(ctx, "k_walls")) != SCF_OK) return rc;
+        T.before(0);
         k_reconstruct<<<bi, NT, 0, ctx->st>>>(D, G, ctx->vf[0], ctx->ls[0], ctx->nx, ctx->ny, ctx->nz, ctx->dis, 1,
                                               ctx->nxl, ctx->nyl, ctx->nzl);
+        T.after();
         if ((rc = launch_check(ctx, "k_reconstruct")) != SCF_OK) return rc;
+        T.before(3);
         k_band_reset<<<bi, NT, 0, ctx->st>>>(nin, ctx->key, ctx->fix);
+        T.after();
         if ((rc = launch_check(ctx, "k_band_reset")) != SCF_OK) return rc;
+        T.before(3);
         k_band_scatter<<<bi, NT, 0, ctx->st>>>(D, G, ctx->vf[0], ctx->ls[0], ctx->nx, ctx->ny, ctx->nz, ctx->dis,
                                                ctx->key, ctx->fix);
+        T.after();
         if ((rc = launch_check(ctx, "k_band_scatter")) != SCF_OK) return rc;
+        T.before(3);
         k_band_value<<<bi, NT, 0, ctx->st>>>(D, G, ctx->vf[0], ctx->dis, ctx->key, ctx->fix, ctx->ls[0]);
+        T.after();
         if ((rc = launch_check(ctx, "k_band_value")) != SCF_OK) return rc;
         launches += 5;
     }
@@ -345,11 +381,27 @@ extern "C" int scf_clsvof_create(scf_clsvof_ctx **out, int32_t imax, int32_t jma
     return SCF_OK;
 }
 
+extern "C" int scf_clsvof_set_timing(scf_clsvof_ctx *ctx, int32_t on)
+{
+    if (!ctx) return SCF_ERR_BAD_ARG;
+    cudaSetDevice(ctx->device);
+    const size_t need = 2 * (size_t)tr::NSUB * 11;   // two events per launch of a step
+    while (on && ctx->tev.size() < need) {
+        cudaEvent_t e = nullptr;
+        TK(cudaEventCreate(&e));
+        ctx->tev.push_back(e);
+    }
+    ctx->tkind.assign(need / 2, 0);
+    ctx->timing = on != 0;
+    return SCF_OK;
+}
+
 extern "C" int scf_clsvof_destroy(scf_clsvof_ctx *ctx)
 {
     if (!ctx) return SCF_ERR_BAD_ARG;
     cudaSetDevice(ctx->device);
     if (ctx->st) cudaStreamSynchronize(ctx->st);
+    for (cudaEvent_t e : ctx->tev) cudaEventDestroy(e);
     for (void *p : ctx->mem) cudaFree(p);
     for (auto &e : ctx->ev)
         if (e) cudaEventDestroy(e);
@@ -419,15 +471,23 @@ extern "C" int scf_clsvof_run(scf_clsvof_ctx *ctx, int32_t steps, scf_clsvof_sta
     }
     cudaSetDevice(ctx->device);
     int launches = 0, rc;
+    double ms_kind[4] = {0.0, 0.0, 0.0, 0.0};
     TK(cudaEventRecord(ctx->ev[0], ctx->st));
-    for (int n = 0; n < steps; ++n)
-        if ((rc = scheme_step(ctx, launches)) != SCF_OK) return rc;
+    for (int n = 0; n < steps; ++n) {
+        Timer T{ctx};
+        if ((rc = scheme_step(ctx, launches, T)) != SCF_OK) return rc;
+        if (ctx->timing) {
+            TK(cudaStreamSynchronize(ctx->st));
+            for (int q = 0; q < T.n; ++q) ms_kind[ctx->tkind[q]] += elapsed(ctx->tev[2 * q], ctx->tev[2 * q + 1]);
+        }
+    }
     TK(cudaEventRecord(ctx->ev[1], ctx->st));
     TK(cudaStreamSynchronize(ctx->st));
     if (stats) {
         stats->ms_run = elapsed(ctx->ev[0], ctx->ev[1]);
         stats->steps = steps;
         stats->gpu_launches = launches;
+        for (int q = 0; q < 4; ++q) stats->ms_kernels[q] = ms_kind[q];
     }
     return SCF_OK;
 }

@@ -101,6 +101,7 @@ def load_library(path: Optional[str] = None):
     L.scf_clsvof_step.argtypes = [C.c_void_p, P(capi.ScfClsvofIn), P(capi.ScfClsvofState),
                                   P(capi.ScfClsvofStats)]
     L.scf_clsvof_uvw_liquid_field.argtypes = [C.c_void_p, P(capi.ScfClsvofVcell), P(capi.ScfClsvofStats)]
+    L.scf_clsvof_set_timing.argtypes = [C.c_void_p, C.c_int32]
     L.scf_clsvof_device_fields.argtypes = [C.c_void_p, P(C.c_void_p), P(C.c_void_p)]
     L.scf_clsvof_last_error.argtypes = [C.c_void_p, C.c_char_p, C.c_size_t]
     _lib = L

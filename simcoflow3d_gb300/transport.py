@@ -118,6 +118,13 @@ class ClsvofScheme:
         if rc != 0:
             self._err(rc)
 
+    def set_timing(self, on: bool):
+        """Per-kernel CUDA-event timing of run() (stats["ms_kernels"]:
+        reconstruct, sweep, walls, redistancing)."""
+        rc = self.L.scf_clsvof_set_timing(self.ctx, int(bool(on)))
+        if rc != 0:
+            self._err(rc)
+
     def run(self, steps: int = 1) -> dict:
         st = capi.ScfClsvofStats()
         rc = self.L.scf_clsvof_run(self.ctx, int(steps), C.byref(st))

@@ -177,6 +177,7 @@ int main(void) {
   P(scf_clsvof_in, lvs_const) P(scf_clsvof_in, vof_const) P(scf_clsvof_in, dt)
   P(scf_clsvof_state, nzl) P(scf_clsvof_state, lvs_bc) P(scf_clsvof_state, vof_bc)
   P(scf_clsvof_stats, bytes_h2d) P(scf_clsvof_stats, steps) P(scf_clsvof_stats, gpu_launches)
+  P(scf_clsvof_stats, ms_kernels)
   printf("scf_clsvof_vcell size %zu\n", sizeof(scf_clsvof_vcell));
   P(scf_clsvof_vcell, phil) P(scf_clsvof_vcell, vofl)
   return 0;
@@ -191,7 +192,7 @@ int main(void) {
     m = {"scf_clsvof_in": capi.ScfClsvofIn, "scf_clsvof_state": capi.ScfClsvofState,
          "scf_clsvof_stats": capi.ScfClsvofStats, "scf_clsvof_vcell": capi.ScfClsvofVcell}
     lines = out.splitlines()
-    assert len(lines) == 19
+    assert len(lines) == 20
     for line in lines:
         t, f, v = line.split()
         if f == "size":
