@@ -182,3 +182,112 @@ def test_uvw_bodies_match_the_oracle(host_lib, seed):
     for f in range(3):
         for k in ("phil", "nxl", "nyl", "nzl", "vofl"):
             np.testing.assert_array_equal(got[f][k], ref[f][k], err_msg=f"family {f} {k}")
+
+
+class _HostLib:
+    """The scf_clsvof_* entry points the front end calls, served by the host
+    build of the kernel bodies: it unpacks the same ctypes structs the real
+    library reads, so the CPU checks simcoflow3d_gb300/transport.py's
+    marshalling.  (State stays in the caller's arrays: fetch is a no-op.)"""
+
+    def __init__(self, L):
+        self.L = L
+        self.staged = None
+
+    def scf_clsvof_create(self, pctx, I, J, K, device):
+        pctx._obj.value = 1
+        self.shape = (I, J, K)
+        return 0
+
+    def scf_clsvof_destroy(self, ctx):
+        return 0
+
+    def scf_clsvof_last_error(self, ctx, buf, n):
+        return 0
+
+    def _step(self, sin, sst):
+        from simcoflow3d_gb300 import capi
+        I, J, K = self.shape
+        dp = C.POINTER(C.c_double)
+        geo = (dp * 6)(sin.x, sin.y, sin.z, sin.dx, sin.dy, sin.dz)
+        rc = self.L.host_clsvof_step(I, J, K, geo, sst.vofl, sst.phil, sst.nxl, sst.nyl, sst.nzl,
+                                     (dp * 3)(sin.nx, sin.ny, sin.nz), (dp * 3)(sin.u, sin.v, sin.w),
+                                     (dp * 3)(sin.bc_u_w, sin.bc_v_s, sin.bc_w_b), sst.lvs_bc, sst.vof_bc,
+                                     (C.c_int * 6)(*sin.lvs_flag), (C.c_double * 6)(*sin.lvs_const),
+                                     (C.c_int * 6)(*sin.vof_flag), (C.c_double * 6)(*sin.vof_const), sin.dt)
+        assert isinstance(sin, capi.ScfClsvofIn) and rc == 0
+
+    def scf_clsvof_step(self, ctx, pin, pstate, pstats):
+        self._step(pin._obj, pstate._obj)
+        pstats._obj.steps, pstats._obj.gpu_launches = 1, 66
+        return 0
+
+    def scf_clsvof_stage(self, ctx, pin, pstate):
+        from simcoflow3d_gb300 import capi
+        self.staged = (capi.ScfClsvofIn.from_buffer_copy(pin._obj), capi.ScfClsvofState.from_buffer_copy(pstate._obj))
+        return 0
+
+    def scf_clsvof_run(self, ctx, steps, pstats):
+        for _ in range(steps):
+            self._step(*self.staged)
+        pstats._obj.steps, pstats._obj.gpu_launches = steps, 66 * steps
+        return 0
+
+    def scf_clsvof_fetch(self, ctx, pstate, pstats):
+        return 0
+
+    def scf_clsvof_uvw_liquid_field(self, ctx, cells, pstats):
+        I, J, K = self.shape
+        sin, sst = self.staged
+        dp = C.POINTER(C.c_double)
+        vg = [p for f in range(3) for p in (cells[f].dx, cells[f].dy, cells[f].dz)]
+        vf = [p for f in range(3) for p in (cells[f].phil, cells[f].nxl, cells[f].nyl, cells[f].nzl, cells[f].vofl)]
+        assert self.L.host_uvw(I, J, K, (dp * 3)(sin.dx, sin.dy, sin.dz),
+                               (dp * 5)(sst.phil, sst.nxl, sst.nyl, sst.nzl, sst.vofl), (dp * 9)(*vg),
+                               (dp * 15)(*vf)) == 0
+        pstats._obj.gpu_launches = 3
+        return 0
+
+
+def test_front_end_marshals_like_the_oracle(host_lib):
+    """ClsvofScheme (the Python front end of scf_clsvof.h) over the host
+    bodies: one step, then two resident steps, then ComputeUVWLiquidField,
+    each equal to the oracle's."""
+    from simcoflow3d_gb300.transport import ClsvofScheme
+    centres, spacings, state, vel, fn, bc_vel, lvs_bc, dt, flags, vflags = _case("shear")
+    kw = dict(lvs_flag=flags[0], lvs_const=flags[1], vof_flag=vflags[0], vof_const=vflags[1])
+    I, J, K = spacings[0].shape
+    fake = _HostLib(host_lib)
+    sch = ClsvofScheme(I, J, K, lib=fake)
+    s_got, p_got = _copy(state, lvs_bc)
+    v_got, st = sch(centres, spacings, s_got, vel, fn, bc_vel, p_got, dt, **kw)
+    assert st["gpu_launches"] == 66
+    s_ref, p_ref = _copy(state, lvs_bc)
+    v_ref = O.clsvof_scheme(centres, spacings, s_ref, vel, fn, bc_vel, p_ref, dt, **kw)
+    for key in s_ref:
+        np.testing.assert_array_equal(s_got[key], s_ref[key], err_msg=key)
+    for q in range(6):
+        np.testing.assert_array_equal(p_got[q], p_ref[q])
+        np.testing.assert_array_equal(v_got[q], v_ref[q])
+    sch.stage(centres, spacings, s_got, vel, fn, bc_vel, p_got, dt, **kw)
+    assert sch.run(2)["gpu_launches"] == 132
+    sch.fetch(s_got, p_got)
+    for _ in range(2):
+        O.clsvof_scheme(centres, spacings, s_ref, vel, fn, bc_vel, p_ref, dt, **kw)
+    for key in s_ref:
+        np.testing.assert_array_equal(s_got[key], s_ref[key], err_msg=key)
+    # the velocity cells from the staged (advanced) P cells
+    rng = np.random.default_rng(9)
+    g = (I + 2, J + 2, K + 2)
+    vgrids = [tuple(np.asfortranarray(a * rng.uniform(0.9, 1.1, a.shape)) for a in spacings) for _ in range(3)]
+    vcells = [{k: np.asfortranarray(rng.normal(size=g)) for k in ("phil", "nxl", "nyl", "nzl", "vofl")}
+              for _ in range(3)]
+    ref = [{k: v.copy(order="F") for k, v in c.items()} for c in vcells]
+    for c in ref:
+        c["vof"] = np.zeros(g, order="F")
+    O.uvw_liquid_field(spacings, {k: s_ref[k] for k in ("phil", "nxl", "nyl", "nzl", "vofl")}, vgrids, ref)
+    assert sch.uvw_liquid_field(vgrids, vcells)["gpu_launches"] == 3
+    for f in range(3):
+        for k in ("phil", "nxl", "nyl", "nzl", "vofl"):
+            np.testing.assert_array_equal(vcells[f][k], ref[f][k], err_msg=f"family {f} {k}")
+    sch.close()
