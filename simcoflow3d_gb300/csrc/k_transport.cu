@@ -16,6 +16,10 @@
 // The VOF and level set ping-pong through three buffers (the sub-step's
 // input, its first sweep's result, which the later sweeps' divergence terms
 // read, and the second sweep's result); every sub-step ends in buffer 0.
+// The sweeps write interior cells only: k_walls writes the ghost faces into
+// all three buffers, and staging fills all three, so their ghosts agree.
+// Kernels over cells run on 3-D grids (i along x, j and k as blockIdx.y/z),
+// so no thread decodes its cell with integer division.
 // Built with -fmad=false: the bodies round like the reference's Fortran.
 #include <algorithm>
 #include <cstdarg>
@@ -59,7 +63,8 @@ struct scf_clsvof_ctx {
 
 namespace {
 
-constexpr int NT = 256;
+constexpr int NT = 256;   // threads per block of the linear kernels
+constexpr int NX = 128;   // threads along i of the 3-D kernels
 
 void tr_err(scf_clsvof_ctx *c, const char *fmt, ...)
 {
@@ -98,44 +103,33 @@ __global__ void k_reconstruct(Dims D, Geo G, const double *__restrict__ vfl, con
                               double *nx, double *ny, double *nz, double *dis, int tail, double *nxl, double *nyl,
                               double *nzl)
 {
-    const size_t nin = D.interior();
-    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nin; t += (size_t)gridDim.x * blockDim.x) {
-        int i, j, k;
-        D.cell_of(t, i, j, k);
-        double n1, n2, n3, d1;
-        tr::reconstruct(D, G, vfl, phi, i, j, k, n1, n2, n3, d1);
-        const size_t g = D.g(i, j, k);
-        nx[g] = n1;
-        ny[g] = n2;
-        nz[g] = n3;
-        if (tail) {
-            nxl[g] = n1;
-            nyl[g] = n2;
-            nzl[g] = n3;
-            d1 = (0.5 * G.dx[t] * fabs(n1) + 0.5 * G.dy[t] * fabs(n2) + 0.5 * G.dz[t] * fabs(n3)) - d1;
-        }
-        dis[g] = d1;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
+    if (i > D.I) return;
+    double n1, n2, n3, d1;
+    tr::reconstruct(D, G, vfl, phi, i, j, k, n1, n2, n3, d1);
+    const size_t g = D.g(i, j, k), t = D.n(i, j, k);
+    nx[g] = n1;
+    ny[g] = n2;
+    nz[g] = n3;
+    if (tail) {
+        nxl[g] = n1;
+        nyl[g] = n2;
+        nzl[g] = n3;
+        d1 = (0.5 * G.dx[t] * fabs(n1) + 0.5 * G.dy[t] * fabs(n2) + 0.5 * G.dz[t] * fabs(n3)) - d1;
     }
+    dis[g] = d1;
 }
 
-// One directional sweep over the ghosted grid: interior cells take their
-// swept values, ghost cells are carried over.
+// One directional sweep over the interior cells.
 __global__ void k_sweep(Dims D, Geo G, tr::SweepIn S, double *__restrict__ vf_out, double *__restrict__ ls_out)
 {
-    const size_t ng = D.ghosted();
-    const int gi = D.I + 2, gj = D.J + 2;
-    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < ng; t += (size_t)gridDim.x * blockDim.x) {
-        const int i = (int)(t % (size_t)gi), j = (int)((t / (size_t)gi) % (size_t)gj), k = (int)(t / ((size_t)gi * gj));
-        if (i < 1 || i > D.I || j < 1 || j > D.J || k < 1 || k > D.K) {
-            vf_out[t] = S.vfl[t];
-            ls_out[t] = S.phi[t];
-            continue;
-        }
-        double a, b;
-        tr::sweep_cell(D, G, S, i, j, k, a, b);
-        vf_out[t] = a;
-        ls_out[t] = b;
-    }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
+    if (i > D.I) return;
+    double a, b;
+    tr::sweep_cell(D, G, S, i, j, k, a, b);
+    const size_t t = D.g(i, j, k);
+    vf_out[t] = a;
+    ls_out[t] = b;
 }
 
 // BoundaryConditionLvsVof: blockIdx.y is the axis, x strides its planes.
@@ -161,24 +155,18 @@ __global__ void k_band_scatter(Dims D, Geo G, const double *__restrict__ vfl, co
                                const double *__restrict__ nz, const double *__restrict__ dis,
                                unsigned long long *key, uint8_t *fix)
 {
-    const size_t nin = D.interior();
-    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nin; t += (size_t)gridDim.x * blockDim.x) {
-        int i, j, k;
-        D.cell_of(t, i, j, k);
-        tr::band_scatter(D, G, vfl, phi, nx, ny, nz, dis, i, j, k, key, fix);
-    }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
+    if (i > D.I) return;
+    tr::band_scatter(D, G, vfl, phi, nx, ny, nz, dis, i, j, k, key, fix);
 }
 
 __global__ void k_band_value(Dims D, Geo G, const double *__restrict__ vfl, const double *__restrict__ dis,
                              const unsigned long long *__restrict__ key, const uint8_t *__restrict__ fix,
                              double *phi)
 {
-    const size_t nin = D.interior();
-    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nin; t += (size_t)gridDim.x * blockDim.x) {
-        int i, j, k;
-        D.cell_of(t, i, j, k);
-        phi[D.g(i, j, k)] = tr::band_value(D, G, vfl, dis, i, j, k, key, fix);
-    }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
+    if (i > D.I) return;
+    phi[D.g(i, j, k)] = tr::band_value(D, G, vfl, dis, i, j, k, key, fix);
 }
 
 // ComputeUVWLiquidField for one family over its ghosted grid: the cells of
@@ -189,23 +177,21 @@ __global__ void k_uvw(Dims D, int fam, Geo G, const double *__restrict__ phil, c
                       const double *__restrict__ vdx, const double *__restrict__ vdy, const double *__restrict__ vdz,
                       double *o_phil, double *o_nxl, double *o_nyl, double *o_nzl, double *o_vofl)
 {
-    const size_t ng = D.ghosted();
-    const int gi = D.I + 2, gj = D.J + 2;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+    if (i > D.I + 1) return;
     const double *pin[4] = {phil, nxl, nyl, nzl};
     const double *d = fam == 0 ? G.dx : fam == 1 ? G.dy : G.dz;
-    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < ng; t += (size_t)gridDim.x * blockDim.x) {
-        const int i = (int)(t % (size_t)gi), j = (int)((t / (size_t)gi) % (size_t)gj), k = (int)(t / ((size_t)gi * gj));
-        if (i < D.I && j < D.J && k < D.K) {
-            double av[4];
-            tr::family_average(D, fam, d, pin, i, j, k, av);
-            o_phil[t] = av[0];
-            o_nxl[t] = av[1];
-            o_nyl[t] = av[2];
-            o_nzl[t] = av[3];
-        }
-        if (i >= 1 && i <= D.I && j >= 1 && j <= D.J && k >= 1 && k <= D.K)
-            o_vofl[t] = tr::family_vofl(D, fam, G.dx, G.dy, G.dz, phil, nxl, nyl, nzl, vofl, vdx, vdy, vdz, i, j, k);
+    const size_t t = D.g(i, j, k);
+    if (i < D.I && j < D.J && k < D.K) {
+        double av[4];
+        tr::family_average(D, fam, d, pin, i, j, k, av);
+        o_phil[t] = av[0];
+        o_nxl[t] = av[1];
+        o_nyl[t] = av[2];
+        o_nzl[t] = av[3];
     }
+    if (i >= 1 && i <= D.I && j >= 1 && j <= D.J && k >= 1 && k <= D.K)
+        o_vofl[t] = tr::family_vofl(D, fam, G.dx, G.dy, G.dz, phil, nxl, nyl, nzl, vofl, vdx, vdy, vdz, i, j, k);
 }
 
 // ---- one time step ---------------------------------------------------------
@@ -244,9 +230,10 @@ int scheme_step(scf_clsvof_ctx *ctx, int &launches, Timer &T)
 {
     const Dims D = ctx->D;
     const Geo G = geo_of(ctx);
-    const size_t nin = D.interior(), ng = D.ghosted();
+    const size_t nin = D.interior();
     const double dtv = ctx->dt / (double)tr::NSUB;
-    const int bi = blocks_for(nin), bg = blocks_for(ng);
+    const int bi = blocks_for(nin);
+    const dim3 gin((D.I + NX - 1) / NX, D.J, D.K);   // interior cells
     size_t pmax = std::max(D.plane_size(0), std::max(D.plane_size(1), D.plane_size(2)));
     int rc;
     for (int kk = 1; kk <= tr::NSUB; ++kk) {
@@ -255,8 +242,8 @@ int scheme_step(scf_clsvof_ctx *ctx, int &launches, Timer &T)
         for (int s = 0; s < 3; ++s) {
             const int ax = (first + s) % 3, out = s == 0 ? 1 : s == 1 ? 2 : 0;
             T.before(0);
-            k_reconstruct<<<bi, NT, 0, ctx->st>>>(D, G, ctx->vf[cur], ctx->ls[cur], ctx->nx, ctx->ny, ctx->nz,
-                                                  ctx->dis, 0, nullptr, nullptr, nullptr);
+            k_reconstruct<<<gin, NX, 0, ctx->st>>>(D, G, ctx->vf[cur], ctx->ls[cur], ctx->nx, ctx->ny, ctx->nz,
+                                                   ctx->dis, 0, nullptr, nullptr, nullptr);
             T.after();
             if ((rc = launch_check(ctx, "k_reconstruct")) != SCF_OK) return rc;
             tr::SweepIn S;
@@ -275,7 +262,7 @@ int scheme_step(scf_clsvof_ctx *ctx, int &launches, Timer &T)
             S.axis = ax;
             S.stage = s;
             T.before(1);
-            k_sweep<<<bg, NT, 0, ctx->st>>>(D, G, S, ctx->vf[out], ctx->ls[out]);
+            k_sweep<<<gin, NX, 0, ctx->st>>>(D, G, S, ctx->vf[out], ctx->ls[out]);
             T.after();
             if ((rc = launch_check(ctx, "k_sweep")) != SCF_OK) return rc;
             launches += 2;
@@ -284,6 +271,10 @@ int scheme_step(scf_clsvof_ctx *ctx, int &launches, Timer &T)
         tr::WallIn W;
         W.phil = ctx->ls[0];
         W.vofl = ctx->vf[0];
+        for (int q = 0; q < 2; ++q) {
+            W.phil_more[q] = ctx->ls[q + 1];
+            W.vofl_more[q] = ctx->vf[q + 1];
+        }
         W.nxl = ctx->nxl;
         W.nx = ctx->fn[0];
         W.ny = ctx->fn[1];
@@ -301,8 +292,8 @@ int scheme_step(scf_clsvof_ctx *ctx, int &launches, Timer &T)
         T.after();
         if ((rc = launch_check(ctx, "k_walls")) != SCF_OK) return rc;
         T.before(0);
-        k_reconstruct<<<bi, NT, 0, ctx->st>>>(D, G, ctx->vf[0], ctx->ls[0], ctx->nx, ctx->ny, ctx->nz, ctx->dis, 1,
-                                              ctx->nxl, ctx->nyl, ctx->nzl);
+        k_reconstruct<<<gin, NX, 0, ctx->st>>>(D, G, ctx->vf[0], ctx->ls[0], ctx->nx, ctx->ny, ctx->nz, ctx->dis, 1,
+                                               ctx->nxl, ctx->nyl, ctx->nzl);
         T.after();
         if ((rc = launch_check(ctx, "k_reconstruct")) != SCF_OK) return rc;
         T.before(3);
@@ -310,12 +301,12 @@ int scheme_step(scf_clsvof_ctx *ctx, int &launches, Timer &T)
         T.after();
         if ((rc = launch_check(ctx, "k_band_reset")) != SCF_OK) return rc;
         T.before(3);
-        k_band_scatter<<<bi, NT, 0, ctx->st>>>(D, G, ctx->vf[0], ctx->ls[0], ctx->nx, ctx->ny, ctx->nz, ctx->dis,
-                                               ctx->key, ctx->fix);
+        k_band_scatter<<<gin, NX, 0, ctx->st>>>(D, G, ctx->vf[0], ctx->ls[0], ctx->nx, ctx->ny, ctx->nz, ctx->dis,
+                                                ctx->key, ctx->fix);
         T.after();
         if ((rc = launch_check(ctx, "k_band_scatter")) != SCF_OK) return rc;
         T.before(3);
-        k_band_value<<<bi, NT, 0, ctx->st>>>(D, G, ctx->vf[0], ctx->dis, ctx->key, ctx->fix, ctx->ls[0]);
+        k_band_value<<<gin, NX, 0, ctx->st>>>(D, G, ctx->vf[0], ctx->dis, ctx->key, ctx->fix, ctx->ls[0]);
         T.after();
         if ((rc = launch_check(ctx, "k_band_value")) != SCF_OK) return rc;
         launches += 5;
@@ -444,6 +435,10 @@ extern "C" int scf_clsvof_stage(scf_clsvof_ctx *ctx, const scf_clsvof_in *in, co
     }
     TK(cudaMemcpyAsync(ctx->vf[0], s->vofl, bg, cudaMemcpyHostToDevice, ctx->st));
     TK(cudaMemcpyAsync(ctx->ls[0], s->phil, bg, cudaMemcpyHostToDevice, ctx->st));
+    for (int b = 1; b < 3; ++b) {   // the ping-pong buffers' ghosts must match buffer 0's
+        TK(cudaMemcpyAsync(ctx->vf[b], ctx->vf[0], bg, cudaMemcpyDeviceToDevice, ctx->st));
+        TK(cudaMemcpyAsync(ctx->ls[b], ctx->ls[0], bg, cudaMemcpyDeviceToDevice, ctx->st));
+    }
     TK(cudaMemcpyAsync(ctx->nxl, s->nxl, bg, cudaMemcpyHostToDevice, ctx->st));
     TK(cudaMemcpyAsync(ctx->nyl, s->nyl, bg, cudaMemcpyHostToDevice, ctx->st));
     TK(cudaMemcpyAsync(ctx->nzl, s->nzl, bg, cudaMemcpyHostToDevice, ctx->st));
@@ -596,7 +591,8 @@ extern "C" int scf_clsvof_uvw_liquid_field(scf_clsvof_ctx *ctx, const scf_clsvof
     TK(cudaEventRecord(ctx->ev[1], ctx->st));
     const Geo G = geo_of(ctx);
     for (int f = 0; f < 3; ++f) {
-        k_uvw<<<blocks_for(ng), NT, 0, ctx->st>>>(ctx->D, f, G, ctx->ls[0], ctx->nxl, ctx->nyl, ctx->nzl, ctx->vf[0],
+        const dim3 gg((ctx->D.I + 2 + NX - 1) / NX, ctx->D.J + 2, ctx->D.K + 2);   // ghosted cells
+        k_uvw<<<gg, NX, 0, ctx->st>>>(ctx->D, f, G, ctx->ls[0], ctx->nxl, ctx->nyl, ctx->nzl, ctx->vf[0],
                                                  ctx->vgeo[f][0], ctx->vgeo[f][1], ctx->vgeo[f][2], ctx->vfld[f][0],
                                                  ctx->vfld[f][1], ctx->vfld[f][2], ctx->vfld[f][3], ctx->vfld[f][4]);
         if ((rc = launch_check(ctx, "k_uvw")) != SCF_OK) return rc;

@@ -5,8 +5,8 @@
 //
 // Layout (column-major, i fastest): "ghosted" (0:I+1,0:J+1,0:K+1), "interior"
 // (1:I,1:J,1:K), wall planes (J,K) for x, (I,K) for y, (I,J) for z.  Every
-// body is a function of one thread index over the interior cells (or over a
-// wall plane), so a kernel is a bounds test and one call.
+// body is a function of one cell (or one wall-plane point), so a kernel is a
+// bounds test and one call.
 //
 // Expressions keep the reference's operation order; the kernels are built
 // with -fmad=false and the host build with -ffp-contract=off, so sqrt,
@@ -69,12 +69,6 @@ struct Dims {
     {
         return axis == 0 ? (size_t)J * K : axis == 1 ? (size_t)I * K : (size_t)I * J;
     }
-    TR_HD void cell_of(size_t t, int &i, int &j, int &k) const
-    {
-        i = (int)(t % (size_t)I) + 1;
-        j = (int)((t / (size_t)I) % (size_t)J) + 1;
-        k = (int)(t / ((size_t)I * J)) + 1;
-    }
 };
 
 struct Geo {   // cell centres and spacings, interior
@@ -82,6 +76,32 @@ struct Geo {   // cell centres and spacings, interior
 };
 
 TR_HD double sgn(double a) { return copysign(1.0, a); }
+
+TR_HD uint64_t bits_of(double v)
+{
+    union { double d; uint64_t u; } c;
+    c.d = v;
+    return c.u;
+}
+TR_HD double from_bits(uint64_t u)
+{
+    union { double d; uint64_t u; } c;
+    c.u = u;
+    return c.d;
+}
+
+// x / d.  When d is a normal power of two its reciprocal is exact and
+// x * (1/d) is the same correctly rounded quotient, without an FP64
+// division (about ten instructions on GB300's narrow FP64 pipes).  Uniform
+// grids with power-of-two spacings, and divisions by 2 or by 1, take it.
+TR_HD double divd(double x, double d)
+{
+    const uint64_t b = bits_of(d);
+    const uint64_t e = (b >> 52) & 0x7FFull;
+    if ((b & 0xFFFFFFFFFFFFFull) == 0 && e >= 1 && e <= 2045)
+        return x * from_bits((b & 0x8000000000000000ull) | ((2046ull - e) << 52));
+    return x / d;
+}
 
 // x**3.d0
 TR_HD double cube(double x)
@@ -229,49 +249,50 @@ TR_HD void normal_irre(const Dims &D, const Geo &G, const double *phi, int i, in
     auto X = [&](int a, int b, int c) { return G.x[D.n(a, b, c)]; };
     auto Y = [&](int a, int b, int c) { return G.y[D.n(a, b, c)]; };
     auto Z = [&](int a, int b, int c) { return G.z[D.n(a, b, c)]; };
+    auto Q = [](double num, double den) { return divd(num, den); };
     double vx, vy, vz, qm, qp;
-    vx = i >= 3 ? (P(i, j, k) - P(i - 2, j, k)) / (X(i, j, k) - X(i - 2, j, k))
-                : (P(i, j, k) - P(i - 1, j, k)) / (X(i, j, k) - X(i - 1, j, k));
-    vy = (P(i - 1, j + 1, k) - P(i - 1, j - 1, k)) / (Y(i - 1, j + 1, k) - Y(i - 1, j - 1, k));
-    vz = (P(i - 1, j, k + 1) - P(i - 1, j, k - 1)) / (Z(i - 1, j, k + 1) - Z(i - 1, j, k - 1));
+    vx = i >= 3 ? Q(P(i, j, k) - P(i - 2, j, k), X(i, j, k) - X(i - 2, j, k))
+                : Q(P(i, j, k) - P(i - 1, j, k), X(i, j, k) - X(i - 1, j, k));
+    vy = Q(P(i - 1, j + 1, k) - P(i - 1, j - 1, k), Y(i - 1, j + 1, k) - Y(i - 1, j - 1, k));
+    vz = Q(P(i - 1, j, k + 1) - P(i - 1, j, k - 1), Z(i - 1, j, k + 1) - Z(i - 1, j, k - 1));
     qm = off_unit(vx, vy, vz);
-    vx = i <= D.I - 2 ? (P(i + 2, j, k) - P(i, j, k)) / (X(i + 2, j, k) - X(i, j, k))
-                      : (P(i + 1, j, k) - P(i, j, k)) / (X(i + 1, j, k) - X(i, j, k));
-    vy = (P(i + 1, j + 1, k) - P(i + 1, j - 1, k)) / (Y(i + 1, j + 1, k) - Y(i + 1, j - 1, k));
-    vz = (P(i + 1, j, k + 1) - P(i + 1, j, k - 1)) / (Z(i + 1, j, k + 1) - Z(i + 1, j, k - 1));
+    vx = i <= D.I - 2 ? Q(P(i + 2, j, k) - P(i, j, k), X(i + 2, j, k) - X(i, j, k))
+                      : Q(P(i + 1, j, k) - P(i, j, k), X(i + 1, j, k) - X(i, j, k));
+    vy = Q(P(i + 1, j + 1, k) - P(i + 1, j - 1, k), Y(i + 1, j + 1, k) - Y(i + 1, j - 1, k));
+    vz = Q(P(i + 1, j, k + 1) - P(i + 1, j, k - 1), Z(i + 1, j, k + 1) - Z(i + 1, j, k - 1));
     qp = off_unit(vx, vy, vz);
     const int sx = side_of(qm, qp);
-    vy = j >= 3 ? (P(i, j, k) - P(i, j - 2, k)) / (Y(i, j, k) - Y(i, j - 2, k))
-                : (P(i, j, k) - P(i, j - 1, k)) / (Y(i, j, k) - Y(i, j - 1, k));
-    vx = (P(i + 1, j - 1, k) - P(i - 1, j - 1, k)) / (X(i + 1, j - 1, k) - X(i - 1, j - 1, k));
-    vz = (P(i, j - 1, k + 1) - P(i, j - 1, k - 1)) / (Z(i, j - 1, k + 1) - Z(i, j - 1, k - 1));
+    vy = j >= 3 ? Q(P(i, j, k) - P(i, j - 2, k), Y(i, j, k) - Y(i, j - 2, k))
+                : Q(P(i, j, k) - P(i, j - 1, k), Y(i, j, k) - Y(i, j - 1, k));
+    vx = Q(P(i + 1, j - 1, k) - P(i - 1, j - 1, k), X(i + 1, j - 1, k) - X(i - 1, j - 1, k));
+    vz = Q(P(i, j - 1, k + 1) - P(i, j - 1, k - 1), Z(i, j - 1, k + 1) - Z(i, j - 1, k - 1));
     qm = off_unit(vx, vy, vz);
-    vx = (P(i + 1, j + 1, k) - P(i - 1, j + 1, k)) / (X(i + 1, j + 1, k) - X(i - 1, j + 1, k));
-    vy = j <= D.J - 2 ? (P(i, j + 2, k) - P(i, j, k)) / (Y(i, j + 2, k) - Y(i, j, k))
-                      : (P(i, j + 1, k) - P(i, j, k)) / (Y(i, j + 1, k) - Y(i, j, k));
-    vz = (P(i, j + 1, k + 1) - P(i, j + 1, k - 1)) / (Z(i, j + 1, k + 1) - Z(i, j + 1, k - 1));
+    vx = Q(P(i + 1, j + 1, k) - P(i - 1, j + 1, k), X(i + 1, j + 1, k) - X(i - 1, j + 1, k));
+    vy = j <= D.J - 2 ? Q(P(i, j + 2, k) - P(i, j, k), Y(i, j + 2, k) - Y(i, j, k))
+                      : Q(P(i, j + 1, k) - P(i, j, k), Y(i, j + 1, k) - Y(i, j, k));
+    vz = Q(P(i, j + 1, k + 1) - P(i, j + 1, k - 1), Z(i, j + 1, k + 1) - Z(i, j + 1, k - 1));
     qp = off_unit(vx, vy, vz);
     const int sy = side_of(qm, qp);
-    vx = (P(i + 1, j, k - 1) - P(i - 1, j, k - 1)) / (X(i + 1, j, k - 1) - X(i - 1, j, k - 1));
-    vy = (P(i, j + 1, k - 1) - P(i, j - 1, k - 1)) / (Y(i, j + 1, k - 1) - Y(i, j - 1, k - 1));
-    vz = k >= 3 ? (P(i, j, k) - P(i, j, k - 2)) / (Z(i, j, k) - Z(i, j, k - 2))
-                : (P(i, j, k) - P(i, j, k - 1)) / (Z(i, j, k) - Z(i, j, k - 1));
+    vx = Q(P(i + 1, j, k - 1) - P(i - 1, j, k - 1), X(i + 1, j, k - 1) - X(i - 1, j, k - 1));
+    vy = Q(P(i, j + 1, k - 1) - P(i, j - 1, k - 1), Y(i, j + 1, k - 1) - Y(i, j - 1, k - 1));
+    vz = k >= 3 ? Q(P(i, j, k) - P(i, j, k - 2), Z(i, j, k) - Z(i, j, k - 2))
+                : Q(P(i, j, k) - P(i, j, k - 1), Z(i, j, k) - Z(i, j, k - 1));
     qm = off_unit(vx, vy, vz);
-    vx = (P(i + 1, j, k + 1) - P(i - 1, j, k + 1)) / (X(i + 1, j, k + 1) - X(i - 1, j, k + 1));
-    vy = (P(i, j + 1, k + 1) - P(i, j - 1, k + 1)) / (Y(i, j + 1, k + 1) - Y(i, j - 1, k + 1));
-    vz = k <= D.K - 2 ? (P(i, j, k + 2) - P(i, j, k)) / (Z(i, j, k + 2) - Z(i, j, k))
-                      : (P(i, j, k + 1) - P(i, j, k)) / (Z(i, j, k + 1) - Z(i, j, k));
+    vx = Q(P(i + 1, j, k + 1) - P(i - 1, j, k + 1), X(i + 1, j, k + 1) - X(i - 1, j, k + 1));
+    vy = Q(P(i, j + 1, k + 1) - P(i, j - 1, k + 1), Y(i, j + 1, k + 1) - Y(i, j - 1, k + 1));
+    vz = k <= D.K - 2 ? Q(P(i, j, k + 2) - P(i, j, k), Z(i, j, k + 2) - Z(i, j, k))
+                      : Q(P(i, j, k + 1) - P(i, j, k), Z(i, j, k + 1) - Z(i, j, k));
     qp = off_unit(vx, vy, vz);
     const int sz = side_of(qm, qp);
-    nxx = sx == -1 ? (P(i, j, k) - P(i - 1, j, k)) / (X(i, j, k) - X(i - 1, j, k))
-        : sx == 1  ? (P(i + 1, j, k) - P(i, j, k)) / (X(i + 1, j, k) - X(i, j, k))
-                   : (P(i + 1, j, k) - P(i - 1, j, k)) / (X(i + 1, j, k) - X(i - 1, j, k));
-    nyy = sy == -1 ? (P(i, j, k) - P(i, j - 1, k)) / (Y(i, j, k) - Y(i, j - 1, k))
-        : sy == 1  ? (P(i, j + 1, k) - P(i, j, k)) / (Y(i, j + 1, k) - Y(i, j, k))
-                   : (P(i, j + 1, k) - P(i, j - 1, k)) / (Y(i, j + 1, k) - Y(i, j - 1, k));
-    nzz = sz == -1 ? (P(i, j, k) - P(i, j, k - 1)) / (Z(i, j, k) - Z(i, j, k - 1))
-        : sz == 1  ? (P(i, j, k + 1) - P(i, j, k)) / (Z(i, j, k + 1) - Z(i, j, k))
-                   : (P(i, j, k + 1) - P(i, j, k - 1)) / (Z(i, j, k + 1) - Z(i, j, k - 1));
+    nxx = sx == -1 ? Q(P(i, j, k) - P(i - 1, j, k), X(i, j, k) - X(i - 1, j, k))
+        : sx == 1  ? Q(P(i + 1, j, k) - P(i, j, k), X(i + 1, j, k) - X(i, j, k))
+                   : Q(P(i + 1, j, k) - P(i - 1, j, k), X(i + 1, j, k) - X(i - 1, j, k));
+    nyy = sy == -1 ? Q(P(i, j, k) - P(i, j - 1, k), Y(i, j, k) - Y(i, j - 1, k))
+        : sy == 1  ? Q(P(i, j + 1, k) - P(i, j, k), Y(i, j + 1, k) - Y(i, j, k))
+                   : Q(P(i, j + 1, k) - P(i, j - 1, k), Y(i, j + 1, k) - Y(i, j - 1, k));
+    nzz = sz == -1 ? Q(P(i, j, k) - P(i, j, k - 1), Z(i, j, k) - Z(i, j, k - 1))
+        : sz == 1  ? Q(P(i, j, k + 1) - P(i, j, k), Z(i, j, k + 1) - Z(i, j, k))
+                   : Q(P(i, j, k + 1) - P(i, j, k - 1), Z(i, j, k + 1) - Z(i, j, k - 1));
 }
 
 // Interface_Reconstruct (1216-1309) of one cell: the unit normal and the
@@ -288,9 +309,9 @@ TR_HD void reconstruct(const Dims &D, const Geo &G, const double *vfl, const dou
         const int ip = i + 1 < D.I ? i + 1 : D.I, im = i - 1 > 1 ? i - 1 : 1;
         const int jp = j + 1 < D.J ? j + 1 : D.J, jm = j - 1 > 1 ? j - 1 : 1;
         const int kp = k + 1 < D.K ? k + 1 : D.K, km = k - 1 > 1 ? k - 1 : 1;
-        n1 = (phi[D.g(ip, j, k)] - phi[D.g(im, j, k)]) / (G.x[D.n(ip, j, k)] - G.x[D.n(im, j, k)]);
-        n2 = (phi[D.g(i, jp, k)] - phi[D.g(i, jm, k)]) / (G.y[D.n(i, jp, k)] - G.y[D.n(i, jm, k)]);
-        n3 = (phi[D.g(i, j, kp)] - phi[D.g(i, j, km)]) / (G.z[D.n(i, j, kp)] - G.z[D.n(i, j, km)]);
+        n1 = divd(phi[D.g(ip, j, k)] - phi[D.g(im, j, k)], G.x[D.n(ip, j, k)] - G.x[D.n(im, j, k)]);
+        n2 = divd(phi[D.g(i, jp, k)] - phi[D.g(i, jm, k)], G.y[D.n(i, jp, k)] - G.y[D.n(i, jm, k)]);
+        n3 = divd(phi[D.g(i, j, kp)] - phi[D.g(i, j, km)], G.z[D.n(i, j, kp)] - G.z[D.n(i, j, km)]);
     }
     const double temp = sqrt(n1 * n1 + n2 * n2 + n3 * n3);
     if (temp < 1.0e-14) {
@@ -379,29 +400,30 @@ TR_HD double ls_face(const Dims &D, const Geo &G, const SweepIn &S, const double
     if (q == 1) {
         if (w >= 0.0) {
             const double den = ax == 0 ? DD(1) : CC(2) - CC(1);
-            ls = PH(1) + DD(1) / 2.0 * (1.0 - w * dtv / DD(1)) * (PH(2) - PH(1)) / den;
+            ls = PH(1) + divd(divd(DD(1), 2.0) * (1.0 - divd(w * dtv, DD(1))) * (PH(2) - PH(1)), den);
         } else if (ax == 0) {
-            ls = PH(2) - DD(2) / 2.0 * (1.0 + w * dtv / DD(2)) * (PH(3) - PH(1)) / 2.0 * DD(2);
+            ls = PH(2) - divd(divd(DD(2), 2.0) * (1.0 + divd(w * dtv, DD(2))) * (PH(3) - PH(1)), 2.0) * DD(2);
         } else if (ax == 1) {
-            ls = PH(2) - DD(2) / 2.0 * (1.0 + w * dtv / DD(2)) * (PH(3) - PH(1)) / (CC(3) - CC(1));
+            ls = PH(2) - divd(divd(DD(2), 2.0) * (1.0 + divd(w * dtv, DD(2))) * (PH(3) - PH(1)), CC(3) - CC(1));
         } else {
-            ls = PH(2) + DD(2) / 2.0 * (1.0 + w * dtv / DD(2)) * (PH(3) - PH(1)) / (CC(3) - CC(1));
+            ls = PH(2) + divd(divd(DD(2), 2.0) * (1.0 + divd(w * dtv, DD(2))) * (PH(3) - PH(1)), CC(3) - CC(1));
         }
         return ls * w * dtv;
     }
     if (q == n) {
         if (w > 0.0) {
-            ls = PH(n) + DD(n) / 2.0 * (1.0 - w * dtv / DD(n)) * (PH(n) - PH(n - 1)) / (CC(n) - CC(n - 1));
+            ls = PH(n) + divd(divd(DD(n), 2.0) * (1.0 - divd(w * dtv, DD(n))) * (PH(n) - PH(n - 1)), CC(n) - CC(n - 1));
         } else {
             const double scale = ax == 2 ? G.dy[line_n(D, ax, n - 1, a, b)] : DD(n - 1);
-            ls = PH(n) - DD(n - 1) / 2.0 * (1.0 + w * dtv / scale) * (PH(n) - PH(n - 1)) / (CC(n) - CC(n - 1));
+            ls = PH(n) - divd(divd(DD(n - 1), 2.0) * (1.0 + divd(w * dtv, scale)) * (PH(n) - PH(n - 1)),
+                              CC(n) - CC(n - 1));
         }
         return ls * w * dtv;
     }
-    const double dm = DD(q);
-    if (w >= 0.0) ls = PH(q) + dm / 2.0 * (1.0 - w * dtv / dm) * (PH(q + 1) - PH(q - 1)) / (2.0 * dm);
-    else if (q <= n - 2) ls = PH(q + 1) - dm / 2.0 * (1.0 + w * dtv / dm) * (PH(q + 2) - PH(q)) / (2.0 * dm);
-    else ls = PH(q + 1) - dm / 2.0 * (1.0 + w * dtv / dm) * (PH(q + 1) - PH(q)) / dm;
+    const double dm = DD(q), half = divd(dm, 2.0), step = divd(w * dtv, dm);
+    if (w >= 0.0) ls = PH(q) + divd(half * (1.0 - step) * (PH(q + 1) - PH(q - 1)), 2.0 * dm);
+    else if (q <= n - 2) ls = PH(q + 1) - divd(half * (1.0 + step) * (PH(q + 2) - PH(q)), 2.0 * dm);
+    else ls = PH(q + 1) - divd(half * (1.0 + step) * (PH(q + 1) - PH(q)), dm);
     return w * ls * dtv;
 }
 
@@ -423,39 +445,41 @@ TR_HD void sweep_cell(const Dims &D, const Geo &G, const SweepIn &S, int i, int 
     const double dm = d[nc];
     // VOF (X_Sweep 835-875)
     double tv = S.vfl[g];
-    if (m >= 2) tv = tv + vof_face(D, G, S, m - 1, a, b) / dm;
-    if (m <= n - 1) tv = tv - vof_face(D, G, S, m, a, b) / dm;
+    if (m >= 2) tv = tv + divd(vof_face(D, G, S, m - 1, a, b), dm);
+    if (m <= n - 1) tv = tv - divd(vof_face(D, G, S, m, a, b), dm);
     if (m == 1) {
         const size_t gw = ax == 0 ? D.g(0, j, k) : ax == 1 ? D.g(i, 0, k) : D.g(i, j, 0);
         const double flux = S.vfl[g] * S.vel[gw] * S.dtv;
-        tv = tv + flux / dm;
+        tv = tv + divd(flux, dm);
     }
     if (m == n) {
         const double flux = S.vfl[g] * S.vel[g] * S.dtv;
-        tv = tv - flux / dm;
+        tv = tv - divd(flux, dm);
     }
     // level set (X_Sweep 877-947)
     double tl = S.phi[g];
-    if (m >= 3) tl = tl + ls_face(D, G, S, d, c, m - 1, a, b) / dm;
-    if (m >= 2 && m <= n - 1) tl = tl - ls_face(D, G, S, d, c, m, a, b) / dm;
+    if (m >= 3) tl = tl + divd(ls_face(D, G, S, d, c, m - 1, a, b), dm);
+    if (m >= 2 && m <= n - 1) tl = tl - divd(ls_face(D, G, S, d, c, m, a, b), dm);
     if (m == 1) {
-        tl = tl - ls_face(D, G, S, d, c, 1, a, b) / dm;
+        tl = tl - divd(ls_face(D, G, S, d, c, 1, a, b), dm);
         const size_t bw = (size_t)(a - 1) + (size_t)D.plane_lead(ax) * (size_t)(b - 1);
         TR_CHECK(bw < D.plane_size(ax), "wall plane");
         const double flux = S.bc_vel[bw] * S.bc_lvs[bw] * S.dtv;
-        tl = tl + flux / dm;
+        tl = tl + divd(flux, dm);
     }
-    if (m == 2) tl = tl + ls_face(D, G, S, d, c, 1, a, b) / dm;
-    if (m == n) tl = tl - ls_face(D, G, S, d, c, n, a, b) / dm;
+    if (m == 2) tl = tl + divd(ls_face(D, G, S, d, c, 1, a, b), dm);
+    if (m == n) tl = tl - divd(ls_face(D, G, S, d, c, n, a, b), dm);
     // the divergence term and the clip
     const size_t gm = ax == 0 ? D.g(i - 1, j, k) : ax == 1 ? D.g(i, j - 1, k) : D.g(i, j, k - 1);
     const double du = S.vel[g] - S.vel[gm];
+    const double rate = divd(S.dtv, dm);
     if (S.stage == 0) {
-        tv = tv / (1.0 - S.dtv / dm * du);
-        tl = tl / (1.0 - S.dtv / dm * du);
+        const double den = 1.0 - rate * du;
+        tv = divd(tv, den);
+        tl = divd(tl, den);
     } else {
-        tv = tv + S.dtv / dm * S.vf_first[g] * du;
-        tl = tl + S.dtv / dm * S.ls_first[g] * du;
+        tv = tv + rate * S.vf_first[g] * du;
+        tl = tl + rate * S.ls_first[g] * du;
     }
     if (tv <= VOFEPS) tv = 0.0;
     if (tv >= 1.0 - VOFEPS) tv = 1.0;
@@ -573,18 +597,8 @@ TR_HD bool band_interface(double v) { return 0.0 + 1.0e-15 < v && v < 1.0 - 1.0e
 TR_HD bool band_target(double v) { return v < 0.0 + 1.0e-15 || v > 1.0 - 1.0e-15; }
 
 // The bits of a non-negative double order like the double.
-TR_HD uint64_t key_of(double v)
-{
-    union { double d; uint64_t u; } c;
-    c.d = v;
-    return c.u;
-}
-TR_HD double value_of(uint64_t u)
-{
-    union { double d; uint64_t u; } c;
-    c.u = u;
-    return c.d;
-}
+TR_HD uint64_t key_of(double v) { return bits_of(v); }
+TR_HD double value_of(uint64_t u) { return from_bits(u); }
 
 TR_HD void atomic_min_key(unsigned long long *slot, unsigned long long key)
 {
@@ -632,7 +646,9 @@ TR_HD double band_value(const Dims &D, const Geo &G, const double *vfl, const do
 // ---- boundary planes (BoundaryConditionLvsVof 2087-2221) -----------------
 
 struct WallIn {
-    double *phil, *vofl;                     // ghosted
+    double *phil, *vofl;                     // ghosted: the sub-step's result
+    double *phil_more[2], *vofl_more[2];     // the other ping-pong buffers, whose
+                                             // ghost faces must match (or null)
     const double *nxl;                       // liquid normal, ghosted
     const double *nx, *ny, *nz;              // fluid normals, ghosted
     double *lvs_bc[6], *vof_bc[6];           // planes W, E, S, N, B, T
@@ -669,14 +685,26 @@ TR_HD void wall_point(const Dims &D, const Geo &G, const WallIn &W, int axis, si
     }
     W.lvs_bc[lo][t] = wlo;
     W.lvs_bc[hi][t] = whi;
-    W.phil[g0] = p1 - fn[g1] * d1;
-    W.phil[gx] = axis == 1 ? pn - fn[gn] * dn : pn + fn[gn] * dn;
+    const double lo_ghost = p1 - fn[g1] * d1;
+    const double hi_ghost = axis == 1 ? pn - fn[gn] * dn : pn + fn[gn] * dn;
+    W.phil[g0] = lo_ghost;
+    W.phil[gx] = hi_ghost;
     // VOF
     const double v1 = W.vofl[g1], vn = W.vofl[gn];
     W.vof_bc[lo][t] = typical_bc(W.vof_flag[lo], W.vof_const[lo], v1, d1);
     W.vof_bc[hi][t] = typical_bc(W.vof_flag[hi], W.vof_const[hi], vn, -dn);
     W.vofl[g0] = v1;
     W.vofl[gx] = vn;
+    for (int q = 0; q < 2; ++q) {
+        if (W.phil_more[q]) {
+            W.phil_more[q][g0] = lo_ghost;
+            W.phil_more[q][gx] = hi_ghost;
+        }
+        if (W.vofl_more[q]) {
+            W.vofl_more[q][g0] = v1;
+            W.vofl_more[q][gx] = vn;
+        }
+    }
 }
 
 // ---- the velocity cells' liquid fields (ComputeUVWLiquidField 174-353) ----
@@ -703,7 +731,7 @@ TR_HD void family_average(const Dims &D, int fam, const double *d, const double 
     if (fam == 1 && j == D.J) j = D.J - 1;
     if (fam == 2 && k == D.K) k = D.K - 1;
     const int i2 = i + (fam == 0), j2 = j + (fam == 1), k2 = k + (fam == 2);
-    const double lamda = d[D.n(i2, j2, k2)] / (d[D.n(i, j, k)] + d[D.n(i2, j2, k2)]);
+    const double lamda = divd(d[D.n(i2, j2, k2)], d[D.n(i, j, k)] + d[D.n(i2, j2, k2)]);
     const size_t a = D.g(i, j, k), b = D.g(i2, j2, k2);
     for (int f = 0; f < 4; ++f) out[f] = lamda * pin[f][a] + (1.0 - lamda) * pin[f][b];
 }
@@ -760,7 +788,7 @@ TR_HD double family_vofl(const Dims &D, int fam, const double *pdx, const double
         right = volume_fraction(pdx[nb], pdy[nb], dcell, nxl[b], nyl[b], nzl[b], dist);
         right = pdx[nb] * pdy[nb] * dcell - right;
     }
-    return (left + right) / vdx[na] / vdy[na] / vdz[na];
+    return divd(divd(divd(left + right, vdx[na]), vdy[na]), vdz[na]);
 }
 
 }  // namespace tr

@@ -40,7 +40,7 @@ def _run_gpu(lib, case, steps=1):
         sch.close()
 
 
-@pytest.mark.parametrize("kind", ["plane", "rest", "shear", "random"])
+@pytest.mark.parametrize("kind", ["plane", "rest", "shear", "random", "pow2"])
 def test_gpu_step_matches_the_oracle(lib, kind):
     case = _case(kind)
     centres, spacings, state, vel, fn, bc_vel, lvs_bc, dt, flags, vflags = case

@@ -62,8 +62,11 @@ def host_step(L, centres, spacings, state, vel, fn, bc_vel, lvs_bc, dt, lvs=((1,
 def _case(kind):
     """Inputs of one Clsvof_Scheme call: a tilted plane in a uniform
     stream, a drop in a shear, a plane at rest with Dirichlet planes, or a
-    drop in a random (divergent) velocity field."""
-    I, J, K = (12, 9, 10) if kind in ("plane", "rest") else (13, 12, 11)
+    drop in a random (divergent) velocity field, on grids whose spacings are
+    not powers of two -- or ("pow2") the random case on a 16x8x16 grid whose
+    spacings are, so that every division by a spacing takes the exact
+    reciprocal product."""
+    I, J, K = {"plane": (12, 9, 10), "rest": (12, 9, 10), "pow2": (16, 8, 16)}.get(kind, (13, 12, 11))
     h = np.array([1.0 / I, 1.0 / J, 1.0 / K])
     cs = [(np.arange(m) + 0.5) * hq for m, hq in zip((I, J, K), h)]
     cg = [(np.arange(m + 2) - 0.5) * hq for m, hq in zip((I, J, K), h)]
@@ -71,7 +74,7 @@ def _case(kind):
     spacings = tuple(np.full((I, J, K), hq, order="F") for hq in h)
     Xg, Yg, Zg = np.meshgrid(*cg, indexing="ij")
     g = Xg.shape
-    rng = np.random.default_rng({"plane": 1, "rest": 2, "shear": 3, "random": 4}[kind])
+    rng = np.random.default_rng({"plane": 1, "rest": 2, "shear": 3, "random": 4, "pow2": 7}[kind])
     if kind in ("plane", "rest"):
         n = np.array([1.0, 0.15, -0.1]) if kind == "rest" else np.array([1.0, 0.0, 0.15])
         n /= np.linalg.norm(n)
@@ -120,7 +123,7 @@ def _copy(state, planes):
     return {k: v.copy(order="F") for k, v in state.items()}, [p.copy(order="F") for p in planes]
 
 
-@pytest.mark.parametrize("kind", ["plane", "rest", "shear", "random"])
+@pytest.mark.parametrize("kind", ["plane", "rest", "shear", "random", "pow2"])
 def test_kernel_bodies_match_the_oracle(host_lib, kind):
     centres, spacings, state, vel, fn, bc_vel, lvs_bc, dt, flags, vflags = _case(kind)
     s_ref, p_ref = _copy(state, lvs_bc)

@@ -30,16 +30,21 @@ extern "C" int host_clsvof_step(int I, int J, int K, const double *const geo[6],
     }
     std::vector<unsigned long long> key(nin);
     std::vector<uint8_t> fix(nin);
-    memcpy(vf[0].data(), vofl, ng * sizeof(double));
-    memcpy(ls[0].data(), phil, ng * sizeof(double));
+    for (int b = 0; b < 3; ++b) {   // staging fills all three buffers
+        memcpy(vf[b].data(), vofl, ng * sizeof(double));
+        memcpy(ls[b].data(), phil, ng * sizeof(double));
+    }
     const double dtv = dt / (double)tr::NSUB;
+    auto cells = [&](auto &&body) {   // the 3-D grid of the interior kernels
+        for (int k = 1; k <= K; ++k)
+            for (int j = 1; j <= J; ++j)
+                for (int i = 1; i <= I; ++i) body(i, j, k);
+    };
     auto reconstruct = [&](int cur, bool tail) {
-        for (size_t t = 0; t < nin; ++t) {   // k_reconstruct
-            int i, j, k;
-            D.cell_of(t, i, j, k);
+        cells([&](int i, int j, int k) {   // k_reconstruct
             double n1, n2, n3, d1;
             tr::reconstruct(D, G, vf[cur].data(), ls[cur].data(), i, j, k, n1, n2, n3, d1);
-            const size_t g = D.g(i, j, k);
+            const size_t g = D.g(i, j, k), t = D.n(i, j, k);
             nx[g] = n1;
             ny[g] = n2;
             nz[g] = n3;
@@ -50,7 +55,7 @@ extern "C" int host_clsvof_step(int I, int J, int K, const double *const geo[6],
                 d1 = (0.5 * G.dx[t] * fabs(n1) + 0.5 * G.dy[t] * fabs(n2) + 0.5 * G.dz[t] * fabs(n3)) - d1;
             }
             dis[g] = d1;
-        }
+        });
     };
     for (int kk = 1; kk <= tr::NSUB; ++kk) {
         const int first = kk % 3 == 0 ? 0 : kk % 3 == 1 ? 1 : 2;
@@ -73,25 +78,22 @@ extern "C" int host_clsvof_step(int I, int J, int K, const double *const geo[6],
             S.dtv = dtv;
             S.axis = ax;
             S.stage = s;
-            const int gi = I + 2, gj = J + 2;
-            for (size_t t = 0; t < ng; ++t) {   // k_sweep
-                const int i = (int)(t % (size_t)gi), j = (int)((t / (size_t)gi) % (size_t)gj),
-                          k = (int)(t / ((size_t)gi * gj));
-                if (i < 1 || i > I || j < 1 || j > J || k < 1 || k > K) {
-                    vf[out][t] = S.vfl[t];
-                    ls[out][t] = S.phi[t];
-                    continue;
-                }
+            cells([&](int i, int j, int k) {   // k_sweep: interior only
                 double a, b;
                 tr::sweep_cell(D, G, S, i, j, k, a, b);
+                const size_t t = D.g(i, j, k);
                 vf[out][t] = a;
                 ls[out][t] = b;
-            }
+            });
             cur = out;
         }
         tr::WallIn W;
         W.phil = ls[0].data();
         W.vofl = vf[0].data();
+        for (int q = 0; q < 2; ++q) {   // k_walls keeps the buffers' ghosts alike
+            W.phil_more[q] = ls[q + 1].data();
+            W.vofl_more[q] = vf[q + 1].data();
+        }
         W.nxl = nxl;
         W.nx = fn[0];
         W.ny = fn[1];
@@ -111,17 +113,13 @@ extern "C" int host_clsvof_step(int I, int J, int K, const double *const geo[6],
             key[t] = (unsigned long long)tr::key_of(1.0e4);
             fix[t] = 0;
         }
-        for (size_t t = 0; t < nin; ++t) {   // k_band_scatter
-            int i, j, k;
-            D.cell_of(t, i, j, k);
+        cells([&](int i, int j, int k) {   // k_band_scatter
             tr::band_scatter(D, G, vf[0].data(), ls[0].data(), nx.data(), ny.data(), nz.data(), dis.data(), i, j, k,
                              key.data(), fix.data());
-        }
-        for (size_t t = 0; t < nin; ++t) {   // k_band_value
-            int i, j, k;
-            D.cell_of(t, i, j, k);
+        });
+        cells([&](int i, int j, int k) {   // k_band_value
             ls[0][D.g(i, j, k)] = tr::band_value(D, G, vf[0].data(), dis.data(), i, j, k, key.data(), fix.data());
-        }
+        });
     }
     memcpy(vofl, vf[0].data(), ng * sizeof(double));
     memcpy(phil, ls[0].data(), ng * sizeof(double));
@@ -136,23 +134,23 @@ extern "C" int host_uvw(int I, int J, int K, const double *const pd[3], const do
 {
     const Dims D{I, J, K};
     const Geo G{nullptr, nullptr, nullptr, pd[0], pd[1], pd[2]};
-    const int gi = I + 2, gj = J + 2;
     const double *pin[4] = {pf[0], pf[1], pf[2], pf[3]};
     for (int fam = 0; fam < 3; ++fam) {
         const double *d = fam == 0 ? G.dx : fam == 1 ? G.dy : G.dz;
         double *const *o = vf + 5 * fam;
-        for (size_t t = 0; t < D.ghosted(); ++t) {
-            const int i = (int)(t % (size_t)gi), j = (int)((t / (size_t)gi) % (size_t)gj),
-                      k = (int)(t / ((size_t)gi * gj));
-            if (i < I && j < J && k < K) {
-                double av[4];
-                tr::family_average(D, fam, d, pin, i, j, k, av);
-                for (int q = 0; q < 4; ++q) o[q][t] = av[q];
-            }
-            if (i >= 1 && i <= I && j >= 1 && j <= J && k >= 1 && k <= K)
-                o[4][t] = tr::family_vofl(D, fam, G.dx, G.dy, G.dz, pf[0], pf[1], pf[2], pf[3], pf[4],
-                                          vg[3 * fam], vg[3 * fam + 1], vg[3 * fam + 2], i, j, k);
-        }
+        for (int k = 0; k <= K + 1; ++k)   // k_uvw's 3-D grid over the ghosted cells
+            for (int j = 0; j <= J + 1; ++j)
+                for (int i = 0; i <= I + 1; ++i) {
+                    const size_t t = D.g(i, j, k);
+                    if (i < I && j < J && k < K) {
+                        double av[4];
+                        tr::family_average(D, fam, d, pin, i, j, k, av);
+                        for (int q = 0; q < 4; ++q) o[q][t] = av[q];
+                    }
+                    if (i >= 1 && i <= I && j >= 1 && j <= J && k >= 1 && k <= K)
+                        o[4][t] = tr::family_vofl(D, fam, G.dx, G.dy, G.dz, pf[0], pf[1], pf[2], pf[3], pf[4],
+                                                  vg[3 * fam], vg[3 * fam + 1], vg[3 * fam + 2], i, j, k);
+                }
     }
     return 0;
 }
