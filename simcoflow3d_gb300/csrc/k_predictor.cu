@@ -288,30 +288,29 @@ __global__ void k_pred_bc(double *pred, MomDev in, Dims d, int comp)
     const int a = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int b = blockIdx.y + 1;
     long long base, s;
-    int n, na, ct_idx;
+    int n, ct_idx;
     const double *varlo, *varhi;
     int flo, fhi;
     long long bidx;
     if (comp == 1) {   // a = j, b = k
         if (a > d.J) return;
-        base = d.sy * a + d.sz * b; s = 1; n = d.I; na = d.J;
+        base = d.sy * a + d.sz * b; s = 1; n = d.I;
         bidx = (a - 1) + (long long)d.J * (b - 1);
         varlo = in.bc[0]; varhi = in.bc[1]; flo = in.flag[0]; fhi = in.flag[1];
         ct_idx = (d.I - 1) + d.I * ((a - 1) + d.J * (b - 1));
     } else if (comp == 2) {   // a = i, b = k
         if (a > d.I) return;
-        base = a + d.sz * b; s = d.sy; n = d.J; na = d.I;
+        base = a + d.sz * b; s = d.sy; n = d.J;
         bidx = (a - 1) + (long long)d.I * (b - 1);
         varlo = in.bc[2]; varhi = in.bc[3]; flo = in.flag[2]; fhi = in.flag[3];
         ct_idx = (a - 1) + d.I * ((d.J - 1) + d.J * (b - 1));
     } else {   // a = i, b = j
         if (a > d.I) return;
-        base = a + d.sy * b; s = d.sz; n = d.K; na = d.I;
+        base = a + d.sy * b; s = d.sz; n = d.K;
         bidx = (a - 1) + (long long)d.I * (b - 1);
         varlo = in.bc[4]; varhi = in.bc[5]; flo = in.flag[4]; fhi = in.flag[5];
         ct_idx = (a - 1) + d.I * ((b - 1) + d.J * (d.K - 1));
     }
-    (void)na;
     double *p = pred + base;
     p[0] = flo == 1 ? p[s] : varlo[bidx];
     const double vh = varhi[bidx];

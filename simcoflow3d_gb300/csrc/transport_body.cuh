@@ -213,10 +213,19 @@ TR_HD double find_distance(double dx, double dy, double dz, double nxx, double n
     return lower ? sc : sm - sc;
 }
 
-// Isinterface (801-815): partly filled, or next to the opposite phase.
+// Isinterface (801-815): partly filled, or next to the opposite phase.  A
+// bulk cell -- exactly +0 or 1 with its six neighbours holding the same
+// bits -- fails every test below, so it is answered with integer compares
+// and no FP64 work.
 TR_HD bool is_interface(const Dims &D, const double *vfl, int i, int j, int k)
 {
     const double v = vfl[D.g(i, j, k)];
+    const uint64_t b = bits_of(v);
+    if ((b == 0 || b == 0x3FF0000000000000ull) && bits_of(vfl[D.g(i - 1, j, k)]) == b &&
+        bits_of(vfl[D.g(i + 1, j, k)]) == b && bits_of(vfl[D.g(i, j - 1, k)]) == b &&
+        bits_of(vfl[D.g(i, j + 1, k)]) == b && bits_of(vfl[D.g(i, j, k - 1)]) == b &&
+        bits_of(vfl[D.g(i, j, k + 1)]) == b)
+        return false;
     const double jump = 1.0 - 2.1 * VOFEPS;
     bool flag = v > VOFEPS && v < 1.0 - VOFEPS;
     if (fabs(vfl[D.g(i - 1, j, k)] - v) >= jump) flag = true;
