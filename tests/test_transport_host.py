@@ -294,3 +294,52 @@ def test_front_end_marshals_like_the_oracle(host_lib):
         for k in ("phil", "nxl", "nyl", "nzl", "vofl"):
             np.testing.assert_array_equal(vcells[f][k], ref[f][k], err_msg=f"family {f} {k}")
     sch.close()
+
+
+_SANITIZED_RUN = r"""
+import sys, ctypes as C
+sys.path[:0] = [sys.argv[2], sys.argv[3]]
+import test_transport_host as T
+L = C.CDLL(sys.argv[1])
+dp = C.POINTER(C.c_double)
+L.host_clsvof_step.argtypes = [C.c_int] * 3 + [dp * 6, dp, dp, dp, dp, dp, dp * 3, dp * 3, dp * 3, dp * 6, dp * 6,
+                                                C.c_int * 6, C.c_double * 6, C.c_int * 6, C.c_double * 6, C.c_double]
+L.host_uvw.argtypes = [C.c_int] * 3 + [dp * 3, dp * 5, dp * 9, dp * 15]
+for kind in ("plane", "rest", "shear", "random", "pow2"):
+    centres, spacings, state, vel, fn, bc_vel, lvs_bc, dt, flags, vflags = T._case(kind)
+    s, p = T._copy(state, lvs_bc)
+    T.host_step(L, centres, spacings, s, vel, fn, bc_vel, p, dt, flags, vflags)
+pgrid, pcell, vgrids, vcells = T._uvw_case(5)
+I, J, K = pgrid[0].shape
+outs = [vcells[f][k] for f in range(3) for k in ("phil", "nxl", "nyl", "nzl", "vofl")]
+vg = [a for f in range(3) for a in vgrids[f]]
+pf = [pcell[k] for k in ("phil", "nxl", "nyl", "nzl", "vofl")]
+assert L.host_uvw(I, J, K, (dp * 3)(*[T._p(a) for a in pgrid]), (dp * 5)(*[T._p(a) for a in pf]),
+                  (dp * 9)(*[T._p(a) for a in vg]), (dp * 15)(*[T._p(a) for a in outs])) == 0
+print("clean")
+"""
+
+
+def test_kernel_bodies_are_memory_clean(tmp_path):
+    """The host build under AddressSanitizer and UBSan over every scheme
+    case and the velocity cells: no out-of-bounds access, no undefined
+    behaviour (the same bodies the kernels run)."""
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("g++ not found")
+    rt = [subprocess.run([cxx, "-print-file-name=" + n], capture_output=True, text=True).stdout.strip()
+          for n in ("libasan.so", "libubsan.so")]
+    if not all(os.path.isabs(p) and os.path.exists(p) for p in rt):
+        pytest.skip("sanitizer runtimes not installed")
+    so = str(tmp_path / "libtransport_host_asan.so")
+    r = subprocess.run([cxx, "-O1", "-g", "-std=c++17", "-shared", "-fPIC", "-ffp-contract=off",
+                        "-fsanitize=address,undefined", "-fno-sanitize-recover=undefined", "-fno-omit-frame-pointer",
+                        "-I" + os.path.join(ROOT, "simcoflow3d_gb300", "csrc"),
+                        os.path.join(HERE, "transport_host.cpp"), "-o", so], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    env = dict(os.environ, LD_PRELOAD=" ".join(rt), ASAN_OPTIONS="detect_leaks=0")
+    import sys
+    r = subprocess.run([sys.executable, "-c", _SANITIZED_RUN, so, HERE, ROOT], capture_output=True, text=True,
+                       env=env, timeout=600)
+    assert r.returncode == 0 and "clean" in r.stdout, r.stderr[-3000:]
+    assert "runtime error" not in r.stderr and "AddressSanitizer" not in r.stderr, r.stderr[-3000:]
