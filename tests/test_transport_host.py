@@ -343,3 +343,63 @@ def test_kernel_bodies_are_memory_clean(tmp_path):
                        env=env, timeout=600)
     assert r.returncode == 0 and "clean" in r.stdout, r.stderr[-3000:]
     assert "runtime error" not in r.stderr and "AddressSanitizer" not in r.stderr, r.stderr[-3000:]
+
+
+class _BenchHostLib(_HostLib):
+    """_HostLib plus what bench.py's transport leg calls: page-locking (a
+    no-op), per-kernel timing and the step statistics, with made-up times
+    so the line's arithmetic runs."""
+
+    def __init__(self, L):
+        super().__init__(L)
+        self.timing = 0
+
+    def scf_host_register(self, ptr, nbytes):
+        return 0
+
+    def scf_host_unregister(self, ptr):
+        return 0
+
+    def scf_clsvof_set_timing(self, ctx, on):
+        self.timing = on
+        return 0
+
+    def scf_clsvof_run(self, ctx, steps, pstats):
+        super().scf_clsvof_run(ctx, steps, pstats)
+        st = pstats._obj
+        st.ms_run = 1.5 * steps
+        if self.timing:
+            st.ms_kernels[:] = [0.4 * steps, 0.8 * steps, 0.01 * steps, 0.2 * steps]
+        return 0
+
+    def scf_clsvof_step(self, ctx, pin, pstate, pstats):
+        super().scf_clsvof_step(ctx, pin, pstate, pstats)
+        st = pstats._obj
+        st.ms_h2d, st.ms_run, st.ms_d2h, st.ms_total, st.bytes_h2d, st.bytes_d2h = 0.5, 1.5, 0.4, 2.4, 1 << 20, 1 << 19
+        return 0
+
+
+def test_bench_transport_leg_runs_over_the_host_build(host_lib, monkeypatch, capsys):
+    """bench.py --config clsvof at 16^3 over the host build: one JSON line
+    with the contract's keys, the live roofline of the heavier kernel kind
+    and the oracle's CPU baseline."""
+    import json
+    import sys
+    import types
+    sys.path.insert(0, ROOT)
+    import bench
+    from simcoflow3d_gb300 import projection
+    fake = _BenchHostLib(host_lib)
+    monkeypatch.setattr(projection, "load_library", lambda: fake)
+    args = types.SimpleNamespace(n=16, warmup=3, steps=2, no_cpu=False, seed=1)
+    assert bench.run_clsvof(args) == 0
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+                "vs_baseline", "dtype", "data", "config", "e2e", "roofline", "clocks", "gpu_launches",
+                "cpu_baseline"):
+        assert key in line, key
+    assert line["value"] == 1.5 and line["gpu_launches"] == 2 * 66 and line["unit"] == "ms/step"
+    rf = line["roofline"]
+    assert rf["kernel"] == "k_sweep" and rf["bytes_per_launch"] == 16 ** 3 * (40 + 2 * 56) // 3
+    assert rf["achieved"] > 0 and line["e2e"]["h2d_bytes_per_step"] == 1 << 20
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["value"] > 0
