@@ -10,7 +10,7 @@ import pytest
 
 from oracle import oracle as O
 
-from test_transport_host import _case, _copy
+from test_transport_host import _case, _copy, _deformation_case
 
 pytestmark = pytest.mark.gpu
 
@@ -39,9 +39,9 @@ def _run_gpu(lib, case, steps=1):
         sch.close()
 
 
-@pytest.mark.parametrize("kind", ["plane", "rest", "shear", "random", "pow2"])
+@pytest.mark.parametrize("kind", ["plane", "rest", "shear", "random", "pow2", "deformation"])
 def test_gpu_step_matches_the_oracle(lib, kind):
-    case = _case(kind)
+    case = _deformation_case() if kind == "deformation" else _case(kind)
     centres, spacings, state, vel, fn, bc_vel, lvs_bc, dt, flags, vflags = case
     s_ref, p_ref = _copy(state, lvs_bc)
     v_ref = O.clsvof_scheme(centres, spacings, s_ref, vel, fn, bc_vel, p_ref, dt, lvs_flag=flags[0],
