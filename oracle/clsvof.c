@@ -103,6 +103,10 @@ static double min3(double a, double b, double c)
     return m < c ? m : c;
 }
 
+/* The two powers, exported for their tests. */
+double oracle_cube_rn(double x) { return cube_rn(x); }
+double oracle_pow_third(double x) { return pow_third(x); }
+
 /* Volume_Fraction_Calc (Clsvof.f90:1475-1550): the volume of the dx*dy*dz
  * box on the positive side of the plane at distance s from the corner along
  * the normal (nxx, nyy, nzz) -- the Griebel-Klitz formula.                 */

@@ -84,6 +84,9 @@ def lib():
         L.oracle_interface_reconstruct.argtypes = [C.c_int, C.c_int, C.c_int] + [dp] * 12
         L.oracle_clsvof_sweep.argtypes = [C.c_int] * 4 + [dp] * 11 + [C.c_double] + [dp] * 6
         L.oracle_clsvof_scheme.argtypes = [C.POINTER(ClsvofArgs)]
+        for name in ("oracle_cube_rn", "oracle_pow_third"):
+            getattr(L, name).argtypes = [C.c_double]
+            getattr(L, name).restype = C.c_double
         L.oracle_clsvof_redistance.argtypes = [C.c_int] * 3 + [dp] * 11
         _lib = L
     return _lib

@@ -589,3 +589,23 @@ def test_scheme_keeps_the_liquid_volume_in_a_shear():
     assert ((after > 0) & (after < 1)).sum() > 100
     assert abs(after.sum() - before) < 1e-11 * before
     assert np.abs(after - vof0).max() > 0.05
+
+
+def test_powers_are_correctly_rounded():
+    """x**3.d0 and x**(1.d0/3.d0) in the oracle are the exact powers rounded
+    once to nearest, against 300-bit arithmetic, on random arguments and on
+    arguments where the C library's pow lands on the wrong side of a
+    near-tie (0.501 against 0.499 ulp)."""
+    mp = pytest.importorskip("mpmath")
+    mp.mp.prec = 300
+    L = O.lib()
+    third = mp.mpf(1.0 / 3.0)   # fl(1/3), the exponent Fortran's 1.d0/3.d0 holds
+    rng = np.random.default_rng(11)
+    xs = list(np.exp(rng.uniform(np.log(1e-30), np.log(1e3), 3000)))
+    ties_cube = ["0x1.29b7c7f567ad7p-4", "0x1.1ea6bb697d9dap-29", "0x1.ccf39d3c80638p-2"]
+    ties_third = ["0x1.e9f8dceb7595ep-8", "0x1.4406cfa26b09p-3", "0x1.f0dc3db8102p-15", "0x1.326eef373a70ap-7"]
+    for x in xs + [float.fromhex(h) for h in ties_cube]:
+        assert L.oracle_cube_rn(x) == float(mp.mpf(x) ** 3), x.hex()
+    for x in xs + [float.fromhex(h) for h in ties_third]:
+        assert L.oracle_pow_third(x) == float(mp.mpf(x) ** third), x.hex()
+    assert L.oracle_pow_third(0.0) == 0.0
