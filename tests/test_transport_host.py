@@ -1,10 +1,13 @@
 """The CLSVOF transport kernels' bodies (simcoflow3d_gb300/csrc/
 transport_body.cuh) compiled for the host with every index range-checked
 (tests/transport_host.cpp drives them over the kernels' thread indices),
-against the oracle's Clsvof_Scheme, bit for bit.  The host build computes
-x**3 and x**(1/3) with the C library's pow like the oracle, so any
-difference is a difference in the kernels' logic or index arithmetic.  CPU
-only; the device run is checked in test_gpu_vof_transport.py."""
+against the oracle, bit for bit: Clsvof_Scheme on six cases and
+ComputeUVWLiquidField on two.  Also on the host build: the same runs under
+AddressSanitizer and UBSan; the independence of the results from the ulp
+the math library's cbrt and log return (so the device reproduces them);
+the Python front end (transport.py) and bench.py's transport leg over a
+stand-in library that unpacks the C ABI's structs into the host build.  CPU
+only; the device runs are in test_gpu_vof_transport.py."""
 import ctypes as C
 import os
 import shutil
