@@ -328,6 +328,17 @@ int scf_host_register(void *ptr, size_t bytes);
 int scf_host_unregister(void *ptr);
 int scf_abi_version(void);
 
+/* ---- test hooks (no counterpart in the reference) ------------------------
+ * Every device buffer of this library (projection, geometry, predictor,
+ * transport and output contexts) is allocated through one counting wrapper.
+ * scf_debug_fail_device_alloc(n) makes the n-th device allocation from now
+ * fail with SCF_ERR_OUT_OF_MEMORY, as a full GPU would, without calling
+ * cudaMalloc for it (n = 0: off); the hook is process-wide and one-shot.
+ * scf_debug_device_buffers() returns how many device buffers the library
+ * holds, so a test can check that a failed create leaks none.             */
+int     scf_debug_fail_device_alloc(int64_t nth);
+int64_t scf_debug_device_buffers(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -25,7 +25,8 @@ from .projection import Projection
 
 
 def _to_np(t: torch.Tensor) -> np.ndarray:
-    assert t.dtype == torch.float64 and t.device.type == "cpu"
+    if t.dtype != torch.float64 or t.device.type != "cpu":
+        raise ValueError("a CPU float64 tensor is required")
     return np.asfortranarray(t.detach().contiguous().numpy().T)
 
 

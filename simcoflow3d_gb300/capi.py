@@ -227,17 +227,28 @@ class ScfClsvofStats(C.Structure):
         return out
 
 
+def require(cond: bool, message: str) -> None:
+    """Argument check that stays active under ``python -O``: a wrong array
+    handed to the C side would be read or written past its end."""
+    if not cond:
+        raise ValueError(message)
+
+
+def require_shape(a: np.ndarray, shape, name: str = "array") -> None:
+    require(tuple(a.shape) == tuple(shape), f"{name} has shape {tuple(a.shape)}, expected {tuple(shape)}")
+
+
 def dptr(a: Optional[np.ndarray]):
     if a is None:
         return c_double_p()
-    assert a.dtype == np.float64 and (a.flags.f_contiguous or a.ndim <= 1), "FP64 Fortran-contiguous array required"
+    require(a.dtype == np.float64 and (a.flags.f_contiguous or a.ndim <= 1), "FP64 Fortran-contiguous array required")
     return a.ctypes.data_as(c_double_p)
 
 
 def iptr(a: Optional[np.ndarray]):
     if a is None:
         return c_int32_p()
-    assert a.dtype == np.int32 and (a.flags.f_contiguous or a.ndim <= 1), "int32 Fortran-contiguous array required"
+    require(a.dtype == np.int32 and (a.flags.f_contiguous or a.ndim <= 1), "int32 Fortran-contiguous array required")
     return a.ctypes.data_as(c_int32_p)
 
 

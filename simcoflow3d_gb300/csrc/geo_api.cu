@@ -11,6 +11,7 @@
 #include "../../include/scf_geometry.h"
 #include "../../include/scf_projection.h"
 #include "geo_kernels.h"
+#include "scf_devmem.h"
 
 struct scf_geo_ctx {
     Dims d;
@@ -55,7 +56,7 @@ int galloc(scf_geo_ctx *ctx, P **ptr, size_t count)
 {
     void *p = nullptr;
     const size_t bytes = count * sizeof(P) > 0 ? count * sizeof(P) : 16;
-    cudaError_t e = cudaMalloc(&p, bytes);
+    cudaError_t e = scf_mem::dev_malloc(&p, bytes);
     if (e != cudaSuccess) {
         geo_err(ctx, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
         return SCF_ERR_OUT_OF_MEMORY;
@@ -199,7 +200,7 @@ int scf_geo_destroy(scf_geo_ctx *ctx)
     if (!ctx) return SCF_ERR_BAD_ARG;
     cudaSetDevice(ctx->device);
     if (ctx->st) cudaStreamSynchronize(ctx->st);
-    for (void *p : ctx->mem) cudaFree(p);
+    for (void *p : ctx->mem) scf_mem::dev_free(p);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     for (int q = 0; q < 8; ++q)

@@ -10,10 +10,15 @@
 // two-sum and the FMA-based two-product -- with every FP32 operation an
 // explicitly rounded intrinsic, so that no contraction changes them.  Each
 // vector occupies the 8 bytes per cell of its FP64 counterpart (the FP64
-// buffers are reused), so memory traffic is unchanged; the FP64 pipe is left
-// to a handful of conversions per thread.  The solution is converted back to
-// FP64 at the end of a CG round and its residual is recomputed in FP64, so
-// the stopping test on the true residual is unchanged.
+// buffers are reused), so memory traffic is unchanged.  The dot products of
+// the iteration -- (p, Ap), (r, z) and (r, r) -- are FP64: each cell's
+// double-float values are widened to FP64 (the FP32 -> FP64 widening is done
+// with integer operations, which are exact), multiplied with an FP64 FMA and
+// accumulated in FP64 per thread, per block and across blocks.  That is two
+// to four FP64 operations per cell and dot, which the memory-bound kernels
+// hide.  The solution is converted back to FP64 at the end of a CG round and
+// its residual is recomputed in FP64, so the stopping test on the true
+// residual is unchanged.
 #include "scf_kernels.h"
 
 namespace {
@@ -51,6 +56,23 @@ __device__ __forceinline__ float2 dfrom(double d)
     return make_float2(hi, __double2float_rn(d - (double)hi));
 }
 __device__ __forceinline__ double dto(float2 x) { return (double)x.x + (double)x.y; }
+
+// FP32 -> FP64 widening on the integer pipe (exact: the exponent is rebiased
+// and the significand shifted into place).  Zeros keep their sign; the rare
+// subnormal inputs, Inf and NaN take the hardware conversion.
+__device__ __forceinline__ double widen(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xffu;
+    if (e - 1u < 254u) {   // normal numbers
+        const unsigned hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7fffffu) >> 3);
+        return __hiloint2double((int)hi, (int)(u << 29));
+    }
+    if ((u & 0x7fffffffu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+    return (double)f;
+}
+// the FP64 value of a double-float: one FP64 addition
+__device__ __forceinline__ double dwide(float2 x) { return widen(x.x) + widen(x.y); }
 __device__ __forceinline__ float2 ld(const float2 *__restrict__ v, int c) { return v[c]; }
 
 #define DF_ZCHUNK(A)                                                   \
@@ -75,19 +97,19 @@ Launch3 df_launch(const DfOp &A)
     return l;
 }
 
-// q = A p, and the block partials of (p, q) and of the sum of q
+// q = A p, and the block partials of (p, q) and of the sum of q, both FP64
 __global__ void __launch_bounds__(128) k_spmv_df(DfOp A, const float2 *__restrict__ p, float2 *__restrict__ q,
                                                  double *__restrict__ part, int n0)
 {
     DF_ZCHUNK(A);
-    float2 v = make_float2(0.f, 0.f), sq = make_float2(0.f, 0.f);
+    double v = 0.0, sq = 0.0;
     if (in) {
         const int sy = A.hi.sy, sz = A.hi.sz;
         int c = i + sy * j + sz * k0;
         float2 xm = ld(p, c - sz), x0 = ld(p, c), tb = cf(A.hi.cT, A.tlo, c - sz);
         // the six neighbour products are summed as a tree (short dependency
         // chains: the kernel is latency-bound, not memory-bound, otherwise)
-        float2 v2 = make_float2(0.f, 0.f), sq2 = make_float2(0.f, 0.f);
+        double v2 = 0.0, sq2 = 0.0;
         int par = 0;
 #pragma unroll 2
         for (int k = k0; k <= k1; ++k, c += sz) {
@@ -100,25 +122,41 @@ __global__ void __launch_bounds__(128) k_spmv_df(DfOp A, const float2 *__restric
             const float2 s = dadd(dadd(sx, syy), sz2);
             const float2 y = dadd(dmul(cf(A.hi.diag, A.dlo, c), x0), dneg(s));
             q[c] = y;
-            if (par) { v2 = dadd(v2, dmul(x0, y)); sq2 = dadd(sq2, y); }
-            else { v = dadd(v, dmul(x0, y)); sq = dadd(sq, y); }
+            const double yd = dwide(y);
+            if (par) { v2 = fma(dwide(x0), yd, v2); sq2 += yd; }
+            else { v = fma(dwide(x0), yd, v); sq += yd; }
             par ^= 1;
             xm = x0; x0 = xp; tb = tt;
         }
-        v = dadd(v, v2);
-        sq = dadd(sq, sq2);
+        v += v2;
+        sq += sq2;
     }
-    double dv = block_sum(dto(v));
+    double dv = block_sum(v);
     __syncthreads();
-    double ds = block_sum(dto(sq));
+    double ds = block_sum(sq);
     if (thread_linear() == 0) {
         part[block_linear()] = dv;
         part[n0 + block_linear()] = ds;
     }
 }
 
-// x += alpha p, r -= alpha (q - mean q), (r, r) (FP32 squares of the hi parts,
-// FP64 across threads: it only feeds the stopping test); also the FP32 copy
+// (r, z) for beta: r double-float, z the FP32 preconditioned residual; FP64
+// products and sums
+__global__ void __launch_bounds__(128) k_dot_rz_df(DfOp A, const float2 *__restrict__ r, const float *__restrict__ z,
+                                                   double *__restrict__ part)
+{
+    DF_ZCHUNK(A);
+    double v = 0.0;
+    if (in) {
+        const int sy = A.hi.sy, sz = A.hi.sz;
+        int c = i + sy * j + sz * k0;
+        for (int k = k0; k <= k1; ++k, c += sz) v = fma(dwide(ld(r, c)), widen(z[c]), v);
+    }
+    v = block_sum(v);
+    if (thread_linear() == 0) part[block_linear()] = v;
+}
+
+// x += alpha p, r -= alpha (q - mean q), (r, r) in FP64; also the FP32 copy
 // of r (its hi part) for the V-cycle and, when x0 is given, the first
 // point-Jacobi smoothing step from a zero guess, x0 = first D^-1 r.
 __global__ void __launch_bounds__(128) k_cg_update_df(DfOp A, float2 *__restrict__ x, float2 *__restrict__ r,
@@ -132,7 +170,6 @@ __global__ void __launch_bounds__(128) k_cg_update_df(DfOp A, float2 *__restrict
         const float2 al = dfrom(scal[S_ALPHA]), mal = dneg(al), qm = dfrom(scal[S_QMEAN]);
         const int sy = A.hi.sy, sz = A.hi.sz;
         int c = i + sy * j + sz * k0;
-        float acc = 0.f;
         for (int k = k0; k <= k1; ++k, c += sz) {
             x[c] = dadd(ld(x, c), dmul(al, ld(p, c)));
             const float dg = A.hi.diag[c];
@@ -142,9 +179,9 @@ __global__ void __launch_bounds__(128) k_cg_update_df(DfOp A, float2 *__restrict
             r[c] = rn;
             rlow[c] = rn.x;
             if (x0) x0[c] = first * (dg > 0.f ? __frcp_rn(dg) : 0.f) * rn.x;
-            acc = __fmaf_rn(rn.x, rn.x, acc);
+            const double rd = dwide(rn);
+            v = fma(rd, rd, v);
         }
-        v = (double)acc;
     }
     v = block_sum(v);
     if (thread_linear() == 0) part[block_linear()] = v;
@@ -190,6 +227,14 @@ void df_spmv_dot(const DfOp &A, const float2 *p, float2 *q, Reducer &R, bool sin
     kt_end(kt, id, st);
     *launches += 1;
     reduce_alpha(R, (int)nblocks(l), singular, st, launches);
+}
+
+void df_dot_rz(const DfOp &A, const float2 *r, const float *z, Reducer &R, cudaStream_t st, int *launches)
+{
+    Launch3 l = df_launch(A);
+    k_dot_rz_df<<<l.grid, l.block, 0, st>>>(A, r, z, R.partials);
+    *launches += 1;
+    reduce_beta(R, (int)nblocks(l), st, launches);
 }
 
 void df_cg_update(const DfOp &A, float2 *x, float2 *r, const float2 *p, const float2 *q, float *rlow, float *x0,

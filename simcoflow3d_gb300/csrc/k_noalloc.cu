@@ -81,8 +81,12 @@ extern "C" int scf_apply_operator_noalloc(int32_t imax, int32_t jmax, int32_t km
                                           const double *x, double *y, double *x_dot_ax, void *stream)
 {
     if (imax < 1 || jmax < 1 || kmax < 1) return SCF_ERR_BAD_ARG;
-    const long long ng = (long long)(imax + 2) * (jmax + 2) * (kmax + 2);
-    if (ng > SCF_NOALLOC_MAX_CELLS) return SCF_ERR_BAD_ARG;
+    // each factor is at most 2^31 + 1, so the first product fits in 64 bits;
+    // the second is formed only once the first is known to be in range
+    const long long g0 = (long long)imax + 2, g1 = (long long)jmax + 2, g2 = (long long)kmax + 2;
+    if (g0 > SCF_NOALLOC_MAX_CELLS || g1 > SCF_NOALLOC_MAX_CELLS || g2 > SCF_NOALLOC_MAX_CELLS) return SCF_ERR_BAD_ARG;
+    const long long g01 = g0 * g1;
+    if (g01 > SCF_NOALLOC_MAX_CELLS || g01 * g2 > SCF_NOALLOC_MAX_CELLS) return SCF_ERR_BAD_ARG;
     if (!diag || !cpl_e || !cpl_n || !cpl_t || !x || !y) return SCF_ERR_BAD_ARG;
     double *scratch = nullptr;
     int rc = scratch_for_current_device(&scratch);

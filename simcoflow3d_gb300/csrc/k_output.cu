@@ -15,6 +15,7 @@
 
 #include "../../include/scf_output.h"
 #include "scf_common.cuh"
+#include "scf_devmem.h"
 
 namespace {
 
@@ -61,7 +62,7 @@ struct Cleanup {
     ~Cleanup()
     {
         for (auto s : st) cudaStreamSynchronize(s);
-        for (void *p : dev) cudaFree(p);
+        for (void *p : dev) scf_mem::dev_free(p);
         for (void *p : host) cudaFreeHost(p);
         for (auto e : ev) cudaEventDestroy(e);
         for (auto s : st) cudaStreamDestroy(s);
@@ -148,7 +149,7 @@ extern "C" int scf_write_vtr(const char *path, int32_t imax, int32_t jmax, int32
                 return SCF_ERR_CUDA;
             c.ev.push_back(e0); c.ev.push_back(e1); c.ev.push_back(e2);
             void *p = nullptr;
-            if (cudaMalloc(&p, sizeof(float) * n) != cudaSuccess) return SCF_ERR_OUT_OF_MEMORY;
+            if (scf_mem::dev_malloc(&p, sizeof(float) * n) != cudaSuccess) return SCF_ERR_OUT_OF_MEMORY;
             c.dev.push_back(p);
             dbuf[s] = (float *)p;
             if (cudaMallocHost(&p, sizeof(float) * n) != cudaSuccess) return SCF_ERR_OUT_OF_MEMORY;
@@ -160,7 +161,7 @@ extern "C" int scf_write_vtr(const char *path, int32_t imax, int32_t jmax, int32
         if (host_fields)
             for (int s = 0; s < 2; ++s) {
                 void *p = nullptr;
-                if (cudaMalloc(&p, sizeof(double) * ng) != cudaSuccess) return SCF_ERR_OUT_OF_MEMORY;
+                if (scf_mem::dev_malloc(&p, sizeof(double) * ng) != cudaSuccess) return SCF_ERR_OUT_OF_MEMORY;
                 c.dev.push_back(p);
                 dsrc[s] = (double *)p;
             }

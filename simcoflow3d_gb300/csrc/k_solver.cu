@@ -252,6 +252,12 @@ void cg_dot_rz(const LevelView<double> &A, const double *r, const T *rlow, const
     *launches += 2;
 }
 
+void reduce_beta(Reducer &R, int nblocks, cudaStream_t st, int *launches)
+{
+    k_reduce<<<1, 1024, 0, st>>>(R.partials, nblocks, R.scal, 0, RM_BETA);
+    *launches += 1;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(128) k_pupdate(LevelView<double> A, const T *__restrict__ z,
                                                  double *__restrict__ p, const double *__restrict__ scal, int first)

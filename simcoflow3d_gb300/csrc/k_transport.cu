@@ -7,12 +7,14 @@
 //                                  with the divergence term fused in;
 //   k_walls                        the wall planes and ghosts;
 //   k_reconstruct (tail)           normals, liquid normals, centre distances;
-//   k_band_reset, k_band_scatter,  the redistancing: every interface cell
-//   k_band_value                   sends its band distances with a 64-bit
-//                                  atomicMin (non-negative doubles order like
-//                                  their bits), so the result is the
-//                                  reference's running minimum whatever the
-//                                  order.
+//   k_band_reset, k_band_pairs,    the redistancing: the reset lists the
+//   k_band_value                   interface cells; then one block per
+//                                  listed cell computes its 9^3 band pairs,
+//                                  one pair per thread, and sends each
+//                                  distance with a 64-bit atomicMin
+//                                  (non-negative doubles order like their
+//                                  bits), so the result is the reference's
+//                                  running minimum whatever the order.
 // The VOF and level set ping-pong through three buffers (the sub-step's
 // input, its first sweep's result, which the later sweeps' divergence terms
 // read, and the second sweep's result); every sub-step ends in buffer 0.
@@ -29,6 +31,7 @@
 
 #include "../../include/scf_clsvof.h"
 #include "transport_body.cuh"
+#include "scf_devmem.h"
 
 using tr::Dims;
 using tr::Geo;
@@ -49,6 +52,8 @@ struct scf_clsvof_ctx {
     double *lvs_bc[6] = {}, *vof_bc[6] = {};
     unsigned long long *key = nullptr;
     uint8_t *fix = nullptr;
+    uint32_t *band_list = nullptr;       // interface cells of the sub-step (interior indices)
+    unsigned *nband = nullptr;           // how many
     double *vgeo[3][3] = {};             // U, V, W grid spacings (allocated on first use)
     double *vfld[3][5] = {};             // U, V, W: phiL, nxL, nyL, nzL, vofL
     int lvs_flag[6] = {}, vof_flag[6] = {};
@@ -141,23 +146,45 @@ __global__ void k_walls(Dims D, Geo G, tr::WallIn W)
         tr::wall_point(D, G, W, axis, t);
 }
 
-__global__ void k_band_reset(size_t nin, unsigned long long *key, uint8_t *fix)
-{
-    const unsigned long long far = (unsigned long long)tr::key_of(1.0e4);
-    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nin; t += (size_t)gridDim.x * blockDim.x) {
-        key[t] = far;
-        fix[t] = 0;
-    }
-}
-
-__global__ void k_band_scatter(Dims D, Geo G, const double *__restrict__ vfl, const double *__restrict__ phi,
-                               const double *__restrict__ nx, const double *__restrict__ ny,
-                               const double *__restrict__ nz, const double *__restrict__ dis,
-                               unsigned long long *key, uint8_t *fix)
+// Resets the band keys and marks, and lists the interface cells (warp-
+// aggregated appends; the list's order does not matter).
+__global__ void k_band_reset(Dims D, const double *__restrict__ vfl, unsigned long long *key, uint8_t *fix,
+                             uint32_t *list, unsigned *count)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
-    if (i > D.I) return;
-    tr::band_scatter(D, G, vfl, phi, nx, ny, nz, dis, i, j, k, key, fix);
+    const bool in = i <= D.I;
+    bool src = false;
+    if (in) {
+        const size_t c = D.n(i, j, k);
+        key[c] = (unsigned long long)tr::key_of(1.0e4);
+        fix[c] = 0;
+        src = tr::band_interface(vfl[D.g(i, j, k)]);
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, src);
+    if (!mask) return;
+    const int lane = threadIdx.x & 31, leader = __ffs(mask) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(count, (unsigned)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (src) list[base + __popc(mask & ((1u << lane) - 1u))] = (uint32_t)D.n(i, j, k);
+}
+
+// The band pairs of the listed interface cells: a block takes one cell at a
+// time and its threads the cell's 729 offsets.
+__global__ void __launch_bounds__(256, 2) k_band_pairs(Dims D, Geo G, const double *__restrict__ vfl,
+                                                    const double *__restrict__ phi, const double *__restrict__ nx,
+                                                    const double *__restrict__ ny, const double *__restrict__ nz,
+                                                    const double *__restrict__ dis, const uint32_t *__restrict__ list,
+                                                    const unsigned *__restrict__ count, unsigned long long *key,
+                                                    uint8_t *fix)
+{
+    const unsigned n = *count;
+    for (unsigned q = blockIdx.x; q < n; q += gridDim.x) {
+        int i, j, k;
+        tr::cell_of(D, list[q], i, j, k);
+        for (int t = threadIdx.x; t < tr::BAND_CELLS; t += blockDim.x)
+            tr::band_pair(D, G, vfl, phi, nx, ny, nz, dis, i, j, k, t, key, fix);
+    }
 }
 
 __global__ void k_band_value(Dims D, Geo G, const double *__restrict__ vfl, const double *__restrict__ dis,
@@ -225,14 +252,16 @@ struct Timer {
     }
 };
 
+// Blocks of k_band_pairs: two per SM (the residency its registers allow),
+// each looping over the listed cells.
+constexpr int kBandBlocks = 152 * 2;
+
 // Clsvof_Scheme (Clsvof.f90:355-798) on the staged state; counts launches.
 int scheme_step(scf_clsvof_ctx *ctx, int &launches, Timer &T)
 {
     const Dims D = ctx->D;
     const Geo G = geo_of(ctx);
-    const size_t nin = D.interior();
     const double dtv = ctx->dt / (double)tr::NSUB;
-    const int bi = blocks_for(nin);
     const dim3 gin((D.I + NX - 1) / NX, D.J, D.K);   // interior cells
     size_t pmax = std::max(D.plane_size(0), std::max(D.plane_size(1), D.plane_size(2)));
     int rc;
@@ -297,14 +326,16 @@ int scheme_step(scf_clsvof_ctx *ctx, int &launches, Timer &T)
         T.after();
         if ((rc = launch_check(ctx, "k_reconstruct")) != SCF_OK) return rc;
         T.before(3);
-        k_band_reset<<<bi, NT, 0, ctx->st>>>(nin, ctx->key, ctx->fix);
+        if (cudaMemsetAsync(ctx->nband, 0, sizeof(unsigned), ctx->st) != cudaSuccess)
+            return launch_check(ctx, "cudaMemsetAsync");
+        k_band_reset<<<gin, NX, 0, ctx->st>>>(D, ctx->vf[0], ctx->key, ctx->fix, ctx->band_list, ctx->nband);
         T.after();
         if ((rc = launch_check(ctx, "k_band_reset")) != SCF_OK) return rc;
         T.before(3);
-        k_band_scatter<<<gin, NX, 0, ctx->st>>>(D, G, ctx->vf[0], ctx->ls[0], ctx->nx, ctx->ny, ctx->nz, ctx->dis,
-                                                ctx->key, ctx->fix);
+        k_band_pairs<<<kBandBlocks, 256, 0, ctx->st>>>(D, G, ctx->vf[0], ctx->ls[0], ctx->nx, ctx->ny, ctx->nz,
+                                                       ctx->dis, ctx->band_list, ctx->nband, ctx->key, ctx->fix);
         T.after();
-        if ((rc = launch_check(ctx, "k_band_scatter")) != SCF_OK) return rc;
+        if ((rc = launch_check(ctx, "k_band_pairs")) != SCF_OK) return rc;
         T.before(3);
         k_band_value<<<gin, NX, 0, ctx->st>>>(D, G, ctx->vf[0], ctx->dis, ctx->key, ctx->fix, ctx->ls[0]);
         T.after();
@@ -319,7 +350,7 @@ int alloc(scf_clsvof_ctx *ctx, P **ptr, size_t count)
 {
     void *p = nullptr;
     const size_t bytes = std::max<size_t>(count * sizeof(P), 16);
-    const cudaError_t e = cudaMalloc(&p, bytes);
+    const cudaError_t e = scf_mem::dev_malloc(&p, bytes);
     if (e != cudaSuccess) {
         tr_err(ctx, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
         return SCF_ERR_OUT_OF_MEMORY;
@@ -343,6 +374,9 @@ extern "C" int scf_clsvof_create(scf_clsvof_ctx **out, int32_t imax, int32_t jma
     if (!out) return SCF_ERR_BAD_ARG;
     *out = nullptr;
     if (imax < 3 || jmax < 3 || kmax < 3 || imax > 65533 || jmax > 65533 || kmax > 65533) return SCF_ERR_BAD_ARG;
+    // the redistancing lists interface cells by 32-bit interior index
+    if ((unsigned long long)imax * (unsigned long long)jmax * (unsigned long long)kmax >= (1ull << 32))
+        return SCF_ERR_BAD_ARG;
     if (cudaSetDevice(device) != cudaSuccess) return SCF_ERR_NO_DEVICE;
     scf_clsvof_ctx *ctx = new scf_clsvof_ctx();
     ctx->device = device;
@@ -366,7 +400,7 @@ extern "C" int scf_clsvof_create(scf_clsvof_ctx **out, int32_t imax, int32_t jma
     for (auto &p : ctx->vel) TRY(p, ng)
     for (int a = 0; a < 3; ++a) TRY(ctx->bc_vel[a], ctx->D.plane_size(a))
     for (int f = 0; f < 6; ++f) { TRY(ctx->lvs_bc[f], ctx->D.plane_size(f / 2)) TRY(ctx->vof_bc[f], ctx->D.plane_size(f / 2)) }
-    TRY(ctx->key, nin) TRY(ctx->fix, nin)
+    TRY(ctx->key, nin) TRY(ctx->fix, nin) TRY(ctx->band_list, nin) TRY(ctx->nband, 1)
 #undef TRY
     *out = ctx;
     return SCF_OK;
@@ -393,7 +427,7 @@ extern "C" int scf_clsvof_destroy(scf_clsvof_ctx *ctx)
     cudaSetDevice(ctx->device);
     if (ctx->st) cudaStreamSynchronize(ctx->st);
     for (cudaEvent_t e : ctx->tev) cudaEventDestroy(e);
-    for (void *p : ctx->mem) cudaFree(p);
+    for (void *p : ctx->mem) scf_mem::dev_free(p);
     for (auto &e : ctx->ev)
         if (e) cudaEventDestroy(e);
     if (ctx->st) cudaStreamDestroy(ctx->st);

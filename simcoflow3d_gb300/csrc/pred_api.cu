@@ -14,6 +14,7 @@
 
 #include "../../include/scf_predictor.h"
 #include "pred_kernels.h"
+#include "scf_devmem.h"
 
 using namespace pred;
 
@@ -72,7 +73,7 @@ int malloc0(scf_mom_ctx *ctx, P **ptr, size_t count)
 {
     void *p = nullptr;
     const size_t bytes = std::max<size_t>(count * sizeof(P), 16);
-    cudaError_t e = cudaMalloc(&p, bytes);
+    cudaError_t e = scf_mem::dev_malloc(&p, bytes);
     if (e != cudaSuccess) {
         mom_err(ctx, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
         return SCF_ERR_OUT_OF_MEMORY;
@@ -223,7 +224,8 @@ int solve_fp64(scf_mom_ctx *ctx, const scf_mom_opts &o, SolveOut &out)
     while (out.iterations < o.max_iter) {
         set_target(ctx->sc, target, ctx->st);
         int rc = SCF_OK;
-        out.iterations += run_batches<double>(ctx, o, m, V, true, o.max_iter - out.iterations, out, rc);
+        const int its = run_batches<double>(ctx, o, m, V, true, o.max_iter - out.iterations, out, rc);
+        out.iterations += its;
         if (rc != SCF_OK) return rc;
         if (!ctx->sc_host->done) break;   // iteration cap
         // converged by the recursive residual, or broken down: check the
@@ -232,7 +234,14 @@ int solve_fp64(scf_mom_ctx *ctx, const scf_mom_opts &o, SolveOut &out)
         out.launches += 2;
         RS();
         rr = ctx->sc_host->rr;
+        if (!std::isfinite(rr)) {
+            mom_err(ctx, "non-finite residual after %d iterations", out.iterations);
+            return SCF_ERR_NONFINITE;
+        }
         if (rr <= target) { out.converged = 1; break; }
+        // a breakdown in the first iteration of a round leaves the residual
+        // as it was, and a restart from it would break down again
+        if (its == 0) break;
         MK(cudaMemcpyAsync(V.r0, V.r, bytes, cudaMemcpyDeviceToDevice, ctx->st));
         ++out.rounds;
     }
@@ -271,8 +280,10 @@ int solve_mixed(scf_mom_ctx *ctx, const scf_mom_opts &o, SolveOut &out)
         MK(cudaMemsetAsync(V.x, 0, bytes32, ctx->st));
         set_target(ctx->sc, inner, ctx->st);
         int rc = SCF_OK;
-        out.iterations += run_batches<float>(ctx, o, m32, V, true, o.max_iter - out.iterations, out, rc);
+        const int its = run_batches<float>(ctx, o, m32, V, true, o.max_iter - out.iterations, out, rc);
+        out.iterations += its;
         if (rc != SCF_OK) return rc;
+        if (its == 0) break;   // breakdown at the round's first iteration: x unchanged, no progress possible
         xadd(d, xa, V.x, ctx->st);
         resid64(d, m, ctx->b, xa, nullptr, V.r, false, ctx->R, ctx->sc, ctx->st);
         out.launches += 3;
@@ -372,7 +383,7 @@ extern "C" int scf_mom_destroy(scf_mom_ctx *ctx)
     if (!ctx) return SCF_OK;
     cudaSetDevice(ctx->device);
     if (ctx->st) cudaStreamSynchronize(ctx->st);
-    for (void *p : ctx->mem) cudaFree(p);
+    for (void *p : ctx->mem) scf_mem::dev_free(p);
     if (ctx->sc_host) cudaFreeHost(ctx->sc_host);
     if (ctx->counts_host) cudaFreeHost(ctx->counts_host);
     for (auto e : ctx->ev)

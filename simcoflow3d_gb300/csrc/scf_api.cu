@@ -13,6 +13,7 @@
 #include <vector>
 #include "scf_kernels.h"
 #include "../../include/scf_projection.h"
+#include "scf_devmem.h"
 
 namespace {
 
@@ -21,7 +22,7 @@ struct DevBuf {
     ~DevBuf() { release(); }
     void release()
     {
-        for (void *p : ptrs) cudaFree(p);
+        for (void *p : ptrs) scf_mem::dev_free(p);
         ptrs.clear();
     }
 };
@@ -131,7 +132,7 @@ int dalloc(scf_ctx *ctx, DevBuf &mem, P **ptr, size_t count)
     void *p = nullptr;
     size_t bytes = count * sizeof(P);
     if (bytes == 0) bytes = 16;
-    cudaError_t e = cudaMalloc(&p, bytes);
+    cudaError_t e = scf_mem::dev_malloc(&p, bytes);
     if (e != cudaSuccess) {
         set_err(ctx, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
         return SCF_ERR_OUT_OF_MEMORY;
@@ -454,6 +455,17 @@ DfOp df_view(scf_ctx *ctx)
     return D;
 }
 
+// beta from (r, z): FP64 vectors, or (mixed) the double-float r with the
+// FP32 z, both in FP64 arithmetic.
+template <typename T>
+void cg_beta(scf_ctx *ctx, const T *z)
+{
+    if constexpr (sizeof(T) == 4)
+        df_dot_rz(df_view(ctx), (const float2 *)ctx->r, z, ctx->R, ctx->st, &ctx->launches);
+    else
+        cg_dot_rz<double>(fine_view(ctx), ctx->r, ctx->r, z, ctx->R, ctx->st, &ctx->launches);
+}
+
 // New search direction p = z + beta p: FP64 vectors, or (mixed) double-float
 // vectors held in the same buffers.
 template <typename T>
@@ -492,10 +504,9 @@ void cg_step(scf_ctx *ctx, MgLevel<T> *L, const ChebCoef &cc, bool singular, KTi
 template <typename T>
 void iteration_kernels(scf_ctx *ctx, MgLevel<T> *L, const ChebCoef &cc, bool singular)
 {
-    const LevelView<double> A = fine_view(ctx);
     KTimer *kt = ctx->kt.on ? &ctx->kt : nullptr;
     T *z = precondition<T>(ctx, L, cc, fuse_first(ctx));
-    cg_dot_rz<T>(A, ctx->r, (const T *)L[0].b, z, ctx->R, ctx->st, &ctx->launches);
+    cg_beta<T>(ctx, z);
     cg_direction<T>(ctx, z, false);
     cg_step<T>(ctx, L, cc, singular, kt);
 }
@@ -589,7 +600,7 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
             df_from_double(ctx->r, (float2 *)ctx->r, ng, ctx->st, &ctx->launches);
         }
         T *z = precondition<T>(ctx, L, cc, false);
-        cg_dot_rz<T>(A, ctx->r, (const T *)L[0].b, z, ctx->R, ctx->st, &ctx->launches);
+        cg_beta<T>(ctx, z);
         cg_direction<T>(ctx, z, true);
         bool conv = false;
         stalled = false;
@@ -1107,9 +1118,8 @@ AdjArgs adj_args(scf_ctx *ctx)
     return A;
 }
 
-int ensure_adj(scf_ctx *ctx)
+int alloc_adj(scf_ctx *ctx)
 {
-    if (ctx->adj_rho) return SCF_OK;
     const int ng = ctx->d.ng;
     DALLOC(ctx->adjmem, ctx->adj_rho, ng);
     DALLOC(ctx->adjmem, ctx->adj_g, ng);
@@ -1120,6 +1130,20 @@ int ensure_adj(scf_ctx *ctx)
     DALLOC(ctx->adjmem, ctx->adj_gw, ng);
     DALLOC(ctx->adjmem, ctx->adj_grho, ng);
     return SCF_OK;
+}
+
+// The adjoint's buffers, allocated on first use; all or none (a failed
+// allocation releases the ones made, so a later call starts over).
+int ensure_adj(scf_ctx *ctx)
+{
+    if (ctx->adj_grho) return SCF_OK;
+    const int rc = alloc_adj(ctx);
+    if (rc) {
+        ctx->adjmem.release();
+        ctx->adj_rho = ctx->adj_g = ctx->adj_r = ctx->adj_pfwd = nullptr;
+        ctx->adj_gu = ctx->adj_gv = ctx->adj_gw = ctx->adj_grho = nullptr;
+    }
+    return rc;
 }
 
 }  // namespace
@@ -1445,7 +1469,21 @@ int scf_host_unregister(void *ptr)
 
 int scf_abi_version(void) { return SCF_ABI_VERSION; }
 
+int scf_debug_fail_device_alloc(int64_t nth)
+{
+    if (nth < 0) return SCF_ERR_BAD_ARG;
+    scf_mem::fail_countdown.store(nth);
+    return SCF_OK;
+}
+
+int64_t scf_debug_device_buffers(void) { return scf_mem::live.load(); }
+
 }  // extern "C"
+
+namespace scf_mem {
+std::atomic<long long> fail_countdown{0};
+std::atomic<long long> live{0};
+}  // namespace scf_mem
 
 extern "C" int scf_ctx_device_fields(scf_ctx *ctx, const double **u, const double **v, const double **w,
                                      const double **p, const double **phil, const double **vofl, const double **vof)

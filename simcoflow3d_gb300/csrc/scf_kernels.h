@@ -161,10 +161,14 @@ void df_cg_update(const DfOp &A, float2 *x, float2 *r, const float2 *p, const fl
                   double first, Reducer &R, cudaStream_t st, int *launches, KTimer *kt = nullptr);
 void df_pupdate(const DfOp &A, const float *z, float2 *p, const double *scal, bool first, cudaStream_t st,
                 int *launches);
+// (r, z) in FP64 from the double-float r and the FP32 z; beta into the scalars
+void df_dot_rz(const DfOp &A, const float2 *r, const float *z, Reducer &R, cudaStream_t st, int *launches);
 void df_from_double(const double *src, float2 *dst, int n, cudaStream_t st, int *launches);
 void df_to_double(const float2 *src, double *dst, int n, cudaStream_t st, int *launches);
 // alpha and the mean of A p from the two-lane partials of an SpMV
 void reduce_alpha(Reducer &R, int nblocks, bool singular, cudaStream_t st, int *launches);
+// beta = (r, z) / (previous (r, z)) from one-lane partials; (r, z) kept
+void reduce_beta(Reducer &R, int nblocks, cudaStream_t st, int *launches);
 
 // CG building blocks on the fine level (FP64 vectors, ghosted layout).
 void cg_spmv_dot(const LevelView<double> &A, const double *p, double *q, Reducer &R, bool singular,

@@ -632,27 +632,55 @@ TR_HD void atomic_min_key(unsigned long long *slot, unsigned long long key)
 #endif
 }
 
-// One interface cell's band (1726-1861): every full or empty cell within
-// BAND cells in each index is marked and keeps the least distance seen.
-// dis holds the distances from the cell centres.
+constexpr int BAND_SPAN = 2 * BAND + 1;
+constexpr int BAND_CELLS = BAND_SPAN * BAND_SPAN * BAND_SPAN;   // 729 offsets
+
+// Offset t (0 .. BAND_CELLS-1) of an interface cell's band, ii fastest.
+TR_HD void band_offset(int t, int &ii, int &jj, int &kk)
+{
+    ii = t % BAND_SPAN - BAND;
+    jj = (t / BAND_SPAN) % BAND_SPAN - BAND;
+    kk = t / (BAND_SPAN * BAND_SPAN) - BAND;
+}
+
+// Interior cell of index c (i fastest), the inverse of Dims::n, in 32-bit
+// arithmetic (the transport context holds fewer than 2^32 interior cells).
+TR_HD void cell_of(const Dims &D, uint32_t c, int &i, int &j, int &k)
+{
+    const uint32_t r = c / (uint32_t)D.I;
+    i = (int)(c - r * (uint32_t)D.I) + 1;
+    const uint32_t kq = r / (uint32_t)D.J;
+    j = (int)(r - kq * (uint32_t)D.J) + 1;
+    k = (int)kq + 1;
+}
+
+// One pair of the band (1726-1861): the interface cell (i, j, k) and its
+// offset t.  A full or empty target cell within BAND cells in each index is
+// marked and keeps the least distance seen; dis holds the distances from
+// the cell centres.  The minimum does not depend on the order of the pairs.
+TR_HD void band_pair(const Dims &D, const Geo &G, const double *vfl, const double *phi, const double *nx,
+                     const double *ny, const double *nz, const double *dis, int i, int j, int k, int t,
+                     unsigned long long *key, uint8_t *fix)
+{
+    int ii, jj, kk;
+    band_offset(t, ii, jj, kk);
+    const int ti = i + ii, tj = j + jj, tk = k + kk;
+    if (!(1 <= ti && ti <= D.I && 1 <= tj && tj <= D.J && 1 <= tk && tk <= D.K)) return;
+    const size_t tg = D.g(ti, tj, tk), tc = D.n(ti, tj, tk);
+    if (!band_target(vfl[tg])) return;
+    const size_t g = D.g(i, j, k), c = D.n(i, j, k);
+    fix[tc] = 1;
+    const double deuc = band_distance(nx[g], ny[g], nz[g], dis[g], ii, jj, kk, G.dx[c], G.dy[c], G.dz[c], phi[tg]);
+    atomic_min_key(key + tc, key_of(deuc));
+}
+
+// One interface cell's whole band, pair by pair.
 TR_HD void band_scatter(const Dims &D, const Geo &G, const double *vfl, const double *phi, const double *nx,
                         const double *ny, const double *nz, const double *dis, int i, int j, int k,
                         unsigned long long *key, uint8_t *fix)
 {
-    const size_t g = D.g(i, j, k), c = D.n(i, j, k);
-    if (!band_interface(vfl[g])) return;
-    for (int ii = -BAND; ii <= BAND; ++ii)
-        for (int jj = -BAND; jj <= BAND; ++jj)
-            for (int kk = -BAND; kk <= BAND; ++kk) {
-                const int ti = i + ii, tj = j + jj, tk = k + kk;
-                if (!(1 <= ti && ti <= D.I && 1 <= tj && tj <= D.J && 1 <= tk && tk <= D.K)) continue;
-                const size_t tg = D.g(ti, tj, tk), tc = D.n(ti, tj, tk);
-                if (!band_target(vfl[tg])) continue;
-                fix[tc] = 1;
-                const double deuc = band_distance(nx[g], ny[g], nz[g], dis[g], ii, jj, kk, G.dx[c], G.dy[c], G.dz[c],
-                                                  phi[tg]);
-                atomic_min_key(key + tc, key_of(deuc));
-            }
+    if (!band_interface(vfl[D.g(i, j, k)])) return;
+    for (int t = 0; t < BAND_CELLS; ++t) band_pair(D, G, vfl, phi, nx, ny, nz, dis, i, j, k, t, key, fix);
 }
 
 // The level set each cell ends with (1866-1882).

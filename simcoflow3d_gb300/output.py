@@ -28,13 +28,14 @@ def write_vtr(path: str, shape: Tuple[int, int, int], axes: Sequence[np.ndarray]
     L = lib or load_library()
     I, J, K = shape
     ax = [np.ascontiguousarray(a, dtype=np.float64) for a in axes]
-    assert [a.size for a in ax] == [I, I, J, J, K, K]
+    capi.require([a.size for a in ax] == [I, I, J, J, K, K], "axes must hold I, I, J, J, K, K values")
     fl = list(fields)
     arr = (capi.ScfVtrField * max(1, len(fl)))()
     keep = []
     for q, (name, data) in enumerate(fl):
         if isinstance(data, np.ndarray):
-            assert data.dtype == np.float64 and data.flags.f_contiguous and data.shape == (I + 2, J + 2, K + 2)
+            capi.require(data.dtype == np.float64 and data.flags.f_contiguous and data.shape == (I + 2, J + 2, K + 2),
+                         f"field {name}: a ghosted Fortran-ordered FP64 array of shape {(I + 2, J + 2, K + 2)} is required")
             keep.append(data)
             arr[q].data = data.ctypes.data
             arr[q].on_device = 0

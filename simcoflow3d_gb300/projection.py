@@ -182,17 +182,28 @@ class Projection:
         self._check(rc, (capi.SCF_ERR_NOT_CONVERGED,) if allow_not_converged else ())
         return pc, pp, st.as_dict()
 
-    def update_puvw(self, w, tvar=None, want_bc: bool = True, allow_not_converged: bool = False, pred=None):
+    def update_puvw(self, w, tvar=None, want_bc: bool = True, allow_not_converged: bool = False, pred=None,
+                    bc_out=None):
         """UpdatePUVW's projection: returns (u, v, w, p, bcvar[4][6] or None, stats).
         ``tvar`` defaults to copies of the workload's TVar arrays; ``pred``
-        optionally replaces the workload's (u*, v*, w*)."""
+        optionally replaces the workload's (u*, v*, w*); ``bc_out``
+        optionally gives the 4 x 6 BC Var planes to write (else new arrays)."""
         a = w.arrays
         if tvar is None:
             tvar = [a[k].copy(order="F") for k in ("tvar_u", "tvar_v", "tvar_w", "tvar_p")]
         u, v, ww, p = tvar
         pin = capi.poisson_in(w, pred)
         cin = capi.correct_in(w)
-        bc_struct, bc = (capi.new_bc_out(*self.shape) if want_bc else (None, None))
+        if want_bc and bc_out is not None:
+            bc = bc_out
+            bc_struct = capi.ScfBcOut()
+            shapes = capi.bc_plane_shapes(*self.shape)
+            for f in range(4):
+                for q in range(6):
+                    capi.require_shape(bc[f][q], shapes[q], "BC plane")
+                    bc_struct.var[f][q] = capi.dptr(bc[f][q])
+        else:
+            bc_struct, bc = (capi.new_bc_out(*self.shape) if want_bc else (None, None))
         st = capi.ScfStats()
         rc = self.L.scf_update_puvw(self.ctx, C.byref(pin), C.byref(cin), capi.dptr(u), capi.dptr(v),
                                     capi.dptr(ww), capi.dptr(p), C.byref(bc_struct) if want_bc else None,

@@ -63,11 +63,11 @@ class ClsvofScheme:
         I, J, K = self.shape
         arrs = [_f64(a) for a in (*centres, *spacings, *vel, *fluid_normals, *bc_vel)]
         for a in arrs[:6]:
-            assert a.shape == (I, J, K)
+            capi.require_shape(a, (I, J, K))
         for a in arrs[6:12]:
-            assert a.shape == (I + 2, J + 2, K + 2)
+            capi.require_shape(a, (I + 2, J + 2, K + 2))
         for a, sh in zip(arrs[12:], ((J, K), (I, K), (I, J))):
-            assert a.shape == sh
+            capi.require_shape(a, sh)
         s = capi.ScfClsvofIn(*(capi.dptr(a) for a in arrs))
         s.lvs_flag[:] = list(lvs_flag)
         s.vof_flag[:] = list(vof_flag)
@@ -81,10 +81,10 @@ class ClsvofScheme:
         I, J, K = self.shape
         fields = [_f64(state[k]) for k in ("vofl", "phil", "nxl", "nyl", "nzl")]
         for a in fields:
-            assert a.shape == (I + 2, J + 2, K + 2)
+            capi.require_shape(a, (I + 2, J + 2, K + 2))
         planes = [_f64(a) for a in (*lvs_bc, *vof_bc)]
         for a, sh in zip(planes, plane_shapes(I, J, K) * 2):
-            assert a.shape == sh
+            capi.require_shape(a, sh)
         s = capi.ScfClsvofState(*(capi.dptr(a) for a in fields))
         s.lvs_bc[:] = [capi.dptr(a) for a in planes[:6]]
         s.vof_bc[:] = [capi.dptr(a) for a in planes[6:]]
@@ -155,9 +155,9 @@ class ClsvofScheme:
             g = [_f64(a) for a in vgrids[f]]
             c = [_f64(vcells[f][k]) for k in ("phil", "nxl", "nyl", "nzl", "vofl")]
             for a in g:
-                assert a.shape == (I, J, K)
+                capi.require_shape(a, (I, J, K))
             for a in c:
-                assert a.shape == (I + 2, J + 2, K + 2)
+                capi.require_shape(a, (I + 2, J + 2, K + 2))
             keep += g + c
             cells[f] = capi.ScfClsvofVcell(*(capi.dptr(a) for a in g + c))
         st = capi.ScfClsvofStats()

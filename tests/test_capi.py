@@ -199,3 +199,20 @@ int main(void) {
             assert C.sizeof(m[t]) == int(v), (t, v)
         else:
             assert getattr(m[t], f).offset == int(v), (t, f, v)
+
+
+def test_noalloc_size_guard_rejects_huge_grids_before_any_launch(lib_path):
+    """The allocation-free apply checks the ghosted size in 64-bit arithmetic:
+    I + 2 near INT32_MAX must not wrap to a small or negative count.  The guard
+    returns SCF_ERR_BAD_ARG before any CUDA call, so this runs without a GPU."""
+    from simcoflow3d_gb300 import capi
+    lib = C.CDLL(lib_path)
+    f = lib.scf_apply_operator_noalloc
+    f.argtypes = [C.c_int32, C.c_int32, C.c_int32] + [C.c_void_p] * 8
+    f.restype = C.c_int
+    dummy = C.c_void_p(16)   # never dereferenced: the size guard comes first
+    big = 2 ** 31 - 1
+    for dims in ((big, 1, 1), (1, big, 1), (1, 1, big), (big, big, big), (2 ** 20, 2 ** 20, 2 ** 20)):
+        rc = f(*dims, dummy, dummy, dummy, dummy, dummy, dummy, None, None)
+        assert rc == capi.SCF_ERR_BAD_ARG, dims
+    assert f(0, 4, 4, dummy, dummy, dummy, dummy, dummy, dummy, None, None) == capi.SCF_ERR_BAD_ARG

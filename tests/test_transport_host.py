@@ -313,6 +313,39 @@ def test_front_end_marshals_like_the_oracle(host_lib):
     sch.close()
 
 
+def test_front_end_rejects_wrong_shapes_before_the_c_side(host_lib):
+    """A wrongly sized array raises ValueError (also under ``python -O``)
+    before any pointer reaches the library, for the step's inputs, its state
+    and the velocity-cell fields."""
+    from simcoflow3d_gb300.transport import ClsvofScheme
+    centres, spacings, state, vel, fn, bc_vel, lvs_bc, dt, flags, vflags = _case("shear")
+    I, J, K = spacings[0].shape
+    calls = []
+
+    class Spy(_HostLib):
+        def __getattribute__(self, name):
+            if name in ("scf_clsvof_step", "scf_clsvof_stage", "scf_clsvof_uvw_liquid_field"):
+                calls.append(name)
+            return object.__getattribute__(self, name)
+
+    sch = ClsvofScheme(I, J, K, lib=Spy(host_lib))
+    short = np.asfortranarray(spacings[0][:-1])
+    with pytest.raises(ValueError):
+        sch(centres, (short, spacings[1], spacings[2]), *_copy(state, lvs_bc)[:1], vel, fn, bc_vel,
+            _copy(state, lvs_bc)[1], dt)
+    s_bad, p_bad = _copy(state, lvs_bc)
+    s_bad["phil"] = np.asfortranarray(s_bad["phil"][:, :, :-1])
+    with pytest.raises(ValueError):
+        sch(centres, spacings, s_bad, vel, fn, bc_vel, p_bad, dt)
+    vgrids = [tuple(spacings) for _ in range(3)]
+    vcells = [{k: np.zeros((I + 1, J + 2, K + 2), order="F") for k in ("phil", "nxl", "nyl", "nzl", "vofl")}
+              for _ in range(3)]
+    with pytest.raises(ValueError):
+        sch.uvw_liquid_field(vgrids, vcells)
+    assert not calls, calls
+    sch.close()
+
+
 _SANITIZED_RUN = r"""
 import sys, ctypes as C
 sys.path[:0] = [sys.argv[2], sys.argv[3]]

@@ -109,14 +109,21 @@ extern "C" int host_clsvof_step(int I, int J, int K, const double *const geo[6],
         for (int axis = 0; axis < 3; ++axis)   // k_walls
             for (size_t t = 0; t < D.plane_size(axis); ++t) tr::wall_point(D, G, W, axis, t);
         reconstruct(0, true);
-        for (size_t t = 0; t < nin; ++t) {   // k_band_reset
-            key[t] = (unsigned long long)tr::key_of(1.0e4);
-            fix[t] = 0;
-        }
-        cells([&](int i, int j, int k) {   // k_band_scatter
-            tr::band_scatter(D, G, vf[0].data(), ls[0].data(), nx.data(), ny.data(), nz.data(), dis.data(), i, j, k,
-                             key.data(), fix.data());
+        std::vector<uint32_t> list;
+        cells([&](int i, int j, int k) {   // k_band_reset: reset, list the interface cells
+            const size_t c = D.n(i, j, k);
+            key[c] = (unsigned long long)tr::key_of(1.0e4);
+            fix[c] = 0;
+            if (tr::band_interface(vf[0][D.g(i, j, k)])) list.push_back((uint32_t)c);
         });
+        for (size_t q = list.size(); q-- > 0;) {   // k_band_pairs (any order of cells and pairs)
+            int i, j, k;
+            tr::cell_of(D, list[q], i, j, k);
+            TR_CHECK(D.n(i, j, k) == list[q], "cell_of");
+            for (int t = tr::BAND_CELLS; t-- > 0;)
+                tr::band_pair(D, G, vf[0].data(), ls[0].data(), nx.data(), ny.data(), nz.data(), dis.data(), i, j, k,
+                              t, key.data(), fix.data());
+        }
         cells([&](int i, int j, int k) {   // k_band_value
             ls[0][D.g(i, j, k)] = tr::band_value(D, G, vf[0].data(), dis.data(), i, j, k, key.data(), fix.data());
         });
