@@ -11,7 +11,7 @@ rebuilds:
 - ``vtr.py``: the VTK RectilinearGrid writer;
 - ``clsvof.c``: the CLSVOF interface transport: Clsvof_Scheme with its
   directional sweeps, Interface_Reconstruct, BoundaryConditionLvsVof and
-  Redistance_Levelset, and ComputeUVWLiquidField (no GPU counterpart yet).
+  Redistance_Levelset, and ComputeUVWLiquidField.
 
 Only the tests, ``__graft_entry__.smoke()`` and the CPU-baseline legs of
 ``bench.py`` use it, and only as the checker or the timed CPU path.
@@ -263,6 +263,32 @@ def project(w, solver="gmg", rel_tol=1e-13, precision=0, north_mass_fix=0, **kw)
     u, v, ww, p, bcv, rc = correct(w, pc, pp, north_mass_fix=north_mass_fix)
     return {"pocoef": pc, "A": A, "b": b, "x": x, "stats": st, "pp": pp, "u": u, "v": v, "w": ww, "p": p,
             "bcvar": bcv, "correct_rc": rc, "singular": sing}
+
+
+def pressure_error(w, pp, pp_ref, singular_: bool) -> float:
+    """Relative L2 difference of two ghosted pressures over the active
+    interior cells (Cell_Type /= 2); for an all-Neumann system, where the
+    pressure is defined up to a constant, the mean difference is removed."""
+    act = w.arrays["cell_type"] != 2
+    a = pp[1:-1, 1:-1, 1:-1][act]
+    b = pp_ref[1:-1, 1:-1, 1:-1][act]
+    d = a - b
+    if singular_:
+        d = d - d.mean()
+        b = b - b.mean()
+    nb = float(np.linalg.norm(b))
+    return float(np.linalg.norm(d)) / nb if nb > 0 else float(np.linalg.norm(d))
+
+
+def velocity_error(fields, ref) -> float:
+    """Largest relative L2 difference of the corrected u, v, w (whole
+    ghosted arrays) against the reference fields."""
+    out = 0.0
+    for a, b in zip(fields, ref):
+        nb = float(np.linalg.norm(b))
+        e = float(np.linalg.norm(a - b))
+        out = max(out, e / nb if nb > 0 else e)
+    return out
 
 
 def num_threads() -> int:

@@ -3,13 +3,25 @@
 surface, Dirichlet-p top): each call gets a freshly seeded prediction and
 starts from the previous call's pressure.  Every call must reach the
 tolerance in both precisions, the warm-started pressure must match a cold
-FP64 solve of the same call, and warm starts must not cost iterations."""
+FP64 solve of the same call, warm starts must not cost iterations, and the
+first and last calls' pressure and corrected velocity must match the
+oracle's projection of the same prediction (FP64 solve to 1e-13,
+ComputePUVW.f90:179-384)."""
 import numpy as np
 import pytest
 
 from simcoflow3d_gb300 import workloads as W
+from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
+
+
+def _oracle_call(w, pred):
+    """The oracle's projection of workload ``w`` with (u*, v*, w*) = pred."""
+    wp = w.copy()
+    for key, a in zip(("u_star", "v_star", "w_star"), pred):
+        wp.arrays[key] = np.asfortranarray(a)
+    return O.project(wp, rel_tol=1e-13)
 
 
 @pytest.mark.parametrize("precision", [0, 1])
@@ -28,7 +40,14 @@ def test_warm_started_sequence_wave_tank(gpu_lib, precision):
         assert st["converged"] == 1 and st["rel_residual"] <= 1e-8
         its_warm.append(st["iterations"])
         pw = np.zeros(w.shape_g, order="F")
-        seq.fetch(pp=pw)
+        uvw = [np.zeros(w.shape_g, order="F") for _ in range(3)]
+        seq.fetch(*uvw, pp=pw)
+        if call in (0, 19):
+            ref = _oracle_call(w, pred)
+            assert ref["stats"]["csr_relres"] <= 2e-13
+            err_p = O.pressure_error(w, pw, ref["pp"], ref["singular"])
+            err_u = O.velocity_error(uvw, (ref["u"], ref["v"], ref["w"]))
+            assert err_p <= 1e-5 and err_u <= 1e-6, (call, err_p, err_u)
         cold.stage(w, pred=pred)
         sc = cold.run()
         its_cold.append(sc["iterations"])
