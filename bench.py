@@ -6,12 +6,19 @@ cut-cell sphere + gas-bubble column (density ratio 1000): GFM coefficients,
 operator and right-hand side, the multigrid-preconditioned CG solve to
 relative residual 1e-8, the pressure scatter, the velocity correction and the
 boundary conditions.  ``value`` is the device time per projection of the
-mixed solver (FP32 V-cycle, FP64 CG/residual/dots/coarsest solve) with the
-inputs resident in HBM; the same projection with the FP64 V-cycle is timed
-beside it.  ``e2e`` is the drop-in call ``scf_update_puvw`` with the
-reference's host arrays in pinned memory (host->device copy of every input
-and device->host copy of u, v, w, p and the BC planes inside the timed
-region).
+mixed solver with the inputs resident in HBM: an FP32 V-cycle (FP32 storage
+and arithmetic), CG vectors and operator in double-float (FP32 pairs, about
+48 significand bits), CG dot products formed from per-cell FP64 products and
+summed in FP64, and an FP64 true residual (iterative refinement) and FP64
+coarsest-grid solve.  The same projection with the FP64 solver (FP64 V-cycle
+and CG) is timed beside it.  ``e2e`` is the drop-in call ``scf_update_puvw``
+with the reference's host arrays in page-locked memory (host->device copy of
+every input and device->host copy of u, v, w, p and the BC planes inside the
+timed region).  After the timed regions the line adds both arms' pressure and
+velocity errors against the oracle's FP64 solve to 1e-13, and the other named
+configurations: c0 (64^3) and c1 (128^3) in FP64 to 1e-10 with their errors,
+the c3 adjoint gradient (128^3) against central differences, and the c4 wave
+tank's 20 warm-started calls in both precisions.
 
 ``--impl reference`` times the CPU path (the oracle's restatement of the
 reference path, multigrid-preconditioned CG with OpenMP on all host cores).
@@ -261,17 +268,123 @@ def time_device(proj, steps, warmup, live_kernel_timing=0):
     return ms, launches, last
 
 
-def cpu_projection_ms(w, threads: int):
+def cpu_projection_ms(w, threads: int, tol: float = 1e-8):
     """One projection on the host cores with the oracle's restatement."""
     os.environ["OMP_NUM_THREADS"] = str(threads)
     from oracle import oracle as O
     t0 = time.perf_counter()
     pc = O.pocoef(w)
     b = O.rhs(w, pc)
-    x, st = O.gmg_solve(w, pc, b, precision=0, rel_tol=1e-8, degree=3)
+    x, st = O.gmg_solve(w, pc, b, precision=0, rel_tol=tol, degree=3)
     pp = O.scatter(w, x)
     O.correct(w, pc, pp)
     return (time.perf_counter() - t0) * 1e3, st
+
+
+def projection_config(args, w, ws: int) -> dict:
+    """The ``config`` of the projection line, the same in both arms."""
+    return {
+        "workload": f"{args.config}: {w.imax}x{w.jmax}x{w.kmax} cut-cell sphere r=0.15 at (0.5,0.5,0.3) + gas "
+                    "bubble r=0.1 at (0.5,0.5,0.65) in a water column, rho ratio 1000, all-Neumann p, "
+                    f"rel res {args.tol:g}" if args.config == "c2" else f"{args.config} at {w.imax}x{w.jmax}x{w.kmax}",
+        "grid": [w.imax, w.jmax, w.kmax],
+        "rel_tol": args.tol,
+        "l2": "inputs larger than L2 (about 3.5 GB resident per projection)",
+        "parallelism": f"replicas x{ws}",
+    }
+
+
+def oracle_errors(w, ref, pp, uvw):
+    """Pressure (the solve's Pp) and corrected-velocity errors of one device
+    projection against the oracle's FP64 solve to 1e-13 (relative L2; the
+    pressure mean-aligned for all-Neumann systems)."""
+    from oracle import oracle as O
+    return {"err_p_vs_oracle": float("%.3e" % O.pressure_error(w, pp, ref["pp"], ref["singular"])),
+            "err_u_vs_oracle": float("%.3e" % O.velocity_error(uvw, (ref["u"], ref["v"], ref["w"])))}
+
+
+def fp64_config_leg(name: str, args, device: int):
+    """c0 (64^3, no solid) or c1 (128^3, with the sphere): the plain FP64
+    projection to relative residual 1e-10, device-resident (W untimed + K
+    timed), its errors against the oracle's FP64 solve to 1e-13, and the
+    oracle's CPU projection to 1e-10 at the same size on all host cores."""
+    import numpy as np
+    from simcoflow3d_gb300 import capi
+    from simcoflow3d_gb300.projection import Projection
+    from oracle import oracle as O
+    w = make_workload(name, args.seed, None)
+    proj = Projection.for_workload(w, precision=capi.SCF_PREC_FP64, rel_tol=1e-10, device=device)
+    proj.stage(w)
+    ms, launches, st = time_device(proj, args.steps, args.warmup)
+    u, v, ww, _, _, su = proj.update_puvw(w, want_bc=False)
+    p = np.zeros(w.shape_g, order="F")      # the solve's pressure Pp
+    proj.fetch(pp=p)
+    proj.close()
+    out = {"grid": [w.imax, w.jmax, w.kmax], "precision": "fp64", "rel_tol": 1e-10,
+           "ms_per_projection": round(statistics.mean(ms), 4), "iterations": st["iterations"],
+           "rel_residual": st["rel_residual"], "gpu_launches": launches}
+    threads = os.cpu_count() or 1
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    ref = O.project(w, rel_tol=1e-13)
+    out.update(oracle_errors(w, ref, p, (u, v, ww)))
+    del ref
+    cpu_ms, cpu_st = cpu_projection_ms(w, threads, tol=1e-10)
+    out["cpu_oracle"] = {"ms_per_projection": round(cpu_ms, 2), "cores": threads,
+                         "iterations": cpu_st["iterations"], "kind": "port"}
+    return out
+
+
+def adjoint_leg(args, device: int, directions: int = 32, eps: float = 1e-6):
+    """c3 (128^3, the c1 geometry, FP64): the loss J = sum over cut cells of
+    p n_z WlLh + 1/2 ||D u||^2 and its adjoint gradient with respect to u*
+    and the cell densities.  Times the forward (projection to 1e-12 + loss)
+    and the backward (one adjoint solve to 1e-10 + gradient kernels) as the
+    library's host calls, W untimed + K timed; then checks the gradient on
+    `directions` seeded random directions each for (u*, v*, w*) and for rho
+    against central finite differences with step eps.  The error is
+    relative to the directional derivatives over the set of directions."""
+    import numpy as np
+    from simcoflow3d_gb300 import workloads as W
+    from simcoflow3d_gb300.autograd import ProjectionLoss
+    from oracle import adjoint as AD
+    w = make_workload("c3", args.seed, None)
+    g = W.pressure_force_weights(w)
+    rho = AD.phase_density(w)
+    R = ProjectionLoss(w, g=g, device=device)
+    a = w.arrays
+    us, vs, ws = a["u_star"], a["v_star"], a["w_star"]
+    fwd, bwd = [], []
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        J, _, sf = R.forward(us, vs, ws, rho)
+        t1 = time.perf_counter()
+        (gu, gv, gw, grho), sb = R.backward()
+        t2 = time.perf_counter()
+        if i >= args.warmup:
+            fwd.append((t1 - t0) * 1e3)
+            bwd.append((t2 - t1) * 1e3)
+    rng = np.random.default_rng(args.seed)
+    fd_u, an_u, fd_r, an_r = [], [], [], []
+    for _ in range(directions):
+        d = [np.asfortranarray(rng.normal(size=w.shape_g)) for _ in range(3)]
+        jp = R.forward(us + eps * d[0], vs + eps * d[1], ws + eps * d[2], rho)[0]
+        jm = R.forward(us - eps * d[0], vs - eps * d[1], ws - eps * d[2], rho)[0]
+        fd_u.append((jp - jm) / (2 * eps))
+        an_u.append(float(np.sum(gu * d[0]) + np.sum(gv * d[1]) + np.sum(gw * d[2])))
+    for _ in range(directions):
+        dr = np.asfortranarray(rng.normal(size=w.shape_g) * rho)
+        jp = R.forward(us, vs, ws, rho + eps * dr)[0]
+        jm = R.forward(us, vs, ws, rho - eps * dr)[0]
+        fd_r.append((jp - jm) / (2 * eps))
+        an_r.append(float(np.sum(grho * dr)))
+    R.proj.close()
+    err = lambda fd, an: float("%.3e" % (np.linalg.norm(np.array(fd) - np.array(an)) / np.linalg.norm(an)))
+    return {"grid": [w.imax, w.jmax, w.kmax], "precision": "fp64",
+            "ms_forward": round(statistics.mean(fwd), 3), "ms_backward": round(statistics.mean(bwd), 3),
+            "forward_iterations": sf["iterations"], "adjoint_iterations": sb["iterations"],
+            "fd_directions": directions, "fd_eps": eps,
+            "grad_rel_err_u_star": err(fd_u, an_u), "grad_rel_err_rho": err(fd_r, an_r),
+            "timing": "host calls (inputs copied in, gradients copied out), W untimed + K timed"}
 
 
 def run_reference(args):
@@ -308,13 +421,18 @@ def run_reference(args):
         return 0
     threads = os.cpu_count() or 1
     os.environ["OMP_NUM_THREADS"] = str(threads)
+    # warm-up steps (untimed) run the same path on a 32^3 grid of the same
+    # configuration: the CPU port has nothing to warm but its threads and
+    # caches, and the K timed full-size steps alone take minutes
+    wsmall = make_workload(args.config, args.seed, 32)
+    for _ in range(args.warmup):
+        cpu_projection_ms(wsmall, threads, tol=args.tol)
     w = make_workload(args.config, args.seed, args.n)
     ms = []
-    for i in range(args.warmup + args.steps):
-        t, st = cpu_projection_ms(w, threads)
-        if i >= args.warmup:
-            ms.append(t)
-        if args.max_cpu_s and sum(ms) / 1e3 > args.max_cpu_s and len(ms) >= 1:
+    for i in range(args.steps):
+        t, st = cpu_projection_ms(w, threads, tol=args.tol)
+        ms.append(t)
+        if args.max_cpu_s and sum(ms) / 1e3 > args.max_cpu_s and len(ms) < args.steps:
             break
     v = statistics.mean(ms)
     line = {
@@ -322,13 +440,15 @@ def run_reference(args):
         "n_gpus": ws, "steps": len(ms), "warmup": args.warmup, "ms_per_step": round(v, 3),
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded u*, cut-cell sphere + gas bubble)",
-        "config": {"workload": f"{args.config}: 256^3 cut-cell sphere r=0.15 + gas bubble r=0.1, rho ratio 1000, "
-                               "all-Neumann p, rel res 1e-8", "grid": [w.imax, w.jmax, w.kmax]},
+        "config": projection_config(args, w, ws),
         "cpu_baseline": {"value": round(v, 3), "unit": "ms/projection", "cores": threads, "kind": "port",
                          "sample": "full projection per step (oracle restatement: coefficients, rhs, "
-                                   "FP64 MG-PCG to 1e-8, scatter, correction)"},
+                                   "FP64 MG-PCG to %g, scatter, correction); warm-ups on a 32^3 grid" % args.tol},
         "e2e": {"value": round(v, 3), "unit": "ms/projection", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "iterations": st.get("iterations"),
+        "steps_requested": args.steps,
+        "max_cpu_s": args.max_cpu_s,
+        "capped": len(ms) < args.steps,
     }
     print(json.dumps(line), flush=True)
     barrier(dist)
@@ -395,9 +515,14 @@ def run_ours(args):
     achieved = k_bytes / (k_ms * 1e-3) / 1e9
     trf = smoother_traffic(w.imax * w.jmax * w.kmax)
 
+    # the FP64 arm's fields of one drop-in call and its pressure Pp, for its
+    # errors against the oracle (computed after every timed region)
+    u64, v64, w64, _, _, _ = results["fp64"]["proj"].update_puvw(w, want_bc=False)
+    p64 = np.zeros(w.shape_g, order="F")
+    results["fp64"]["proj"].fetch(pp=p64)
+    results["fp64"]["proj"].close()     # only the mixed context stays on the device
     # end to end through the drop-in call: every input and output array in
     # page-locked host memory allocated once, outside the timed region
-    results["fp64"]["proj"].close()     # only the mixed context stays on the device
     unpin(lib, pinned)
     pinned = []
     wh = pinned_workload(w)
@@ -427,6 +552,10 @@ def run_ours(args):
             e2e_stats = st
     gc.enable()
     e2e_total = allreduce_max(dist, sum(e2e_ms))
+    mixed_out = [x.copy(order="F") for x in (u, v, ww)] + [np.zeros(w.shape_g, order="F")]
+    mixed.fetch(pp=mixed_out[3])
+    mixed.close()
+    del wh, tv, bc
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -435,6 +564,29 @@ def run_ours(args):
         cpu = {"value": round(cpu_ms, 3), "unit": "ms/projection", "cores": threads, "kind": "port",
                "sample": "one full 256^3 projection (oracle restatement: coefficients, rhs, FP64 MG-PCG to "
                          f"1e-8 in {cpu_st['iterations']} iterations, scatter, correction), OpenMP"}
+
+    # errors of both arms against the oracle's FP64 solve to 1e-13, and the
+    # other named configurations (c0, c1 in FP64; the c3 adjoint; the c4
+    # warm-started sequence in both precisions): all after the timed regions
+    errors, configs = {}, {}
+    if rank == 0 and ws == 1 and not args.no_oracle:
+        from oracle import oracle as O
+        os.environ["OMP_NUM_THREADS"] = str(os.cpu_count() or 1)
+        ref = O.project(w, rel_tol=1e-13)
+        errors["mixed"] = oracle_errors(w, ref, mixed_out[3], mixed_out[:3])
+        errors["fp64"] = oracle_errors(w, ref, p64, (u64, v64, w64))
+        errors["oracle"] = {"rel_tol": 1e-13, "iterations": ref["stats"]["iterations"],
+                            "residual_in_reference_matrix": ref["stats"]["csr_relres"]}
+        del ref
+    del mixed_out, u64, v64, w64, p64
+    if rank == 0 and ws == 1 and not args.no_configs and args.config == "c2" and args.n is None:
+        for name in ("c0", "c1"):
+            configs[name] = fp64_config_leg(name, args, local)
+        configs["c3_adjoint"] = adjoint_leg(args, local)
+        w4 = make_workload("c4", args.seed, None)
+        configs["c4_sequence"] = {"grid": [w4.imax, w4.jmax, w4.kmax], "rel_tol": args.tol,
+                                  "arms": sequence_arms(w4, 20, args.tol, args.seed, device=local)}
+        del w4
 
     if rank != 0:
         barrier(dist)
@@ -454,20 +606,14 @@ def run_ours(args):
         "higher_is_better": False,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32 V-cycle / f64 CG",
+        "dtype": "f32 V-cycle, double-float CG vectors, f64 CG dots / true residual / coarsest solve",
         "data": "synthetic (seeded u*, cut-cell sphere + gas bubble)",
-        "config": {
-            "workload": f"{args.config}: 256^3 cut-cell sphere r=0.15 at (0.5,0.5,0.3) + gas bubble r=0.1 at "
-                        "(0.5,0.5,0.65) in a water column, rho ratio 1000, all-Neumann p, rel res 1e-8",
-            "grid": [w.imax, w.jmax, w.kmax],
-            "rel_tol": args.tol,
-            "l2": "inputs larger than L2 (about 3.5 GB resident per projection)",
-            "parallelism": f"replicas x{ws}",
-        },
+        "config": projection_config(args, w, ws),
         "fp64": {"ms_per_projection": round(fp64, 4), "iterations": s64["iterations"],
                  "smoother_degree": degree["fp64"],
-                 "rel_residual": s64["rel_residual"]},
+                 "rel_residual": s64["rel_residual"], **errors.get("fp64", {})},
         "mixed": {"iterations": smx["iterations"], "rel_residual": smx["rel_residual"],
+                  **errors.get("mixed", {}),
                   "smoother_degree": degree["mixed"],
                   "ms_steps": [round(x, 3) for x in results["mixed"]["ms"]],
                   "ms_assemble": round(smx["ms_assemble"], 3), "ms_solve": round(smx["ms_solve"], 3),
@@ -497,6 +643,8 @@ def run_ours(args):
                      "traffic": round(trf["bytes"]) if trf else None,
                      "traffic_note": trf["note"] if trf else None},
         "kernels_live": live,
+        "oracle_solve": errors.get("oracle"),
+        "configs": configs or None,
         "clocks": clocks,
         "gpu_launches": results["mixed"]["launches"],
         "cpu_baseline": cpu,
@@ -506,34 +654,44 @@ def run_ours(args):
     return 0
 
 
-def run_sequence(args):
-    """A sequence of warm-started projections on a fixed geometry (default:
-    the 512x256x256 wave tank): each call gets a freshly seeded prediction,
-    staged outside the timed region, and starts from the previous call's
-    pressure.  Prints one JSON line per precision."""
+def sequence_arms(w, calls: int, tol: float, seed: int, device: int = 0):
+    """A sequence of warm-started projections on a fixed geometry: each call
+    gets a freshly seeded prediction, staged outside the timed region, and
+    starts from the previous call's pressure (call 0 cold).  Both precisions,
+    each at its fastest Chebyshev degree on the z-stretched wave tank (sweep
+    3-8): 8 for the FP32 line-block V-cycle, 6 for the FP64 one.  The first
+    pass over the calls warms the context up; the second is timed."""
     from simcoflow3d_gb300 import capi, workloads as W
     from simcoflow3d_gb300.projection import Projection
-    w = make_workload(args.config, args.seed, args.n)
-    preds = W.PredictionSequence(w, seed=args.seed + 1)
-    # each arm at its fastest Chebyshev degree on the z-stretched wave tank
-    # (sweep 3-8): 8 for the FP32 line-block V-cycle, 6 for the FP64 one
+    preds = W.PredictionSequence(w, seed=seed + 1)
     degree = {"mixed": 8, "fp64": 6}
+    out = []
     for name, prec in (("mixed", capi.SCF_PREC_MIXED), ("fp64", capi.SCF_PREC_FP64)):
-        proj = Projection.for_workload(w, precision=prec, rel_tol=args.tol, smoother_degree=degree[name])
-        for timed in (False, True):     # the first pass warms the context up
-            ms, its = [], []
-            for c in range(args.sequence):
-                proj.set_opts(warm_start=0 if c == 0 else 1)   # call 0 starts cold
+        proj = Projection.for_workload(w, precision=prec, rel_tol=tol, smoother_degree=degree[name], device=device)
+        for timed in (False, True):
+            ms, its, res = [], [], []
+            for c in range(calls):
+                proj.set_opts(warm_start=0 if c == 0 else 1)
                 proj.stage(w, pred=preds(c))
                 st = proj.run()
                 ms.append(st["ms_total"])
                 its.append(st["iterations"])
-        print(json.dumps({"sequence": args.config, "precision": name, "smoother_degree": degree[name],
-                          "grid": [w.imax, w.jmax, w.kmax],
-                          "calls": len(ms), "ms_per_call": round(statistics.mean(ms), 3),
-                          "ms_min": round(min(ms), 3), "ms_max": round(max(ms), 3),
-                          "iterations": its, "rel_tol": args.tol, "bcp_flag": list(w.bcp_flag)}), flush=True)
+                res.append(st["rel_residual"])
+        out.append({"precision": name, "smoother_degree": degree[name], "calls": len(ms),
+                    "ms_per_call": round(statistics.mean(ms), 3), "ms_min": round(min(ms), 3),
+                    "ms_max": round(max(ms), 3), "iterations": its, "max_rel_residual": max(res)})
         proj.close()
+    return out
+
+
+def run_sequence(args):
+    """The warm-started sequence (default: the 512x256x256 wave tank); one
+    JSON line per precision."""
+    w = make_workload(args.config, args.seed, args.n)
+    for arm in sequence_arms(w, args.sequence, args.tol, args.seed):
+        arm.update({"sequence": args.config, "grid": [w.imax, w.jmax, w.kmax], "rel_tol": args.tol,
+                    "bcp_flag": list(w.bcp_flag)})
+        print(json.dumps(arm), flush=True)
     return 0
 
 
@@ -968,9 +1126,14 @@ def main():
     ap.add_argument("--only", choices=["mixed", "fp64"], default=None,
                     help="time one precision device-resident only (profiling captures)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-oracle", action="store_true",
+                    help="skip the errors against the oracle's FP64 solve (c2 line)")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the c0, c1, c3 and c4-sequence legs of the default line")
     ap.add_argument("--pred-geometry", choices=["c2", "c4"], default="c2",
                     help="geometry of --config predictor (c4: the z-stretched wave tank, 512x256x256)")
-    ap.add_argument("--max-cpu-s", type=float, default=150.0, help="stop the reference arm after this many s")
+    ap.add_argument("--max-cpu-s", type=float, default=330.0,
+                    help="stop the reference arm's timed steps after this many s (recorded in its line)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -97,19 +97,23 @@ Launch3 df_launch(const DfOp &A)
     return l;
 }
 
-// q = A p, and the block partials of (p, q) and of the sum of q, both FP64
+// q = A p, and the block partials of (p, q) (FP64 products and sums) and of
+// the sum of q (for the mean of A p in all-Neumann systems, which is zero in
+// exact arithmetic: double-float per thread, FP64 across threads)
 __global__ void __launch_bounds__(128) k_spmv_df(DfOp A, const float2 *__restrict__ p, float2 *__restrict__ q,
                                                  double *__restrict__ part, int n0)
 {
     DF_ZCHUNK(A);
-    double v = 0.0, sq = 0.0;
+    double v = 0.0;
+    float2 sq = make_float2(0.f, 0.f);
     if (in) {
         const int sy = A.hi.sy, sz = A.hi.sz;
         int c = i + sy * j + sz * k0;
         float2 xm = ld(p, c - sz), x0 = ld(p, c), tb = cf(A.hi.cT, A.tlo, c - sz);
         // the six neighbour products are summed as a tree (short dependency
         // chains: the kernel is latency-bound, not memory-bound, otherwise)
-        double v2 = 0.0, sq2 = 0.0;
+        double v2 = 0.0;
+        float2 sq2 = make_float2(0.f, 0.f);
         int par = 0;
 #pragma unroll 2
         for (int k = k0; k <= k1; ++k, c += sz) {
@@ -122,18 +126,17 @@ __global__ void __launch_bounds__(128) k_spmv_df(DfOp A, const float2 *__restric
             const float2 s = dadd(dadd(sx, syy), sz2);
             const float2 y = dadd(dmul(cf(A.hi.diag, A.dlo, c), x0), dneg(s));
             q[c] = y;
-            const double yd = dwide(y);
-            if (par) { v2 = fma(dwide(x0), yd, v2); sq2 += yd; }
-            else { v = fma(dwide(x0), yd, v); sq += yd; }
+            if (par) { v2 = fma(dwide(x0), dwide(y), v2); sq2 = dadd(sq2, y); }
+            else { v = fma(dwide(x0), dwide(y), v); sq = dadd(sq, y); }
             par ^= 1;
             xm = x0; x0 = xp; tb = tt;
         }
         v += v2;
-        sq += sq2;
+        sq = dadd(sq, sq2);
     }
     double dv = block_sum(v);
     __syncthreads();
-    double ds = block_sum(sq);
+    double ds = block_sum(dto(sq));
     if (thread_linear() == 0) {
         part[block_linear()] = dv;
         part[n0 + block_linear()] = ds;
