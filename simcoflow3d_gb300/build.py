@@ -35,6 +35,7 @@ UNITS = {
     "k_bicgstab.cu": [],
     "pred_api.cu": [],
     "k_transport.cu": ["-fmad=false"],
+    "scf_stage.cu": [],
 }
 
 

@@ -12,6 +12,7 @@
 #include "../../include/scf_projection.h"
 #include "geo_kernels.h"
 #include "scf_devmem.h"
+#include "scf_stage.h"
 
 struct scf_geo_ctx {
     Dims d;
@@ -225,7 +226,7 @@ int scf_geo_stage(scf_geo_ctx *ctx, const scf_geo_cells *p, const scf_geo_cells 
         std::vector<void *> hout;
         host_ptrs(fams[f], ctx->has_moex[f], hin, hout);
         for (size_t q = 0; q < din.size(); ++q)
-            GK(cudaMemcpyAsync(din[q].dev, hin[q], din[q].bytes, cudaMemcpyHostToDevice, ctx->st));
+            GK(stage_h2d(din[q].dev, hin[q], din[q].bytes, ctx->st, 0, nullptr, nullptr));
     }
     GK(cudaStreamSynchronize(ctx->st));
     ctx->staged = true;

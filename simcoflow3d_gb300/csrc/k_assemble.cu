@@ -394,59 +394,6 @@ __device__ __noinline__ double vof_term(double vf, double vo, double dx, double 
 {
     return (vf - vo) * dx * dy * dz / dt;
 }
-// d - (double)hi rounded to FP32, where hi is d rounded to FP32: the lo part
-// of the double-float form of d.  Computed on the integer pipe (the
-// significands of d and hi aligned to d's exponent differ by less than
-// 2^29 units of d's last place); FP64 arithmetic is this GPU's scarcest
-// resource and this kernel is bound by it.  Zeros give +0; subnormals and
-// non-finite values take the FP64 route.
-__device__ __forceinline__ float lo_part(double d, float hi)
-{
-    const long long db = __double_as_longlong(d);
-    if (((unsigned long long)db << 1) == 0) return 0.0f;   // d - (double)hi = +0 for d = +-0
-    const int ed = (int)((db >> 52) & 0x7ff);
-    const int hb = __float_as_int(hi);
-    const int eh8 = (hb >> 23) & 0xff;
-    if (ed != 0 && ed != 0x7ff && eh8 != 0 && eh8 != 0xff) {
-        const long long md = (db & 0xfffffffffffffLL) | (1LL << 52);
-        const long long mh = (long long)((hb & 0x7fffff) | 0x800000) << 29;
-        const int eh = eh8 - 127 + 1023;
-        long long diff;
-        bool ok = true;
-        if (eh == ed) diff = md - mh;
-        else if (eh == ed + 1) diff = md - (mh << 1);
-        else { diff = 0; ok = false; }
-        if (ok && diff > -(1LL << 30) && diff < (1LL << 30)) {
-            if (diff == 0) return 0.0f;
-            if (db < 0) diff = -diff;
-            const int fb = __float_as_int(__int2float_rn((int)diff));
-            const int ef = ((fb >> 23) & 0xff) + (ed - 1075);
-            if (ef >= 1 && ef <= 254) return __int_as_float((fb & ~(0xff << 23)) | (ef << 23));
-        }
-    }
-    return (float)(d - (double)hi);
-}
-
-// d rounded to FP32 (round to nearest even) on the integer pipe, for results
-// in FP32's normal range, and of zeros; the rest (subnormal or out-of-range
-// results, non-finite values) take the conversion instruction, which runs on
-// the FP64 pipe.
-__device__ __forceinline__ float to_f32(double d)
-{
-    const unsigned long long b = bits(d);
-    const int e = (int)((b >> 52) & 0x7ff);
-    if ((b << 1) == 0) return __uint_as_float((unsigned)(b >> 32));   // +-0
-    if (e >= 1023 - 126 && e <= 1023 + 127) {
-        const unsigned long long m = b & 0xfffffffffffffull;
-        const unsigned hi = (unsigned)(m >> 29), rem = (unsigned)(m & 0x1fffffffu);
-        unsigned r = ((unsigned)(e - 1023 + 127) << 23) | hi;
-        if (rem > 0x10000000u || (rem == 0x10000000u && (hi & 1u))) r += 1u;   // a carry rounds into the exponent
-        r |= (unsigned)(b >> 32) & 0x80000000u;
-        return __uint_as_float(r);
-    }
-    return (float)d;
-}
-
 // a*u with a == 1.0 short-cut (exact: 1.0*u == u)
 __device__ __forceinline__ double amul(double ar, double u)
 {
@@ -565,7 +512,7 @@ __global__ void __launch_bounds__(OP_THREADS) k_operator(AsmArgs a, OpArgs o)
             bits(t5) != rt[4] || bits(t6) != rt[5]) {
             dg = row_diag(t1, t2, t3, t4, t5, t6, nb);
             if (!MIXED) dinv = recip_slow(dg);
-            if (MIXED) d32 = to_f32(dg);
+            if (MIXED) d32 = scf_to_f32(dg);
             rnb = nb;
             rt[0] = bits(t1); rt[1] = bits(t2); rt[2] = bits(t3); rt[3] = bits(t4); rt[4] = bits(t5); rt[5] = bits(t6);
         }
@@ -624,13 +571,13 @@ __global__ void __launch_bounds__(OP_THREADS) k_operator(AsmArgs a, OpArgs o)
         o.active[g] = 1;
         if (MIXED) {
             o.diag32[g] = d32;
-            o.diag_lo[g] = lo_part(dg, d32);
-            const float e32 = to_f32(cE), n32 = to_f32(cN), t32 = to_f32(cT);
+            o.diag_lo[g] = scf_lo_part(dg, d32);
+            const float e32 = scf_to_f32(cE), n32 = scf_to_f32(cN), t32 = scf_to_f32(cT);
             o.cE32[g] = e32; o.cN32[g] = n32; o.cT32[g] = t32;
-            o.cE_lo[g] = lo_part(cE, e32);
-            o.cN_lo[g] = lo_part(cN, n32);
-            o.cT_lo[g] = lo_part(cT, t32);
-            o.extra32[g] = to_f32(ex);
+            o.cE_lo[g] = scf_lo_part(cE, e32);
+            o.cN_lo[g] = scf_lo_part(cN, n32);
+            o.cT_lo[g] = scf_lo_part(cT, t32);
+            o.extra32[g] = scf_to_f32(ex);
         }
     }
 }

@@ -50,10 +50,12 @@ __device__ __forceinline__ float2 dmul(float2 x, float2 y)
     e = __fmaf_rn(x.y, y.x, e);
     return quick_two_sum(p, e);
 }
+// the double-float form of d: hi = d rounded to FP32, lo = d - hi rounded
+// to FP32, both on the integer pipe (scf_common.cuh)
 __device__ __forceinline__ float2 dfrom(double d)
 {
-    const float hi = __double2float_rn(d);
-    return make_float2(hi, __double2float_rn(d - (double)hi));
+    const float hi = scf_to_f32(d);
+    return make_float2(hi, scf_lo_part(d, hi));
 }
 __device__ __forceinline__ double dto(float2 x) { return (double)x.x + (double)x.y; }
 
@@ -213,11 +215,21 @@ __global__ void k_df_from_double(const double *src, float2 *dst, int n)
         dst[e] = dfrom(d);
     }
 }
+// the residual at the start of a CG round: its double-float form in place
+// and its FP32 copy (the hi part) for the V-cycle, in one pass
+__global__ void k_df_round_start(double *r, float *rlow, int n)
+{
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+        const float2 v = dfrom(r[e]);
+        ((float2 *)r)[e] = v;
+        rlow[e] = v.x;
+    }
+}
 __global__ void k_df_to_double(const float2 *src, double *dst, int n)
 {
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
         const float2 v = src[e];
-        dst[e] = dto(v);
+        dst[e] = dwide(v);
     }
 }
 
@@ -262,6 +274,12 @@ void df_pupdate(const DfOp &A, const float *z, float2 *p, const double *scal, bo
 void df_from_double(const double *src, float2 *dst, int n, cudaStream_t st, int *launches)
 {
     k_df_from_double<<<152 * 8, 256, 0, st>>>(src, dst, n);
+    *launches += 1;
+}
+
+void df_round_start(double *r, float *rlow, int n, cudaStream_t st, int *launches)
+{
+    k_df_round_start<<<152 * 8, 256, 0, st>>>(r, rlow, n);
     *launches += 1;
 }
 

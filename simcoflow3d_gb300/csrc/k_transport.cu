@@ -8,10 +8,12 @@
 //   k_walls                        the wall planes and ghosts;
 //   k_reconstruct (tail)           normals, liquid normals, centre distances;
 //   k_band_reset, k_band_pairs,    the redistancing: the reset lists the
-//   k_band_value                   interface cells; then one block per
-//                                  listed cell computes its 9^3 band pairs,
-//                                  one pair per thread, and sends each
-//                                  distance with a 64-bit atomicMin
+//   k_band_far, k_band_value       interface cells; then one block per
+//                                  listed cell takes its 9^3 band pairs,
+//                                  one pair per thread, settling the short
+//                                  cases and queueing the long one for
+//                                  k_band_far (full warps); each distance
+//                                  goes out with a 64-bit atomicMin
 //                                  (non-negative doubles order like their
 //                                  bits), so the result is the reference's
 //                                  running minimum whatever the order.
@@ -32,6 +34,7 @@
 #include "../../include/scf_clsvof.h"
 #include "transport_body.cuh"
 #include "scf_devmem.h"
+#include "scf_stage.h"
 
 using tr::Dims;
 using tr::Geo;
@@ -53,7 +56,9 @@ struct scf_clsvof_ctx {
     unsigned long long *key = nullptr;
     uint8_t *fix = nullptr;
     uint32_t *band_list = nullptr;       // interface cells of the sub-step (interior indices)
-    unsigned *nband = nullptr;           // how many
+    unsigned *nband = nullptr;           // how many, and how many far pairs were queued
+    uint32_t *far_queue = nullptr;       // band pairs left to k_band_far
+    unsigned far_cap = 0;
     double *vgeo[3][3] = {};             // U, V, W grid spacings (allocated on first use)
     double *vfld[3][5] = {};             // U, V, W: phiL, nxL, nyL, nzL, vofL
     int lvs_flag[6] = {}, vof_flag[6] = {};
@@ -169,21 +174,63 @@ __global__ void k_band_reset(Dims D, const double *__restrict__ vfl, unsigned lo
     if (src) list[base + __popc(mask & ((1u << lane) - 1u))] = (uint32_t)D.n(i, j, k);
 }
 
-// The band pairs of the listed interface cells: a block takes one cell at a
-// time and its threads the cell's 729 offsets.
+// The band pairs of the listed interface cells, first part: a block takes
+// one cell at a time and its threads the cell's 729 offsets; each pair is
+// marked and, in band_distance's first two cases, settled.  A pair needing
+// the third case (the plane's trace on a face, several times longer) is
+// appended to the far queue (warp-aggregated), so that k_band_far runs those
+// in full warps instead of a few lanes of many warps; when the queue is full
+// the pair is finished here.  Every lane of a warp makes the same three
+// trips over the offsets, so the warp-wide ballot is safe.
 __global__ void __launch_bounds__(256, 2) k_band_pairs(Dims D, Geo G, const double *__restrict__ vfl,
                                                     const double *__restrict__ phi, const double *__restrict__ nx,
                                                     const double *__restrict__ ny, const double *__restrict__ nz,
                                                     const double *__restrict__ dis, const uint32_t *__restrict__ list,
-                                                    const unsigned *__restrict__ count, unsigned long long *key,
-                                                    uint8_t *fix)
+                                                    const unsigned *__restrict__ counts, unsigned long long *key,
+                                                    uint8_t *fix, uint32_t *far_queue, unsigned far_cap,
+                                                    unsigned *far_count)
 {
-    const unsigned n = *count;
+    const unsigned n = counts[0];
+    const int lane = threadIdx.x & 31;
     for (unsigned q = blockIdx.x; q < n; q += gridDim.x) {
         int i, j, k;
         tr::cell_of(D, list[q], i, j, k);
-        for (int t = threadIdx.x; t < tr::BAND_CELLS; t += blockDim.x)
-            tr::band_pair(D, G, vfl, phi, nx, ny, nz, dis, i, j, k, t, key, fix);
+        const bool queueable = q < tr::FAR_Q_LIMIT;
+        for (int t0 = 0; t0 < tr::BAND_CELLS; t0 += blockDim.x) {
+            const int t = t0 + threadIdx.x;
+            bool need = false;
+            if (t < tr::BAND_CELLS) need = !tr::band_pair_near(D, G, vfl, phi, nx, ny, nz, dis, i, j, k, t, key, fix);
+            const unsigned m = __ballot_sync(0xffffffffu, need && queueable);
+            unsigned base = 0;
+            if (m) {
+                const int leader = __ffs(m) - 1;
+                if (lane == leader) base = atomicAdd(far_count, (unsigned)__popc(m));
+                base = __shfl_sync(0xffffffffu, base, leader);
+            }
+            if (need) {
+                const unsigned slot = base + (unsigned)__popc(m & ((1u << lane) - 1u));
+                if (queueable && slot < far_cap) far_queue[slot] = tr::far_pack(q, t);
+                else tr::band_pair_far(D, G, phi, nx, ny, nz, dis, i, j, k, t, key);
+            }
+        }
+    }
+}
+
+// Second part: the queued pairs, one per thread.
+__global__ void __launch_bounds__(256, 2) k_band_far(Dims D, Geo G, const double *__restrict__ phi,
+                                                  const double *__restrict__ nx, const double *__restrict__ ny,
+                                                  const double *__restrict__ nz, const double *__restrict__ dis,
+                                                  const uint32_t *__restrict__ list,
+                                                  const uint32_t *__restrict__ far_queue, unsigned far_cap,
+                                                  const unsigned *__restrict__ far_count, unsigned long long *key)
+{
+    const unsigned nf = min(*far_count, far_cap);
+    for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < nf; e += gridDim.x * blockDim.x) {
+        uint32_t q;
+        int t, i, j, k;
+        tr::far_unpack(far_queue[e], q, t);
+        tr::cell_of(D, list[q], i, j, k);
+        tr::band_pair_far(D, G, phi, nx, ny, nz, dis, i, j, k, t, key);
     }
 }
 
@@ -240,13 +287,13 @@ struct Timer {
     int n = 0;
     void before(int kind)
     {
-        if (!ctx->timing) return;
+        if (!ctx->timing || (size_t)(2 * n + 1) >= ctx->tev.size()) return;
         cudaEventRecord(ctx->tev[2 * n], ctx->st);
         ctx->tkind[n] = kind;
     }
     void after()
     {
-        if (!ctx->timing) return;
+        if (!ctx->timing || (size_t)(2 * n + 1) >= ctx->tev.size()) return;
         cudaEventRecord(ctx->tev[2 * n + 1], ctx->st);
         ++n;
     }
@@ -326,21 +373,28 @@ int scheme_step(scf_clsvof_ctx *ctx, int &launches, Timer &T)
         T.after();
         if ((rc = launch_check(ctx, "k_reconstruct")) != SCF_OK) return rc;
         T.before(3);
-        if (cudaMemsetAsync(ctx->nband, 0, sizeof(unsigned), ctx->st) != cudaSuccess)
+        if (cudaMemsetAsync(ctx->nband, 0, 2 * sizeof(unsigned), ctx->st) != cudaSuccess)
             return launch_check(ctx, "cudaMemsetAsync");
         k_band_reset<<<gin, NX, 0, ctx->st>>>(D, ctx->vf[0], ctx->key, ctx->fix, ctx->band_list, ctx->nband);
         T.after();
         if ((rc = launch_check(ctx, "k_band_reset")) != SCF_OK) return rc;
         T.before(3);
         k_band_pairs<<<kBandBlocks, 256, 0, ctx->st>>>(D, G, ctx->vf[0], ctx->ls[0], ctx->nx, ctx->ny, ctx->nz,
-                                                       ctx->dis, ctx->band_list, ctx->nband, ctx->key, ctx->fix);
+                                                       ctx->dis, ctx->band_list, ctx->nband, ctx->key, ctx->fix,
+                                                       ctx->far_queue, ctx->far_cap, ctx->nband + 1);
         T.after();
         if ((rc = launch_check(ctx, "k_band_pairs")) != SCF_OK) return rc;
+        T.before(3);
+        k_band_far<<<kBandBlocks, 256, 0, ctx->st>>>(D, G, ctx->ls[0], ctx->nx, ctx->ny, ctx->nz, ctx->dis,
+                                                     ctx->band_list, ctx->far_queue, ctx->far_cap, ctx->nband + 1,
+                                                     ctx->key);
+        T.after();
+        if ((rc = launch_check(ctx, "k_band_far")) != SCF_OK) return rc;
         T.before(3);
         k_band_value<<<gin, NX, 0, ctx->st>>>(D, G, ctx->vf[0], ctx->dis, ctx->key, ctx->fix, ctx->ls[0]);
         T.after();
         if ((rc = launch_check(ctx, "k_band_value")) != SCF_OK) return rc;
-        launches += 5;
+        launches += 6;
     }
     return SCF_OK;
 }
@@ -400,7 +454,9 @@ extern "C" int scf_clsvof_create(scf_clsvof_ctx **out, int32_t imax, int32_t jma
     for (auto &p : ctx->vel) TRY(p, ng)
     for (int a = 0; a < 3; ++a) TRY(ctx->bc_vel[a], ctx->D.plane_size(a))
     for (int f = 0; f < 6; ++f) { TRY(ctx->lvs_bc[f], ctx->D.plane_size(f / 2)) TRY(ctx->vof_bc[f], ctx->D.plane_size(f / 2)) }
-    TRY(ctx->key, nin) TRY(ctx->fix, nin) TRY(ctx->band_list, nin) TRY(ctx->nband, 1)
+    ctx->far_cap = (unsigned)std::max<size_t>(nin / 2, (size_t)1 << 20);
+    TRY(ctx->key, nin) TRY(ctx->fix, nin) TRY(ctx->band_list, nin) TRY(ctx->nband, 2)
+    TRY(ctx->far_queue, ctx->far_cap)
 #undef TRY
     *out = ctx;
     return SCF_OK;
@@ -410,7 +466,7 @@ extern "C" int scf_clsvof_set_timing(scf_clsvof_ctx *ctx, int32_t on)
 {
     if (!ctx) return SCF_ERR_BAD_ARG;
     cudaSetDevice(ctx->device);
-    const size_t need = 2 * (size_t)tr::NSUB * 11;   // two events per launch of a step
+    const size_t need = 2 * (size_t)tr::NSUB * 12;   // two events per launch of a step
     while (on && ctx->tev.size() < need) {
         cudaEvent_t e = nullptr;
         TK(cudaEventCreate(&e));
@@ -458,24 +514,23 @@ extern "C" int scf_clsvof_stage(scf_clsvof_ctx *ctx, const scf_clsvof_in *in, co
     const size_t nin = ctx->D.interior(), ng = ctx->D.ghosted();
     const size_t bi = nin * sizeof(double), bg = ng * sizeof(double);
     const double *geo[6] = {in->x, in->y, in->z, in->dx, in->dy, in->dz};
-    for (int q = 0; q < 6; ++q) TK(cudaMemcpyAsync(ctx->geo[q], geo[q], bi, cudaMemcpyHostToDevice, ctx->st));
+    for (int q = 0; q < 6; ++q) TK(stage_h2d(ctx->geo[q], geo[q], bi, ctx->st, 0, nullptr, nullptr));
     const double *vel[3] = {in->u, in->v, in->w}, *fn[3] = {in->nx, in->ny, in->nz};
     const double *bcv[3] = {in->bc_u_w, in->bc_v_s, in->bc_w_b};
     for (int a = 0; a < 3; ++a) {
-        TK(cudaMemcpyAsync(ctx->vel[a], vel[a], bg, cudaMemcpyHostToDevice, ctx->st));
-        TK(cudaMemcpyAsync(ctx->fn[a], fn[a], bg, cudaMemcpyHostToDevice, ctx->st));
-        TK(cudaMemcpyAsync(ctx->bc_vel[a], bcv[a], ctx->D.plane_size(a) * sizeof(double), cudaMemcpyHostToDevice,
-                           ctx->st));
+        TK(stage_h2d(ctx->vel[a], vel[a], bg, ctx->st, 0, nullptr, nullptr));
+        TK(stage_h2d(ctx->fn[a], fn[a], bg, ctx->st, 0, nullptr, nullptr));
+        TK(stage_h2d(ctx->bc_vel[a], bcv[a], ctx->D.plane_size(a) * sizeof(double), ctx->st, 0, nullptr, nullptr));
     }
-    TK(cudaMemcpyAsync(ctx->vf[0], s->vofl, bg, cudaMemcpyHostToDevice, ctx->st));
-    TK(cudaMemcpyAsync(ctx->ls[0], s->phil, bg, cudaMemcpyHostToDevice, ctx->st));
+    TK(stage_h2d(ctx->vf[0], s->vofl, bg, ctx->st, 0, nullptr, nullptr));
+    TK(stage_h2d(ctx->ls[0], s->phil, bg, ctx->st, 0, nullptr, nullptr));
     for (int b = 1; b < 3; ++b) {   // the ping-pong buffers' ghosts must match buffer 0's
         TK(cudaMemcpyAsync(ctx->vf[b], ctx->vf[0], bg, cudaMemcpyDeviceToDevice, ctx->st));
         TK(cudaMemcpyAsync(ctx->ls[b], ctx->ls[0], bg, cudaMemcpyDeviceToDevice, ctx->st));
     }
-    TK(cudaMemcpyAsync(ctx->nxl, s->nxl, bg, cudaMemcpyHostToDevice, ctx->st));
-    TK(cudaMemcpyAsync(ctx->nyl, s->nyl, bg, cudaMemcpyHostToDevice, ctx->st));
-    TK(cudaMemcpyAsync(ctx->nzl, s->nzl, bg, cudaMemcpyHostToDevice, ctx->st));
+    TK(stage_h2d(ctx->nxl, s->nxl, bg, ctx->st, 0, nullptr, nullptr));
+    TK(stage_h2d(ctx->nyl, s->nyl, bg, ctx->st, 0, nullptr, nullptr));
+    TK(stage_h2d(ctx->nzl, s->nzl, bg, ctx->st, 0, nullptr, nullptr));
     for (int f = 0; f < 6; ++f)
         TK(cudaMemcpyAsync(ctx->lvs_bc[f], s->lvs_bc[f], ctx->D.plane_size(f / 2) * sizeof(double),
                            cudaMemcpyHostToDevice, ctx->st));
@@ -618,9 +673,9 @@ extern "C" int scf_clsvof_uvw_liquid_field(scf_clsvof_ctx *ctx, const scf_clsvof
         const double *g[3] = {c.dx, c.dy, c.dz};
         double *h[5] = {c.phil, c.nxl, c.nyl, c.nzl, c.vofl};
         for (int q = 0; q < 3; ++q)
-            TK(cudaMemcpyAsync(ctx->vgeo[f][q], g[q], nin * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+            TK(stage_h2d(ctx->vgeo[f][q], g[q], nin * sizeof(double), ctx->st, 0, nullptr, nullptr));
         for (int q = 0; q < 5; ++q)
-            TK(cudaMemcpyAsync(ctx->vfld[f][q], h[q], ng * sizeof(double), cudaMemcpyHostToDevice, ctx->st));
+            TK(stage_h2d(ctx->vfld[f][q], h[q], ng * sizeof(double), ctx->st, 0, nullptr, nullptr));
     }
     TK(cudaEventRecord(ctx->ev[1], ctx->st));
     const Geo G = geo_of(ctx);

@@ -15,6 +15,7 @@
 #include "../../include/scf_predictor.h"
 #include "pred_kernels.h"
 #include "scf_devmem.h"
+#include "scf_stage.h"
 
 using namespace pred;
 
@@ -412,7 +413,7 @@ extern "C" int scf_mom_stage(scf_mom_ctx *ctx, const scf_mom_in in[3])
     MK(cudaSetDevice(ctx->device));
     for (int c = 0; c < 3; ++c) {
         for (const Copy &cp : comp_copies(ctx, c, in[c]))
-            MK(cudaMemcpyAsync(cp.dev, cp.host, cp.bytes, cudaMemcpyHostToDevice, ctx->st));
+            MK(stage_h2d(cp.dev, cp.host, cp.bytes, ctx->st, 0, nullptr, nullptr));
         for (int f = 0; f < 6; ++f) ctx->comp[c].flag[f] = in[c].bc_flag[f];
         ctx->comp[c].extcell = in[c].extcell;
     }
@@ -624,7 +625,12 @@ extern "C" int scf_predict_solves(scf_mom_ctx *ctx, const scf_mom_in in[3], cons
         for (int c = 0; c < 3; ++c) {
             if (e == cudaSuccess)
                 for (const Copy &cp : comp_copies(ctx, c, in[c])) {
-                    e = cudaMemcpyAsync(cp.dev, cp.host, cp.bytes, cudaMemcpyHostToDevice, ctx->cin);
+                    // the first component's inputs are on the critical path
+                    // (copy kernel, scf_stage.h); the others overlap the
+                    // earlier components' solves and take the copy engine,
+                    // which leaves the SMs to the solves
+                    e = c == 0 ? stage_h2d(cp.dev, cp.host, cp.bytes, ctx->cin, 0, nullptr, nullptr)
+                               : cudaMemcpyAsync(cp.dev, cp.host, cp.bytes, cudaMemcpyHostToDevice, ctx->cin);
                     if (e != cudaSuccess) break;
                 }
             if (e == cudaSuccess) e = cudaEventRecord(ctx->staged_ev[c], ctx->cin);

@@ -14,6 +14,7 @@
 #include "scf_kernels.h"
 #include "../../include/scf_projection.h"
 #include "scf_devmem.h"
+#include "scf_stage.h"
 
 namespace {
 
@@ -592,13 +593,17 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
     bool stalled = false, have_best = false;
     double best_rel = HUGE_VAL;
     const int ng = ctx->d.ng;
+    // x is zero before a cold first round; the double-float zero has the
+    // same bits as the FP64 zero, so that x needs no conversion
+    bool x_zero = !(ctx->opts.warm_start && ctx->warm_ok);
     for (;;) {
         if (mixed) {
-            // x and r (FP64 here) become double-float for the round
-            copy_to_low(A, ctx->r, rlow, ctx->st, &ctx->launches);
-            df_from_double(ctx->x, (float2 *)ctx->x, ng, ctx->st, &ctx->launches);
-            df_from_double(ctx->r, (float2 *)ctx->r, ng, ctx->st, &ctx->launches);
+            // x and r (FP64 here) become double-float for the round, and r's
+            // FP32 copy is the V-cycle's right-hand side
+            if (!x_zero) df_from_double(ctx->x, (float2 *)ctx->x, ng, ctx->st, &ctx->launches);
+            df_round_start(ctx->r, rlow, ng, ctx->st, &ctx->launches);
         }
+        x_zero = false;
         T *z = precondition<T>(ctx, L, cc, false);
         cg_beta<T>(ctx, z);
         cg_direction<T>(ctx, z, true);
@@ -753,11 +758,18 @@ int run(scf_ctx *ctx, bool with_correction, scf_stats *stats)
     return solve_rc;
 }
 
+// Blocks of the copy kernels that bring the correction's inputs in on the
+// second stream while the solve runs: enough to move them within the solve
+// (about 1 GB in 16 ms at 256^3), few enough to leave the SMs to the solve.
+constexpr int kSideCopyBlocks = 64;
+
+// One input array to the device: by a copy kernel when the caller's array
+// is page-locked and device-mapped, else by the copy engine (scf_stage.h).
 template <typename P>
 int h2d(scf_ctx *ctx, P *dst, const P *src, size_t n, int64_t *bytes, cudaStream_t st)
 {
     if (!src) { set_err(ctx, "null input array"); return SCF_ERR_BAD_ARG; }
-    CK(cudaMemcpyAsync(dst, src, n * sizeof(P), cudaMemcpyHostToDevice, st));
+    CK(stage_h2d(dst, src, n * sizeof(P), st, st == ctx->st ? 0 : kSideCopyBlocks, nullptr, nullptr));
     *bytes += (int64_t)(n * sizeof(P));
     return SCF_OK;
 }
@@ -845,7 +857,7 @@ template <typename P>
 int d2h(scf_ctx *ctx, P *dst, const P *src, size_t n, int64_t *bytes)
 {
     if (!dst) return SCF_OK;
-    CK(cudaMemcpyAsync(dst, src, n * sizeof(P), cudaMemcpyDeviceToHost, ctx->st));
+    CK(stage_d2h(dst, src, n * sizeof(P), ctx->st, 0, nullptr, nullptr));
     *bytes += (int64_t)(n * sizeof(P));
     return SCF_OK;
 }
@@ -1458,7 +1470,9 @@ int scf_last_error(const scf_ctx *ctx, char *buf, size_t len)
 int scf_host_register(void *ptr, size_t bytes)
 {
     if (!ptr || !bytes) return SCF_ERR_BAD_ARG;
-    return cudaHostRegister(ptr, bytes, cudaHostRegisterDefault) == cudaSuccess ? SCF_OK : SCF_ERR_CUDA;
+    return cudaHostRegister(ptr, bytes, cudaHostRegisterMapped | cudaHostRegisterPortable) == cudaSuccess
+               ? SCF_OK
+               : SCF_ERR_CUDA;
 }
 
 int scf_host_unregister(void *ptr)

@@ -102,3 +102,62 @@ __device__ __forceinline__ double block_sum(double v)
 
 __device__ __forceinline__ int block_linear() { return blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z); }
 __device__ __forceinline__ int thread_linear() { return threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z); }
+
+#if defined(__CUDACC__)
+// ---- FP64 -> FP32 on the integer pipe ---------------------------------------
+// FP64 arithmetic is this GPU's scarcest resource; these two conversions
+// (used by the assembly and the mixed solver's double-float vectors) run on
+// the integer pipe and match the IEEE conversions bit for bit.
+
+// d - (double)hi rounded to FP32, where hi is d rounded to FP32: the lo part
+// of the double-float form of d.  Computed on the integer pipe (the
+// significands of d and hi aligned to d's exponent differ by less than
+// 2^29 units of d's last place).  Zeros give +0; subnormals and non-finite
+// values take the FP64 route.
+__device__ __forceinline__ float scf_lo_part(double d, float hi)
+{
+    const long long db = __double_as_longlong(d);
+    if (((unsigned long long)db << 1) == 0) return 0.0f;   // d - (double)hi = +0 for d = +-0
+    const int ed = (int)((db >> 52) & 0x7ff);
+    const int hb = __float_as_int(hi);
+    const int eh8 = (hb >> 23) & 0xff;
+    if (ed != 0 && ed != 0x7ff && eh8 != 0 && eh8 != 0xff) {
+        const long long md = (db & 0xfffffffffffffLL) | (1LL << 52);
+        const long long mh = (long long)((hb & 0x7fffff) | 0x800000) << 29;
+        const int eh = eh8 - 127 + 1023;
+        long long diff;
+        bool ok = true;
+        if (eh == ed) diff = md - mh;
+        else if (eh == ed + 1) diff = md - (mh << 1);
+        else { diff = 0; ok = false; }
+        if (ok && diff > -(1LL << 30) && diff < (1LL << 30)) {
+            if (diff == 0) return 0.0f;
+            if (db < 0) diff = -diff;
+            const int fb = __float_as_int(__int2float_rn((int)diff));
+            const int ef = ((fb >> 23) & 0xff) + (ed - 1075);
+            if (ef >= 1 && ef <= 254) return __int_as_float((fb & ~(0xff << 23)) | (ef << 23));
+        }
+    }
+    return (float)(d - (double)hi);
+}
+
+// d rounded to FP32 (round to nearest even) on the integer pipe, for results
+// in FP32's normal range, and of zeros; the rest (subnormal or out-of-range
+// results, non-finite values) take the conversion instruction, which runs on
+// the FP64 pipe.
+__device__ __forceinline__ float scf_to_f32(double d)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const int e = (int)((b >> 52) & 0x7ff);
+    if ((b << 1) == 0) return __uint_as_float((unsigned)(b >> 32));   // +-0
+    if (e >= 1023 - 126 && e <= 1023 + 127) {
+        const unsigned long long m = b & 0xfffffffffffffull;
+        const unsigned hi = (unsigned)(m >> 29), rem = (unsigned)(m & 0x1fffffffu);
+        unsigned r = ((unsigned)(e - 1023 + 127) << 23) | hi;
+        if (rem > 0x10000000u || (rem == 0x10000000u && (hi & 1u))) r += 1u;   // a carry rounds into the exponent
+        r |= (unsigned)(b >> 32) & 0x80000000u;
+        return __uint_as_float(r);
+    }
+    return (float)d;
+}
+#endif

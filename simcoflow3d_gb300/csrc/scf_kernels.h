@@ -164,6 +164,9 @@ void df_pupdate(const DfOp &A, const float *z, float2 *p, const double *scal, bo
 // (r, z) in FP64 from the double-float r and the FP32 z; beta into the scalars
 void df_dot_rz(const DfOp &A, const float2 *r, const float *z, Reducer &R, cudaStream_t st, int *launches);
 void df_from_double(const double *src, float2 *dst, int n, cudaStream_t st, int *launches);
+// the residual r (FP64, whole padded array) to double-float in place, with
+// its FP32 hi part written to rlow
+void df_round_start(double *r, float *rlow, int n, cudaStream_t st, int *launches);
 void df_to_double(const float2 *src, double *dst, int n, cudaStream_t st, int *launches);
 // alpha and the mean of A p from the two-lane partials of an SpMV
 void reduce_alpha(Reducer &R, int nblocks, bool singular, cudaStream_t st, int *launches);
