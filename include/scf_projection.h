@@ -322,8 +322,11 @@ int scf_apply_operator_noalloc(int32_t imax, int32_t jmax, int32_t kmax,
 const char *scf_status_string(int status);
 /* Copies the context's last error message (NUL-terminated) into buf.       */
 int scf_last_error(const scf_ctx *ctx, char *buf, size_t len);
-/* Pins a caller-owned host array so that later copies run at full link
- * speed (cudaHostRegister); undo with scf_host_unregister.                  */
+/* Pins a caller-owned host array and maps it into the device's address
+ * space (cudaHostRegister, mapped and portable); undo with
+ * scf_host_unregister.  The library moves page-locked, mapped arrays with
+ * copy kernels that load from (and store to) host memory directly, and
+ * other arrays with cudaMemcpyAsync.                                       */
 int scf_host_register(void *ptr, size_t bytes);
 int scf_host_unregister(void *ptr);
 int scf_abi_version(void);

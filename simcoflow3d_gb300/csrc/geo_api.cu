@@ -298,7 +298,7 @@ int scf_geo_fetch(scf_geo_ctx *ctx, scf_geo_cells *p, scf_geo_cells *u, scf_geo_
         std::vector<void *> hout;
         host_ptrs(fams[f], ctx->has_moex[f], hin, hout);
         for (size_t q = 0; q < dout.size(); ++q)
-            GK(cudaMemcpyAsync(hout[q], dout[q].dev, dout[q].bytes, cudaMemcpyDeviceToHost, ctx->st));
+            GK(stage_d2h(hout[q], dout[q].dev, dout[q].bytes, ctx->st, 0, nullptr, nullptr));
         fams[f]->ext_cell = ctx->ext_cell[f];
     }
     GK(cudaStreamSynchronize(ctx->st));

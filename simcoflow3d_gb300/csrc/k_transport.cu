@@ -8,12 +8,10 @@
 //   k_walls                        the wall planes and ghosts;
 //   k_reconstruct (tail)           normals, liquid normals, centre distances;
 //   k_band_reset, k_band_pairs,    the redistancing: the reset lists the
-//   k_band_far, k_band_value       interface cells; then one block per
-//                                  listed cell takes its 9^3 band pairs,
-//                                  one pair per thread, settling the short
-//                                  cases and queueing the long one for
-//                                  k_band_far (full warps); each distance
-//                                  goes out with a 64-bit atomicMin
+//   k_band_value                   interface cells; then one block per
+//                                  listed cell computes its 9^3 band pairs,
+//                                  one pair per thread, and sends each
+//                                  distance with a 64-bit atomicMin
 //                                  (non-negative doubles order like their
 //                                  bits), so the result is the reference's
 //                                  running minimum whatever the order.
@@ -56,9 +54,7 @@ struct scf_clsvof_ctx {
     unsigned long long *key = nullptr;
     uint8_t *fix = nullptr;
     uint32_t *band_list = nullptr;       // interface cells of the sub-step (interior indices)
-    unsigned *nband = nullptr;           // how many, and how many far pairs were queued
-    uint32_t *far_queue = nullptr;       // band pairs left to k_band_far
-    unsigned far_cap = 0;
+    unsigned *nband = nullptr;           // how many
     double *vgeo[3][3] = {};             // U, V, W grid spacings (allocated on first use)
     double *vfld[3][5] = {};             // U, V, W: phiL, nxL, nyL, nzL, vofL
     int lvs_flag[6] = {}, vof_flag[6] = {};
@@ -174,63 +170,21 @@ __global__ void k_band_reset(Dims D, const double *__restrict__ vfl, unsigned lo
     if (src) list[base + __popc(mask & ((1u << lane) - 1u))] = (uint32_t)D.n(i, j, k);
 }
 
-// The band pairs of the listed interface cells, first part: a block takes
-// one cell at a time and its threads the cell's 729 offsets; each pair is
-// marked and, in band_distance's first two cases, settled.  A pair needing
-// the third case (the plane's trace on a face, several times longer) is
-// appended to the far queue (warp-aggregated), so that k_band_far runs those
-// in full warps instead of a few lanes of many warps; when the queue is full
-// the pair is finished here.  Every lane of a warp makes the same three
-// trips over the offsets, so the warp-wide ballot is safe.
+// The band pairs of the listed interface cells: a block takes one cell at a
+// time and its threads the cell's 729 offsets.
 __global__ void __launch_bounds__(256, 2) k_band_pairs(Dims D, Geo G, const double *__restrict__ vfl,
                                                     const double *__restrict__ phi, const double *__restrict__ nx,
                                                     const double *__restrict__ ny, const double *__restrict__ nz,
                                                     const double *__restrict__ dis, const uint32_t *__restrict__ list,
-                                                    const unsigned *__restrict__ counts, unsigned long long *key,
-                                                    uint8_t *fix, uint32_t *far_queue, unsigned far_cap,
-                                                    unsigned *far_count)
+                                                    const unsigned *__restrict__ count, unsigned long long *key,
+                                                    uint8_t *fix)
 {
-    const unsigned n = counts[0];
-    const int lane = threadIdx.x & 31;
+    const unsigned n = *count;
     for (unsigned q = blockIdx.x; q < n; q += gridDim.x) {
         int i, j, k;
         tr::cell_of(D, list[q], i, j, k);
-        const bool queueable = q < tr::FAR_Q_LIMIT;
-        for (int t0 = 0; t0 < tr::BAND_CELLS; t0 += blockDim.x) {
-            const int t = t0 + threadIdx.x;
-            bool need = false;
-            if (t < tr::BAND_CELLS) need = !tr::band_pair_near(D, G, vfl, phi, nx, ny, nz, dis, i, j, k, t, key, fix);
-            const unsigned m = __ballot_sync(0xffffffffu, need && queueable);
-            unsigned base = 0;
-            if (m) {
-                const int leader = __ffs(m) - 1;
-                if (lane == leader) base = atomicAdd(far_count, (unsigned)__popc(m));
-                base = __shfl_sync(0xffffffffu, base, leader);
-            }
-            if (need) {
-                const unsigned slot = base + (unsigned)__popc(m & ((1u << lane) - 1u));
-                if (queueable && slot < far_cap) far_queue[slot] = tr::far_pack(q, t);
-                else tr::band_pair_far(D, G, phi, nx, ny, nz, dis, i, j, k, t, key);
-            }
-        }
-    }
-}
-
-// Second part: the queued pairs, one per thread.
-__global__ void __launch_bounds__(256, 2) k_band_far(Dims D, Geo G, const double *__restrict__ phi,
-                                                  const double *__restrict__ nx, const double *__restrict__ ny,
-                                                  const double *__restrict__ nz, const double *__restrict__ dis,
-                                                  const uint32_t *__restrict__ list,
-                                                  const uint32_t *__restrict__ far_queue, unsigned far_cap,
-                                                  const unsigned *__restrict__ far_count, unsigned long long *key)
-{
-    const unsigned nf = min(*far_count, far_cap);
-    for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < nf; e += gridDim.x * blockDim.x) {
-        uint32_t q;
-        int t, i, j, k;
-        tr::far_unpack(far_queue[e], q, t);
-        tr::cell_of(D, list[q], i, j, k);
-        tr::band_pair_far(D, G, phi, nx, ny, nz, dis, i, j, k, t, key);
+        for (int t = threadIdx.x; t < tr::BAND_CELLS; t += blockDim.x)
+            tr::band_pair(D, G, vfl, phi, nx, ny, nz, dis, i, j, k, t, key, fix);
     }
 }
 
@@ -373,28 +327,21 @@ int scheme_step(scf_clsvof_ctx *ctx, int &launches, Timer &T)
         T.after();
         if ((rc = launch_check(ctx, "k_reconstruct")) != SCF_OK) return rc;
         T.before(3);
-        if (cudaMemsetAsync(ctx->nband, 0, 2 * sizeof(unsigned), ctx->st) != cudaSuccess)
+        if (cudaMemsetAsync(ctx->nband, 0, sizeof(unsigned), ctx->st) != cudaSuccess)
             return launch_check(ctx, "cudaMemsetAsync");
         k_band_reset<<<gin, NX, 0, ctx->st>>>(D, ctx->vf[0], ctx->key, ctx->fix, ctx->band_list, ctx->nband);
         T.after();
         if ((rc = launch_check(ctx, "k_band_reset")) != SCF_OK) return rc;
         T.before(3);
         k_band_pairs<<<kBandBlocks, 256, 0, ctx->st>>>(D, G, ctx->vf[0], ctx->ls[0], ctx->nx, ctx->ny, ctx->nz,
-                                                       ctx->dis, ctx->band_list, ctx->nband, ctx->key, ctx->fix,
-                                                       ctx->far_queue, ctx->far_cap, ctx->nband + 1);
+                                                       ctx->dis, ctx->band_list, ctx->nband, ctx->key, ctx->fix);
         T.after();
         if ((rc = launch_check(ctx, "k_band_pairs")) != SCF_OK) return rc;
-        T.before(3);
-        k_band_far<<<kBandBlocks, 256, 0, ctx->st>>>(D, G, ctx->ls[0], ctx->nx, ctx->ny, ctx->nz, ctx->dis,
-                                                     ctx->band_list, ctx->far_queue, ctx->far_cap, ctx->nband + 1,
-                                                     ctx->key);
-        T.after();
-        if ((rc = launch_check(ctx, "k_band_far")) != SCF_OK) return rc;
         T.before(3);
         k_band_value<<<gin, NX, 0, ctx->st>>>(D, G, ctx->vf[0], ctx->dis, ctx->key, ctx->fix, ctx->ls[0]);
         T.after();
         if ((rc = launch_check(ctx, "k_band_value")) != SCF_OK) return rc;
-        launches += 6;
+        launches += 5;
     }
     return SCF_OK;
 }
@@ -454,9 +401,7 @@ extern "C" int scf_clsvof_create(scf_clsvof_ctx **out, int32_t imax, int32_t jma
     for (auto &p : ctx->vel) TRY(p, ng)
     for (int a = 0; a < 3; ++a) TRY(ctx->bc_vel[a], ctx->D.plane_size(a))
     for (int f = 0; f < 6; ++f) { TRY(ctx->lvs_bc[f], ctx->D.plane_size(f / 2)) TRY(ctx->vof_bc[f], ctx->D.plane_size(f / 2)) }
-    ctx->far_cap = (unsigned)std::max<size_t>(nin / 2, (size_t)1 << 20);
-    TRY(ctx->key, nin) TRY(ctx->fix, nin) TRY(ctx->band_list, nin) TRY(ctx->nband, 2)
-    TRY(ctx->far_queue, ctx->far_cap)
+    TRY(ctx->key, nin) TRY(ctx->fix, nin) TRY(ctx->band_list, nin) TRY(ctx->nband, 1)
 #undef TRY
     *out = ctx;
     return SCF_OK;
@@ -466,7 +411,7 @@ extern "C" int scf_clsvof_set_timing(scf_clsvof_ctx *ctx, int32_t on)
 {
     if (!ctx) return SCF_ERR_BAD_ARG;
     cudaSetDevice(ctx->device);
-    const size_t need = 2 * (size_t)tr::NSUB * 12;   // two events per launch of a step
+    const size_t need = 2 * (size_t)tr::NSUB * 11;   // two events per launch of a step
     while (on && ctx->tev.size() < need) {
         cudaEvent_t e = nullptr;
         TK(cudaEventCreate(&e));
@@ -591,16 +536,16 @@ extern "C" int scf_clsvof_fetch(scf_clsvof_ctx *ctx, scf_clsvof_state *s, scf_cl
     cudaSetDevice(ctx->device);
     const size_t bg = ctx->D.ghosted() * sizeof(double);
     TK(cudaEventRecord(ctx->ev[2], ctx->st));
-    TK(cudaMemcpyAsync(s->vofl, ctx->vf[0], bg, cudaMemcpyDeviceToHost, ctx->st));
-    TK(cudaMemcpyAsync(s->phil, ctx->ls[0], bg, cudaMemcpyDeviceToHost, ctx->st));
-    TK(cudaMemcpyAsync(s->nxl, ctx->nxl, bg, cudaMemcpyDeviceToHost, ctx->st));
-    TK(cudaMemcpyAsync(s->nyl, ctx->nyl, bg, cudaMemcpyDeviceToHost, ctx->st));
-    TK(cudaMemcpyAsync(s->nzl, ctx->nzl, bg, cudaMemcpyDeviceToHost, ctx->st));
+    TK(stage_d2h(s->vofl, ctx->vf[0], bg, ctx->st, 0, nullptr, nullptr));
+    TK(stage_d2h(s->phil, ctx->ls[0], bg, ctx->st, 0, nullptr, nullptr));
+    TK(stage_d2h(s->nxl, ctx->nxl, bg, ctx->st, 0, nullptr, nullptr));
+    TK(stage_d2h(s->nyl, ctx->nyl, bg, ctx->st, 0, nullptr, nullptr));
+    TK(stage_d2h(s->nzl, ctx->nzl, bg, ctx->st, 0, nullptr, nullptr));
     int64_t planes = 0;
     for (int f = 0; f < 6; ++f) {
         const size_t pb = ctx->D.plane_size(f / 2) * sizeof(double);
-        TK(cudaMemcpyAsync(s->lvs_bc[f], ctx->lvs_bc[f], pb, cudaMemcpyDeviceToHost, ctx->st));
-        TK(cudaMemcpyAsync(s->vof_bc[f], ctx->vof_bc[f], pb, cudaMemcpyDeviceToHost, ctx->st));
+        TK(stage_d2h(s->lvs_bc[f], ctx->lvs_bc[f], pb, ctx->st, 0, nullptr, nullptr));
+        TK(stage_d2h(s->vof_bc[f], ctx->vof_bc[f], pb, ctx->st, 0, nullptr, nullptr));
         planes += 2 * (int64_t)pb;
     }
     TK(cudaEventRecord(ctx->ev[3], ctx->st));
@@ -691,7 +636,7 @@ extern "C" int scf_clsvof_uvw_liquid_field(scf_clsvof_ctx *ctx, const scf_clsvof
         const scf_clsvof_vcell &c = cells[f];
         double *h[5] = {c.phil, c.nxl, c.nyl, c.nzl, c.vofl};
         for (int q = 0; q < 5; ++q)
-            TK(cudaMemcpyAsync(h[q], ctx->vfld[f][q], ng * sizeof(double), cudaMemcpyDeviceToHost, ctx->st));
+            TK(stage_d2h(h[q], ctx->vfld[f][q], ng * sizeof(double), ctx->st, 0, nullptr, nullptr));
     }
     TK(cudaEventRecord(ctx->ev[3], ctx->st));
     TK(cudaStreamSynchronize(ctx->st));

@@ -616,35 +616,6 @@ TR_HD double band_distance(double nxx, double nyy, double nzz, double diss, int 
     return sqrt((X - s[0]) * (X - s[0]) + (Y - s[1]) * (Y - s[1]) + (Z - s[2]) * (Z - s[2]));
 }
 
-// band_distance's first two cases -- the facing boundary point, or the
-// foot of the perpendicular inside the cell -- with the same operations (the
-// point is chosen first, then the one distance expression is evaluated on
-// it).  Returns false when neither applies and the plane's trace on a face
-// is needed (band_distance's third case, much the longest).
-TR_HD bool band_distance_near(double nxx, double nyy, double nzz, double diss, int ii, int jj, int kk, double dx,
-                              double dy, double dz, double side, double &dist)
-{
-    const int l = ii < -1 ? -1 : ii > 1 ? 1 : ii;
-    const int m = jj < -1 ? -1 : jj > 1 ? 1 : jj;
-    const int n = kk < -1 ? -1 : kk > 1 ? 1 : kk;
-    const double xv = dx * (double)l / 2.0, yv = dy * (double)m / 2.0, zv = dz * (double)n / 2.0;
-    const double dv = nxx * xv + nyy * yv + nzz * zv + diss;
-    const double X = dx * (double)ii, Y = dy * (double)jj, Z = dz * (double)kk;
-    double sx, sy, sz;
-    if (dv * sgn(side) <= 0.0) {
-        sx = xv; sy = yv; sz = zv;
-    } else {
-        const double dij1 = nxx * dx * (double)ii + nyy * dy * (double)jj + nzz * dz * (double)kk + diss;
-        const double xp = X - dij1 * nxx, yp = Y - dij1 * nyy, zp = Z - dij1 * nzz;
-        if (!(-0.5 * dx <= xp && xp <= 0.5 * dx && -0.5 * dy <= yp && yp <= 0.5 * dy && -0.5 * dz <= zp &&
-              zp <= 0.5 * dz))
-            return false;
-        sx = xp; sy = yp; sz = zp;
-    }
-    dist = sqrt((X - sx) * (X - sx) + (Y - sy) * (Y - sy) + (Z - sz) * (Z - sz));
-    return true;
-}
-
 TR_HD bool band_interface(double v) { return 0.0 + 1.0e-15 < v && v < 1.0 - 1.0e-15; }
 TR_HD bool band_target(double v) { return v < 0.0 + 1.0e-15 || v > 1.0 - 1.0e-15; }
 
@@ -687,38 +658,18 @@ TR_HD void cell_of(const Dims &D, uint32_t c, int &i, int &j, int &k)
 // offset t.  A full or empty target cell within BAND cells in each index is
 // marked and keeps the least distance seen; dis holds the distances from
 // the cell centres.  The minimum does not depend on the order of the pairs.
-// The pair is done in two parts so that a kernel can gather the long third
-// case of band_distance into full warps: band_pair_near marks the target
-// and settles the first two cases, and returns false (leaving the pair to
-// band_pair_far) for the third.
-TR_HD bool band_pair_near(const Dims &D, const Geo &G, const double *vfl, const double *phi, const double *nx,
-                          const double *ny, const double *nz, const double *dis, int i, int j, int k, int t,
-                          unsigned long long *key, uint8_t *fix)
+TR_HD void band_pair(const Dims &D, const Geo &G, const double *vfl, const double *phi, const double *nx,
+                     const double *ny, const double *nz, const double *dis, int i, int j, int k, int t,
+                     unsigned long long *key, uint8_t *fix)
 {
     int ii, jj, kk;
     band_offset(t, ii, jj, kk);
     const int ti = i + ii, tj = j + jj, tk = k + kk;
-    if (!(1 <= ti && ti <= D.I && 1 <= tj && tj <= D.J && 1 <= tk && tk <= D.K)) return true;
+    if (!(1 <= ti && ti <= D.I && 1 <= tj && tj <= D.J && 1 <= tk && tk <= D.K)) return;
     const size_t tg = D.g(ti, tj, tk), tc = D.n(ti, tj, tk);
-    if (!band_target(vfl[tg])) return true;
+    if (!band_target(vfl[tg])) return;
     const size_t g = D.g(i, j, k), c = D.n(i, j, k);
     fix[tc] = 1;
-    double deuc;
-    if (!band_distance_near(nx[g], ny[g], nz[g], dis[g], ii, jj, kk, G.dx[c], G.dy[c], G.dz[c], phi[tg], deuc))
-        return false;
-    atomic_min_key(key + tc, key_of(deuc));
-    return true;
-}
-
-// The third case of a pair that band_pair_near left (the target is in the
-// domain, full or empty, and already marked).
-TR_HD void band_pair_far(const Dims &D, const Geo &G, const double *phi, const double *nx, const double *ny,
-                         const double *nz, const double *dis, int i, int j, int k, int t, unsigned long long *key)
-{
-    int ii, jj, kk;
-    band_offset(t, ii, jj, kk);
-    const size_t tg = D.g(i + ii, j + jj, k + kk), tc = D.n(i + ii, j + jj, k + kk);
-    const size_t g = D.g(i, j, k), c = D.n(i, j, k);
     const double deuc = band_distance(nx[g], ny[g], nz[g], dis[g], ii, jj, kk, G.dx[c], G.dy[c], G.dz[c], phi[tg]);
     atomic_min_key(key + tc, key_of(deuc));
 }
@@ -729,20 +680,7 @@ TR_HD void band_scatter(const Dims &D, const Geo &G, const double *vfl, const do
                         unsigned long long *key, uint8_t *fix)
 {
     if (!band_interface(vfl[D.g(i, j, k)])) return;
-    for (int t = 0; t < BAND_CELLS; ++t)
-        if (!band_pair_near(D, G, vfl, phi, nx, ny, nz, dis, i, j, k, t, key, fix))
-            band_pair_far(D, G, phi, nx, ny, nz, dis, i, j, k, t, key);
-}
-
-// A queued far pair: the interface cell's list index q and the offset t in
-// one 32-bit word (q < 2^22).
-constexpr int FAR_T_BITS = 10;
-constexpr uint32_t FAR_Q_LIMIT = 1u << (32 - FAR_T_BITS);
-TR_HD uint32_t far_pack(uint32_t q, int t) { return (q << FAR_T_BITS) | (uint32_t)t; }
-TR_HD void far_unpack(uint32_t e, uint32_t &q, int &t)
-{
-    q = e >> FAR_T_BITS;
-    t = (int)(e & ((1u << FAR_T_BITS) - 1u));
+    for (int t = 0; t < BAND_CELLS; ++t) band_pair(D, G, vfl, phi, nx, ny, nz, dis, i, j, k, t, key, fix);
 }
 
 // The level set each cell ends with (1866-1882).

@@ -239,7 +239,7 @@ class _HostLib:
 
     def scf_clsvof_step(self, ctx, pin, pstate, pstats):
         self._step(pin._obj, pstate._obj)
-        pstats._obj.steps, pstats._obj.gpu_launches = 1, 72
+        pstats._obj.steps, pstats._obj.gpu_launches = 1, 66
         return 0
 
     def scf_clsvof_stage(self, ctx, pin, pstate):
@@ -250,7 +250,7 @@ class _HostLib:
     def scf_clsvof_run(self, ctx, steps, pstats):
         for _ in range(steps):
             self._step(*self.staged)
-        pstats._obj.steps, pstats._obj.gpu_launches = steps, 72 * steps
+        pstats._obj.steps, pstats._obj.gpu_launches = steps, 66 * steps
         return 0
 
     def scf_clsvof_fetch(self, ctx, pstate, pstats):
@@ -281,7 +281,7 @@ def test_front_end_marshals_like_the_oracle(host_lib):
     sch = ClsvofScheme(I, J, K, lib=fake)
     s_got, p_got = _copy(state, lvs_bc)
     v_got, st = sch(centres, spacings, s_got, vel, fn, bc_vel, p_got, dt, **kw)
-    assert st["gpu_launches"] == 72
+    assert st["gpu_launches"] == 66
     s_ref, p_ref = _copy(state, lvs_bc)
     v_ref = O.clsvof_scheme(centres, spacings, s_ref, vel, fn, bc_vel, p_ref, dt, **kw)
     for key in s_ref:
@@ -290,7 +290,7 @@ def test_front_end_marshals_like_the_oracle(host_lib):
         np.testing.assert_array_equal(p_got[q], p_ref[q])
         np.testing.assert_array_equal(v_got[q], v_ref[q])
     sch.stage(centres, spacings, s_got, vel, fn, bc_vel, p_got, dt, **kw)
-    assert sch.run(2)["gpu_launches"] == 144
+    assert sch.run(2)["gpu_launches"] == 132
     sch.fetch(s_got, p_got)
     for _ in range(2):
         O.clsvof_scheme(centres, spacings, s_ref, vel, fn, bc_vel, p_ref, dt, **kw)
@@ -448,7 +448,7 @@ def test_bench_transport_leg_runs_over_the_host_build(host_lib, monkeypatch, cap
                 "vs_baseline", "dtype", "data", "config", "e2e", "roofline", "clocks", "gpu_launches",
                 "cpu_baseline"):
         assert key in line, key
-    assert line["value"] == 1.5 and line["gpu_launches"] == 2 * 72 and line["unit"] == "ms/step"
+    assert line["value"] == 1.5 and line["gpu_launches"] == 2 * 66 and line["unit"] == "ms/step"
     rf = line["roofline"]
     assert rf["kernel"] == "k_sweep" and rf["bytes_per_launch"] == 16 ** 3 * (40 + 2 * 56) // 3
     assert rf["achieved"] > 0 and line["e2e"]["h2d_bytes_per_step"] == 1 << 20

@@ -116,23 +116,13 @@ extern "C" int host_clsvof_step(int I, int J, int K, const double *const geo[6],
             fix[c] = 0;
             if (tr::band_interface(vf[0][D.g(i, j, k)])) list.push_back((uint32_t)c);
         });
-        std::vector<uint32_t> far;
         for (size_t q = list.size(); q-- > 0;) {   // k_band_pairs (any order of cells and pairs)
             int i, j, k;
             tr::cell_of(D, list[q], i, j, k);
             TR_CHECK(D.n(i, j, k) == list[q], "cell_of");
             for (int t = tr::BAND_CELLS; t-- > 0;)
-                if (!tr::band_pair_near(D, G, vf[0].data(), ls[0].data(), nx.data(), ny.data(), nz.data(), dis.data(),
-                                        i, j, k, t, key.data(), fix.data()))
-                    far.push_back(tr::far_pack((uint32_t)q, t));
-        }
-        for (size_t e = 0; e < far.size(); ++e) {   // k_band_far
-            uint32_t q;
-            int t, i, j, k;
-            tr::far_unpack(far[e], q, t);
-            TR_CHECK(q < list.size() && t >= 0 && t < tr::BAND_CELLS, "far queue");
-            tr::cell_of(D, list[q], i, j, k);
-            tr::band_pair_far(D, G, ls[0].data(), nx.data(), ny.data(), nz.data(), dis.data(), i, j, k, t, key.data());
+                tr::band_pair(D, G, vf[0].data(), ls[0].data(), nx.data(), ny.data(), nz.data(), dis.data(), i, j, k,
+                              t, key.data(), fix.data());
         }
         cells([&](int i, int j, int k) {   // k_band_value
             ls[0][D.g(i, j, k)] = tr::band_value(D, G, vf[0].data(), dis.data(), i, j, k, key.data(), fix.data());
