@@ -9,10 +9,17 @@
  * where they live, normally in device memory (the projection context's
  * corrected velocities and pressure, its level set and volume fractions):
  * a kernel gathers the interior cells and rounds them to FP32, so only the
- * Float32 values cross to the host.  The arrays are stored raw in an
- * appended section (one UInt64 byte count before each), where the
- * reference's VTKFortran writer encodes them inline in base64; the values
- * are the same.
+ * Float32 values cross to the host.  Two layouts of the same values:
+ *  - scf_write_vtr: the arrays raw in an appended section, one UInt64 byte
+ *    count before each (the compact form, 3/4 of the inline size);
+ *  - scf_write_vtr_binary: VTKFortran's "BINARY" layout, the one
+ *    PrintResultVTK asks for (a_vtk_file%initialize(format='BINARY'),
+ *    src/PrintResult.f90:364; xml_writer_binary_local of
+ *    src/VTKFortran/src/lib/vtk_fortran_vtk_file_xml_writer_binary_local.f90):
+ *    each array inline, the base64 of its Int32 byte count followed by the
+ *    data (encode_binary_dataarray), with VTKFortran's tag text and
+ *    indentation, so that the file is byte for byte the reference's.  The
+ *    base64 is encoded on the device.
  */
 #ifndef SCF_OUTPUT_H
 #define SCF_OUTPUT_H
@@ -50,6 +57,14 @@ typedef struct scf_vtr_stats {
 int scf_write_vtr(const char *path, int32_t imax, int32_t jmax, int32_t kmax, const double *xc,
                   const double *dx, const double *yc, const double *dy, const double *zc, const double *dz,
                   int32_t nfields, const scf_vtr_field *fields, int32_t device, scf_vtr_stats *stats);
+
+/* The same snapshot in VTKFortran's inline base64 layout (above), the file
+ * PrintResultVTK writes (src/PrintResult.f90:328-391).  Its byte counts are
+ * Int32 as in VTKFortran, so I*J*K is at most 536,870,911; larger grids
+ * return SCF_ERR_BAD_ARG.                                                  */
+int scf_write_vtr_binary(const char *path, int32_t imax, int32_t jmax, int32_t kmax, const double *xc,
+                         const double *dx, const double *yc, const double *dy, const double *zc, const double *dz,
+                         int32_t nfields, const scf_vtr_field *fields, int32_t device, scf_vtr_stats *stats);
 
 /* Device pointers (ghosted FP64, on the context's device) of the fields a
  * projection context holds: u, v, w, p as corrected by the last

@@ -19,11 +19,14 @@ PRINT_RESULT_VTK_FIELDS = ("p", "u", "v", "w", "LiquidLvs", "FluidLvs", "LiquidV
 
 
 def write_vtr(path: str, shape: Tuple[int, int, int], axes: Sequence[np.ndarray],
-              fields: Iterable[Tuple[str, object]], device: int = 0, lib=None) -> dict:
+              fields: Iterable[Tuple[str, object]], device: int = 0, lib=None, encoding: str = "appended") -> dict:
     """Writes ``fields`` to ``path``.  ``axes`` = (xc, dx, yc, dy, zc, dz), the
     cell centres and widths of each axis (host, FP64).  Each field is
     (name, array) with a ghosted Fortran-ordered FP64 host array, or
-    (name, int) with a device pointer to one.  Returns the call's stats."""
+    (name, int) with a device pointer to one.  ``encoding``: "appended"
+    (raw arrays in an appended section, scf_write_vtr) or "binary"
+    (VTKFortran's inline base64, the reference's own file,
+    scf_write_vtr_binary).  Returns the call's stats."""
     from .projection import load_library, ScfError
     L = lib or load_library()
     I, J, K = shape
@@ -44,17 +47,22 @@ def write_vtr(path: str, shape: Tuple[int, int, int], axes: Sequence[np.ndarray]
             arr[q].on_device = 1
         arr[q].name = name.encode()
     st = capi.ScfVtrStats()
-    rc = L.scf_write_vtr(path.encode(), I, J, K, *(capi.dptr(a) for a in ax), len(fl), arr, device, C.byref(st))
+    capi.require(encoding in ("appended", "binary"), "encoding must be 'appended' or 'binary'")
+    fn = L.scf_write_vtr if encoding == "appended" else L.scf_write_vtr_binary
+    rc = fn(path.encode(), I, J, K, *(capi.dptr(a) for a in ax), len(fl), arr, device, C.byref(st))
     if rc != 0:
         raise ScfError(rc, "scf_write_vtr failed for %s" % path)
     return {k: getattr(st, k) for k, _ in capi.ScfVtrStats._fields_}
 
 
 def read_vtr(path: str) -> Dict[str, np.ndarray]:
-    """The arrays of a file written by write_vtr (appended raw, UInt64
-    headers): X/Y/Z_COORDINATES as 1-D Float32, cell fields as (I, J, K)
-    Float32 arrays in Fortran order."""
+    """The arrays of a file written by write_vtr, in either layout:
+    the coordinates (X_COORDINATES ... in the appended layout, X, Y, Z in
+    the inline one) as 1-D Float32, cell fields as (I, J, K) Float32 arrays
+    in Fortran order."""
     raw = open(path, "rb").read()
+    if b'format="binary"' in raw:
+        return _read_vtr_binary(raw)
     head_end = raw.index(b'<AppendedData encoding="raw">') + len(b'<AppendedData encoding="raw">')
     head = raw[:head_end].decode()
     base = raw.index(b"_", head_end) + 1
@@ -69,4 +77,18 @@ def read_vtr(path: str) -> Dict[str, np.ndarray]:
             out[name] = a
         else:
             out[name] = a.reshape((I, J, K), order="F")
+    return out
+
+
+def _read_vtr_binary(raw: bytes) -> Dict[str, np.ndarray]:
+    import base64
+    text = raw.decode()
+    ext = [int(v) for v in re.search(r'WholeExtent="([^"]+)"', text).group(1).split()]
+    I, J, K = ext[1] - 1, ext[3] - 1, ext[5] - 1
+    out = {}
+    for name, code in re.findall(r'Name="([^"]+)" format="binary">\s*([A-Za-z0-9+/=]+)\s*</DataArray>', text):
+        b = base64.b64decode(code)
+        nb = int(np.frombuffer(b, dtype="<i4", count=1)[0])
+        a = np.frombuffer(b, dtype="<f4", count=nb // 4, offset=4).copy()
+        out[name] = a if name in ("X", "Y", "Z") else a.reshape((I, J, K), order="F")
     return out

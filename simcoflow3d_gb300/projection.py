@@ -81,6 +81,7 @@ def load_library(path: Optional[str] = None):
     L.scf_geo_last_error.argtypes = [C.c_void_p, C.c_char_p, C.c_size_t]
     L.scf_write_vtr.argtypes = [C.c_char_p, C.c_int32, C.c_int32, C.c_int32] + [capi.c_double_p] * 6 + [
         C.c_int32, P(capi.ScfVtrField), C.c_int32, P(capi.ScfVtrStats)]
+    L.scf_write_vtr_binary.argtypes = L.scf_write_vtr.argtypes
     L.scf_ctx_device_fields.argtypes = [C.c_void_p] + [P(C.c_void_p)] * 7
     L.scf_apply_operator_noalloc.argtypes = [C.c_int32, C.c_int32, C.c_int32] + [C.c_void_p] * 8
     P_M = P(capi.ScfMomIn)

@@ -1,8 +1,9 @@
 """GPU field output (include/scf_output.h): the projection context's
 device-resident fields (corrected u, v, w, p and the staged phiL, vofL, vof)
-and a host field (the solid level set) written by scf_write_vtr give a file
-byte-identical to the oracle's (oracle/vtr.py) from the same values on the
-host, in PrintResultVTK's field order."""
+and a host field (the solid level set) written by scf_write_vtr (appended
+raw) and scf_write_vtr_binary (VTKFortran's inline base64, the reference's
+own file) give files byte-identical to the oracle's (oracle/vtr.py) from the
+same values on the host, in PrintResultVTK's field order."""
 import numpy as np
 import pytest
 
@@ -18,8 +19,9 @@ def _axes(w):
     return (np.cumsum(dx) - dx / 2, dx, np.cumsum(dy) - dy / 2, dy, np.cumsum(dz) - dz / 2, dz)
 
 
-@pytest.mark.parametrize("name,n", [("c1", 24), ("c4", 12)])
-def test_device_fields_to_vtr(gpu_lib, tmp_path, name, n):
+@pytest.mark.parametrize("encoding", ["appended", "binary"])
+@pytest.mark.parametrize("name,n", [("c1", 24), ("c4", 12), ("c1", 17)])
+def test_device_fields_to_vtr(gpu_lib, tmp_path, name, n, encoding):
     from simcoflow3d_gb300.projection import Projection
     w = W.config(name, n=n)
     p = Projection.for_workload(w, rel_tol=1e-10)
@@ -35,10 +37,11 @@ def test_device_fields_to_vtr(gpu_lib, tmp_path, name, n):
     axes = _axes(w)
     shape = (w.imax, w.jmax, w.kmax)
     f_gpu, f_ref = str(tmp_path / "gpu.vtr"), str(tmp_path / "ref.vtr")
-    st = OUT.write_vtr(f_gpu, shape, axes, gpu_fields)
-    V.write_vtr(f_ref, shape, axes, host_fields)
+    st = OUT.write_vtr(f_gpu, shape, axes, gpu_fields, encoding=encoding)
+    (V.write_vtr if encoding == "appended" else V.write_vtr_binary)(f_ref, shape, axes, host_fields)
     assert open(f_gpu, "rb").read() == open(f_ref, "rb").read()
-    assert st["gpu_launches"] == 8 and st["bytes_file"] == len(open(f_gpu, "rb").read())
+    launches = 8 if encoding == "appended" else 16
+    assert st["gpu_launches"] == launches and st["bytes_file"] == len(open(f_gpu, "rb").read())
     got = OUT.read_vtr(f_gpu)
     assert np.array_equal(got["u"], u[1:-1, 1:-1, 1:-1].astype(np.float32))
     p.close()
