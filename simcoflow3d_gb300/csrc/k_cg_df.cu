@@ -11,17 +11,14 @@
 // explicitly rounded intrinsic, so that no contraction changes them.  Each
 // vector occupies the 8 bytes per cell of its FP64 counterpart (the FP64
 // buffers are reused), so memory traffic is unchanged.  The dot products of
-// the iteration -- (p, Ap), (r, z) and (r, r) -- are accumulated in FP64 per
-// thread, per block and across blocks, with one FP64 FMA per cell and dot:
-// the product of the hi parts, which is exact in FP64 (24 x 24 bits), is
-// added to the FP64 sum; the hi x lo cross terms, 2^-24 of it, are formed
-// and summed in FP32 beside it and added to the FP64 sum once per thread
-// (their rounding is 2^-48 of the product, the precision of the
-// double-float values themselves; lo x lo, 2^-48, is left out).  The
-// FP32 -> FP64 widening is exact and runs on the integer pipe.  The
-// solution is converted back to FP64 at the end of a CG round and its
-// residual is recomputed in FP64, so the stopping test on the true residual
-// is unchanged.
+// the iteration -- (p, Ap), (r, z) and (r, r) -- are FP64: each cell's
+// double-float values are widened to FP64 (the FP32 -> FP64 widening is done
+// with integer operations, which are exact), multiplied with an FP64 FMA and
+// accumulated in FP64 per thread, per block and across blocks.  That is two
+// to four FP64 operations per cell and dot, which the memory-bound kernels
+// hide.  The solution is converted back to FP64 at the end of a CG round and
+// its residual is recomputed in FP64, so the stopping test on the true
+// residual is unchanged.
 #include "scf_kernels.h"
 
 namespace {
@@ -110,7 +107,6 @@ __global__ void __launch_bounds__(128) k_spmv_df(DfOp A, const float2 *__restric
 {
     DF_ZCHUNK(A);
     double v = 0.0;
-    float cv = 0.f;
     float2 sq = make_float2(0.f, 0.f);
     if (in) {
         const int sy = A.hi.sy, sz = A.hi.sz;
@@ -132,14 +128,12 @@ __global__ void __launch_bounds__(128) k_spmv_df(DfOp A, const float2 *__restric
             const float2 s = dadd(dadd(sx, syy), sz2);
             const float2 y = dadd(dmul(cf(A.hi.diag, A.dlo, c), x0), dneg(s));
             q[c] = y;
-            cv = __fmaf_rn(x0.x, y.y, __fmaf_rn(x0.y, y.x, cv));
-            if (par) { v2 = fma(widen(x0.x), widen(y.x), v2); sq2 = dadd(sq2, y); }
-            else { v = fma(widen(x0.x), widen(y.x), v); sq = dadd(sq, y); }
+            if (par) { v2 = fma(dwide(x0), dwide(y), v2); sq2 = dadd(sq2, y); }
+            else { v = fma(dwide(x0), dwide(y), v); sq = dadd(sq, y); }
             par ^= 1;
             xm = x0; x0 = xp; tb = tt;
         }
         v += v2;
-        v += widen(cv);
         sq = dadd(sq, sq2);
     }
     double dv = block_sum(v);
@@ -151,8 +145,8 @@ __global__ void __launch_bounds__(128) k_spmv_df(DfOp A, const float2 *__restric
     }
 }
 
-// (r, z) for beta: r double-float, z the FP32 preconditioned residual; r.hi
-// z exact in the FP64 sum, r.lo z in FP32 beside it
+// (r, z) for beta: r double-float, z the FP32 preconditioned residual; FP64
+// products and sums
 __global__ void __launch_bounds__(128) k_dot_rz_df(DfOp A, const float2 *__restrict__ r, const float *__restrict__ z,
                                                    double *__restrict__ part)
 {
@@ -161,21 +155,13 @@ __global__ void __launch_bounds__(128) k_dot_rz_df(DfOp A, const float2 *__restr
     if (in) {
         const int sy = A.hi.sy, sz = A.hi.sz;
         int c = i + sy * j + sz * k0;
-        float cv = 0.f;
-        for (int k = k0; k <= k1; ++k, c += sz) {
-            const float2 rr = ld(r, c);
-            const float zz = z[c];
-            v = fma(widen(rr.x), widen(zz), v);
-            cv = __fmaf_rn(rr.y, zz, cv);
-        }
-        v += widen(cv);
+        for (int k = k0; k <= k1; ++k, c += sz) v = fma(dwide(ld(r, c)), widen(z[c]), v);
     }
     v = block_sum(v);
     if (thread_linear() == 0) part[block_linear()] = v;
 }
 
-// x += alpha p, r -= alpha (q - mean q), (r, r) (hi x hi in the FP64 sum,
-// 2 hi x lo in FP32 beside it); also the FP32 copy
+// x += alpha p, r -= alpha (q - mean q), (r, r) in FP64; also the FP32 copy
 // of r (its hi part) for the V-cycle and, when x0 is given, the first
 // point-Jacobi smoothing step from a zero guess, x0 = first D^-1 r.
 __global__ void __launch_bounds__(128) k_cg_update_df(DfOp A, float2 *__restrict__ x, float2 *__restrict__ r,
@@ -185,7 +171,6 @@ __global__ void __launch_bounds__(128) k_cg_update_df(DfOp A, float2 *__restrict
 {
     DF_ZCHUNK(A);
     double v = 0.0;
-    float cv = 0.f;
     if (in) {
         const float2 al = dfrom(scal[S_ALPHA]), mal = dneg(al), qm = dfrom(scal[S_QMEAN]);
         const int sy = A.hi.sy, sz = A.hi.sz;
@@ -199,10 +184,9 @@ __global__ void __launch_bounds__(128) k_cg_update_df(DfOp A, float2 *__restrict
             r[c] = rn;
             rlow[c] = rn.x;
             if (x0) x0[c] = first * (dg > 0.f ? __frcp_rn(dg) : 0.f) * rn.x;
-            v = fma(widen(rn.x), widen(rn.x), v);
-            cv = __fmaf_rn(__fadd_rn(rn.x, rn.x), rn.y, cv);
+            const double rd = dwide(rn);
+            v = fma(rd, rd, v);
         }
-        v += widen(cv);
     }
     v = block_sum(v);
     if (thread_linear() == 0) part[block_linear()] = v;
