@@ -118,6 +118,17 @@ __device__ __noinline__ double beta_interface(double phic, double phin, double t
     return pc == 1 ? lam * betam + (1.0 - lam) * betap : lam * betap + (1.0 - lam) * betam;
 }
 
+// The B face of cell k has the inputs of the T face of cell k-1 whenever both
+// cells are in the same phase (Dp(k-1), DGrid(k-1) and the phase's beta):
+// before the B face's own memo, it looks at the T face's memo, which still
+// holds cell k-1's result when the B face of cell k is formed.
+__device__ __forceinline__ bool memo_hit(const CoefMemo &m, double dp, double dg, double beta)
+{
+    return m.valid && (unsigned long long)__double_as_longlong(dp) == m.dp &&
+           (unsigned long long)__double_as_longlong(dg) == m.dg &&
+           (unsigned long long)__double_as_longlong(beta) == m.beta;
+}
+
 __device__ __forceinline__ double coef_memo(CoefMemo &m, double dp, double dg, double beta, double betap,
                                             double betam)
 {
@@ -230,7 +241,9 @@ __global__ void __launch_bounds__(128) k_pocoef(AsmArgs a)
                         if (pc == 1) { carryW[f] = beta; maskW |= 1u << f; }
                         else { carryD[f] = beta; maskD |= 1u << f; }
                     }
-                    coef = coef_memo(memo[f], dp, dg, beta, a.betap, a.betam);
+                    coef = f == 2 && memo_hit(memo[5], dp, dg, beta)
+                               ? memo[5].coef
+                               : coef_memo(memo[f], dp, dg, beta, a.betap, a.betam);
                 }
             }
             a.pocoef[nc + (long long)d.n * f] = coef;
@@ -343,18 +356,27 @@ __device__ __forceinline__ bool finite_bits(double x)
 __device__ __forceinline__ unsigned long long bits(double x) { return (unsigned long long)__double_as_longlong(x); }
 
 // ((p*area)*d1)*d2, the face term of SetPoissonMatrix, memoised on its inputs.
+// The memo also keeps the partial product (p*ar)*d1: along a column only d2
+// (the cell's dz for the x and y faces) often changes in its last bits, and
+// then one multiplication finishes the term, in the expression's own order.
 struct TermMemo {
     unsigned long long p, ar, d1, d2;
-    double t;
+    double pd1, t;
     bool valid;
 };
-__device__ __noinline__ double prod4(double p, double ar, double d1, double d2) { return p * ar * d1 * d2; }
+__device__ __noinline__ double prod3(double p, double ar, double d1) { return p * ar * d1; }
 __device__ __noinline__ double mul_slow(double a, double b) { return a * b; }
 __device__ __forceinline__ double term_memo(TermMemo &m, double p, double ar, double d1, double d2)
 {
-    if (!m.valid || bits(p) != m.p || bits(ar) != m.ar || bits(d1) != m.d1 || bits(d2) != m.d2) {
-        m.p = bits(p); m.ar = bits(ar); m.d1 = bits(d1); m.d2 = bits(d2); m.valid = true;
-        m.t = prod4(p, ar, d1, d2);
+    const bool head = m.valid && bits(p) == m.p && bits(ar) == m.ar && bits(d1) == m.d1;
+    if (!head) {
+        m.p = bits(p); m.ar = bits(ar); m.d1 = bits(d1); m.valid = true;
+        m.pd1 = prod3(p, ar, d1);
+        m.d2 = bits(d2);
+        m.t = mul_slow(m.pd1, d2);
+    } else if (bits(d2) != m.d2) {
+        m.d2 = bits(d2);
+        m.t = mul_slow(m.pd1, d2);
     }
     return m.t;
 }
@@ -441,7 +463,7 @@ __device__ __forceinline__ void op_issue(const AsmArgs &a, double *sd, int *si, 
 // inputs of cell k+1 are copied into shared memory while cell k is
 // computed (two stages).
 template <bool MIXED>
-__global__ void __launch_bounds__(OP_THREADS) k_operator(AsmArgs a, OpArgs o)
+__global__ void __launch_bounds__(OP_THREADS, 3) k_operator(AsmArgs a, OpArgs o)
 {
     extern __shared__ __align__(16) unsigned char op_smem[];
     double *sd0 = (double *)op_smem;
@@ -455,7 +477,9 @@ __global__ void __launch_bounds__(OP_THREADS) k_operator(AsmArgs a, OpArgs o)
     const int *fl = a.flag;
     TermMemo tm[6];
 #pragma unroll
-    for (int f = 0; f < 6; ++f) { tm[f].valid = false; tm[f].p = tm[f].ar = tm[f].d1 = tm[f].d2 = 0ull; tm[f].t = 0.0; }
+    for (int f = 0; f < 6; ++f) {
+        tm[f].valid = false; tm[f].p = tm[f].ar = tm[f].d1 = tm[f].d2 = 0ull; tm[f].pd1 = tm[f].t = 0.0;
+    }
     // memo of the row (diag and dependants) on the six terms and the
     // Neumann-face mask
     unsigned long long rt[6] = {0, 0, 0, 0, 0, 0};
@@ -502,7 +526,14 @@ __global__ void __launch_bounds__(OP_THREADS) k_operator(AsmArgs a, OpArgs o)
         const double nS = SV(V_NS), nN = SV(V_NN);
         const double tB = SV(V_TB), tT = SV(V_TT);
         const double t1 = term_memo(tm[0], p1, eW, dy, dz), t2 = term_memo(tm[1], p2, nS, dx, dz);
-        const double t3 = term_memo(tm[2], p3, tB, dx, dy), t4 = term_memo(tm[3], p4, eE, dy, dz);
+        // the B term of cell k is the T term of cell k-1 when its inputs are
+        // (same coefficient, the same TEArea entry, and dx, dy of a tensor
+        // grid): tm[5] still holds cell k-1's T term here
+        const double t3 = (tm[5].valid && bits(p3) == tm[5].p && bits(tB) == tm[5].ar && bits(dx) == tm[5].d1 &&
+                           bits(dy) == tm[5].d2)
+                              ? tm[5].t
+                              : term_memo(tm[2], p3, tB, dx, dy);
+        const double t4 = term_memo(tm[3], p4, eE, dy, dz);
         const double t5 = term_memo(tm[4], p5, nN, dx, dz), t6 = term_memo(tm[5], p6, tT, dx, dy);
         const bool bnd = i == 1 || j == 1 || k == 1 || i == d.I || j == d.J || k == d.K;
         const int nb = (fl[0] == 1 && i == 1 ? 1 : 0) | (fl[2] == 1 && j == 1 ? 2 : 0) |
