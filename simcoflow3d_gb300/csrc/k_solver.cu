@@ -468,52 +468,6 @@ __global__ void __launch_bounds__(256) k_cheb_step(LevelView<T> L, const T *__re
     if (dout) dout[c] = dn;
 }
 
-// The same step for the large levels with each thread marching KM cells of
-// one (i, j) column: x at k-1 and k and cT at k-1 stay in registers, so a
-// cell issues 11 loads instead of 14, and the loads of the next cells are in
-// flight while the current one is computed.  The arithmetic of each cell is
-// that of k_cheb_step, in the same order.
-constexpr int CHEB_KM = 16;
-
-template <typename T>
-__global__ void __launch_bounds__(256) k_cheb_march(LevelView<T> L, const T *__restrict__ b, const T *xin,
-                                                    const T *dprev, T *__restrict__ xout, T *dout, T c1, T c2)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    if (i > L.n0 || j > L.n1) return;
-    const int k0 = blockIdx.z * CHEB_KM + 1, k1 = min(k0 + CHEB_KM - 1, L.n2);
-    const int sy = L.sy, sz = L.sz;
-    int c = i + sy * j + sz * k0;
-    T xm = xin[c - sz], x0 = xin[c], tb = L.cT[c - sz];
-#pragma unroll 4
-    for (int k = k0; k <= k1; ++k, c += sz) {
-        const T xp = xin[c + sz], tt = L.cT[c];
-        const T ax = L.diag[c] * x0 - (L.cE[c] * xin[c + 1] + L.cE[c - 1] * xin[c - 1] + L.cN[c] * xin[c + sy] +
-                                       L.cN[c - sy] * xin[c - sy] + tt * xp + tb * xm);
-        const T r = b[c] - ax;
-        const T dn = c1 * dprev[c] + c2 * dinv_at(L, c) * r;
-        xout[c] = x0 + dn;
-        if (dout) dout[c] = dn;
-        xm = x0; x0 = xp; tb = tt;
-    }
-}
-
-// One Chebyshev step of level F: the marching kernel on FP32 levels of at
-// least 64^3 cells, the one-cell-per-thread kernel otherwise.
-template <typename T>
-void cheb_step(const MgLevel<T> &F, const T *b, const T *xin, const T *dprev, T *xout, T *dout, T c1, T c2,
-               cudaStream_t st)
-{
-    if (sizeof(T) == 4 && (long long)F.n0 * F.n1 * F.n2 >= (1LL << 18)) {
-        const dim3 blk(32, 8, 1), grd((F.n0 + 31) / 32, (F.n1 + 7) / 8, (F.n2 + CHEB_KM - 1) / CHEB_KM);
-        k_cheb_march<T><<<grd, blk, 0, st>>>(F.view(), b, xin, dprev, xout, dout, c1, c2);
-    } else {
-        Launch3 lf = launch_interior(F.n0, F.n1, F.n2);
-        k_cheb_step<T><<<lf.grid, lf.block, 0, st>>>(F.view(), b, xin, dprev, xout, dout, c1, c2);
-    }
-}
-
 // Chebyshev step with z-line Jacobi blocks: the preconditioner of the
 // Chebyshev iteration is T^-1, T the block diagonal of A whose blocks are
 // segments of LINE_SEG cells along k of one (i, j) column (the diagonal and
@@ -923,7 +877,7 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
             const T *dprev = (s == 1) ? xa : F.d;
             T *dout = (s == cc.degree - 1) ? nullptr : F.d;
             const int id = l == 0 ? kt_begin(kt, KC_SMOOTH, st, smooth_bytes<T>(F, s == 1, dout != nullptr)) : -1;
-            cheb_step<T>(F, F.b, xa, dprev, xb, dout, (T)cc.c1[s], (T)cc.c2[s], st);
+            k_cheb_step<T><<<lf.grid, lf.block, 0, st>>>(v, F.b, xa, dprev, xb, dout, (T)cc.c1[s], (T)cc.c2[s]);
             kt_end(kt, id, st);
             *launches += 1;
             T *tmp = xa; xa = xb; xb = tmp;
@@ -974,7 +928,8 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
             k_prolong<T><<<lf.grid, lf.block, 0, st>>>(v, F.active, xa, C.view(), cur[l + 1], F.f0 - 1, F.f1 - 1,
                                                        F.f2 - 1);
             // first post-smoothing step from x: the previous update term is 0
-            cheb_step<T>(F, F.b, xa, xa, xb, more ? F.d : nullptr, T(0), (T)cc.first, st);
+            k_cheb_step<T><<<lf.grid, lf.block, 0, st>>>(v, F.b, xa, xa, xb, more ? F.d : nullptr, T(0),
+                                                         (T)cc.first);
             kt_end(kt, idp, st);
             *launches += 2;
         } else {
@@ -988,7 +943,8 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
         for (int s = 1; s < cc.degree; ++s) {
             const bool last_step = s == cc.degree - 1;
             const int id = l == 0 ? kt_begin(kt, KC_SMOOTH, st, smooth_bytes<T>(F, false, !last_step)) : -1;
-            cheb_step<T>(F, F.b, xa, F.d, xb, last_step ? nullptr : F.d, (T)cc.c1[s], (T)cc.c2[s], st);
+            k_cheb_step<T><<<lf.grid, lf.block, 0, st>>>(v, F.b, xa, F.d, xb, last_step ? nullptr : F.d,
+                                                         (T)cc.c1[s], (T)cc.c2[s]);
             kt_end(kt, id, st);
             *launches += 1;
             T *tmp = xa; xa = xb; xb = tmp;
@@ -1003,8 +959,9 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
 template <typename T>
 void probe_smooth(MgLevel<T> &F, const ChebCoef &cc, cudaStream_t st)
 {
+    Launch3 lf = launch_interior(F.n0, F.n1, F.n2);
     const int s = cc.degree > 1 ? 1 : 0;
-    cheb_step<T>(F, F.b, F.x, F.d, F.xb, F.d, (T)cc.c1[s], (T)cc.c2[s], st);
+    k_cheb_step<T><<<lf.grid, lf.block, 0, st>>>(F.view(), F.b, F.x, F.d, F.xb, F.d, (T)cc.c1[s], (T)cc.c2[s]);
 }
 
 template <typename T>
