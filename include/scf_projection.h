@@ -269,10 +269,13 @@ int scf_debug_operator_f32(scf_ctx *ctx, float *diag_hi, float *e_hi, float *n_h
  * touched once per cell).  kernel: SCF_K_SMOOTH (fine-level Chebyshev step
  * of the V-cycle, in its precision), SCF_K_SPMV (FP64 CG operator apply with
  * its dot product), SCF_K_RESTRICT (fine residual + restriction),
- * SCF_K_PROLONG (prolongation + first post-smoothing step), SCF_K_CGUPDATE
- * (FP64 x/r update with its dot product).  Needs a previous run.          */
+ * SCF_K_PROLONG (prolongation + first post-smoothing step; on large FP32
+ * levels fused with the next step), SCF_K_CGUPDATE (FP64 x/r update with
+ * its dot product), SCF_K_SMOOTH2 (two fused fine-level Chebyshev steps of
+ * a SCF_PREC_MIXED context).  Needs a previous run.                        */
 enum scf_kernel_class {
-    SCF_K_SMOOTH = 0, SCF_K_SPMV = 1, SCF_K_RESTRICT = 2, SCF_K_PROLONG = 3, SCF_K_CGUPDATE = 4
+    SCF_K_SMOOTH = 0, SCF_K_SPMV = 1, SCF_K_RESTRICT = 2, SCF_K_PROLONG = 3, SCF_K_CGUPDATE = 4,
+    SCF_K_SMOOTH2 = 5
 };
 int scf_debug_time_kernel(scf_ctx *ctx, int kernel, int reps, double *ms_per_launch,
                           double *bytes_per_launch);
@@ -341,6 +344,13 @@ int scf_abi_version(void);
  * holds, so a test can check that a failed create leaks none.             */
 int     scf_debug_fail_device_alloc(int64_t nth);
 int64_t scf_debug_device_buffers(void);
+
+/* FP32 V-cycle levels of at least 2^18 cells apply their Chebyshev steps in
+ * fused pairs, one pass over the level for two steps (on = 1, the default),
+ * or one step per pass (on = 0); both give the same bits.  planes: k-planes
+ * per thread block of the fused kernel (0: the default, 32).  Process-wide;
+ * applies from the next solve of every context.                           */
+int scf_debug_smoother_pairs(int on, int planes);
 
 #ifdef __cplusplus
 }

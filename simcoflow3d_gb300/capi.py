@@ -34,6 +34,7 @@ SCF_K_SPMV = 1
 SCF_K_RESTRICT = 2
 SCF_K_PROLONG = 3
 SCF_K_CGUPDATE = 4
+SCF_K_SMOOTH2 = 5
 
 SCF_PREC_FP64 = 0
 SCF_PREC_MIXED = 1

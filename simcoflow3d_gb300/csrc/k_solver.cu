@@ -10,6 +10,8 @@
 // diagonal is the sum of the coarse couplings plus half the children's
 // Dirichlet terms.  Dot products are reduced per block and then in one block
 // in a fixed order, so results are bitwise reproducible.
+#include <cuda_pipeline.h>
+
 #include "scf_kernels.h"
 
 #define INTERIOR_IJK(L)                                       \
@@ -455,6 +457,34 @@ __global__ void __launch_bounds__(256) k_cheb_first(LevelView<T> L, const T *__r
     if (in) x[c] = coef * dinv_at(L, c) * b[c];
 }
 
+// Arithmetic of one Chebyshev update with every operation spelled out (no
+// contraction left to the compiler), so that the one-step kernel and the
+// fused two-step kernel give the same bits: the six neighbour products
+// summed by FMA in the order E, W, N, S, T, B; A x = diag x - s;
+// r = b - A x; the update dn = (c2 dinv) r + c1 dprev.
+__device__ __forceinline__ float fx_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double fx_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float fx_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double fx_fma(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float fx_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double fx_sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float fx_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double fx_add(double a, double b) { return __dadd_rn(a, b); }
+
+template <typename T>
+__device__ __forceinline__ T cheb_update(T b, T dg, T dinv, T x0, T xe, T xw, T xn, T xs, T xt, T xb, T ce, T cw,
+                                         T cn, T cs, T ct, T cb, T dprev, T c1, T c2)
+{
+    T s = fx_mul(ce, xe);
+    s = fx_fma(cw, xw, s);
+    s = fx_fma(cn, xn, s);
+    s = fx_fma(cs, xs, s);
+    s = fx_fma(ct, xt, s);
+    s = fx_fma(cb, xb, s);
+    const T r = fx_sub(b, fx_fma(dg, x0, -s));
+    return fx_fma(fx_mul(c2, dinv), r, fx_mul(c1, dprev));
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_cheb_step(LevelView<T> L, const T *__restrict__ b,
                                                    const T *__restrict__ xin, const T *dprev,
@@ -462,10 +492,263 @@ __global__ void __launch_bounds__(256) k_cheb_step(LevelView<T> L, const T *__re
 {
     INTERIOR_IJK(L);
     if (!in) return;
-    const T r = b[c] - apply_row(L, xin, c);
-    const T dn = c1 * dprev[c] + c2 * dinv_at(L, c) * r;
-    xout[c] = xin[c] + dn;
+    const int sy = L.sy, sz = L.sz;
+    const T x0 = xin[c];
+    const T dn = cheb_update(b[c], L.diag[c], dinv_at(L, c), x0, xin[c + 1], xin[c - 1], xin[c + sy], xin[c - sy],
+                             xin[c + sz], xin[c - sz], L.cE[c], L.cE[c - 1], L.cN[c], L.cN[c - sy], L.cT[c],
+                             L.cT[c - sz], dprev[c], c1, c2);
+    xout[c] = fx_add(x0, dn);
     if (dout) dout[c] = dn;
+}
+
+// ---------------------------------------------------------------------------
+// Two Chebyshev steps in one pass over a large FP32 level (2.5-D temporal
+// blocking).  A block owns a tile of 32 x 8 (i, j) columns and marches along
+// k over `planes` planes.  For plane kk it
+//   1. copies the operator, right-hand side and previous update of plane
+//      kk + 1 on the tile with a one-cell halo into a five-plane ring
+//      (cp.async, in flight while plane kk is computed), and loads x of
+//      plane kk + 2 with a two-cell halo through registers (prolonged from
+//      the coarse correction first when asked, as k_prolong does);
+//   2. applies the first step on the 34 x 10 cells of plane kk (ghost cells
+//      give 0, the value the one-step kernel leaves there) into a
+//      three-plane ring in shared memory;
+//   3. applies the second step on the 32 x 8 cells of plane kk - 1.
+// Each array is read from DRAM about once per pass (halo columns come from
+// L2), so two steps move about the bytes of one.  Both steps go through
+// cheb_update: the result is that of two k_cheb_step launches, bit for bit.
+// The output x must not be the input x, nor dout the previous update when
+// both are given: neighbouring tiles read their halos from them.
+constexpr int C2_TX = 32, C2_TY = 8, C2_THREADS = C2_TX * C2_TY;
+constexpr int C2_EX = C2_TX + 2, C2_EY = C2_TY + 2, C2_NE = C2_EX * C2_EY;  // first-step cells
+constexpr int C2_XX = C2_TX + 4, C2_XY = C2_TY + 4, C2_NX = C2_XX * C2_XY;  // x, two-cell halo
+constexpr int C2_NCE = (C2_EX + 1) * C2_EY;                              // cE from column i - 1
+constexpr int C2_NCN = C2_EX * (C2_EY + 1);                              // cN from row j - 1
+constexpr int C2_NH = C2_NE - C2_THREADS;                                // halo cells of step 1
+constexpr int C2_RD = 5, C2_RX = 4, C2_R1 = 3;                           // ring depths (planes)
+constexpr int C2_B = 0, C2_D = C2_NE, C2_P = 2 * C2_NE, C2_T = 3 * C2_NE, C2_E = 4 * C2_NE,
+              C2_N = 4 * C2_NE + C2_NCE, C2_SLOT = 4 * C2_NE + C2_NCE + C2_NCN;
+constexpr size_t C2_SMEM = sizeof(float) * (C2_RD * C2_SLOT + C2_RX * C2_NX + C2_R1 * C2_NE);
+constexpr int C2_PLANES = 32;
+static_assert(C2_NH <= C2_THREADS && C2_NX <= 2 * C2_THREADS, "one halo cell and two x cells per thread");
+
+struct PairArgs {
+    LevelView<float> F;
+    const float *b, *x;
+    const float *dprev;          // nullptr: the first step's previous update is x itself
+    float *xout, *dout;          // dout nullptr: the second step's update is not kept
+    const unsigned char *act;    // non-null: x += e(parent) on the active cells first
+    const float *e;
+    int esy, esz, s0, s1, s2;
+    float c1a, c2a, c1b, c2b;
+    int planes;
+};
+
+__device__ __forceinline__ bool c2_in(const LevelView<float> &F, int i, int j)
+{
+    return (unsigned)i <= (unsigned)(F.n0 + 1) && (unsigned)j <= (unsigned)(F.n1 + 1);
+}
+
+// Asynchronous copies of plane P's first-step inputs into one ring slot
+// (only cells of the ghosted array; the others are never read).
+__device__ __forceinline__ void c2_stage(const PairArgs &a, float *slot, int i0, int j0, int P, int tid)
+{
+    const LevelView<float> &F = a.F;
+    if (P < 0 || P > F.n2) return;
+    const int base = F.sz * P;
+    for (int q = tid; q < C2_NE; q += C2_THREADS) {
+        const int qy = q / C2_EX, qx = q - qy * C2_EX;
+        const int i = i0 - 1 + qx, j = j0 - 1 + qy;
+        if (!c2_in(F, i, j)) continue;
+        const int c = base + i + F.sy * j;
+        __pipeline_memcpy_async(slot + C2_B + q, a.b + c, sizeof(float));
+        __pipeline_memcpy_async(slot + C2_D + q, F.diag + c, sizeof(float));
+        if (a.dprev) __pipeline_memcpy_async(slot + C2_P + q, a.dprev + c, sizeof(float));
+        __pipeline_memcpy_async(slot + C2_T + q, F.cT + c, sizeof(float));
+    }
+    for (int q = tid; q < C2_NCE; q += C2_THREADS) {
+        const int qy = q / (C2_EX + 1), qx = q - qy * (C2_EX + 1);
+        const int i = i0 - 2 + qx, j = j0 - 1 + qy;
+        if (c2_in(F, i, j)) __pipeline_memcpy_async(slot + C2_E + q, F.cE + base + i + F.sy * j, sizeof(float));
+    }
+    for (int q = tid; q < C2_NCN; q += C2_THREADS) {
+        const int qy = q / C2_EX, qx = q - qy * C2_EX;
+        const int i = i0 - 1 + qx, j = j0 - 2 + qy;
+        if (c2_in(F, i, j)) __pipeline_memcpy_async(slot + C2_N + q, F.cN + base + i + F.sy * j, sizeof(float));
+    }
+}
+
+// x of plane X on this thread's two cells of the 36 x 12 tile (0 outside
+// the ghosted array), with the coarse correction of the active interior
+// cells when prolonging.
+struct C2X {
+    float v[2];
+};
+
+__device__ __forceinline__ C2X c2_load_x(const PairArgs &a, int i0, int j0, int X, int tid)
+{
+    const LevelView<float> &F = a.F;
+    C2X r;
+    float e[2] = {0.f, 0.f};
+    bool on[2] = {false, false};
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        r.v[h] = 0.f;
+        const int q = tid + h * C2_THREADS;
+        if (q >= C2_NX || X < 0 || X > F.n2 + 1) continue;
+        const int qy = q / C2_XX, qx = q - qy * C2_XX;
+        const int i = i0 - 2 + qx, j = j0 - 2 + qy;
+        if (!c2_in(F, i, j)) continue;
+        const int c = i + F.sy * j + F.sz * X;
+        r.v[h] = a.x[c];
+        if (a.act && i >= 1 && i <= F.n0 && j >= 1 && j <= F.n1 && X >= 1 && X <= F.n2) {
+            on[h] = a.act[c] != 0;
+            e[h] = a.e[(((i - 1) >> a.s0) + 1) + a.esy * (((j - 1) >> a.s1) + 1) + a.esz * (((X - 1) >> a.s2) + 1)];
+        }
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+        if (on[h]) r.v[h] = fx_add(r.v[h], e[h]);
+    return r;
+}
+
+__device__ __forceinline__ void c2_store_x(float *sx, const C2X &r, int tid)
+{
+    sx[tid] = r.v[0];
+    if (tid + C2_THREADS < C2_NX) sx[tid + C2_THREADS] = r.v[1];
+}
+
+// First step at plane P on cell (ex, ey) of the 34 x 10 tile: writes x
+// after the step into o1 and returns the update.
+__device__ __forceinline__ float c2_first(const PairArgs &a, const float *dc, const float *dm, const float *xm,
+                                          const float *x0, const float *xp, float *o1, int ex, int ey, int i0,
+                                          int j0, int P)
+{
+    const LevelView<float> &F = a.F;
+    const int i = i0 - 1 + ex, j = j0 - 1 + ey, q = ex + C2_EX * ey;
+    if (i < 1 || i > F.n0 || j < 1 || j > F.n1 || P < 1 || P > F.n2) {
+        o1[q] = 0.f;
+        return 0.f;
+    }
+    const int qx = (ex + 1) + C2_XX * (ey + 1);
+    const float xc = x0[qx], dg = dc[C2_D + q];
+    const float dn = cheb_update(dc[C2_B + q], dg, dg > 0.f ? __frcp_rn(dg) : 0.f, xc, x0[qx + 1], x0[qx - 1],
+                                 x0[qx + C2_XX], x0[qx - C2_XX], xp[qx], xm[qx],
+                                 dc[C2_E + (ex + 1) + (C2_EX + 1) * ey], dc[C2_E + ex + (C2_EX + 1) * ey],
+                                 dc[C2_N + ex + C2_EX * (ey + 1)], dc[C2_N + q], dc[C2_T + q], dm[C2_T + q],
+                                 a.dprev ? dc[C2_P + q] : xc, a.c1a, a.c2a);
+    o1[q] = fx_add(xc, dn);
+    return dn;
+}
+
+__global__ void __launch_bounds__(C2_THREADS, 4) k_cheb_pair(PairArgs a)
+{
+    extern __shared__ __align__(16) float c2_smem[];
+    float *sd = c2_smem;                   // C2_RD slots of first-step inputs
+    float *sx = sd + C2_RD * C2_SLOT;      // C2_RX planes of x
+    float *s1 = sx + C2_RX * C2_NX;        // C2_R1 planes of x after the first step
+    const LevelView<float> &F = a.F;
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + C2_TX * ty;
+    const int i0 = blockIdx.x * C2_TX + 1, j0 = blockIdx.y * C2_TY + 1;
+    const int k0 = blockIdx.z * a.planes + 1, k1 = min(k0 + a.planes - 1, F.n2);
+    // planes from k0 - 2 on: slot indices stay non-negative
+    auto dslot = [&](int P) { return sd + ((P + 2) % C2_RD) * C2_SLOT; };
+    auto xslot = [&](int P) { return sx + ((P + 2) % C2_RX) * C2_NX; };
+    auto oslot = [&](int P) { return s1 + ((P + 2) % C2_R1) * C2_NE; };
+    // this thread's halo cell of the first step (the ring around the 32 x 8 tile)
+    int hx = -1, hy = -1;
+    if (tid < C2_EX) { hx = tid; hy = 0; }
+    else if (tid < 2 * C2_EX) { hx = tid - C2_EX; hy = C2_EY - 1; }
+    else if (tid < 2 * C2_EX + C2_TY) { hx = 0; hy = tid - 2 * C2_EX + 1; }
+    else if (tid < C2_NH) { hx = C2_EX - 1; hy = tid - 2 * C2_EX - C2_TY + 1; }
+
+    c2_stage(a, dslot(k0 - 2), i0, j0, k0 - 2, tid);
+    __pipeline_commit();
+    c2_stage(a, dslot(k0 - 1), i0, j0, k0 - 1, tid);
+    __pipeline_commit();
+    for (int X = k0 - 2; X <= k0; ++X) c2_store_x(xslot(X), c2_load_x(a, i0, j0, X, tid), tid);
+
+    float d1 = 0.f;     // first-step update of this thread's column, plane below
+    for (int kk = k0 - 1; kk <= k1 + 1; ++kk) {
+        if (kk + 1 <= k1 + 1) c2_stage(a, dslot(kk + 1), i0, j0, kk + 1, tid);
+        __pipeline_commit();
+        C2X xr = {};
+        if (kk <= k1) xr = c2_load_x(a, i0, j0, kk + 2, tid);
+        __pipeline_wait_prior(1);
+        __syncthreads();
+        const float *dc = dslot(kk), *dm = dslot(kk - 1);
+        const float *xm = xslot(kk - 1), *x0 = xslot(kk), *xp = xslot(kk + 1);
+        float *o1 = oslot(kk);
+        const float dn1 = c2_first(a, dc, dm, xm, x0, xp, o1, tx + 1, ty + 1, i0, j0, kk);
+        if (hx >= 0) c2_first(a, dc, dm, xm, x0, xp, o1, hx, hy, i0, j0, kk);
+        __syncthreads();
+        const int Q = kk - 1, i = i0 + tx, j = j0 + ty;
+        if (Q >= k0 && i <= F.n0 && j <= F.n1) {
+            const float *qc = dslot(Q), *qm = dslot(Q - 1);
+            const float *y0 = oslot(Q), *ym = oslot(Q - 1), *yp = oslot(Q + 1);
+            const int q = (tx + 1) + C2_EX * (ty + 1);
+            const float xc = y0[q], dg = qc[C2_D + q];
+            const float dn = cheb_update(qc[C2_B + q], dg, dg > 0.f ? __frcp_rn(dg) : 0.f, xc, y0[q + 1], y0[q - 1],
+                                         y0[q + C2_EX], y0[q - C2_EX], yp[q], ym[q],
+                                         qc[C2_E + (tx + 2) + (C2_EX + 1) * (ty + 1)],
+                                         qc[C2_E + (tx + 1) + (C2_EX + 1) * (ty + 1)],
+                                         qc[C2_N + (tx + 1) + C2_EX * (ty + 2)], qc[C2_N + q], qc[C2_T + q],
+                                         qm[C2_T + q], d1, a.c1b, a.c2b);
+            const int c = i + F.sy * j + F.sz * Q;
+            a.xout[c] = fx_add(xc, dn);
+            if (a.dout) a.dout[c] = dn;
+        }
+        d1 = dn1;
+        if (kk <= k1) c2_store_x(xslot(kk + 2), xr, tid);
+    }
+    __pipeline_wait_prior(0);
+}
+
+// Smoother pairing: on (1, the default) or off (0, one-step kernels only);
+// k-planes per block of the pair kernel.
+static int g_pairs = 1, g_pair_planes = C2_PLANES;
+
+void set_smoother_pairs(int on, int planes)
+{
+    g_pairs = on ? 1 : 0;
+    g_pair_planes = planes > 0 ? planes : C2_PLANES;
+}
+
+int smoother_pairs_state() { return g_pairs + 2 * g_pair_planes; }
+
+template <typename T>
+bool use_pairs(const MgLevel<T> &F)
+{
+    return sizeof(T) == 4 && g_pairs && (long long)F.n0 * F.n1 * F.n2 >= (1LL << 18);
+}
+
+cudaError_t pair_smem_attr()
+{
+    static const cudaError_t rc =
+        cudaFuncSetAttribute(k_cheb_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C2_SMEM);
+    return rc;
+}
+
+// Two Chebyshev steps (c1a, c2a) then (c1b, c2b) of FP32 level F from xin
+// into xout; dprev nullptr means the first step's previous update is xin
+// itself; with C and e, the coarse correction e is first added to xin on
+// the active cells.
+void cheb_pair(const MgLevel<float> &F, const float *xin, const float *dprev, float *xout, float *dout, double c1a,
+               double c2a, double c1b, double c2b, const MgLevel<float> *C, const float *e, cudaStream_t st)
+{
+    PairArgs a;
+    a.F = F.view();
+    a.b = F.b; a.x = xin; a.dprev = dprev; a.xout = xout; a.dout = dout;
+    a.act = C ? F.active : nullptr;
+    a.e = e;
+    a.esy = C ? C->sy : 0; a.esz = C ? C->sz : 0;
+    a.s0 = F.f0 - 1; a.s1 = F.f1 - 1; a.s2 = F.f2 - 1;
+    a.c1a = (float)c1a; a.c2a = (float)c2a; a.c1b = (float)c1b; a.c2b = (float)c2b;
+    a.planes = g_pair_planes;
+    pair_smem_attr();
+    const dim3 blk(C2_TX, C2_TY, 1);
+    const dim3 grd((F.n0 + C2_TX - 1) / C2_TX, (F.n1 + C2_TY - 1) / C2_TY, (F.n2 + a.planes - 1) / a.planes);
+    k_cheb_pair<<<grd, blk, C2_SMEM, st>>>(a);
 }
 
 // Chebyshev step with z-line Jacobi blocks: the preconditioner of the
@@ -833,6 +1116,15 @@ double prolong_bytes(const MgLevel<T> &F, bool writes_d)
     return cells * (2.0 * s + 1.0 + s / 8.0 + (6 + (sizeof(T) == 8 ? 1 : 0) + 1 + (writes_d ? 1 : 0)) * s);
 }
 
+// Algorithmic bytes of a fused pair of steps: b, diag, cE, cN, cT and x
+// read (+ the previous update), x (+ the update) written; when prolonging,
+// the active mask and the coarse correction read.
+double pair_bytes(const MgLevel<float> &F, bool reads_d, bool writes_d, bool prolong)
+{
+    const double cells = (double)F.n0 * F.n1 * F.n2;
+    return cells * (4.0 * (7 + (reads_d ? 1 : 0) + (writes_d ? 1 : 0)) + (prolong ? 1.0 + 4.0 / 8.0 : 0.0));
+}
+
 template <typename T>
 T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, const int *map, int ncoarse,
              bool singular, bool first_done, cudaStream_t st, int *launches, KTimer *kt)
@@ -871,7 +1163,30 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
             k_cheb_first<T><<<lf.grid, lf.block, 0, st>>>(v, F.b, xa, (T)cc.first);
             *launches += 1;
         }
-        for (int s = 1; s < cc.degree; ++s) {
+        int s = 1;
+        if constexpr (sizeof(T) == 4) {
+            // steps 1 and 2 in one pass (step 1's previous update is x
+            // itself), and steps 3 and 4 too when they are the last two
+            const int m = cc.degree - 1;
+            if (use_pairs(F) && m >= 2) {
+                T *dout = m > 2 ? F.d : nullptr;
+                const int id = l == 0 ? kt_begin(kt, KC_SMOOTH2, st, pair_bytes(F, false, dout != nullptr, false)) : -1;
+                cheb_pair(F, xa, nullptr, xb, dout, cc.c1[1], cc.c2[1], cc.c1[2], cc.c2[2], nullptr, nullptr, st);
+                kt_end(kt, id, st);
+                *launches += 1;
+                { T *tmp = xa; xa = xb; xb = tmp; }
+                s = 3;
+                if (m == 4) {
+                    const int id2 = l == 0 ? kt_begin(kt, KC_SMOOTH2, st, pair_bytes(F, true, false, false)) : -1;
+                    cheb_pair(F, xa, F.d, xb, nullptr, cc.c1[3], cc.c2[3], cc.c1[4], cc.c2[4], nullptr, nullptr, st);
+                    kt_end(kt, id2, st);
+                    *launches += 1;
+                    { T *tmp = xa; xa = xb; xb = tmp; }
+                    s = 5;
+                }
+            }
+        }
+        for (; s < cc.degree; ++s) {
             // the first step's previous update is x itself (zero guess); the
             // last step's update is not needed by anything that follows
             const T *dprev = (s == 1) ? xa : F.d;
@@ -923,7 +1238,34 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
             cur[l] = xa;
             continue;
         }
-        if ((long long)F.n0 * F.n1 * F.n2 >= (1LL << 18)) {
+        int s = 1;
+        bool paired = false;
+        if constexpr (sizeof(T) == 4) {
+            // prolongation, the first post-smoothing step (its previous
+            // update term is 0) and step 1 in one pass; steps 2 and 3 too
+            // when they are the last two
+            const int m = cc.degree - 1;
+            if (use_pairs(F) && m >= 1) {
+                T *dout = m >= 2 ? F.d : nullptr;
+                const int idp = l == 0 ? kt_begin(kt, KC_PROLONG, st, pair_bytes(F, false, dout != nullptr, true)) : -1;
+                cheb_pair(F, xa, nullptr, xb, dout, 0.0, cc.first, cc.c1[1], cc.c2[1], &C, cur[l + 1], st);
+                kt_end(kt, idp, st);
+                *launches += 1;
+                { T *tmp = xa; xa = xb; xb = tmp; }
+                s = 2;
+                if (m == 3) {
+                    const int id2 = l == 0 ? kt_begin(kt, KC_SMOOTH2, st, pair_bytes(F, true, false, false)) : -1;
+                    cheb_pair(F, xa, F.d, xb, nullptr, cc.c1[2], cc.c2[2], cc.c1[3], cc.c2[3], nullptr, nullptr, st);
+                    kt_end(kt, id2, st);
+                    *launches += 1;
+                    { T *tmp = xa; xa = xb; xb = tmp; }
+                    s = 4;
+                }
+                paired = true;
+            }
+        }
+        if (paired) {
+        } else if ((long long)F.n0 * F.n1 * F.n2 >= (1LL << 18)) {
             const int idp = l == 0 ? kt_begin(kt, KC_PROLONG, st, prolong_bytes<T>(F, more)) : -1;
             k_prolong<T><<<lf.grid, lf.block, 0, st>>>(v, F.active, xa, C.view(), cur[l + 1], F.f0 - 1, F.f1 - 1,
                                                        F.f2 - 1);
@@ -939,8 +1281,8 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
             kt_end(kt, idp, st);
             *launches += 1;
         }
-        { T *tmp = xa; xa = xb; xb = tmp; }
-        for (int s = 1; s < cc.degree; ++s) {
+        if (!paired) { T *tmp = xa; xa = xb; xb = tmp; }
+        for (; s < cc.degree; ++s) {
             const bool last_step = s == cc.degree - 1;
             const int id = l == 0 ? kt_begin(kt, KC_SMOOTH, st, smooth_bytes<T>(F, false, !last_step)) : -1;
             k_cheb_step<T><<<lf.grid, lf.block, 0, st>>>(v, F.b, xa, F.d, xb, last_step ? nullptr : F.d,
@@ -962,6 +1304,11 @@ void probe_smooth(MgLevel<T> &F, const ChebCoef &cc, cudaStream_t st)
     Launch3 lf = launch_interior(F.n0, F.n1, F.n2);
     const int s = cc.degree > 1 ? 1 : 0;
     k_cheb_step<T><<<lf.grid, lf.block, 0, st>>>(F.view(), F.b, F.x, F.d, F.xb, F.d, (T)cc.c1[s], (T)cc.c2[s]);
+}
+
+void probe_smooth2(MgLevel<float> &F, const ChebCoef &cc, cudaStream_t st)
+{
+    cheb_pair(F, F.x, F.d, F.xb, nullptr, cc.c1[1], cc.c2[1], cc.c1[2], cc.c2[2], nullptr, nullptr, st);
 }
 
 template <typename T>

@@ -244,6 +244,8 @@ int ensure_mg(scf_ctx *ctx)
         DALLOC(ctx->mgmem, L0.b, L0.tot);
         L0.diag = ctx->diag32; L0.dinv = nullptr; L0.cE = ctx->cE32; L0.cN = ctx->cN32; L0.cT = ctx->cT32;
         L0.extra = ctx->extra32; L0.active = ctx->active;
+        // the two-step smoother's shared memory (set here, outside any capture)
+        CK(pair_smem_attr());
     }
     // coarsest dense map
     const int last = ctx->nlev - 1;
@@ -386,6 +388,7 @@ double kernel_bytes(const scf_ctx *ctx, int kernel)
     case SCF_K_RESTRICT: return 6.0 * s * n + s * n / 8.0;                // b,x,diag,cE,cN,cT in; coarse b out
     case SCF_K_PROLONG: return (mixed ? 8.0 : 9.0) * s * n + s * n / 8.0; // + coarse e; x,d out
     case SCF_K_CGUPDATE: return (mixed ? 60.0 : 64.0) * n;                // x,r,p,q,diag|dinv in; x,r,[rlow],x0 out
+    case SCF_K_SMOOTH2: return mixed ? 8.0 * s * n : -1.0;              // b,x,d,diag,cE,cN,cT in; x out
     default: return -1.0;
     }
 }
@@ -518,7 +521,8 @@ void run_iteration(scf_ctx *ctx, MgLevel<T> *L, const ChebCoef &cc, bool singula
     const unsigned long long key = 1ull + (unsigned long long)ctx->mg_gen * 1000003ull +
                                    (unsigned long long)cc.degree * 131ull + (singular ? 7ull : 0ull) +
                                    (ctx->kt.on ? 3ull : 0ull) + (sizeof(T) == 4 ? 11ull : 0ull) +
-                                   (unsigned long long)ctx->nlev * 17ull + (cc.lines ? 5ull : 0ull);
+                                   (unsigned long long)ctx->nlev * 17ull + (cc.lines ? 5ull : 0ull) +
+                                   (unsigned long long)smoother_pairs_state() * 7919ull;
     if (ctx->graphs_ok && (!ctx->iter_exec || ctx->iter_key != key)) {
         if (ctx->iter_exec) { cudaGraphExecDestroy(ctx->iter_exec); ctx->iter_exec = nullptr; }
         cudaGraph_t g = nullptr;
@@ -1384,6 +1388,7 @@ int scf_debug_time_kernel(scf_ctx *ctx, int kernel, int reps, double *ms_per_lau
             if (mixed) probe_prolong<float>(ctx->L32[0], ctx->L32[1], cc, ctx->st);
             else probe_prolong<double>(ctx->L64[0], ctx->L64[1], cc, ctx->st);
             break;
+        case SCF_K_SMOOTH2: probe_smooth2(ctx->L32[0], cc, ctx->st); break;
         default: {
             int dummy = 0;
             if (mixed)
@@ -1491,6 +1496,13 @@ int scf_debug_fail_device_alloc(int64_t nth)
 }
 
 int64_t scf_debug_device_buffers(void) { return scf_mem::live.load(); }
+
+int scf_debug_smoother_pairs(int on, int planes)
+{
+    if (planes < 0) return SCF_ERR_BAD_ARG;
+    set_smoother_pairs(on, planes);
+    return SCF_OK;
+}
 
 }  // extern "C"
 

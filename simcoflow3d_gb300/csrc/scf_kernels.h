@@ -83,7 +83,8 @@ void mg_coarse_inverse(const MgLevel<T> &L, double *ainv, int *map, int n, bool 
 // Live per-launch timing: CUDA events on the launching stream around the
 // fine-level launches of the kernel classes below (the same numbering as the
 // public scf_kernel_class).  Pairs beyond CAP in one solve go untimed.
-enum KClass { KC_SMOOTH = 0, KC_SPMV = 1, KC_RESTRICT = 2, KC_PROLONG = 3, KC_CGUPDATE = 4, KC_NUM = 5 };
+enum KClass { KC_SMOOTH = 0, KC_SPMV = 1, KC_RESTRICT = 2, KC_PROLONG = 3, KC_CGUPDATE = 4, KC_SMOOTH2 = 5,
+              KC_NUM = 6 };
 // Pairs [0, EAGER) time eagerly launched kernels (reset after every
 // harvest); pairs [EAGER, CAP) belong to the captured CG-iteration graph,
 // whose event-record nodes fire on every replay.
@@ -147,6 +148,14 @@ void probe_restrict(MgLevel<T> &F, MgLevel<T> &C, cudaStream_t st);
 template <typename T>
 void probe_prolong(MgLevel<T> &F, MgLevel<T> &C, const ChebCoef &cc, cudaStream_t st);
 void probe_spmv(const LevelView<double> &A, const double *p, double *q, Reducer &R, cudaStream_t st);
+void probe_smooth2(MgLevel<float> &F, const ChebCoef &cc, cudaStream_t st);
+
+// Large FP32 levels smooth two Chebyshev steps per pass (on: 1, the
+// default) or one (0); planes: k-planes per block of the two-step kernel
+// (0: the default).
+void set_smoother_pairs(int on, int planes);
+int smoother_pairs_state();          // changes whenever the setting does
+cudaError_t pair_smem_attr();        // the two-step kernel's shared-memory opt-in
 
 // Fine operator of the mixed solver's CG in double-float form: hi parts are
 // the FP32 level-0 copy, lo parts the rounding remainders written by the

@@ -84,6 +84,7 @@ def load_library(path: Optional[str] = None):
     L.scf_write_vtr_binary.argtypes = L.scf_write_vtr.argtypes
     L.scf_ctx_device_fields.argtypes = [C.c_void_p] + [P(C.c_void_p)] * 7
     L.scf_apply_operator_noalloc.argtypes = [C.c_int32, C.c_int32, C.c_int32] + [C.c_void_p] * 8
+    L.scf_debug_smoother_pairs.argtypes = [C.c_int, C.c_int]
     P_M = P(capi.ScfMomIn)
     L.scf_mom_create.argtypes = [P(C.c_void_p), C.c_int32, C.c_int32, C.c_int32, C.c_int32]
     L.scf_mom_destroy.argtypes = [C.c_void_p]
@@ -114,6 +115,15 @@ def capi_status(s: int) -> str:
         return load_library().scf_status_string(int(s)).decode()
     except Exception:
         return f"status {s}"
+
+
+def smoother_pairs(on: bool = True, planes: int = 0):
+    """Fused pairs of Chebyshev steps on the large FP32 V-cycle levels (the
+    default) or one step per pass; the two give the same bits."""
+    L = load_library()
+    rc = L.scf_debug_smoother_pairs(1 if on else 0, int(planes))
+    if rc != capi.SCF_OK:
+        raise ScfError(rc, capi_status(rc))
 
 
 def default_opts(**kw) -> capi.ScfOpts:

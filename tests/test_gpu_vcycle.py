@@ -45,3 +45,40 @@ def test_vcycle_matches_oracle(gpu_lib, name, kw, precision, tol, degree, lines)
         err = np.linalg.norm(z - zr) / np.linalg.norm(zr)
         assert err <= tol, (trial, err)
         assert not z[~act].any()
+
+
+def _big_odd():
+    # 70 x 45 x 85 = 267,750 cells: a large level whose tiles are ragged in
+    # every direction (70 = 2*32 + 6, 45 = 5*8 + 5, 85 = 2*32 + 21)
+    return W.build_workload("odd-large", 70, 45, 85, solid=W.SPHERE_C1, liquid=("bubble", 0.5, 0.5, 0.6, 0.2),
+                            rho_l=1000.0, rho_g=1.2)
+
+
+@pytest.mark.parametrize("degree", [2, 3, 4, 5])
+def test_paired_smoother_equals_one_step_sweeps(gpu_lib, degree):
+    """The two-step kernel (one pass per pair of Chebyshev steps on levels of
+    at least 2^18 cells, fused with the prolongation after the coarse
+    correction) gives the V-cycle and the projection of one-step sweeps bit
+    for bit, whatever the k-planes per block."""
+    from simcoflow3d_gb300.projection import Projection, smoother_pairs
+    w = _big_odd()
+    act = np.zeros(w.shape_g, dtype=bool)
+    act[1:-1, 1:-1, 1:-1] = w.arrays["cell_type"] != 2
+    r = np.where(act, np.random.default_rng(5).normal(size=w.shape_g), 0.0)
+    r[act] -= r[act].mean()
+    r = np.asfortranarray(r)
+    out = {}
+    try:
+        for key, on, planes in (("one", False, 0), ("pairs", True, 0), ("pairs7", True, 7), ("pairs1", True, 1)):
+            smoother_pairs(on, planes)
+            p = Projection.for_workload(w, rel_tol=1e-8, precision=1, smoother_degree=degree, smoother_lines=0)
+            _, pp, st = p.poisson_solve(w, want_pocoef=False)
+            out[key] = (p.debug_precondition(r), pp, st["iterations"])
+            p.close()
+    finally:
+        smoother_pairs(True, 0)
+    z0, p0, n0 = out["one"]
+    for key in ("pairs", "pairs7", "pairs1"):
+        z, pp, n = out[key]
+        assert np.array_equal(z, z0), key
+        assert n == n0 and np.array_equal(pp, p0), key
