@@ -505,11 +505,11 @@ __global__ void __launch_bounds__(256) k_cheb_step(LevelView<T> L, const T *__re
 // Two Chebyshev steps in one pass over a large FP32 level (2.5-D temporal
 // blocking).  A block owns a tile of 32 x 8 (i, j) columns and marches along
 // k over `planes` planes.  For plane kk it
-//   1. copies the operator, right-hand side and previous update of plane
-//      kk + 1 on the tile with a one-cell halo into a five-plane ring
-//      (cp.async, in flight while plane kk is computed), and loads x of
-//      plane kk + 2 with a two-cell halo through registers (prolonged from
-//      the coarse correction first when asked, as k_prolong does);
+//   1. issues the asynchronous copies (cp.async) of plane kk + C2_AHEAD:
+//      operator, right-hand side and previous update on the tile with a
+//      one-cell halo, and x of the plane above it with a two-cell halo, into
+//      rings in shared memory, so that C2_AHEAD planes are in flight while
+//      plane kk is computed;
 //   2. applies the first step on the 34 x 10 cells of plane kk (ghost cells
 //      give 0, the value the one-step kernel leaves there) into a
 //      three-plane ring in shared memory;
@@ -525,97 +525,94 @@ constexpr int C2_XX = C2_TX + 4, C2_XY = C2_TY + 4, C2_NX = C2_XX * C2_XY;  // x
 constexpr int C2_NCE = (C2_EX + 1) * C2_EY;                              // cE from column i - 1
 constexpr int C2_NCN = C2_EX * (C2_EY + 1);                              // cN from row j - 1
 constexpr int C2_NH = C2_NE - C2_THREADS;                                // halo cells of step 1
-constexpr int C2_RD = 5, C2_RX = 4, C2_R1 = 3;                           // ring depths (planes)
+constexpr int C2_AHEAD = 2;                                              // planes copied ahead
+// ring depths in planes: inputs in use from kk - 3 (the slowest warp's
+// second step) to kk + C2_AHEAD; x from kk - 1 to kk + C2_AHEAD + 1
+constexpr int C2_RD = C2_AHEAD + 4, C2_RX = C2_AHEAD + 3, C2_R1 = 3;
 constexpr int C2_B = 0, C2_D = C2_NE, C2_P = 2 * C2_NE, C2_T = 3 * C2_NE, C2_E = 4 * C2_NE,
               C2_N = 4 * C2_NE + C2_NCE, C2_SLOT = 4 * C2_NE + C2_NCE + C2_NCN;
 constexpr size_t C2_SMEM = sizeof(float) * (C2_RD * C2_SLOT + C2_RX * C2_NX + C2_R1 * C2_NE);
 constexpr int C2_PLANES = 32;
-static_assert(C2_NH <= C2_THREADS && C2_NX <= 2 * C2_THREADS, "one halo cell and two x cells per thread");
+static_assert(C2_NH <= C2_THREADS && C2_NE <= 2 * C2_THREADS && C2_NCE <= 2 * C2_THREADS &&
+                  C2_NCN <= 2 * C2_THREADS && C2_NX <= 2 * C2_THREADS,
+              "at most two elements of each tile per thread");
 
 struct PairArgs {
     LevelView<float> F;
     const float *b, *x;
     const float *dprev;          // nullptr: the first step's previous update is x itself
     float *xout, *dout;          // dout nullptr: the second step's update is not kept
-    const unsigned char *act;    // non-null: x += e(parent) on the active cells first
-    const float *e;
-    int esy, esz, s0, s1, s2;
     float c1a, c2a, c1b, c2b;
     int planes;
 };
 
-__device__ __forceinline__ bool c2_in(const LevelView<float> &F, int i, int j)
-{
-    return (unsigned)i <= (unsigned)(F.n0 + 1) && (unsigned)j <= (unsigned)(F.n1 + 1);
-}
-
-// Asynchronous copies of plane P's first-step inputs into one ring slot
-// (only cells of the ghosted array; the others are never read).
-__device__ __forceinline__ void c2_stage(const PairArgs &a, float *slot, int i0, int j0, int P, int tid)
-{
-    const LevelView<float> &F = a.F;
-    if (P < 0 || P > F.n2) return;
-    const int base = F.sz * P;
-    for (int q = tid; q < C2_NE; q += C2_THREADS) {
-        const int qy = q / C2_EX, qx = q - qy * C2_EX;
-        const int i = i0 - 1 + qx, j = j0 - 1 + qy;
-        if (!c2_in(F, i, j)) continue;
-        const int c = base + i + F.sy * j;
-        __pipeline_memcpy_async(slot + C2_B + q, a.b + c, sizeof(float));
-        __pipeline_memcpy_async(slot + C2_D + q, F.diag + c, sizeof(float));
-        if (a.dprev) __pipeline_memcpy_async(slot + C2_P + q, a.dprev + c, sizeof(float));
-        __pipeline_memcpy_async(slot + C2_T + q, F.cT + c, sizeof(float));
-    }
-    for (int q = tid; q < C2_NCE; q += C2_THREADS) {
-        const int qy = q / (C2_EX + 1), qx = q - qy * (C2_EX + 1);
-        const int i = i0 - 2 + qx, j = j0 - 1 + qy;
-        if (c2_in(F, i, j)) __pipeline_memcpy_async(slot + C2_E + q, F.cE + base + i + F.sy * j, sizeof(float));
-    }
-    for (int q = tid; q < C2_NCN; q += C2_THREADS) {
-        const int qy = q / C2_EX, qx = q - qy * C2_EX;
-        const int i = i0 - 1 + qx, j = j0 - 2 + qy;
-        if (c2_in(F, i, j)) __pipeline_memcpy_async(slot + C2_N + q, F.cN + base + i + F.sy * j, sizeof(float));
-    }
-}
-
-// x of plane X on this thread's two cells of the 36 x 12 tile (0 outside
-// the ghosted array), with the coarse correction of the active interior
-// cells when prolonging.
-struct C2X {
-    float v[2];
+// In-plane offsets (i + sy j) of this thread's elements of the four tile
+// shapes (two each) and a bit per element inside the ghosted array: the
+// same for every plane, so each copy is one add.
+struct C2Offs {
+    int e[2], ce[2], cn[2], x[2];
+    unsigned ok;
 };
 
-__device__ __forceinline__ C2X c2_load_x(const PairArgs &a, int i0, int j0, int X, int tid)
+__device__ __forceinline__ void c2_off(const LevelView<float> &F, int q, int n, int w, int di, int dj, int i0,
+                                       int j0, int *off, unsigned *ok, unsigned bit)
 {
-    const LevelView<float> &F = a.F;
-    C2X r;
-    float e[2] = {0.f, 0.f};
-    bool on[2] = {false, false};
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        r.v[h] = 0.f;
-        const int q = tid + h * C2_THREADS;
-        if (q >= C2_NX || X < 0 || X > F.n2 + 1) continue;
-        const int qy = q / C2_XX, qx = q - qy * C2_XX;
-        const int i = i0 - 2 + qx, j = j0 - 2 + qy;
-        if (!c2_in(F, i, j)) continue;
-        const int c = i + F.sy * j + F.sz * X;
-        r.v[h] = a.x[c];
-        if (a.act && i >= 1 && i <= F.n0 && j >= 1 && j <= F.n1 && X >= 1 && X <= F.n2) {
-            on[h] = a.act[c] != 0;
-            e[h] = a.e[(((i - 1) >> a.s0) + 1) + a.esy * (((j - 1) >> a.s1) + 1) + a.esz * (((X - 1) >> a.s2) + 1)];
-        }
-    }
-#pragma unroll
-    for (int h = 0; h < 2; ++h)
-        if (on[h]) r.v[h] = fx_add(r.v[h], e[h]);
-    return r;
+    const int qy = q / w, qx = q - qy * w;
+    const int i = i0 + di + qx, j = j0 + dj + qy;
+    *off = i + F.sy * j;
+    if (q < n && (unsigned)i <= (unsigned)(F.n0 + 1) && (unsigned)j <= (unsigned)(F.n1 + 1)) *ok |= bit;
 }
 
-__device__ __forceinline__ void c2_store_x(float *sx, const C2X &r, int tid)
+__device__ __forceinline__ C2Offs c2_offsets(const LevelView<float> &F, int i0, int j0, int tid)
 {
-    sx[tid] = r.v[0];
-    if (tid + C2_THREADS < C2_NX) sx[tid + C2_THREADS] = r.v[1];
+    C2Offs o;
+    o.ok = 0u;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int q = tid + h * C2_THREADS;
+        c2_off(F, q, C2_NE, C2_EX, -1, -1, i0, j0, &o.e[h], &o.ok, 1u << h);
+        c2_off(F, q, C2_NCE, C2_EX + 1, -2, -1, i0, j0, &o.ce[h], &o.ok, 4u << h);
+        c2_off(F, q, C2_NCN, C2_EX, -1, -2, i0, j0, &o.cn[h], &o.ok, 16u << h);
+        c2_off(F, q, C2_NX, C2_XX, -2, -2, i0, j0, &o.x[h], &o.ok, 64u << h);
+    }
+    return o;
+}
+
+__device__ __forceinline__ void c2_cp(float *dst, const float *src)
+{
+    __pipeline_memcpy_async(dst, src, sizeof(float));
+}
+
+// Copies of plane P's first-step inputs into `slot` (planes 0..n2: plane 0
+// only for its cT) and of x of plane X into `xs` (planes 0..n2+1).  Cells
+// outside the ghosted array are not copied; no first step of an interior
+// cell reads them.
+__device__ __forceinline__ void c2_issue(const PairArgs &a, const C2Offs &o, float *slot, int P, float *xs, int X,
+                                         int tid)
+{
+    const LevelView<float> &F = a.F;
+    if (P >= 0 && P <= F.n2) {
+        const int base = F.sz * P;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int q = tid + h * C2_THREADS;
+            if (o.ok & (1u << h)) {
+                const int c = base + o.e[h];
+                c2_cp(slot + C2_B + q, a.b + c);
+                c2_cp(slot + C2_D + q, F.diag + c);
+                if (a.dprev) c2_cp(slot + C2_P + q, a.dprev + c);
+                c2_cp(slot + C2_T + q, F.cT + c);
+            }
+            if (o.ok & (4u << h)) c2_cp(slot + C2_E + q, F.cE + base + o.ce[h]);
+            if (o.ok & (16u << h)) c2_cp(slot + C2_N + q, F.cN + base + o.cn[h]);
+        }
+    }
+    if (X >= 0 && X <= F.n2 + 1) {
+        const int base = F.sz * X;
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+            if (o.ok & (64u << h)) c2_cp(xs + tid + h * C2_THREADS, a.x + base + o.x[h]);
+    }
 }
 
 // First step at plane P on cell (ex, ey) of the 34 x 10 tile: writes x
@@ -641,7 +638,7 @@ __device__ __forceinline__ float c2_first(const PairArgs &a, const float *dc, co
     return dn;
 }
 
-__global__ void __launch_bounds__(C2_THREADS, 4) k_cheb_pair(PairArgs a)
+__global__ void __launch_bounds__(C2_THREADS, 3) k_cheb_pair(PairArgs a)
 {
     extern __shared__ __align__(16) float c2_smem[];
     float *sd = c2_smem;                   // C2_RD slots of first-step inputs
@@ -651,10 +648,11 @@ __global__ void __launch_bounds__(C2_THREADS, 4) k_cheb_pair(PairArgs a)
     const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + C2_TX * ty;
     const int i0 = blockIdx.x * C2_TX + 1, j0 = blockIdx.y * C2_TY + 1;
     const int k0 = blockIdx.z * a.planes + 1, k1 = min(k0 + a.planes - 1, F.n2);
-    // planes from k0 - 2 on: slot indices stay non-negative
+    // planes from k0 - 2 on: ring indices stay non-negative
     auto dslot = [&](int P) { return sd + ((P + 2) % C2_RD) * C2_SLOT; };
     auto xslot = [&](int P) { return sx + ((P + 2) % C2_RX) * C2_NX; };
     auto oslot = [&](int P) { return s1 + ((P + 2) % C2_R1) * C2_NE; };
+    const C2Offs o = c2_offsets(F, i0, j0, tid);
     // this thread's halo cell of the first step (the ring around the 32 x 8 tile)
     int hx = -1, hy = -1;
     if (tid < C2_EX) { hx = tid; hy = 0; }
@@ -662,19 +660,19 @@ __global__ void __launch_bounds__(C2_THREADS, 4) k_cheb_pair(PairArgs a)
     else if (tid < 2 * C2_EX + C2_TY) { hx = 0; hy = tid - 2 * C2_EX + 1; }
     else if (tid < C2_NH) { hx = C2_EX - 1; hy = tid - 2 * C2_EX - C2_TY + 1; }
 
-    c2_stage(a, dslot(k0 - 2), i0, j0, k0 - 2, tid);
-    __pipeline_commit();
-    c2_stage(a, dslot(k0 - 1), i0, j0, k0 - 1, tid);
-    __pipeline_commit();
-    for (int X = k0 - 2; X <= k0; ++X) c2_store_x(xslot(X), c2_load_x(a, i0, j0, X, tid), tid);
-
+    // group g: inputs of plane g and x of plane g + 1 (the first group also
+    // x of plane k0 - 2); groups k0 - 2 .. k0 - 2 + C2_AHEAD before the loop
+    c2_issue(a, o, dslot(k0 - 2), k0 - 2, xslot(k0 - 2), k0 - 2, tid);
+    for (int g = k0 - 2; g <= k0 - 2 + C2_AHEAD; ++g) {
+        c2_issue(a, o, dslot(g), g == k0 - 2 ? -1 : g, xslot(g + 1), g + 1, tid);
+        __pipeline_commit();
+    }
     float d1 = 0.f;     // first-step update of this thread's column, plane below
     for (int kk = k0 - 1; kk <= k1 + 1; ++kk) {
-        if (kk + 1 <= k1 + 1) c2_stage(a, dslot(kk + 1), i0, j0, kk + 1, tid);
+        const int g = kk + C2_AHEAD;
+        if (g <= k1 + 1) c2_issue(a, o, dslot(g), g, xslot(g + 1), g + 1, tid);
         __pipeline_commit();
-        C2X xr = {};
-        if (kk <= k1) xr = c2_load_x(a, i0, j0, kk + 2, tid);
-        __pipeline_wait_prior(1);
+        __pipeline_wait_prior(C2_AHEAD);    // groups up to kk have landed
         __syncthreads();
         const float *dc = dslot(kk), *dm = dslot(kk - 1);
         const float *xm = xslot(kk - 1), *x0 = xslot(kk), *xp = xslot(kk + 1);
@@ -699,7 +697,6 @@ __global__ void __launch_bounds__(C2_THREADS, 4) k_cheb_pair(PairArgs a)
             if (a.dout) a.dout[c] = dn;
         }
         d1 = dn1;
-        if (kk <= k1) c2_store_x(xslot(kk + 2), xr, tid);
     }
     __pipeline_wait_prior(0);
 }
@@ -731,18 +728,13 @@ cudaError_t pair_smem_attr()
 
 // Two Chebyshev steps (c1a, c2a) then (c1b, c2b) of FP32 level F from xin
 // into xout; dprev nullptr means the first step's previous update is xin
-// itself; with C and e, the coarse correction e is first added to xin on
-// the active cells.
+// itself.
 void cheb_pair(const MgLevel<float> &F, const float *xin, const float *dprev, float *xout, float *dout, double c1a,
-               double c2a, double c1b, double c2b, const MgLevel<float> *C, const float *e, cudaStream_t st)
+               double c2a, double c1b, double c2b, cudaStream_t st)
 {
     PairArgs a;
     a.F = F.view();
     a.b = F.b; a.x = xin; a.dprev = dprev; a.xout = xout; a.dout = dout;
-    a.act = C ? F.active : nullptr;
-    a.e = e;
-    a.esy = C ? C->sy : 0; a.esz = C ? C->sz : 0;
-    a.s0 = F.f0 - 1; a.s1 = F.f1 - 1; a.s2 = F.f2 - 1;
     a.c1a = (float)c1a; a.c2a = (float)c2a; a.c1b = (float)c1b; a.c2b = (float)c2b;
     a.planes = g_pair_planes;
     pair_smem_attr();
@@ -1117,12 +1109,13 @@ double prolong_bytes(const MgLevel<T> &F, bool writes_d)
 }
 
 // Algorithmic bytes of a fused pair of steps: b, diag, cE, cN, cT and x
-// read (+ the previous update), x (+ the update) written; when prolonging,
-// the active mask and the coarse correction read.
+// read (+ the previous update), x (+ the update) written; with the
+// prolongation before it, x read and written once more, the active mask and
+// the coarse correction read.
 double pair_bytes(const MgLevel<float> &F, bool reads_d, bool writes_d, bool prolong)
 {
     const double cells = (double)F.n0 * F.n1 * F.n2;
-    return cells * (4.0 * (7 + (reads_d ? 1 : 0) + (writes_d ? 1 : 0)) + (prolong ? 1.0 + 4.0 / 8.0 : 0.0));
+    return cells * (4.0 * (7 + (reads_d ? 1 : 0) + (writes_d ? 1 : 0)) + (prolong ? 8.0 + 1.0 + 4.0 / 8.0 : 0.0));
 }
 
 template <typename T>
@@ -1171,14 +1164,14 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
             if (use_pairs(F) && m >= 2) {
                 T *dout = m > 2 ? F.d : nullptr;
                 const int id = l == 0 ? kt_begin(kt, KC_SMOOTH2, st, pair_bytes(F, false, dout != nullptr, false)) : -1;
-                cheb_pair(F, xa, nullptr, xb, dout, cc.c1[1], cc.c2[1], cc.c1[2], cc.c2[2], nullptr, nullptr, st);
+                cheb_pair(F, xa, nullptr, xb, dout, cc.c1[1], cc.c2[1], cc.c1[2], cc.c2[2], st);
                 kt_end(kt, id, st);
                 *launches += 1;
                 { T *tmp = xa; xa = xb; xb = tmp; }
                 s = 3;
                 if (m == 4) {
                     const int id2 = l == 0 ? kt_begin(kt, KC_SMOOTH2, st, pair_bytes(F, true, false, false)) : -1;
-                    cheb_pair(F, xa, F.d, xb, nullptr, cc.c1[3], cc.c2[3], cc.c1[4], cc.c2[4], nullptr, nullptr, st);
+                    cheb_pair(F, xa, F.d, xb, nullptr, cc.c1[3], cc.c2[3], cc.c1[4], cc.c2[4], st);
                     kt_end(kt, id2, st);
                     *launches += 1;
                     { T *tmp = xa; xa = xb; xb = tmp; }
@@ -1241,21 +1234,23 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
         int s = 1;
         bool paired = false;
         if constexpr (sizeof(T) == 4) {
-            // prolongation, the first post-smoothing step (its previous
-            // update term is 0) and step 1 in one pass; steps 2 and 3 too
-            // when they are the last two
+            // prolongation (in place), then the first post-smoothing step
+            // (its previous update term is 0) and step 1 in one pass; steps
+            // 2 and 3 too when they are the last two
             const int m = cc.degree - 1;
             if (use_pairs(F) && m >= 1) {
                 T *dout = m >= 2 ? F.d : nullptr;
                 const int idp = l == 0 ? kt_begin(kt, KC_PROLONG, st, pair_bytes(F, false, dout != nullptr, true)) : -1;
-                cheb_pair(F, xa, nullptr, xb, dout, 0.0, cc.first, cc.c1[1], cc.c2[1], &C, cur[l + 1], st);
+                k_prolong<T><<<lf.grid, lf.block, 0, st>>>(v, F.active, xa, C.view(), cur[l + 1], F.f0 - 1, F.f1 - 1,
+                                                           F.f2 - 1);
+                cheb_pair(F, xa, nullptr, xb, dout, 0.0, cc.first, cc.c1[1], cc.c2[1], st);
                 kt_end(kt, idp, st);
-                *launches += 1;
+                *launches += 2;
                 { T *tmp = xa; xa = xb; xb = tmp; }
                 s = 2;
                 if (m == 3) {
                     const int id2 = l == 0 ? kt_begin(kt, KC_SMOOTH2, st, pair_bytes(F, true, false, false)) : -1;
-                    cheb_pair(F, xa, F.d, xb, nullptr, cc.c1[2], cc.c2[2], cc.c1[3], cc.c2[3], nullptr, nullptr, st);
+                    cheb_pair(F, xa, F.d, xb, nullptr, cc.c1[2], cc.c2[2], cc.c1[3], cc.c2[3], st);
                     kt_end(kt, id2, st);
                     *launches += 1;
                     { T *tmp = xa; xa = xb; xb = tmp; }
@@ -1308,7 +1303,7 @@ void probe_smooth(MgLevel<T> &F, const ChebCoef &cc, cudaStream_t st)
 
 void probe_smooth2(MgLevel<float> &F, const ChebCoef &cc, cudaStream_t st)
 {
-    cheb_pair(F, F.x, F.d, F.xb, nullptr, cc.c1[1], cc.c2[1], cc.c1[2], cc.c2[2], nullptr, nullptr, st);
+    cheb_pair(F, F.x, F.d, F.xb, nullptr, cc.c1[1], cc.c2[1], cc.c1[2], cc.c2[2], st);
 }
 
 template <typename T>
