@@ -525,10 +525,12 @@ constexpr int C2_XX = C2_TX + 4, C2_XY = C2_TY + 4, C2_NX = C2_XX * C2_XY;  // x
 constexpr int C2_NCE = (C2_EX + 1) * C2_EY;                              // cE from column i - 1
 constexpr int C2_NCN = C2_EX * (C2_EY + 1);                              // cN from row j - 1
 constexpr int C2_NH = C2_NE - C2_THREADS;                                // halo cells of step 1
-constexpr int C2_AHEAD = 2;                                              // planes copied ahead
-// ring depths in planes: inputs in use from kk - 3 (the slowest warp's
-// second step) to kk + C2_AHEAD; x from kk - 1 to kk + C2_AHEAD + 1
-constexpr int C2_RD = C2_AHEAD + 4, C2_RX = C2_AHEAD + 3, C2_R1 = 3;
+constexpr int C2_AHEAD = 3;                                              // planes copied ahead
+// ring depths in planes: when plane kk + C2_AHEAD is issued, inputs of
+// planes kk - 1 .. kk + C2_AHEAD - 1 and x of planes kk - 1 .. kk + C2_AHEAD
+// are in use or on their way (the second step reads no inputs: the thread
+// keeps its column's from the first step)
+constexpr int C2_RD = C2_AHEAD + 2, C2_RX = C2_AHEAD + 3, C2_R1 = 3;
 constexpr int C2_B = 0, C2_D = C2_NE, C2_P = 2 * C2_NE, C2_T = 3 * C2_NE, C2_E = 4 * C2_NE,
               C2_N = 4 * C2_NE + C2_NCE, C2_SLOT = 4 * C2_NE + C2_NCE + C2_NCN;
 constexpr size_t C2_SMEM = sizeof(float) * (C2_RD * C2_SLOT + C2_RX * C2_NX + C2_R1 * C2_NE);
@@ -615,28 +617,41 @@ __device__ __forceinline__ void c2_issue(const PairArgs &a, const C2Offs &o, flo
     }
 }
 
-// First step at plane P on cell (ex, ey) of the 34 x 10 tile: writes x
-// after the step into o1 and returns the update.
+// Inputs of one cell's update, kept by the thread that applied the first
+// step to its own column for the second step one plane later.
+struct C2Cell {
+    float b, dg, dinv, ce, cw, cn, cs, ct, cb;
+};
+
+// First step at plane P on cell q = ex + 34 ey of the tile (qx: the same
+// cell in the x tile), `in` whether (i, j) is an interior column: writes x
+// after the step into o1, returns the update and the cell's inputs.
 __device__ __forceinline__ float c2_first(const PairArgs &a, const float *dc, const float *dm, const float *xm,
-                                          const float *x0, const float *xp, float *o1, int ex, int ey, int i0,
-                                          int j0, int P)
+                                          const float *x0, const float *xp, float *o1, int q, int qe, int qn,
+                                          int qx, bool in, C2Cell &k)
 {
-    const LevelView<float> &F = a.F;
-    const int i = i0 - 1 + ex, j = j0 - 1 + ey, q = ex + C2_EX * ey;
-    if (i < 1 || i > F.n0 || j < 1 || j > F.n1 || P < 1 || P > F.n2) {
+    if (!in) {
         o1[q] = 0.f;
         return 0.f;
     }
-    const int qx = (ex + 1) + C2_XX * (ey + 1);
-    const float xc = x0[qx], dg = dc[C2_D + q];
-    const float dn = cheb_update(dc[C2_B + q], dg, dg > 0.f ? __frcp_rn(dg) : 0.f, xc, x0[qx + 1], x0[qx - 1],
-                                 x0[qx + C2_XX], x0[qx - C2_XX], xp[qx], xm[qx],
-                                 dc[C2_E + (ex + 1) + (C2_EX + 1) * ey], dc[C2_E + ex + (C2_EX + 1) * ey],
-                                 dc[C2_N + ex + C2_EX * (ey + 1)], dc[C2_N + q], dc[C2_T + q], dm[C2_T + q],
-                                 a.dprev ? dc[C2_P + q] : xc, a.c1a, a.c2a);
+    k.b = dc[C2_B + q];
+    k.dg = dc[C2_D + q];
+    k.dinv = k.dg > 0.f ? __frcp_rn(k.dg) : 0.f;
+    k.ce = dc[C2_E + qe + 1];
+    k.cw = dc[C2_E + qe];
+    k.cn = dc[C2_N + qn + C2_EX];
+    k.cs = dc[C2_N + qn];
+    k.ct = dc[C2_T + q];
+    k.cb = dm[C2_T + q];
+    const float xc = x0[qx];
+    const float dn = cheb_update(k.b, k.dg, k.dinv, xc, x0[qx + 1], x0[qx - 1], x0[qx + C2_XX], x0[qx - C2_XX],
+                                 xp[qx], xm[qx], k.ce, k.cw, k.cn, k.cs, k.ct, k.cb, a.dprev ? dc[C2_P + q] : xc,
+                                 a.c1a, a.c2a);
     o1[q] = fx_add(xc, dn);
     return dn;
 }
+
+__device__ __forceinline__ int c2_wrap(int i, int r) { return i >= r ? i - r : i; }
 
 __global__ void __launch_bounds__(C2_THREADS, 3) k_cheb_pair(PairArgs a)
 {
@@ -648,55 +663,79 @@ __global__ void __launch_bounds__(C2_THREADS, 3) k_cheb_pair(PairArgs a)
     const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + C2_TX * ty;
     const int i0 = blockIdx.x * C2_TX + 1, j0 = blockIdx.y * C2_TY + 1;
     const int k0 = blockIdx.z * a.planes + 1, k1 = min(k0 + a.planes - 1, F.n2);
-    // planes from k0 - 2 on: ring indices stay non-negative
-    auto dslot = [&](int P) { return sd + ((P + 2) % C2_RD) * C2_SLOT; };
-    auto xslot = [&](int P) { return sx + ((P + 2) % C2_RX) * C2_NX; };
-    auto oslot = [&](int P) { return s1 + ((P + 2) % C2_R1) * C2_NE; };
     const C2Offs o = c2_offsets(F, i0, j0, tid);
-    // this thread's halo cell of the first step (the ring around the 32 x 8 tile)
-    int hx = -1, hy = -1;
+    // this thread's column (tx + 1, ty + 1) of the 34 x 10 tile and its halo
+    // cell (the ring around the 32 x 8 tile), as tile indices
+    auto idx = [&](int ex, int ey, int &q, int &qe, int &qn, int &qx, bool &in) {
+        const int i = i0 - 1 + ex, j = j0 - 1 + ey;
+        q = ex + C2_EX * ey;
+        qe = ex + (C2_EX + 1) * ey;
+        qn = ex + C2_EX * ey;
+        qx = (ex + 1) + C2_XX * (ey + 1);
+        in = i >= 1 && i <= F.n0 && j >= 1 && j <= F.n1;
+    };
+    int q0, qe0, qn0, qx0, qh = 0, qeh = 0, qnh = 0, qxh = 0;
+    bool in0, inh = false;
+    idx(tx + 1, ty + 1, q0, qe0, qn0, qx0, in0);
+    int hx = -1, hy = 0;
     if (tid < C2_EX) { hx = tid; hy = 0; }
     else if (tid < 2 * C2_EX) { hx = tid - C2_EX; hy = C2_EY - 1; }
     else if (tid < 2 * C2_EX + C2_TY) { hx = 0; hy = tid - 2 * C2_EX + 1; }
     else if (tid < C2_NH) { hx = C2_EX - 1; hy = tid - 2 * C2_EX - C2_TY + 1; }
+    const bool halo = hx >= 0;
+    if (halo) idx(hx, hy, qh, qeh, qnh, qxh, inh);
 
     // group g: inputs of plane g and x of plane g + 1 (the first group also
-    // x of plane k0 - 2); groups k0 - 2 .. k0 - 2 + C2_AHEAD before the loop
-    c2_issue(a, o, dslot(k0 - 2), k0 - 2, xslot(k0 - 2), k0 - 2, tid);
+    // x of plane k0 - 2); groups k0 - 2 .. k0 - 2 + C2_AHEAD before the loop.
+    // Ring index of plane P: (P + 2) mod depth (P >= k0 - 2 >= -1).
+    c2_issue(a, o, sd + ((k0) % C2_RD) * C2_SLOT, k0 - 2, sx + ((k0) % C2_RX) * C2_NX, k0 - 2, tid);
     for (int g = k0 - 2; g <= k0 - 2 + C2_AHEAD; ++g) {
-        c2_issue(a, o, dslot(g), g == k0 - 2 ? -1 : g, xslot(g + 1), g + 1, tid);
+        c2_issue(a, o, sd + ((g + 2) % C2_RD) * C2_SLOT, g == k0 - 2 ? -1 : g, sx + ((g + 3) % C2_RX) * C2_NX, g + 1,
+                 tid);
         __pipeline_commit();
     }
+    // ring indices of plane kk (and the planes around it), advanced by one per plane
+    int rd = (k0 + 1) % C2_RD, rx = (k0 + 1) % C2_RX, r1 = (k0 + 1) % C2_R1;
     float d1 = 0.f;     // first-step update of this thread's column, plane below
+    C2Cell kc = {}, kp = {};
+    const bool out_ok = tx + i0 <= F.n0 && ty + j0 <= F.n1;
     for (int kk = k0 - 1; kk <= k1 + 1; ++kk) {
         const int g = kk + C2_AHEAD;
-        if (g <= k1 + 1) c2_issue(a, o, dslot(g), g, xslot(g + 1), g + 1, tid);
+        if (g <= k1 + 1)
+            c2_issue(a, o, sd + c2_wrap(rd + C2_AHEAD, C2_RD) * C2_SLOT, g,
+                     sx + c2_wrap(rx + C2_AHEAD + 1, C2_RX) * C2_NX, g + 1, tid);
         __pipeline_commit();
         __pipeline_wait_prior(C2_AHEAD);    // groups up to kk have landed
         __syncthreads();
-        const float *dc = dslot(kk), *dm = dslot(kk - 1);
-        const float *xm = xslot(kk - 1), *x0 = xslot(kk), *xp = xslot(kk + 1);
-        float *o1 = oslot(kk);
-        const float dn1 = c2_first(a, dc, dm, xm, x0, xp, o1, tx + 1, ty + 1, i0, j0, kk);
-        if (hx >= 0) c2_first(a, dc, dm, xm, x0, xp, o1, hx, hy, i0, j0, kk);
+        const float *dc = sd + rd * C2_SLOT, *dm = sd + (rd == 0 ? C2_RD - 1 : rd - 1) * C2_SLOT;
+        const float *x0 = sx + rx * C2_NX, *xm = sx + (rx == 0 ? C2_RX - 1 : rx - 1) * C2_NX;
+        const float *xp = sx + c2_wrap(rx + 1, C2_RX) * C2_NX;
+        float *o1 = s1 + r1 * C2_NE;
+        const bool plane_in = kk >= 1 && kk <= F.n2;
+        const float dn1 = c2_first(a, dc, dm, xm, x0, xp, o1, q0, qe0, qn0, qx0, in0 && plane_in, kc);
+        if (halo) {
+            C2Cell kh;
+            c2_first(a, dc, dm, xm, x0, xp, o1, qh, qeh, qnh, qxh, inh && plane_in, kh);
+        }
         __syncthreads();
-        const int Q = kk - 1, i = i0 + tx, j = j0 + ty;
-        if (Q >= k0 && i <= F.n0 && j <= F.n1) {
-            const float *qc = dslot(Q), *qm = dslot(Q - 1);
-            const float *y0 = oslot(Q), *ym = oslot(Q - 1), *yp = oslot(Q + 1);
-            const int q = (tx + 1) + C2_EX * (ty + 1);
-            const float xc = y0[q], dg = qc[C2_D + q];
-            const float dn = cheb_update(qc[C2_B + q], dg, dg > 0.f ? __frcp_rn(dg) : 0.f, xc, y0[q + 1], y0[q - 1],
-                                         y0[q + C2_EX], y0[q - C2_EX], yp[q], ym[q],
-                                         qc[C2_E + (tx + 2) + (C2_EX + 1) * (ty + 1)],
-                                         qc[C2_E + (tx + 1) + (C2_EX + 1) * (ty + 1)],
-                                         qc[C2_N + (tx + 1) + C2_EX * (ty + 2)], qc[C2_N + q], qc[C2_T + q],
-                                         qm[C2_T + q], d1, a.c1b, a.c2b);
-            const int c = i + F.sy * j + F.sz * Q;
+        const int Q = kk - 1;
+        if (Q >= k0 && out_ok) {
+            // second step at plane Q from the first-step planes Q - 1, Q, Q + 1
+            const int r1m = r1 == 0 ? C2_R1 - 1 : r1 - 1, r1m2 = r1m == 0 ? C2_R1 - 1 : r1m - 1;
+            const float *y0 = s1 + r1m * C2_NE, *ym = s1 + r1m2 * C2_NE, *yp = o1;
+            const int q = q0;
+            const float xc = y0[q];
+            const float dn = cheb_update(kp.b, kp.dg, kp.dinv, xc, y0[q + 1], y0[q - 1], y0[q + C2_EX], y0[q - C2_EX],
+                                         yp[q], ym[q], kp.ce, kp.cw, kp.cn, kp.cs, kp.ct, kp.cb, d1, a.c1b, a.c2b);
+            const int c = (i0 + tx) + F.sy * (j0 + ty) + F.sz * Q;
             a.xout[c] = fx_add(xc, dn);
             if (a.dout) a.dout[c] = dn;
         }
         d1 = dn1;
+        kp = kc;
+        rd = c2_wrap(rd + 1, C2_RD);
+        rx = c2_wrap(rx + 1, C2_RX);
+        r1 = c2_wrap(r1 + 1, C2_R1);
     }
     __pipeline_wait_prior(0);
 }
