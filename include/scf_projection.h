@@ -345,11 +345,13 @@ int scf_abi_version(void);
 int     scf_debug_fail_device_alloc(int64_t nth);
 int64_t scf_debug_device_buffers(void);
 
-/* FP32 V-cycle levels of at least 2^18 cells apply their Chebyshev steps in
- * fused pairs, one pass over the level for two steps (on = 1, the default),
- * or one step per pass (on = 0); both give the same bits.  planes: k-planes
- * per thread block of the fused kernel (0: the default, 32).  Process-wide;
- * applies from the next solve of every context.                           */
+/* Large FP32 V-cycle levels can apply their Chebyshev steps in fused pairs,
+ * one pass over the level for two steps.  on = 1 (the default): on levels of
+ * at least 2^22 cells whose grid of 32 x 8 x planes blocks fills the GPU
+ * twice; on = 2: on every FP32 level of at least 2^18 cells; on = 0: one
+ * step per pass.  All give the same bits.  planes: k-planes per thread block
+ * of the fused kernel (0: the default, 32).  Process-wide; applies from the
+ * next solve of every context.                                             */
 int scf_debug_smoother_pairs(int on, int planes);
 
 #ifdef __cplusplus

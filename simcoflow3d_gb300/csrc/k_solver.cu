@@ -740,22 +740,39 @@ __global__ void __launch_bounds__(C2_THREADS, 3) k_cheb_pair(PairArgs a)
     __pipeline_wait_prior(0);
 }
 
-// Smoother pairing: on (1, the default) or off (0, one-step kernels only);
-// k-planes per block of the pair kernel.
+// Smoother pairing: 1 (the default) on the levels where the pair kernel
+// measured faster than two one-step launches -- at least 2^22 cells, with
+// at least two waves of three blocks per SM -- 2 on every FP32 level of at
+// least 2^18 cells, 0 off; k-planes per block of the pair kernel (fewer
+// when that fills the grid).
 static int g_pairs = 1, g_pair_planes = C2_PLANES;
 
 void set_smoother_pairs(int on, int planes)
 {
-    g_pairs = on ? 1 : 0;
+    g_pairs = on < 0 ? 0 : (on > 2 ? 2 : on);
     g_pair_planes = planes > 0 ? planes : C2_PLANES;
 }
 
-int smoother_pairs_state() { return g_pairs + 2 * g_pair_planes; }
+int smoother_pairs_state() { return g_pairs + 3 * g_pair_planes; }
+
+// k-planes per block of the pair kernel on level F, 0: one-step kernels.
+template <typename T>
+int pair_planes(const MgLevel<T> &F)
+{
+    const long long cells = (long long)F.n0 * F.n1 * F.n2;
+    if (sizeof(T) != 4 || g_pairs == 0 || cells < (1LL << 18)) return 0;
+    if (g_pairs == 2) return g_pair_planes;
+    if (cells < (1LL << 22)) return 0;
+    const long long tiles = (long long)((F.n0 + C2_TX - 1) / C2_TX) * ((F.n1 + C2_TY - 1) / C2_TY);
+    for (int planes = g_pair_planes; planes >= 8; planes /= 2)
+        if (tiles * ((F.n2 + planes - 1) / planes) >= 2LL * 3 * 152) return planes;
+    return 0;
+}
 
 template <typename T>
 bool use_pairs(const MgLevel<T> &F)
 {
-    return sizeof(T) == 4 && g_pairs && (long long)F.n0 * F.n1 * F.n2 >= (1LL << 18);
+    return pair_planes(F) > 0;
 }
 
 cudaError_t pair_smem_attr()
@@ -775,7 +792,7 @@ void cheb_pair(const MgLevel<float> &F, const float *xin, const float *dprev, fl
     a.F = F.view();
     a.b = F.b; a.x = xin; a.dprev = dprev; a.xout = xout; a.dout = dout;
     a.c1a = (float)c1a; a.c2a = (float)c2a; a.c1b = (float)c1b; a.c2b = (float)c2b;
-    a.planes = g_pair_planes;
+    a.planes = pair_planes(F) > 0 ? pair_planes(F) : g_pair_planes;
     pair_smem_attr();
     const dim3 blk(C2_TX, C2_TY, 1);
     const dim3 grd((F.n0 + C2_TX - 1) / C2_TX, (F.n1 + C2_TY - 1) / C2_TY, (F.n2 + a.planes - 1) / a.planes);

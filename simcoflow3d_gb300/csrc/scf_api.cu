@@ -1499,7 +1499,7 @@ int64_t scf_debug_device_buffers(void) { return scf_mem::live.load(); }
 
 int scf_debug_smoother_pairs(int on, int planes)
 {
-    if (planes < 0) return SCF_ERR_BAD_ARG;
+    if (planes < 0 || on < 0 || on > 2) return SCF_ERR_BAD_ARG;
     set_smoother_pairs(on, planes);
     return SCF_OK;
 }

@@ -117,11 +117,12 @@ def capi_status(s: int) -> str:
         return f"status {s}"
 
 
-def smoother_pairs(on: bool = True, planes: int = 0):
-    """Fused pairs of Chebyshev steps on the large FP32 V-cycle levels (the
-    default) or one step per pass; the two give the same bits."""
+def smoother_pairs(on: int = 1, planes: int = 0):
+    """Fused pairs of Chebyshev steps: 1 on the large FP32 V-cycle levels
+    where they are faster (the default), 2 on every FP32 level of at least
+    2^18 cells, 0 one step per pass; all give the same bits."""
     L = load_library()
-    rc = L.scf_debug_smoother_pairs(1 if on else 0, int(planes))
+    rc = L.scf_debug_smoother_pairs(int(on), int(planes))
     if rc != capi.SCF_OK:
         raise ScfError(rc, capi_status(rc))
 

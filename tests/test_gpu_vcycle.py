@@ -56,10 +56,10 @@ def _big_odd():
 
 @pytest.mark.parametrize("degree", [2, 3, 4, 5])
 def test_paired_smoother_equals_one_step_sweeps(gpu_lib, degree):
-    """The two-step kernel (one pass per pair of Chebyshev steps on levels of
-    at least 2^18 cells, fused with the prolongation after the coarse
-    correction) gives the V-cycle and the projection of one-step sweeps bit
-    for bit, whatever the k-planes per block."""
+    """The two-step kernel (one pass per pair of Chebyshev steps), forced
+    onto every level of at least 2^18 cells, gives the V-cycle and the
+    projection of one-step sweeps bit for bit, whatever the k-planes per
+    block."""
     from simcoflow3d_gb300.projection import Projection, smoother_pairs
     w = _big_odd()
     act = np.zeros(w.shape_g, dtype=bool)
@@ -69,14 +69,14 @@ def test_paired_smoother_equals_one_step_sweeps(gpu_lib, degree):
     r = np.asfortranarray(r)
     out = {}
     try:
-        for key, on, planes in (("one", False, 0), ("pairs", True, 0), ("pairs7", True, 7), ("pairs1", True, 1)):
+        for key, on, planes in (("one", 0, 0), ("pairs", 2, 0), ("pairs7", 2, 7), ("pairs1", 2, 1)):
             smoother_pairs(on, planes)
             p = Projection.for_workload(w, rel_tol=1e-8, precision=1, smoother_degree=degree, smoother_lines=0)
             _, pp, st = p.poisson_solve(w, want_pocoef=False)
             out[key] = (p.debug_precondition(r), pp, st["iterations"])
             p.close()
     finally:
-        smoother_pairs(True, 0)
+        smoother_pairs(1, 0)
     z0, p0, n0 = out["one"]
     for key in ("pairs", "pairs7", "pairs1"):
         z, pp, n = out[key]
