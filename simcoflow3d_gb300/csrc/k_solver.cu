@@ -520,10 +520,13 @@ __global__ void __launch_bounds__(256) k_cheb_step(LevelView<T> L, const T *__re
 // The output x must not be the input x, nor dout the previous update when
 // both are given: neighbouring tiles read their halos from them.
 constexpr int C2_TX = 32, C2_TY = 8, C2_THREADS = C2_TX * C2_TY;
-constexpr int C2_EX = C2_TX + 2, C2_EY = C2_TY + 2, C2_NE = C2_EX * C2_EY;  // first-step cells
-constexpr int C2_XX = C2_TX + 4, C2_XY = C2_TY + 4, C2_NX = C2_XX * C2_XY;  // x, two-cell halo
-constexpr int C2_NCE = (C2_EX + 1) * C2_EY;                              // cE from column i - 1
-constexpr int C2_NCN = C2_EX * (C2_EY + 1);                              // cN from row j - 1
+// Tiles in shared memory, each starting on an even column (i0 - 1 or
+// i0 - 3): with an even row length n0 + 2 every row starts 8-byte aligned,
+// so each thread copies at most one pair of cells of each tile per plane.
+constexpr int C2_EX = C2_TX + 2, C2_EY = C2_TY + 2, C2_NE = C2_EX * C2_EY;  // first-step cells, from (i0-1, j0-1)
+constexpr int C2_WE = C2_TX + 4, C2_NCE = C2_WE * C2_EY;                 // cE from column i0 - 3
+constexpr int C2_NCN = C2_EX * (C2_EY + 1);                              // cN from row j0 - 2
+constexpr int C2_XX = C2_TX + 6, C2_XY = C2_TY + 4, C2_NX = C2_XX * C2_XY;  // x from (i0-3, j0-2)
 constexpr int C2_NH = C2_NE - C2_THREADS;                                // halo cells of step 1
 constexpr int C2_AHEAD = 3;                                              // planes copied ahead
 // ring depths in planes: when plane kk + C2_AHEAD is issued, inputs of
@@ -537,7 +540,10 @@ constexpr size_t C2_SMEM = sizeof(float) * (C2_RD * C2_SLOT + C2_RX * C2_NX + C2
 constexpr int C2_PLANES = 32;
 static_assert(C2_NH <= C2_THREADS && C2_NE <= 2 * C2_THREADS && C2_NCE <= 2 * C2_THREADS &&
                   C2_NCN <= 2 * C2_THREADS && C2_NX <= 2 * C2_THREADS,
-              "at most two elements of each tile per thread");
+              "one pair of cells of each tile per thread");
+static_assert(C2_EX % 2 == 0 && C2_WE % 2 == 0 && C2_XX % 2 == 0 && C2_SLOT % 2 == 0 && C2_NX % 2 == 0 &&
+                  C2_D % 2 == 0 && C2_N % 2 == 0,
+              "tile rows and ring slots of whole pairs");
 
 struct PairArgs {
     LevelView<float> F;
@@ -548,73 +554,62 @@ struct PairArgs {
     int planes;
 };
 
-// In-plane offsets (i + sy j) of this thread's elements of the four tile
-// shapes (two each) and a bit per element inside the ghosted array: the
-// same for every plane, so each copy is one add.
+// In-plane offsets (i + sy j) of this thread's pair of cells of each tile
+// and a bit per tile when the pair lies in the ghosted array: the same for
+// every plane, so each copy is one add.
 struct C2Offs {
-    int e[2], ce[2], cn[2], x[2];
+    int e, ce, cn, x;
     unsigned ok;
 };
 
-__device__ __forceinline__ void c2_off(const LevelView<float> &F, int q, int n, int w, int di, int dj, int i0,
+// Pair p of a tile w cells wide starting at (i0 + di, j0 + dj) with n cells.
+__device__ __forceinline__ void c2_off(const LevelView<float> &F, int p, int n, int w, int di, int dj, int i0,
                                        int j0, int *off, unsigned *ok, unsigned bit)
 {
-    const int qy = q / w, qx = q - qy * w;
+    const int wp = w / 2, qy = p / wp, qx = 2 * (p - qy * wp);
     const int i = i0 + di + qx, j = j0 + dj + qy;
     *off = i + F.sy * j;
-    if (q < n && (unsigned)i <= (unsigned)(F.n0 + 1) && (unsigned)j <= (unsigned)(F.n1 + 1)) *ok |= bit;
+    if (2 * p < n && i >= 0 && i + 1 <= F.n0 + 1 && (unsigned)j <= (unsigned)(F.n1 + 1)) *ok |= bit;
 }
 
 __device__ __forceinline__ C2Offs c2_offsets(const LevelView<float> &F, int i0, int j0, int tid)
 {
     C2Offs o;
     o.ok = 0u;
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const int q = tid + h * C2_THREADS;
-        c2_off(F, q, C2_NE, C2_EX, -1, -1, i0, j0, &o.e[h], &o.ok, 1u << h);
-        c2_off(F, q, C2_NCE, C2_EX + 1, -2, -1, i0, j0, &o.ce[h], &o.ok, 4u << h);
-        c2_off(F, q, C2_NCN, C2_EX, -1, -2, i0, j0, &o.cn[h], &o.ok, 16u << h);
-        c2_off(F, q, C2_NX, C2_XX, -2, -2, i0, j0, &o.x[h], &o.ok, 64u << h);
-    }
+    c2_off(F, tid, C2_NE, C2_EX, -1, -1, i0, j0, &o.e, &o.ok, 1u);
+    c2_off(F, tid, C2_NCE, C2_WE, -3, -1, i0, j0, &o.ce, &o.ok, 2u);
+    c2_off(F, tid, C2_NCN, C2_EX, -1, -2, i0, j0, &o.cn, &o.ok, 4u);
+    c2_off(F, tid, C2_NX, C2_XX, -3, -2, i0, j0, &o.x, &o.ok, 8u);
     return o;
 }
 
 __device__ __forceinline__ void c2_cp(float *dst, const float *src)
 {
-    __pipeline_memcpy_async(dst, src, sizeof(float));
+    __pipeline_memcpy_async(dst, src, 2 * sizeof(float));
 }
 
 // Copies of plane P's first-step inputs into `slot` (planes 0..n2: plane 0
-// only for its cT) and of x of plane X into `xs` (planes 0..n2+1).  Cells
+// only for its cT) and of x of plane X into `xs` (planes 0..n2+1).  Pairs
 // outside the ghosted array are not copied; no first step of an interior
 // cell reads them.
 __device__ __forceinline__ void c2_issue(const PairArgs &a, const C2Offs &o, float *slot, int P, float *xs, int X,
                                          int tid)
 {
     const LevelView<float> &F = a.F;
+    const int q = 2 * tid;
     if (P >= 0 && P <= F.n2) {
         const int base = F.sz * P;
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int q = tid + h * C2_THREADS;
-            if (o.ok & (1u << h)) {
-                const int c = base + o.e[h];
-                c2_cp(slot + C2_B + q, a.b + c);
-                c2_cp(slot + C2_D + q, F.diag + c);
-                if (a.dprev) c2_cp(slot + C2_P + q, a.dprev + c);
-                c2_cp(slot + C2_T + q, F.cT + c);
-            }
-            if (o.ok & (4u << h)) c2_cp(slot + C2_E + q, F.cE + base + o.ce[h]);
-            if (o.ok & (16u << h)) c2_cp(slot + C2_N + q, F.cN + base + o.cn[h]);
+        if (o.ok & 1u) {
+            const int c = base + o.e;
+            c2_cp(slot + C2_B + q, a.b + c);
+            c2_cp(slot + C2_D + q, F.diag + c);
+            if (a.dprev) c2_cp(slot + C2_P + q, a.dprev + c);
+            c2_cp(slot + C2_T + q, F.cT + c);
         }
+        if (o.ok & 2u) c2_cp(slot + C2_E + q, F.cE + base + o.ce);
+        if (o.ok & 4u) c2_cp(slot + C2_N + q, F.cN + base + o.cn);
     }
-    if (X >= 0 && X <= F.n2 + 1) {
-        const int base = F.sz * X;
-#pragma unroll
-        for (int h = 0; h < 2; ++h)
-            if (o.ok & (64u << h)) c2_cp(xs + tid + h * C2_THREADS, a.x + base + o.x[h]);
-    }
+    if (X >= 0 && X <= F.n2 + 1 && (o.ok & 8u)) c2_cp(xs + q, a.x + F.sz * X + o.x);
 }
 
 // Inputs of one cell's update, kept by the thread that applied the first
@@ -637,8 +632,8 @@ __device__ __forceinline__ float c2_first(const PairArgs &a, const float *dc, co
     k.b = dc[C2_B + q];
     k.dg = dc[C2_D + q];
     k.dinv = k.dg > 0.f ? __frcp_rn(k.dg) : 0.f;
-    k.ce = dc[C2_E + qe + 1];
-    k.cw = dc[C2_E + qe];
+    k.ce = dc[C2_E + qe + 2];
+    k.cw = dc[C2_E + qe + 1];
     k.cn = dc[C2_N + qn + C2_EX];
     k.cs = dc[C2_N + qn];
     k.ct = dc[C2_T + q];
@@ -669,9 +664,9 @@ __global__ void __launch_bounds__(C2_THREADS, 3) k_cheb_pair(PairArgs a)
     auto idx = [&](int ex, int ey, int &q, int &qe, int &qn, int &qx, bool &in) {
         const int i = i0 - 1 + ex, j = j0 - 1 + ey;
         q = ex + C2_EX * ey;
-        qe = ex + (C2_EX + 1) * ey;
+        qe = ex + C2_WE * ey;
         qn = ex + C2_EX * ey;
-        qx = (ex + 1) + C2_XX * (ey + 1);
+        qx = (ex + 2) + C2_XX * (ey + 1);
         in = i >= 1 && i <= F.n0 && j >= 1 && j <= F.n1;
     };
     int q0, qe0, qn0, qx0, qh = 0, qeh = 0, qnh = 0, qxh = 0;
@@ -760,7 +755,7 @@ template <typename T>
 int pair_planes(const MgLevel<T> &F)
 {
     const long long cells = (long long)F.n0 * F.n1 * F.n2;
-    if (sizeof(T) != 4 || g_pairs == 0 || cells < (1LL << 18)) return 0;
+    if (sizeof(T) != 4 || g_pairs == 0 || cells < (1LL << 18) || (F.n0 & 1)) return 0;
     if (g_pairs == 2) return g_pair_planes;
     if (cells < (1LL << 22)) return 0;
     const long long tiles = (long long)((F.n0 + C2_TX - 1) / C2_TX) * ((F.n1 + C2_TY - 1) / C2_TY);
@@ -784,10 +779,12 @@ cudaError_t pair_smem_attr()
 
 // Two Chebyshev steps (c1a, c2a) then (c1b, c2b) of FP32 level F from xin
 // into xout; dprev nullptr means the first step's previous update is xin
-// itself.
-void cheb_pair(const MgLevel<float> &F, const float *xin, const float *dprev, float *xout, float *dout, double c1a,
-               double c2a, double c1b, double c2b, cudaStream_t st)
+// itself.  Needs an even n0 (rows 8-byte aligned); otherwise launches
+// nothing and returns cudaErrorInvalidValue.
+cudaError_t cheb_pair(const MgLevel<float> &F, const float *xin, const float *dprev, float *xout, float *dout,
+                      double c1a, double c2a, double c1b, double c2b, cudaStream_t st)
 {
+    if (F.n0 & 1) return cudaErrorInvalidValue;
     PairArgs a;
     a.F = F.view();
     a.b = F.b; a.x = xin; a.dprev = dprev; a.xout = xout; a.dout = dout;
@@ -797,6 +794,7 @@ void cheb_pair(const MgLevel<float> &F, const float *xin, const float *dprev, fl
     const dim3 blk(C2_TX, C2_TY, 1);
     const dim3 grd((F.n0 + C2_TX - 1) / C2_TX, (F.n1 + C2_TY - 1) / C2_TY, (F.n2 + a.planes - 1) / a.planes);
     k_cheb_pair<<<grd, blk, C2_SMEM, st>>>(a);
+    return cudaSuccess;
 }
 
 // Chebyshev step with z-line Jacobi blocks: the preconditioner of the
@@ -1357,9 +1355,9 @@ void probe_smooth(MgLevel<T> &F, const ChebCoef &cc, cudaStream_t st)
     k_cheb_step<T><<<lf.grid, lf.block, 0, st>>>(F.view(), F.b, F.x, F.d, F.xb, F.d, (T)cc.c1[s], (T)cc.c2[s]);
 }
 
-void probe_smooth2(MgLevel<float> &F, const ChebCoef &cc, cudaStream_t st)
+cudaError_t probe_smooth2(MgLevel<float> &F, const ChebCoef &cc, cudaStream_t st)
 {
-    cheb_pair(F, F.x, F.d, F.xb, nullptr, cc.c1[1], cc.c2[1], cc.c1[2], cc.c2[2], st);
+    return cheb_pair(F, F.x, F.d, F.xb, nullptr, cc.c1[1], cc.c2[1], cc.c1[2], cc.c2[2], st);
 }
 
 template <typename T>

@@ -388,7 +388,8 @@ double kernel_bytes(const scf_ctx *ctx, int kernel)
     case SCF_K_RESTRICT: return 6.0 * s * n + s * n / 8.0;                // b,x,diag,cE,cN,cT in; coarse b out
     case SCF_K_PROLONG: return (mixed ? 8.0 : 9.0) * s * n + s * n / 8.0; // + coarse e; x,d out
     case SCF_K_CGUPDATE: return (mixed ? 60.0 : 64.0) * n;                // x,r,p,q,diag|dinv in; x,r,[rlow],x0 out
-    case SCF_K_SMOOTH2: return mixed ? 8.0 * s * n : -1.0;              // b,x,d,diag,cE,cN,cT in; x out
+    case SCF_K_SMOOTH2:                                                  // b,x,d,diag,cE,cN,cT in; x out
+        return mixed && ctx->d.I % 2 == 0 ? 8.0 * s * n : -1.0;        // (rows of whole pairs: even I)
     default: return -1.0;
     }
 }

@@ -148,7 +148,7 @@ void probe_restrict(MgLevel<T> &F, MgLevel<T> &C, cudaStream_t st);
 template <typename T>
 void probe_prolong(MgLevel<T> &F, MgLevel<T> &C, const ChebCoef &cc, cudaStream_t st);
 void probe_spmv(const LevelView<double> &A, const double *p, double *q, Reducer &R, cudaStream_t st);
-void probe_smooth2(MgLevel<float> &F, const ChebCoef &cc, cudaStream_t st);
+cudaError_t probe_smooth2(MgLevel<float> &F, const ChebCoef &cc, cudaStream_t st);   // n0 even
 
 // Large FP32 levels smooth two Chebyshev steps per pass (on: 1, the
 // default) or one (0); planes: k-planes per block of the two-step kernel
