@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(128) k_cg_update_df(DfOp A, float2 *__restrict
             const float2 rn = dadd(ld(r, c), dmul(mal, qq));
             r[c] = rn;
             rlow[c] = rn.x;
-            if (x0) x0[c] = first * (dg > 0.f ? __frcp_rn(dg) : 0.f) * rn.x;
+            if (x0) x0[c] = first * jacobi_inv(dg) * rn.x;
             const double rd = dwide(rn);
             v = fma(rd, rd, v);
         }

@@ -22,17 +22,16 @@
     const int c = i + (L).sy * j + (L).sz * k;
 
 // ---------------------------------------------------------------------------
-// Jacobi scaling.  FP32 levels compute 1/diag on the fly (FP32 division is
-// cheap, and it saves one array per pass); FP64 levels read a stored inverse
-// (FP64 division is slow on this GPU).  Inactive cells carry diag = -1 and
+// Jacobi scaling.  FP32 levels compute 1/diag on the fly with the hardware
+// reciprocal (one instruction, and it saves one array per pass); FP64 levels
+// read a stored inverse (FP64 division is slow on this GPU).  Inactive cells carry diag = -1 and
 // get no update and no coarse correction.
 template <typename T>
 __device__ __forceinline__ T dinv_at(const LevelView<T> &L, int c);
 template <>
 __device__ __forceinline__ float dinv_at<float>(const LevelView<float> &L, int c)
 {
-    const float d = L.diag[c];
-    return d > 0.0f ? __frcp_rn(d) : 0.0f;
+    return jacobi_inv(L.diag[c]);
 }
 template <>
 __device__ __forceinline__ double dinv_at<double>(const LevelView<double> &L, int c)
@@ -631,7 +630,7 @@ __device__ __forceinline__ float c2_first(const PairArgs &a, const float *dc, co
     }
     k.b = dc[C2_B + q];
     k.dg = dc[C2_D + q];
-    k.dinv = k.dg > 0.f ? __frcp_rn(k.dg) : 0.f;
+    k.dinv = jacobi_inv(k.dg);
     k.ce = dc[C2_E + qe + 2];
     k.cw = dc[C2_E + qe + 1];
     k.cn = dc[C2_N + qn + C2_EX];

@@ -60,6 +60,18 @@ struct LevelView {
     const T *diag, *dinv, *cE, *cN, *cT;
 };
 
+// Jacobi scaling of the FP32 V-cycle levels: 1/diag by the hardware
+// reciprocal (rcp.approx.ftz.f32, one instruction, within one unit in the
+// last place), 0 on inactive cells (diag <= 0).  Every FP32 smoothing
+// kernel uses it, so they agree bit for bit; the smoother needs no
+// correctly rounded reciprocal.
+__device__ __forceinline__ float jacobi_inv(float d)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(d));
+    return d > 0.0f ? r : 0.0f;
+}
+
 template <typename T>
 __device__ __forceinline__ T apply_row(const LevelView<T> &L, const T *__restrict__ x, int c)
 {
