@@ -582,77 +582,82 @@ __device__ __forceinline__ C2Offs c2_offsets(const LevelView<float> &F, int i0, 
     return o;
 }
 
-__device__ __forceinline__ void c2_cp(float *dst, const float *src)
+__device__ __forceinline__ void c2_cp(unsigned dst, const float *src)
 {
-    __pipeline_memcpy_async(dst, src, 2 * sizeof(float));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(dst), "l"(src) : "memory");
 }
 
-// Copies of plane P's first-step inputs into `slot` (planes 0..n2: plane 0
-// only for its cT) and of x of plane X into `xs` (planes 0..n2+1).  Pairs
+// Copies of plane P's first-step inputs into the ring slot at shared
+// address `slot` (planes 0..n2: plane 0 only for its cT) and of x of plane
+// X into the x plane at shared address `xs` (planes 0..n2+1).  Pairs
 // outside the ghosted array are not copied; no first step of an interior
 // cell reads them.
-__device__ __forceinline__ void c2_issue(const PairArgs &a, const C2Offs &o, float *slot, int P, float *xs, int X,
+template <bool DP>
+__device__ __forceinline__ void c2_issue(const PairArgs &a, const C2Offs &o, unsigned slot, int P, unsigned xs, int X,
                                          int tid)
 {
     const LevelView<float> &F = a.F;
-    const int q = 2 * tid;
+    const unsigned q = 8u * tid;     // bytes
     if (P >= 0 && P <= F.n2) {
         const int base = F.sz * P;
         if (o.ok & 1u) {
             const int c = base + o.e;
-            c2_cp(slot + C2_B + q, a.b + c);
-            c2_cp(slot + C2_D + q, F.diag + c);
-            if (a.dprev) c2_cp(slot + C2_P + q, a.dprev + c);
-            c2_cp(slot + C2_T + q, F.cT + c);
+            c2_cp(slot + 4u * C2_B + q, a.b + c);
+            c2_cp(slot + 4u * C2_D + q, F.diag + c);
+            if (DP) c2_cp(slot + 4u * C2_P + q, a.dprev + c);
+            c2_cp(slot + 4u * C2_T + q, F.cT + c);
         }
-        if (o.ok & 2u) c2_cp(slot + C2_E + q, F.cE + base + o.ce);
-        if (o.ok & 4u) c2_cp(slot + C2_N + q, F.cN + base + o.cn);
+        if (o.ok & 2u) c2_cp(slot + 4u * C2_E + q, F.cE + base + o.ce);
+        if (o.ok & 4u) c2_cp(slot + 4u * C2_N + q, F.cN + base + o.cn);
     }
     if (X >= 0 && X <= F.n2 + 1 && (o.ok & 8u)) c2_cp(xs + q, a.x + F.sz * X + o.x);
 }
 
-// Inputs of one cell's update, kept by the thread that applied the first
-// step to its own column for the second step one plane later.
 struct C2Cell {
     float b, dg, dinv, ce, cw, cn, cs, ct, cb;
 };
 
-// First step at plane P on cell q = ex + 34 ey of the tile (qx: the same
-// cell in the x tile), `in` whether (i, j) is an interior column: writes x
-// after the step into o1, returns the update and the cell's inputs.
-__device__ __forceinline__ float c2_first(const PairArgs &a, const float *dc, const float *dm, const float *xm,
-                                          const float *x0, const float *xp, float *o1, int q, int qe, int qn,
-                                          int qx, bool in, C2Cell &k)
+// First step at plane P on cell q = ex + 34 ey of the tile: the plane's
+// inputs at offset dc (the plane below at dm) of the shared array S, x of
+// planes P - 1, P, P + 1 at xm, x0, xp (qx: the cell in the x tile), x after
+// the step written at o1; `in` whether the cell is interior.  Returns the
+// update and the cell's inputs.
+template <bool DP>
+__device__ __forceinline__ float c2_first(const PairArgs &a, float *S, int dc, int dm, int xm, int x0, int xp, int o1,
+                                          int q, int qe, int qn, int qx, bool in, C2Cell &k)
 {
     if (!in) {
-        o1[q] = 0.f;
+        S[o1 + q] = 0.f;
         return 0.f;
     }
-    k.b = dc[C2_B + q];
-    k.dg = dc[C2_D + q];
+    k.b = S[dc + C2_B + q];
+    k.dg = S[dc + C2_D + q];
     k.dinv = jacobi_inv(k.dg);
-    k.ce = dc[C2_E + qe + 2];
-    k.cw = dc[C2_E + qe + 1];
-    k.cn = dc[C2_N + qn + C2_EX];
-    k.cs = dc[C2_N + qn];
-    k.ct = dc[C2_T + q];
-    k.cb = dm[C2_T + q];
-    const float xc = x0[qx];
-    const float dn = cheb_update(k.b, k.dg, k.dinv, xc, x0[qx + 1], x0[qx - 1], x0[qx + C2_XX], x0[qx - C2_XX],
-                                 xp[qx], xm[qx], k.ce, k.cw, k.cn, k.cs, k.ct, k.cb, a.dprev ? dc[C2_P + q] : xc,
-                                 a.c1a, a.c2a);
-    o1[q] = fx_add(xc, dn);
+    k.ce = S[dc + C2_E + qe + 2];
+    k.cw = S[dc + C2_E + qe + 1];
+    k.cn = S[dc + C2_N + qn + C2_EX];
+    k.cs = S[dc + C2_N + qn];
+    k.ct = S[dc + C2_T + q];
+    k.cb = S[dm + C2_T + q];
+    const float xc = S[x0 + qx];
+    const float dn = cheb_update(k.b, k.dg, k.dinv, xc, S[x0 + qx + 1], S[x0 + qx - 1], S[x0 + qx + C2_XX],
+                                 S[x0 + qx - C2_XX], S[xp + qx], S[xm + qx], k.ce, k.cw, k.cn, k.cs, k.ct, k.cb,
+                                 DP ? S[dc + C2_P + q] : xc, a.c1a, a.c2a);
+    S[o1 + q] = fx_add(xc, dn);
     return dn;
 }
 
 __device__ __forceinline__ int c2_wrap(int i, int r) { return i >= r ? i - r : i; }
 
+template <bool DP, bool DO>
 __global__ void __launch_bounds__(C2_THREADS, 3) k_cheb_pair(PairArgs a)
 {
     extern __shared__ __align__(16) float c2_smem[];
-    float *sd = c2_smem;                   // C2_RD slots of first-step inputs
-    float *sx = sd + C2_RD * C2_SLOT;      // C2_RX planes of x
-    float *s1 = sx + C2_RX * C2_NX;        // C2_R1 planes of x after the first step
+    float *S = c2_smem;
+    // offsets in S: C2_RD slots of first-step inputs, C2_RX planes of x,
+    // C2_R1 planes of x after the first step
+    constexpr int SD = 0, SX = C2_RD * C2_SLOT, S1 = SX + C2_RX * C2_NX;
+    const unsigned sbase = (unsigned)__cvta_generic_to_shared(c2_smem);
     const LevelView<float> &F = a.F;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + C2_TX * ty;
     const int i0 = blockIdx.x * C2_TX + 1, j0 = blockIdx.y * C2_TY + 1;
@@ -682,10 +687,12 @@ __global__ void __launch_bounds__(C2_THREADS, 3) k_cheb_pair(PairArgs a)
     // group g: inputs of plane g and x of plane g + 1 (the first group also
     // x of plane k0 - 2); groups k0 - 2 .. k0 - 2 + C2_AHEAD before the loop.
     // Ring index of plane P: (P + 2) mod depth (P >= k0 - 2 >= -1).
-    c2_issue(a, o, sd + ((k0) % C2_RD) * C2_SLOT, k0 - 2, sx + ((k0) % C2_RX) * C2_NX, k0 - 2, tid);
+    auto issue = [&](int rslot, int P, int rxs, int X) {
+        c2_issue<DP>(a, o, sbase + 4u * (SD + rslot * C2_SLOT), P, sbase + 4u * (SX + rxs * C2_NX), X, tid);
+    };
+    issue(k0 % C2_RD, k0 - 2, k0 % C2_RX, k0 - 2);
     for (int g = k0 - 2; g <= k0 - 2 + C2_AHEAD; ++g) {
-        c2_issue(a, o, sd + ((g + 2) % C2_RD) * C2_SLOT, g == k0 - 2 ? -1 : g, sx + ((g + 3) % C2_RX) * C2_NX, g + 1,
-                 tid);
+        issue((g + 2) % C2_RD, g == k0 - 2 ? -1 : g, (g + 3) % C2_RX, g + 1);
         __pipeline_commit();
     }
     // ring indices of plane kk (and the planes around it), advanced by one per plane
@@ -693,37 +700,35 @@ __global__ void __launch_bounds__(C2_THREADS, 3) k_cheb_pair(PairArgs a)
     float d1 = 0.f;     // first-step update of this thread's column, plane below
     C2Cell kc = {}, kp = {};
     const bool out_ok = tx + i0 <= F.n0 && ty + j0 <= F.n1;
-    for (int kk = k0 - 1; kk <= k1 + 1; ++kk) {
+    int c = (i0 + tx) + F.sy * (j0 + ty) + F.sz * (k0 - 2);   // output cell at plane kk - 1
+    for (int kk = k0 - 1; kk <= k1 + 1; ++kk, c += F.sz) {
         const int g = kk + C2_AHEAD;
-        if (g <= k1 + 1)
-            c2_issue(a, o, sd + c2_wrap(rd + C2_AHEAD, C2_RD) * C2_SLOT, g,
-                     sx + c2_wrap(rx + C2_AHEAD + 1, C2_RX) * C2_NX, g + 1, tid);
+        if (g <= k1 + 1) issue(c2_wrap(rd + C2_AHEAD, C2_RD), g, c2_wrap(rx + C2_AHEAD + 1, C2_RX), g + 1);
         __pipeline_commit();
         __pipeline_wait_prior(C2_AHEAD);    // groups up to kk have landed
         __syncthreads();
-        const float *dc = sd + rd * C2_SLOT, *dm = sd + (rd == 0 ? C2_RD - 1 : rd - 1) * C2_SLOT;
-        const float *x0 = sx + rx * C2_NX, *xm = sx + (rx == 0 ? C2_RX - 1 : rx - 1) * C2_NX;
-        const float *xp = sx + c2_wrap(rx + 1, C2_RX) * C2_NX;
-        float *o1 = s1 + r1 * C2_NE;
+        const int dc = SD + rd * C2_SLOT, dm = SD + (rd == 0 ? C2_RD - 1 : rd - 1) * C2_SLOT;
+        const int x0 = SX + rx * C2_NX, xm = SX + (rx == 0 ? C2_RX - 1 : rx - 1) * C2_NX;
+        const int xp = SX + c2_wrap(rx + 1, C2_RX) * C2_NX;
+        const int o1 = S1 + r1 * C2_NE;
         const bool plane_in = kk >= 1 && kk <= F.n2;
-        const float dn1 = c2_first(a, dc, dm, xm, x0, xp, o1, q0, qe0, qn0, qx0, in0 && plane_in, kc);
+        const float dn1 = c2_first<DP>(a, S, dc, dm, xm, x0, xp, o1, q0, qe0, qn0, qx0, in0 && plane_in, kc);
         if (halo) {
             C2Cell kh;
-            c2_first(a, dc, dm, xm, x0, xp, o1, qh, qeh, qnh, qxh, inh && plane_in, kh);
+            c2_first<DP>(a, S, dc, dm, xm, x0, xp, o1, qh, qeh, qnh, qxh, inh && plane_in, kh);
         }
         __syncthreads();
-        const int Q = kk - 1;
-        if (Q >= k0 && out_ok) {
-            // second step at plane Q from the first-step planes Q - 1, Q, Q + 1
-            const int r1m = r1 == 0 ? C2_R1 - 1 : r1 - 1, r1m2 = r1m == 0 ? C2_R1 - 1 : r1m - 1;
-            const float *y0 = s1 + r1m * C2_NE, *ym = s1 + r1m2 * C2_NE, *yp = o1;
+        if (kk - 1 >= k0 && out_ok) {
+            // second step at plane kk - 1 from the first-step planes kk - 2 .. kk
+            const int r1m = r1 == 0 ? C2_R1 - 1 : r1 - 1;
+            const int y0 = S1 + r1m * C2_NE, ym = S1 + (r1m == 0 ? C2_R1 - 1 : r1m - 1) * C2_NE, yp = o1;
             const int q = q0;
-            const float xc = y0[q];
-            const float dn = cheb_update(kp.b, kp.dg, kp.dinv, xc, y0[q + 1], y0[q - 1], y0[q + C2_EX], y0[q - C2_EX],
-                                         yp[q], ym[q], kp.ce, kp.cw, kp.cn, kp.cs, kp.ct, kp.cb, d1, a.c1b, a.c2b);
-            const int c = (i0 + tx) + F.sy * (j0 + ty) + F.sz * Q;
+            const float xc = S[y0 + q];
+            const float dn = cheb_update(kp.b, kp.dg, kp.dinv, xc, S[y0 + q + 1], S[y0 + q - 1], S[y0 + q + C2_EX],
+                                         S[y0 + q - C2_EX], S[yp + q], S[ym + q], kp.ce, kp.cw, kp.cn, kp.cs, kp.ct,
+                                         kp.cb, d1, a.c1b, a.c2b);
             a.xout[c] = fx_add(xc, dn);
-            if (a.dout) a.dout[c] = dn;
+            if (DO) a.dout[c] = dn;
         }
         d1 = dn1;
         kp = kc;
@@ -771,8 +776,16 @@ bool use_pairs(const MgLevel<T> &F)
 
 cudaError_t pair_smem_attr()
 {
-    static const cudaError_t rc =
-        cudaFuncSetAttribute(k_cheb_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C2_SMEM);
+    static const cudaError_t rc = [] {
+        cudaError_t e = cudaSuccess;
+        const void *fns[4] = {(const void *)k_cheb_pair<false, false>, (const void *)k_cheb_pair<false, true>,
+                              (const void *)k_cheb_pair<true, false>, (const void *)k_cheb_pair<true, true>};
+        for (const void *f : fns) {
+            const cudaError_t r = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C2_SMEM);
+            if (r != cudaSuccess) e = r;
+        }
+        return e;
+    }();
     return rc;
 }
 
@@ -792,7 +805,10 @@ cudaError_t cheb_pair(const MgLevel<float> &F, const float *xin, const float *dp
     pair_smem_attr();
     const dim3 blk(C2_TX, C2_TY, 1);
     const dim3 grd((F.n0 + C2_TX - 1) / C2_TX, (F.n1 + C2_TY - 1) / C2_TY, (F.n2 + a.planes - 1) / a.planes);
-    k_cheb_pair<<<grd, blk, C2_SMEM, st>>>(a);
+    if (dprev && dout) k_cheb_pair<true, true><<<grd, blk, C2_SMEM, st>>>(a);
+    else if (dprev) k_cheb_pair<true, false><<<grd, blk, C2_SMEM, st>>>(a);
+    else if (dout) k_cheb_pair<false, true><<<grd, blk, C2_SMEM, st>>>(a);
+    else k_cheb_pair<false, false><<<grd, blk, C2_SMEM, st>>>(a);
     return cudaSuccess;
 }
 
