@@ -527,7 +527,7 @@ constexpr int C2_WE = C2_TX + 4, C2_NCE = C2_WE * C2_EY;                 // cE f
 constexpr int C2_NCN = C2_EX * (C2_EY + 1);                              // cN from row j0 - 2
 constexpr int C2_XX = C2_TX + 6, C2_XY = C2_TY + 4, C2_NX = C2_XX * C2_XY;  // x from (i0-3, j0-2)
 constexpr int C2_NH = C2_NE - C2_THREADS;                                // halo cells of step 1
-constexpr int C2_AHEAD = 3;                                              // planes copied ahead
+constexpr int C2_AHEAD = 1;                                              // planes copied ahead
 // ring depths in planes: when plane kk + C2_AHEAD is issued, inputs of
 // planes kk - 1 .. kk + C2_AHEAD - 1 and x of planes kk - 1 .. kk + C2_AHEAD
 // are in use or on their way (the second step reads no inputs: the thread
@@ -650,7 +650,7 @@ __device__ __forceinline__ float c2_first(const PairArgs &a, float *S, int dc, i
 __device__ __forceinline__ int c2_wrap(int i, int r) { return i >= r ? i - r : i; }
 
 template <bool DP, bool DO>
-__global__ void __launch_bounds__(C2_THREADS, 3) k_cheb_pair(PairArgs a)
+__global__ void __launch_bounds__(C2_THREADS, 4) k_cheb_pair(PairArgs a)
 {
     extern __shared__ __align__(16) float c2_smem[];
     float *S = c2_smem;
@@ -741,7 +741,7 @@ __global__ void __launch_bounds__(C2_THREADS, 3) k_cheb_pair(PairArgs a)
 
 // Smoother pairing: 1 (the default) on the levels where the pair kernel
 // measured faster than two one-step launches -- at least 2^22 cells, with
-// at least two waves of three blocks per SM -- 2 on every FP32 level of at
+// at least two waves of four blocks per SM -- 2 on every FP32 level of at
 // least 2^18 cells, 0 off; k-planes per block of the pair kernel (fewer
 // when that fills the grid).
 static int g_pairs = 1, g_pair_planes = C2_PLANES;
@@ -764,7 +764,7 @@ int pair_planes(const MgLevel<T> &F)
     if (cells < (1LL << 22)) return 0;
     const long long tiles = (long long)((F.n0 + C2_TX - 1) / C2_TX) * ((F.n1 + C2_TY - 1) / C2_TY);
     for (int planes = g_pair_planes; planes >= 8; planes /= 2)
-        if (tiles * ((F.n2 + planes - 1) / planes) >= 2LL * 3 * 152) return planes;
+        if (tiles * ((F.n2 + planes - 1) / planes) >= 2LL * 4 * 152) return planes;
     return 0;
 }
 
