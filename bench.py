@@ -158,7 +158,9 @@ def measured_peaks():
 SMOOTH_TRAFFIC_256 = {
     "smooth": {"bytes": 213.5e6 * 16777216 / 7077888,
                "note": "first pre-smoothing step (32 B/cell algorithmic), ncu at 192^3 scaled by cells"},
-    "smooth2": None,
+    "smooth2": {"bytes": 216.8e6 * 16777216 / 7077888,
+                "note": "first pre-smoothing pair (32 B/cell algorithmic for two steps), ncu at 192^3 "
+                        "(16 k-planes per block there, 32 at 256^3) scaled by cells"},
 }
 
 
@@ -651,7 +653,9 @@ def run_ours(args):
                                % max(1, args.steps // 5),
                      "ms_per_launch_isolated": round(iso_ms, 5),
                      "traffic": round(trf["bytes"]) if trf else None,
-                     "traffic_note": trf["note"] if trf else None},
+                     "traffic_note": trf["note"] if trf else None,
+                     # a pair launch does the work of two one-step launches
+                     "one_step_equivalent_gbs": round(2 * achieved, 1) if kind == "smooth2" else None},
         "kernels_live": live,
         "oracle_solve": errors.get("oracle"),
         "configs": configs or None,
