@@ -353,6 +353,11 @@ int64_t scf_debug_device_buffers(void);
  * of the fused kernel (0: the default, 32).  Process-wide; applies from the
  * next solve of every context.                                             */
 int scf_debug_smoother_pairs(int on, int planes);
+/* Process-wide counts of fused-pair launches: those of the TMA-staged
+ * kernel, and those that ran as two one-step launches instead because a
+ * tensor map could not be encoded (none expected).  Either pointer may be
+ * NULL.                                                                    */
+int scf_debug_smoother_pair_counts(int64_t *tma_launches, int64_t *fallbacks);
 
 #ifdef __cplusplus
 }

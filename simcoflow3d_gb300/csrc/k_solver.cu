@@ -10,7 +10,11 @@
 // diagonal is the sum of the coarse couplings plus half the children's
 // Dirichlet terms.  Dot products are reduced per block and then in one block
 // in a fixed order, so results are bitwise reproducible.
-#include <cuda_pipeline.h>
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <stdint.h>
+
+#include <atomic>
 
 #include "scf_kernels.h"
 
@@ -501,242 +505,292 @@ __global__ void __launch_bounds__(256) k_cheb_step(LevelView<T> L, const T *__re
 }
 
 // ---------------------------------------------------------------------------
+// ---------------------------------------------------------------------------
 // Two Chebyshev steps in one pass over a large FP32 level (2.5-D temporal
-// blocking).  A block owns a tile of 32 x 8 (i, j) columns and marches along
-// k over `planes` planes.  For plane kk it
-//   1. issues the asynchronous copies (cp.async) of plane kk + C2_AHEAD:
-//      operator, right-hand side and previous update on the tile with a
-//      one-cell halo, and x of the plane above it with a two-cell halo, into
-//      rings in shared memory, so that C2_AHEAD planes are in flight while
-//      plane kk is computed;
-//   2. applies the first step on the 34 x 10 cells of plane kk (ghost cells
-//      give 0, the value the one-step kernel leaves there) into a
-//      three-plane ring in shared memory;
-//   3. applies the second step on the 32 x 8 cells of plane kk - 1.
-// Each array is read from DRAM about once per pass (halo columns come from
-// L2), so two steps move about the bytes of one.  Both steps go through
-// cheb_update: the result is that of two k_cheb_step launches, bit for bit.
-// The output x must not be the input x, nor dout the previous update when
-// both are given: neighbouring tiles read their halos from them.
+// blocking), with the inputs staged by the Tensor Memory Accelerator.
+//
+// A block owns a tile of 32 x 8 (i, j) columns and marches along k over
+// `planes` planes.  Group P holds plane P's inputs on the tile and its halo
+// (b, diag, cT and the previous update on 34 x 10 cells, cE one column
+// wider to the west, cN one row wider to the south) and x of plane P with a
+// two-cell halo.  For plane kk the block
+//   1. has one thread issue the TMA copies of group kk + 2 into a four-slot
+//      ring in shared memory; they complete on that slot's mbarrier;
+//   2. waits for group kk + 1 (groups kk - 1 and kk landed earlier) and
+//      applies the first step on the 34 x 10 cells of plane kk (ghost cells
+//      give 0, the value the one-step kernel leaves there) into a four-plane
+//      ring in shared memory;
+//   3. after one block barrier, applies the second step on the 32 x 8 cells
+//      of plane kk - 1.
+// The four-deep rings make that single barrier per plane enough: the slot a
+// copy or a first step overwrites was last read before the previous
+// plane's barrier.  Each array is read from DRAM about once per pass (halo
+// columns come from L2), so two steps move about the bytes of one, and no
+// thread spends instructions on copies.  Both steps go through cheb_update:
+// the result is that of two k_cheb_step launches, bit for bit.  The output
+// x must not be the input x, nor dout the previous update when both are
+// given: neighbouring tiles read their halos from them.
+//
+// Row pairs.  TMA wants every global stride to be a multiple of 16 bytes; a
+// row of the padded layout (n0 + 2 floats) is one only when n0 + 2 is a
+// multiple of 4, but with n0 even two consecutive rows are.  So the tensor
+// map views a level as (2 sy, (n1 + 2) / 2, n2 + 2) floats -- row pair, row
+// pairs, planes -- and each array's tile arrives as two boxes: one over the
+// even rows of its row pairs (x = i) and one over the odd rows (x = sy + i).
+// A box's first x is rounded down to a multiple of 4 floats (16 bytes), as
+// TMA requires; the tile's columns then start 0, 2 or 4 floats into it.
+// Coordinates outside the tensor (the ghost ring's outside, a last unpaired
+// row when n1 is odd, planes -1 and n2 + 2) read as 0.  Conditions: n0 even
+// and sy (n1 + 2) a multiple of 4 (the plane stride in 16-byte units);
+// other levels smooth with one-step launches.
 constexpr int C2_TX = 32, C2_TY = 8, C2_THREADS = C2_TX * C2_TY;
-// Tiles in shared memory, each starting on an even column (i0 - 1 or
-// i0 - 3): with an even row length n0 + 2 every row starts 8-byte aligned,
-// so each thread copies at most one pair of cells of each tile per plane.
 constexpr int C2_EX = C2_TX + 2, C2_EY = C2_TY + 2, C2_NE = C2_EX * C2_EY;  // first-step cells, from (i0-1, j0-1)
-constexpr int C2_WE = C2_TX + 4, C2_NCE = C2_WE * C2_EY;                 // cE from column i0 - 3
-constexpr int C2_NCN = C2_EX * (C2_EY + 1);                              // cN from row j0 - 2
-constexpr int C2_XX = C2_TX + 6, C2_XY = C2_TY + 4, C2_NX = C2_XX * C2_XY;  // x from (i0-3, j0-2)
 constexpr int C2_NH = C2_NE - C2_THREADS;                                // halo cells of step 1
-constexpr int C2_AHEAD = 1;                                              // planes copied ahead
-// ring depths in planes: when plane kk + C2_AHEAD is issued, inputs of
-// planes kk - 1 .. kk + C2_AHEAD - 1 and x of planes kk - 1 .. kk + C2_AHEAD
-// are in use or on their way (the second step reads no inputs: the thread
-// keeps its column's from the first step)
-constexpr int C2_RD = C2_AHEAD + 2, C2_RX = C2_AHEAD + 3, C2_R1 = 3;
-constexpr int C2_B = 0, C2_D = C2_NE, C2_P = 2 * C2_NE, C2_T = 3 * C2_NE, C2_E = 4 * C2_NE,
-              C2_N = 4 * C2_NE + C2_NCE, C2_SLOT = 4 * C2_NE + C2_NCE + C2_NCN;
-constexpr size_t C2_SMEM = sizeof(float) * (C2_RD * C2_SLOT + C2_RX * C2_NX + C2_R1 * C2_NE);
+// box widths (floats) and heights (row pairs): b, diag, cT, dprev and cN
+// from column i0 - 1 (36 wide), cE and x from column i0 - 2 (40 wide); b,
+// diag, cT, dprev and cE from row j0 - 1 (5 pairs), cN from row j0 - 3
+// (6 pairs), x from row j0 - 3 (7 pairs)
+constexpr int C2_WA = 36, C2_WE = 40, C2_HA = 5, C2_HN = 6, C2_HX = 7;
+// one box per parity, each starting on a 128-byte boundary (floats)
+constexpr int C2_BA = 192, C2_BE = 224, C2_BN = 224, C2_BX = 288;
+static_assert(C2_WA * C2_HA <= C2_BA && C2_WE * C2_HA <= C2_BE && C2_WA * C2_HN <= C2_BN && C2_WE * C2_HX <= C2_BX,
+              "boxes fit their slots");
+static_assert(C2_BA % 32 == 0 && C2_BE % 32 == 0 && C2_BN % 32 == 0 && C2_BX % 32 == 0, "128-byte boxes");
+// a group slot: b, diag, cT, dprev, cE, cN, x (two boxes each)
+constexpr int C2_GB = 0, C2_GD = 2 * C2_BA, C2_GT = 4 * C2_BA, C2_GP = 6 * C2_BA, C2_GE = 8 * C2_BA,
+              C2_GN = C2_GE + 2 * C2_BE, C2_GX = C2_GN + 2 * C2_BN, C2_SLOT = C2_GX + 2 * C2_BX;
+constexpr int C2_DEPTH = 4;                                 // group slots (ring of planes)
+constexpr int C2_R1 = 4;                                    // first-step result planes
+constexpr int C2_R1N = ((C2_R1 * C2_NE + 31) / 32) * 32;    // floats, rounded to 128 bytes
+constexpr size_t C2_SMEM = 128 + sizeof(float) * (C2_DEPTH * C2_SLOT + C2_R1N) + 8 * C2_DEPTH;
 constexpr int C2_PLANES = 32;
-static_assert(C2_NH <= C2_THREADS && C2_NE <= 2 * C2_THREADS && C2_NCE <= 2 * C2_THREADS &&
-                  C2_NCN <= 2 * C2_THREADS && C2_NX <= 2 * C2_THREADS,
-              "one pair of cells of each tile per thread");
-static_assert(C2_EX % 2 == 0 && C2_WE % 2 == 0 && C2_XX % 2 == 0 && C2_SLOT % 2 == 0 && C2_NX % 2 == 0 &&
-                  C2_D % 2 == 0 && C2_N % 2 == 0,
-              "tile rows and ring slots of whole pairs");
+// bytes a group's copies deliver (full boxes, out-of-range parts as 0)
+constexpr unsigned C2_TX_BYTES_NODP = 2u * 4u * (3 * C2_WA * C2_HA + C2_WE * C2_HA + C2_WA * C2_HN + C2_WE * C2_HX);
+constexpr unsigned C2_TX_BYTES_DP = C2_TX_BYTES_NODP + 2u * 4u * C2_WA * C2_HA;
+static_assert(C2_NH <= C2_THREADS, "one halo cell per thread at most");
+// polls of an mbarrier before a wait gives up (each poll may suspend the
+// thread for a while; together well over a second, far beyond any copy)
+constexpr unsigned C2_WAIT_POLLS = 1u << 22;
+
+// tensor maps of the pair kernel's inputs: b, diag, cT, dprev, cE, cN, x
+struct PairMaps {
+    CUtensorMap m[7];
+};
 
 struct PairArgs {
     LevelView<float> F;
-    const float *b, *x;
-    const float *dprev;          // nullptr: the first step's previous update is x itself
     float *xout, *dout;          // dout nullptr: the second step's update is not kept
+    unsigned *flags;             // FLAG_WAIT_TIMEOUT if a copy never landed
     float c1a, c2a, c1b, c2b;
     int planes;
 };
 
-// In-plane offsets (i + sy j) of this thread's pair of cells of each tile
-// and a bit per tile when the pair lies in the ghosted array: the same for
-// every plane, so each copy is one add.
-struct C2Offs {
-    int e, ce, cn, x;
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity)
+{
     unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for the phase of the given parity; false if it gave up.
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity)
+{
+    for (unsigned it = 0; it < C2_WAIT_POLLS; ++it)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+// 3-D tiled TMA load of one box into shared memory, completing on `bar`.
+__device__ __forceinline__ void tma_load3(unsigned dst, const CUtensorMap *map, int x, int y, int z, unsigned bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];\n" ::"r"(dst),
+        "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
+        : "memory");
+}
+
+// Offsets in a group slot (floats) of one first-step cell (ex, ey) of the
+// 34 x 10 tile: its b/diag/cT/dprev element (a), cE (e; cE of the west
+// neighbour at e - 1), cN (n) and cN of the south neighbour (s), x (x; east
+// and west at x +- 1) and x of the north and south neighbours (xn, xs).
+// shA/shE: the column in a box of the tile's first column, per row parity.
+struct C2Idx {
+    int a, e, n, s, x, xn, xs;
 };
 
-// Pair p of a tile w cells wide starting at (i0 + di, j0 + dj) with n cells.
-__device__ __forceinline__ void c2_off(const LevelView<float> &F, int p, int n, int w, int di, int dj, int i0,
-                                       int j0, int *off, unsigned *ok, unsigned bit)
+__device__ __forceinline__ C2Idx c2_idx(int ex, int ey, const int shA[2], const int shE[2])
 {
-    const int wp = w / 2, qy = p / wp, qx = 2 * (p - qy * wp);
-    const int i = i0 + di + qx, j = j0 + dj + qy;
-    *off = i + F.sy * j;
-    if (2 * p < n && i >= 0 && i + 1 <= F.n0 + 1 && (unsigned)j <= (unsigned)(F.n1 + 1)) *ok |= bit;
-}
-
-__device__ __forceinline__ C2Offs c2_offsets(const LevelView<float> &F, int i0, int j0, int tid)
-{
-    C2Offs o;
-    o.ok = 0u;
-    c2_off(F, tid, C2_NE, C2_EX, -1, -1, i0, j0, &o.e, &o.ok, 1u);
-    c2_off(F, tid, C2_NCE, C2_WE, -3, -1, i0, j0, &o.ce, &o.ok, 2u);
-    c2_off(F, tid, C2_NCN, C2_EX, -1, -2, i0, j0, &o.cn, &o.ok, 4u);
-    c2_off(F, tid, C2_NX, C2_XX, -3, -2, i0, j0, &o.x, &o.ok, 8u);
-    return o;
-}
-
-__device__ __forceinline__ void c2_cp(unsigned dst, const float *src)
-{
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(dst), "l"(src) : "memory");
-}
-
-// Copies of plane P's first-step inputs into the ring slot at shared
-// address `slot` (planes 0..n2: plane 0 only for its cT) and of x of plane
-// X into the x plane at shared address `xs` (planes 0..n2+1).  Pairs
-// outside the ghosted array are not copied; no first step of an interior
-// cell reads them.
-template <bool DP>
-__device__ __forceinline__ void c2_issue(const PairArgs &a, const C2Offs &o, unsigned slot, int P, unsigned xs, int X,
-                                         int tid)
-{
-    const LevelView<float> &F = a.F;
-    const unsigned q = 8u * tid;     // bytes
-    if (P >= 0 && P <= F.n2) {
-        const int base = F.sz * P;
-        if (o.ok & 1u) {
-            const int c = base + o.e;
-            c2_cp(slot + 4u * C2_B + q, a.b + c);
-            c2_cp(slot + 4u * C2_D + q, F.diag + c);
-            if (DP) c2_cp(slot + 4u * C2_P + q, a.dprev + c);
-            c2_cp(slot + 4u * C2_T + q, F.cT + c);
-        }
-        if (o.ok & 2u) c2_cp(slot + 4u * C2_E + q, F.cE + base + o.ce);
-        if (o.ok & 4u) c2_cp(slot + 4u * C2_N + q, F.cN + base + o.cn);
-    }
-    if (X >= 0 && X <= F.n2 + 1 && (o.ok & 8u)) c2_cp(xs + q, a.x + F.sz * X + o.x);
+    const int p = ey & 1, q = p ^ 1;
+    C2Idx t;
+    t.a = p * C2_BA + (ey >> 1) * C2_WA + ex + shA[p];
+    t.e = C2_GE + p * C2_BE + (ey >> 1) * C2_WE + ex + shE[p];
+    t.n = C2_GN + p * C2_BN + ((ey + 2) >> 1) * C2_WA + ex + shA[p];
+    t.s = C2_GN + q * C2_BN + ((ey + 1) >> 1) * C2_WA + ex + shA[q];
+    t.x = C2_GX + p * C2_BX + ((ey + 2) >> 1) * C2_WE + ex + shE[p];
+    t.xn = C2_GX + q * C2_BX + ((ey + 3) >> 1) * C2_WE + ex + shE[q];
+    t.xs = C2_GX + q * C2_BX + ((ey + 1) >> 1) * C2_WE + ex + shE[q];
+    return t;
 }
 
 struct C2Cell {
     float b, dg, dinv, ce, cw, cn, cs, ct, cb;
 };
 
-// First step at plane P on cell q = ex + 34 ey of the tile: the plane's
-// inputs at offset dc (the plane below at dm) of the shared array S, x of
-// planes P - 1, P, P + 1 at xm, x0, xp (qx: the cell in the x tile), x after
-// the step written at o1; `in` whether the cell is interior.  Returns the
-// update and the cell's inputs.
+// First step on one cell: G, Gm, Gp the group slots of planes kk, kk - 1,
+// kk + 1; x after the step written at o1[q]; `in` whether the cell is
+// interior.  Returns the update and the cell's inputs.
 template <bool DP>
-__device__ __forceinline__ float c2_first(const PairArgs &a, float *S, int dc, int dm, int xm, int x0, int xp, int o1,
-                                          int q, int qe, int qn, int qx, bool in, C2Cell &k)
+__device__ __forceinline__ float c2_first(const PairArgs &a, const float *G, const float *Gm, const float *Gp,
+                                          const C2Idx &t, float *o1, int q, bool in, C2Cell &k)
 {
     if (!in) {
-        S[o1 + q] = 0.f;
+        o1[q] = 0.f;
         return 0.f;
     }
-    k.b = S[dc + C2_B + q];
-    k.dg = S[dc + C2_D + q];
+    k.b = G[C2_GB + t.a];
+    k.dg = G[C2_GD + t.a];
     k.dinv = jacobi_inv(k.dg);
-    k.ce = S[dc + C2_E + qe + 2];
-    k.cw = S[dc + C2_E + qe + 1];
-    k.cn = S[dc + C2_N + qn + C2_EX];
-    k.cs = S[dc + C2_N + qn];
-    k.ct = S[dc + C2_T + q];
-    k.cb = S[dm + C2_T + q];
-    const float xc = S[x0 + qx];
-    const float dn = cheb_update(k.b, k.dg, k.dinv, xc, S[x0 + qx + 1], S[x0 + qx - 1], S[x0 + qx + C2_XX],
-                                 S[x0 + qx - C2_XX], S[xp + qx], S[xm + qx], k.ce, k.cw, k.cn, k.cs, k.ct, k.cb,
-                                 DP ? S[dc + C2_P + q] : xc, a.c1a, a.c2a);
-    S[o1 + q] = fx_add(xc, dn);
+    k.ce = G[t.e];
+    k.cw = G[t.e - 1];
+    k.cn = G[t.n];
+    k.cs = G[t.s];
+    k.ct = G[C2_GT + t.a];
+    k.cb = Gm[C2_GT + t.a];
+    const float xc = G[t.x];
+    const float dn = cheb_update(k.b, k.dg, k.dinv, xc, G[t.x + 1], G[t.x - 1], G[t.xn], G[t.xs], Gp[t.x],
+                                 Gm[t.x], k.ce, k.cw, k.cn, k.cs, k.ct, k.cb, DP ? G[C2_GP + t.a] : xc, a.c1a,
+                                 a.c2a);
+    o1[q] = fx_add(xc, dn);
     return dn;
 }
 
-__device__ __forceinline__ int c2_wrap(int i, int r) { return i >= r ? i - r : i; }
-
 template <bool DP, bool DO>
-__global__ void __launch_bounds__(C2_THREADS, 4) k_cheb_pair(PairArgs a)
+__global__ void __launch_bounds__(C2_THREADS, 4) k_cheb_pair(const __grid_constant__ PairMaps tm, PairArgs a)
 {
-    extern __shared__ __align__(16) float c2_smem[];
-    float *S = c2_smem;
-    // offsets in S: C2_RD slots of first-step inputs, C2_RX planes of x,
-    // C2_R1 planes of x after the first step
-    constexpr int SD = 0, SX = C2_RD * C2_SLOT, S1 = SX + C2_RX * C2_NX;
-    const unsigned sbase = (unsigned)__cvta_generic_to_shared(c2_smem);
+    extern __shared__ __align__(128) float c2_raw[];
+    const unsigned raw = (unsigned)__cvta_generic_to_shared(c2_raw);
+    const unsigned sb = (raw + 127u) & ~127u;            // 128-byte aligned start of the rings
+    float *S = c2_raw + (sb - raw) / 4;
+    float *R1 = S + C2_DEPTH * C2_SLOT;                  // first-step results, C2_R1 planes of 34 x 10
+    const unsigned bar0 = sb + 4u * (C2_DEPTH * C2_SLOT + C2_R1N);
     const LevelView<float> &F = a.F;
     const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + C2_TX * ty;
-    const int i0 = blockIdx.x * C2_TX + 1, j0 = blockIdx.y * C2_TY + 1;
+    const int bx = blockIdx.x * C2_TX, by = blockIdx.y * C2_TY;   // (i0 - 1, j0 - 1)
+    const int i0 = bx + 1, j0 = by + 1;
     const int k0 = blockIdx.z * a.planes + 1, k1 = min(k0 + a.planes - 1, F.n2);
-    const C2Offs o = c2_offsets(F, i0, j0, tid);
+    // the tile's first column in each box, per row parity (box origins: x
+    // rounded down to a multiple of 4 floats)
+    int shA[2], shE[2];
+#pragma unroll
+    for (int p = 0; p < 2; ++p) {
+        shA[p] = (p * F.sy + bx) & 3;
+        shE[p] = p * F.sy + bx - ((p * F.sy + bx - 1) & ~3);
+    }
     // this thread's column (tx + 1, ty + 1) of the 34 x 10 tile and its halo
-    // cell (the ring around the 32 x 8 tile), as tile indices
-    auto idx = [&](int ex, int ey, int &q, int &qe, int &qn, int &qx, bool &in) {
-        const int i = i0 - 1 + ex, j = j0 - 1 + ey;
-        q = ex + C2_EX * ey;
-        qe = ex + C2_WE * ey;
-        qn = ex + C2_EX * ey;
-        qx = (ex + 2) + C2_XX * (ey + 1);
-        in = i >= 1 && i <= F.n0 && j >= 1 && j <= F.n1;
-    };
-    int q0, qe0, qn0, qx0, qh = 0, qeh = 0, qnh = 0, qxh = 0;
-    bool in0, inh = false;
-    idx(tx + 1, ty + 1, q0, qe0, qn0, qx0, in0);
+    // cell (the ring around the 32 x 8 tile)
+    const C2Idx t0 = c2_idx(tx + 1, ty + 1, shA, shE);
+    const int q0 = (tx + 1) + C2_EX * (ty + 1);
+    const bool in0 = i0 + tx <= F.n0 && j0 + ty <= F.n1;
     int hx = -1, hy = 0;
     if (tid < C2_EX) { hx = tid; hy = 0; }
     else if (tid < 2 * C2_EX) { hx = tid - C2_EX; hy = C2_EY - 1; }
     else if (tid < 2 * C2_EX + C2_TY) { hx = 0; hy = tid - 2 * C2_EX + 1; }
     else if (tid < C2_NH) { hx = C2_EX - 1; hy = tid - 2 * C2_EX - C2_TY + 1; }
     const bool halo = hx >= 0;
-    if (halo) idx(hx, hy, qh, qeh, qnh, qxh, inh);
+    const C2Idx th = c2_idx(halo ? hx : 0, hy, shA, shE);
+    const int qh = (halo ? hx : 0) + C2_EX * hy;
+    const bool inh = halo && bx + hx >= 1 && bx + hx <= F.n0 && by + hy >= 1 && by + hy <= F.n1;
 
-    // group g: inputs of plane g and x of plane g + 1 (the first group also
-    // x of plane k0 - 2); groups k0 - 2 .. k0 - 2 + C2_AHEAD before the loop.
-    // Ring index of plane P: (P + 2) mod depth (P >= k0 - 2 >= -1).
-    auto issue = [&](int rslot, int P, int rxs, int X) {
-        c2_issue<DP>(a, o, sbase + 4u * (SD + rslot * C2_SLOT), P, sbase + 4u * (SX + rxs * C2_NX), X, tid);
-    };
-    issue(k0 % C2_RD, k0 - 2, k0 % C2_RX, k0 - 2);
-    for (int g = k0 - 2; g <= k0 - 2 + C2_AHEAD; ++g) {
-        issue((g + 2) % C2_RD, g == k0 - 2 ? -1 : g, (g + 3) % C2_RX, g + 1);
-        __pipeline_commit();
+    const int g0 = k0 - 2, glast = k1 + 2;               // groups this block needs
+    if (tid == 0) {
+#pragma unroll
+        for (int s = 0; s < C2_DEPTH; ++s) mbar_init(bar0 + 8u * s, 1u);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
-    // ring indices of plane kk (and the planes around it), advanced by one per plane
-    int rd = (k0 + 1) % C2_RD, rx = (k0 + 1) % C2_RX, r1 = (k0 + 1) % C2_R1;
-    float d1 = 0.f;     // first-step update of this thread's column, plane below
+    __syncthreads();
+    // group P: slot (P + 2) mod 4 (P >= -1), parity of its use of the slot
+    // (thread 0 only; box origins recomputed here rather than held in
+    // registers by every thread)
+    auto issue = [&](int P) {
+        const int s = (P + 2) & (C2_DEPTH - 1);
+        const unsigned dst = sb + 4u * (unsigned)(s * C2_SLOT), bar = bar0 + 8u * s;
+        const int bxi = blockIdx.x * C2_TX, yA = blockIdx.y * (C2_TY / 2), yN = yA - 1;
+        mbar_expect_tx(bar, DP ? C2_TX_BYTES_DP : C2_TX_BYTES_NODP);
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+            const int xA = (p * F.sy + bxi) & ~3, xE = (p * F.sy + bxi - 1) & ~3;
+            tma_load3(dst + 4u * (C2_GB + p * C2_BA), &tm.m[0], xA, yA, P, bar);
+            tma_load3(dst + 4u * (C2_GD + p * C2_BA), &tm.m[1], xA, yA, P, bar);
+            tma_load3(dst + 4u * (C2_GT + p * C2_BA), &tm.m[2], xA, yA, P, bar);
+            if (DP) tma_load3(dst + 4u * (C2_GP + p * C2_BA), &tm.m[3], xA, yA, P, bar);
+            tma_load3(dst + 4u * (C2_GE + p * C2_BE), &tm.m[4], xE, yA, P, bar);
+            tma_load3(dst + 4u * (C2_GN + p * C2_BN), &tm.m[5], xA, yN, P, bar);
+            tma_load3(dst + 4u * (C2_GX + p * C2_BX), &tm.m[6], xE, yN, P, bar);
+        }
+    };
+    if (tid == 0)
+        for (int P = g0; P <= g0 + 2 && P <= glast; ++P) issue(P);
+    int wnext = g0;             // next group to wait for
+    bool gave_up = false;
+    float d1 = 0.f;             // first-step update of this thread's column, plane below
     C2Cell kc = {}, kp = {};
-    const bool out_ok = tx + i0 <= F.n0 && ty + j0 <= F.n1;
+    const bool out_ok = in0;
     int c = (i0 + tx) + F.sy * (j0 + ty) + F.sz * (k0 - 2);   // output cell at plane kk - 1
     for (int kk = k0 - 1; kk <= k1 + 1; ++kk, c += F.sz) {
-        const int g = kk + C2_AHEAD;
-        if (g <= k1 + 1) issue(c2_wrap(rd + C2_AHEAD, C2_RD), g, c2_wrap(rx + C2_AHEAD + 1, C2_RX), g + 1);
-        __pipeline_commit();
-        __pipeline_wait_prior(C2_AHEAD);    // groups up to kk have landed
-        __syncthreads();
-        const int dc = SD + rd * C2_SLOT, dm = SD + (rd == 0 ? C2_RD - 1 : rd - 1) * C2_SLOT;
-        const int x0 = SX + rx * C2_NX, xm = SX + (rx == 0 ? C2_RX - 1 : rx - 1) * C2_NX;
-        const int xp = SX + c2_wrap(rx + 1, C2_RX) * C2_NX;
-        const int o1 = S1 + r1 * C2_NE;
+        if (tid == 0 && kk + 2 <= glast) issue(kk + 2);
+        for (; wnext <= kk + 1; ++wnext)
+            if (!mbar_wait(bar0 + 8u * ((wnext + 2) & (C2_DEPTH - 1)), (unsigned)((wnext - g0) >> 2) & 1u))
+                gave_up = true;
+        const float *G = S + ((kk + 2) & (C2_DEPTH - 1)) * C2_SLOT;
+        const float *Gm = S + ((kk + 1) & (C2_DEPTH - 1)) * C2_SLOT;
+        const float *Gp = S + ((kk + 3) & (C2_DEPTH - 1)) * C2_SLOT;
+        float *o1 = R1 + ((kk + 1) & (C2_R1 - 1)) * C2_NE;
         const bool plane_in = kk >= 1 && kk <= F.n2;
-        const float dn1 = c2_first<DP>(a, S, dc, dm, xm, x0, xp, o1, q0, qe0, qn0, qx0, in0 && plane_in, kc);
+        const float dn1 = c2_first<DP>(a, G, Gm, Gp, t0, o1, q0, in0 && plane_in, kc);
         if (halo) {
             C2Cell kh;
-            c2_first<DP>(a, S, dc, dm, xm, x0, xp, o1, qh, qeh, qnh, qxh, inh && plane_in, kh);
+            c2_first<DP>(a, G, Gm, Gp, th, o1, qh, inh && plane_in, kh);
         }
         __syncthreads();
         if (kk - 1 >= k0 && out_ok) {
             // second step at plane kk - 1 from the first-step planes kk - 2 .. kk
-            const int r1m = r1 == 0 ? C2_R1 - 1 : r1 - 1;
-            const int y0 = S1 + r1m * C2_NE, ym = S1 + (r1m == 0 ? C2_R1 - 1 : r1m - 1) * C2_NE, yp = o1;
+            const float *y0 = R1 + (kk & (C2_R1 - 1)) * C2_NE;
+            const float *ym = R1 + ((kk + 3) & (C2_R1 - 1)) * C2_NE;
+            const float *yp = o1;
             const int q = q0;
-            const float xc = S[y0 + q];
-            const float dn = cheb_update(kp.b, kp.dg, kp.dinv, xc, S[y0 + q + 1], S[y0 + q - 1], S[y0 + q + C2_EX],
-                                         S[y0 + q - C2_EX], S[yp + q], S[ym + q], kp.ce, kp.cw, kp.cn, kp.cs, kp.ct,
-                                         kp.cb, d1, a.c1b, a.c2b);
+            const float xc = y0[q];
+            const float dn = cheb_update(kp.b, kp.dg, kp.dinv, xc, y0[q + 1], y0[q - 1], y0[q + C2_EX],
+                                         y0[q - C2_EX], yp[q], ym[q], kp.ce, kp.cw, kp.cn, kp.cs, kp.ct, kp.cb, d1,
+                                         a.c1b, a.c2b);
             a.xout[c] = fx_add(xc, dn);
             if (DO) a.dout[c] = dn;
         }
         d1 = dn1;
         kp = kc;
-        rd = c2_wrap(rd + 1, C2_RD);
-        rx = c2_wrap(rx + 1, C2_RX);
-        r1 = c2_wrap(r1 + 1, C2_R1);
     }
-    __pipeline_wait_prior(0);
+    if (gave_up) {
+        atomicOr(a.flags, (unsigned)FLAG_WAIT_TIMEOUT);
+        // no copy may still be writing into this block's shared memory when
+        // it exits: wait once more (bounded) for the last groups issued
+        if (tid == 0)
+            for (int P = glast - (C2_DEPTH - 1) > g0 ? glast - (C2_DEPTH - 1) : g0; P <= glast; ++P)
+                mbar_wait(bar0 + 8u * ((P + 2) & (C2_DEPTH - 1)), (unsigned)((P - g0) >> 2) & 1u);
+    }
 }
 
 // Smoother pairing: 1 (the default) on the levels where the pair kernel
@@ -745,6 +799,15 @@ __global__ void __launch_bounds__(C2_THREADS, 4) k_cheb_pair(PairArgs a)
 // least 2^18 cells, 0 off; k-planes per block of the pair kernel (fewer
 // when that fills the grid).
 static int g_pairs = 1, g_pair_planes = C2_PLANES;
+// launches of the TMA pair kernel, and pairs that ran as one-step launches
+// because a tensor map did not encode (process-wide)
+static std::atomic<long long> g_pair_tma{0}, g_pair_fallback{0};
+
+void smoother_pair_counts(long long *tma, long long *fallback)
+{
+    *tma = g_pair_tma.load();
+    *fallback = g_pair_fallback.load();
+}
 
 void set_smoother_pairs(int on, int planes)
 {
@@ -754,12 +817,53 @@ void set_smoother_pairs(int on, int planes)
 
 int smoother_pairs_state() { return g_pairs + 3 * g_pair_planes; }
 
+namespace {
+// cuTensorMapEncodeTiled from the driver, found through the runtime (no
+// link-time dependence on the driver library); nullptr if unavailable.
+PFN_cuTensorMapEncodeTiled_v12000 encode_tiled()
+{
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+// The level's shape allows the row-pair view (see k_cheb_pair).
+bool pair_shape_ok(int n0, int n1, int sy)
+{
+    return (n0 & 1) == 0 && ((long long)sy * (n1 + 2)) % 4 == 0;
+}
+
+// Tensor map of one FP32 array of level F in the row-pair view, box w
+// floats x h row pairs x 1 plane.
+bool encode_pair_map(CUtensorMap *m, const float *base, const LevelView<float> &F, int w, int h)
+{
+    const PFN_cuTensorMapEncodeTiled_v12000 fn = encode_tiled();
+    if (!fn || !base || ((uintptr_t)base & 15u) || !pair_shape_ok(F.n0, F.n1, F.sy)) return false;
+    const cuuint64_t dim[3] = {(cuuint64_t)(2 * F.sy), (cuuint64_t)((F.n1 + 2) / 2), (cuuint64_t)(F.n2 + 2)};
+    const cuuint64_t stride[2] = {(cuuint64_t)(2 * F.sy) * 4u, (cuuint64_t)F.sz * 4u};
+    const cuuint32_t box[3] = {(cuuint32_t)w, (cuuint32_t)h, 1u};
+    const cuuint32_t estride[3] = {1u, 1u, 1u};
+    return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(base), dim, stride, box, estride,
+              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+}  // namespace
+
 // k-planes per block of the pair kernel on level F, 0: one-step kernels.
 template <typename T>
 int pair_planes(const MgLevel<T> &F)
 {
     const long long cells = (long long)F.n0 * F.n1 * F.n2;
-    if (sizeof(T) != 4 || g_pairs == 0 || cells < (1LL << 18) || (F.n0 & 1)) return 0;
+    if (sizeof(T) != 4 || g_pairs == 0 || cells < (1LL << 18) || !pair_shape_ok(F.n0, F.n1, F.sy) ||
+        !encode_tiled())
+        return 0;
     if (g_pairs == 2) return g_pair_planes;
     if (cells < (1LL << 22)) return 0;
     const long long tiles = (long long)((F.n0 + C2_TX - 1) / C2_TX) * ((F.n1 + C2_TY - 1) / C2_TY);
@@ -791,24 +895,42 @@ cudaError_t pair_smem_attr()
 
 // Two Chebyshev steps (c1a, c2a) then (c1b, c2b) of FP32 level F from xin
 // into xout; dprev nullptr means the first step's previous update is xin
-// itself.  Needs an even n0 (rows 8-byte aligned); otherwise launches
-// nothing and returns cudaErrorInvalidValue.
+// itself.  Callers check use_pairs(F) first.  Should a tensor map still not
+// encode, the two steps run as one-step launches (xin is then overwritten,
+// as the callers allow: it is their scratch buffer after the pair).
 cudaError_t cheb_pair(const MgLevel<float> &F, const float *xin, const float *dprev, float *xout, float *dout,
                       double c1a, double c2a, double c1b, double c2b, cudaStream_t st)
 {
-    if (F.n0 & 1) return cudaErrorInvalidValue;
     PairArgs a;
     a.F = F.view();
-    a.b = F.b; a.x = xin; a.dprev = dprev; a.xout = xout; a.dout = dout;
+    a.xout = xout; a.dout = dout; a.flags = F.flags;
     a.c1a = (float)c1a; a.c2a = (float)c2a; a.c1b = (float)c1b; a.c2b = (float)c2b;
     a.planes = pair_planes(F) > 0 ? pair_planes(F) : g_pair_planes;
-    pair_smem_attr();
+    PairMaps tm;
+    const LevelView<float> v = a.F;
+    bool ok = F.flags != nullptr && encode_pair_map(&tm.m[0], F.b, v, C2_WA, C2_HA) &&
+              encode_pair_map(&tm.m[1], F.diag, v, C2_WA, C2_HA) && encode_pair_map(&tm.m[2], F.cT, v, C2_WA, C2_HA) &&
+              (!dprev || encode_pair_map(&tm.m[3], dprev, v, C2_WA, C2_HA)) &&
+              encode_pair_map(&tm.m[4], F.cE, v, C2_WE, C2_HA) && encode_pair_map(&tm.m[5], F.cN, v, C2_WA, C2_HN) &&
+              encode_pair_map(&tm.m[6], xin, v, C2_WE, C2_HX);
+    if (!dprev) tm.m[3] = tm.m[6];   // not read
+    if (ok) ok = pair_smem_attr() == cudaSuccess;
+    if (!ok) {
+        g_pair_fallback.fetch_add(1);
+        Launch3 lf = launch_interior(F.n0, F.n1, F.n2);
+        float *x1 = xout, *x2 = const_cast<float *>(xin);
+        k_cheb_step<float><<<lf.grid, lf.block, 0, st>>>(v, F.b, xin, dprev ? dprev : xin, x1, F.d, (float)c1a,
+                                                         (float)c2a);
+        k_cheb_step<float><<<lf.grid, lf.block, 0, st>>>(v, F.b, x1, F.d, x2, dout, (float)c1b, (float)c2b);
+        return cudaMemcpyAsync(xout, x2, sizeof(float) * (size_t)F.tot, cudaMemcpyDeviceToDevice, st);
+    }
+    g_pair_tma.fetch_add(1);
     const dim3 blk(C2_TX, C2_TY, 1);
     const dim3 grd((F.n0 + C2_TX - 1) / C2_TX, (F.n1 + C2_TY - 1) / C2_TY, (F.n2 + a.planes - 1) / a.planes);
-    if (dprev && dout) k_cheb_pair<true, true><<<grd, blk, C2_SMEM, st>>>(a);
-    else if (dprev) k_cheb_pair<true, false><<<grd, blk, C2_SMEM, st>>>(a);
-    else if (dout) k_cheb_pair<false, true><<<grd, blk, C2_SMEM, st>>>(a);
-    else k_cheb_pair<false, false><<<grd, blk, C2_SMEM, st>>>(a);
+    if (dprev && dout) k_cheb_pair<true, true><<<grd, blk, C2_SMEM, st>>>(tm, a);
+    else if (dprev) k_cheb_pair<true, false><<<grd, blk, C2_SMEM, st>>>(tm, a);
+    else if (dout) k_cheb_pair<false, true><<<grd, blk, C2_SMEM, st>>>(tm, a);
+    else k_cheb_pair<false, false><<<grd, blk, C2_SMEM, st>>>(tm, a);
     return cudaSuccess;
 }
 

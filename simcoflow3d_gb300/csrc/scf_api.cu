@@ -161,6 +161,7 @@ template <typename T>
 int alloc_level(scf_ctx *ctx, MgLevel<T> &L, int n0, int n1, int n2, bool own_op)
 {
     L.n0 = n0; L.n1 = n1; L.n2 = n2;
+    L.flags = ctx->flags;
     L.sy = n0 + 2;
     L.sz = L.sy * (n1 + 2);
     L.tot = L.sz * (n2 + 2);
@@ -666,6 +667,15 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
     }
     if (singular) shift_solution(A, ctx->active, ctx->x, ctx->R.scal, ctx->st, &ctx->launches);
     kt_harvest(ctx);
+    if (mixed) {
+        // the two-step smoother's bounded waits for its own copies
+        CK(cudaMemcpyAsync(ctx->h_u32, ctx->flags, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->st));
+        CK(cudaStreamSynchronize(ctx->st));
+        if (*ctx->h_u32 & FLAG_WAIT_TIMEOUT) {
+            set_err(ctx, "a smoother kernel gave up waiting for its shared-memory copies");
+            return SCF_ERR_CUDA;
+        }
+    }
     stats->iterations = its;
     stats->rounds = restarts + 1;
     stats->rel_residual = rel;
@@ -1502,6 +1512,15 @@ int scf_debug_smoother_pairs(int on, int planes)
 {
     if (planes < 0 || on < 0 || on > 2) return SCF_ERR_BAD_ARG;
     set_smoother_pairs(on, planes);
+    return SCF_OK;
+}
+
+int scf_debug_smoother_pair_counts(int64_t *tma_launches, int64_t *fallbacks)
+{
+    long long t = 0, f = 0;
+    smoother_pair_counts(&t, &f);
+    if (tma_launches) *tma_launches = t;
+    if (fallbacks) *fallbacks = f;
     return SCF_OK;
 }
 

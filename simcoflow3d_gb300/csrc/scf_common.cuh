@@ -31,6 +31,7 @@ enum ScfFlag : unsigned {
     FLAG_NONFINITE = 8u,          // NaN/Inf in the assembled system
     FLAG_BAD_DIAG = 16u,          // active row with diagonal <= 0
     FLAG_NEITHER_ACTIVE = 32u,    // active cell that is neither wet nor dry
+    FLAG_WAIT_TIMEOUT = 64u,      // a kernel's bounded wait for its own copies gave up
 };
 
 // Scalars kept on the device during CG (no host round trip for alpha/beta).

@@ -51,6 +51,7 @@ struct MgLevel {
     T *diag, *dinv, *cE, *cN, *cT, *extra;
     unsigned char *active;
     T *x, *xb, *d, *b;              // x/xb ping-pong, Chebyshev update, rhs
+    unsigned *flags;                // the context's device error flags
     LevelView<T> view() const
     {
         LevelView<T> v;
@@ -155,6 +156,7 @@ cudaError_t probe_smooth2(MgLevel<float> &F, const ChebCoef &cc, cudaStream_t st
 // (0: the default).
 void set_smoother_pairs(int on, int planes);
 int smoother_pairs_state();          // changes whenever the setting does
+void smoother_pair_counts(long long *tma, long long *fallback);
 cudaError_t pair_smem_attr();        // the two-step kernel's shared-memory opt-in
 
 // Fine operator of the mixed solver's CG in double-float form: hi parts are

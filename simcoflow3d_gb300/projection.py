@@ -85,6 +85,7 @@ def load_library(path: Optional[str] = None):
     L.scf_ctx_device_fields.argtypes = [C.c_void_p] + [P(C.c_void_p)] * 7
     L.scf_apply_operator_noalloc.argtypes = [C.c_int32, C.c_int32, C.c_int32] + [C.c_void_p] * 8
     L.scf_debug_smoother_pairs.argtypes = [C.c_int, C.c_int]
+    L.scf_debug_smoother_pair_counts.argtypes = [C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     P_M = P(capi.ScfMomIn)
     L.scf_mom_create.argtypes = [P(C.c_void_p), C.c_int32, C.c_int32, C.c_int32, C.c_int32]
     L.scf_mom_destroy.argtypes = [C.c_void_p]
@@ -125,6 +126,15 @@ def smoother_pairs(on: int = 1, planes: int = 0):
     rc = L.scf_debug_smoother_pairs(int(on), int(planes))
     if rc != capi.SCF_OK:
         raise ScfError(rc, capi_status(rc))
+
+
+def smoother_pair_counts():
+    """(launches of the TMA-staged pair kernel, pairs that fell back to
+    one-step launches), process-wide."""
+    L = load_library()
+    t, f = C.c_int64(0), C.c_int64(0)
+    L.scf_debug_smoother_pair_counts(C.byref(t), C.byref(f))
+    return t.value, f.value
 
 
 def default_opts(**kw) -> capi.ScfOpts:

@@ -47,21 +47,26 @@ def test_vcycle_matches_oracle(gpu_lib, name, kw, precision, tol, degree, lines)
         assert not z[~act].any()
 
 
-def _big_odd():
+def _big_odd(n0=70, n1=45, n2=85):
     # 70 x 45 x 85 = 267,750 cells: a large level whose tiles are ragged in
     # every direction (70 = 2*32 + 6, 45 = 5*8 + 5, 85 = 2*32 + 21)
-    return W.build_workload("odd-large", 70, 45, 85, solid=W.SPHERE_C1, liquid=("bubble", 0.5, 0.5, 0.6, 0.2),
+    return W.build_workload("odd-large", n0, n1, n2, solid=W.SPHERE_C1, liquid=("bubble", 0.5, 0.5, 0.6, 0.2),
                             rho_l=1000.0, rho_g=1.2)
 
 
+# Row lengths n0 + 2 of both residues mod 4 that the two-step kernel's
+# row-pair view takes: 72 (odd rows start on a 16-byte boundary, n1 may be
+# odd) and 70 (odd rows start 8 bytes past one, n1 even); 68 x 46 x 85 =
+# 266,016 cells, tiles ragged in every direction too.
+@pytest.mark.parametrize("shape", [(70, 45, 85), (68, 46, 85)])
 @pytest.mark.parametrize("degree", [2, 3, 4, 5])
-def test_paired_smoother_equals_one_step_sweeps(gpu_lib, degree):
+def test_paired_smoother_equals_one_step_sweeps(gpu_lib, degree, shape):
     """The two-step kernel (one pass per pair of Chebyshev steps), forced
     onto every level of at least 2^18 cells, gives the V-cycle and the
     projection of one-step sweeps bit for bit, whatever the k-planes per
     block."""
-    from simcoflow3d_gb300.projection import Projection, smoother_pairs
-    w = _big_odd()
+    from simcoflow3d_gb300.projection import Projection, smoother_pair_counts, smoother_pairs
+    w = _big_odd(*shape)
     act = np.zeros(w.shape_g, dtype=bool)
     act[1:-1, 1:-1, 1:-1] = w.arrays["cell_type"] != 2
     r = np.where(act, np.random.default_rng(5).normal(size=w.shape_g), 0.0)
@@ -77,6 +82,9 @@ def test_paired_smoother_equals_one_step_sweeps(gpu_lib, degree):
             p.close()
     finally:
         smoother_pairs(1, 0)
+    # the fused runs went through the TMA-staged kernel, with no fallback
+    tma, fallback = smoother_pair_counts()
+    assert tma > 0 and fallback == 0, (tma, fallback)
     z0, p0, n0 = out["one"]
     for key in ("pairs", "pairs7", "pairs1"):
         z, pp, n = out[key]
