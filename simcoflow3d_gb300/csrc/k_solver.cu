@@ -509,11 +509,11 @@ __global__ void __launch_bounds__(256) k_cheb_step(LevelView<T> L, const T *__re
 // Two Chebyshev steps in one pass over a large FP32 level (2.5-D temporal
 // blocking), with the inputs staged by the Tensor Memory Accelerator.
 //
-// A block owns a tile of 32 x 8 (i, j) columns and marches along k over
-// `planes` planes.  Group P holds plane P's inputs on the tile and its halo
-// (b, diag, cT and the previous update on 34 x 10 cells, cE one column
-// wider to the west, cN one row wider to the south) and x of plane P with a
-// two-cell halo.  For plane kk the block
+// A block of 256 threads owns a tile of 32 x 8 (i, j) columns and marches
+// along k over `planes` planes.  Group P holds plane P's inputs on the tile
+// and its halo (b, diag, cT and the previous update on 34 x 10 cells, cE one
+// column wider to the west, cN one row wider to the south) and x of plane P
+// with a two-cell halo.  For plane kk the block
 //   1. has one thread issue the TMA copies of group kk + 2 into a four-slot
 //      ring in shared memory; they complete on that slot's mbarrier;
 //   2. waits for group kk + 1 (groups kk - 1 and kk landed earlier) and
@@ -522,6 +522,10 @@ __global__ void __launch_bounds__(256) k_cheb_step(LevelView<T> L, const T *__re
 //      ring in shared memory;
 //   3. after one block barrier, applies the second step on the 32 x 8 cells
 //      of plane kk - 1.
+// The first step's 84 halo cells go to the first three warps, so the other
+// five carry no halo code path.  (Tiles of 32 x 16 with 512 threads, a 20%
+// halo instead of 33%, measured slower: 0.158 against 0.155 ms per pair at
+// 256^3.)
 // The four-deep rings make that single barrier per plane enough: the slot a
 // copy or a first step overwrites was last read before the previous
 // plane's barrier.  Each array is read from DRAM about once per pass (halo
@@ -544,15 +548,19 @@ __global__ void __launch_bounds__(256) k_cheb_step(LevelView<T> L, const T *__re
 // and sy (n1 + 2) a multiple of 4 (the plane stride in 16-byte units);
 // other levels smooth with one-step launches.
 constexpr int C2_TX = 32, C2_TY = 8, C2_THREADS = C2_TX * C2_TY;
+constexpr int C2_BLOCKS_PER_SM = 4;
 constexpr int C2_EX = C2_TX + 2, C2_EY = C2_TY + 2, C2_NE = C2_EX * C2_EY;  // first-step cells, from (i0-1, j0-1)
 constexpr int C2_NH = C2_NE - C2_THREADS;                                // halo cells of step 1
 // box widths (floats) and heights (row pairs): b, diag, cT, dprev and cN
 // from column i0 - 1 (36 wide), cE and x from column i0 - 2 (40 wide); b,
-// diag, cT, dprev and cE from row j0 - 1 (5 pairs), cN from row j0 - 3
-// (6 pairs), x from row j0 - 3 (7 pairs)
-constexpr int C2_WA = 36, C2_WE = 40, C2_HA = 5, C2_HN = 6, C2_HX = 7;
+// diag, cT, dprev and cE from row j0 - 1 (C2_TY/2 + 1 pairs), cN from row
+// j0 - 3 (one pair more), x from row j0 - 3 (two pairs more)
+constexpr int C2_WA = 36, C2_WE = 40, C2_HA = C2_TY / 2 + 1, C2_HN = C2_HA + 1, C2_HX = C2_HA + 2;
 // one box per parity, each starting on a 128-byte boundary (floats)
-constexpr int C2_BA = 192, C2_BE = 224, C2_BN = 224, C2_BX = 288;
+constexpr int c2_round(int v) { return (v + 31) / 32 * 32; }
+constexpr int C2_BA = c2_round(C2_WA * C2_HA), C2_BE = c2_round(C2_WE * C2_HA), C2_BN = c2_round(C2_WA * C2_HN),
+              C2_BX = c2_round(C2_WE * C2_HX);
+static_assert(C2_TY % 2 == 0, "tiles of whole row pairs");
 static_assert(C2_WA * C2_HA <= C2_BA && C2_WE * C2_HA <= C2_BE && C2_WA * C2_HN <= C2_BN && C2_WE * C2_HX <= C2_BX,
               "boxes fit their slots");
 static_assert(C2_BA % 32 == 0 && C2_BE % 32 == 0 && C2_BN % 32 == 0 && C2_BX % 32 == 0, "128-byte boxes");
@@ -680,7 +688,8 @@ __device__ __forceinline__ float c2_first(const PairArgs &a, const float *G, con
 }
 
 template <bool DP, bool DO>
-__global__ void __launch_bounds__(C2_THREADS, 4) k_cheb_pair(const __grid_constant__ PairMaps tm, PairArgs a)
+__global__ void __launch_bounds__(C2_THREADS, C2_BLOCKS_PER_SM) k_cheb_pair(const __grid_constant__ PairMaps tm,
+                                                                          PairArgs a)
 {
     extern __shared__ __align__(128) float c2_raw[];
     const unsigned raw = (unsigned)__cvta_generic_to_shared(c2_raw);
@@ -795,7 +804,7 @@ __global__ void __launch_bounds__(C2_THREADS, 4) k_cheb_pair(const __grid_consta
 
 // Smoother pairing: 1 (the default) on the levels where the pair kernel
 // measured faster than two one-step launches -- at least 2^22 cells, with
-// at least two waves of four blocks per SM -- 2 on every FP32 level of at
+// at least two waves of blocks -- 2 on every FP32 level of at
 // least 2^18 cells, 0 off; k-planes per block of the pair kernel (fewer
 // when that fills the grid).
 static int g_pairs = 1, g_pair_planes = C2_PLANES;
@@ -868,7 +877,7 @@ int pair_planes(const MgLevel<T> &F)
     if (cells < (1LL << 22)) return 0;
     const long long tiles = (long long)((F.n0 + C2_TX - 1) / C2_TX) * ((F.n1 + C2_TY - 1) / C2_TY);
     for (int planes = g_pair_planes; planes >= 8; planes /= 2)
-        if (tiles * ((F.n2 + planes - 1) / planes) >= 2LL * 4 * 152) return planes;
+        if (tiles * ((F.n2 + planes - 1) / planes) >= 2LL * C2_BLOCKS_PER_SM * 152) return planes;
     return 0;
 }
 
@@ -1311,7 +1320,7 @@ double pair_bytes(const MgLevel<float> &F, bool reads_d, bool writes_d, bool pro
 
 template <typename T>
 T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, const int *map, int ncoarse,
-             bool singular, bool first_done, cudaStream_t st, int *launches, KTimer *kt)
+             bool singular, bool first_done, cudaStream_t st, int *launches, KTimer *kt, cudaEvent_t coarse_ready)
 {
     T *cur[32];
     const int last = nlev - 1;
@@ -1391,6 +1400,7 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
     }
     {
         MgLevel<T> &Cst = L[last];
+        if (coarse_ready) cudaStreamWaitEvent(st, coarse_ready, 0);
         k_coarse_solve<T><<<1, 128, 0, st>>>(Cst.b, Cst.x, Cst.active, ainv, map, ncoarse, singular ? 1 : 0);
         *launches += 1;
         cur[last] = Cst.x;
@@ -1531,9 +1541,9 @@ template void mg_coarsen<double>(const MgLevel<double> &, MgLevel<double> &, cud
 template void mg_coarse_inverse<float>(const MgLevel<float> &, double *, int *, int, bool, cudaStream_t, int *);
 template void mg_coarse_inverse<double>(const MgLevel<double> &, double *, int *, int, bool, cudaStream_t, int *);
 template float *mg_vcycle<float>(MgLevel<float> *, int, const ChebCoef &, const double *, const int *, int, bool,
-                                 bool, cudaStream_t, int *, KTimer *);
+                                 bool, cudaStream_t, int *, KTimer *, cudaEvent_t);
 template double *mg_vcycle<double>(MgLevel<double> *, int, const ChebCoef &, const double *, const int *, int, bool,
-                                   bool, cudaStream_t, int *, KTimer *);
+                                   bool, cudaStream_t, int *, KTimer *, cudaEvent_t);
 template void cg_update<float>(const LevelView<double> &, double *, double *, const double *, const double *, float *,
                                const LevelView<float> &, float *, double, Reducer &, cudaStream_t, int *, KTimer *);
 template void cg_update<double>(const LevelView<double> &, double *, double *, const double *, const double *,

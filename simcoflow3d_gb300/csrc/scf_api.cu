@@ -36,6 +36,11 @@ struct scf_ctx {
     cudaStream_t st = nullptr;
     cudaStream_t cst = nullptr;   // copies of the correction's inputs, overlapping the solve
     cudaEvent_t corr_ready = nullptr;
+    // the coarsest level's dense inverse is formed on its own stream (one SM)
+    // while the first V-cycle's downward sweep runs on the others
+    cudaStream_t ist = nullptr;
+    cudaEvent_t inv_start = nullptr, inv_ready = nullptr;
+    bool inv_pending = false;     // the next V-cycle must wait for inv_ready
     bool corr_pending = false;    // st must wait for corr_ready before the correction
     char err[512] = {0};
     DevBuf mem, mgmem;
@@ -217,6 +222,8 @@ int ensure_mg(scf_ctx *ctx)
 {
     const int prec = ctx->opts.precision;
     if (ctx->mg_precision == prec) return SCF_OK;
+    if (ctx->ist) cudaStreamSynchronize(ctx->ist);   // no inverse in flight into the buffers freed here
+    ctx->inv_pending = false;
     ctx->mgmem.release();
     ctx->mg_gen++;
     if (ctx->iter_exec) { cudaGraphExecDestroy(ctx->iter_exec); ctx->iter_exec = nullptr; }
@@ -340,11 +347,26 @@ int assemble(scf_ctx *ctx)
 }
 
 template <typename T>
-void build_hierarchy(scf_ctx *ctx, MgLevel<T> *L)
+int build_hierarchy(scf_ctx *ctx, MgLevel<T> *L)
 {
     for (int l = 0; l + 1 < ctx->nlev; ++l) mg_coarsen<T>(L[l], L[l + 1], ctx->st, &ctx->launches);
-    mg_coarse_inverse<T>(L[ctx->nlev - 1], ctx->ainv, ctx->map, ctx->ncoarse, is_singular(ctx), ctx->st,
+    CK(cudaEventRecord(ctx->inv_start, ctx->st));
+    CK(cudaStreamWaitEvent(ctx->ist, ctx->inv_start, 0));
+    mg_coarse_inverse<T>(L[ctx->nlev - 1], ctx->ainv, ctx->map, ctx->ncoarse, is_singular(ctx), ctx->ist,
                          &ctx->launches);
+    CK(cudaEventRecord(ctx->inv_ready, ctx->ist));
+    ctx->inv_pending = true;
+    return SCF_OK;
+}
+
+// Stream order after the coarsest inverse, outside any capture.
+int join_inverse(scf_ctx *ctx)
+{
+    if (ctx->inv_pending) {
+        CK(cudaStreamWaitEvent(ctx->st, ctx->inv_ready, 0));
+        ctx->inv_pending = false;
+    }
+    return SCF_OK;
 }
 
 ChebCoef cheb_coef(int degree, int lines)
@@ -448,8 +470,12 @@ bool fuse_first(const scf_ctx *ctx) { return ctx->nlev > 1 && !use_lines(ctx); }
 template <typename T>
 T *precondition(scf_ctx *ctx, MgLevel<T> *L, const ChebCoef &cc, bool first_done)
 {
+    // the first V-cycle after a new hierarchy waits for the coarsest inverse
+    // just before its coarsest solve
+    cudaEvent_t ready = ctx->inv_pending ? ctx->inv_ready : nullptr;
+    ctx->inv_pending = false;
     return mg_vcycle<T>(L, ctx->nlev, cc, ctx->ainv, ctx->map, ctx->ncoarse, is_singular(ctx), first_done,
-                        ctx->st, &ctx->launches, ctx->kt.on ? &ctx->kt : nullptr);
+                        ctx->st, &ctx->launches, ctx->kt.on ? &ctx->kt : nullptr, ready);
 }
 
 // Fine operator of the mixed CG in double-float form.
@@ -525,6 +551,7 @@ void run_iteration(scf_ctx *ctx, MgLevel<T> *L, const ChebCoef &cc, bool singula
                                    (ctx->kt.on ? 3ull : 0ull) + (sizeof(T) == 4 ? 11ull : 0ull) +
                                    (unsigned long long)ctx->nlev * 17ull + (cc.lines ? 5ull : 0ull) +
                                    (unsigned long long)smoother_pairs_state() * 7919ull;
+    if (ctx->inv_pending) join_inverse(ctx);   // (a captured V-cycle cannot wait on it)
     if (ctx->graphs_ok && (!ctx->iter_exec || ctx->iter_key != key)) {
         if (ctx->iter_exec) { cudaGraphExecDestroy(ctx->iter_exec); ctx->iter_exec = nullptr; }
         cudaGraph_t g = nullptr;
@@ -571,7 +598,10 @@ int solve_impl(scf_ctx *ctx, MgLevel<T> *L, scf_stats *stats)
     const ChebCoef cc = cheb_for(ctx);
     auto t0 = std::chrono::steady_clock::now();
     rhs_prologue(A, ctx->active, ctx->b, singular, ctx->R, ctx->st, &ctx->launches);
-    build_hierarchy<T>(ctx, L);
+    {
+        const int rh = build_hierarchy<T>(ctx, L);
+        if (rh) return rh;
+    }
     const double bb = read_scal(ctx, S_BB);
     const double bn = std::sqrt(bb);
     stats->rhs_norm = bn;
@@ -990,6 +1020,10 @@ int scf_ctx_create(scf_ctx **out, int32_t imax, int32_t jmax, int32_t kmax, cons
     if (cudaStreamCreateWithFlags(&ctx->st, cudaStreamNonBlocking) != cudaSuccess) return fail(SCF_ERR_CUDA);
     if (cudaStreamCreateWithFlags(&ctx->cst, cudaStreamNonBlocking) != cudaSuccess) return fail(SCF_ERR_CUDA);
     if (cudaEventCreateWithFlags(&ctx->corr_ready, cudaEventDisableTiming) != cudaSuccess) return fail(SCF_ERR_CUDA);
+    if (cudaStreamCreateWithFlags(&ctx->ist, cudaStreamNonBlocking) != cudaSuccess) return fail(SCF_ERR_CUDA);
+    if (cudaEventCreateWithFlags(&ctx->inv_start, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->inv_ready, cudaEventDisableTiming) != cudaSuccess)
+        return fail(SCF_ERR_CUDA);
     for (int e = 0; e < 8; ++e) cudaEventCreate(&ctx->ev[e]);
     if (cudaMallocHost(&ctx->h_scal, 64 * sizeof(double)) != cudaSuccess) return fail(SCF_ERR_OUT_OF_MEMORY);
     if (cudaMallocHost(&ctx->h_u32, 64 * sizeof(unsigned)) != cudaSuccess) return fail(SCF_ERR_OUT_OF_MEMORY);
@@ -1005,6 +1039,7 @@ int scf_ctx_destroy(scf_ctx *ctx)
     if (!ctx) return SCF_OK;
     cudaSetDevice(ctx->opts.device);
     if (ctx->st) cudaStreamSynchronize(ctx->st);
+    if (ctx->ist) cudaStreamSynchronize(ctx->ist);
     ctx->mgmem.release();
     ctx->adjmem.release();
     ctx->mem.release();
@@ -1017,6 +1052,9 @@ int scf_ctx_destroy(scf_ctx *ctx)
     if (ctx->h_u32) cudaFreeHost(ctx->h_u32);
     if (ctx->cst) { cudaStreamSynchronize(ctx->cst); cudaStreamDestroy(ctx->cst); }
     if (ctx->corr_ready) cudaEventDestroy(ctx->corr_ready);
+    if (ctx->ist) cudaStreamDestroy(ctx->ist);
+    if (ctx->inv_start) cudaEventDestroy(ctx->inv_start);
+    if (ctx->inv_ready) cudaEventDestroy(ctx->inv_ready);
     if (ctx->st) cudaStreamDestroy(ctx->st);
     delete ctx;
     return SCF_OK;

@@ -136,10 +136,12 @@ inline void kt_end(KTimer *kt, int id, cudaStream_t st)
 
 // One V-cycle: level 0 rhs in L[0].b, result in *z (== L[0].x or L[0].xb).
 // first_done: level 0's first Chebyshev step was already written to L[0].x
-// (fused into the CG update).
+// (fused into the CG update).  coarse_ready: an event the coarsest solve
+// waits for (the dense inverse formed on another stream), or nullptr.
 template <typename T>
 T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, const int *map, int ncoarse,
-             bool singular, bool first_done, cudaStream_t st, int *launches, KTimer *kt = nullptr);
+             bool singular, bool first_done, cudaStream_t st, int *launches, KTimer *kt = nullptr,
+             cudaEvent_t coarse_ready = nullptr);
 
 // Single launches of the fine-level kernels, for timing.
 template <typename T>
