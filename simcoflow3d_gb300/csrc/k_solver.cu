@@ -10,13 +10,12 @@
 // diagonal is the sum of the coarse couplings plus half the children's
 // Dirichlet terms.  Dot products are reduced per block and then in one block
 // in a fixed order, so results are bitwise reproducible.
-#include <cuda.h>
-#include <cudaTypedefs.h>
 #include <stdint.h>
 
 #include <atomic>
 
 #include "scf_kernels.h"
+#include "scf_tma.cuh"
 
 #define INTERIOR_IJK(L)                                       \
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1; \
@@ -576,9 +575,6 @@ constexpr int C2_PLANES = 32;
 constexpr unsigned C2_TX_BYTES_NODP = 2u * 4u * (3 * C2_WA * C2_HA + C2_WE * C2_HA + C2_WA * C2_HN + C2_WE * C2_HX);
 constexpr unsigned C2_TX_BYTES_DP = C2_TX_BYTES_NODP + 2u * 4u * C2_WA * C2_HA;
 static_assert(C2_NH <= C2_THREADS, "one halo cell per thread at most");
-// polls of an mbarrier before a wait gives up (each poll may suspend the
-// thread for a while; together well over a second, far beyond any copy)
-constexpr unsigned C2_WAIT_POLLS = 1u << 22;
 
 // tensor maps of the pair kernel's inputs: b, diag, cT, dprev, cE, cN, x
 struct PairMaps {
@@ -592,45 +588,6 @@ struct PairArgs {
     float c1a, c2a, c1b, c2b;
     int planes;
 };
-
-__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity)
-{
-    unsigned ok;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// Bounded wait for the phase of the given parity; false if it gave up.
-__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity)
-{
-    for (unsigned it = 0; it < C2_WAIT_POLLS; ++it)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
-}
-
-// 3-D tiled TMA load of one box into shared memory, completing on `bar`.
-__device__ __forceinline__ void tma_load3(unsigned dst, const CUtensorMap *map, int x, int y, int z, unsigned bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-        "[%5];\n" ::"r"(dst),
-        "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
-        : "memory");
-}
 
 // Offsets in a group slot (floats) of one first-step cell (ex, ey) of the
 // 34 x 10 tile: its b/diag/cT/dprev element (a), cE (e; cE of the west
@@ -729,7 +686,7 @@ __global__ void __launch_bounds__(C2_THREADS, C2_BLOCKS_PER_SM) k_cheb_pair(cons
     if (tid == 0) {
 #pragma unroll
         for (int s = 0; s < C2_DEPTH; ++s) mbar_init(bar0 + 8u * s, 1u);
-        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        mbar_fence_init();
     }
     __syncthreads();
     // group P: slot (P + 2) mod 4 (P >= -1), parity of its use of the slot
@@ -826,10 +783,7 @@ void set_smoother_pairs(int on, int planes)
 
 int smoother_pairs_state() { return g_pairs + 3 * g_pair_planes; }
 
-namespace {
-// cuTensorMapEncodeTiled from the driver, found through the runtime (no
-// link-time dependence on the driver library); nullptr if unavailable.
-PFN_cuTensorMapEncodeTiled_v12000 encode_tiled()
+PFN_cuTensorMapEncodeTiled_v12000 tma_encode_fn()
 {
     static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
         void *p = nullptr;
@@ -843,25 +797,29 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_tiled()
     return fn;
 }
 
-// The level's shape allows the row-pair view (see k_cheb_pair).
-bool pair_shape_ok(int n0, int n1, int sy)
+bool tma_pair_shape_ok(int n0, int n1, int sy)
 {
     return (n0 & 1) == 0 && ((long long)sy * (n1 + 2)) % 4 == 0;
 }
 
-// Tensor map of one FP32 array of level F in the row-pair view, box w
-// floats x h row pairs x 1 plane.
-bool encode_pair_map(CUtensorMap *m, const float *base, const LevelView<float> &F, int w, int h)
+bool tma_encode_f32_pairs(CUtensorMap *m, const float *base, int n0, int n1, int n2, int sy, int sz, int w, int h)
 {
-    const PFN_cuTensorMapEncodeTiled_v12000 fn = encode_tiled();
-    if (!fn || !base || ((uintptr_t)base & 15u) || !pair_shape_ok(F.n0, F.n1, F.sy)) return false;
-    const cuuint64_t dim[3] = {(cuuint64_t)(2 * F.sy), (cuuint64_t)((F.n1 + 2) / 2), (cuuint64_t)(F.n2 + 2)};
-    const cuuint64_t stride[2] = {(cuuint64_t)(2 * F.sy) * 4u, (cuuint64_t)F.sz * 4u};
+    const PFN_cuTensorMapEncodeTiled_v12000 fn = tma_encode_fn();
+    if (!fn || !base || ((uintptr_t)base & 15u) || !tma_pair_shape_ok(n0, n1, sy)) return false;
+    const cuuint64_t dim[3] = {(cuuint64_t)(2 * sy), (cuuint64_t)((n1 + 2) / 2), (cuuint64_t)(n2 + 2)};
+    const cuuint64_t stride[2] = {(cuuint64_t)(2 * sy) * 4u, (cuuint64_t)sz * 4u};
     const cuuint32_t box[3] = {(cuuint32_t)w, (cuuint32_t)h, 1u};
     const cuuint32_t estride[3] = {1u, 1u, 1u};
     return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(base), dim, stride, box, estride,
               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+namespace {
+// Tensor map of one FP32 array of level F in the row-pair view.
+bool encode_pair_map(CUtensorMap *m, const float *base, const LevelView<float> &F, int w, int h)
+{
+    return tma_encode_f32_pairs(m, base, F.n0, F.n1, F.n2, F.sy, F.sz, w, h);
 }
 }  // namespace
 
@@ -870,8 +828,8 @@ template <typename T>
 int pair_planes(const MgLevel<T> &F)
 {
     const long long cells = (long long)F.n0 * F.n1 * F.n2;
-    if (sizeof(T) != 4 || g_pairs == 0 || cells < (1LL << 18) || !pair_shape_ok(F.n0, F.n1, F.sy) ||
-        !encode_tiled())
+    if (sizeof(T) != 4 || g_pairs == 0 || cells < (1LL << 18) || !tma_pair_shape_ok(F.n0, F.n1, F.sy) ||
+        !tma_encode_fn())
         return 0;
     if (g_pairs == 2) return g_pair_planes;
     if (cells < (1LL << 22)) return 0;
