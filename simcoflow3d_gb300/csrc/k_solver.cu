@@ -689,11 +689,11 @@ __global__ void __launch_bounds__(C2_THREADS, C2_BLOCKS_PER_SM) k_cheb_pair(cons
         mbar_fence_init();
     }
     __syncthreads();
-    // group P: slot (P + 2) mod 4 (P >= -1), parity of its use of the slot
+    // group P: slot (P - g0) mod 4, phase parity ((P - g0) / 4) mod 2
     // (thread 0 only; box origins recomputed here rather than held in
     // registers by every thread)
     auto issue = [&](int P) {
-        const int s = (P + 2) & (C2_DEPTH - 1);
+        const int s = (P - g0) & (C2_DEPTH - 1);
         const unsigned dst = sb + 4u * (unsigned)(s * C2_SLOT), bar = bar0 + 8u * s;
         const int bxi = blockIdx.x * C2_TX, yA = blockIdx.y * (C2_TY / 2), yN = yA - 1;
         mbar_expect_tx(bar, DP ? C2_TX_BYTES_DP : C2_TX_BYTES_NODP);
@@ -709,23 +709,31 @@ __global__ void __launch_bounds__(C2_THREADS, C2_BLOCKS_PER_SM) k_cheb_pair(cons
             tma_load3(dst + 4u * (C2_GX + p * C2_BX), &tm.m[6], xE, yN, P, bar);
         }
     };
+    // a block has at least five groups (g0 .. g0 + 4 <= glast)
     if (tid == 0)
-        for (int P = g0; P <= g0 + 2 && P <= glast; ++P) issue(P);
-    int wnext = g0;             // next group to wait for
+        for (int P = g0; P <= g0 + 2; ++P) issue(P);
     bool gave_up = false;
+    if (!mbar_wait(bar0, 0u)) gave_up = true;          // group g0
+    if (!mbar_wait(bar0 + 8u, 0u)) gave_up = true;     // group g0 + 1
     float d1 = 0.f;             // first-step update of this thread's column, plane below
     C2Cell kc = {}, kp = {};
     const bool out_ok = in0;
     int c = (i0 + tx) + F.sy * (j0 + ty) + F.sz * (k0 - 2);   // output cell at plane kk - 1
-    for (int kk = k0 - 1; kk <= k1 + 1; ++kk, c += F.sz) {
+    // iteration it handles plane kk = k0 - 1 + it; every ring index is a
+    // function of it mod 4, so the unrolled copies address shared memory
+    // with constant offsets: groups kk - 1, kk, kk + 1 in slots it, it + 1,
+    // it + 2 (mod 4), first-step results of plane kk in R1 slot it mod 4
+    const int nit = k1 - k0 + 3;
+#pragma unroll 4
+    for (int it = 0; it < nit; ++it, c += F.sz) {
+        const int kk = k0 - 1 + it;
         if (tid == 0 && kk + 2 <= glast) issue(kk + 2);
-        for (; wnext <= kk + 1; ++wnext)
-            if (!mbar_wait(bar0 + 8u * ((wnext + 2) & (C2_DEPTH - 1)), (unsigned)((wnext - g0) >> 2) & 1u))
-                gave_up = true;
-        const float *G = S + ((kk + 2) & (C2_DEPTH - 1)) * C2_SLOT;
-        const float *Gm = S + ((kk + 1) & (C2_DEPTH - 1)) * C2_SLOT;
-        const float *Gp = S + ((kk + 3) & (C2_DEPTH - 1)) * C2_SLOT;
-        float *o1 = R1 + ((kk + 1) & (C2_R1 - 1)) * C2_NE;
+        if (!mbar_wait(bar0 + 8u * ((it + 2) & (C2_DEPTH - 1)), (unsigned)((it + 2) >> 2) & 1u))
+            gave_up = true;    // group kk + 1
+        const float *G = S + ((it + 1) & (C2_DEPTH - 1)) * C2_SLOT;
+        const float *Gm = S + (it & (C2_DEPTH - 1)) * C2_SLOT;
+        const float *Gp = S + ((it + 2) & (C2_DEPTH - 1)) * C2_SLOT;
+        float *o1 = R1 + (it & (C2_R1 - 1)) * C2_NE;
         const bool plane_in = kk >= 1 && kk <= F.n2;
         const float dn1 = c2_first<DP>(a, G, Gm, Gp, t0, o1, q0, in0 && plane_in, kc);
         if (halo) {
@@ -733,10 +741,10 @@ __global__ void __launch_bounds__(C2_THREADS, C2_BLOCKS_PER_SM) k_cheb_pair(cons
             c2_first<DP>(a, G, Gm, Gp, th, o1, qh, inh && plane_in, kh);
         }
         __syncthreads();
-        if (kk - 1 >= k0 && out_ok) {
+        if (it >= 2 && out_ok) {
             // second step at plane kk - 1 from the first-step planes kk - 2 .. kk
-            const float *y0 = R1 + (kk & (C2_R1 - 1)) * C2_NE;
-            const float *ym = R1 + ((kk + 3) & (C2_R1 - 1)) * C2_NE;
+            const float *y0 = R1 + ((it + 3) & (C2_R1 - 1)) * C2_NE;
+            const float *ym = R1 + ((it + 2) & (C2_R1 - 1)) * C2_NE;
             const float *yp = o1;
             const int q = q0;
             const float xc = y0[q];
@@ -755,7 +763,7 @@ __global__ void __launch_bounds__(C2_THREADS, C2_BLOCKS_PER_SM) k_cheb_pair(cons
         // it exits: wait once more (bounded) for the last groups issued
         if (tid == 0)
             for (int P = glast - (C2_DEPTH - 1) > g0 ? glast - (C2_DEPTH - 1) : g0; P <= glast; ++P)
-                mbar_wait(bar0 + 8u * ((P + 2) & (C2_DEPTH - 1)), (unsigned)((P - g0) >> 2) & 1u);
+                mbar_wait(bar0 + 8u * ((P - g0) & (C2_DEPTH - 1)), (unsigned)((P - g0) >> 2) & 1u);
     }
 }
 
