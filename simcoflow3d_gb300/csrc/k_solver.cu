@@ -1062,15 +1062,47 @@ __global__ void __launch_bounds__(256) k_post_first(LevelView<T> F, const T *__r
 // x += e(parent) on the active cells (piecewise-constant prolongation of
 // the coarse correction, in place); on large levels this and a plain first
 // Chebyshev step replace k_post_first, whose seven recomputed neighbour
-// prolongations cost more than one extra pass over x.
+// prolongations cost more than one extra pass over x.  A thread owns
+// PR_KZ cells of one (i, j) column and issues all their loads (mask, x and
+// the parent's correction) before any store, so they are in flight
+// together (one cell per thread, the load of x waiting on the mask, ran at
+// a third of the HBM bandwidth).
+constexpr int PR_KZ = 4;
 template <typename T>
 __global__ void __launch_bounds__(256) k_prolong(LevelView<T> F, const unsigned char *__restrict__ act,
                                                  T *__restrict__ x, LevelView<T> C, const T *__restrict__ e, int s0,
                                                  int s1, int s2)
 {
-    INTERIOR_IJK(F);
-    if (!in || !act[c]) return;
-    x[c] += e[(((i - 1) >> s0) + 1) + C.sy * (((j - 1) >> s1) + 1) + C.sz * (((k - 1) >> s2) + 1)];
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int kb = blockIdx.z * PR_KZ + 1;
+    if (i > F.n0 || j > F.n1) return;
+    const int c0 = i + F.sy * j;
+    const int pc = (((i - 1) >> s0) + 1) + C.sy * (((j - 1) >> s1) + 1);
+    unsigned char a[PR_KZ];
+    T xv[PR_KZ], ev[PR_KZ];
+#pragma unroll
+    for (int m = 0; m < PR_KZ; ++m) {
+        const int k = kb + m;
+        a[m] = 0;
+        if (k <= F.n2) {
+            const int c = c0 + F.sz * k;
+            a[m] = act[c];
+            xv[m] = x[c];
+            ev[m] = e[pc + C.sz * (((k - 1) >> s2) + 1)];
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < PR_KZ; ++m)
+        if (a[m]) x[c0 + F.sz * (kb + m)] = xv[m] + ev[m];
+}
+
+template <typename T>
+void launch_prolong(const MgLevel<T> &F, const MgLevel<T> &C, T *x, const T *e, cudaStream_t st)
+{
+    const dim3 blk(32, 8, 1);
+    const dim3 grd((F.n0 + 31) / 32, (F.n1 + 7) / 8, (F.n2 + PR_KZ - 1) / PR_KZ);
+    k_prolong<T><<<grd, blk, 0, st>>>(F.view(), F.active, x, C.view(), e, F.f0 - 1, F.f1 - 1, F.f2 - 1);
 }
 
 // coarsest level: y = Ainv (b - mean) on the active cells (one block)
@@ -1381,8 +1413,7 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
         const bool more = cc.degree > 1;
         if (cc.lines) {
             const int idp = l == 0 ? kt_begin(kt, KC_PROLONG, st, prolong_bytes<T>(F, more)) : -1;
-            k_prolong<T><<<lf.grid, lf.block, 0, st>>>(v, F.active, xa, C.view(), cur[l + 1], F.f0 - 1, F.f1 - 1,
-                                                       F.f2 - 1);
+            launch_prolong<T>(F, C, xa, cur[l + 1], st);
             launch_cheb_line<T>(F, xa, xa, xb, more ? F.d : nullptr, 0.0, cc.first, false, st);
             kt_end(kt, idp, st);
             *launches += 2;
@@ -1408,8 +1439,7 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
             if (use_pairs(F) && m >= 1) {
                 T *dout = m >= 2 ? F.d : nullptr;
                 const int idp = l == 0 ? kt_begin(kt, KC_PROLONG, st, pair_bytes(F, false, dout != nullptr, true)) : -1;
-                k_prolong<T><<<lf.grid, lf.block, 0, st>>>(v, F.active, xa, C.view(), cur[l + 1], F.f0 - 1, F.f1 - 1,
-                                                           F.f2 - 1);
+                launch_prolong<T>(F, C, xa, cur[l + 1], st);
                 cheb_pair(F, xa, nullptr, xb, dout, 0.0, cc.first, cc.c1[1], cc.c2[1], st);
                 kt_end(kt, idp, st);
                 *launches += 2;
@@ -1429,8 +1459,7 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
         if (paired) {
         } else if ((long long)F.n0 * F.n1 * F.n2 >= (1LL << 18)) {
             const int idp = l == 0 ? kt_begin(kt, KC_PROLONG, st, prolong_bytes<T>(F, more)) : -1;
-            k_prolong<T><<<lf.grid, lf.block, 0, st>>>(v, F.active, xa, C.view(), cur[l + 1], F.f0 - 1, F.f1 - 1,
-                                                       F.f2 - 1);
+            launch_prolong<T>(F, C, xa, cur[l + 1], st);
             // first post-smoothing step from x: the previous update term is 0
             k_cheb_step<T><<<lf.grid, lf.block, 0, st>>>(v, F.b, xa, xa, xb, more ? F.d : nullptr, T(0),
                                                          (T)cc.first);
