@@ -102,7 +102,7 @@ Launch3 df_launch(const DfOp &A)
 // q = A p, and the block partials of (p, q) (FP64 products and sums) and of
 // the sum of q (for the mean of A p in all-Neumann systems, which is zero in
 // exact arithmetic: double-float per thread, FP64 across threads)
-__global__ void __launch_bounds__(128) k_spmv_df(DfOp A, const float2 *__restrict__ p, float2 *__restrict__ q,
+__global__ void __launch_bounds__(128, 8) k_spmv_df(DfOp A, const float2 *__restrict__ p, float2 *__restrict__ q,
                                                  double *__restrict__ part, int n0)
 {
     DF_ZCHUNK(A);
@@ -113,11 +113,9 @@ __global__ void __launch_bounds__(128) k_spmv_df(DfOp A, const float2 *__restric
         int c = i + sy * j + sz * k0;
         float2 xm = ld(p, c - sz), x0 = ld(p, c), tb = cf(A.hi.cT, A.tlo, c - sz);
         // the six neighbour products are summed as a tree (short dependency
-        // chains: the kernel is latency-bound, not memory-bound, otherwise)
-        double v2 = 0.0;
-        float2 sq2 = make_float2(0.f, 0.f);
-        int par = 0;
-#pragma unroll 2
+        // chains: the kernel is latency-bound, not memory-bound, otherwise);
+        // one accumulator each keeps the kernel within 64 registers, eight
+        // blocks per SM
         for (int k = k0; k <= k1; ++k, c += sz) {
             const float2 xp = ld(p, c + sz), tt = cf(A.hi.cT, A.tlo, c);
             const float2 sx = dadd(dmul(cf(A.hi.cE, A.elo, c), ld(p, c + 1)),
@@ -128,13 +126,10 @@ __global__ void __launch_bounds__(128) k_spmv_df(DfOp A, const float2 *__restric
             const float2 s = dadd(dadd(sx, syy), sz2);
             const float2 y = dadd(dmul(cf(A.hi.diag, A.dlo, c), x0), dneg(s));
             q[c] = y;
-            if (par) { v2 = fma(dwide(x0), dwide(y), v2); sq2 = dadd(sq2, y); }
-            else { v = fma(dwide(x0), dwide(y), v); sq = dadd(sq, y); }
-            par ^= 1;
+            v = fma(dwide(x0), dwide(y), v);
+            sq = dadd(sq, y);
             xm = x0; x0 = xp; tb = tt;
         }
-        v += v2;
-        sq = dadd(sq, sq2);
     }
     double dv = block_sum(v);
     __syncthreads();
