@@ -473,9 +473,11 @@ __device__ __forceinline__ double fx_sub(double a, double b) { return __dsub_rn(
 __device__ __forceinline__ float fx_add(float a, float b) { return __fadd_rn(a, b); }
 __device__ __forceinline__ double fx_add(double a, double b) { return __dadd_rn(a, b); }
 
+// r = b - A x of one cell, the residual both the Chebyshev update and the
+// restriction use, so a fused residual gives the bits of a separate one.
 template <typename T>
-__device__ __forceinline__ T cheb_update(T b, T dg, T dinv, T x0, T xe, T xw, T xn, T xs, T xt, T xb, T ce, T cw,
-                                         T cn, T cs, T ct, T cb, T dprev, T c1, T c2)
+__device__ __forceinline__ T cheb_residual(T b, T dg, T x0, T xe, T xw, T xn, T xs, T xt, T xb, T ce, T cw, T cn,
+                                           T cs, T ct, T cb)
 {
     T s = fx_mul(ce, xe);
     s = fx_fma(cw, xw, s);
@@ -483,7 +485,14 @@ __device__ __forceinline__ T cheb_update(T b, T dg, T dinv, T x0, T xe, T xw, T 
     s = fx_fma(cs, xs, s);
     s = fx_fma(ct, xt, s);
     s = fx_fma(cb, xb, s);
-    const T r = fx_sub(b, fx_fma(dg, x0, -s));
+    return fx_sub(b, fx_fma(dg, x0, -s));
+}
+
+template <typename T>
+__device__ __forceinline__ T cheb_update(T b, T dg, T dinv, T x0, T xe, T xw, T xn, T xs, T xt, T xb, T ce, T cw,
+                                         T cn, T cs, T ct, T cb, T dprev, T c1, T c2)
+{
+    const T r = cheb_residual(b, dg, x0, xe, xw, xn, xs, xt, xb, ce, cw, cn, cs, ct, cb);
     return fx_fma(fx_mul(c2, dinv), r, fx_mul(c1, dprev));
 }
 
@@ -569,7 +578,10 @@ constexpr int C2_GB = 0, C2_GD = 2 * C2_BA, C2_GT = 4 * C2_BA, C2_GP = 6 * C2_BA
 constexpr int C2_DEPTH = 4;                                 // group slots (ring of planes)
 constexpr int C2_R1 = 4;                                    // first-step result planes
 constexpr int C2_R1N = ((C2_R1 * C2_NE + 31) / 32) * 32;    // floats, rounded to 128 bytes
-constexpr size_t C2_SMEM = 128 + sizeof(float) * (C2_DEPTH * C2_SLOT + C2_R1N) + 8 * C2_DEPTH;
+// restriction mode: the second rows' residuals of a plane pair, handed to
+// the first rows through shared memory (two buffers, by coarse plane parity)
+constexpr int C2_XCH = 2 * (C2_TY / 2) * C2_TX;                  // float2 entries
+constexpr size_t C2_SMEM = 128 + sizeof(float) * (C2_DEPTH * C2_SLOT + C2_R1N) + 8 * C2_DEPTH + 8 * C2_XCH;
 constexpr int C2_PLANES = 32;
 // bytes a group's copies deliver (full boxes, out-of-range parts as 0)
 constexpr unsigned C2_TX_BYTES_NODP = 2u * 4u * (3 * C2_WA * C2_HA + C2_WE * C2_HA + C2_WA * C2_HN + C2_WE * C2_HX);
@@ -587,6 +599,8 @@ struct PairArgs {
     unsigned *flags;             // FLAG_WAIT_TIMEOUT if a copy never landed
     float c1a, c2a, c1b, c2b;
     int planes;
+    LevelView<float> C;          // restriction mode: the coarse level and its rhs
+    float *bc;
 };
 
 // Offsets in a group slot (floats) of one first-step cell (ex, ey) of the
@@ -644,7 +658,11 @@ __device__ __forceinline__ float c2_first(const PairArgs &a, const float *G, con
     return dn;
 }
 
-template <bool DP, bool DO>
+// RS (restriction mode, with DP and without DO): the first step is the last
+// pre-smoothing step, written to xout, and the second phase forms its
+// residual and restricts it to the coarse right-hand side a.bc, as
+// k_restrict would (planes per block even, coarsening factors 2).
+template <bool DP, bool DO, bool RS>
 __global__ void __launch_bounds__(C2_THREADS, C2_BLOCKS_PER_SM) k_cheb_pair(const __grid_constant__ PairMaps tm,
                                                                           PairArgs a)
 {
@@ -681,6 +699,31 @@ __global__ void __launch_bounds__(C2_THREADS, C2_BLOCKS_PER_SM) k_cheb_pair(cons
     const C2Idx th = c2_idx(halo ? hx : 0, hy, shA, shE);
     const int qh = (halo ? hx : 0) + C2_EX * hy;
     const bool inh = halo && bx + hx >= 1 && bx + hx <= F.n0 && by + hy >= 1 && by + hy <= F.n1;
+
+    // restriction mode: this thread's row is the first (j odd) or second of
+    // its row pair; the first rows finish a coarse cell one plane after its
+    // last fine plane, from the second rows' residuals in xch
+    float2 *xch = reinterpret_cast<float2 *>(S + C2_DEPTH * C2_SLOT + C2_R1N + 2 * C2_DEPTH);
+    const bool row_ok = j0 + ty <= F.n1;
+    const bool first_row = (ty & 1) == 0;
+    const bool has_second = j0 + ty + 1 <= F.n1;
+    float r0 = 0.f, sacc = 0.f;       // residual of the pair's first plane; the first row's partial sum
+    int pendK = 0;                    // coarse plane awaiting completion (0: none)
+    bool pend_two = false;            // it had two fine planes
+    auto complete = [&]() {           // first rows: add the second row's residuals, then lanes i, i^1
+        float sres = sacc;
+        if (has_second) {
+            const float2 v = xch[(pendK & 1) * (C2_TY / 2) * C2_TX + (ty >> 1) * C2_TX + tx];
+            sres = fx_add(sres, v.x);
+            if (pend_two) sres = fx_add(sres, v.y);
+        }
+        const float o = __shfl_xor_sync(0xffffffffu, sres, 1);
+        const int i = i0 + tx;
+        if ((tx & 1) == 0 && i <= F.n0) {
+            sres = fx_add(sres, o);
+            a.bc[(((i - 1) >> 1) + 1) + a.C.sy * (((j0 + ty - 1) >> 1) + 1) + a.C.sz * pendK] = sres;
+        }
+    };
 
     const int g0 = k0 - 2, glast = k1 + 2;               // groups this block needs
     if (tid == 0) {
@@ -741,7 +784,39 @@ __global__ void __launch_bounds__(C2_THREADS, C2_BLOCKS_PER_SM) k_cheb_pair(cons
             c2_first<DP>(a, G, Gm, Gp, th, o1, qh, inh && plane_in, kh);
         }
         __syncthreads();
-        if (it >= 2 && out_ok) {
+        if constexpr (RS) {
+            // the smoothed x of plane kk - 1, its residual, and the restriction
+            // of the plane pair it ends
+            if (it >= 2 && row_ok) {
+                if (pendK && first_row) complete();
+                pendK = 0;
+                const int pk = kk - 1;
+                const float *y0 = R1 + ((it + 3) & (C2_R1 - 1)) * C2_NE;
+                const float *ym = R1 + ((it + 2) & (C2_R1 - 1)) * C2_NE;
+                const float *yp = o1;
+                const int q = q0;
+                float r = 0.f;
+                if (out_ok) {
+                    const float xc = y0[q];
+                    a.xout[c] = xc;
+                    r = cheb_residual(kp.b, kp.dg, xc, y0[q + 1], y0[q - 1], y0[q + C2_EX], y0[q - C2_EX], yp[q],
+                                      ym[q], kp.ce, kp.cw, kp.cn, kp.cs, kp.ct, kp.cb);
+                }
+                const bool pfirst = (pk & 1) != 0;
+                if (pfirst) r0 = r;
+                if (!pfirst || pk == F.n2) {      // the pair ends at this plane
+                    const int K = ((pk - 1) >> 1) + 1;
+                    if (first_row) {
+                        sacc = fx_add(0.f, r0);
+                        if (!pfirst) sacc = fx_add(sacc, r);
+                    } else {
+                        xch[(K & 1) * (C2_TY / 2) * C2_TX + (ty >> 1) * C2_TX + tx] = make_float2(r0, r);
+                    }
+                    pendK = K;
+                    pend_two = !pfirst;
+                }
+            }
+        } else if (it >= 2 && out_ok) {
             // second step at plane kk - 1 from the first-step planes kk - 2 .. kk
             const float *y0 = R1 + ((it + 3) & (C2_R1 - 1)) * C2_NE;
             const float *ym = R1 + ((it + 2) & (C2_R1 - 1)) * C2_NE;
@@ -756,6 +831,10 @@ __global__ void __launch_bounds__(C2_THREADS, C2_BLOCKS_PER_SM) k_cheb_pair(cons
         }
         d1 = dn1;
         kp = kc;
+    }
+    if constexpr (RS) {
+        __syncthreads();
+        if (pendK && first_row && row_ok) complete();
     }
     if (gave_up) {
         atomicOr(a.flags, (unsigned)FLAG_WAIT_TIMEOUT);
@@ -857,8 +936,9 @@ cudaError_t pair_smem_attr()
 {
     static const cudaError_t rc = [] {
         cudaError_t e = cudaSuccess;
-        const void *fns[4] = {(const void *)k_cheb_pair<false, false>, (const void *)k_cheb_pair<false, true>,
-                              (const void *)k_cheb_pair<true, false>, (const void *)k_cheb_pair<true, true>};
+        const void *fns[5] = {(const void *)k_cheb_pair<false, false, false>,
+                              (const void *)k_cheb_pair<false, true, false>, (const void *)k_cheb_pair<true, false, false>,
+                              (const void *)k_cheb_pair<true, true, false>, (const void *)k_cheb_pair<true, false, true>};
         for (const void *f : fns) {
             const cudaError_t r = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C2_SMEM);
             if (r != cudaSuccess) e = r;
@@ -902,11 +982,42 @@ cudaError_t cheb_pair(const MgLevel<float> &F, const float *xin, const float *dp
     g_pair_tma.fetch_add(1);
     const dim3 blk(C2_TX, C2_TY, 1);
     const dim3 grd((F.n0 + C2_TX - 1) / C2_TX, (F.n1 + C2_TY - 1) / C2_TY, (F.n2 + a.planes - 1) / a.planes);
-    if (dprev && dout) k_cheb_pair<true, true><<<grd, blk, C2_SMEM, st>>>(tm, a);
-    else if (dprev) k_cheb_pair<true, false><<<grd, blk, C2_SMEM, st>>>(tm, a);
-    else if (dout) k_cheb_pair<false, true><<<grd, blk, C2_SMEM, st>>>(tm, a);
-    else k_cheb_pair<false, false><<<grd, blk, C2_SMEM, st>>>(tm, a);
+    if (dprev && dout) k_cheb_pair<true, true, false><<<grd, blk, C2_SMEM, st>>>(tm, a);
+    else if (dprev) k_cheb_pair<true, false, false><<<grd, blk, C2_SMEM, st>>>(tm, a);
+    else if (dout) k_cheb_pair<false, true, false><<<grd, blk, C2_SMEM, st>>>(tm, a);
+    else k_cheb_pair<false, false, false><<<grd, blk, C2_SMEM, st>>>(tm, a);
     return cudaSuccess;
+}
+
+// The last pre-smoothing step fused with the restriction: one Chebyshev
+// step (c1, c2) of FP32 level F from xin with the previous update F.d into
+// xout, and the residual of the result restricted to C.b, with the bits of
+// a k_cheb_step launch followed by k_restrict.  Needs coarsening factors 2
+// and a level that takes the two-step kernel; returns false (launching
+// nothing) otherwise.
+bool cheb_restrict(const MgLevel<float> &F, const MgLevel<float> &C, const float *xin, float *xout, double c1,
+                   double c2, cudaStream_t st)
+{
+    if (F.f0 != 2 || F.f1 != 2 || F.f2 != 2 || !use_pairs(F) || !F.flags) return false;
+    PairArgs a;
+    a.F = F.view();
+    a.xout = xout; a.dout = nullptr; a.flags = F.flags;
+    a.c1a = (float)c1; a.c2a = (float)c2; a.c1b = 0.f; a.c2b = 0.f;
+    const int planes = pair_planes(F);
+    a.planes = planes + (planes & 1);     // whole plane pairs per block
+    a.C = C.view(); a.bc = C.b;
+    PairMaps tm;
+    const LevelView<float> v = a.F;
+    const bool ok = encode_pair_map(&tm.m[0], F.b, v, C2_WA, C2_HA) && encode_pair_map(&tm.m[1], F.diag, v, C2_WA, C2_HA) &&
+                    encode_pair_map(&tm.m[2], F.cT, v, C2_WA, C2_HA) && encode_pair_map(&tm.m[3], F.d, v, C2_WA, C2_HA) &&
+                    encode_pair_map(&tm.m[4], F.cE, v, C2_WE, C2_HA) && encode_pair_map(&tm.m[5], F.cN, v, C2_WA, C2_HN) &&
+                    encode_pair_map(&tm.m[6], xin, v, C2_WE, C2_HX) && pair_smem_attr() == cudaSuccess;
+    if (!ok) return false;
+    g_pair_tma.fetch_add(1);
+    const dim3 blk(C2_TX, C2_TY, 1);
+    const dim3 grd((F.n0 + C2_TX - 1) / C2_TX, (F.n1 + C2_TY - 1) / C2_TY, (F.n2 + a.planes - 1) / a.planes);
+    k_cheb_pair<true, false, true><<<grd, blk, C2_SMEM, st>>>(tm, a);
+    return true;
 }
 
 // Chebyshev step with z-line Jacobi blocks: the preconditioner of the
@@ -999,8 +1110,10 @@ void launch_cheb_line(const MgLevel<T> &F, const T *x, const T *dprev, T *xout, 
 
 // Residual of the fine level summed over each coarse cell's children.  One
 // thread per fine i and coarse (J,K): it sums the residuals of its (up to
-// 2x2) fine cells in j and k, then lanes i and i^1 add their sums with a
-// shuffle (always in the order even + odd), so the result is reproducible.
+// 2x2) fine cells in j and k (j outer, k inner, from 0), then lanes i and
+// i^1 add their sums with a shuffle (always in the order even + odd), so the
+// result is reproducible; the fused smoothing step and restriction of the
+// two-step kernel forms the same sums in the same order.
 template <typename T>
 __global__ void __launch_bounds__(128) k_restrict(LevelView<T> F, const T *__restrict__ b,
                                                   const T *__restrict__ x, LevelView<T> C, T *__restrict__ bc,
@@ -1017,12 +1130,15 @@ __global__ void __launch_bounds__(128) k_restrict(LevelView<T> F, const T *__res
         for (int jj = j0; jj <= j1; ++jj)
             for (int kk = k0; kk <= k1; ++kk) {
                 const int fc = i + F.sy * jj + F.sz * kk;
-                s += b[fc] - apply_row(F, x, fc);
+                const T r = cheb_residual(b[fc], F.diag[fc], x[fc], x[fc + 1], x[fc - 1], x[fc + F.sy],
+                                          x[fc - F.sy], x[fc + F.sz], x[fc - F.sz], F.cE[fc], F.cE[fc - 1],
+                                          F.cN[fc], F.cN[fc - F.sy], F.cT[fc], F.cT[fc - F.sz]);
+                s = fx_add(s, r);
             }
     }
     if (f0 == 2) {
         const T o = __shfl_xor_sync(0xffffffffu, s, 1);
-        if ((threadIdx.x & 1) == 0) s = s + o;
+        if ((threadIdx.x & 1) == 0) s = fx_add(s, o);
         else return;
     }
     if (!in) return;
@@ -1316,6 +1432,19 @@ double pair_bytes(const MgLevel<float> &F, bool reads_d, bool writes_d, bool pro
     return cells * (4.0 * (7 + (reads_d ? 1 : 0) + (writes_d ? 1 : 0)) + (prolong ? 8.0 + 1.0 + 4.0 / 8.0 : 0.0));
 }
 
+// Algorithmic bytes of the fused last step and restriction: b, x, the
+// previous update, diag, cE, cN, cT read, x written, the coarse rhs written.
+double restrict_fused_bytes(const MgLevel<float> &F)
+{
+    const double cells = (double)F.n0 * F.n1 * F.n2;
+    return cells * (4.0 * 8 + 4.0 / 8.0);
+}
+template <typename T>
+double restrict_fused_bytes(const MgLevel<T> &)
+{
+    return -1.0;
+}
+
 template <typename T>
 T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, const int *map, int ncoarse,
              bool singular, bool first_done, cudaStream_t st, int *launches, KTimer *kt, cudaEvent_t coarse_ready)
@@ -1374,6 +1503,19 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
                     *launches += 1;
                     { T *tmp = xa; xa = xb; xb = tmp; }
                     s = 5;
+                }
+            }
+        }
+        if constexpr (sizeof(T) == 4) {
+            // a single last step before the restriction: both in one pass
+            if (s == cc.degree - 1 && s >= 3 && F.f0 == 2 && F.f1 == 2 && F.f2 == 2 && use_pairs(F)) {
+                const int id = l == 0 ? kt_begin(kt, KC_RESTRICT, st, restrict_fused_bytes(F)) : -1;
+                const bool fused = cheb_restrict(F, L[l + 1], xa, xb, cc.c1[s], cc.c2[s], st);
+                kt_end(kt, id, st);
+                if (fused) {
+                    *launches += 1;
+                    cur[l] = xb;
+                    continue;
                 }
             }
         }
