@@ -149,16 +149,16 @@ def measured_peaks():
     return FALLBACK_HBM_GBS, "fallback"
 
 
-# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of
-# the fine-level FP32 Chebyshev step, from the ncu capture summarised in
-# profiles/k_cheb_step_f32_c2_192.md: 213.5 MB for a first pre-smoothing step
-# at 192^3, scaled to 256^3 by the number of cells (x 16777216/7077888).
-# DRAM bytes (read + write) of one launch at 256^3, from ncu captures at
-# 192^3 scaled by cells; None where no capture exists
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch at
+# 256^3, from ncu captures at 192^3 scaled by the number of cells
+# (x 16777216/7077888): the fine-level FP32 Chebyshev step, 213.5 MB for a
+# first pre-smoothing step (profiles/k_cheb_step_f32_c2_192.md), and the
+# TMA-staged two-step kernel, 184.1 + 43.8 MB for the first pre-smoothing
+# pair (profiles/k_cheb_pair_c2_192.md)
 SMOOTH_TRAFFIC_256 = {
     "smooth": {"bytes": 213.5e6 * 16777216 / 7077888,
                "note": "first pre-smoothing step (32 B/cell algorithmic), ncu at 192^3 scaled by cells"},
-    "smooth2": {"bytes": 216.8e6 * 16777216 / 7077888,
+    "smooth2": {"bytes": (184.1e6 + 43.8e6) * 16777216 / 7077888,
                 "note": "first pre-smoothing pair (32 B/cell algorithmic for two steps), ncu at 192^3 "
                         "(16 k-planes per block there, 32 at 256^3) scaled by cells"},
 }
