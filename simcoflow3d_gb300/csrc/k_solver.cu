@@ -601,6 +601,8 @@ struct PairArgs {
     int planes;
     LevelView<float> C;          // restriction mode: the coarse level and its rhs
     float *bc;
+    float *xc;                   // and, unless null, its first smoothing step (factor firstc)
+    float firstc;
 };
 
 // Offsets in a group slot (floats) of one first-step cell (ex, ey) of the
@@ -721,7 +723,9 @@ __global__ void __launch_bounds__(C2_THREADS, C2_BLOCKS_PER_SM) k_cheb_pair(cons
         const int i = i0 + tx;
         if ((tx & 1) == 0 && i <= F.n0) {
             sres = fx_add(sres, o);
-            a.bc[(((i - 1) >> 1) + 1) + a.C.sy * (((j0 + ty - 1) >> 1) + 1) + a.C.sz * pendK] = sres;
+            const int cc = (((i - 1) >> 1) + 1) + a.C.sy * (((j0 + ty - 1) >> 1) + 1) + a.C.sz * pendK;
+            a.bc[cc] = sres;
+            if (a.xc) a.xc[cc] = a.firstc * jacobi_inv(a.C.diag[cc]) * sres;
         }
     };
 
@@ -996,7 +1000,7 @@ cudaError_t cheb_pair(const MgLevel<float> &F, const float *xin, const float *dp
 // and a level that takes the two-step kernel; returns false (launching
 // nothing) otherwise.
 bool cheb_restrict(const MgLevel<float> &F, const MgLevel<float> &C, const float *xin, float *xout, double c1,
-                   double c2, cudaStream_t st)
+                   double c2, float *xc, double first, cudaStream_t st)
 {
     if (F.f0 != 2 || F.f1 != 2 || F.f2 != 2 || !use_pairs(F) || !F.flags) return false;
     PairArgs a;
@@ -1006,6 +1010,7 @@ bool cheb_restrict(const MgLevel<float> &F, const MgLevel<float> &C, const float
     const int planes = pair_planes(F);
     a.planes = planes + (planes & 1);     // whole plane pairs per block
     a.C = C.view(); a.bc = C.b;
+    a.xc = xc; a.firstc = (float)first;
     PairMaps tm;
     const LevelView<float> v = a.F;
     const bool ok = encode_pair_map(&tm.m[0], F.b, v, C2_WA, C2_HA) && encode_pair_map(&tm.m[1], F.diag, v, C2_WA, C2_HA) &&
@@ -1108,7 +1113,9 @@ void launch_cheb_line(const MgLevel<T> &F, const T *x, const T *dprev, T *xout, 
     k_cheb_line<T><<<grd, blk, 0, st>>>(F.view(), F.b, x, dprev, xout, dout, (T)c1, (T)c2, zero_guess ? 1 : 0);
 }
 
-// Residual of the fine level summed over each coarse cell's children.  One
+// Residual of the fine level summed over each coarse cell's children (and,
+// with xc given, the coarse level's first smoothing step x = D^-1 b / theta
+// from that sum, which saves a launch per level and V-cycle).  One
 // thread per fine i and coarse (J,K): it sums the residuals of its (up to
 // 2x2) fine cells in j and k (j outer, k inner, from 0), then lanes i and
 // i^1 add their sums with a shuffle (always in the order even + odd), so the
@@ -1117,7 +1124,7 @@ void launch_cheb_line(const MgLevel<T> &F, const T *x, const T *dprev, T *xout, 
 template <typename T>
 __global__ void __launch_bounds__(128) k_restrict(LevelView<T> F, const T *__restrict__ b,
                                                   const T *__restrict__ x, LevelView<T> C, T *__restrict__ bc,
-                                                  int f0, int f1, int f2)
+                                                  int f0, int f1, int f2, T *__restrict__ xc, T first)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int J = blockIdx.y * blockDim.y + threadIdx.y + 1;
@@ -1143,7 +1150,11 @@ __global__ void __launch_bounds__(128) k_restrict(LevelView<T> F, const T *__res
     }
     if (!in) return;
     const int I = f0 == 2 ? ((i - 1) >> 1) + 1 : i;
-    bc[I + C.sy * J + C.sz * K] = s;
+    const int cc = I + C.sy * J + C.sz * K;
+    bc[cc] = s;
+    // the coarse level's first Chebyshev step from a zero guess, as
+    // k_cheb_first forms it (same operands, same order)
+    if (xc) xc[cc] = first * dinv_at(C, cc) * s;
 }
 
 // prolongation (piecewise constant, active cells only) fused with the first
@@ -1450,6 +1461,7 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
              bool singular, bool first_done, cudaStream_t st, int *launches, KTimer *kt, cudaEvent_t coarse_ready)
 {
     T *cur[32];
+    bool first_written[32] = {};    // level l's first step already written by the restriction into it
     const int last = nlev - 1;
     for (int l = 0; l < last; ++l) {
         MgLevel<T> &F = L[l];
@@ -1474,12 +1486,12 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
             MgLevel<T> &C = L[l + 1];
             dim3 rg((F.n0 + 31) / 32, (C.n1 + 3) / 4, C.n2), rb(32, 4, 1);
             const int id = l == 0 ? kt_begin(kt, KC_RESTRICT, st) : -1;
-            k_restrict<T><<<rg, rb, 0, st>>>(v, F.b, xa, C.view(), C.b, F.f0, F.f1, F.f2);
+            k_restrict<T><<<rg, rb, 0, st>>>(v, F.b, xa, C.view(), C.b, F.f0, F.f1, F.f2, nullptr, T(0));
             kt_end(kt, id, st);
             *launches += 1;
             continue;
         }
-        if (!(l == 0 && first_done)) {
+        if (!(l == 0 ? first_done : first_written[l])) {
             k_cheb_first<T><<<lf.grid, lf.block, 0, st>>>(v, F.b, xa, (T)cc.first);
             *launches += 1;
         }
@@ -1510,11 +1522,14 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
             // a single last step before the restriction: both in one pass
             if (s == cc.degree - 1 && s >= 3 && F.f0 == 2 && F.f1 == 2 && F.f2 == 2 && use_pairs(F)) {
                 const int id = l == 0 ? kt_begin(kt, KC_RESTRICT, st, restrict_fused_bytes(F)) : -1;
-                const bool fused = cheb_restrict(F, L[l + 1], xa, xb, cc.c1[s], cc.c2[s], st);
+                const bool wx = l + 1 < last;
+                const bool fused = cheb_restrict(F, L[l + 1], xa, xb, cc.c1[s], cc.c2[s], wx ? L[l + 1].x : nullptr,
+                                                 cc.first, st);
                 kt_end(kt, id, st);
                 if (fused) {
                     *launches += 1;
                     cur[l] = xb;
+                    first_written[l + 1] = wx;
                     continue;
                 }
             }
@@ -1534,7 +1549,10 @@ T *mg_vcycle(MgLevel<T> *L, int nlev, const ChebCoef &cc, const double *ainv, co
         MgLevel<T> &C = L[l + 1];
         dim3 rg((F.n0 + 31) / 32, (C.n1 + 3) / 4, C.n2), rb(32, 4, 1);
         const int id = l == 0 ? kt_begin(kt, KC_RESTRICT, st) : -1;
-        k_restrict<T><<<rg, rb, 0, st>>>(v, F.b, xa, C.view(), C.b, F.f0, F.f1, F.f2);
+        const bool wx = l + 1 < last;
+        k_restrict<T><<<rg, rb, 0, st>>>(v, F.b, xa, C.view(), C.b, F.f0, F.f1, F.f2, wx ? C.x : nullptr,
+                                         (T)cc.first);
+        first_written[l + 1] = wx;
         kt_end(kt, id, st);
         *launches += 1;
     }
@@ -1648,7 +1666,7 @@ template <typename T>
 void probe_restrict(MgLevel<T> &F, MgLevel<T> &C, cudaStream_t st)
 {
     dim3 rg((F.n0 + 31) / 32, (C.n1 + 3) / 4, C.n2), rb(32, 4, 1);
-    k_restrict<T><<<rg, rb, 0, st>>>(F.view(), F.b, F.x, C.view(), C.b, F.f0, F.f1, F.f2);
+    k_restrict<T><<<rg, rb, 0, st>>>(F.view(), F.b, F.x, C.view(), C.b, F.f0, F.f1, F.f2, nullptr, T(0));
 }
 
 template <typename T>
