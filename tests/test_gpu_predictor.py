@@ -123,6 +123,29 @@ def test_not_converged_is_reported(lib):
     assert e.value.status == capi.SCF_ERR_NOT_CONVERGED
 
 
+@pytest.mark.timeout(300)
+@pytest.mark.parametrize("field", ["df_ew", "flux_div"])
+@pytest.mark.parametrize("prec", [capi.SCF_PREC_FP64, capi.SCF_PREC_MIXED], ids=["fp64", "mixed"])
+def test_non_finite_input_ends_the_solve(lib, field, prec):
+    """A NaN in a matrix coefficient (a diffusive flux weight) or in the
+    right-hand side (the flux divergence) of one cell makes the first
+    BiCGStab step of a round break down.  The solve must end with an error
+    status, not restart from the same residual again and again."""
+    import time
+    inp = PR.momentum_inputs(O.grid_preprocess(GM.geometry_inputs("c1", n=12)))
+    a = inp.comps[0].arrays[field]
+    a[tuple(n // 2 for n in a.shape)] = np.nan
+    ps = PR.PredictSolves(inp.imax, inp.jmax, inp.kmax)
+    t0 = time.perf_counter()
+    with pytest.raises(ScfError) as e:
+        ps(inp, PR.default_opts(precision=prec))
+    assert e.value.status in (capi.SCF_ERR_NONFINITE, capi.SCF_ERR_BAD_INPUT), e.value.status
+    assert time.perf_counter() - t0 < 30.0
+    # the context stays usable
+    ok = PR.momentum_inputs(O.grid_preprocess(GM.geometry_inputs("c1", n=12)))
+    ps(ok, PR.default_opts(precision=prec))
+
+
 @pytest.mark.parametrize("prec", [capi.SCF_PREC_FP64, capi.SCF_PREC_MIXED], ids=["fp64", "mixed"])
 def test_dirichlet_faces_and_tiny_grid(lib, prec):
     """All six faces Dirichlet with seeded boundary values (and stronger
