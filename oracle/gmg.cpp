@@ -2,7 +2,7 @@
 //
 // TEST INFRASTRUCTURE ONLY (oracle and timed CPU baseline; never linked into
 // the product).  It restates, on the host cores, the solver design of the CUDA
-// library so that parity of the device solution can be judged by an
+// library so that parity of the device solution can be checked against an
 // independent FP64 implementation and so that the benchmark has a CPU path of
 // the same algorithm family as the reference's HYPRE PCG + BoomerAMG
 // (src/ProjectionP.f90:267-299) to time.
